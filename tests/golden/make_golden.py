@@ -1,0 +1,132 @@
+"""Generate golden vectors from the reference implementation itself.
+
+Run where the reference source tree is available (it is not needed at test
+time):
+
+    python tests/golden/make_golden.py /path/to/MLFF-Distiller
+
+It imports the reference StudentForceField by file path
+(src/mlff_distiller/models/student_model.py; the package __init__ needs
+modules that are not in the reference tree), builds it right after
+torch.manual_seed(0), and records energies, forces and edge lists for small
+seeded inputs in float32 (the reference's own dtype) and float64
+(model.double()).  Outputs go next to this script:
+
+* weights_seed0.npz       -- the seed-0 state_dict (reference key names)
+* bias_perturbation.npz   -- seeded non-zero biases (trained-like weights)
+* golden_cases.npz        -- per case: Z, pos, mol_ptr, edge_index, E/F in
+                             float32 and float64, for seed and biased weights
+* golden_norm.npz         -- float32 vectors with |d| near 5 A and the
+                             reference's torch.norm decision |d| <= 5
+"""
+from __future__ import annotations
+
+import importlib.util
+import os
+import sys
+import types
+
+import numpy as np
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "mlff-distiller_gb300"))
+
+from mlff_gb300 import systems  # noqa: E402
+
+
+def load_reference(ref_root: str):
+    for name in ["mlff_distiller", "mlff_distiller.models"]:
+        if name not in sys.modules:
+            m = types.ModuleType(name)
+            m.__path__ = []
+            sys.modules[name] = m
+    path = os.path.join(ref_root, "src", "mlff_distiller", "models", "student_model.py")
+    spec = importlib.util.spec_from_file_location("mlff_distiller.models.student_model", path)
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[spec.name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def ref_eval(model, Z, pos, batch=None, dtype=torch.float32):
+    m = model.to(dtype)
+    x = torch.tensor(pos, dtype=dtype).requires_grad_(True)
+    Zt = torch.tensor(Z, dtype=torch.long)
+    bt = None if batch is None else torch.tensor(batch, dtype=torch.long)
+    E = m(Zt, x, batch=bt)
+    F = -torch.autograd.grad(E, x, grad_outputs=torch.ones_like(E))[0]
+    return np.atleast_1d(E.detach().numpy()).astype(np.float64), F.detach().numpy().astype(np.float64)
+
+
+def main(ref_root: str):
+    sm = load_reference(ref_root)
+    torch.manual_seed(0)
+    model = sm.StudentForceField(use_torch_cluster=False)
+    model.eval()
+    sd = {k: v.detach().numpy().copy() for k, v in model.state_dict().items()}
+    np.savez_compressed(os.path.join(HERE, "weights_seed0.npz"), **sd)
+
+    rng = np.random.default_rng(1234)
+    pert = {k: (0.05 * rng.standard_normal(v.shape)).astype(np.float32)
+            for k, v in sd.items() if k.endswith(".bias")}
+    np.savez_compressed(os.path.join(HERE, "bias_perturbation.npz"), **pert)
+    biased = sm.StudentForceField(use_torch_cluster=False)
+    biased.load_state_dict({k: torch.tensor(sd[k] + pert[k]) if k in pert else torch.tensor(sd[k])
+                            for k in sd})
+    biased.eval()
+
+    cases = {}
+
+    def add_case(name, sysm: systems.System):
+        pos32 = sysm.pos.astype(np.float32)
+        batch = np.repeat(np.arange(sysm.n_mol), np.diff(sysm.mol_ptr))
+        bt = torch.tensor(batch, dtype=torch.long) if sysm.n_mol > 1 else None
+        ei = sm.radius_graph_native(torch.tensor(pos32), 5.0, bt, loop=False).numpy()
+        cases[f"{name}/Z"] = sysm.Z
+        cases[f"{name}/pos"] = pos32
+        cases[f"{name}/mol_ptr"] = sysm.mol_ptr
+        cases[f"{name}/edge_index"] = ei
+        b = batch if sysm.n_mol > 1 else None
+        for tag, mdl in (("seed", model), ("bias", biased)):
+            E32, F32 = ref_eval(mdl, sysm.Z, pos32, b, torch.float32)
+            E64, F64 = ref_eval(mdl, sysm.Z, pos32.astype(np.float64), b, torch.float64)
+            mdl.float()
+            cases[f"{name}/{tag}/E32"] = E32
+            cases[f"{name}/{tag}/F32"] = F32
+            cases[f"{name}/{tag}/E64"] = E64
+            cases[f"{name}/{tag}/F64"] = F64
+
+    add_case("molecule60", systems.lattice_molecule(60, seed=0))
+    add_case("batch6", systems.molecule_batch(6, 10, 40, seed=7))
+    water = systems.System(np.array([8, 1, 1]), np.array([[0.0, 0, 0], [0.96, 0, 0], [-0.24, 0.93, 0]]),
+                           np.array([0, 3]), np.zeros((1, 3)), np.zeros(1, bool), "water")
+    methane = systems.System(np.array([6, 1, 1, 1, 1]),
+                             np.array([[0.0, 0, 0], [0.63, 0.63, 0.63], [-0.63, -0.63, 0.63],
+                                       [-0.63, 0.63, -0.63], [0.63, -0.63, -0.63]]),
+                             np.array([0, 5]), np.zeros((1, 3)), np.zeros(1, bool), "methane")
+    add_case("water", water)
+    add_case("methane", methane)
+    # a pair at exactly 5.0 A (kept by <=, zero cutoff weight), an isolated
+    # atom, and a pair just inside the cutoff
+    edge = systems.System(np.array([6, 8, 1, 7]),
+                          np.array([[0.0, 0, 0], [3.0, 4.0, 0], [40.0, 0, 0], [0.0, 0, 4.999]]),
+                          np.array([0, 4]), np.zeros((1, 3)), np.zeros(1, bool), "cutoff_edge")
+    add_case("cutoff_edge", edge)
+    np.savez_compressed(os.path.join(HERE, "golden_cases.npz"), **cases)
+
+    # edge decision: vectors whose float32 norm straddles the cutoff
+    g = np.random.default_rng(99)
+    dirs = g.standard_normal((40_000, 3))
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    radii = 5.0 + g.uniform(-4e-6, 4e-6, size=(40_000, 1))
+    vec = (dirs * radii).astype(np.float32)
+    dist = torch.norm(torch.tensor(vec), dim=1).numpy()
+    np.savez_compressed(os.path.join(HERE, "golden_norm.npz"), vec=vec, dist=dist,
+                        keep=(dist <= 5.0))
+    print("wrote", sorted(os.listdir(HERE)))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
