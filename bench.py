@@ -1,0 +1,343 @@
+#!/usr/bin/env python
+"""Benchmark: batched energy + force evaluation (atom-steps/s) on GB300.
+
+Default workload: 256 open H/C/N/O molecules with 10-120 atoms each
+(about 16.5k atoms, seeded; the reference ships no dataset), seed-0
+StudentForceField weights (hidden 128, 3 blocks, 20 RBF, 5 A cutoff).  One
+step = one full evaluation of the batch: radius graph, model, hand-written
+force adjoint.  ``value`` is device-timed with inputs resident in HBM; the
+e2e figure goes through the public module API with host buffers (H2D of
+positions, numbers and offsets; D2H of energies and forces) inside the
+timed region.  An L2-sized buffer is rewritten between timed steps.
+
+  python bench.py [--gpus N --steps K --warmup W] [--workload batch256]
+                  [--path bf16x3|tuned_fp32|fp32] [--impl ours|reference]
+
+Under torchrun (N>1) every rank evaluates its own copy of the workload
+(independent batches, no collective on the data path): weak scaling.
+``--impl reference`` times the oracle port of the reference's CPU path
+(float32 torch, all host threads) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "mlff-distiller_gb300")
+for p in (ROOT, PKG):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+import numpy as np  # noqa: E402
+import torch  # noqa: E402
+
+METRIC = "atom-steps/s E+F on 1 GB300: tuned vs plain FP32, force err <=1e-3 eV/A vs FP64"
+UNIT = "atom-steps/s"
+GEMM_FLOP_PER_EDGE = 2 * (20 * 128 + 128 * 384)      # filter MLP, per directed edge and layer
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="batch256")
+    ap.add_argument("--path", default="bf16x3", choices=["bf16x3", "tuned_fp32", "fp32"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi sampled every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.proc = None
+        self.path = None
+        try:
+            uuid = str(torch.cuda.get_device_properties(device_index).uuid)
+            self.id = uuid if uuid.startswith("GPU-") else f"GPU-{uuid}"
+        except Exception:
+            self.id = str(device_index)
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", self.id, f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        self.proc.wait()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        loaded = [s for s in sm if mx and s >= 0.5 * max(mx)] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+
+
+# -------------------------------------------------------------- workload
+def seed_model(precision):
+    from mlff_gb300.student_model import StudentForceField
+    torch.manual_seed(0)
+    return StudentForceField(precision=precision)
+
+
+def cpu_baseline(sysm, seconds, n_threads=None):
+    """Oracle port of the reference CPU path (float32 torch autograd, C
+    radius graph) on a bounded sample of the workload's molecules."""
+    from oracle import painn
+    if n_threads:
+        torch.set_num_threads(n_threads)
+    model = seed_model("tuned_fp32")
+    W = {k: v.numpy() for k, v in model.state_dict().items()}
+    n_take = min(sysm.n_mol, 16)
+    sub = sysm.subset(list(range(n_take))) if sysm.n_mol > 1 else sysm
+    pos = sub.pos.astype(np.float32).astype(np.float64)
+    painn.energy_forces(W, sub.Z, pos, sub.mol_ptr, box=sub.box, pbc=sub.pbc, dtype=torch.float32)
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        painn.energy_forces(W, sub.Z, pos, sub.mol_ptr, box=sub.box, pbc=sub.pbc, dtype=torch.float32)
+        reps += 1
+        el = time.perf_counter() - t0
+        if (el >= seconds and reps >= 3) or el >= 4 * seconds:
+            break
+    return {"value": sub.n_atoms * reps / el, "unit": UNIT, "cores": torch.get_num_threads(), "kind": "port",
+            "sample": f"{n_take} of {sysm.n_mol} structures ({sub.n_atoms} atoms), {reps} E+F evaluations, "
+                      f"float32 torch autograd on the host CPU"}
+
+
+def read_traffic(kernel_kind, workload):
+    """DRAM bytes per launch from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", f"{kernel_kind}_{workload}.md")
+    if not os.path.exists(path):
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(path).read())
+    return float(m.group(1)) if m else None
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("bf16_tflops_sustained", 1700.0), d.get("hbm_gbs", 6800.0), "measured"
+    return 1700.0, 6800.0, "fallback"
+
+
+def run_reference(args, world, rank):
+    from mlff_gb300 import systems
+    if rank != 0:
+        return
+    sysm = systems.workload(args.workload)
+    n_thr = os.cpu_count() or 1
+    torch.set_num_threads(n_thr)
+    step_s = max(1.0, args.cpu_seconds / max(1, args.steps))
+    for _ in range(args.warmup):
+        cpu_baseline(sysm, 0.0, n_thr)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(sysm, step_s, n_thr))
+    total = time.perf_counter() - t0
+    v = statistics.mean(x["value"] for x in vals)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded), seed-0 weights",
+            "config": {"workload": args.workload, "structures_sampled": min(16, sysm.n_mol)},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": n_thr, "kind": "port",
+                             "sample": vals[0]["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    from mlff_gb300 import _lib, systems
+    from mlff_gb300.engine import make_batch
+
+    sysm = systems.workload(args.workload)
+    model = seed_model(args.path).cuda().eval()
+    eng = model.engine()
+    path = model.path
+    batch = make_batch(sysm.Z, sysm.pos, sysm.mol_ptr, sysm.box if sysm.pbc.any() else None,
+                       sysm.pbc if sysm.pbc.any() else None)
+    eng.energy_forces(batch, path)            # sizes the edge capacity, checks status
+    _, n_edges, _ = eng.status()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    for _ in range(max(3, args.warmup)):
+        eng.energy_forces(batch, path, check=False)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    barrier()
+    clocks.start()
+    time.sleep(0.3)
+    with _lib.Profile() as prof:
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            starts[i].record()
+            eng.energy_forces(batch, path, check=False)
+            ends[i].record()
+        barrier()
+    ck = clocks.stop()
+    code, _, _ = eng.status()
+    if code != _lib.OK:
+        raise RuntimeError(f"device status {code} during the timed region")
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_s = sum(step_ms) / 1000.0
+    if world > 1:
+        t = torch.tensor([total_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_s = float(t.item())
+    atoms_all = sysm.n_atoms * world
+    value = atoms_all * args.steps / total_s
+
+    # dominant kernel and its roofline (algorithmic GEMM FLOPs of the filter MLP)
+    L = model.num_interactions
+    kinds = {k: v for k, v in prof.ms.items() if prof.launches.get(k, 0) > 0}
+    dom = max(kinds, key=kinds.get)
+    launches = prof.launches[dom]
+    avg_ms = prof.ms[dom] / max(1, launches)
+    peak_tf, hbm, peak_src = measured_peaks()
+    if dom == "edge_fwd":
+        flop = n_edges * GEMM_FLOP_PER_EDGE
+    elif dom == "edge_bwd":
+        flop = 2 * n_edges * GEMM_FLOP_PER_EDGE
+    elif dom == "plain_gemm":
+        # plain path GEMM launches: per layer 2 forward + 2 reverse filter GEMMs and 4 update GEMMs
+        flop = None
+    else:
+        flop = None
+    roof = None
+    if flop is not None:
+        ach = flop / (avg_ms * 1e-3) / 1e12
+        roof = {"bound": "tensor", "kernel": dom, "achieved": round(ach, 2), "peak": peak_tf, "unit": "TFLOP/s",
+                "frac": round(ach / peak_tf, 4), "peak_source": f"{peak_src} bf16 sustained",
+                "traffic": read_traffic(dom, args.workload), "avg_launch_ms": round(avg_ms, 4),
+                "flop_per_launch": flop,
+                "mma_work_factor": (3.0 * (2 * (32 * 128 + 128 * 384)) / GEMM_FLOP_PER_EDGE
+                                    if path == _lib.PATH_TUNED_BF16X3 else None)}
+    gpu_launches = sum(prof.launches.values())
+
+    # e2e through the public module API with host buffers
+    e2e = None
+    if not args.no_e2e:
+        Zh = torch.from_numpy(sysm.Z.astype(np.int64)).pin_memory()
+        Ph = torch.from_numpy(sysm.pos.astype(np.float32)).pin_memory()
+        bh = torch.from_numpy(np.repeat(np.arange(sysm.n_mol), np.diff(sysm.mol_ptr)).astype(np.int64)).pin_memory()
+        cell = pbc = None
+        if sysm.pbc.any():
+            cell = torch.from_numpy(np.diag(sysm.box[0]).astype(np.float32))
+            pbc = torch.ones(3, dtype=torch.bool)
+
+        def e2e_step():
+            Z = Zh.to("cuda", non_blocking=True)
+            P = Ph.to("cuda", non_blocking=True)
+            b = bh.to("cuda", non_blocking=True)
+            E, F = model.energy_and_forces(Z, P, batch=b if sysm.n_mol > 1 else None,
+                                           cell=None if cell is None else cell.cuda(), pbc=pbc)
+            return E.cpu(), F.cpu()
+        for _ in range(2):
+            e2e_step()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        barrier()
+        el = time.perf_counter() - t0
+        if world > 1:
+            t = torch.tensor([el], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            el = float(t.item())
+        h2d = Zh.numel() * 8 + Ph.numel() * 4 + bh.numel() * 8
+        d2h = sysm.n_mol * 8 + sysm.n_atoms * 12
+        e2e = {"value": atoms_all * args.steps / el, "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h}
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = cpu_baseline(sysm, args.cpu_seconds, os.cpu_count())
+    dtype = {"bf16x3": "bf16x3 (split-bf16, fp32 accumulate)", "tuned_fp32": "f32", "fp32": "f32"}[args.path]
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * total_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": dtype,
+            "data": "synthetic (seeded), seed-0 weights",
+            "config": {"workload": args.workload, "atoms": sysm.n_atoms, "structures": sysm.n_mol,
+                       "directed_edges": n_edges, "path": args.path, "l2": "256 MiB buffer rewritten "
+                       "between timed steps", "per_rank": "independent copy of the workload"},
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches,
+            "kernel_ms": {k: round(v, 3) for k, v in prof.ms.items() if v > 0},
+            "clocks": ck}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

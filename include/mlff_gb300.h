@@ -1,0 +1,196 @@
+/*
+ * mlff_gb300 -- C ABI of the GB300 (sm_103a) energy/force/MD library for a
+ * PaiNN-style StudentForceField.
+ *
+ * The reference (MLFF-Distiller) is pure Python/PyTorch: it has no native
+ * FFI.  Each entry point below replaces one Python call on the hot path; the
+ * comment names that call (file:line inside the reference project).  The
+ * Python package mlff_gb300 binds these with ctypes.
+ *
+ * Conventions
+ *  - Every pointer to array data is a DEVICE pointer owned by the caller
+ *    (e.g. a torch tensor's data_ptr()) unless the comment says "host".
+ *  - The library never allocates device memory: the caller provides the
+ *    packed-weight blob and one workspace, sized by the *_size() queries.
+ *  - Every call is asynchronous on the given stream (cudaStream_t; NULL =
+ *    legacy default stream) and returns an int status; errors found on the
+ *    device (edge capacity, bad box) are written to a status word inside the
+ *    workspace and read back with mlff_read_status().  Nothing traps, exits
+ *    or throws across the ABI.
+ *  - Threading: one host thread per workspace at a time (the reference's
+ *    calculator is not re-entrant either).
+ */
+#ifndef MLFF_GB300_H
+#define MLFF_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *mlff_stream_t; /* same type as cudaStream_t */
+
+/* status codes */
+#define MLFF_OK 0
+#define MLFF_ERR_INVALID 1     /* bad argument (host-side check) */
+#define MLFF_ERR_CAPACITY 2    /* more edges than edge_capacity; read n_edges */
+#define MLFF_ERR_CUDA 3        /* CUDA runtime error; see mlff_last_error_string */
+#define MLFF_ERR_TIMEOUT 4     /* a bounded device wait gave up */
+#define MLFF_ERR_UNSUPPORTED 5 /* model shape outside what the kernels implement */
+#define MLFF_ERR_BOX 6         /* periodic box edge < 2*cutoff or non-finite */
+#define MLFF_ERR_ROW 7         /* one atom has more neighbours than a row holds */
+#define MLFF_ERR_WORKSPACE 8   /* workspace or packed blob smaller than required */
+
+/* evaluation paths */
+#define MLFF_PATH_PLAIN_FP32 0    /* per-op FP32 kernels (the plain drop-in) */
+#define MLFF_PATH_TUNED_BF16X3 1  /* fused edge kernels, tcgen05 split-BF16 */
+#define MLFF_PATH_TUNED_FP32 2    /* fused edge kernels, FP32 CUDA cores */
+
+#define MLFF_MAX_LAYERS 8
+
+/* Model shape: StudentForceField(hidden_dim, num_interactions, num_rbf,
+ * cutoff, max_z) -- src/mlff_distiller/models/student_model.py:566-575. */
+typedef struct {
+    int32_t hidden;    /* hidden_dim; the kernels implement 128 */
+    int32_t n_rbf;     /* num_rbf, 1..32 */
+    int32_t n_layers;  /* num_interactions, 1..8 */
+    int32_t n_species; /* max_z + 1 */
+    float cutoff;      /* Angstrom */
+} mlff_dims;
+
+/* Float32 parameters, one device pointer per state_dict tensor, in the
+ * reference's shapes (student_model.py:566-628; keys in the comments). */
+typedef struct {
+    const float *embedding;   /* embedding.weight [S,H] */
+    const float *rbf_centers; /* rbf.centers [R] */
+    const float *rbf_widths;  /* rbf.widths [R] */
+    const float *filter_w1[MLFF_MAX_LAYERS]; /* interactions.l.message.rbf_to_scalar.0.weight [H,R] */
+    const float *filter_b1[MLFF_MAX_LAYERS]; /* ...rbf_to_scalar.0.bias [H] */
+    const float *filter_w2[MLFF_MAX_LAYERS]; /* ...rbf_to_scalar.2.weight [3H,H] */
+    const float *filter_b2[MLFF_MAX_LAYERS]; /* ...rbf_to_scalar.2.bias [3H] */
+    const float *mixing[MLFF_MAX_LAYERS];    /* interactions.l.update.mixing_matrix [3,3] */
+    const float *update_w1[MLFF_MAX_LAYERS]; /* ...update.update_mlp.0.weight [H,2H] */
+    const float *update_b1[MLFF_MAX_LAYERS]; /* ...update_mlp.0.bias [H] */
+    const float *update_w2[MLFF_MAX_LAYERS]; /* ...update_mlp.2.weight [3H,H] */
+    const float *update_b2[MLFF_MAX_LAYERS]; /* ...update_mlp.2.bias [3H] */
+    const float *head_w1, *head_b1; /* energy_head.0 [H/2,H], [H/2] */
+    const float *head_w2, *head_b2; /* energy_head.2 [H/4,H/2], [H/4] */
+    const float *head_w3, *head_b3; /* energy_head.4 [1,H/4], [1] */
+} mlff_params;
+
+/* A ragged batch of structures (ase_calculator.py:647-706 _prepare_batch):
+ * structure m owns atoms mol_ptr[m] .. mol_ptr[m+1]-1.  Edges never cross
+ * structures (student_model.py:94-95).  A periodic structure is an
+ * orthorhombic box, periodic on all three axes, edge >= 2*cutoff. */
+typedef struct {
+    int32_t n_atoms;
+    int32_t n_mol;
+    const float *pos;       /* [N,3] float32, Angstrom */
+    const int64_t *Z;       /* [N] atomic numbers (0..n_species-1) */
+    const int64_t *mol_ptr; /* [B+1] */
+    const float *box;       /* [B,3] box edge lengths, or NULL (all open) */
+    const uint8_t *pbc;     /* [B] 1 = periodic, or NULL (all open) */
+} mlff_system;
+
+typedef struct {
+    double *energy;      /* [B] per-structure energy (eV), required */
+    float *forces;       /* [N,3] -dE/dpos (eV/A), or NULL for energy only */
+    double *virial;      /* [B,3,3] dE/d(strain), or NULL */
+    float *atom_energy;  /* [N] per-atom energies, or NULL */
+} mlff_outputs;
+
+/* Library version, major*10000 + minor*100 + patch. */
+int mlff_version(void);
+
+/* Last host-side error message of the calling thread ("" if none). */
+const char *mlff_last_error_string(void);
+
+/* Bytes of the packed weight blob for these dims. */
+size_t mlff_packed_weights_size(const mlff_dims *dims);
+
+/* Pack float32 state_dict tensors into the kernels' layouts (transposes,
+ * zero padding, split-BF16 hi/lo tiles).  Replaces nothing in the reference
+ * (its nn.Linear layers read the state_dict directly); call once after
+ * StudentForceField.load / load_state_dict (student_model.py:1101-1176). */
+int mlff_pack_weights(const mlff_dims *dims, const mlff_params *params, void *packed,
+                      size_t packed_bytes, mlff_stream_t stream);
+
+/* Workspace bytes for a batch of n_atoms atoms in n_mol structures with
+ * room for edge_capacity directed edges, for the given path. */
+size_t mlff_workspace_size(const mlff_dims *dims, int32_t n_atoms, int32_t n_mol,
+                           int64_t edge_capacity, int32_t path);
+
+/* Radius graph: replaces radius_graph / radius_graph_native
+ * (student_model.py:63-109, 165-191) plus a minimum-image rule for periodic
+ * boxes.  Builds a receiver-sorted CSR in the workspace whose rows and
+ * columns, read as [row; col], equal the reference's edge_index bit for
+ * bit.  On overflow the status word holds MLFF_ERR_CAPACITY and the number
+ * of edges needed. */
+int mlff_build_neighbors(const mlff_dims *dims, const mlff_system *sys, int64_t edge_capacity,
+                         void *workspace, size_t workspace_bytes, mlff_stream_t stream);
+
+/* Copy the CSR built by the last neighbour build out of the workspace:
+ * row_ptr [N+1] int32 and col [E] int32 (device), E = row_ptr[N]. */
+int mlff_copy_neighbors(const void *workspace, int32_t n_atoms, int32_t n_mol,
+                        int64_t edge_capacity, int32_t path, int32_t *row_ptr, int32_t *col,
+                        mlff_stream_t stream);
+
+/* Energies, forces (and virial): replaces StudentForceField.forward +
+ * torch.autograd.grad in predict_energy_and_forces (student_model.py:634-795)
+ * and the batched path of StudentForceFieldCalculator._batch_forward
+ * (ase_calculator.py:708-770).  Runs the neighbour build first. */
+int mlff_energy_forces(const mlff_dims *dims, const void *packed, const mlff_system *sys,
+                       int64_t edge_capacity, int32_t path, const mlff_outputs *out,
+                       void *workspace, size_t workspace_bytes, mlff_stream_t stream);
+
+/* Synchronise the stream and read the device status word: code (MLFF_OK or
+ * a device-side MLFF_ERR_*), edges found by the last neighbour build, and
+ * the first offending atom or structure (or -1).  Host pointers. */
+int mlff_read_status(const void *workspace, int32_t *code, int64_t *n_edges, int32_t *where,
+                     mlff_stream_t stream);
+
+/* Clear the device status word (asynchronous). */
+int mlff_clear_status(void *workspace, mlff_stream_t stream);
+
+/* Velocity-Verlet NVE steps in float64 state: replaces ASE VelocityVerlet
+ * driven by NVEMDHarness.run_simulation (testing/nve_harness.py:173-261).
+ * Per step: v += dt/2 * F/m; r += dt * v; F = F(r); v += dt/2 * F/m.
+ * pos/vel are float64 [N,3] (Angstrom, Angstrom per ASE time unit), forces
+ * float32 [N,3] hold F(r) on entry and on exit, inv_mass float64 [N]
+ * (1/amu).  energy receives the potential energy per structure after the
+ * last step, kinetic (optional) the kinetic energy.  No host
+ * synchronisation, so a fixed number of steps can be captured in a CUDA
+ * graph once the edge capacity is known to suffice. */
+typedef struct {
+    double *pos;
+    double *vel;
+    const double *inv_mass;
+    float *forces;
+    double *energy;
+    double *kinetic;
+} mlff_md_state;
+
+int mlff_verlet_steps(const mlff_dims *dims, const void *packed, const mlff_system *sys,
+                      int64_t edge_capacity, int32_t path, mlff_md_state *state, double dt,
+                      int32_t n_steps, void *workspace, size_t workspace_bytes,
+                      mlff_stream_t stream);
+
+/* Kernel timing for benchmarks (no counterpart in the reference, whose
+ * timers wrap whole Python calls: cuda/benchmark_utils.py:147-194).
+ * Between begin and end the library brackets its kernel groups with CUDA
+ * events on the launching stream and counts its kernel launches.  end
+ * synchronises those events and returns, per kind, the summed milliseconds
+ * and the number of launches.  Kinds: 0 neighbours, 1 fused edge forward,
+ * 2 fused edge reverse, 3 update forward, 4 update reverse, 5 readout,
+ * 6 forces, 7 plain-path GEMMs, 8 plain-path edge ops, 9 other, 10 MD
+ * integrator.  Do not enable while a stream is being captured. */
+#define MLFF_PROFILE_KINDS 11
+int mlff_profile_begin(void);
+int mlff_profile_end(double *ms_by_kind, int64_t *launches_by_kind, int32_t n_kinds);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MLFF_GB300_H */

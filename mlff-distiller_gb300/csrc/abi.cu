@@ -1,0 +1,279 @@
+// extern "C" entry points of libmlff_gb300.so (declared in
+// include/mlff_gb300.h), workspace layout and host-side validation.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <algorithm>
+#include "common.cuh"
+#include "workspace.h"
+
+namespace mlff {
+
+static thread_local char g_err[512] = "";
+
+void set_error(const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+int cuda_status(cudaError_t e, const char* what) {
+    set_error("CUDA error %d (%s) in %s", (int)e, cudaGetErrorString(e), what);
+    return MLFF_ERR_CUDA;
+}
+
+int persistent_ctas(int32_t path) {
+    // SIMT fused kernels: 4 CTAs of 128 threads per SM; tensor-core kernels
+    // are launched with one CTA per SM and walk several partitions each.
+    (void)path;
+    return 152 * 4;
+}
+
+WsLayout ws_layout(const mlff_dims& d, int32_t n_atoms, int32_t n_mol, int64_t cap, int32_t path) {
+    WsLayout L{};
+    L.N = n_atoms;
+    L.B = n_mol;
+    L.L = d.n_layers;
+    L.P = persistent_ctas(path);
+    L.cap = cap;
+    L.ncell_cap = (int64_t)n_atoms + 27LL * n_mol;
+    size_t p = 0;
+    auto take = [&](size_t bytes) {
+        size_t r = p;
+        p += (bytes + 255) & ~size_t(255);
+        return r;
+    };
+    const int64_t N = n_atoms, B = n_mol, Ly = d.n_layers;
+    const int64_t scan_n = std::max<int64_t>(N + 1, L.ncell_cap + 1);
+    L.status = take(sizeof(Status));
+    L.pos4 = take(sizeof(float4) * N);
+    L.atom_mol = take(4 * N);
+    L.row_ptr = take(4 * (N + 1));
+    L.col = take(4 * cap);
+    L.erecv = take(4 * cap);
+    L.rev = take(4 * cap);
+    L.edge_acc = take(sizeof(float4) * cap);
+    L.scan_tmp = take(4 * ((scan_n + 1023) / 1024 + 2));
+    L.mol_grid = take(sizeof(int4) * B);
+    L.cell_count = take(4 * (L.ncell_cap + 1));
+    L.cell_fill = take(4 * L.ncell_cap);
+    L.cell_atoms = take(4 * N);
+    L.atom_cell = take(4 * N);
+    L.part = take(4 * (L.P + 1));
+    L.X = take(sizeof(float) * (Ly + 1) * N * 4 * H);
+    L.Xt = take(sizeof(float) * Ly * N * 4 * H);
+    L.uz = take(sizeof(float) * Ly * N * H);
+    L.ua = take(sizeof(float) * Ly * N * H3);
+    // two adjoint buffers; the second also holds the per-atom virial (9 doubles)
+    L.xbar = take(sizeof(float) * 2 * N * 4 * H);
+    L.e_atom = take(sizeof(float) * N);
+    L.md_pos32 = take(sizeof(float) * 3 * N);
+    if (path == MLFF_PATH_PLAIN_FP32) {
+        L.geo = take(sizeof(float4) * cap);
+        L.erbf = take(sizeof(float) * cap * RMAX);
+        L.erbf_d = take(sizeof(float) * cap * RMAX);
+        L.fz = take(sizeof(float) * Ly * cap * H);
+        L.ff = take(sizeof(float) * Ly * cap * H3);
+        L.fh = take(sizeof(float) * cap * H);
+        L.fbar = take(sizeof(float) * cap * H3);
+        L.comb = take(sizeof(float) * N * 2 * H);
+        L.uh = take(sizeof(float) * N * H);
+        L.abar = take(sizeof(float) * N * H3);
+    }
+    L.total = p;
+    return L;
+}
+
+static int check_dims(const mlff_dims* d) {
+    if (!d) { set_error("dims is NULL"); return MLFF_ERR_INVALID; }
+    if (d->hidden != H) {
+        set_error("hidden=%d: the kernels implement hidden_dim=128", d->hidden);
+        return MLFF_ERR_UNSUPPORTED;
+    }
+    if (d->n_rbf < 1 || d->n_rbf > RMAX) {
+        set_error("n_rbf=%d outside 1..%d", d->n_rbf, RMAX);
+        return MLFF_ERR_UNSUPPORTED;
+    }
+    if (d->n_layers < 1 || d->n_layers > MAXL) {
+        set_error("n_layers=%d outside 1..%d", d->n_layers, MAXL);
+        return MLFF_ERR_UNSUPPORTED;
+    }
+    if (d->n_species < 1) { set_error("n_species=%d", d->n_species); return MLFF_ERR_INVALID; }
+    if (!(d->cutoff > 0.0f)) { set_error("cutoff must be > 0"); return MLFF_ERR_INVALID; }
+    return MLFF_OK;
+}
+
+static int check_sys(const mlff_system* s, int64_t cap) {
+    if (!s) { set_error("system is NULL"); return MLFF_ERR_INVALID; }
+    if (s->n_atoms < 1 || s->n_mol < 1) { set_error("empty system (n_atoms=%d n_mol=%d)", s->n_atoms, s->n_mol); return MLFF_ERR_INVALID; }
+    if (!s->pos || !s->Z || !s->mol_ptr) { set_error("pos, Z and mol_ptr are required"); return MLFF_ERR_INVALID; }
+    if ((s->box == nullptr) != (s->pbc == nullptr)) { set_error("box and pbc must both be given or both be NULL"); return MLFF_ERR_INVALID; }
+    if (cap < 0 || cap > INT32_MAX) { set_error("edge_capacity %lld outside 0..2^31-1", (long long)cap); return MLFF_ERR_INVALID; }
+    return MLFF_OK;
+}
+
+static int check_path(int32_t path) {
+    if (path != MLFF_PATH_PLAIN_FP32 && path != MLFF_PATH_TUNED_BF16X3 && path != MLFF_PATH_TUNED_FP32) {
+        set_error("unknown path %d", path);
+        return MLFF_ERR_INVALID;
+    }
+    return MLFF_OK;
+}
+
+int pack_fp32(const mlff_dims& d, const mlff_params& p, float* out, const PackedOffsets& o, cudaStream_t st);
+int pack_bf16(const mlff_dims& d, float* out, const PackedOffsets& o, cudaStream_t st);
+
+}  // namespace mlff
+
+namespace mlff {
+// neighbour build + model + reverse pass; leaves the status word alone so
+// that an error raised in an earlier MD step stays visible
+int energy_forces_impl(const mlff_dims& d, const void* packed, const mlff_system& sys, const WsLayout& L,
+                       int32_t path, const mlff_outputs& out, void* ws, cudaStream_t st) {
+    PackedOffsets po = packed_offsets(d);
+    int r = launch_neighbors(d, sys, L, ws, st);
+    if (r) return r;
+    const float* P = static_cast<const float*>(packed);
+    if (path == MLFF_PATH_PLAIN_FP32) return run_plain(d, P, po, sys, L, ws, out, st);
+    return run_tuned(d, P, po, sys, L, ws, out, path, st);
+}
+int md_kick_drift(const WsLayout& L, void* ws, mlff_md_state* s, double dt, cudaStream_t st);
+int md_kick(const WsLayout& L, void* ws, mlff_md_state* s, double dt, const int64_t* mol_ptr, int32_t n_mol,
+            bool kinetic, cudaStream_t st);
+}  // namespace mlff
+
+using namespace mlff;
+
+extern "C" {
+
+int mlff_version(void) { return 100; }
+
+const char* mlff_last_error_string(void) { return g_err; }
+
+size_t mlff_packed_weights_size(const mlff_dims* dims) {
+    if (check_dims(dims)) return 0;
+    return sizeof(float) * (size_t)packed_offsets(*dims).total;
+}
+
+int mlff_pack_weights(const mlff_dims* dims, const mlff_params* params, void* packed, size_t packed_bytes,
+                      mlff_stream_t stream) {
+    int r = check_dims(dims);
+    if (r) return r;
+    if (!params || !packed) { set_error("params and packed are required"); return MLFF_ERR_INVALID; }
+    PackedOffsets o = packed_offsets(*dims);
+    if (packed_bytes < sizeof(float) * (size_t)o.total) {
+        set_error("packed blob %zu bytes < %zu needed", packed_bytes, sizeof(float) * (size_t)o.total);
+        return MLFF_ERR_WORKSPACE;
+    }
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if ((r = pack_fp32(*dims, *params, static_cast<float*>(packed), o, st))) return r;
+    return pack_bf16(*dims, static_cast<float*>(packed), o, st);
+}
+
+size_t mlff_workspace_size(const mlff_dims* dims, int32_t n_atoms, int32_t n_mol, int64_t edge_capacity,
+                           int32_t path) {
+    if (check_dims(dims) || check_path(path) || n_atoms < 0 || n_mol < 0 || edge_capacity < 0) return 0;
+    return ws_layout(*dims, n_atoms, n_mol, edge_capacity, path).total;
+}
+
+static int prepare(const mlff_dims* dims, const mlff_system* sys, int64_t cap, int32_t path, void* ws,
+                   size_t ws_bytes, WsLayout& L) {
+    int r = check_dims(dims);
+    if (r) return r;
+    if ((r = check_sys(sys, cap))) return r;
+    if ((r = check_path(path))) return r;
+    if (!ws) { set_error("workspace is NULL"); return MLFF_ERR_INVALID; }
+    L = ws_layout(*dims, sys->n_atoms, sys->n_mol, cap, path);
+    if (ws_bytes < L.total) {
+        set_error("workspace %zu bytes < %zu needed", ws_bytes, L.total);
+        return MLFF_ERR_WORKSPACE;
+    }
+    return MLFF_OK;
+}
+
+int mlff_build_neighbors(const mlff_dims* dims, const mlff_system* sys, int64_t edge_capacity, void* workspace,
+                         size_t workspace_bytes, mlff_stream_t stream) {
+    WsLayout L;
+    int r = prepare(dims, sys, edge_capacity, MLFF_PATH_TUNED_FP32, workspace, workspace_bytes, L);
+    if (r) return r;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    MLFF_CUDA(cudaMemsetAsync(ws_ptr<Status>(workspace, L.status), 0, sizeof(Status), st));
+    return launch_neighbors(*dims, *sys, L, workspace, st);
+}
+
+int mlff_copy_neighbors(const void* workspace, int32_t n_atoms, int32_t n_mol, int64_t edge_capacity, int32_t path,
+                        int32_t* row_ptr, int32_t* col, mlff_stream_t stream) {
+    if (!workspace || !row_ptr || !col) { set_error("workspace, row_ptr and col are required"); return MLFF_ERR_INVALID; }
+    mlff_dims d{H, RMAX, 1, 1, 5.0f};
+    WsLayout L = ws_layout(d, n_atoms, n_mol, edge_capacity, path);
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    MLFF_CUDA(cudaMemcpyAsync(row_ptr, ws_ptr<int32_t>(workspace, L.row_ptr), 4 * ((size_t)n_atoms + 1),
+                              cudaMemcpyDeviceToDevice, st));
+    MLFF_CUDA(cudaMemcpyAsync(col, ws_ptr<int32_t>(workspace, L.col), 4 * (size_t)edge_capacity,
+                              cudaMemcpyDeviceToDevice, st));
+    return MLFF_OK;
+}
+
+
+int mlff_energy_forces(const mlff_dims* dims, const void* packed, const mlff_system* sys, int64_t edge_capacity,
+                       int32_t path, const mlff_outputs* out, void* workspace, size_t workspace_bytes,
+                       mlff_stream_t stream) {
+    WsLayout L;
+    int r = prepare(dims, sys, edge_capacity, path, workspace, workspace_bytes, L);
+    if (r) return r;
+    if (!packed || !out || !out->energy) { set_error("packed weights and out->energy are required"); return MLFF_ERR_INVALID; }
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    MLFF_CUDA(cudaMemsetAsync(ws_ptr<Status>(workspace, L.status), 0, sizeof(Status), st));
+    return energy_forces_impl(*dims, packed, *sys, L, path, *out, workspace, st);
+}
+
+int mlff_verlet_steps(const mlff_dims* dims, const void* packed, const mlff_system* sys, int64_t edge_capacity,
+                      int32_t path, mlff_md_state* state, double dt, int32_t n_steps, void* workspace,
+                      size_t workspace_bytes, mlff_stream_t stream) {
+    if (!sys || !state || !state->pos || !state->vel || !state->inv_mass || !state->forces || !state->energy) {
+        set_error("system and md state (pos, vel, inv_mass, forces, energy) are required");
+        return MLFF_ERR_INVALID;
+    }
+    if (n_steps < 0 || !(dt > 0.0)) { set_error("n_steps >= 0 and dt > 0 required"); return MLFF_ERR_INVALID; }
+    if (!packed) { set_error("packed weights are required"); return MLFF_ERR_INVALID; }
+    mlff_system s2 = *sys;
+    WsLayout L;
+    {
+        // validate with a non-null placeholder position pointer
+        s2.pos = reinterpret_cast<const float*>(workspace);
+        int r = prepare(dims, &s2, edge_capacity, path, workspace, workspace_bytes, L);
+        if (r) return r;
+    }
+    s2.pos = ws_ptr<float>(workspace, L.md_pos32);
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    mlff_outputs out{state->energy, state->forces, nullptr, nullptr};
+    MLFF_CUDA(cudaMemsetAsync(ws_ptr<Status>(workspace, L.status), 0, sizeof(Status), st));
+    int r;
+    for (int s = 0; s < n_steps; ++s) {
+        if ((r = md_kick_drift(L, workspace, state, dt, st))) return r;
+        if ((r = energy_forces_impl(*dims, packed, s2, L, path, out, workspace, st))) return r;
+        if ((r = md_kick(L, workspace, state, dt, sys->mol_ptr, sys->n_mol, s == n_steps - 1, st))) return r;
+    }
+    return MLFF_OK;
+}
+
+int mlff_read_status(const void* workspace, int32_t* code, int64_t* n_edges, int32_t* where, mlff_stream_t stream) {
+    if (!workspace) { set_error("workspace is NULL"); return MLFF_ERR_INVALID; }
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    Status s;
+    MLFF_CUDA(cudaMemcpyAsync(&s, workspace, sizeof(Status), cudaMemcpyDeviceToHost, st));
+    MLFF_CUDA(cudaStreamSynchronize(st));
+    if (code) *code = s.code;
+    if (n_edges) *n_edges = ((int64_t)s.n_edges_hi << 31) | (int64_t)(uint32_t)s.n_edges;
+    if (where) *where = s.code ? s.where : -1;
+    return MLFF_OK;
+}
+
+int mlff_clear_status(void* workspace, mlff_stream_t stream) {
+    if (!workspace) { set_error("workspace is NULL"); return MLFF_ERR_INVALID; }
+    MLFF_CUDA(cudaMemsetAsync(workspace, 0, sizeof(Status), reinterpret_cast<cudaStream_t>(stream)));
+    return MLFF_OK;
+}
+
+}  // extern "C"

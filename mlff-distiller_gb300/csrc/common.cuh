@@ -1,0 +1,137 @@
+// Shared definitions for the mlff_gb300 CUDA library (sm_103a).
+#pragma once
+#include <cstdint>
+#include <cstddef>
+#include <cuda_runtime.h>
+#include "../../include/mlff_gb300.h"
+
+namespace mlff {
+
+constexpr int H = 128;        // hidden width (StudentForceField default)
+constexpr int H3 = 3 * H;     // filter / update output width
+constexpr int RMAX = 32;      // padded number of radial basis functions
+constexpr int MAXL = 8;       // maximum number of interaction blocks
+
+// Device status word layout (int32[8], lives in the workspace).
+//   [0] status code (MLFF_OK or an MLFF_ERR_* value)
+//   [1] edges found by the neighbour build (low 31 bits; saturates)
+//   [2] first offending atom / molecule for row or box errors
+//   [3] edge count high word (edges >> 31)
+struct Status {
+    int32_t code;
+    int32_t n_edges;
+    int32_t where;
+    int32_t n_edges_hi;
+    int32_t pad[4];
+};
+
+__device__ __forceinline__ void set_status(Status* st, int code, int where) {
+    if (atomicCAS(&st->code, 0, code) == 0) st->where = where;
+}
+
+__device__ __forceinline__ float silu_f(float x) {
+    return x / (1.0f + expf(-x));
+}
+// sigmoid and silu'(z) = s (1 + z (1 - s))
+__device__ __forceinline__ float sigmoid_f(float x) { return 1.0f / (1.0f + expf(-x)); }
+__device__ __forceinline__ float dsilu_f(float x) {
+    float s = sigmoid_f(x);
+    return s * (1.0f + x * (1.0f - s));
+}
+
+// float32 |d| rounded as the reference's torch.norm: x*x rounded, then two
+// fused multiply-adds, then a correctly rounded square root.
+__device__ __forceinline__ float pair_distance(float dx, float dy, float dz) {
+    return __fsqrt_rn(__fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx))));
+}
+
+// Minimum image along one periodic axis: k = rint(dx / L) (via the rounded
+// reciprocal), dx' = fma(-k, L, dx).  Exactly antisymmetric in dx.
+__device__ __forceinline__ float min_image(float dx, float L, float invL) {
+    float k = rintf(__fmul_rn(dx, invL));
+    return __fmaf_rn(-k, L, dx);
+}
+
+struct Box {
+    float L[3];
+    float invL[3];
+    int periodic;
+};
+
+// Edge vector r = pos[src] - pos[dst] (+ minimum image) exactly as the
+// neighbour build decided it.
+__device__ __forceinline__ float3 edge_vector(float4 ps, float4 pd, const Box& b) {
+    float dx = __fsub_rn(ps.x, pd.x);
+    float dy = __fsub_rn(ps.y, pd.y);
+    float dz = __fsub_rn(ps.z, pd.z);
+    if (b.periodic) {
+        dx = min_image(dx, b.L[0], b.invL[0]);
+        dy = min_image(dy, b.L[1], b.invL[1]);
+        dz = min_image(dz, b.L[2], b.invL[2]);
+    }
+    return make_float3(dx, dy, dz);
+}
+
+// Packed fp32 parameters (built by mlff_pack_weights from the state_dict).
+// All offsets are in floats from the start of the packed blob.
+struct LayerOffsets {
+    int64_t w1t;    // [RMAX][H]   filter Linear(R->H) weight, transposed, zero padded
+    int64_t w1;     // [H][RMAX]   same, original orientation
+    int64_t b1;     // [H]
+    int64_t w2t;    // [H][H3]     filter Linear(H->3H) weight, transposed
+    int64_t w2;     // [H3][H]     original orientation
+    int64_t b2;     // [H3]
+    int64_t mix;    // [9]
+    int64_t u1t;    // [2H][H]     update Linear(2H->H), transposed
+    int64_t u1;     // [H][2H]
+    int64_t c1;     // [H]
+    int64_t u2t;    // [H][H3]     update Linear(H->3H), transposed
+    int64_t u2;     // [H3][H]
+    int64_t c2;     // [H3]
+    int64_t w1_bf;  // bf16 hi/lo tiles for the tensor-core filter (bytes offset / 4)
+    int64_t w2_bf;
+    int64_t u1_bf;
+    int64_t u2_bf;
+};
+
+struct PackedOffsets {
+    int64_t emb;       // [S][H]
+    int64_t centers;   // [RMAX]
+    int64_t gamma;     // [RMAX]  1/w^2 (0 for padding)
+    int64_t head_w1t;  // [H][64]
+    int64_t head_w1;   // [64][H]
+    int64_t head_b1;   // [64]
+    int64_t head_w2t;  // [64][32]
+    int64_t head_w2;   // [32][64]
+    int64_t head_b2;   // [32]
+    int64_t head_w3;   // [32]
+    int64_t head_b3;   // [1]
+    LayerOffsets layer[MAXL];
+    int64_t total;     // floats
+};
+
+PackedOffsets packed_offsets(const mlff_dims& d);
+
+}  // namespace mlff
+
+// ----- error handling shared by the host side of the library -----
+namespace mlff {
+void set_error(const char* fmt, ...);
+int cuda_status(cudaError_t e, const char* what);
+void prof_count_launch();   // profile.cu: one kernel launch of the current kind
+}
+
+#define MLFF_CUDA(call)                                                     \
+    do {                                                                    \
+        cudaError_t _e = (call);                                            \
+        if (_e != cudaSuccess) return mlff::cuda_status(_e, #call);         \
+    } while (0)
+
+// Every kernel launch is followed by this check (it also counts the launch
+// for the optional benchmark profile).
+#define MLFF_LAUNCH_CHECK(what)                                             \
+    do {                                                                    \
+        cudaError_t _e = cudaGetLastError();                                \
+        mlff::prof_count_launch();                                          \
+        if (_e != cudaSuccess) return mlff::cuda_status(_e, what);          \
+    } while (0)

@@ -1,0 +1,474 @@
+// Radius graph on the GPU: bit-exact with the reference's
+// radius_graph_native (src/mlff_distiller/models/student_model.py:63-109)
+// plus an orthorhombic minimum-image rule for periodic boxes.
+//
+// Output: receiver-sorted CSR.  Row a lists, in ascending order, every atom
+// b of the same structure with |pos[b] - pos[a]| <= cutoff (float32, same
+// rounding as torch.norm), b != a.  Read as [row; col] this equals the
+// reference's edge_index (src-major, then dst) element for element.  In the
+// model kernels row a is the receiver of the message b -> a.
+//
+// Open structures: every atom pair of the structure is tested (one warp per
+// row, warp-ballot compaction keeps the ascending order).  Periodic boxes:
+// atoms are binned into cells of edge >= cutoff, each row gathers
+// candidates from the 27 (or fewer, for small grids) neighbouring cells,
+// compacts hits with a warp ballot into shared memory and rank-sorts them.
+#include "common.cuh"
+#include "workspace.h"
+#include "profile.h"
+
+namespace mlff {
+
+constexpr int NBR_WARPS = 8;        // warps per block in the row kernels
+constexpr int ROW_CAP = 512;        // neighbours one periodic row can hold
+
+// ------------------------------------------------------------------ scan
+__global__ void scan_local_kernel(int32_t* __restrict__ data, int64_t n, int32_t* __restrict__ sums) {
+    __shared__ int32_t warp_tot[8];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const int64_t base = (int64_t)blockIdx.x * 1024 + (int64_t)t * 4;
+    int32_t v[4], s = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        int64_t idx = base + i;
+        v[i] = idx < n ? data[idx] : 0;
+        s += v[i];
+    }
+    int32_t x = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int32_t wt = lane < 8 ? warp_tot[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1) {
+            int32_t y = __shfl_up_sync(0xffffffffu, wt, o);
+            if (lane >= o) wt += y;
+        }
+        if (lane < 8) warp_tot[lane] = wt;
+    }
+    __syncthreads();
+    int32_t run = x - s + (w > 0 ? warp_tot[w - 1] : 0);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        int64_t idx = base + i;
+        if (idx < n) data[idx] = run;
+        run += v[i];
+    }
+    if (t == 255) sums[blockIdx.x] = run;
+}
+
+// exclusive scan of sums[0..nb) by one block; sums[nb] receives the total
+__global__ void scan_blocks_kernel(int32_t* __restrict__ sums, int64_t nb) {
+    __shared__ int32_t warp_tot[32];
+    __shared__ int32_t carry;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    if (t == 0) carry = 0;
+    __syncthreads();
+    for (int64_t c0 = 0; c0 < nb; c0 += 1024) {
+        int64_t idx = c0 + t;
+        int32_t v = idx < nb ? sums[idx] : 0;
+        int32_t x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_tot[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            int32_t wt = warp_tot[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int32_t y = __shfl_up_sync(0xffffffffu, wt, o);
+                if (lane >= o) wt += y;
+            }
+            warp_tot[lane] = wt;
+        }
+        __syncthreads();
+        int32_t excl = carry + x - v + (w > 0 ? warp_tot[w - 1] : 0);
+        if (idx < nb) sums[idx] = excl;
+        __syncthreads();
+        if (t == 1023) carry = excl + v;
+        __syncthreads();
+    }
+    if (t == 0) sums[nb] = carry;
+}
+
+__global__ void scan_add_kernel(int32_t* __restrict__ data, int64_t n, const int32_t* __restrict__ sums) {
+    const int64_t base = (int64_t)blockIdx.x * 1024;
+    const int32_t add = sums[blockIdx.x];
+    for (int i = threadIdx.x; i < 1024; i += blockDim.x) {
+        int64_t idx = base + i;
+        if (idx < n) data[idx] += add;
+    }
+}
+
+// In-place exclusive scan of n int32 values; tmp holds ceil(n/1024)+1 ints.
+int launch_scan(int32_t* data, int64_t n, int32_t* tmp, cudaStream_t st) {
+    if (n <= 0) return MLFF_OK;
+    int64_t nb = (n + 1023) / 1024;
+    scan_local_kernel<<<(unsigned)nb, 256, 0, st>>>(data, n, tmp);
+    MLFF_LAUNCH_CHECK("scan_local");
+    scan_blocks_kernel<<<1, 1024, 0, st>>>(tmp, nb);
+    MLFF_LAUNCH_CHECK("scan_blocks");
+    if (nb > 1) {
+        scan_add_kernel<<<(unsigned)nb, 256, 0, st>>>(data, n, tmp);
+        MLFF_LAUNCH_CHECK("scan_add");
+    }
+    return MLFF_OK;
+}
+
+// ------------------------------------------------------------ atom setup
+__global__ void prep_atoms_kernel(const float* __restrict__ pos, const int64_t* __restrict__ mol_ptr,
+                                  int32_t n_mol, int32_t n_atoms, float4* __restrict__ pos4,
+                                  int32_t* __restrict__ atom_mol) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_atoms; i += gridDim.x * blockDim.x) {
+        pos4[i] = make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0.0f);
+        // last m with mol_ptr[m] <= i
+        int lo = 0, hi = n_mol - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (mol_ptr[mid] <= i) lo = mid; else hi = mid - 1;
+        }
+        atom_mol[i] = lo;
+    }
+}
+
+// One block: per periodic structure choose the cell grid (cells of edge
+// >= cutoff, at most max(n_atoms, 27) cells) and the first cell index.
+__global__ void mol_grid_kernel(const int64_t* __restrict__ mol_ptr, const float* __restrict__ box,
+                                const uint8_t* __restrict__ pbc, int32_t n_mol, float cutoff,
+                                int4* __restrict__ grid, Status* st) {
+    __shared__ int32_t warp_tot[32];
+    __shared__ int32_t carry;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    if (t == 0) carry = 0;
+    __syncthreads();
+    for (int c0 = 0; c0 < n_mol; c0 += 1024) {
+        int m = c0 + t;
+        int ncell = 0, nc[3] = {0, 0, 0};
+        if (m < n_mol && pbc != nullptr && box != nullptr && pbc[m]) {
+            int n_m = (int)(mol_ptr[m + 1] - mol_ptr[m]);
+            bool ok = true;
+            for (int a = 0; a < 3; ++a) {
+                float L = box[3 * m + a];
+                if (!(L >= 2.0f * cutoff) || !isfinite(L)) ok = false;
+                else nc[a] = max(1, (int)floorf(L / (cutoff * 1.0001f)));  // cell edge > cutoff with margin
+            }
+            if (!ok) {
+                set_status(st, MLFF_ERR_BOX, m);
+                nc[0] = nc[1] = nc[2] = 1;
+            }
+            int lim = max(n_m, 27);
+            while ((long long)nc[0] * nc[1] * nc[2] > lim) {
+                int a = (nc[0] >= nc[1] && nc[0] >= nc[2]) ? 0 : (nc[1] >= nc[2] ? 1 : 2);
+                nc[a] -= 1;
+            }
+            ncell = nc[0] * nc[1] * nc[2];
+        }
+        int32_t x = ncell;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_tot[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            int32_t wt = warp_tot[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int32_t y = __shfl_up_sync(0xffffffffu, wt, o);
+                if (lane >= o) wt += y;
+            }
+            warp_tot[lane] = wt;
+        }
+        __syncthreads();
+        int32_t excl = carry + x - ncell + (w > 0 ? warp_tot[w - 1] : 0);
+        if (m < n_mol) grid[m] = make_int4(nc[0], nc[1], nc[2], excl);
+        __syncthreads();
+        if (t == 1023) carry = excl + ncell;
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ bool mol_periodic(const uint8_t* pbc, const float* box, int m) {
+    return pbc != nullptr && box != nullptr && pbc[m] != 0;
+}
+
+__device__ __forceinline__ Box load_box(const float* box, const uint8_t* pbc, int m) {
+    Box b;
+    b.periodic = mol_periodic(pbc, box, m) ? 1 : 0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        b.L[a] = b.periodic ? box[3 * m + a] : 1.0f;
+        b.invL[a] = __fdiv_rn(1.0f, b.L[a]);
+    }
+    return b;
+}
+
+__device__ __forceinline__ int cell_coord(float x, float L, float invL, int nc) {
+    float w = x - L * floorf(x * invL);
+    int c = (int)(w * invL * (float)nc);
+    return min(max(c, 0), nc - 1);
+}
+
+__global__ void cell_count_kernel(const float4* __restrict__ pos4, const int32_t* __restrict__ atom_mol,
+                                  const float* __restrict__ box, const uint8_t* __restrict__ pbc,
+                                  const int4* __restrict__ grid, int32_t n_atoms,
+                                  int32_t* __restrict__ atom_cell, int32_t* __restrict__ cell_count) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_atoms; i += gridDim.x * blockDim.x) {
+        int m = atom_mol[i];
+        if (!mol_periodic(pbc, box, m)) { atom_cell[i] = -1; continue; }
+        int4 g = grid[m];
+        Box b = load_box(box, pbc, m);
+        float4 p = pos4[i];
+        int cx = cell_coord(p.x, b.L[0], b.invL[0], g.x);
+        int cy = cell_coord(p.y, b.L[1], b.invL[1], g.y);
+        int cz = cell_coord(p.z, b.L[2], b.invL[2], g.z);
+        int c = g.w + (cx * g.y + cy) * g.z + cz;
+        atom_cell[i] = c;
+        atomicAdd(&cell_count[c], 1);
+    }
+}
+
+__global__ void cell_fill_kernel(const int32_t* __restrict__ atom_cell, const int32_t* __restrict__ cell_start,
+                                 int32_t n_atoms, int32_t* __restrict__ cell_fill,
+                                 int32_t* __restrict__ cell_atoms) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_atoms; i += gridDim.x * blockDim.x) {
+        int c = atom_cell[i];
+        if (c < 0) continue;
+        int slot = atomicAdd(&cell_fill[c], 1);
+        cell_atoms[cell_start[c] + slot] = i;
+    }
+}
+
+// -------------------------------------------------------------- rows
+struct NbrArgs {
+    const float4* pos4;
+    const int32_t* atom_mol;
+    const int64_t* mol_ptr;
+    const float* box;
+    const uint8_t* pbc;
+    const int4* grid;
+    const int32_t* cell_start;
+    const int32_t* cell_atoms;
+    const int32_t* atom_cell;
+    int32_t n_atoms;
+    float cutoff;
+    int64_t cap;
+    int32_t* counts;   // count pass: per-row counts; fill pass: row_ptr
+    int32_t* col;
+    int32_t* erecv;
+    Status* st;
+};
+
+template <bool FILL>
+__global__ void __launch_bounds__(NBR_WARPS * 32) nbr_rows_kernel(NbrArgs a) {
+    __shared__ int32_t sbuf[FILL ? NBR_WARPS : 1][FILL ? ROW_CAP : 1];
+    if (FILL && a.st->code != 0) return;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int nwarps = gridDim.x * NBR_WARPS;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    for (int i = blockIdx.x * NBR_WARPS + wib; i < a.n_atoms; i += nwarps) {
+        const int m = a.atom_mol[i];
+        const float4 pi = a.pos4[i];
+        const Box b = load_box(a.box, a.pbc, m);
+        int cnt = 0;
+        const int base = FILL ? a.counts[i] : 0;
+        if (!b.periodic) {
+            const int a0 = (int)a.mol_ptr[m], a1 = (int)a.mol_ptr[m + 1];
+            for (int j0 = a0; j0 < a1; j0 += 32) {
+                const int j = j0 + lane;
+                bool ok = false;
+                if (j < a1 && j != i) {
+                    float4 pj = a.pos4[j];
+                    float3 r = edge_vector(pj, pi, b);
+                    ok = pair_distance(r.x, r.y, r.z) <= a.cutoff;
+                }
+                const unsigned mask = __ballot_sync(0xffffffffu, ok);
+                if (FILL && ok) {
+                    int64_t p = (int64_t)base + cnt + __popc(mask & lt_mask);
+                    a.col[p] = j;
+                    a.erecv[p] = i;
+                }
+                cnt += __popc(mask);
+            }
+        } else {
+            const int4 g = a.grid[m];
+            const int ci = a.atom_cell[i] - g.w;
+            const int cc[3] = {ci / (g.y * g.z), (ci / g.z) % g.y, ci % g.z};
+            const int ncs[3] = {g.x, g.y, g.z};
+            int lo[3], hi[3];
+#pragma unroll
+            for (int ax = 0; ax < 3; ++ax) {
+                if (ncs[ax] >= 3) { lo[ax] = -1; hi[ax] = 1; }
+                else { lo[ax] = 0; hi[ax] = ncs[ax] - 1; }
+            }
+            bool overflow = false;
+            for (int ox = lo[0]; ox <= hi[0]; ++ox)
+            for (int oy = lo[1]; oy <= hi[1]; ++oy)
+            for (int oz = lo[2]; oz <= hi[2]; ++oz) {
+                int q[3];
+                const int o[3] = {ox, oy, oz};
+#pragma unroll
+                for (int ax = 0; ax < 3; ++ax)
+                    q[ax] = ncs[ax] >= 3 ? ((cc[ax] + o[ax]) % ncs[ax] + ncs[ax]) % ncs[ax] : o[ax];
+                const int qc = g.w + (q[0] * g.y + q[1]) * g.z + q[2];
+                const int t0 = a.cell_start[qc], t1 = a.cell_start[qc + 1];
+                for (int t = t0; t < t1; t += 32) {
+                    bool ok = false;
+                    int j = -1;
+                    if (t + lane < t1) {
+                        j = a.cell_atoms[t + lane];
+                        if (j != i) {
+                            float4 pj = a.pos4[j];
+                            float3 r = edge_vector(pj, pi, b);
+                            ok = pair_distance(r.x, r.y, r.z) <= a.cutoff;
+                        }
+                    }
+                    const unsigned mask = __ballot_sync(0xffffffffu, ok);
+                    if (FILL) {
+                        const int slot = cnt + __popc(mask & lt_mask);
+                        if (ok && slot < ROW_CAP) sbuf[wib][slot] = j;
+                    }
+                    cnt += __popc(mask);
+                }
+            }
+            if (cnt > ROW_CAP) overflow = true;
+            if (FILL) {
+                __syncwarp();
+                if (overflow) {
+                    if (lane == 0) set_status(a.st, MLFF_ERR_ROW, i);
+                } else {
+                    // rank sort: neighbour indices in a row are distinct
+                    for (int k = lane; k < cnt; k += 32) {
+                        const int v = sbuf[wib][k];
+                        int rank = 0;
+                        for (int q2 = 0; q2 < cnt; ++q2) rank += sbuf[wib][q2] < v ? 1 : 0;
+                        int64_t p = (int64_t)base + rank;
+                        a.col[p] = v;
+                        a.erecv[p] = i;
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        if (!FILL && lane == 0) a.counts[i] = cnt;
+    }
+}
+
+__global__ void check_edges_kernel(const int32_t* __restrict__ row_ptr, int32_t n_atoms, int64_t cap,
+                                   const int32_t* __restrict__ counts_total, Status* st) {
+    int64_t e = (int64_t)(uint32_t)row_ptr[n_atoms];
+    st->n_edges = (int32_t)(e & 0x7fffffff);
+    st->n_edges_hi = (int32_t)(e >> 31);
+    if (e > cap) set_status(st, MLFF_ERR_CAPACITY, -1);
+    (void)counts_total;
+}
+
+// rev[k]: position of the reversed edge (row b, col a) for edge k = (row a, col b)
+__global__ void rev_kernel(const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
+                           const int32_t* __restrict__ erecv, int32_t n_atoms,
+                           int32_t* __restrict__ rev, Status* st) {
+    if (st->code != 0) return;
+    const int32_t E = row_ptr[n_atoms];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < E; k += gridDim.x * blockDim.x) {
+        const int a = erecv[k], b = col[k];
+        int lo = row_ptr[b], hi = row_ptr[b + 1] - 1, found = -1;
+        while (lo <= hi) {
+            int mid = (lo + hi) >> 1;
+            int v = col[mid];
+            if (v == a) { found = mid; break; }
+            if (v < a) lo = mid + 1; else hi = mid - 1;
+        }
+        if (found < 0) set_status(st, MLFF_ERR_INVALID, k);
+        rev[k] = found < 0 ? k : found;
+    }
+}
+
+// receiver partition for the persistent edge kernels: part[p] is the first
+// receiver whose row starts at or after p*E/P
+__global__ void partition_kernel(const int32_t* __restrict__ row_ptr, int32_t n_atoms, int32_t P,
+                                 int32_t* __restrict__ part) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p > P) return;
+    const int64_t E = row_ptr[n_atoms];
+    if (p == 0) { part[0] = 0; return; }
+    if (p == P) { part[P] = n_atoms; return; }
+    const int64_t target = (E * p + P - 1) / P;
+    int lo = 0, hi = n_atoms;   // first a with row_ptr[a] >= target
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (row_ptr[mid] >= target) hi = mid; else lo = mid + 1;
+    }
+    part[p] = lo;
+}
+
+int launch_partition(const WsLayout& L, void* ws, cudaStream_t st) {
+    ProfScope prof(PK_NEIGHBORS, st);
+    partition_kernel<<<(L.P + 1 + 255) / 256, 256, 0, st>>>(ws_ptr<int32_t>(ws, L.row_ptr), L.N, L.P,
+                                                            ws_ptr<int32_t>(ws, L.part));
+    MLFF_LAUNCH_CHECK("partition");
+    return MLFF_OK;
+}
+
+int launch_neighbors(const mlff_dims& d, const mlff_system& sys, const WsLayout& L, void* ws,
+                     cudaStream_t st) {
+    ProfScope prof(PK_NEIGHBORS, st);
+    const int N = sys.n_atoms;
+    Status* status = ws_ptr<Status>(ws, L.status);
+    float4* pos4 = ws_ptr<float4>(ws, L.pos4);
+    int32_t* atom_mol = ws_ptr<int32_t>(ws, L.atom_mol);
+    int32_t* row_ptr = ws_ptr<int32_t>(ws, L.row_ptr);
+    int32_t* scan_tmp = ws_ptr<int32_t>(ws, L.scan_tmp);
+    const bool any_pbc = sys.pbc != nullptr && sys.box != nullptr;
+    const int tb = 256;
+    const int gb = (int)std::min<int64_t>((N + tb - 1) / tb, 152 * 16);
+    prep_atoms_kernel<<<std::max(gb, 1), tb, 0, st>>>(sys.pos, sys.mol_ptr, sys.n_mol, N, pos4, atom_mol);
+    MLFF_LAUNCH_CHECK("prep_atoms");
+    int4* grid = ws_ptr<int4>(ws, L.mol_grid);
+    int32_t* cell_count = ws_ptr<int32_t>(ws, L.cell_count);
+    int32_t* cell_fill = ws_ptr<int32_t>(ws, L.cell_fill);
+    int32_t* cell_atoms = ws_ptr<int32_t>(ws, L.cell_atoms);
+    int32_t* atom_cell = ws_ptr<int32_t>(ws, L.atom_cell);
+    if (any_pbc) {
+        mol_grid_kernel<<<1, 1024, 0, st>>>(sys.mol_ptr, sys.box, sys.pbc, sys.n_mol, d.cutoff, grid, status);
+        MLFF_LAUNCH_CHECK("mol_grid");
+        MLFF_CUDA(cudaMemsetAsync(cell_count, 0, sizeof(int32_t) * (L.ncell_cap + 1), st));
+        MLFF_CUDA(cudaMemsetAsync(cell_fill, 0, sizeof(int32_t) * L.ncell_cap, st));
+        cell_count_kernel<<<std::max(gb, 1), tb, 0, st>>>(pos4, atom_mol, sys.box, sys.pbc, grid, N,
+                                                          atom_cell, cell_count);
+        MLFF_LAUNCH_CHECK("cell_count");
+        int r = launch_scan(cell_count, L.ncell_cap + 1, scan_tmp, st);
+        if (r) return r;
+        cell_fill_kernel<<<std::max(gb, 1), tb, 0, st>>>(atom_cell, cell_count, N, cell_fill, cell_atoms);
+        MLFF_LAUNCH_CHECK("cell_fill");
+    }
+    NbrArgs a;
+    a.pos4 = pos4; a.atom_mol = atom_mol; a.mol_ptr = sys.mol_ptr; a.box = sys.box; a.pbc = sys.pbc;
+    a.grid = grid; a.cell_start = cell_count; a.cell_atoms = cell_atoms; a.atom_cell = atom_cell;
+    a.n_atoms = N; a.cutoff = d.cutoff; a.cap = L.cap; a.counts = row_ptr;
+    a.col = ws_ptr<int32_t>(ws, L.col); a.erecv = ws_ptr<int32_t>(ws, L.erecv); a.st = status;
+    const int rows_blocks = (int)std::max<int64_t>(1, std::min<int64_t>((N + NBR_WARPS - 1) / NBR_WARPS, 152 * 32));
+    MLFF_CUDA(cudaMemsetAsync(row_ptr + N, 0, sizeof(int32_t), st));
+    nbr_rows_kernel<false><<<rows_blocks, NBR_WARPS * 32, 0, st>>>(a);
+    MLFF_LAUNCH_CHECK("nbr_count");
+    int r = launch_scan(row_ptr, (int64_t)N + 1, scan_tmp, st);
+    if (r) return r;
+    check_edges_kernel<<<1, 1, 0, st>>>(row_ptr, N, L.cap, nullptr, status);
+    MLFF_LAUNCH_CHECK("check_edges");
+    nbr_rows_kernel<true><<<rows_blocks, NBR_WARPS * 32, 0, st>>>(a);
+    MLFF_LAUNCH_CHECK("nbr_fill");
+    const int eb = (int)std::min<int64_t>((L.cap + 255) / 256, 152 * 16);
+    rev_kernel<<<std::max(eb, 1), 256, 0, st>>>(row_ptr, a.col, a.erecv, N, ws_ptr<int32_t>(ws, L.rev), status);
+    MLFF_LAUNCH_CHECK("rev");
+    return MLFF_OK;
+}
+
+}  // namespace mlff

@@ -1,0 +1,85 @@
+// Workspace layout: one caller-owned device buffer carved into the arrays
+// the kernels need.  Everything is addressed by byte offsets aligned to 256.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include "common.cuh"
+
+namespace mlff {
+
+struct WsLayout {
+    int32_t N, B, L, P;        // atoms, structures, layers, persistent CTAs
+    int64_t cap;               // edge capacity
+    int64_t ncell_cap;         // cell-list capacity (periodic structures)
+    size_t status;             // Status
+    size_t pos4;               // float4 [N]
+    size_t atom_mol;           // int32 [N]
+    size_t row_ptr;            // int32 [N+1]
+    size_t col;                // int32 [cap]  sender of each edge
+    size_t erecv;              // int32 [cap]  receiver of each edge
+    size_t rev;                // int32 [cap]  index of the reversed edge
+    size_t edge_acc;           // float4 [cap] (dE/dd, dE/du) summed over layers
+    size_t scan_tmp;           // int32 [scan_blocks + 1]
+    size_t mol_grid;           // int4 [B]  (ncx, ncy, ncz, first cell)
+    size_t cell_count;         // int32 [ncell_cap + 1]
+    size_t cell_fill;          // int32 [ncell_cap]
+    size_t cell_atoms;         // int32 [N]
+    size_t atom_cell;          // int32 [N]
+    size_t part;               // int32 [P + 1] receiver partition
+    size_t X;                  // float [L+1][N][4][H]  layer inputs (s, v_x, v_y, v_z)
+    size_t Xt;                 // float [L][N][4][H]    after the message step
+    size_t uz;                 // float [L][N][H]       update MLP pre-activation
+    size_t ua;                 // float [L][N][3H]      update MLP output (ds, g1, g2)
+    size_t xbar;               // float [2][N][4][H]    adjoints
+    size_t e_atom;             // float [N]
+    size_t md_pos32;           // float [N][3]  positions the integrator hands to the force call
+    // plain path (materialised per-edge tensors, like the reference's graph)
+    size_t geo;                // float4 [cap] (u_x, u_y, u_z, d)
+    size_t erbf;               // float [cap][RMAX]
+    size_t erbf_d;             // float [cap][RMAX]
+    size_t fz;                 // float [L][cap][H]
+    size_t ff;                 // float [L][cap][3H]
+    size_t fh;                 // float [cap][H]
+    size_t fbar;               // float [cap][3H]
+    size_t comb;               // float [N][2H]
+    size_t uh;                 // float [N][H]
+    size_t abar;               // float [N][3H]
+    size_t total;
+};
+
+WsLayout ws_layout(const mlff_dims& d, int32_t n_atoms, int32_t n_mol, int64_t cap, int32_t path);
+
+template <typename T>
+inline T* ws_ptr(void* ws, size_t off) {
+    return reinterpret_cast<T*>(static_cast<char*>(ws) + off);
+}
+template <typename T>
+inline const T* ws_ptr(const void* ws, size_t off) {
+    return reinterpret_cast<const T*>(static_cast<const char*>(ws) + off);
+}
+
+// Kernel launch helpers implemented in the .cu files.
+int launch_neighbors(const mlff_dims& d, const mlff_system& sys, const WsLayout& L, void* ws,
+                     cudaStream_t st);
+int launch_embed(const mlff_dims& d, const float* packed, const PackedOffsets& po,
+                 const mlff_system& sys, const WsLayout& L, void* ws, cudaStream_t st);
+int launch_readout(const mlff_dims& d, const float* packed, const PackedOffsets& po,
+                   const mlff_system& sys, const WsLayout& L, void* ws, const mlff_outputs& out,
+                   int want_grad, cudaStream_t st);
+int launch_forces(const mlff_dims& d, const mlff_system& sys, const WsLayout& L, void* ws,
+                  const mlff_outputs& out, cudaStream_t st);
+int run_plain(const mlff_dims& d, const float* packed, const PackedOffsets& po,
+              const mlff_system& sys, const WsLayout& L, void* ws, const mlff_outputs& out,
+              cudaStream_t st);
+int run_tuned(const mlff_dims& d, const float* packed, const PackedOffsets& po,
+              const mlff_system& sys, const WsLayout& L, void* ws, const mlff_outputs& out,
+              int path, cudaStream_t st);
+int launch_partition(const WsLayout& L, void* ws, cudaStream_t st);
+int launch_scan(int32_t* data, int64_t n, int32_t* tmp, cudaStream_t st);
+int launch_update_fwd(const mlff_dims& d, const float* packed, const LayerOffsets& lo,
+                      const WsLayout& L, void* ws, int layer, cudaStream_t st);
+int launch_update_bwd(const mlff_dims& d, const float* packed, const LayerOffsets& lo,
+                      const WsLayout& L, void* ws, int layer, const float* xbar_out,
+                      float* xtbar, cudaStream_t st);
+
+}  // namespace mlff

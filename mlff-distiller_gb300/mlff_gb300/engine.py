@@ -1,0 +1,203 @@
+"""Device-side evaluation engine: packed weights + one workspace + the
+C-ABI calls, on the current torch CUDA stream.
+
+``Engine.energy_forces`` is the single entry the module, the calculator,
+the MD driver and the benchmark use.  It grows the edge capacity and the
+workspace when the neighbour build reports that they were too small and
+re-runs the call.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from typing import Dict, Optional, Tuple
+
+import torch
+
+from . import _lib
+
+DEFAULT_EDGES_PER_ATOM = 64
+
+
+def _stream_handle() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+@dataclass
+class Batch:
+    """A ragged batch on the device (int64 Z, float32 positions, CSR
+    molecule offsets, optional orthorhombic boxes and periodic flags)."""
+    Z: torch.Tensor
+    pos: torch.Tensor
+    mol_ptr: torch.Tensor
+    box: Optional[torch.Tensor] = None
+    pbc: Optional[torch.Tensor] = None
+
+    @property
+    def n_atoms(self) -> int:
+        return int(self.Z.shape[0])
+
+    @property
+    def n_mol(self) -> int:
+        return int(self.mol_ptr.shape[0] - 1)
+
+    def system(self) -> _lib.System:
+        s = _lib.System()
+        s.n_atoms = self.n_atoms
+        s.n_mol = self.n_mol
+        s.pos = self.pos.data_ptr()
+        s.Z = self.Z.data_ptr()
+        s.mol_ptr = self.mol_ptr.data_ptr()
+        s.box = None if self.box is None else self.box.data_ptr()
+        s.pbc = None if self.pbc is None else self.pbc.data_ptr()
+        return s
+
+
+def make_batch(Z, pos, mol_ptr, box=None, pbc=None, device="cuda") -> Batch:
+    dev = torch.device(device)
+    Zt = torch.as_tensor(Z).to(device=dev, dtype=torch.int64).contiguous()
+    Pt = torch.as_tensor(pos).to(device=dev, dtype=torch.float32).contiguous()
+    Mt = torch.as_tensor(mol_ptr).to(device=dev, dtype=torch.int64).contiguous()
+    Bt = Ct = None
+    if pbc is not None:
+        pb = torch.as_tensor(pbc).to(dtype=torch.bool).reshape(-1)
+        if bool(pb.any()):
+            Bt = torch.as_tensor(box).to(device=dev, dtype=torch.float32).reshape(-1, 3).contiguous()
+            Ct = pb.to(device=dev, dtype=torch.uint8).contiguous()
+    return Batch(Zt, Pt, Mt, Bt, Ct)
+
+
+def dims_of(hidden, n_rbf, n_layers, n_species, cutoff) -> _lib.Dims:
+    d = _lib.Dims()
+    d.hidden, d.n_rbf, d.n_layers, d.n_species, d.cutoff = hidden, n_rbf, n_layers, n_species, cutoff
+    return d
+
+
+class Engine:
+    """Owns the packed weights and a growable workspace for one model."""
+
+    def __init__(self, dims: _lib.Dims, device="cuda"):
+        if not torch.cuda.is_available():
+            raise RuntimeError("mlff_gb300 needs a CUDA device (GB300, sm_103a); none is available")
+        self.lib = _lib.load()
+        self.dims = dims
+        self.device = torch.device(device)
+        nbytes = self.lib.mlff_packed_weights_size(ctypes.byref(dims))
+        if nbytes == 0:
+            raise _lib.MLFFError(_lib.ERR_UNSUPPORTED, _lib.last_error())
+        self.packed = torch.zeros(nbytes // 4, dtype=torch.float32, device=self.device)
+        self.workspace: Optional[torch.Tensor] = None
+        self.edge_capacity: Dict[int, int] = {}
+        self._param_version = None
+
+    # -------------------------------------------------------------- weights
+    def pack(self, sd: Dict[str, torch.Tensor]):
+        """Pack a reference-layout state_dict (float32 tensors on device)."""
+        L = self.dims.n_layers
+        t = {k: v.detach().to(device=self.device, dtype=torch.float32).contiguous() for k, v in sd.items()}
+        self._keep = t
+        p = _lib.Params()
+        p.embedding = t["embedding.weight"].data_ptr()
+        p.rbf_centers = t["rbf.centers"].data_ptr()
+        p.rbf_widths = t["rbf.widths"].data_ptr()
+        for l in range(L):
+            pre = f"interactions.{l}."
+            p.filter_w1[l] = t[pre + "message.rbf_to_scalar.0.weight"].data_ptr()
+            p.filter_b1[l] = t[pre + "message.rbf_to_scalar.0.bias"].data_ptr()
+            p.filter_w2[l] = t[pre + "message.rbf_to_scalar.2.weight"].data_ptr()
+            p.filter_b2[l] = t[pre + "message.rbf_to_scalar.2.bias"].data_ptr()
+            p.mixing[l] = t[pre + "update.mixing_matrix"].data_ptr()
+            p.update_w1[l] = t[pre + "update.update_mlp.0.weight"].data_ptr()
+            p.update_b1[l] = t[pre + "update.update_mlp.0.bias"].data_ptr()
+            p.update_w2[l] = t[pre + "update.update_mlp.2.weight"].data_ptr()
+            p.update_b2[l] = t[pre + "update.update_mlp.2.bias"].data_ptr()
+        for i, k in ((1, "0"), (2, "2"), (3, "4")):
+            setattr(p, f"head_w{i}", t[f"energy_head.{k}.weight"].data_ptr())
+            setattr(p, f"head_b{i}", t[f"energy_head.{k}.bias"].data_ptr())
+        _lib.check(self.lib.mlff_pack_weights(ctypes.byref(self.dims), ctypes.byref(p),
+                                              self.packed.data_ptr(), self.packed.numel() * 4,
+                                              _stream_handle()))
+        torch.cuda.current_stream().synchronize()
+        del self._keep
+
+    # ------------------------------------------------------------ workspace
+    def workspace_for(self, n_atoms: int, n_mol: int, cap: int, path: int) -> torch.Tensor:
+        need = self.lib.mlff_workspace_size(ctypes.byref(self.dims), n_atoms, n_mol, cap, path)
+        if need == 0:
+            raise _lib.MLFFError(_lib.ERR_INVALID, _lib.last_error())
+        if self.workspace is None or self.workspace.numel() < need:
+            self.workspace = None
+            self.workspace = torch.empty(need, dtype=torch.uint8, device=self.device)
+        return self.workspace
+
+    def capacity(self, n_atoms: int, path: int) -> int:
+        return max(self.edge_capacity.get(path, 0), DEFAULT_EDGES_PER_ATOM * n_atoms, 1024)
+
+    def status(self):
+        code = ctypes.c_int32()
+        ne = ctypes.c_int64()
+        where = ctypes.c_int32()
+        _lib.check(self.lib.mlff_read_status(self.workspace.data_ptr(), ctypes.byref(code), ctypes.byref(ne),
+                                             ctypes.byref(where), _stream_handle()))
+        return code.value, ne.value, where.value
+
+    # ---------------------------------------------------------------- calls
+    def energy_forces(self, batch: Batch, path: int = _lib.PATH_TUNED_BF16X3, forces: bool = True,
+                      virial: bool = False, atom_energy: bool = False, check: bool = True
+                      ) -> Tuple[torch.Tensor, Optional[torch.Tensor], Optional[torch.Tensor]]:
+        """Energies [B] (float64), forces [N,3] (float32), dE/dstrain [B,3,3]."""
+        N, B = batch.n_atoms, batch.n_mol
+        dev = self.device
+        E = torch.empty(B, dtype=torch.float64, device=dev)
+        F = torch.empty(N, 3, dtype=torch.float32, device=dev) if forces else None
+        V = torch.empty(B, 3, 3, dtype=torch.float64, device=dev) if virial else None
+        A = torch.empty(N, dtype=torch.float32, device=dev) if atom_energy else None
+        out = _lib.Outputs()
+        out.energy, out.forces, out.virial = E.data_ptr(), _lib.ptr(F), _lib.ptr(V)
+        out.atom_energy = _lib.ptr(A)
+        sysd = batch.system()
+        for _ in range(4):
+            cap = self.capacity(N, path)
+            ws = self.workspace_for(N, B, cap, path)
+            _lib.check(self.lib.mlff_energy_forces(ctypes.byref(self.dims), self.packed.data_ptr(),
+                                                   ctypes.byref(sysd), cap, path, ctypes.byref(out),
+                                                   ws.data_ptr(), ws.numel(), _stream_handle()))
+            if not check:
+                break
+            code, n_edges, where = self.status()
+            if code == _lib.ERR_CAPACITY:
+                self.edge_capacity[path] = int(n_edges * 1.25) + 1024
+                continue
+            if code != _lib.OK:
+                raise _lib.MLFFError(code, f"device status {code} at index {where}")
+            # keep headroom for the next call (MD steps change edge counts)
+            self.edge_capacity[path] = max(self.edge_capacity.get(path, 0), int(n_edges * 1.15) + 1024)
+            break
+        else:
+            raise _lib.MLFFError(_lib.ERR_CAPACITY, "edge capacity did not converge")
+        if atom_energy:
+            return E, F, V, A
+        return E, F, V
+
+    def neighbors(self, batch: Batch):
+        """CSR (row_ptr, col) of the radius graph, for tests and tools."""
+        N, B = batch.n_atoms, batch.n_mol
+        path = _lib.PATH_TUNED_FP32
+        sysd = batch.system()
+        for _ in range(4):
+            cap = self.capacity(N, path)
+            ws = self.workspace_for(N, B, cap, path)
+            _lib.check(self.lib.mlff_build_neighbors(ctypes.byref(self.dims), ctypes.byref(sysd), cap,
+                                                     ws.data_ptr(), ws.numel(), _stream_handle()))
+            code, n_edges, where = self.status()
+            if code == _lib.ERR_CAPACITY:
+                self.edge_capacity[path] = int(n_edges * 1.25) + 1024
+                continue
+            if code != _lib.OK:
+                raise _lib.MLFFError(code, f"device status {code} at index {where}")
+            row_ptr = torch.empty(N + 1, dtype=torch.int32, device=self.device)
+            col = torch.empty(max(cap, 1), dtype=torch.int32, device=self.device)
+            _lib.check(self.lib.mlff_copy_neighbors(ws.data_ptr(), N, B, cap, path, row_ptr.data_ptr(),
+                                                    col.data_ptr(), _stream_handle()))
+            return row_ptr, col[:n_edges]
+        raise _lib.MLFFError(_lib.ERR_CAPACITY, "edge capacity did not converge")

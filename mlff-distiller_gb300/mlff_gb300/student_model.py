@@ -1,0 +1,325 @@
+"""Drop-in ``StudentForceField`` evaluated by the GB300 CUDA library.
+
+Same constructor, same parameters and buffers, same state_dict keys and
+shapes, same seeded initialisation and the same ``save``/``load`` checkpoint
+format as the reference module
+(src/mlff_distiller/models/student_model.py:532-1176).  ``forward`` and
+``predict_energy_and_forces`` run the whole model -- radius graph, edge
+filters, messages, updates, readout and the hand-written force adjoint --
+in libmlff_gb300.so on the current CUDA stream.  There is no CPU path.
+
+Differences from the reference, on purpose:
+* ``cell``/``pbc`` are honoured (orthorhombic, minimum image) when
+  ``periodic=True`` (default); the reference ignores them
+  (student_model.py:694-703).  ``periodic=False`` reproduces that.
+* ``precision`` picks the evaluation path: ``"bf16x3"`` (fused edge
+  kernels, tcgen05 tensor cores with split-BF16 operands and FP32
+  accumulation), ``"tuned_fp32"`` (same fused kernels on FP32 CUDA cores)
+  or ``"fp32"`` (plain per-op FP32 kernels).
+* Gradients flow to positions only (forces); parameter gradients for
+  force-matching training come from ``mlff_gb300.training``.
+"""
+from __future__ import annotations
+
+import logging
+import math
+import warnings
+from pathlib import Path
+from typing import Optional, Tuple, Union
+
+import numpy as np
+import torch
+import torch.nn as nn
+
+from . import _lib
+from .engine import Batch, Engine, dims_of
+
+logger = logging.getLogger(__name__)
+
+
+class GaussianRBF(nn.Module):
+    """exp(-(d - mu_k)^2 / w_k^2), mu = linspace(0, cutoff, n), w = cutoff/n
+    (student_model.py:196-255).  ``centers``/``widths`` are buffers, or
+    parameters when learnable."""
+
+    def __init__(self, num_rbf: int = 20, cutoff: float = 5.0, learnable: bool = False):
+        super().__init__()
+        self.num_rbf = num_rbf
+        self.cutoff = cutoff
+        centers = torch.linspace(0, cutoff, num_rbf)
+        widths = torch.ones(num_rbf) * (cutoff / num_rbf)
+        if learnable:
+            self.centers = nn.Parameter(centers)
+            self.widths = nn.Parameter(widths)
+        else:
+            self.register_buffer("centers", centers)
+            self.register_buffer("widths", widths)
+
+    def forward(self, distances: torch.Tensor) -> torch.Tensor:
+        diff = distances.unsqueeze(-1) - self.centers
+        return torch.exp(-(1.0 / self.widths ** 2) * diff ** 2)
+
+
+class CosineCutoff(nn.Module):
+    """0.5 (cos(pi d / rc) + 1) for d < rc, else 0 (student_model.py:258-292)."""
+
+    def __init__(self, cutoff: float = 5.0):
+        super().__init__()
+        self.cutoff = cutoff
+
+    def forward(self, distances: torch.Tensor) -> torch.Tensor:
+        return 0.5 * (torch.cos(math.pi * distances / self.cutoff) + 1.0) * (distances < self.cutoff).float()
+
+
+class PaiNNMessage(nn.Module):
+    """Parameter container of the message block: ``rbf_to_scalar`` =
+    Linear(R, H) - SiLU - Linear(H, 3H) (student_model.py:297-322).  It is
+    evaluated only inside the fused edge kernels."""
+
+    def __init__(self, hidden_dim: int, num_rbf: int):
+        super().__init__()
+        self.hidden_dim = hidden_dim
+        self.rbf_to_scalar = nn.Sequential(nn.Linear(num_rbf, hidden_dim), nn.SiLU(),
+                                           nn.Linear(hidden_dim, hidden_dim * 3))
+
+    def forward(self, *args, **kwargs):
+        raise NotImplementedError("mlff_gb300 evaluates interaction blocks only inside StudentForceField "
+                                  "(fused CUDA edge kernels)")
+
+
+class PaiNNUpdate(nn.Module):
+    """Parameter container of the update block: ``update_mlp`` =
+    Linear(2H, H) - SiLU - Linear(H, 3H) and the 3x3 ``mixing_matrix``
+    over the xyz axis (student_model.py:390-416)."""
+
+    def __init__(self, hidden_dim: int):
+        super().__init__()
+        self.hidden_dim = hidden_dim
+        self.update_mlp = nn.Sequential(nn.Linear(hidden_dim * 2, hidden_dim), nn.SiLU(),
+                                        nn.Linear(hidden_dim, hidden_dim * 3))
+        self.mixing_matrix = nn.Parameter(torch.randn(3, 3) / np.sqrt(3))
+
+    def forward(self, *args, **kwargs):
+        raise NotImplementedError("mlff_gb300 evaluates interaction blocks only inside StudentForceField "
+                                  "(fused CUDA update kernels)")
+
+
+class PaiNNInteraction(nn.Module):
+    """message + update (student_model.py:473-527)."""
+
+    def __init__(self, hidden_dim: int, num_rbf: int):
+        super().__init__()
+        self.message = PaiNNMessage(hidden_dim, num_rbf)
+        self.update = PaiNNUpdate(hidden_dim)
+
+    def forward(self, *args, **kwargs):
+        raise NotImplementedError("mlff_gb300 evaluates interaction blocks only inside StudentForceField")
+
+
+class _EnergyForces(torch.autograd.Function):
+    """E = model(positions) with dE/dpos from the CUDA adjoint.  The forward
+    computes forces eagerly; backward scales them by the incoming energy
+    gradient of each structure."""
+
+    @staticmethod
+    def forward(ctx, positions, model, batch, mol_index):
+        need_grad = positions.requires_grad
+        E, F, _ = model._engine_call(batch, forces=need_grad)
+        ctx.save_for_backward(F if need_grad else torch.empty(0, device=positions.device), mol_index)
+        return E.to(positions.dtype)
+
+    @staticmethod
+    def backward(ctx, grad_E):
+        F, mol_index = ctx.saved_tensors
+        if F.numel() == 0:
+            return None, None, None, None
+        g = grad_E.to(torch.float32)[mol_index].unsqueeze(1)
+        return (-F * g).to(grad_E.dtype), None, None, None
+
+
+class StudentForceField(nn.Module):
+    """PaiNN-style energy model (student_model.py:532-1176) on GB300."""
+
+    def __init__(self, hidden_dim: int = 128, num_interactions: int = 3, num_rbf: int = 20,
+                 cutoff: float = 5.0, max_z: int = 118, learnable_rbf: bool = False,
+                 use_torch_cluster: bool = True, precision: str = "tuned_fp32", periodic: bool = True):
+        super().__init__()
+        self.hidden_dim = hidden_dim
+        self.num_interactions = num_interactions
+        self.num_rbf = num_rbf
+        self.cutoff = cutoff
+        self.max_z = max_z
+        self.use_torch_cluster = use_torch_cluster
+        self.precision = precision
+        self.periodic = periodic
+        self.embedding = nn.Embedding(max_z + 1, hidden_dim)
+        self.rbf = GaussianRBF(num_rbf, cutoff, learnable_rbf)
+        self.cutoff_fn = CosineCutoff(cutoff)
+        self.interactions = nn.ModuleList([PaiNNInteraction(hidden_dim, num_rbf)
+                                           for _ in range(num_interactions)])
+        self.energy_head = nn.Sequential(nn.Linear(hidden_dim, hidden_dim // 2), nn.SiLU(),
+                                         nn.Linear(hidden_dim // 2, hidden_dim // 4), nn.SiLU(),
+                                         nn.Linear(hidden_dim // 4, 1))
+        self._initialize_parameters()
+        self._engine: Optional[Engine] = None
+        self._packed_version = None
+
+    def _initialize_parameters(self):
+        """Same initialisation as the reference (student_model.py:618-628)."""
+        nn.init.uniform_(self.embedding.weight, -np.sqrt(3), np.sqrt(3))
+        for module in self.modules():
+            if isinstance(module, nn.Linear):
+                nn.init.xavier_uniform_(module.weight)
+                if module.bias is not None:
+                    nn.init.zeros_(module.bias)
+
+    def num_parameters(self) -> int:
+        return sum(p.numel() for p in self.parameters() if p.requires_grad)
+
+    # ------------------------------------------------------------- engine
+    @property
+    def path(self) -> int:
+        try:
+            return _lib.PATHS[self.precision]
+        except KeyError:
+            raise ValueError(f"unknown precision {self.precision!r}; use one of {sorted(_lib.PATHS)}")
+
+    def _weights_version(self):
+        return tuple((p.data_ptr(), p._version) for p in self.state_dict(keep_vars=True).values())
+
+    def engine(self) -> Engine:
+        dev = self.embedding.weight.device
+        if dev.type != "cuda":
+            raise RuntimeError("mlff_gb300 computes on a CUDA device: move the model with .to('cuda')")
+        if self._engine is None or self._engine.device != dev:
+            self._engine = Engine(dims_of(self.hidden_dim, self.num_rbf, self.num_interactions,
+                                          self.max_z + 1, float(self.cutoff)), dev)
+            self._packed_version = None
+        v = self._weights_version()
+        if v != self._packed_version:
+            self._engine.pack(self.state_dict())
+            self._packed_version = v
+        return self._engine
+
+    def _engine_call(self, batch: Batch, forces: bool = True, virial: bool = False):
+        return self.engine().energy_forces(batch, self.path, forces=forces, virial=virial)
+
+    def _make_batch(self, atomic_numbers, positions, cell, pbc, batch):
+        dev = self.embedding.weight.device
+        if positions.device != dev:
+            raise RuntimeError(f"positions on {positions.device} but model on {dev}")
+        N = int(atomic_numbers.shape[0])
+        if batch is None:
+            mol_ptr = torch.tensor([0, N], dtype=torch.int64, device=dev)
+            mol_index = torch.zeros(N, dtype=torch.int64, device=dev)
+            n_mol = 1
+        else:
+            b = batch.to(torch.int64)
+            if N and bool((b[1:] < b[:-1]).any()):
+                raise ValueError("batch indices must be non-decreasing (atoms grouped by structure)")
+            n_mol = int(b.max().item()) + 1 if N else 0
+            counts = torch.bincount(b, minlength=n_mol)
+            mol_ptr = torch.zeros(n_mol + 1, dtype=torch.int64, device=dev)
+            mol_ptr[1:] = torch.cumsum(counts, 0)
+            mol_index = b
+        box = pbc_t = None
+        if self.periodic and pbc is not None and cell is not None and bool(torch.as_tensor(pbc).any()):
+            cell_t = torch.as_tensor(cell, dtype=torch.float32, device=dev).reshape(-1, 3, 3)
+            pbc_b = torch.as_tensor(pbc, device=dev).reshape(-1, 3).to(torch.bool)
+            if cell_t.shape[0] == 1 and n_mol > 1:
+                cell_t = cell_t.expand(n_mol, 3, 3)
+                pbc_b = pbc_b.expand(n_mol, 3)
+            off = cell_t - torch.diag_embed(torch.diagonal(cell_t, dim1=1, dim2=2))
+            if bool((off.abs() > 0).any()):
+                raise NotImplementedError("periodic cells must be orthorhombic (diagonal cell matrix)")
+            mixed = pbc_b.any(dim=1) & ~pbc_b.all(dim=1)
+            if bool(mixed.any()):
+                raise NotImplementedError("periodicity must be on all three axes or none")
+            box = torch.diagonal(cell_t, dim1=1, dim2=2).contiguous()
+            pbc_t = pbc_b.all(dim=1).to(torch.uint8).contiguous()
+        bt = Batch(atomic_numbers.to(torch.int64).contiguous(),
+                   positions.detach().to(torch.float32).contiguous(), mol_ptr, box, pbc_t)
+        return bt, mol_index, n_mol
+
+    # ------------------------------------------------------------- forward
+    def forward(self, atomic_numbers: torch.Tensor, positions: torch.Tensor,
+                cell: Optional[torch.Tensor] = None, pbc: Optional[torch.Tensor] = None,
+                batch: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """Total energy: 0-dim for one structure, [B] for a batch
+        (student_model.py:634-757).  Differentiable w.r.t. positions."""
+        bt, mol_index, n_mol = self._make_batch(atomic_numbers, positions, cell, pbc, batch)
+        if self.training and torch.is_grad_enabled() and any(p.requires_grad for p in self.parameters()):
+            warnings.warn("mlff_gb300.StudentForceField gives position gradients only; use "
+                          "mlff_gb300.training for parameter gradients", stacklevel=2)
+        E = _EnergyForces.apply(positions, self, bt, mol_index)
+        # one structure -> 0-dim, several -> [B]  (student_model.py:739-755)
+        return E.sum() if n_mol <= 1 else E
+
+    def predict_energy_and_forces(self, atomic_numbers: torch.Tensor, positions: torch.Tensor,
+                                  cell: Optional[torch.Tensor] = None, pbc: Optional[torch.Tensor] = None
+                                  ) -> Tuple[torch.Tensor, torch.Tensor]:
+        """(energy, forces) with forces from the CUDA adjoint
+        (student_model.py:759-795)."""
+        bt, _, _ = self._make_batch(atomic_numbers, positions, cell, pbc, None)
+        E, F, _ = self._engine_call(bt, forces=True)
+        return E[0].to(positions.dtype), F.to(positions.dtype)
+
+    def energy_and_forces(self, atomic_numbers: torch.Tensor, positions: torch.Tensor,
+                          batch: Optional[torch.Tensor] = None, cell=None, pbc=None
+                          ) -> Tuple[torch.Tensor, torch.Tensor]:
+        """Batched (energies [B] float64, forces [N,3] float32) in one call,
+        without autograd -- the batched calculator path
+        (ase_calculator.py:708-770)."""
+        bt, _, _ = self._make_batch(atomic_numbers, positions, cell, pbc, batch)
+        E, F, _ = self._engine_call(bt, forces=True)
+        return E, F
+
+    def energy_forces_virial(self, atomic_numbers, positions, cell=None, pbc=None, batch=None):
+        """Energies [B], forces [N,3] and dE/d(strain) [B,3,3] in one call."""
+        bt, _, _ = self._make_batch(atomic_numbers, positions, cell, pbc, batch)
+        return self._engine_call(bt, forces=True, virial=True)
+
+    # ---------------------------------------------------------- checkpoint
+    def save(self, path: Union[str, Path]):
+        """Reference checkpoint format (student_model.py:1075-1099)."""
+        path = Path(path)
+        path.parent.mkdir(parents=True, exist_ok=True)
+        torch.save({"model_state_dict": self.state_dict(),
+                    "config": {"hidden_dim": self.hidden_dim, "num_interactions": self.num_interactions,
+                               "num_rbf": self.num_rbf, "cutoff": self.cutoff, "max_z": self.max_z,
+                               "use_torch_cluster": self.use_torch_cluster},
+                    "num_parameters": self.num_parameters()}, path)
+
+    @classmethod
+    def load(cls, path: Union[str, Path], device: str = "cpu", **kwargs):
+        """Load a reference checkpoint, inferring missing config entries
+        from state_dict shapes (student_model.py:1101-1176).  A trainer
+        checkpoint's ``model.`` key prefix is stripped."""
+        ckpt = torch.load(path, map_location="cpu", weights_only=False)
+        config = dict(ckpt.get("config", {}))
+        config.setdefault("use_torch_cluster", True)
+        keep = {"hidden_dim", "num_interactions", "num_rbf", "cutoff", "max_z", "learnable_rbf",
+                "use_torch_cluster"}
+        cfg = {k: v for k, v in config.items() if k in keep}
+        sd = ckpt["model_state_dict"]
+        if any(k.startswith("model.") for k in sd):
+            sd = {k[len("model."):] if k.startswith("model.") else k: v for k, v in sd.items()}
+        if "hidden_dim" not in cfg and "embedding.weight" in sd:
+            cfg["hidden_dim"] = sd["embedding.weight"].shape[1]
+        if "num_rbf" not in cfg and "rbf.centers" in sd:
+            cfg["num_rbf"] = sd["rbf.centers"].shape[0]
+        if "num_interactions" not in cfg:
+            ids = {int(k.split(".")[1]) for k in sd if k.startswith("interactions.")}
+            if ids:
+                cfg["num_interactions"] = len(ids)
+        cfg.setdefault("cutoff", 5.0)
+        if "max_z" not in cfg and "embedding.weight" in sd:
+            cfg["max_z"] = sd["embedding.weight"].shape[0] - 1
+        cfg.update(kwargs)
+        model = cls(**cfg)
+        model.load_state_dict(sd)
+        return model.to(device)
+
+
+__all__ = ["StudentForceField", "PaiNNInteraction", "PaiNNMessage", "PaiNNUpdate", "GaussianRBF",
+           "CosineCutoff"]

@@ -147,7 +147,7 @@ int64_t oracle_radius_graph_pbc_cells(const float *pos, int64_t n, const float *
         L[a] = box[a];
         if (!(L[a] >= 2.0f * cutoff)) return -1;
         invL[a] = 1.0f / L[a];
-        nc[a] = (int)floorf(L[a] / cutoff);
+        nc[a] = (int)floorf(L[a] / (cutoff * 1.0001f)); /* cell edge > cutoff with margin */
         if (nc[a] < 1) nc[a] = 1;
     }
     int64_t ncell = (int64_t)nc[0] * nc[1] * nc[2];

@@ -112,9 +112,11 @@ def energy_forces(params, Z, pos, mol_ptr, cutoff=5.0, box=None, pbc=None,
     x = torch.as_tensor(pos_np, dtype=dtype).clone().requires_grad_(True)
     eps = torch.zeros(n_mol, 3, 3, dtype=dtype, requires_grad=virial)
     if virial:
+        # r' = (I + eps) r for every position and image shift, so that
+        # dE/deps_ab = sum_edges (dE/dr_a) r_b
         strain = torch.eye(3, dtype=dtype) + eps
-        xs = torch.einsum("na,nab->nb", x, strain[mol])
-        sv = torch.einsum("ea,eab->eb", shift_t, strain[mol[dst_t]])
+        xs = torch.einsum("nab,nb->na", strain[mol], x)
+        sv = torch.einsum("eab,eb->ea", strain[mol[dst_t]], shift_t)
     else:
         xs, sv = x, shift_t
     E = energy(p, Zt, xs, src_t, dst_t, sv, mol, n_mol, cutoff)

@@ -1,0 +1,103 @@
+"""The C-ABI library builds, loads and exports every symbol the header
+declares (no compute calls: runs without a GPU)."""
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+
+def header_symbols():
+    txt = open(os.path.join(ROOT, "include", "mlff_gb300.h")).read()
+    return sorted(set(re.findall(r"\b(mlff_[a-z_]+)\s*\(", txt)))
+
+
+def test_header_lists_all_bound_symbols():
+    from mlff_gb300 import _lib
+    assert sorted(_lib.EXPORTS) == header_symbols()
+
+
+def test_library_loads_and_exports():
+    from mlff_gb300 import _build, _lib
+    _build.build()
+    lib = _lib.load()
+    for name in header_symbols():
+        assert hasattr(lib, name), name
+    assert lib.mlff_version() == 100
+
+
+def test_size_queries_without_gpu():
+    import ctypes
+    from mlff_gb300 import _lib
+    from mlff_gb300.engine import dims_of
+    lib = _lib.load()
+    d = dims_of(128, 20, 3, 119, 5.0)
+    n = lib.mlff_packed_weights_size(ctypes.byref(d))
+    # 429,596 parameters plus transposed copies and split-BF16 tiles
+    assert n > 4 * 429_596
+    ws_plain = lib.mlff_workspace_size(ctypes.byref(d), 1000, 4, 64_000, _lib.PATH_PLAIN_FP32)
+    ws_tuned = lib.mlff_workspace_size(ctypes.byref(d), 1000, 4, 64_000, _lib.PATH_TUNED_BF16X3)
+    assert ws_plain > ws_tuned > 0
+
+
+def test_unsupported_shape_is_reported():
+    import ctypes
+    from mlff_gb300 import _lib
+    from mlff_gb300.engine import dims_of
+    lib = _lib.load()
+    d = dims_of(64, 20, 3, 119, 5.0)
+    assert lib.mlff_packed_weights_size(ctypes.byref(d)) == 0
+    assert b"hidden" in lib.mlff_last_error_string()
+
+
+def test_invalid_arguments_rejected_on_host():
+    import ctypes
+    from mlff_gb300 import _lib
+    from mlff_gb300.engine import dims_of
+    lib = _lib.load()
+    d = dims_of(128, 20, 3, 119, 5.0)
+    s = _lib.System()
+    s.n_atoms = 0
+    s.n_mol = 1
+    out = _lib.Outputs()
+    r = lib.mlff_energy_forces(ctypes.byref(d), None, ctypes.byref(s), 0, 1, ctypes.byref(out), None, 0, None)
+    assert r == _lib.ERR_INVALID
+    assert b"empty" in lib.mlff_last_error_string()
+
+
+def test_seeded_init_matches_reference_weights(weights_seed0):
+    import numpy as np
+    import torch
+    from mlff_gb300.student_model import StudentForceField
+    torch.manual_seed(0)
+    m = StudentForceField()
+    sd = m.state_dict()
+    assert set(sd) == set(weights_seed0)
+    for k, v in weights_seed0.items():
+        np.testing.assert_array_equal(sd[k].numpy(), v)
+
+
+def test_checkpoint_roundtrip(tmp_path, weights_seed0):
+    import numpy as np
+    import torch
+    from mlff_gb300.student_model import StudentForceField
+    m = StudentForceField()
+    m.load_state_dict({k: torch.tensor(v) for k, v in weights_seed0.items()})
+    p = tmp_path / "ckpt.pt"
+    m.save(p)
+    m2 = StudentForceField.load(p)
+    for k, v in m2.state_dict().items():
+        np.testing.assert_array_equal(v.numpy(), weights_seed0[k])
+    # legacy checkpoint without config, trainer-style "model." prefix
+    torch.save({"model_state_dict": {"model." + k: torch.tensor(v) for k, v in weights_seed0.items()}}, p)
+    m3 = StudentForceField.load(p)
+    assert m3.num_interactions == 3 and m3.hidden_dim == 128 and m3.max_z == 118
+
+
+def test_model_refuses_cpu_compute(weights_seed0):
+    import torch
+    from mlff_gb300.student_model import StudentForceField
+    m = StudentForceField()
+    with pytest.raises(RuntimeError, match="CUDA"):
+        m(torch.tensor([1, 1]), torch.tensor([[0.0, 0, 0], [1.0, 0, 0]]))
