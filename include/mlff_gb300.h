@@ -190,6 +190,23 @@ int mlff_verlet_steps(const mlff_dims *dims, const void *packed, const mlff_syst
 int mlff_profile_begin(void);
 int mlff_profile_end(double *ms_by_kind, int64_t *launches_by_kind, int32_t n_kinds);
 
+/* Radius graph that allocates nothing.  No counterpart in the reference:
+ * it exists for callers that cannot call cudaMalloc or hand over a
+ * workspace (hosts that own every allocation, allocation-free regions).
+ * Same CSR as mlff_build_neighbors (row_ptr [N+1], col [edge_capacity],
+ * caller-owned outputs) plus status [4] int32 (code, edges found, first
+ * offending index, edges >> 31), all device pointers.  Scratch lives in one
+ * file-scope device array of about 5.6 MB, so sizes are capped: n_atoms <=
+ * 16384, n_mol <= 4096, edge_capacity <= 1048576 (MLFF_ERR_INVALID above
+ * that).  The first call on a device looks up the array's address; make it
+ * before any stream capture.  Calls share the array: calls that overlap on
+ * the GPU race. */
+#define MLFF_NOALLOC_MAX_ATOMS 16384
+#define MLFF_NOALLOC_MAX_MOLS 4096
+#define MLFF_NOALLOC_MAX_EDGES 1048576
+int mlff_radius_graph_noalloc(const mlff_system *sys, float cutoff, int64_t edge_capacity,
+                              int32_t *row_ptr, int32_t *col, int32_t *status, mlff_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

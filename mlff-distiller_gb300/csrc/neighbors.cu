@@ -472,3 +472,48 @@ int launch_neighbors(const mlff_dims& d, const mlff_system& sys, const WsLayout&
 }
 
 }  // namespace mlff
+
+namespace mlff {
+
+// Same launch sequence as launch_neighbors (without the reversed-edge map
+// and the partition), on explicitly given buffers.  Used by the
+// allocation-free entry point in noalloc.cu.
+int launch_neighbors_into(const mlff_dims& d, const mlff_system& sys, const NbrBuffers& b, cudaStream_t st) {
+    const int N = sys.n_atoms;
+    const bool any_pbc = sys.pbc != nullptr && sys.box != nullptr;
+    const int tb = 256;
+    const int gb = (int)std::max<int64_t>(1, std::min<int64_t>((N + tb - 1) / tb, 152 * 16));
+    prep_atoms_kernel<<<gb, tb, 0, st>>>(sys.pos, sys.mol_ptr, sys.n_mol, N, b.pos4, b.atom_mol);
+    MLFF_LAUNCH_CHECK("prep_atoms");
+    if (any_pbc) {
+        mol_grid_kernel<<<1, 1024, 0, st>>>(sys.mol_ptr, sys.box, sys.pbc, sys.n_mol, d.cutoff, b.mol_grid, b.status);
+        MLFF_LAUNCH_CHECK("mol_grid");
+        MLFF_CUDA(cudaMemsetAsync(b.cell_count, 0, sizeof(int32_t) * (b.ncell_cap + 1), st));
+        MLFF_CUDA(cudaMemsetAsync(b.cell_fill, 0, sizeof(int32_t) * b.ncell_cap, st));
+        cell_count_kernel<<<gb, tb, 0, st>>>(b.pos4, b.atom_mol, sys.box, sys.pbc, b.mol_grid, N, b.atom_cell,
+                                             b.cell_count);
+        MLFF_LAUNCH_CHECK("cell_count");
+        int r = launch_scan(b.cell_count, b.ncell_cap + 1, b.scan_tmp, st);
+        if (r) return r;
+        cell_fill_kernel<<<gb, tb, 0, st>>>(b.atom_cell, b.cell_count, N, b.cell_fill, b.cell_atoms);
+        MLFF_LAUNCH_CHECK("cell_fill");
+    }
+    NbrArgs a;
+    a.pos4 = b.pos4; a.atom_mol = b.atom_mol; a.mol_ptr = sys.mol_ptr; a.box = sys.box; a.pbc = sys.pbc;
+    a.grid = b.mol_grid; a.cell_start = b.cell_count; a.cell_atoms = b.cell_atoms; a.atom_cell = b.atom_cell;
+    a.n_atoms = N; a.cutoff = d.cutoff; a.cap = b.cap; a.counts = b.row_ptr;
+    a.col = b.col; a.erecv = b.erecv; a.st = b.status;
+    const int rows_blocks = (int)std::max<int64_t>(1, std::min<int64_t>((N + NBR_WARPS - 1) / NBR_WARPS, 152 * 32));
+    MLFF_CUDA(cudaMemsetAsync(b.row_ptr + N, 0, sizeof(int32_t), st));
+    nbr_rows_kernel<false><<<rows_blocks, NBR_WARPS * 32, 0, st>>>(a);
+    MLFF_LAUNCH_CHECK("nbr_count");
+    int r = launch_scan(b.row_ptr, (int64_t)N + 1, b.scan_tmp, st);
+    if (r) return r;
+    check_edges_kernel<<<1, 1, 0, st>>>(b.row_ptr, N, b.cap, nullptr, b.status);
+    MLFF_LAUNCH_CHECK("check_edges");
+    nbr_rows_kernel<true><<<rows_blocks, NBR_WARPS * 32, 0, st>>>(a);
+    MLFF_LAUNCH_CHECK("nbr_fill");
+    return MLFF_OK;
+}
+
+}  // namespace mlff

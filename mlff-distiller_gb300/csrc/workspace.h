@@ -58,7 +58,26 @@ inline const T* ws_ptr(const void* ws, size_t off) {
     return reinterpret_cast<const T*>(static_cast<const char*>(ws) + off);
 }
 
+// Buffers of one radius-graph build given as explicit device pointers.
+struct NbrBuffers {
+    Status* status;
+    float4* pos4;           // [N]
+    int32_t* atom_mol;      // [N]
+    int32_t* row_ptr;       // [N+1]
+    int32_t* col;           // [cap]
+    int32_t* erecv;         // [cap]
+    int32_t* scan_tmp;      // [(max(N+1, ncell_cap+1) + 1023) / 1024 + 2]
+    int4* mol_grid;         // [B]
+    int32_t* cell_count;    // [ncell_cap + 1]
+    int32_t* cell_fill;     // [ncell_cap]
+    int32_t* cell_atoms;    // [N]
+    int32_t* atom_cell;     // [N]
+    int64_t ncell_cap;      // N + 27 B
+    int64_t cap;            // edge capacity
+};
+
 // Kernel launch helpers implemented in the .cu files.
+int launch_neighbors_into(const mlff_dims& d, const mlff_system& sys, const NbrBuffers& b, cudaStream_t st);
 int launch_neighbors(const mlff_dims& d, const mlff_system& sys, const WsLayout& L, void* ws,
                      cudaStream_t st);
 int launch_embed(const mlff_dims& d, const float* packed, const PackedOffsets& po,

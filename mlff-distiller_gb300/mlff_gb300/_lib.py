@@ -40,7 +40,7 @@ ERROR_NAMES = {ERR_INVALID: "invalid argument", ERR_CAPACITY: "edge capacity exc
 EXPORTS = ["mlff_version", "mlff_last_error_string", "mlff_packed_weights_size", "mlff_pack_weights",
            "mlff_workspace_size", "mlff_build_neighbors", "mlff_copy_neighbors", "mlff_energy_forces",
            "mlff_read_status", "mlff_clear_status", "mlff_verlet_steps", "mlff_profile_begin",
-           "mlff_profile_end"]
+           "mlff_profile_end", "mlff_radius_graph_noalloc"]
 
 PROFILE_KINDS = ["neighbors", "edge_fwd", "edge_bwd", "update_fwd", "update_bwd", "readout", "forces",
                  "plain_gemm", "plain_edge", "other", "md"]
@@ -135,6 +135,8 @@ def load(build_if_missing: bool = True):
         lib.mlff_profile_begin.restype = ctypes.c_int
         lib.mlff_profile_end.restype = ctypes.c_int
         lib.mlff_profile_end.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(i64), i32]
+        lib.mlff_radius_graph_noalloc.restype = ctypes.c_int
+        lib.mlff_radius_graph_noalloc.argtypes = [ctypes.POINTER(System), ctypes.c_float, i64, _P, _P, _P, _P]
         _lib = lib
         return lib
 
