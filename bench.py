@@ -11,7 +11,7 @@ positions, numbers and offsets; D2H of energies and forces) inside the
 timed region.  An L2-sized buffer is rewritten between timed steps.
 
   python bench.py [--gpus N --steps K --warmup W] [--workload batch256]
-                  [--path bf16x3|tuned_fp32|fp32] [--impl ours|reference]
+                  [--path fp16x3|tuned_fp32|fp32] [--impl ours|reference]
 
 Under torchrun (N>1) every rank evaluates its own copy of the workload
 (independent batches, no collective on the data path): weak scaling.
@@ -52,7 +52,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batch256")
-    ap.add_argument("--path", default="bf16x3", choices=["bf16x3", "tuned_fp32", "fp32"])
+    ap.add_argument("--path", default="fp16x3", choices=["fp16x3", "tuned_fp32", "fp32"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -278,7 +278,7 @@ def main():
                 "traffic": read_traffic(dom, args.workload), "avg_launch_ms": round(avg_ms, 4),
                 "flop_per_launch": flop,
                 "mma_work_factor": (3.0 * (2 * (32 * 128 + 128 * 384)) / GEMM_FLOP_PER_EDGE
-                                    if path == _lib.PATH_TUNED_BF16X3 else None)}
+                                    if path == _lib.PATH_TUNED_TC else None)}
     gpu_launches = sum(prof.launches.values())
 
     # e2e through the public module API with host buffers
@@ -323,7 +323,7 @@ def main():
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(sysm, args.cpu_seconds, os.cpu_count())
-    dtype = {"bf16x3": "bf16x3 (split-bf16, fp32 accumulate)", "tuned_fp32": "f32", "fp32": "f32"}[args.path]
+    dtype = {"fp16x3": "fp16x3 (split-fp16 operands, fp32 accumulate)", "tuned_fp32": "f32", "fp32": "f32"}[args.path]
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000 * total_s / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": dtype,

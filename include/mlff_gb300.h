@@ -45,7 +45,7 @@ typedef struct CUstream_st *mlff_stream_t; /* same type as cudaStream_t */
 
 /* evaluation paths */
 #define MLFF_PATH_PLAIN_FP32 0    /* per-op FP32 kernels (the plain drop-in) */
-#define MLFF_PATH_TUNED_BF16X3 1  /* fused edge kernels, tcgen05 split-BF16 */
+#define MLFF_PATH_TUNED_TC 1      /* fused edge kernels, tcgen05, split-FP16 operands */
 #define MLFF_PATH_TUNED_FP32 2    /* fused edge kernels, FP32 CUDA cores */
 
 #define MLFF_MAX_LAYERS 8

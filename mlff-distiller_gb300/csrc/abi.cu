@@ -23,11 +23,22 @@ int cuda_status(cudaError_t e, const char* what) {
     return MLFF_ERR_CUDA;
 }
 
+int num_sms() {
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+            sms = 152;
+    }
+    return sms;
+}
+
 int persistent_ctas(int32_t path) {
-    // SIMT fused kernels: 4 CTAs of 128 threads per SM; tensor-core kernels
-    // are launched with one CTA per SM and walk several partitions each.
-    (void)path;
-    return 152 * 4;
+    // Receiver partitions: the CUDA-core fused kernels run 4 CTAs of 128
+    // threads per SM; the tensor-core kernels run one CTA per SM, one
+    // partition each (fewer partial edge tiles).
+    return path == MLFF_PATH_TUNED_TC ? num_sms() : num_sms() * 4;
 }
 
 WsLayout ws_layout(const mlff_dims& d, int32_t n_atoms, int32_t n_mol, int64_t cap, int32_t path) {
@@ -114,7 +125,7 @@ static int check_sys(const mlff_system* s, int64_t cap) {
 }
 
 static int check_path(int32_t path) {
-    if (path != MLFF_PATH_PLAIN_FP32 && path != MLFF_PATH_TUNED_BF16X3 && path != MLFF_PATH_TUNED_FP32) {
+    if (path != MLFF_PATH_PLAIN_FP32 && path != MLFF_PATH_TUNED_TC && path != MLFF_PATH_TUNED_FP32) {
         set_error("unknown path %d", path);
         return MLFF_ERR_INVALID;
     }

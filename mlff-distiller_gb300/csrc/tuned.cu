@@ -322,7 +322,7 @@ int run_tuned(const mlff_dims& d, const float* P, const PackedOffsets& po, const
     a.eacc = ws_ptr<float4>(ws, L.edge_acc);
     float* X = ws_ptr<float>(ws, L.X);
     float* Xt = ws_ptr<float>(ws, L.Xt);
-    const bool tc = path == MLFF_PATH_TUNED_BF16X3;
+    const bool tc = path == MLFF_PATH_TUNED_TC;
     for (int l = 0; l < d.n_layers; ++l) {
         a.lo = po.layer[l];
         a.X = X + l * NX;

@@ -25,11 +25,11 @@ ERR_ROW = 7
 ERR_WORKSPACE = 8
 
 PATH_PLAIN_FP32 = 0
-PATH_TUNED_BF16X3 = 1
+PATH_TUNED_TC = 1
 PATH_TUNED_FP32 = 2
 
 PATHS = {"plain": PATH_PLAIN_FP32, "fp32": PATH_PLAIN_FP32, "plain_fp32": PATH_PLAIN_FP32,
-         "bf16x3": PATH_TUNED_BF16X3, "tuned": PATH_TUNED_BF16X3, "tuned_bf16x3": PATH_TUNED_BF16X3,
+         "fp16x3": PATH_TUNED_TC, "tc": PATH_TUNED_TC, "tuned": PATH_TUNED_TC,
          "tuned_fp32": PATH_TUNED_FP32}
 
 ERROR_NAMES = {ERR_INVALID: "invalid argument", ERR_CAPACITY: "edge capacity exceeded",

@@ -142,7 +142,7 @@ class Engine:
         return code.value, ne.value, where.value
 
     # ---------------------------------------------------------------- calls
-    def energy_forces(self, batch: Batch, path: int = _lib.PATH_TUNED_BF16X3, forces: bool = True,
+    def energy_forces(self, batch: Batch, path: int = _lib.PATH_TUNED_TC, forces: bool = True,
                       virial: bool = False, atom_energy: bool = False, check: bool = True
                       ) -> Tuple[torch.Tensor, Optional[torch.Tensor], Optional[torch.Tensor]]:
         """Energies [B] (float64), forces [N,3] (float32), dE/dstrain [B,3,3]."""

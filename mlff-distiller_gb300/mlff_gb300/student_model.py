@@ -12,10 +12,10 @@ Differences from the reference, on purpose:
 * ``cell``/``pbc`` are honoured (orthorhombic, minimum image) when
   ``periodic=True`` (default); the reference ignores them
   (student_model.py:694-703).  ``periodic=False`` reproduces that.
-* ``precision`` picks the evaluation path: ``"bf16x3"`` (fused edge
-  kernels, tcgen05 tensor cores with split-BF16 operands and FP32
-  accumulation), ``"tuned_fp32"`` (same fused kernels on FP32 CUDA cores)
-  or ``"fp32"`` (plain per-op FP32 kernels).
+* ``precision`` picks the evaluation path: ``"fp16x3"`` (fused edge
+  kernels, tcgen05 tensor cores with split-FP16 operands -- x = hi + lo,
+  three MMAs -- and FP32 accumulation), ``"tuned_fp32"`` (same fused
+  kernels on FP32 CUDA cores) or ``"fp32"`` (plain per-op FP32 kernels).
 * Gradients flow to positions only (forces); parameter gradients for
   force-matching training come from ``mlff_gb300.training``.
 """
@@ -142,7 +142,7 @@ class StudentForceField(nn.Module):
 
     def __init__(self, hidden_dim: int = 128, num_interactions: int = 3, num_rbf: int = 20,
                  cutoff: float = 5.0, max_z: int = 118, learnable_rbf: bool = False,
-                 use_torch_cluster: bool = True, precision: str = "tuned_fp32", periodic: bool = True):
+                 use_torch_cluster: bool = True, precision: str = "fp16x3", periodic: bool = True):
         super().__init__()
         self.hidden_dim = hidden_dim
         self.num_interactions = num_interactions

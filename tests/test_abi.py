@@ -37,7 +37,7 @@ def test_size_queries_without_gpu():
     # 429,596 parameters plus transposed copies and split-BF16 tiles
     assert n > 4 * 429_596
     ws_plain = lib.mlff_workspace_size(ctypes.byref(d), 1000, 4, 64_000, _lib.PATH_PLAIN_FP32)
-    ws_tuned = lib.mlff_workspace_size(ctypes.byref(d), 1000, 4, 64_000, _lib.PATH_TUNED_BF16X3)
+    ws_tuned = lib.mlff_workspace_size(ctypes.byref(d), 1000, 4, 64_000, _lib.PATH_TUNED_TC)
     assert ws_plain > ws_tuned > 0
 
 

@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 
 F_TOL = 1e-3
 E_TOL_PER_ATOM = 2e-5
-PATHS = ["fp32", "tuned_fp32", "bf16x3"]
+PATHS = ["fp32", "tuned_fp32", "fp16x3"]
 CASES = ["batch6", "cutoff_edge", "methane", "molecule60", "water"]
 
 
@@ -143,7 +143,7 @@ def test_forces_match_fd_of_oracle_energy(golden_cases, weights_bias):
             assert abs(fd - F[a, x]) < 1e-3, (a, x, fd, F[a, x])
 
 
-@pytest.mark.parametrize("path", ["tuned_fp32", "bf16x3"])
+@pytest.mark.parametrize("path", ["tuned_fp32", "fp16x3"])
 def test_fused_path_is_deterministic(golden_cases, weights_bias, path):
     g = golden_cases
     m = engine_for(weights_bias, path)
