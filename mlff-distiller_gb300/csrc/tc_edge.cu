@@ -13,9 +13,11 @@
 //     coalesced gathers of the senders' feature rows;
 //   * split-FP16 operands: x = hi + lo (both fp16), three MMAs per K-step
 //     (hi*hi + hi*lo + lo*hi) with FP32 accumulation in TMEM;
-//   * W1 (128 x 32) stays in shared memory; W2 (384 x 128) streams through
-//     a ring of 8 KB hi/lo slabs filled by cp.async.bulk and recycled by
-//     tcgen05.commit on per-slot mbarriers;
+//   * W1 (128 x 32) and the hi half of W2 (384 x 128) stay in shared
+//     memory; the lo half of W2 streams through a ring of 4 KB tiles filled
+//     by cp.async.bulk and recycled by tcgen05.commit on per-slot mbarriers
+//     (one SM's bulk stream, ~27 B/clk, cannot feed the whole of W2 per
+//     tile at MMA speed, half of it it can);
 //   * every wait is bounded (clock64 budget); on expiry the kernel records
 //     MLFF_ERR_TIMEOUT, drains its own copies, frees TMEM and returns.
 //
@@ -39,10 +41,11 @@ using namespace tc;
 constexpr uint32_t A_TILE = 4096;
 constexpr uint32_t A_LBO = 2048;
 constexpr uint32_t A_SBO = 128;
-constexpr uint32_t SLAB = 2 * A_TILE;         // hi + lo of one 128 x 16 block
-constexpr int W2_SLABS = 24;                  // 3 channel chunks x 8 K-steps, q = g * 8 + s
+constexpr uint32_t SLAB = 2 * A_TILE;         // hi + lo of one 128 x 16 block (W1)
+constexpr int W2_TILES = 24;                  // 3 channel chunks x 8 K-steps, q = g * 8 + s
 constexpr uint32_t W1_BYTES = 2 * SLAB;       // 2 K-steps
-constexpr int NSLOT = 12;                     // W2 ring depth
+constexpr uint32_t W2_HALF = W2_TILES * A_TILE;   // all hi tiles (96 KB), then all lo tiles
+constexpr int NSLOT = 8;                      // ring depth for the streamed lo tiles
 
 __host__ __device__ constexpr uint32_t a_off(int m, int k) {
     return (uint32_t)((k >> 3) * 2048 + (m >> 3) * 128 + (m & 7) * 16 + (k & 7) * 2);
@@ -61,7 +64,8 @@ __device__ __forceinline__ uint32_t b_off(int n_rows, int row, int k) {
 constexpr uint32_t align1k(uint32_t x) { return (x + 1023u) & ~1023u; }
 
 // ------------------------------------------------------------- packing
-// W1 [H][RMAX] -> 2 K-step blocks (hi, lo); W2 [3H][H] -> 24 slabs.
+// W1 [H][RMAX] -> 2 K-step blocks (hi, lo); W2 [3H][H] -> 24 hi tiles
+// followed by the 24 matching lo tiles.
 __global__ void pack_tc_kernel(const float* __restrict__ w1, const float* __restrict__ w2,
                                unsigned char* __restrict__ w1_out, unsigned char* __restrict__ w2_out) {
     const int stride = gridDim.x * blockDim.x;
@@ -72,13 +76,13 @@ __global__ void pack_tc_kernel(const float* __restrict__ w1, const float* __rest
         *reinterpret_cast<__half*>(w1_out + s * SLAB + a_off(m, kk)) = hi;
         *reinterpret_cast<__half*>(w1_out + s * SLAB + A_TILE + a_off(m, kk)) = lo;
     }
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < W2_SLABS * 128 * 16; i += stride) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < W2_TILES * 128 * 16; i += stride) {
         const int q = i / 2048, m = (i / 16) % 128, kk = i % 16;
         const int g = q / 8, s = q % 8;
         __half hi, lo;
         split_f16(w2[(g * 128 + m) * H + 16 * s + kk], hi, lo);
-        *reinterpret_cast<__half*>(w2_out + q * SLAB + a_off(m, kk)) = hi;
-        *reinterpret_cast<__half*>(w2_out + q * SLAB + A_TILE + a_off(m, kk)) = lo;
+        *reinterpret_cast<__half*>(w2_out + q * A_TILE + a_off(m, kk)) = hi;
+        *reinterpret_cast<__half*>(w2_out + W2_HALF + q * A_TILE + a_off(m, kk)) = lo;
     }
 }
 
@@ -94,23 +98,35 @@ int pack_bf16(const mlff_dims& d, float* out, const PackedOffsets& o, cudaStream
 
 // -------------------------------------------------------- shared pieces
 constexpr long long WAIT_BUDGET = 1LL << 32;   // ~2 s at 2 GHz
+constexpr int NT = 512;                        // threads per CTA (16 warps)
 
 __device__ __forceinline__ void signal_timeout(const EdgeArgs& a, volatile int* abort_flag, int where) {
     set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, where);
     *abort_flag = 1;
 }
 
-// Ring producer: fill number p goes to slot p % NSLOT with slab p % 24.
-__device__ __forceinline__ bool produce_slab(uint32_t p, unsigned char* ring, const unsigned char* w2,
-                                             uint64_t* full, uint64_t* empty) {
+// Ring producer: fill number p brings lo tile p % 24 of W2 into slot p % NSLOT.
+__device__ __forceinline__ bool produce_lo(uint32_t p, unsigned char* ring, const unsigned char* w2lo,
+                                           uint64_t* full, uint64_t* empty) {
     const uint32_t slot = p % NSLOT;
     if (p >= (uint32_t)NSLOT) {
         if (!mbar_wait(&empty[slot], ((p / NSLOT) - 1) & 1, WAIT_BUDGET)) return false;
     }
-    mbar_expect_tx(&full[slot], SLAB);
-    bulk_g2s(ring + slot * SLAB, w2 + (size_t)(p % W2_SLABS) * SLAB, SLAB, &full[slot]);
+    mbar_expect_tx(&full[slot], A_TILE);
+    bulk_g2s(ring + slot * A_TILE, w2lo + (size_t)(p % W2_TILES) * A_TILE, A_TILE, &full[slot]);
     return true;
 }
+
+// Resident hi half of W2: six 16 KB bulk copies on one mbarrier.
+__device__ __forceinline__ void load_w2_hi(unsigned char* dst, const unsigned char* w2hi, uint64_t* bar) {
+    mbar_expect_tx(bar, W2_HALF);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) bulk_g2s(dst + i * (W2_HALF / 6), w2hi + i * (W2_HALF / 6), W2_HALF / 6, bar);
+}
+
+// sigmoid via the fast exponential and reciprocal; silu = z s,
+// silu' = s (1 + z (1 - s)).  Both are exact in the limits z -> +-inf.
+__device__ __forceinline__ float fast_sigmoid(float z) { return __fdividef(1.0f, 1.0f + __expf(-z)); }
 
 // rbf(d)_r * fc(d) for r in [r0, r0 + 16) (0 beyond R or for padding edges)
 __device__ __forceinline__ void rbf16(float d, bool valid, int r0, int R, const float* cent, const float* gam,
@@ -120,7 +136,7 @@ __device__ __forceinline__ void rbf16(float d, bool valid, int r0, int R, const 
     for (int i = 0; i < 16; ++i) {
         const int r = r0 + i;
         const float diff = d - cent[r];
-        out[i] = (valid && r < R) ? expf(-gam[r] * diff * diff) * fc : 0.0f;
+        out[i] = (valid && r < R) ? __expf(-gam[r] * diff * diff) * fc : 0.0f;
     }
 }
 __device__ __forceinline__ void rbf16_d(float d, bool valid, int r0, int R, const float* cent, const float* gam,
@@ -131,40 +147,103 @@ __device__ __forceinline__ void rbf16_d(float d, bool valid, int r0, int R, cons
     for (int i = 0; i < 16; ++i) {
         const int r = r0 + i;
         const float diff = d - cent[r];
-        const float g = expf(-gam[r] * diff * diff);
+        const float g = __expf(-gam[r] * diff * diff);
         out[i] = (valid && r < R) ? g * (dfc - 2.0f * gam[r] * diff * fc) : 0.0f;
     }
+}
+
+// x = hi + lo for two values at once (packed conversions)
+__device__ __forceinline__ void split2(float a, float b, __half2& hi, __half2& lo) {
+    hi = __floats2half2_rn(a, b);
+    const float2 f = __half22float2(hi);
+    lo = __floats2half2_rn(a - f.x, b - f.y);
 }
 
 // store 16 consecutive K values (one K-step, both 8-column chunks) of one
 // row as split fp16 into a B-operand tile (hi half, lo half)
 __device__ __forceinline__ void store_row16(unsigned char* tile, uint32_t half_bytes, int n_rows, int row, int s,
                                             const float (&v)[16]) {
-    __align__(16) __half hi[16];
-    __align__(16) __half lo[16];
+    __align__(16) __half2 hi[8];
+    __align__(16) __half2 lo[8];
 #pragma unroll
-    for (int i = 0; i < 16; ++i) split_f16(v[i], hi[i], lo[i]);
+    for (int i = 0; i < 8; ++i) split2(v[2 * i], v[2 * i + 1], hi[i], lo[i]);
     const uint32_t o0 = b_off(n_rows, row, 16 * s);
     const uint32_t o1 = b_off(n_rows, row, 16 * s + 8);
     *reinterpret_cast<uint4*>(tile + o0) = *reinterpret_cast<const uint4*>(&hi[0]);
-    *reinterpret_cast<uint4*>(tile + o1) = *reinterpret_cast<const uint4*>(&hi[8]);
+    *reinterpret_cast<uint4*>(tile + o1) = *reinterpret_cast<const uint4*>(&hi[4]);
     *reinterpret_cast<uint4*>(tile + half_bytes + o0) = *reinterpret_cast<const uint4*>(&lo[0]);
-    *reinterpret_cast<uint4*>(tile + half_bytes + o1) = *reinterpret_cast<const uint4*>(&lo[8]);
+    *reinterpret_cast<uint4*>(tile + half_bytes + o1) = *reinterpret_cast<const uint4*>(&lo[4]);
 }
 
-// Receiver flush for two of the four feature components (s, v_x, v_y, v_z):
-// out[cur] = base[cur] + acc, then out[j] = base[j] for receivers without
-// edges up to next.
-__device__ __noinline__ void flush2(const float* __restrict__ base, float* __restrict__ out, int c, int comp0,
-                                    int comp1, int cur, int next, float acc0, float acc1) {
-    const int64_t r0 = (int64_t)cur * 4 * H;
-    out[r0 + comp0 * H + c] = base[r0 + comp0 * H + c] + acc0;
-    out[r0 + comp1 * H + c] = base[r0 + comp1 * H + c] + acc1;
-    for (int j = cur + 1; j < next; ++j) {
-        const int64_t rj = (int64_t)j * 4 * H;
-        out[rj + comp0 * H + c] = base[rj + comp0 * H + c];
-        out[rj + comp1 * H + c] = base[rj + comp1 * H + c];
+// Rows row and row+1, column k of a B-operand tile: store the split fp16
+// values of a pair of edges.
+__device__ __forceinline__ void store_col_pair(unsigned char* tile, uint32_t half_bytes, int n_rows, int row, int k,
+                                               float a, float b) {
+    __half2 hi, lo;
+    split2(a, b, hi, lo);
+    const uint32_t o0 = b_off(n_rows, row, k), o1 = b_off(n_rows, row + 1, k);
+    *reinterpret_cast<__half*>(tile + o0) = __low2half(hi);
+    *reinterpret_cast<__half*>(tile + o1) = __high2half(hi);
+    *reinterpret_cast<__half*>(tile + half_bytes + o0) = __low2half(lo);
+    *reinterpret_cast<__half*>(tile + half_bytes + o1) = __high2half(lo);
+}
+
+// Receiver flush for one feature component: out[cur] = value (the sum over
+// the receiver's edges), then 0 for receivers without edges up to next.
+// The caller adds the per-atom term afterwards in one vectorised pass.
+__device__ __noinline__ void flush_sum(float* __restrict__ out, int idx, int cur, int next, float value) {
+    out[(int64_t)cur * 4 * H + idx] = value;
+    for (int j = cur + 1; j < next; ++j) out[(int64_t)j * 4 * H + idx] = 0.0f;
+}
+
+// Per-tile prep by threads otherwise idle during the E-tile phase: sender
+// (and receiver) row offsets, u components, and a bitmask of the edges whose
+// receiver differs from the previous edge's (edge 0 compares with prev).
+template <int N>
+__device__ __forceinline__ void tile_prep(int e, int n, int prev, const int* src_s, const int* rcv_s,
+                                          const float4* us, int* soff, int* roff, float* uc, uint32_t* chg) {
+    const bool valid = e < n;
+    const int ra = rcv_s[e];
+    soff[e] = src_s[e] * 4 * H;
+    if (roff) roff[e] = max(ra, 0) * 4 * H;
+    if (uc) {
+        const float4 u = us[e];
+        uc[e] = u.x;
+        uc[N + e] = u.y;
+        uc[2 * N + e] = u.z;
     }
+    const int before = e == 0 ? prev : rcv_s[e - 1];
+    const unsigned m = __ballot_sync(0xffffffffu, valid && ra != before);
+    if ((e & 31) == 0) chg[e >> 5] = m;
+}
+
+// Sum 8 per-lane values over the 32 lanes of a warp with 9 shuffles
+// (reduce-scatter).  Afterwards lanes with (lane & 3) == 0 hold the sum of
+// value index = bits 4..2 of the lane id.
+__device__ __forceinline__ float warp_reduce_scatter8(const float (&v)[8], int lane) {
+    float w4[4], w2[2];
+    const bool b16 = lane & 16, b8 = lane & 8, b4 = lane & 4;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const float send = b16 ? v[j] : v[j + 4];
+        const float keep = b16 ? v[j + 4] : v[j];
+        w4[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        const float send = b8 ? w4[j] : w4[j + 2];
+        const float keep = b8 ? w4[j + 2] : w4[j];
+        w2[j] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
+    const float send = b4 ? w2[0] : w2[1];
+    const float keep = b4 ? w2[1] : w2[0];
+    float w1 = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    w1 += __shfl_xor_sync(0xffffffffu, w1, 2);
+    w1 += __shfl_xor_sync(0xffffffffu, w1, 1);
+    return w1;
+}
+__device__ __forceinline__ int reduce_scatter8_index(int lane) {
+    return ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
 }
 
 // ------------------------------------------------------- forward kernel
@@ -172,26 +251,34 @@ constexpr int FN = 128;                                   // edges per tile
 constexpr uint32_t F_EH = 2 * b_kstep(FN);                // E tile, one half (2 K-steps)
 constexpr uint32_t F_HH = 8 * b_kstep(FN);                // H tile, one half (8 K-steps)
 constexpr uint32_t F_OFF_W1 = 0;
-constexpr uint32_t F_OFF_E = F_OFF_W1 + W1_BYTES;
-constexpr uint32_t F_OFF_H = align1k(F_OFF_E + 2 * F_EH);
+constexpr uint32_t F_OFF_W2H = F_OFF_W1 + W1_BYTES;
+constexpr uint32_t F_OFF_H = align1k(F_OFF_W2H + W2_HALF);     // H tile; the E tile shares its start
 constexpr uint32_t F_OFF_RING = align1k(F_OFF_H + 2 * F_HH);
-constexpr uint32_t F_OFF_US = F_OFF_RING + NSLOT * SLAB;
+constexpr uint32_t F_OFF_US = F_OFF_RING + NSLOT * A_TILE;
 constexpr uint32_t F_OFF_SRC = F_OFF_US + FN * 16;
 constexpr uint32_t F_OFF_RCV = F_OFF_SRC + FN * 4;
 constexpr uint32_t F_OFF_B1 = F_OFF_RCV + FN * 4;
 constexpr uint32_t F_OFF_B2 = F_OFF_B1 + H * 4;
 constexpr uint32_t F_OFF_CG = F_OFF_B2 + H3 * 4;
-constexpr uint32_t F_OFF_BAR = F_OFF_CG + 2 * RMAX * 4;
-constexpr uint32_t F_OFF_MISC = F_OFF_BAR + 8 * (1 + 2 * NSLOT);
+constexpr uint32_t F_OFF_SOFF = F_OFF_CG + 2 * RMAX * 4;
+constexpr uint32_t F_OFF_UC = F_OFF_SOFF + FN * 4;
+constexpr uint32_t F_OFF_CHG = F_OFF_UC + 3 * FN * 4;
+constexpr uint32_t F_OFF_BAR = F_OFF_CHG + (FN / 32) * 4 + 16;
+constexpr uint32_t F_OFF_MISC = F_OFF_BAR + 8 * (2 + 2 * NSLOT);
 constexpr uint32_t F_SMEM = align1k(F_OFF_MISC + 16);
+static_assert(2 * F_EH <= 2 * F_HH, "E tile fits in the H tile's space");
 static_assert(F_SMEM <= 232448, "forward kernel shared memory");
 
-__global__ void __launch_bounds__(256, 1) edge_fwd_tc_kernel(EdgeArgs a, const unsigned char* __restrict__ w1g,
-                                                             const unsigned char* __restrict__ w2g) {
+// 16 warps.  Epilogue roles: warp w reads TMEM lane quarter q = w % 4
+// (channels / hidden units 32q..32q+31); r = w / 4 selects the edge quarter
+// (epilogue 1) or the feature component s, v_x, v_y, v_z (epilogue 2).
+__global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const unsigned char* __restrict__ w1g,
+                                                            const unsigned char* __restrict__ w2g) {
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* w1s = smem + F_OFF_W1;
-    unsigned char* Es = smem + F_OFF_E;
+    unsigned char* w2h = smem + F_OFF_W2H;
     unsigned char* Hs = smem + F_OFF_H;
+    unsigned char* Es = smem + F_OFF_H;            // E tile lives in the H tile's space
     unsigned char* ring = smem + F_OFF_RING;
     float4* us = reinterpret_cast<float4*>(smem + F_OFF_US);
     int* src_s = reinterpret_cast<int*>(smem + F_OFF_SRC);
@@ -200,8 +287,13 @@ __global__ void __launch_bounds__(256, 1) edge_fwd_tc_kernel(EdgeArgs a, const u
     float* b2s = reinterpret_cast<float*>(smem + F_OFF_B2);
     float* cent = reinterpret_cast<float*>(smem + F_OFF_CG);
     float* gam = cent + RMAX;
+    int* soff = reinterpret_cast<int*>(smem + F_OFF_SOFF);
+    float* uc = reinterpret_cast<float*>(smem + F_OFF_UC);
+    uint32_t* chg = reinterpret_cast<uint32_t*>(smem + F_OFF_CHG);
+    int* prev_s = reinterpret_cast<int*>(smem + F_OFF_CHG + (FN / 32) * 4);
     uint64_t* mma_bar = reinterpret_cast<uint64_t*>(smem + F_OFF_BAR);
-    uint64_t* full = mma_bar + 1;
+    uint64_t* w2h_bar = mma_bar + 1;
+    uint64_t* full = mma_bar + 2;
     uint64_t* empty = full + NSLOT;
     uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + F_OFF_MISC);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + F_OFF_MISC + 4);
@@ -209,12 +301,14 @@ __global__ void __launch_bounds__(256, 1) edge_fwd_tc_kernel(EdgeArgs a, const u
 
     if (a.st->code != 0) return;
     const int t = threadIdx.x, w = t >> 5, lane = t & 31;
+    const unsigned char* w2lo = w2g + W2_HALF;
     if (w == 0) {
         tmem_alloc(tslot, 512);
         tmem_relinquish();
     }
     if (t == 0) {
         mbar_init(mma_bar, 1);
+        mbar_init(w2h_bar, 1);
         for (int i = 0; i < NSLOT; ++i) {
             mbar_init(&full[i], 1);
             mbar_init(&empty[i], 1);
@@ -223,10 +317,10 @@ __global__ void __launch_bounds__(256, 1) edge_fwd_tc_kernel(EdgeArgs a, const u
         *abort_flag = 0;
         *ccount_s = 0;
     }
-    for (int i = t; i < (int)(W1_BYTES / 16); i += 256)
+    for (int i = t; i < (int)(W1_BYTES / 16); i += NT)
         reinterpret_cast<uint4*>(w1s)[i] = reinterpret_cast<const uint4*>(w1g)[i];
     if (t < H) b1s[t] = a.P[a.lo.b1 + t];
-    for (int i = t; i < H3; i += 256) b2s[i] = a.P[a.lo.b2 + i];
+    for (int i = t; i < H3; i += NT) b2s[i] = a.P[a.lo.b2 + i];
     if (t < RMAX) {
         cent[t] = a.centers[t];
         gam[t] = a.gamma[t];
@@ -241,14 +335,15 @@ __global__ void __launch_bounds__(256, 1) edge_fwd_tc_kernel(EdgeArgs a, const u
     uint32_t mma_phase = 0;
     uint32_t pcount = 0, ccount = 0;   // ring fills (thread 32) / uses (thread 0)
     uint32_t tiles = 0;
+    bool w2h_ready = false;
     if (t == 32) {
-        for (int i = 0; i < NSLOT; ++i) produce_slab(pcount++, ring, w2g, full, empty);
+        load_w2_hi(w2h, w2g, w2h_bar);
+        for (int i = 0; i < NSLOT; ++i) produce_lo(pcount++, ring, w2lo, full, empty);
     }
 
-    // epilogue-2 role: lane quarter q (channels 32q..32q+31), components
-    const int q = w & 3, role = w >> 2;
+    const int q = w & 3, r = w >> 2;
     const int c = 32 * q + lane;
-    const int comp0 = role == 0 ? 0 : 2, comp1 = role == 0 ? 1 : 3;
+    const int fidx = r * H + c;                      // this thread's feature element in a [4][H] row
     const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
 
     bool aborted = false;
@@ -257,16 +352,19 @@ __global__ void __launch_bounds__(256, 1) edge_fwd_tc_kernel(EdgeArgs a, const u
         if (j0 >= j1) continue;
         const int e0 = a.row_ptr[j0], e1 = a.row_ptr[j1];
         int cur = j0;
-        float acc0 = 0.f, acc1 = 0.f;
+        float acc = 0.f;
         for (int t0 = e0; t0 < e1; t0 += FN) {
             const int n = min(FN, e1 - t0);
             if (t < FN) load_edge(a, t0, t, n, us, src_s, rcv_s);
+            if (t == FN) *prev_s = cur;   // receiver before this tile
             __syncthreads();
-            {   // E tile: edge row, 16 RBF columns (one K-step) per thread
+            if (t < 2 * FN) {   // E tile: edge row, 16 RBF columns (one K-step) per thread
                 const int e = t & (FN - 1), s = t >> 7;
                 float v[16];
                 rbf16(us[e].w, e < n, 16 * s, a.R, cent, gam, a.cutoff, v);
                 store_row16(Es, F_EH, FN, e, s, v);
+            } else if (t < 3 * FN) {
+                tile_prep<FN>(t - 2 * FN, n, *prev_s, src_s, rcv_s, us, soff, nullptr, uc, chg);
             }
             fence_async_smem();
             __syncthreads();
@@ -283,49 +381,50 @@ __global__ void __launch_bounds__(256, 1) edge_fwd_tc_kernel(EdgeArgs a, const u
                     }
                 mma_commit(mma_bar);
             }
+            if (w == 0) __syncwarp();
             if (!mbar_wait(mma_bar, mma_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 1);
             mma_phase ^= 1;
             fence_after_sync();
-            {   // epilogue 1: h = silu(z + b1) -> H tile (split fp16)
-                const int k = 32 * q + lane, half = w >> 2;
+            {   // epilogue 1: h = silu(z + b1) -> H tile (split fp16), 32 edges per warp
+                const int k = c, col = 32 * r;
                 const float bias = b1s[k];
+                float z[32];
+                tmem_ld32(lane_base + col, z);
+                tmem_ld_wait();
 #pragma unroll
-                for (int blk = 0; blk < 2; ++blk) {
-                    const int col = 64 * half + 32 * blk;
-                    float z[32];
-                    tmem_ld32(lane_base + col, z);
-                    tmem_ld_wait();
-#pragma unroll
-                    for (int i = 0; i < 32; ++i) {
-                        __half hi, lo;
-                        split_f16(silu_f(z[i] + bias), hi, lo);
-                        const uint32_t off = b_off(FN, col + i, k);
-                        *reinterpret_cast<__half*>(Hs + off) = hi;
-                        *reinterpret_cast<__half*>(Hs + F_HH + off) = lo;
-                    }
+                for (int i = 0; i < 32; i += 2) {
+                    const float z0 = z[i] + bias, z1 = z[i + 1] + bias;
+                    store_col_pair(Hs, F_HH, FN, col + i, k, z0 * fast_sigmoid(z0), z1 * fast_sigmoid(z1));
                 }
             }
             fence_async_smem();
             fence_before_sync();
             __syncthreads();
-            if (t == 0) {   // GEMM2: f^T = W2 h^T, W2 streamed slab by slab
+            if (w == 0 && lane == 0) {   // GEMM2: f^T = W2 h^T
                 fence_after_sync();
-                bool ok = true;
-                for (int qq = 0; qq < W2_SLABS && ok; ++qq) {
+                if (!w2h_ready) {
+                    if (!mbar_wait(w2h_bar, 0, WAIT_BUDGET)) signal_timeout(a, abort_flag, 6);
+                    w2h_ready = true;
+                }
+                // resident hi tiles: W2hi h_hi + W2hi h_lo
+#pragma unroll 1
+                for (int qq = 0; qq < W2_TILES; ++qq) {
+                    const int g = qq / 8, s = qq % 8;
+                    const uint64_t ad = sdesc(smem_u32(w2h + qq * A_TILE), A_LBO, A_SBO);
+                    const uint32_t d = tmem + 128 + 128 * g;
+                    mma_f16(d, ad, sdesc(smem_u32(Hs + s * b_kstep(FN)), b_lbo(FN), 128), idesc, s != 0);
+                    mma_f16(d, ad, sdesc(smem_u32(Hs + F_HH + s * b_kstep(FN)), b_lbo(FN), 128), idesc, 1);
+                }
+                // streamed lo tiles: W2lo h_hi
+                for (int qq = 0; qq < W2_TILES; ++qq) {
                     const uint32_t slot = ccount % NSLOT;
                     if (!mbar_wait(&full[slot], (ccount / NSLOT) & 1, WAIT_BUDGET)) {
                         signal_timeout(a, abort_flag, 2);
-                        ok = false;
                         break;
                     }
                     const int g = qq / 8, s = qq % 8;
-#pragma unroll
-                    for (int pr = 0; pr < 3; ++pr) {
-                        const uint32_t ahl = pr == 2 ? 1 : 0, bhl = pr == 1 ? 1 : 0;
-                        const uint64_t ad = sdesc(smem_u32(ring + slot * SLAB + ahl * A_TILE), A_LBO, A_SBO);
-                        const uint64_t bd = sdesc(smem_u32(Hs + bhl * F_HH + s * b_kstep(FN)), b_lbo(FN), 128);
-                        mma_f16(tmem + 128 + 128 * g, ad, bd, idesc, (s | pr) != 0);
-                    }
+                    mma_f16(tmem + 128 + 128 * g, sdesc(smem_u32(ring + slot * A_TILE), A_LBO, A_SBO),
+                            sdesc(smem_u32(Hs + s * b_kstep(FN)), b_lbo(FN), 128), idesc, 1);
                     mma_commit(&empty[slot]);
                     ++ccount;
                 }
@@ -333,56 +432,64 @@ __global__ void __launch_bounds__(256, 1) edge_fwd_tc_kernel(EdgeArgs a, const u
                 *ccount_s = ccount;
             }
             if (t == 32) {
-                const uint32_t target = (uint32_t)W2_SLABS * (tiles + 1);
+                const uint32_t target = (uint32_t)W2_TILES * (tiles + 1);
                 while (pcount < target) {
-                    if (!produce_slab(pcount, ring, w2g, full, empty)) {
+                    if (!produce_lo(pcount, ring, w2lo, full, empty)) {
                         signal_timeout(a, abort_flag, 3);
                         break;
                     }
                     ++pcount;
                 }
             }
+            if (w < 2) __syncwarp();   // lanes 1-31 of the issuing / producing warps wait here, not in a spin loop
             if (!mbar_wait(mma_bar, mma_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 4);
             mma_phase ^= 1;
             fence_after_sync();
             ++tiles;
             if (t == 32 && !*abort_flag) {
-                // the ring is idle: prefetch the first slabs of the next tile
-                const uint32_t target = (uint32_t)W2_SLABS * tiles + NSLOT;
-                while (pcount < target && produce_slab(pcount, ring, w2g, full, empty)) ++pcount;
+                // the ring is idle: prefetch the first lo tiles of the next tile
+                const uint32_t target = (uint32_t)W2_TILES * tiles + NSLOT;
+                while (pcount < target && produce_lo(pcount, ring, w2lo, full, empty)) ++pcount;
             }
-            {   // epilogue 2: messages, receiver-segmented sums (no atomics)
-                const float bs = b2s[c], bv1 = b2s[H + c], bv2 = b2s[2 * H + c];
-                for (int blk = 0; blk < FN / 32; ++blk) {
-                    const int col = 32 * blk;
-                    if (col >= n) break;
-                    float fs[32], fv1[32], fv2[32];
-                    tmem_ld32(lane_base + 256 + col, fv1);
-                    tmem_ld32(lane_base + 384 + col, fv2);
-                    if (role == 0) tmem_ld32(lane_base + 128 + col, fs);
-                    tmem_ld_wait();
+            if (w == 1) __syncwarp();
+            {   // epilogue 2: component r of the message sums, segmented by receiver;
+                // 16-edge blocks, the next block's gathers in flight
+                const float bias1 = r == 0 ? b2s[c] : b2s[H + c], bias2 = b2s[2 * H + c];
+                const float* ur = uc + (r == 0 ? 0 : (r - 1) * FN);
+                const uint32_t f1col = r == 0 ? 128 : 256;
+                float xa[16], xn[16];
+                auto gather16 = [&](float (&x)[16], int col) {
 #pragma unroll
-                    for (int i = 0; i < 32; ++i) {
-                        const int e = col + i;
-                        if (e < n) {
-                            const int ra = rcv_s[e];
-                            if (ra != cur) {
-                                flush2(a.X, a.Xt, c, comp0, comp1, cur, ra, acc0, acc1);
-                                acc0 = acc1 = 0.f;
+                    for (int i = 0; i < 16; ++i) x[i] = __ldg(a.X + soff[col + i] + fidx);
+                };
+                auto process16 = [&](const float (&x)[16], int col) {
+                    float f1[16], f2[16];
+                    tmem_ld16(lane_base + f1col + col, f1);
+                    if (r != 0) tmem_ld16(lane_base + 384 + col, f2);
+                    tmem_ld_wait();
+                    const uint32_t mask = chg[col >> 5] >> (col & 31);
+                    const int m = min(16, n - col);
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) {
+                        if (i < m) {
+                            if (mask & (1u << i)) {
+                                const int ra = rcv_s[col + i];
+                                flush_sum(a.Xt, fidx, cur, ra, acc);
                                 cur = ra;
+                                acc = 0.f;
                             }
-                            const float* xb = a.X + (int64_t)src_s[e] * 4 * H;
-                            const float4 u = us[e];
-                            const float p1 = fv1[i] + bv1, p2 = fv2[i] + bv2;
-                            if (role == 0) {
-                                acc0 = fmaf(xb[c], fs[i] + bs, acc0);
-                                acc1 = fmaf(xb[H + c], p1, fmaf(u.x, p2, acc1));
-                            } else {
-                                acc0 = fmaf(xb[2 * H + c], p1, fmaf(u.y, p2, acc0));
-                                acc1 = fmaf(xb[3 * H + c], p1, fmaf(u.z, p2, acc1));
-                            }
+                            if (r == 0) acc = fmaf(x[i], f1[i] + bias1, acc);
+                            else acc = fmaf(x[i], f1[i] + bias1, fmaf(ur[col + i], f2[i] + bias2, acc));
                         }
                     }
+                };
+                gather16(xa, 0);
+                for (int col = 0; col < n; col += 32) {
+                    if (col + 16 < n) gather16(xn, col + 16);
+                    process16(xa, col);
+                    if (col + 16 >= n) break;
+                    if (col + 32 < n) gather16(xa, col + 32);
+                    process16(xn, col + 16);
                 }
             }
             fence_before_sync();
@@ -392,11 +499,13 @@ __global__ void __launch_bounds__(256, 1) edge_fwd_tc_kernel(EdgeArgs a, const u
                 break;
             }
         }
-        if (!aborted) flush2(a.X, a.Xt, c, comp0, comp1, cur, j1, acc0, acc1);
+        if (!aborted) flush_sum(a.Xt, fidx, cur, j1, acc);
     }
-    // drain: every ring fill issued must have landed before the CTA exits
+    // drain: the resident-tile load and every ring fill issued must have
+    // landed before the CTA exits
     __syncthreads();
     if (t == 32) {
+        if (!mbar_wait(w2h_bar, 0, WAIT_BUDGET)) set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 7);
         const uint32_t used = *ccount_s;
         for (uint32_t f = used; f < pcount; ++f)
             if (!mbar_wait(&full[f % NSLOT], (f / NSLOT) & 1, WAIT_BUDGET)) {
@@ -415,27 +524,32 @@ constexpr int BN = 64;
 constexpr uint32_t B_EH = 2 * b_kstep(BN);
 constexpr uint32_t B_HH = 8 * b_kstep(BN);
 constexpr uint32_t B_OFF_W1 = 0;
-constexpr uint32_t B_OFF_E = B_OFF_W1 + W1_BYTES;          // E then E'
-constexpr uint32_t B_OFF_H = align1k(B_OFF_E + 4 * B_EH);   // H then H'
+constexpr uint32_t B_OFF_W2H = B_OFF_W1 + W1_BYTES;
+constexpr uint32_t B_OFF_H = align1k(B_OFF_W2H + W2_HALF);     // H then H'; E, E' share the start
 constexpr uint32_t B_OFF_RING = align1k(B_OFF_H + 4 * B_HH);
-constexpr uint32_t B_OFF_US = B_OFF_RING + NSLOT * SLAB;
+constexpr uint32_t B_OFF_US = B_OFF_RING + NSLOT * A_TILE;
 constexpr uint32_t B_OFF_SRC = B_OFF_US + BN * 16;
 constexpr uint32_t B_OFF_RCV = B_OFF_SRC + BN * 4;
 constexpr uint32_t B_OFF_B1 = B_OFF_RCV + BN * 4;
 constexpr uint32_t B_OFF_B2 = B_OFF_B1 + H * 4;
 constexpr uint32_t B_OFF_CG = B_OFF_B2 + H3 * 4;
-constexpr uint32_t B_OFF_RED = B_OFF_CG + 2 * RMAX * 4;
-constexpr uint32_t B_OFF_BAR = B_OFF_RED + 8 * BN * 3 * 4;
-constexpr uint32_t B_OFF_MISC = B_OFF_BAR + 8 * (1 + 2 * NSLOT);
+constexpr uint32_t B_OFF_SOFF = B_OFF_CG + 2 * RMAX * 4;
+constexpr uint32_t B_OFF_ROFF = B_OFF_SOFF + BN * 4;
+constexpr uint32_t B_OFF_CHG = B_OFF_ROFF + BN * 4;
+constexpr uint32_t B_OFF_RED = B_OFF_CHG + (BN / 32) * 4 + 16;
+constexpr uint32_t B_OFF_BAR = B_OFF_RED + 16 * BN * 2 * 4;
+constexpr uint32_t B_OFF_MISC = B_OFF_BAR + 8 * (2 + 2 * NSLOT);
 constexpr uint32_t B_SMEM = align1k(B_OFF_MISC + 16);
+static_assert(4 * B_EH <= 4 * B_HH, "E tiles fit in the H tiles' space");
 static_assert(B_SMEM <= 232448, "reverse kernel shared memory");
 
-__global__ void __launch_bounds__(256, 1) edge_bwd_tc_kernel(EdgeArgs a, const unsigned char* __restrict__ w1g,
-                                                             const unsigned char* __restrict__ w2g) {
+__global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const unsigned char* __restrict__ w1g,
+                                                            const unsigned char* __restrict__ w2g) {
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* w1s = smem + B_OFF_W1;
-    unsigned char* Es = smem + B_OFF_E;            // [E hi, E lo, E' hi, E' lo]
+    unsigned char* w2h = smem + B_OFF_W2H;
     unsigned char* Hs = smem + B_OFF_H;            // [H hi, H lo, H' hi, H' lo]
+    unsigned char* Es = smem + B_OFF_H;            // [E hi, E lo, E' hi, E' lo], before H is written
     unsigned char* ring = smem + B_OFF_RING;
     float4* us = reinterpret_cast<float4*>(smem + B_OFF_US);
     int* src_s = reinterpret_cast<int*>(smem + B_OFF_SRC);
@@ -444,9 +558,14 @@ __global__ void __launch_bounds__(256, 1) edge_bwd_tc_kernel(EdgeArgs a, const u
     float* b2s = reinterpret_cast<float*>(smem + B_OFF_B2);
     float* cent = reinterpret_cast<float*>(smem + B_OFF_CG);
     float* gam = cent + RMAX;
-    float* red = reinterpret_cast<float*>(smem + B_OFF_RED);   // [8 warps][BN][3]
+    float* red = reinterpret_cast<float*>(smem + B_OFF_RED);   // [16 warps][BN][2]
+    int* soff = reinterpret_cast<int*>(smem + B_OFF_SOFF);
+    int* roff = reinterpret_cast<int*>(smem + B_OFF_ROFF);
+    uint32_t* chg = reinterpret_cast<uint32_t*>(smem + B_OFF_CHG);
+    int* prev_s = reinterpret_cast<int*>(smem + B_OFF_CHG + (BN / 32) * 4);
     uint64_t* mma_bar = reinterpret_cast<uint64_t*>(smem + B_OFF_BAR);
-    uint64_t* full = mma_bar + 1;
+    uint64_t* w2h_bar = mma_bar + 1;
+    uint64_t* full = mma_bar + 2;
     uint64_t* empty = full + NSLOT;
     uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + B_OFF_MISC);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + B_OFF_MISC + 4);
@@ -454,12 +573,14 @@ __global__ void __launch_bounds__(256, 1) edge_bwd_tc_kernel(EdgeArgs a, const u
 
     if (a.st->code != 0) return;
     const int t = threadIdx.x, w = t >> 5, lane = t & 31;
+    const unsigned char* w2lo = w2g + W2_HALF;
     if (w == 0) {
         tmem_alloc(tslot, 512);
         tmem_relinquish();
     }
     if (t == 0) {
         mbar_init(mma_bar, 1);
+        mbar_init(w2h_bar, 1);
         for (int i = 0; i < NSLOT; ++i) {
             mbar_init(&full[i], 1);
             mbar_init(&empty[i], 1);
@@ -468,10 +589,10 @@ __global__ void __launch_bounds__(256, 1) edge_bwd_tc_kernel(EdgeArgs a, const u
         *abort_flag = 0;
         *ccount_s = 0;
     }
-    for (int i = t; i < (int)(W1_BYTES / 16); i += 256)
+    for (int i = t; i < (int)(W1_BYTES / 16); i += NT)
         reinterpret_cast<uint4*>(w1s)[i] = reinterpret_cast<const uint4*>(w1g)[i];
     if (t < H) b1s[t] = a.P[a.lo.b1 + t];
-    for (int i = t; i < H3; i += 256) b2s[i] = a.P[a.lo.b2 + i];
+    for (int i = t; i < H3; i += NT) b2s[i] = a.P[a.lo.b2 + i];
     if (t < RMAX) {
         cent[t] = a.centers[t];
         gam[t] = a.gamma[t];
@@ -486,13 +607,16 @@ __global__ void __launch_bounds__(256, 1) edge_bwd_tc_kernel(EdgeArgs a, const u
     uint32_t mma_phase = 0;
     uint32_t pcount = 0, ccount = 0;
     uint32_t tiles = 0;
+    bool w2h_ready = false;
     if (t == 32) {
-        for (int i = 0; i < NSLOT; ++i) produce_slab(pcount++, ring, w2g, full, empty);
+        load_w2_hi(w2h, w2g, w2h_bar);
+        for (int i = 0; i < NSLOT; ++i) produce_lo(pcount++, ring, w2lo, full, empty);
     }
-    const int q = w & 3, role = w >> 2;
+    const int q = w & 3, r = w >> 2;
     const int c = 32 * q + lane;
-    const int comp0 = role == 0 ? 0 : 2, comp1 = role == 0 ? 1 : 3;
+    const int fidx = r * H + c;
     const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
+    const int rs_idx = reduce_scatter8_index(lane);
 
     bool aborted = false;
     for (int p = blockIdx.x; p < a.nparts && !aborted; p += gridDim.x) {
@@ -500,23 +624,20 @@ __global__ void __launch_bounds__(256, 1) edge_bwd_tc_kernel(EdgeArgs a, const u
         if (j0 >= j1) continue;
         const int e0 = a.row_ptr[j0], e1 = a.row_ptr[j1];
         int cur = j0;
-        float acc0 = 0.f, acc1 = 0.f;
-        float ta0, ta1;   // receiver adjoint (dE/dXt) for this thread's two components
-        {
-            const float* tr = a.xtbar + (int64_t)cur * 4 * H;
-            ta0 = tr[comp0 * H + c];
-            ta1 = tr[comp1 * H + c];
-        }
+        float acc = 0.f;
         for (int t0 = e0; t0 < e1; t0 += BN) {
             const int n = min(BN, e1 - t0);
             if (t < BN) load_edge(a, t0, t, n, us, src_s, rcv_s);
+            if (t == BN) *prev_s = cur;   // receiver before this tile
             __syncthreads();
-            {   // E (rbf * fc) and E' (its d-derivative) tiles
+            if (t < 4 * BN) {   // E (rbf * fc) and E' (its d-derivative) tiles
                 const int e = t & (BN - 1), s = (t >> 6) & 1, which = t >> 7;
                 float v[16];
                 if (which == 0) rbf16(us[e].w, e < n, 16 * s, a.R, cent, gam, a.cutoff, v);
                 else rbf16_d(us[e].w, e < n, 16 * s, a.R, cent, gam, a.cutoff, v);
                 store_row16(Es + which * 2 * B_EH, B_EH, BN, e, s, v);
+            } else if (t < 5 * BN) {
+                tile_prep<BN>(t - 4 * BN, n, *prev_s, src_s, rcv_s, us, soff, roff, nullptr, chg);
             }
             fence_async_smem();
             __syncthreads();
@@ -536,53 +657,59 @@ __global__ void __launch_bounds__(256, 1) edge_bwd_tc_kernel(EdgeArgs a, const u
                         }
                 mma_commit(mma_bar);
             }
+            if (w == 0) __syncwarp();
             if (!mbar_wait(mma_bar, mma_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 11);
             mma_phase ^= 1;
             fence_after_sync();
-            {   // epilogue 1: h = silu(z + b1), h' = silu'(z + b1) z'
-                const int k = 32 * q + lane, col = 32 * (w >> 2);
+            {   // epilogue 1: h = silu(z + b1), h' = silu'(z + b1) z', 16 edges per warp
+                const int k = c, col = 16 * r;
                 const float bias = b1s[k];
-                float z[32], zd[32];
-                tmem_ld32(lane_base + col, z);
-                tmem_ld32(lane_base + 64 + col, zd);
+                float z[16], zd[16];
+                tmem_ld16(lane_base + col, z);
+                tmem_ld16(lane_base + 64 + col, zd);
                 tmem_ld_wait();
 #pragma unroll
-                for (int i = 0; i < 32; ++i) {
-                    const float zz = z[i] + bias;
-                    __half hi, lo, dhi, dlo;
-                    split_f16(silu_f(zz), hi, lo);
-                    split_f16(dsilu_f(zz) * zd[i], dhi, dlo);
-                    const uint32_t off = b_off(BN, col + i, k);
-                    *reinterpret_cast<__half*>(Hs + off) = hi;
-                    *reinterpret_cast<__half*>(Hs + B_HH + off) = lo;
-                    *reinterpret_cast<__half*>(Hs + 2 * B_HH + off) = dhi;
-                    *reinterpret_cast<__half*>(Hs + 3 * B_HH + off) = dlo;
+                for (int i = 0; i < 16; i += 2) {
+                    const float z0 = z[i] + bias, z1 = z[i + 1] + bias;
+                    const float s0 = fast_sigmoid(z0), s1 = fast_sigmoid(z1);
+                    store_col_pair(Hs, B_HH, BN, col + i, k, z0 * s0, z1 * s1);
+                    store_col_pair(Hs + 2 * B_HH, B_HH, BN, col + i, k, s0 * (1.0f + z0 * (1.0f - s0)) * zd[i],
+                                   s1 * (1.0f + z1 * (1.0f - s1)) * zd[i + 1]);
                 }
             }
             fence_async_smem();
             fence_before_sync();
             __syncthreads();
-            if (t == 0) {   // f^T = W2 h^T and f'^T = W2 h'^T share each W2 slab
+            if (w == 0 && lane == 0) {   // f^T = W2 h^T and f'^T = W2 h'^T
                 fence_after_sync();
-                bool ok = true;
-                for (int qq = 0; qq < W2_SLABS && ok; ++qq) {
+                if (!w2h_ready) {
+                    if (!mbar_wait(w2h_bar, 0, WAIT_BUDGET)) signal_timeout(a, abort_flag, 16);
+                    w2h_ready = true;
+                }
+#pragma unroll 1
+                for (int qq = 0; qq < W2_TILES; ++qq) {
+                    const int g = qq / 8, s = qq % 8;
+                    const uint64_t ad = sdesc(smem_u32(w2h + qq * A_TILE), A_LBO, A_SBO);
+#pragma unroll
+                    for (int which = 0; which < 2; ++which) {
+                        const uint32_t d = tmem + 128 + 192 * which + 64 * g;
+                        unsigned char* hb = Hs + which * 2 * B_HH + s * b_kstep(BN);
+                        mma_f16(d, ad, sdesc(smem_u32(hb), b_lbo(BN), 128), idesc, s != 0);
+                        mma_f16(d, ad, sdesc(smem_u32(hb + B_HH), b_lbo(BN), 128), idesc, 1);
+                    }
+                }
+                for (int qq = 0; qq < W2_TILES; ++qq) {
                     const uint32_t slot = ccount % NSLOT;
                     if (!mbar_wait(&full[slot], (ccount / NSLOT) & 1, WAIT_BUDGET)) {
                         signal_timeout(a, abort_flag, 12);
-                        ok = false;
                         break;
                     }
                     const int g = qq / 8, s = qq % 8;
+                    const uint64_t ad = sdesc(smem_u32(ring + slot * A_TILE), A_LBO, A_SBO);
 #pragma unroll
                     for (int which = 0; which < 2; ++which)
-#pragma unroll
-                        for (int pr = 0; pr < 3; ++pr) {
-                            const uint32_t ahl = pr == 2 ? 1 : 0, bhl = pr == 1 ? 1 : 0;
-                            const uint64_t ad = sdesc(smem_u32(ring + slot * SLAB + ahl * A_TILE), A_LBO, A_SBO);
-                            const uint64_t bd = sdesc(smem_u32(Hs + which * 2 * B_HH + bhl * B_HH + s * b_kstep(BN)),
-                                                      b_lbo(BN), 128);
-                            mma_f16(tmem + 128 + 192 * which + 64 * g, ad, bd, idesc, (s | pr) != 0);
-                        }
+                        mma_f16(tmem + 128 + 192 * which + 64 * g, ad,
+                                sdesc(smem_u32(Hs + which * 2 * B_HH + s * b_kstep(BN)), b_lbo(BN), 128), idesc, 1);
                     mma_commit(&empty[slot]);
                     ++ccount;
                 }
@@ -590,105 +717,110 @@ __global__ void __launch_bounds__(256, 1) edge_bwd_tc_kernel(EdgeArgs a, const u
                 *ccount_s = ccount;
             }
             if (t == 32) {
-                const uint32_t target = (uint32_t)W2_SLABS * (tiles + 1);
+                const uint32_t target = (uint32_t)W2_TILES * (tiles + 1);
                 while (pcount < target) {
-                    if (!produce_slab(pcount, ring, w2g, full, empty)) {
+                    if (!produce_lo(pcount, ring, w2lo, full, empty)) {
                         signal_timeout(a, abort_flag, 13);
                         break;
                     }
                     ++pcount;
                 }
             }
+            if (w < 2) __syncwarp();   // lanes 1-31 of the issuing / producing warps wait here, not in a spin loop
             if (!mbar_wait(mma_bar, mma_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 14);
             mma_phase ^= 1;
             fence_after_sync();
             ++tiles;
             if (t == 32 && !*abort_flag) {
-                const uint32_t target = (uint32_t)W2_SLABS * tiles + NSLOT;
-                while (pcount < target && produce_slab(pcount, ring, w2g, full, empty)) ++pcount;
+                const uint32_t target = (uint32_t)W2_TILES * tiles + NSLOT;
+                while (pcount < target && produce_lo(pcount, ring, w2lo, full, empty)) ++pcount;
             }
-            {   // epilogue 2: node adjoints (gathered), per-edge dE/dd and dE/du partials
+            if (w == 1) __syncwarp();
+            {   // epilogue 2: component r of the node adjoints (gathered from the
+                // sender side, summed per receiver) and this component's share
+                // of dE/dd, dE/du; 8-edge blocks, the next block's gathers in flight
                 const float bs = b2s[c], bv1 = b2s[H + c], bv2 = b2s[2 * H + c];
-                for (int blk = 0; blk < BN / 16; ++blk) {
-                    const int col = 16 * blk;
-                    if (col >= n) break;
-                    float fs[16], fv1[16], fv2[16], ds[16], dv1[16], dv2[16];
-                    tmem_ld16(lane_base + 128 + 64 + col, fv1);
-                    tmem_ld16(lane_base + 128 + 128 + col, fv2);
-                    tmem_ld16(lane_base + 320 + 64 + col, dv1);
-                    tmem_ld16(lane_base + 320 + 128 + col, dv2);
-                    if (role == 0) {
-                        tmem_ld16(lane_base + 128 + col, fs);
-                        tmem_ld16(lane_base + 320 + col, ds);
+                const float bias1 = r == 0 ? bs : bv1;
+                const uint32_t f1col = r == 0 ? 128 : 192, d1col = r == 0 ? 320 : 384;
+                float tba[8], xba[8], tra[8], tbn[8], xbn[8], trn[8];
+                auto gather8 = [&](float (&tb)[8], float (&xb)[8], float (&tr)[8], int col) {
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        const int so = soff[col + i] + fidx;
+                        tb[i] = __ldg(a.xtbar + so);
+                        xb[i] = __ldg(a.X + so);
+                        tr[i] = __ldg(a.xtbar + roff[col + i] + fidx);
+                    }
+                };
+                auto process8 = [&](const float (&tb)[8], const float (&xb)[8], const float (&tr)[8], int col) {
+                    float f1[8], f2[8], d1[8], d2[8];
+                    tmem_ld8(lane_base + f1col + col, f1);   // phi_s or phi_v1
+                    tmem_ld8(lane_base + d1col + col, d1);   // its d-derivative
+                    if (r != 0) {
+                        tmem_ld8(lane_base + 256 + col, f2);  // phi_v2
+                        tmem_ld8(lane_base + 448 + col, d2);  // dphi_v2/dd
                     }
                     tmem_ld_wait();
+                    const uint32_t mask = chg[col >> 5] >> (col & 31);
+                    const int m = min(8, n - col);
+                    float p0[8], p1[8];
 #pragma unroll
-                    for (int i = 0; i < 16; ++i) {
-                        const int e = col + i;
-                        if (e < n) {
-                            const int ra = rcv_s[e];
-                            if (ra != cur) {
-                                flush2(a.xtbar, a.xbar, c, comp0, comp1, cur, ra, acc0, acc1);
-                                acc0 = acc1 = 0.f;
+                    for (int i = 0; i < 8; ++i) {
+                        p0[i] = 0.f;
+                        p1[i] = 0.f;
+                        if (i < m) {
+                            if (mask & (1u << i)) {
+                                const int ra = rcv_s[col + i];
+                                if (a.write_nodes) flush_sum(a.xbar, fidx, cur, ra, acc);
                                 cur = ra;
-                                const float* tr = a.xtbar + (int64_t)cur * 4 * H;
-                                ta0 = tr[comp0 * H + c];
-                                ta1 = tr[comp1 * H + c];
+                                acc = 0.f;
                             }
-                            const int64_t rb = (int64_t)src_s[e] * 4 * H;
-                            const float tb0 = a.xtbar[rb + comp0 * H + c], tb1 = a.xtbar[rb + comp1 * H + c];
-                            const float xb0 = a.X[rb + comp0 * H + c], xb1 = a.X[rb + comp1 * H + c];
-                            const float4 u = us[e];
-                            const float p1 = fv1[i] + bv1, p2 = fv2[i] + bv2;
-                            float r0, r1, r2;
-                            if (role == 0) {   // components s, v_x
-                                acc0 = fmaf(tb0, fs[i] + bs, acc0);
-                                acc1 = fmaf(tb1, p1, acc1);
-                                r0 = (ta0 * xb0) * ds[i] + (ta1 * xb1) * dv1[i] + (ta1 * u.x) * dv2[i];
-                                r1 = ta1 * p2;
-                                r2 = 0.f;
-                            } else {           // components v_y, v_z
-                                acc0 = fmaf(tb0, p1, acc0);
-                                acc1 = fmaf(tb1, p1, acc1);
-                                r0 = (ta0 * xb0 + ta1 * xb1) * dv1[i] + (ta0 * u.y + ta1 * u.z) * dv2[i];
-                                r1 = ta0 * p2;
-                                r2 = ta1 * p2;
-                            }
-#pragma unroll
-                            for (int o = 16; o > 0; o >>= 1) {
-                                r0 += __shfl_xor_sync(0xffffffffu, r0, o);
-                                r1 += __shfl_xor_sync(0xffffffffu, r1, o);
-                                r2 += __shfl_xor_sync(0xffffffffu, r2, o);
-                            }
-                            if (lane == 0) {
-                                float* rr = red + ((size_t)w * BN + e) * 3;
-                                rr[0] = r0;
-                                rr[1] = r1;
-                                rr[2] = r2;
+                            const float ta = tr[i];
+                            acc = fmaf(tb[i], f1[i] + bias1, acc);
+                            if (r == 0) {
+                                p0[i] = (ta * xb[i]) * d1[i];
+                            } else {
+                                const float4 u = us[col + i];
+                                const float ue = r == 1 ? u.x : (r == 2 ? u.y : u.z);
+                                p0[i] = ta * (xb[i] * d1[i] + ue * d2[i]);
+                                p1[i] = ta * (f2[i] + bv2);
                             }
                         }
                     }
+                    const float s0 = warp_reduce_scatter8(p0, lane);
+                    float s1 = 0.f;
+                    if (r != 0) s1 = warp_reduce_scatter8(p1, lane);
+                    if ((lane & 3) == 0) {
+                        float* rr = red + ((size_t)w * BN + col + rs_idx) * 2;
+                        rr[0] = s0;
+                        rr[1] = s1;
+                    }
+                };
+                gather8(tba, xba, tra, 0);
+                for (int col = 0; col < n; col += 16) {
+                    if (col + 8 < n) gather8(tbn, xbn, trn, col + 8);
+                    process8(tba, xba, tra, col);
+                    if (col + 8 >= n) break;
+                    if (col + 16 < n) gather8(tba, xba, tra, col + 16);
+                    process8(tbn, xbn, trn, col + 8);
                 }
             }
             fence_before_sync();
             __syncthreads();
             if (t < n) {
-                float dd = 0.f, dux = 0.f, duy = 0.f, duz = 0.f;
+                float dd = 0.f, du[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-                for (int qq = 0; qq < 4; ++qq) {
-                    const float* r0p = red + ((size_t)qq * BN + t) * 3;         // role 0 warps
-                    const float* r1p = red + ((size_t)(4 + qq) * BN + t) * 3;   // role 1 warps
-                    dd += r0p[0] + r1p[0];
-                    dux += r0p[1];
-                    duy += r1p[1];
-                    duz += r1p[2];
+                for (int ww = 0; ww < 16; ++ww) {
+                    const float* rr = red + ((size_t)ww * BN + t) * 2;
+                    dd += rr[0];
+                    if (ww >= 4) du[(ww >> 2) - 1] += rr[1];
                 }
-                float4 acc = a.eacc[t0 + t];
-                acc.x += dd;
-                acc.y += dux;
-                acc.z += duy;
-                acc.w += duz;
-                a.eacc[t0 + t] = acc;
+                float4 ea = a.eacc[t0 + t];
+                ea.x += dd;
+                ea.y += du[0];
+                ea.z += du[1];
+                ea.w += du[2];
+                a.eacc[t0 + t] = ea;
             }
             __syncthreads();
             if (*abort_flag) {
@@ -696,10 +828,11 @@ __global__ void __launch_bounds__(256, 1) edge_bwd_tc_kernel(EdgeArgs a, const u
                 break;
             }
         }
-        if (!aborted) flush2(a.xtbar, a.xbar, c, comp0, comp1, cur, j1, acc0, acc1);
+        if (!aborted && a.write_nodes) flush_sum(a.xbar, fidx, cur, j1, acc);
     }
     __syncthreads();
     if (t == 32) {
+        if (!mbar_wait(w2h_bar, 0, WAIT_BUDGET)) set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 17);
         const uint32_t used = *ccount_s;
         for (uint32_t f = used; f < pcount; ++f)
             if (!mbar_wait(&full[f % NSLOT], (f / NSLOT) & 1, WAIT_BUDGET)) {
@@ -735,7 +868,7 @@ int launch_edge_fwd_tc(const EdgeArgs& a, int layer, cudaStream_t st) {
     if (attr_err != cudaSuccess) return cuda_status(attr_err, "edge_fwd_tc smem attribute");
     const unsigned char* w1 = reinterpret_cast<const unsigned char*>(a.P + a.lo.w1_bf);
     const unsigned char* w2 = reinterpret_cast<const unsigned char*>(a.P + a.lo.w2_bf);
-    edge_fwd_tc_kernel<<<tc_grid(a.nparts), 256, F_SMEM, st>>>(a, w1, w2);
+    edge_fwd_tc_kernel<<<tc_grid(a.nparts), NT, F_SMEM, st>>>(a, w1, w2);
     MLFF_LAUNCH_CHECK("edge_fwd_tc");
     return MLFF_OK;
 }
@@ -750,7 +883,7 @@ int launch_edge_bwd_tc(const EdgeArgs& a, int layer, cudaStream_t st) {
     if (attr_err != cudaSuccess) return cuda_status(attr_err, "edge_bwd_tc smem attribute");
     const unsigned char* w1 = reinterpret_cast<const unsigned char*>(a.P + a.lo.w1_bf);
     const unsigned char* w2 = reinterpret_cast<const unsigned char*>(a.P + a.lo.w2_bf);
-    edge_bwd_tc_kernel<<<tc_grid(a.nparts), 256, B_SMEM, st>>>(a, w1, w2);
+    edge_bwd_tc_kernel<<<tc_grid(a.nparts), NT, B_SMEM, st>>>(a, w1, w2);
     MLFF_LAUNCH_CHECK("edge_bwd_tc");
     return MLFF_OK;
 }

@@ -295,6 +295,31 @@ __global__ void __launch_bounds__(128) edge_bwd_simt_kernel(EdgeArgs a) {
 int launch_edge_fwd_tc(const EdgeArgs& a, int layer, cudaStream_t st);
 int launch_edge_bwd_tc(const EdgeArgs& a, int layer, cudaStream_t st);
 
+// dst += src over n4 float4 elements (the tensor-core edge kernels write
+// per-receiver sums only; the per-atom term is added here)
+__global__ void add_rows_kernel(float4* __restrict__ dst, const float4* __restrict__ src, int64_t n4,
+                                const Status* st) {
+    if (st->code != 0) return;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n4; i += (int64_t)gridDim.x * blockDim.x) {
+        float4 d = dst[i];
+        const float4 v = src[i];
+        d.x += v.x;
+        d.y += v.y;
+        d.z += v.z;
+        d.w += v.w;
+        dst[i] = d;
+    }
+}
+
+static int add_rows(float* dst, const float* src, int64_t n, const Status* st, cudaStream_t s) {
+    const int64_t n4 = n / 4;
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((n4 + 255) / 256, 152 * 8));
+    add_rows_kernel<<<blocks, 256, 0, s>>>(reinterpret_cast<float4*>(dst), reinterpret_cast<const float4*>(src), n4,
+                                           st);
+    MLFF_LAUNCH_CHECK("add_rows");
+    return MLFF_OK;
+}
+
 int run_tuned(const mlff_dims& d, const float* P, const PackedOffsets& po, const mlff_system& sys,
               const WsLayout& L, void* ws, const mlff_outputs& out, int path, cudaStream_t st) {
     const int N = sys.n_atoms;
@@ -331,6 +356,7 @@ int run_tuned(const mlff_dims& d, const float* P, const PackedOffsets& po, const
             ProfScope prof(PK_EDGE_FWD, st);
             if (tc) {
                 if ((r = launch_edge_fwd_tc(a, l, st))) return r;
+                if ((r = add_rows(a.Xt, a.X, NX, a.st, st))) return r;
             } else {
                 edge_fwd_simt_kernel<<<L.P, 128, 0, st>>>(a);
                 MLFF_LAUNCH_CHECK("edge_fwd_simt");
@@ -351,10 +377,12 @@ int run_tuned(const mlff_dims& d, const float* P, const PackedOffsets& po, const
         a.X = X + l * NX;
         a.xtbar = xtb;
         a.xbar = xbo;
+        a.write_nodes = l > 0 ? 1 : 0;
         {
             ProfScope prof(PK_EDGE_BWD, st);
             if (tc) {
                 if ((r = launch_edge_bwd_tc(a, l, st))) return r;
+                if (l > 0 && (r = add_rows(xbo, xtb, NX, a.st, st))) return r;
             } else {
                 edge_bwd_simt_kernel<<<L.P, 128, 0, st>>>(a);
                 MLFF_LAUNCH_CHECK("edge_bwd_simt");
