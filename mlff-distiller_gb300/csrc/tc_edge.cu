@@ -382,8 +382,12 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                 mma_commit(mma_bar);
             }
             if (w == 0) __syncwarp();
-            if (!mbar_wait(mma_bar, mma_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 1);
+            // only warp 0 polls the MMA barrier; the others wait at the CTA
+            // barrier instead of spinning on shared memory the MMAs read from
+            if (w == 0 && !mbar_wait(mma_bar, mma_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 1);
             mma_phase ^= 1;
+            fence_before_sync();
+            __syncthreads();
             fence_after_sync();
             {   // epilogue 1: h = silu(z + b1) -> H tile (split fp16), 32 edges per warp
                 const int k = c, col = 32 * r;
@@ -442,8 +446,12 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                 }
             }
             if (w < 2) __syncwarp();   // lanes 1-31 of the issuing / producing warps wait here, not in a spin loop
-            if (!mbar_wait(mma_bar, mma_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 4);
+            // only warp 0 polls the MMA barrier; the others wait at the CTA
+            // barrier instead of spinning on shared memory the MMAs read from
+            if (w == 0 && !mbar_wait(mma_bar, mma_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 4);
             mma_phase ^= 1;
+            fence_before_sync();
+            __syncthreads();
             fence_after_sync();
             ++tiles;
             if (t == 32 && !*abort_flag) {
@@ -658,8 +666,12 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                 mma_commit(mma_bar);
             }
             if (w == 0) __syncwarp();
-            if (!mbar_wait(mma_bar, mma_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 11);
+            // only warp 0 polls the MMA barrier; the others wait at the CTA
+            // barrier instead of spinning on shared memory the MMAs read from
+            if (w == 0 && !mbar_wait(mma_bar, mma_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 11);
             mma_phase ^= 1;
+            fence_before_sync();
+            __syncthreads();
             fence_after_sync();
             {   // epilogue 1: h = silu(z + b1), h' = silu'(z + b1) z', 16 edges per warp
                 const int k = c, col = 16 * r;
@@ -727,8 +739,12 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                 }
             }
             if (w < 2) __syncwarp();   // lanes 1-31 of the issuing / producing warps wait here, not in a spin loop
-            if (!mbar_wait(mma_bar, mma_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 14);
+            // only warp 0 polls the MMA barrier; the others wait at the CTA
+            // barrier instead of spinning on shared memory the MMAs read from
+            if (w == 0 && !mbar_wait(mma_bar, mma_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 14);
             mma_phase ^= 1;
+            fence_before_sync();
+            __syncthreads();
             fence_after_sync();
             ++tiles;
             if (t == 32 && !*abort_flag) {
