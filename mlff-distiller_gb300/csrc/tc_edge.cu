@@ -45,20 +45,36 @@ constexpr uint32_t SLAB = 2 * A_TILE;         // hi + lo of one 128 x 16 block (
 constexpr int W2_TILES = 24;                  // 3 channel chunks x 8 K-steps, q = g * 8 + s
 constexpr uint32_t W1_BYTES = 2 * SLAB;       // 2 K-steps
 constexpr uint32_t W2_HALF = W2_TILES * A_TILE;   // all hi tiles (96 KB), then all lo tiles
-constexpr int NSLOT = 8;                      // ring depth for the streamed lo tiles
+constexpr int NSLOT = 8;                      // ring: the 8 lo tiles of W2 chunk 2, one round per edge tile
+
+// TMEM columns (512 allocated): [0,128) the lo halves of W2 chunks 0 and 1
+// as MMA A operands (chunk g, K-step s at 64 g + 8 s); [128,512) the GEMM2
+// accumulators, chunk g at 128 + 128 g; GEMM1 writes z into chunk 2's
+// columns, which epilogue 1 reads before it refills them with the bias.
+constexpr uint32_t TM_W2LO = 0;
+constexpr uint32_t TM_F = 128;
+constexpr uint32_t TM_Z = 384;
 
 __host__ __device__ constexpr uint32_t a_off(int m, int k) {
     return (uint32_t)((k >> 3) * 2048 + (m >> 3) * 128 + (m & 7) * 16 + (k & 7) * 2);
 }
 
-// B operand (edge rows) with N rows: per K-step two 8-column chunks, the
-// second LB = N*16 + 16 bytes after the first (the extra 16 bytes spread
-// the epilogue's 2-byte stores over distinct banks).
-__host__ __device__ constexpr uint32_t b_lbo(int n) { return (uint32_t)(n * 16 + 16); }
-__host__ __device__ constexpr uint32_t b_kstep(int n) { return 2 * b_lbo(n); }
+// B operand (edge rows x K, fp16) in the K-major 128-byte-swizzle layout:
+// K-blocks of 64 columns, each n_rows x 128 bytes; inside a block, 8-row
+// groups of 1024 bytes, and row r's 16-byte chunk j (columns 8j..8j+7) sits
+// at chunk position j ^ (r % 8).  A warp storing 32 consecutive columns of
+// one row touches one 128-byte line, and the MMA reads whole lines.
+__host__ __device__ constexpr uint32_t b_block(int n_rows) { return (uint32_t)n_rows * 128; }
 __device__ __forceinline__ uint32_t b_off(int n_rows, int row, int k) {
-    return (uint32_t)((k >> 4) * b_kstep(n_rows) + ((k >> 3) & 1) * b_lbo(n_rows) + (row >> 3) * 128 +
-                      (row & 7) * 16 + (k & 7) * 2);
+    return (uint32_t)((k >> 6) * b_block(n_rows) + (row >> 3) * 1024 + (row & 7) * 128 +
+                      ((((k >> 3) & 7) ^ (row & 7)) << 4) + (k & 7) * 2);
+}
+// descriptor start offset of K-step s (columns 16s..16s+15)
+__host__ __device__ constexpr uint32_t b_kstep_off(int n_rows, int s) {
+    return (uint32_t)((s >> 2) * b_block(n_rows) + (s & 3) * 32);
+}
+__device__ __forceinline__ uint64_t sdesc_b(uint32_t saddr) {
+    return sdesc(saddr, 16, 1024) | ((uint64_t)2 << 61);   // layout 2: 128-byte swizzle
 }
 
 constexpr uint32_t align1k(uint32_t x) { return (x + 1023u) & ~1023u; }
@@ -105,16 +121,35 @@ __device__ __forceinline__ void signal_timeout(const EdgeArgs& a, volatile int* 
     *abort_flag = 1;
 }
 
-// Ring producer: fill number p brings lo tile p % 24 of W2 into slot p % NSLOT.
-__device__ __forceinline__ bool produce_lo(uint32_t p, unsigned char* ring, const unsigned char* w2lo,
-                                           uint64_t* full, uint64_t* empty) {
-    const uint32_t slot = p % NSLOT;
-    if (p >= (uint32_t)NSLOT) {
-        if (!mbar_wait(&empty[slot], ((p / NSLOT) - 1) & 1, WAIT_BUDGET)) return false;
+// Ring producer: the 8 lo tiles of W2 chunk 2 (tiles 16..23), one per slot.
+// Called once the MMAs of the previous edge tile have completed.
+__device__ __forceinline__ void fill_lo_ring(unsigned char* ring, const unsigned char* w2lo, uint64_t* full) {
+#pragma unroll 1
+    for (int slot = 0; slot < NSLOT; ++slot) {
+        mbar_expect_tx(&full[slot], A_TILE);
+        bulk_g2s(ring + slot * A_TILE, w2lo + (size_t)(16 + slot) * A_TILE, A_TILE, &full[slot]);
     }
-    mbar_expect_tx(&full[slot], A_TILE);
-    bulk_g2s(ring + slot * A_TILE, w2lo + (size_t)(p % W2_TILES) * A_TILE, A_TILE, &full[slot]);
-    return true;
+}
+
+// Lo halves of W2 chunks 0 and 1 into TMEM columns [0,128), as A operands:
+// warp (q, r) writes rows 32q..32q+31 (its TMEM lane quarter), K-steps
+// 4r..4r+3 of the 16 (chunk (4r) / 8), i.e. columns 32r..32r+31.
+__device__ __forceinline__ void load_w2_lo_tmem(uint32_t lane_base, const float* w2, int r, int m) {
+    uint32_t v[32];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int ks = 4 * r + i, g = ks >> 3, s = ks & 7;
+        const float* row = w2 + (size_t)(g * 128 + m) * H + 16 * s;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            __half hi0, lo0, hi1, lo1;
+            split_f16(row[2 * j], hi0, lo0);
+            split_f16(row[2 * j + 1], hi1, lo1);
+            __half2 pr = __halves2half2(lo0, lo1);
+            v[8 * i + j] = *reinterpret_cast<uint32_t*>(&pr);
+        }
+    }
+    tmem_st32u(lane_base + TM_W2LO + 32 * r, v);
 }
 
 // Resident hi half of W2: six 16 KB bulk copies on one mbarrier.
@@ -188,14 +223,6 @@ __device__ __forceinline__ void store_col_pair(unsigned char* tile, uint32_t hal
     *reinterpret_cast<__half*>(tile + half_bytes + o1) = __high2half(lo);
 }
 
-// Receiver flush for one feature component: out[cur] = value (the sum over
-// the receiver's edges), then 0 for receivers without edges up to next.
-// The caller adds the per-atom term afterwards in one vectorised pass.
-__device__ __noinline__ void flush_sum(float* __restrict__ out, int idx, int cur, int next, float value) {
-    out[(int64_t)cur * 4 * H + idx] = value;
-    for (int j = cur + 1; j < next; ++j) out[(int64_t)j * 4 * H + idx] = 0.0f;
-}
-
 // Per-tile prep by threads otherwise idle during the E-tile phase: sender
 // (and receiver) row offsets, u components, and a bitmask of the edges whose
 // receiver differs from the previous edge's (edge 0 compares with prev).
@@ -246,10 +273,54 @@ __device__ __forceinline__ int reduce_scatter8_index(int lane) {
     return ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
 }
 
+// GEMM2 of one tile, issued by one thread: D chunk g (TMEM columns
+// 128 + 128 g) += W2[g] B^T with B a 128-row split-fp16 tile at Hs (hi half,
+// then lo half HALF128 bytes later).  Per K-step and chunk: the resident hi
+// tile (shared memory) times both halves of B, then the lo tile times the hi
+// half -- from TMEM for chunks 0 and 1, from the ring slot for chunk 2.  Every
+// MMA accumulates (the epilogue filled TMEM with the bias).  `round` is the
+// ring round of this tile.  Returns false on a ring timeout.
+constexpr uint32_t HALF128 = 2 * b_block(128);   // K = 128: two K-blocks
+__device__ __forceinline__ bool issue_gemm2(uint32_t tmem, const unsigned char* w2h, const unsigned char* ring,
+                                            const unsigned char* Hs, uint64_t* full, uint32_t round) {
+    constexpr uint32_t idesc = idesc_f16(128);
+    constexpr uint64_t DA = A_TILE >> 4, DH = HALF128 >> 4;
+    const uint64_t a_hi = sdesc(smem_u32(w2h), A_LBO, A_SBO);
+    const uint64_t a_lo = sdesc(smem_u32(ring), A_LBO, A_SBO);
+    const uint64_t b0 = sdesc_b(smem_u32(Hs));
+#pragma unroll 1
+    for (int s = 0; s < 8; ++s) {
+        const uint64_t bh = b0 + (uint64_t)(b_kstep_off(128, s) >> 4);
+        const uint64_t ah = a_hi + (uint64_t)s * DA;
+#pragma unroll
+        for (int g = 0; g < 2; ++g) {
+            const uint32_t d = tmem + TM_F + 128 * g;
+            mma_f16(d, ah + (uint64_t)(8 * g) * DA, bh, idesc, 1);
+            mma_f16(d, ah + (uint64_t)(8 * g) * DA, bh + DH, idesc, 1);
+            mma_f16_ts(d, tmem + TM_W2LO + 64 * g + 8 * s, bh, idesc, 1);
+        }
+        const uint32_t d2 = tmem + TM_F + 256;
+        mma_f16(d2, ah + 16 * DA, bh, idesc, 1);
+        mma_f16(d2, ah + 16 * DA, bh + DH, idesc, 1);
+        if (!mbar_wait(&full[s], round & 1, WAIT_BUDGET)) return false;
+        mma_f16(d2, a_lo + (uint64_t)s * DA, bh, idesc, 1);
+    }
+    return true;
+}
+
+// Receivers in [j0, j1) without edges get a zero row (the epilogues store
+// one value per receiver that has edges).
+__device__ __forceinline__ void zero_empty_rows(float* out, const int32_t* row_ptr, int j0, int j1, int w, int lane) {
+    for (int j = j0 + w; j < j1; j += NT / 32)
+        if (row_ptr[j] == row_ptr[j + 1])
+            for (int k = lane; k < 4 * H; k += 32) out[(int64_t)j * 4 * H + k] = 0.0f;
+}
+
 // ------------------------------------------------------- forward kernel
 constexpr int FN = 128;                                   // edges per tile
-constexpr uint32_t F_EH = 2 * b_kstep(FN);                // E tile, one half (2 K-steps)
-constexpr uint32_t F_HH = 8 * b_kstep(FN);                // H tile, one half (8 K-steps)
+constexpr uint32_t F_EH = b_block(FN);                    // E tile, one half (K = 32 in one K-block)
+constexpr uint32_t F_HH = 2 * b_block(FN);                // H tile, one half (K = 128)
+static_assert(F_HH == HALF128, "GEMM2 B layout");
 constexpr uint32_t F_OFF_W1 = 0;
 constexpr uint32_t F_OFF_W2H = F_OFF_W1 + W1_BYTES;
 constexpr uint32_t F_OFF_H = align1k(F_OFF_W2H + W2_HALF);     // H tile; the E tile shares its start
@@ -264,7 +335,7 @@ constexpr uint32_t F_OFF_SOFF = F_OFF_CG + 2 * RMAX * 4;
 constexpr uint32_t F_OFF_UC = F_OFF_SOFF + FN * 4;
 constexpr uint32_t F_OFF_CHG = F_OFF_UC + 3 * FN * 4;
 constexpr uint32_t F_OFF_BAR = F_OFF_CHG + (FN / 32) * 4 + 16;
-constexpr uint32_t F_OFF_MISC = F_OFF_BAR + 8 * (2 + 2 * NSLOT);
+constexpr uint32_t F_OFF_MISC = F_OFF_BAR + 8 * (2 + NSLOT);
 constexpr uint32_t F_SMEM = align1k(F_OFF_MISC + 16);
 static_assert(2 * F_EH <= 2 * F_HH, "E tile fits in the H tile's space");
 static_assert(F_SMEM <= 232448, "forward kernel shared memory");
@@ -294,7 +365,6 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
     uint64_t* mma_bar = reinterpret_cast<uint64_t*>(smem + F_OFF_BAR);
     uint64_t* w2h_bar = mma_bar + 1;
     uint64_t* full = mma_bar + 2;
-    uint64_t* empty = full + NSLOT;
     uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + F_OFF_MISC);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + F_OFF_MISC + 4);
     uint32_t* ccount_s = reinterpret_cast<uint32_t*>(smem + F_OFF_MISC + 8);
@@ -309,10 +379,7 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
     if (t == 0) {
         mbar_init(mma_bar, 1);
         mbar_init(w2h_bar, 1);
-        for (int i = 0; i < NSLOT; ++i) {
-            mbar_init(&full[i], 1);
-            mbar_init(&empty[i], 1);
-        }
+        for (int i = 0; i < NSLOT; ++i) mbar_init(&full[i], 1);
         fence_mbar_init();
         *abort_flag = 0;
         *ccount_s = 0;
@@ -330,29 +397,35 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
     __syncthreads();
     fence_after_sync();
     const uint32_t tmem = *tslot;
-    const uint32_t idesc = idesc_f16(FN);
 
     uint32_t mma_phase = 0;
-    uint32_t pcount = 0, ccount = 0;   // ring fills (thread 32) / uses (thread 0)
+    uint32_t pcount = 0, ccount = 0;   // ring fills (thread 32) / uses (thread 0), NSLOT per edge tile
     uint32_t tiles = 0;
     bool w2h_ready = false;
     if (t == 32) {
         load_w2_hi(w2h, w2g, w2h_bar);
-        for (int i = 0; i < NSLOT; ++i) produce_lo(pcount++, ring, w2lo, full, empty);
+        fill_lo_ring(ring, w2lo, full);
+        pcount += NSLOT;
     }
 
     const int q = w & 3, r = w >> 2;
     const int c = 32 * q + lane;
     const int fidx = r * H + c;                      // this thread's feature element in a [4][H] row
     const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
+    load_w2_lo_tmem(lane_base, a.P + a.lo.w2, r, c);
+    tmem_st_wait();
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
 
     bool aborted = false;
     for (int p = blockIdx.x; p < a.nparts && !aborted; p += gridDim.x) {
         const int j0 = a.part[p], j1 = a.part[p + 1];
         if (j0 >= j1) continue;
         const int e0 = a.row_ptr[j0], e1 = a.row_ptr[j1];
+        zero_empty_rows(a.Xt, a.row_ptr, j0, j1, w, lane);
         int cur = j0;
-        float acc = 0.f;
+        float acc = 0.f, accu = 0.f;   // x * phi and u * phi_v2 parts of the current receiver's sum
         for (int t0 = e0; t0 < e1; t0 += FN) {
             const int n = min(FN, e1 - t0);
             if (t < FN) load_edge(a, t0, t, n, us, src_s, rcv_s);
@@ -370,14 +443,15 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
             __syncthreads();
             if (t == 0) {   // GEMM1: z^T = W1 e^T
                 fence_after_sync();
+                constexpr uint32_t idesc = idesc_f16(FN);
 #pragma unroll
                 for (int s = 0; s < 2; ++s)
 #pragma unroll
                     for (int pr = 0; pr < 3; ++pr) {
                         const uint32_t ahl = pr == 2 ? 1 : 0, bhl = pr == 1 ? 1 : 0;
                         const uint64_t ad = sdesc(smem_u32(w1s + s * SLAB + ahl * A_TILE), A_LBO, A_SBO);
-                        const uint64_t bd = sdesc(smem_u32(Es + bhl * F_EH + s * b_kstep(FN)), b_lbo(FN), 128);
-                        mma_f16(tmem, ad, bd, idesc, (s | pr) != 0);
+                        const uint64_t bd = sdesc_b(smem_u32(Es + bhl * F_EH + b_kstep_off(FN, s)));
+                        mma_f16(tmem + TM_Z, ad, bd, idesc, (s | pr) != 0);
                     }
                 mma_commit(mma_bar);
             }
@@ -393,13 +467,27 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                 const int k = c, col = 32 * r;
                 const float bias = b1s[k];
                 float z[32];
-                tmem_ld32(lane_base + col, z);
+                tmem_ld32(lane_base + TM_Z + col, z);
                 tmem_ld_wait();
 #pragma unroll
                 for (int i = 0; i < 32; i += 2) {
                     const float z0 = z[i] + bias, z1 = z[i + 1] + bias;
                     store_col_pair(Hs, F_HH, FN, col + i, k, z0 * fast_sigmoid(z0), z1 * fast_sigmoid(z1));
                 }
+                // GEMM2 accumulates onto b2[g * 128 + channel]: this warp refills
+                // the 32 chunk-2 cells it has just read, and 64 columns of
+                // chunks 0 and 1 (warps r = 0, 1: chunk 0; r = 2, 3: chunk 1)
+                float bv[16];
+                const float b2c = b2s[2 * H + c], b01 = b2s[(r >> 1) * H + c];
+#pragma unroll
+                for (int i = 0; i < 16; ++i) bv[i] = b2c;
+                tmem_st16(lane_base + TM_Z + col, bv);
+                tmem_st16(lane_base + TM_Z + col + 16, bv);
+#pragma unroll
+                for (int i = 0; i < 16; ++i) bv[i] = b01;
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk) tmem_st16(lane_base + TM_F + 64 * r + 16 * kk, bv);
+                tmem_st_wait();
             }
             fence_async_smem();
             fence_before_sync();
@@ -410,42 +498,12 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                     if (!mbar_wait(w2h_bar, 0, WAIT_BUDGET)) signal_timeout(a, abort_flag, 6);
                     w2h_ready = true;
                 }
-                // resident hi tiles: W2hi h_hi + W2hi h_lo
-#pragma unroll 1
-                for (int qq = 0; qq < W2_TILES; ++qq) {
-                    const int g = qq / 8, s = qq % 8;
-                    const uint64_t ad = sdesc(smem_u32(w2h + qq * A_TILE), A_LBO, A_SBO);
-                    const uint32_t d = tmem + 128 + 128 * g;
-                    mma_f16(d, ad, sdesc(smem_u32(Hs + s * b_kstep(FN)), b_lbo(FN), 128), idesc, s != 0);
-                    mma_f16(d, ad, sdesc(smem_u32(Hs + F_HH + s * b_kstep(FN)), b_lbo(FN), 128), idesc, 1);
-                }
-                // streamed lo tiles: W2lo h_hi
-                for (int qq = 0; qq < W2_TILES; ++qq) {
-                    const uint32_t slot = ccount % NSLOT;
-                    if (!mbar_wait(&full[slot], (ccount / NSLOT) & 1, WAIT_BUDGET)) {
-                        signal_timeout(a, abort_flag, 2);
-                        break;
-                    }
-                    const int g = qq / 8, s = qq % 8;
-                    mma_f16(tmem + 128 + 128 * g, sdesc(smem_u32(ring + slot * A_TILE), A_LBO, A_SBO),
-                            sdesc(smem_u32(Hs + s * b_kstep(FN)), b_lbo(FN), 128), idesc, 1);
-                    mma_commit(&empty[slot]);
-                    ++ccount;
-                }
+                if (issue_gemm2(tmem, w2h, ring, Hs, full, tiles)) ccount += NSLOT;
+                else signal_timeout(a, abort_flag, 2);
                 mma_commit(mma_bar);
                 *ccount_s = ccount;
             }
-            if (t == 32) {
-                const uint32_t target = (uint32_t)W2_TILES * (tiles + 1);
-                while (pcount < target) {
-                    if (!produce_lo(pcount, ring, w2lo, full, empty)) {
-                        signal_timeout(a, abort_flag, 3);
-                        break;
-                    }
-                    ++pcount;
-                }
-            }
-            if (w < 2) __syncwarp();   // lanes 1-31 of the issuing / producing warps wait here, not in a spin loop
+            if (w == 0) __syncwarp();   // lanes 1-31 of the issuing warp wait here, not in a spin loop
             // only warp 0 polls the MMA barrier; the others wait at the CTA
             // barrier instead of spinning on shared memory the MMAs read from
             if (w == 0 && !mbar_wait(mma_bar, mma_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 4);
@@ -455,39 +513,57 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
             fence_after_sync();
             ++tiles;
             if (t == 32 && !*abort_flag) {
-                // the ring is idle: prefetch the first lo tiles of the next tile
-                const uint32_t target = (uint32_t)W2_TILES * tiles + NSLOT;
-                while (pcount < target && produce_lo(pcount, ring, w2lo, full, empty)) ++pcount;
+                // this tile's MMAs are done, so the ring is free: fetch the next tile's lo tiles
+                fill_lo_ring(ring, w2lo, full);
+                pcount += NSLOT;
             }
             if (w == 1) __syncwarp();
             {   // epilogue 2: component r of the message sums, segmented by receiver;
-                // 16-edge blocks, the next block's gathers in flight
-                const float bias1 = r == 0 ? b2s[c] : b2s[H + c], bias2 = b2s[2 * H + c];
+                // 16-edge blocks, the next block's gathers in flight.  Padding
+                // edges gather 0 (and have u = 0), so they add nothing.
                 const float* ur = uc + (r == 0 ? 0 : (r - 1) * FN);
                 const uint32_t f1col = r == 0 ? 128 : 256;
+                float* out = a.Xt + fidx;
                 float xa[16], xn[16];
                 auto gather16 = [&](float (&x)[16], int col) {
 #pragma unroll
-                    for (int i = 0; i < 16; ++i) x[i] = __ldg(a.X + soff[col + i] + fidx);
+                    for (int i = 0; i < 16; i += 4) {
+                        const int4 so = *reinterpret_cast<const int4*>(soff + col + i);
+                        x[i] = col + i < n ? __ldg(a.X + so.x + fidx) : 0.f;
+                        x[i + 1] = col + i + 1 < n ? __ldg(a.X + so.y + fidx) : 0.f;
+                        x[i + 2] = col + i + 2 < n ? __ldg(a.X + so.z + fidx) : 0.f;
+                        x[i + 3] = col + i + 3 < n ? __ldg(a.X + so.w + fidx) : 0.f;
+                    }
                 };
                 auto process16 = [&](const float (&x)[16], int col) {
                     float f1[16], f2[16];
                     tmem_ld16(lane_base + f1col + col, f1);
                     if (r != 0) tmem_ld16(lane_base + 384 + col, f2);
+                    const uint32_t mask = (chg[col >> 5] >> (col & 31)) & 0xFFFFu;
                     tmem_ld_wait();
-                    const uint32_t mask = chg[col >> 5] >> (col & 31);
-                    const int m = min(16, n - col);
+                    const float* u = ur + col;
+                    if (mask == 0) {
+                        if (r == 0) {
 #pragma unroll
-                    for (int i = 0; i < 16; ++i) {
-                        if (i < m) {
-                            if (mask & (1u << i)) {
-                                const int ra = rcv_s[col + i];
-                                flush_sum(a.Xt, fidx, cur, ra, acc);
-                                cur = ra;
-                                acc = 0.f;
+                            for (int i = 0; i < 16; ++i) acc = fmaf(x[i], f1[i], acc);
+                        } else {
+#pragma unroll
+                            for (int i = 0; i < 16; ++i) {
+                                acc = fmaf(x[i], f1[i], acc);
+                                accu = fmaf(u[i], f2[i], accu);
                             }
-                            if (r == 0) acc = fmaf(x[i], f1[i] + bias1, acc);
-                            else acc = fmaf(x[i], f1[i] + bias1, fmaf(ur[col + i], f2[i] + bias2, acc));
+                        }
+                    } else {   // a receiver changes in this block: flush its finished sum
+#pragma unroll
+                        for (int i = 0; i < 16; ++i) {
+                            if (mask & (1u << i)) {
+                                out[(int64_t)cur * 4 * H] = acc + accu;
+                                cur = rcv_s[col + i];
+                                acc = 0.f;
+                                accu = 0.f;
+                            }
+                            acc = fmaf(x[i], f1[i], acc);
+                            if (r != 0) accu = fmaf(u[i], f2[i], accu);
                         }
                     }
                 };
@@ -507,7 +583,7 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                 break;
             }
         }
-        if (!aborted) flush_sum(a.Xt, fidx, cur, j1, acc);
+        if (!aborted) a.Xt[(int64_t)cur * 4 * H + fidx] = acc + accu;
     }
     // drain: the resident-tile load and every ring fill issued must have
     // landed before the CTA exits
@@ -528,13 +604,18 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
 }
 
 // ------------------------------------------------------- reverse kernel
+// 64-edge tiles; E and E' (and then H and H') are stacked as rows 0-63 and
+// 64-127 of one 128-row B tile, so every MMA is N = 128: TMEM columns
+// [0,64) z^T, [64,128) z'^T, and per chunk g at 128 + 128 g: [0,64) f^T,
+// [64,128) f'^T.
 constexpr int BN = 64;
-constexpr uint32_t B_EH = 2 * b_kstep(BN);
-constexpr uint32_t B_HH = 8 * b_kstep(BN);
+constexpr uint32_t B_EH = b_block(2 * BN);
+constexpr uint32_t B_HH = 2 * b_block(2 * BN);
+static_assert(B_HH == HALF128, "GEMM2 B layout");
 constexpr uint32_t B_OFF_W1 = 0;
 constexpr uint32_t B_OFF_W2H = B_OFF_W1 + W1_BYTES;
-constexpr uint32_t B_OFF_H = align1k(B_OFF_W2H + W2_HALF);     // H then H'; E, E' share the start
-constexpr uint32_t B_OFF_RING = align1k(B_OFF_H + 4 * B_HH);
+constexpr uint32_t B_OFF_H = align1k(B_OFF_W2H + W2_HALF);     // [H; H'] tile; the [E; E'] tile shares its start
+constexpr uint32_t B_OFF_RING = align1k(B_OFF_H + 2 * B_HH);
 constexpr uint32_t B_OFF_US = B_OFF_RING + NSLOT * A_TILE;
 constexpr uint32_t B_OFF_SRC = B_OFF_US + BN * 16;
 constexpr uint32_t B_OFF_RCV = B_OFF_SRC + BN * 4;
@@ -543,12 +624,13 @@ constexpr uint32_t B_OFF_B2 = B_OFF_B1 + H * 4;
 constexpr uint32_t B_OFF_CG = B_OFF_B2 + H3 * 4;
 constexpr uint32_t B_OFF_SOFF = B_OFF_CG + 2 * RMAX * 4;
 constexpr uint32_t B_OFF_ROFF = B_OFF_SOFF + BN * 4;
-constexpr uint32_t B_OFF_CHG = B_OFF_ROFF + BN * 4;
+constexpr uint32_t B_OFF_UC = B_OFF_ROFF + BN * 4;
+constexpr uint32_t B_OFF_CHG = B_OFF_UC + 3 * BN * 4;
 constexpr uint32_t B_OFF_RED = B_OFF_CHG + (BN / 32) * 4 + 16;
 constexpr uint32_t B_OFF_BAR = B_OFF_RED + 16 * BN * 2 * 4;
-constexpr uint32_t B_OFF_MISC = B_OFF_BAR + 8 * (2 + 2 * NSLOT);
+constexpr uint32_t B_OFF_MISC = B_OFF_BAR + 8 * (2 + NSLOT);
 constexpr uint32_t B_SMEM = align1k(B_OFF_MISC + 16);
-static_assert(4 * B_EH <= 4 * B_HH, "E tiles fit in the H tiles' space");
+static_assert(2 * B_EH <= 2 * B_HH, "E tile fits in the H tile's space");
 static_assert(B_SMEM <= 232448, "reverse kernel shared memory");
 
 __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const unsigned char* __restrict__ w1g,
@@ -556,8 +638,8 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* w1s = smem + B_OFF_W1;
     unsigned char* w2h = smem + B_OFF_W2H;
-    unsigned char* Hs = smem + B_OFF_H;            // [H hi, H lo, H' hi, H' lo]
-    unsigned char* Es = smem + B_OFF_H;            // [E hi, E lo, E' hi, E' lo], before H is written
+    unsigned char* Hs = smem + B_OFF_H;            // [H; H'] hi, then lo
+    unsigned char* Es = smem + B_OFF_H;            // [E; E'] hi, then lo, before H is written
     unsigned char* ring = smem + B_OFF_RING;
     float4* us = reinterpret_cast<float4*>(smem + B_OFF_US);
     int* src_s = reinterpret_cast<int*>(smem + B_OFF_SRC);
@@ -569,12 +651,12 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
     float* red = reinterpret_cast<float*>(smem + B_OFF_RED);   // [16 warps][BN][2]
     int* soff = reinterpret_cast<int*>(smem + B_OFF_SOFF);
     int* roff = reinterpret_cast<int*>(smem + B_OFF_ROFF);
+    float* uc = reinterpret_cast<float*>(smem + B_OFF_UC);
     uint32_t* chg = reinterpret_cast<uint32_t*>(smem + B_OFF_CHG);
     int* prev_s = reinterpret_cast<int*>(smem + B_OFF_CHG + (BN / 32) * 4);
     uint64_t* mma_bar = reinterpret_cast<uint64_t*>(smem + B_OFF_BAR);
     uint64_t* w2h_bar = mma_bar + 1;
     uint64_t* full = mma_bar + 2;
-    uint64_t* empty = full + NSLOT;
     uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + B_OFF_MISC);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + B_OFF_MISC + 4);
     uint32_t* ccount_s = reinterpret_cast<uint32_t*>(smem + B_OFF_MISC + 8);
@@ -589,10 +671,7 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
     if (t == 0) {
         mbar_init(mma_bar, 1);
         mbar_init(w2h_bar, 1);
-        for (int i = 0; i < NSLOT; ++i) {
-            mbar_init(&full[i], 1);
-            mbar_init(&empty[i], 1);
-        }
+        for (int i = 0; i < NSLOT; ++i) mbar_init(&full[i], 1);
         fence_mbar_init();
         *abort_flag = 0;
         *ccount_s = 0;
@@ -610,20 +689,25 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
     __syncthreads();
     fence_after_sync();
     const uint32_t tmem = *tslot;
-    const uint32_t idesc = idesc_f16(BN);
 
     uint32_t mma_phase = 0;
-    uint32_t pcount = 0, ccount = 0;
+    uint32_t pcount = 0, ccount = 0;   // ring fills (thread 32) / uses (thread 0), NSLOT per edge tile
     uint32_t tiles = 0;
     bool w2h_ready = false;
     if (t == 32) {
         load_w2_hi(w2h, w2g, w2h_bar);
-        for (int i = 0; i < NSLOT; ++i) produce_lo(pcount++, ring, w2lo, full, empty);
+        fill_lo_ring(ring, w2lo, full);
+        pcount += NSLOT;
     }
     const int q = w & 3, r = w >> 2;
     const int c = 32 * q + lane;
     const int fidx = r * H + c;
     const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
+    load_w2_lo_tmem(lane_base, a.P + a.lo.w2, r, c);
+    tmem_st_wait();
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
     const int rs_idx = reduce_scatter8_index(lane);
 
     bool aborted = false;
@@ -631,6 +715,7 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
         const int j0 = a.part[p], j1 = a.part[p + 1];
         if (j0 >= j1) continue;
         const int e0 = a.row_ptr[j0], e1 = a.row_ptr[j1];
+        if (a.write_nodes) zero_empty_rows(a.xbar, a.row_ptr, j0, j1, w, lane);
         int cur = j0;
         float acc = 0.f;
         for (int t0 = e0; t0 < e1; t0 += BN) {
@@ -638,31 +723,29 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
             if (t < BN) load_edge(a, t0, t, n, us, src_s, rcv_s);
             if (t == BN) *prev_s = cur;   // receiver before this tile
             __syncthreads();
-            if (t < 4 * BN) {   // E (rbf * fc) and E' (its d-derivative) tiles
+            if (t < 4 * BN) {   // E (rbf * fc) rows 0-63 and E' (its d-derivative) rows 64-127
                 const int e = t & (BN - 1), s = (t >> 6) & 1, which = t >> 7;
                 float v[16];
                 if (which == 0) rbf16(us[e].w, e < n, 16 * s, a.R, cent, gam, a.cutoff, v);
                 else rbf16_d(us[e].w, e < n, 16 * s, a.R, cent, gam, a.cutoff, v);
-                store_row16(Es + which * 2 * B_EH, B_EH, BN, e, s, v);
+                store_row16(Es, B_EH, 2 * BN, which * BN + e, s, v);
             } else if (t < 5 * BN) {
-                tile_prep<BN>(t - 4 * BN, n, *prev_s, src_s, rcv_s, us, soff, roff, nullptr, chg);
+                tile_prep<BN>(t - 4 * BN, n, *prev_s, src_s, rcv_s, us, soff, roff, uc, chg);
             }
             fence_async_smem();
             __syncthreads();
-            if (t == 0) {   // z^T = W1 e^T, z'^T = W1 e'^T
+            if (t == 0) {   // [z; z']^T = W1 [e; e']^T
                 fence_after_sync();
+                constexpr uint32_t idesc = idesc_f16(2 * BN);
 #pragma unroll
-                for (int which = 0; which < 2; ++which)
+                for (int s = 0; s < 2; ++s)
 #pragma unroll
-                    for (int s = 0; s < 2; ++s)
-#pragma unroll
-                        for (int pr = 0; pr < 3; ++pr) {
-                            const uint32_t ahl = pr == 2 ? 1 : 0, bhl = pr == 1 ? 1 : 0;
-                            const uint64_t ad = sdesc(smem_u32(w1s + s * SLAB + ahl * A_TILE), A_LBO, A_SBO);
-                            const uint64_t bd = sdesc(smem_u32(Es + which * 2 * B_EH + bhl * B_EH + s * b_kstep(BN)),
-                                                      b_lbo(BN), 128);
-                            mma_f16(tmem + 64 * which, ad, bd, idesc, (s | pr) != 0);
-                        }
+                    for (int pr = 0; pr < 3; ++pr) {
+                        const uint32_t ahl = pr == 2 ? 1 : 0, bhl = pr == 1 ? 1 : 0;
+                        const uint64_t ad = sdesc(smem_u32(w1s + s * SLAB + ahl * A_TILE), A_LBO, A_SBO);
+                        const uint64_t bd = sdesc_b(smem_u32(Es + bhl * B_EH + b_kstep_off(2 * BN, s)));
+                        mma_f16(tmem + TM_Z, ad, bd, idesc, (s | pr) != 0);
+                    }
                 mma_commit(mma_bar);
             }
             if (w == 0) __syncwarp();
@@ -673,72 +756,56 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
             fence_before_sync();
             __syncthreads();
             fence_after_sync();
-            {   // epilogue 1: h = silu(z + b1), h' = silu'(z + b1) z', 16 edges per warp
+            {   // epilogue 1: h = silu(z + b1) (rows 0-63), h' = silu'(z + b1) z'
+                // (rows 64-127), 16 edges per warp
                 const int k = c, col = 16 * r;
                 const float bias = b1s[k];
                 float z[16], zd[16];
-                tmem_ld16(lane_base + col, z);
-                tmem_ld16(lane_base + 64 + col, zd);
+                tmem_ld16(lane_base + TM_Z + col, z);
+                tmem_ld16(lane_base + TM_Z + BN + col, zd);
                 tmem_ld_wait();
 #pragma unroll
                 for (int i = 0; i < 16; i += 2) {
                     const float z0 = z[i] + bias, z1 = z[i + 1] + bias;
                     const float s0 = fast_sigmoid(z0), s1 = fast_sigmoid(z1);
-                    store_col_pair(Hs, B_HH, BN, col + i, k, z0 * s0, z1 * s1);
-                    store_col_pair(Hs + 2 * B_HH, B_HH, BN, col + i, k, s0 * (1.0f + z0 * (1.0f - s0)) * zd[i],
+                    store_col_pair(Hs, B_HH, 2 * BN, col + i, k, z0 * s0, z1 * s1);
+                    store_col_pair(Hs, B_HH, 2 * BN, BN + col + i, k, s0 * (1.0f + z0 * (1.0f - s0)) * zd[i],
                                    s1 * (1.0f + z1 * (1.0f - s1)) * zd[i + 1]);
                 }
+                // f = W2 h accumulates onto b2 and f' = W2 h' onto 0 (each chunk:
+                // 64 columns f^T, then 64 columns f'^T).  This warp refills the
+                // chunk-2 cells it has just read (f then f'), and 64 columns of
+                // chunks 0 and 1: r = 0 chunk 0 f, 1 chunk 0 f', 2 chunk 1 f, 3 chunk 1 f'.
+                float bv[16];
+                const float b2c = b2s[2 * H + c];
+#pragma unroll
+                for (int i = 0; i < 16; ++i) bv[i] = b2c;
+                tmem_st16(lane_base + TM_Z + col, bv);
+#pragma unroll
+                for (int i = 0; i < 16; ++i) bv[i] = 0.0f;
+                tmem_st16(lane_base + TM_Z + BN + col, bv);
+                const float b01 = (r & 1) ? 0.0f : b2s[(r >> 1) * H + c];
+#pragma unroll
+                for (int i = 0; i < 16; ++i) bv[i] = b01;
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk) tmem_st16(lane_base + TM_F + 64 * r + 16 * kk, bv);
+                tmem_st_wait();
             }
             fence_async_smem();
             fence_before_sync();
             __syncthreads();
-            if (w == 0 && lane == 0) {   // f^T = W2 h^T and f'^T = W2 h'^T
+            if (w == 0 && lane == 0) {   // [f; f']^T = W2 [h; h']^T
                 fence_after_sync();
                 if (!w2h_ready) {
                     if (!mbar_wait(w2h_bar, 0, WAIT_BUDGET)) signal_timeout(a, abort_flag, 16);
                     w2h_ready = true;
                 }
-#pragma unroll 1
-                for (int qq = 0; qq < W2_TILES; ++qq) {
-                    const int g = qq / 8, s = qq % 8;
-                    const uint64_t ad = sdesc(smem_u32(w2h + qq * A_TILE), A_LBO, A_SBO);
-#pragma unroll
-                    for (int which = 0; which < 2; ++which) {
-                        const uint32_t d = tmem + 128 + 192 * which + 64 * g;
-                        unsigned char* hb = Hs + which * 2 * B_HH + s * b_kstep(BN);
-                        mma_f16(d, ad, sdesc(smem_u32(hb), b_lbo(BN), 128), idesc, s != 0);
-                        mma_f16(d, ad, sdesc(smem_u32(hb + B_HH), b_lbo(BN), 128), idesc, 1);
-                    }
-                }
-                for (int qq = 0; qq < W2_TILES; ++qq) {
-                    const uint32_t slot = ccount % NSLOT;
-                    if (!mbar_wait(&full[slot], (ccount / NSLOT) & 1, WAIT_BUDGET)) {
-                        signal_timeout(a, abort_flag, 12);
-                        break;
-                    }
-                    const int g = qq / 8, s = qq % 8;
-                    const uint64_t ad = sdesc(smem_u32(ring + slot * A_TILE), A_LBO, A_SBO);
-#pragma unroll
-                    for (int which = 0; which < 2; ++which)
-                        mma_f16(tmem + 128 + 192 * which + 64 * g, ad,
-                                sdesc(smem_u32(Hs + which * 2 * B_HH + s * b_kstep(BN)), b_lbo(BN), 128), idesc, 1);
-                    mma_commit(&empty[slot]);
-                    ++ccount;
-                }
+                if (issue_gemm2(tmem, w2h, ring, Hs, full, tiles)) ccount += NSLOT;
+                else signal_timeout(a, abort_flag, 12);
                 mma_commit(mma_bar);
                 *ccount_s = ccount;
             }
-            if (t == 32) {
-                const uint32_t target = (uint32_t)W2_TILES * (tiles + 1);
-                while (pcount < target) {
-                    if (!produce_lo(pcount, ring, w2lo, full, empty)) {
-                        signal_timeout(a, abort_flag, 13);
-                        break;
-                    }
-                    ++pcount;
-                }
-            }
-            if (w < 2) __syncwarp();   // lanes 1-31 of the issuing / producing warps wait here, not in a spin loop
+            if (w == 0) __syncwarp();   // lanes 1-31 of the issuing warp wait here, not in a spin loop
             // only warp 0 polls the MMA barrier; the others wait at the CTA
             // barrier instead of spinning on shared memory the MMAs read from
             if (w == 0 && !mbar_wait(mma_bar, mma_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 14);
@@ -748,59 +815,67 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
             fence_after_sync();
             ++tiles;
             if (t == 32 && !*abort_flag) {
-                const uint32_t target = (uint32_t)W2_TILES * tiles + NSLOT;
-                while (pcount < target && produce_lo(pcount, ring, w2lo, full, empty)) ++pcount;
+                fill_lo_ring(ring, w2lo, full);
+                pcount += NSLOT;
             }
             if (w == 1) __syncwarp();
             {   // epilogue 2: component r of the node adjoints (gathered from the
                 // sender side, summed per receiver) and this component's share
-                // of dE/dd, dE/du; 8-edge blocks, the next block's gathers in flight
-                const float bs = b2s[c], bv1 = b2s[H + c], bv2 = b2s[2 * H + c];
-                const float bias1 = r == 0 ? bs : bv1;
-                const uint32_t f1col = r == 0 ? 128 : 192, d1col = r == 0 ? 320 : 384;
+                // of dE/dd, dE/du; 8-edge blocks, the next block's gathers in
+                // flight.  Padding edges gather 0, so they add nothing.
+                const uint32_t f1col = r == 0 ? 128 : 256, d1col = f1col + BN;
+                const float* ur = uc + (r == 0 ? 0 : (r - 1) * BN);
+                float* out = a.xbar + fidx;
                 float tba[8], xba[8], tra[8], tbn[8], xbn[8], trn[8];
                 auto gather8 = [&](float (&tb)[8], float (&xb)[8], float (&tr)[8], int col) {
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) {
-                        const int so = soff[col + i] + fidx;
-                        tb[i] = __ldg(a.xtbar + so);
-                        xb[i] = __ldg(a.X + so);
-                        tr[i] = __ldg(a.xtbar + roff[col + i] + fidx);
+                    for (int i = 0; i < 8; i += 4) {
+                        const int4 so = *reinterpret_cast<const int4*>(soff + col + i);
+                        const int4 ro = *reinterpret_cast<const int4*>(roff + col + i);
+                        const int sv[4] = {so.x, so.y, so.z, so.w}, rv[4] = {ro.x, ro.y, ro.z, ro.w};
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) {
+                            const bool ok = col + i + k < n;
+                            tb[i + k] = ok ? __ldg(a.xtbar + sv[k] + fidx) : 0.f;
+                            xb[i + k] = ok ? __ldg(a.X + sv[k] + fidx) : 0.f;
+                            tr[i + k] = ok ? __ldg(a.xtbar + rv[k] + fidx) : 0.f;
+                        }
                     }
                 };
                 auto process8 = [&](const float (&tb)[8], const float (&xb)[8], const float (&tr)[8], int col) {
                     float f1[8], f2[8], d1[8], d2[8];
-                    tmem_ld8(lane_base + f1col + col, f1);   // phi_s or phi_v1
+                    tmem_ld8(lane_base + f1col + col, f1);   // phi_s or phi_v1 (bias included)
                     tmem_ld8(lane_base + d1col + col, d1);   // its d-derivative
                     if (r != 0) {
-                        tmem_ld8(lane_base + 256 + col, f2);  // phi_v2
-                        tmem_ld8(lane_base + 448 + col, d2);  // dphi_v2/dd
+                        tmem_ld8(lane_base + 384 + col, f2);       // phi_v2 (bias included)
+                        tmem_ld8(lane_base + 384 + BN + col, d2);  // dphi_v2/dd
                     }
+                    const uint32_t mask = (chg[col >> 5] >> (col & 31)) & 0xFFu;
                     tmem_ld_wait();
-                    const uint32_t mask = chg[col >> 5] >> (col & 31);
-                    const int m = min(8, n - col);
-                    float p0[8], p1[8];
+                    if (mask == 0) {
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) {
-                        p0[i] = 0.f;
-                        p1[i] = 0.f;
-                        if (i < m) {
+                        for (int i = 0; i < 8; ++i) acc = fmaf(tb[i], f1[i], acc);
+                    } else {   // a receiver changes in this block: flush its finished sum
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) {
                             if (mask & (1u << i)) {
-                                const int ra = rcv_s[col + i];
-                                if (a.write_nodes) flush_sum(a.xbar, fidx, cur, ra, acc);
-                                cur = ra;
+                                if (a.write_nodes) out[(int64_t)cur * 4 * H] = acc;
+                                cur = rcv_s[col + i];
                                 acc = 0.f;
                             }
-                            const float ta = tr[i];
-                            acc = fmaf(tb[i], f1[i] + bias1, acc);
-                            if (r == 0) {
-                                p0[i] = (ta * xb[i]) * d1[i];
-                            } else {
-                                const float4 u = us[col + i];
-                                const float ue = r == 1 ? u.x : (r == 2 ? u.y : u.z);
-                                p0[i] = ta * (xb[i] * d1[i] + ue * d2[i]);
-                                p1[i] = ta * (f2[i] + bv2);
-                            }
+                            acc = fmaf(tb[i], f1[i], acc);
+                        }
+                    }
+                    float p0[8], p1[8];
+                    if (r == 0) {
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) p0[i] = (tr[i] * xb[i]) * d1[i];
+                    } else {
+                        const float* u = ur + col;
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) {
+                            p0[i] = tr[i] * fmaf(xb[i], d1[i], u[i] * d2[i]);
+                            p1[i] = tr[i] * f2[i];
                         }
                     }
                     const float s0 = warp_reduce_scatter8(p0, lane);
@@ -844,7 +919,7 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                 break;
             }
         }
-        if (!aborted && a.write_nodes) flush_sum(a.xbar, fidx, cur, j1, acc);
+        if (!aborted && a.write_nodes) a.xbar[(int64_t)cur * 4 * H + fidx] = acc;
     }
     __syncthreads();
     if (t == 32) {
