@@ -160,9 +160,12 @@ int mlff_clear_status(void *workspace, mlff_stream_t stream);
  * pos/vel are float64 [N,3] (Angstrom, Angstrom per ASE time unit), forces
  * float32 [N,3] hold F(r) on entry and on exit, inv_mass float64 [N]
  * (1/amu).  energy receives the potential energy per structure after the
- * last step, kinetic (optional) the kinetic energy.  No host
- * synchronisation, so a fixed number of steps can be captured in a CUDA
- * graph once the edge capacity is known to suffice. */
+ * last step, kinetic (optional) the kinetic energy.  energy_trace and
+ * kinetic_trace (optional, [n_steps][n_mol]) receive both after every step
+ * -- the per-step record NVEMDHarness._collect_data keeps on the host
+ * (nve_harness.py:239-265).  No host synchronisation, so a fixed number of
+ * steps can be captured in a CUDA graph once the edge capacity is known to
+ * suffice. */
 typedef struct {
     double *pos;
     double *vel;
@@ -170,6 +173,8 @@ typedef struct {
     float *forces;
     double *energy;
     double *kinetic;
+    double *energy_trace;
+    double *kinetic_trace;
 } mlff_md_state;
 
 int mlff_verlet_steps(const mlff_dims *dims, const void *packed, const mlff_system *sys,

@@ -258,13 +258,27 @@ int mlff_verlet_steps(const mlff_dims* dims, const void* packed, const mlff_syst
     }
     s2.pos = ws_ptr<float>(workspace, L.md_pos32);
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    mlff_outputs out{state->energy, state->forces, nullptr, nullptr};
     MLFF_CUDA(cudaMemsetAsync(ws_ptr<Status>(workspace, L.status), 0, sizeof(Status), st));
+    const int64_t B = sys->n_mol;
     int r;
     for (int s = 0; s < n_steps; ++s) {
+        const bool last = s == n_steps - 1;
+        mlff_outputs out{state->energy_trace && !last ? state->energy_trace + s * B : state->energy, state->forces,
+                         nullptr, nullptr};
+        mlff_md_state ks = *state;
+        if (state->kinetic_trace) ks.kinetic = state->kinetic_trace + s * B;
         if ((r = md_kick_drift(L, workspace, state, dt, st))) return r;
         if ((r = energy_forces_impl(*dims, packed, s2, L, path, out, workspace, st))) return r;
-        if ((r = md_kick(L, workspace, state, dt, sys->mol_ptr, sys->n_mol, s == n_steps - 1, st))) return r;
+        if ((r = md_kick(L, workspace, &ks, dt, sys->mol_ptr, sys->n_mol, last || state->kinetic_trace, st)))
+            return r;
+        if (last) {
+            if (state->energy_trace)
+                MLFF_CUDA(cudaMemcpyAsync(state->energy_trace + s * B, state->energy, sizeof(double) * B,
+                                          cudaMemcpyDeviceToDevice, st));
+            if (state->kinetic_trace && state->kinetic)
+                MLFF_CUDA(cudaMemcpyAsync(state->kinetic, state->kinetic_trace + s * B, sizeof(double) * B,
+                                          cudaMemcpyDeviceToDevice, st));
+        }
     }
     return MLFF_OK;
 }

@@ -74,7 +74,7 @@ class Outputs(ctypes.Structure):
 
 class MDState(ctypes.Structure):
     _fields_ = [("pos", _P), ("vel", _P), ("inv_mass", _P), ("forces", _P), ("energy", _P),
-                ("kinetic", _P)]
+                ("kinetic", _P), ("energy_trace", _P), ("kinetic_trace", _P)]
 
 
 class MLFFError(RuntimeError):

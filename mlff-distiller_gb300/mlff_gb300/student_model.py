@@ -25,7 +25,7 @@ import logging
 import math
 import warnings
 from pathlib import Path
-from typing import Optional, Tuple, Union
+from typing import Dict, Optional, Tuple, Union
 
 import numpy as np
 import torch
@@ -296,12 +296,19 @@ class StudentForceField(nn.Module):
         from state_dict shapes (student_model.py:1101-1176).  A trainer
         checkpoint's ``model.`` key prefix is stripped."""
         ckpt = torch.load(path, map_location="cpu", weights_only=False)
-        config = dict(ckpt.get("config", {}))
+        return cls.from_state_dict(ckpt["model_state_dict"], config=ckpt.get("config", {}), **kwargs).to(device)
+
+    @classmethod
+    def from_state_dict(cls, sd: Dict[str, torch.Tensor], config: Optional[dict] = None, **kwargs):
+        """Model from a reference-layout state_dict (checkpoint, trainer
+        checkpoint with ``model.`` keys, or a TorchScript archive's
+        state_dict), config entries missing from ``config`` inferred from the
+        tensor shapes."""
+        config = dict(config or {})
         config.setdefault("use_torch_cluster", True)
         keep = {"hidden_dim", "num_interactions", "num_rbf", "cutoff", "max_z", "learnable_rbf",
                 "use_torch_cluster"}
         cfg = {k: v for k, v in config.items() if k in keep}
-        sd = ckpt["model_state_dict"]
         if any(k.startswith("model.") for k in sd):
             sd = {k[len("model."):] if k.startswith("model.") else k: v for k, v in sd.items()}
         if "hidden_dim" not in cfg and "embedding.weight" in sd:
@@ -318,7 +325,7 @@ class StudentForceField(nn.Module):
         cfg.update(kwargs)
         model = cls(**cfg)
         model.load_state_dict(sd)
-        return model.to(device)
+        return model
 
 
 __all__ = ["StudentForceField", "PaiNNInteraction", "PaiNNMessage", "PaiNNUpdate", "GaussianRBF",

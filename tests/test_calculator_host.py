@@ -1,0 +1,148 @@
+"""Host-side behaviour of the drop-in ASE calculator and the MD helpers
+(no GPU): the reference's error contract (ase_calculator.py:240-244,
+405-412, 414-459), the Atoms stand-in's caching, and the initial-velocity
+recipe of nve_harness.py:141-170."""
+import numpy as np
+import pytest
+import torch
+
+from mlff_gb300 import md, units
+from mlff_gb300.ase_calculator import StudentForceFieldCalculator
+from mlff_gb300.ase_compat import Atoms
+from mlff_gb300.student_model import StudentForceField
+
+
+@pytest.fixture()
+def ckpt(tmp_path):
+    torch.manual_seed(0)
+    m = StudentForceField()
+    p = tmp_path / "model.pt"
+    m.save(p)
+    return p
+
+
+def test_missing_checkpoint():
+    with pytest.raises(FileNotFoundError):
+        StudentForceFieldCalculator("/nonexistent/model.pt", device="cpu")
+
+
+def test_jit_without_path(ckpt):
+    with pytest.raises(ValueError):
+        StudentForceFieldCalculator(ckpt, device="cpu", use_jit=True)
+
+
+def test_properties(ckpt):
+    c = StudentForceFieldCalculator(ckpt, device="cpu")
+    assert c.implemented_properties == ["energy", "forces"]
+    c = StudentForceFieldCalculator(ckpt, device="cpu", enable_stress=True)
+    assert c.implemented_properties == ["energy", "forces", "stress"]
+    assert c.model.num_parameters() == 429596
+
+
+@pytest.mark.parametrize("bad", ["empty", "z0", "z119", "nan"])
+def test_invalid_input_raises_value_error(ckpt, bad):
+    c = StudentForceFieldCalculator(ckpt, device="cpu")
+    pos = np.zeros((3, 3)) + np.arange(3)[:, None]
+    z = np.array([1, 6, 8])
+    if bad == "empty":
+        pos, z = np.zeros((0, 3)), np.zeros(0, dtype=np.int64)
+    elif bad == "z0":
+        z = np.array([0, 6, 8])
+    elif bad == "z119":
+        z = np.array([119, 6, 8])
+    else:
+        pos[1, 2] = np.nan
+    atoms = Atoms(numbers=z, positions=pos)
+    atoms.calc = c
+    with pytest.raises(ValueError):
+        atoms.get_potential_energy()
+
+
+def test_compute_without_cuda_is_runtime_error(ckpt):
+    """Anything but invalid input surfaces as RuntimeError (ase_calculator.py:
+    408-412); on a machine without a GPU that is the missing CUDA device --
+    there is no CPU fallback."""
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    c = StudentForceFieldCalculator(ckpt, device="cpu")
+    atoms = Atoms(numbers=[1, 8, 1], positions=[[0, 0, 0], [0.96, 0, 0], [1.2, 0.9, 0]])
+    atoms.calc = c
+    with pytest.raises(RuntimeError):
+        atoms.get_forces()
+
+
+def test_atoms_standin_caching():
+    from mlff_gb300.ase_compat import Calculator, HAVE_ASE
+    if HAVE_ASE:
+        pytest.skip("real ASE in use")
+
+    class Counting(Calculator):
+        implemented_properties = ["energy", "forces"]
+
+        def __init__(self):
+            super().__init__()
+            self.calls = 0
+
+        def calculate(self, atoms=None, properties=("energy",), system_changes=()):
+            Calculator.calculate(self, atoms, properties, system_changes)
+            self.calls += 1
+            self.results = {"energy": float(atoms.positions.sum()), "forces": -atoms.positions.copy()}
+
+    a = Atoms(numbers=[1, 1], positions=[[0, 0, 0], [0.7, 0, 0]])
+    a.calc = Counting()
+    e1 = a.get_potential_energy()
+    a.get_forces()
+    assert a.calc.calls == 1
+    a.set_positions(a.get_positions() + 0.1)
+    assert a.get_potential_energy() != e1
+    assert a.calc.calls == 2
+
+
+def test_units():
+    # 1 fs in Angstrom * sqrt(amu / eV) units
+    assert abs(units.fs - 0.09822694788464063) < 1e-9
+    assert units.ATOMIC_MASSES[1] == 1.008 and units.ATOMIC_MASSES[8] == 15.999
+
+
+def test_initial_velocities():
+    rng = np.random.default_rng(0)
+    n, B = 64, 32
+    ptr = np.arange(B + 1) * n
+    pos = rng.normal(size=(n * B, 3)) * 3.0
+    m = units.masses_of(rng.choice([1, 6, 7, 8], size=n * B))
+    v = md.maxwell_boltzmann(m, 300.0, rng)
+    # equipartition: <m v^2> = 3 kB T per atom, within sampling error
+    t = (m[:, None] * v * v).sum() / (3 * len(m) * units.kB)
+    assert abs(t - 300.0) < 15.0
+    v = md.stationary(v, m, ptr)
+    v = md.zero_rotation(pos, v, m, ptr)
+    for b in range(B):
+        s = slice(ptr[b], ptr[b + 1])
+        p = (m[s, None] * v[s]).sum(0)
+        r = pos[s] - (m[s, None] * pos[s]).sum(0) / m[s].sum()
+        L = (m[s, None] * np.cross(r, v[s])).sum(0)
+        assert np.abs(p).max() < 1e-10
+        assert np.abs(L).max() < 1e-8
+
+
+def test_oracle_verlet_harmonic():
+    """The restated integrator on a harmonic oscillator: second order in dt,
+    energy bounded."""
+    from oracle.md import velocity_verlet
+    k, m0 = 2.0, 3.0
+
+    def f(r):
+        return np.array([0.5 * k * (r * r).sum()]), -k * r
+
+    r0, v0 = np.array([[1.0, 0, 0]]), np.array([[0.0, 0.5, 0]])
+    w = np.sqrt(k / m0)
+    errs = []
+    for dt in (0.02, 0.01):
+        n = int(round(2.0 / dt))
+        r, v, F, ep, ek = velocity_verlet(r0, v0, [m0], f, dt, n, np.array([0, 1]))
+        t = n * dt
+        exact = np.array([np.cos(w * t), 0.5 / w * np.sin(w * t), 0])
+        errs.append(np.abs(r[0] - exact).max())
+        e = ep[:, 0] + ek[:, 0]
+        assert np.ptp(e) < 1e-3
+    assert 3.5 < errs[0] / errs[1] < 4.5
