@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--md-steps", type=int, default=0,
+                    help="MD workloads: further untimed steps for the energy drift (20000 = 10 ps)")
     return ap.parse_args()
 
 
@@ -197,6 +199,84 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+MD_BLOCK = 50   # MD steps per CUDA-graph replay
+
+
+def run_md(args, world, rank, local):
+    """MD replicas: velocity-Verlet NVE at 0.5 fs from Maxwell-Boltzmann
+    velocities at 300 K, whole blocks of steps replayed from one CUDA graph.
+    A bench step is one replay of MD_BLOCK steps of every replica."""
+    from mlff_gb300 import _lib, systems
+    from mlff_gb300.md import VelocityVerletGPU, kinetic_energy, replica_drift
+    sysm = systems.workload(args.workload)
+    model = seed_model(args.path).cuda().eval()
+    drv = VelocityVerletGPU(model, sysm.Z, sysm.pos, sysm.mol_ptr, timestep_fs=0.5)
+    drv.initialize_velocities(300.0, seed=rank)
+    E0, _ = drv.compute_forces()
+    K0 = kinetic_energy(drv.velocities(), drv.masses, sysm.mol_ptr)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    for _ in range(max(3, args.warmup)):
+        drv.run(MD_BLOCK, graph=True, block=MD_BLOCK, record=False)
+    g = drv._graph(MD_BLOCK, drv._capacity(), False)["graph"]
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        starts[i].record()
+        g.replay()
+        ends[i].record()
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    code, _, _ = drv.engine.status()
+    if code != _lib.OK:
+        raise RuntimeError(f"device status {code} during the timed MD region")
+    blk_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    total_s = sum(blk_ms) / 1000.0
+    if world > 1:
+        t = torch.tensor([total_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_s = float(t.item())
+    n_md = args.steps * MD_BLOCK
+    value = sysm.n_atoms * world * n_md / total_s
+    # energy drift over --md-steps further steps (not timed)
+    drift = None
+    if args.md_steps > 0:
+        # restart from the timed trajectory's end: E0 at the current state
+        E0, _ = drv.compute_forces()
+        K0 = kinetic_energy(drv.velocities(), drv.masses, sysm.mol_ptr)
+        tr = drv.run(args.md_steps, graph=True, block=MD_BLOCK)
+        rel, ab = replica_drift(tr["potential_energy"], tr["kinetic_energy"], E0, K0)
+        n_per = np.diff(sysm.mol_ptr)
+        mev = 1000.0 * ab / n_per
+        et = tr["potential_energy"] + tr["kinetic_energy"]
+        drift = {"steps": args.md_steps, "time_ps": args.md_steps * 0.5e-3,
+                 "rel_drift_pct_median": float(np.median(rel)), "rel_drift_pct_max_abs": float(np.abs(rel).max()),
+                 "abs_drift_mev_per_atom_median": float(np.median(mev)),
+                 "abs_drift_mev_per_atom_max_abs": float(np.abs(mev).max()),
+                 "max_excursion_mev_per_atom": float(1000.0 * (np.abs(et - (E0 + K0)[None, :]) / n_per).max())}
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * total_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp16x3 filters, f32 model, f64 Verlet state" if args.path == "fp16x3" else "f32, f64 Verlet state",
+            "data": "synthetic (seeded), seed-0 weights",
+            "config": {"workload": args.workload, "atoms": sysm.n_atoms, "replicas": sysm.n_mol,
+                       "md_steps_per_bench_step": MD_BLOCK, "dt_fs": 0.5, "temperature_K": 300.0,
+                       "path": args.path, "graph": "one CUDA graph per 50 MD steps",
+                       "l2": "256 MiB buffer rewritten between timed graph replays"},
+            "md_step_latency_ms_p50": statistics.median(blk_ms) / MD_BLOCK,
+            "drift": drift, "clocks": ck}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_env()
@@ -207,6 +287,11 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
+    if args.workload.startswith("replicas"):
+        run_md(args, world, rank, local)
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
     from mlff_gb300 import _lib, systems
     from mlff_gb300.engine import make_batch
 
