@@ -80,6 +80,7 @@ WsLayout ws_layout(const mlff_dims& d, int32_t n_atoms, int32_t n_mol, int64_t c
     L.xbar = take(sizeof(float) * 2 * N * 4 * H);
     L.e_atom = take(sizeof(float) * N);
     L.md_pos32 = take(sizeof(float) * 3 * N);
+    if (path == MLFF_PATH_TUNED_TC) L.geo = take(sizeof(float4) * cap);
     if (path == MLFF_PATH_PLAIN_FP32) {
         L.geo = take(sizeof(float4) * cap);
         L.erbf = take(sizeof(float) * cap * RMAX);

@@ -8,6 +8,7 @@ constexpr float PI_FC = 3.14159265358979f;
 
 struct EdgeArgs {
     const float4* pos4;
+    const float4* geo;        // optional per-edge (u_x, u_y, u_z, d), computed once per call
     const int32_t* atom_mol;
     const float* box;
     const uint8_t* pbc;
@@ -52,7 +53,12 @@ __device__ __forceinline__ void cutoff_fn_d(float d, float rc, float& fc, float&
 // Padding slots get d = 0 (masked out by the callers through n).
 __device__ __forceinline__ void load_edge(const EdgeArgs& a, int t0, int t, int n, float4* us, int* src_s,
                                           int* rcv_s) {
-    if (t < n) {
+    if (t < n && a.geo) {
+        const int k = t0 + t;
+        us[t] = a.geo[k];
+        src_s[t] = a.col[k];
+        rcv_s[t] = a.erecv[k];
+    } else if (t < n) {
         const int k = t0 + t;
         const int ra = a.erecv[k], sb = a.col[k];
         const int m = a.atom_mol[ra];
@@ -75,5 +81,9 @@ __device__ __forceinline__ void load_edge(const EdgeArgs& a, int t0, int t, int 
         rcv_s[t] = -1;
     }
 }
+
+// Per-edge geometry for edges [0, n_edges): (u, d) exactly as load_edge
+// computes it, once per call instead of once per layer and pass.
+__global__ void edge_geom_kernel(EdgeArgs a, float4* __restrict__ geo);
 
 }  // namespace mlff

@@ -320,6 +320,18 @@ static int add_rows(float* dst, const float* src, int64_t n, const Status* st, c
     return MLFF_OK;
 }
 
+__global__ void edge_geom_kernel(EdgeArgs a, float4* __restrict__ geo) {
+    if (a.st->code != 0) return;
+    const int n_edges = a.row_ptr[a.n_atoms];
+    __shared__ float4 us[256];
+    __shared__ int src_s[256], rcv_s[256];
+    for (int t0 = blockIdx.x * 256; t0 < n_edges; t0 += gridDim.x * 256) {
+        const int n = min(256, n_edges - t0);
+        load_edge(a, t0, threadIdx.x, n, us, src_s, rcv_s);
+        if ((int)threadIdx.x < n) geo[t0 + threadIdx.x] = us[threadIdx.x];
+    }
+}
+
 int run_tuned(const mlff_dims& d, const float* P, const PackedOffsets& po, const mlff_system& sys,
               const WsLayout& L, void* ws, const mlff_outputs& out, int path, cudaStream_t st) {
     const int N = sys.n_atoms;
@@ -348,6 +360,14 @@ int run_tuned(const mlff_dims& d, const float* P, const PackedOffsets& po, const
     float* X = ws_ptr<float>(ws, L.X);
     float* Xt = ws_ptr<float>(ws, L.Xt);
     const bool tc = path == MLFF_PATH_TUNED_TC;
+    if (tc) {
+        float4* geo = ws_ptr<float4>(ws, L.geo);
+        ProfScope prof(PK_NEIGHBORS, st);
+        const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((L.cap + 255) / 256, 152 * 8));
+        edge_geom_kernel<<<blocks, 256, 0, st>>>(a, geo);
+        MLFF_LAUNCH_CHECK("edge_geom");
+        a.geo = geo;
+    }
     for (int l = 0; l < d.n_layers; ++l) {
         a.lo = po.layer[l];
         a.X = X + l * NX;
