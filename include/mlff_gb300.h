@@ -47,6 +47,7 @@ typedef struct CUstream_st *mlff_stream_t; /* same type as cudaStream_t */
 #define MLFF_PATH_PLAIN_FP32 0    /* per-op FP32 kernels (the plain drop-in) */
 #define MLFF_PATH_TUNED_TC 1      /* fused edge kernels, tcgen05, split-FP16 operands */
 #define MLFF_PATH_TUNED_FP32 2    /* fused edge kernels, FP32 CUDA cores */
+#define MLFF_PATH_TRAIN 3         /* plain FP32 path plus parameter gradients (workspace sizing) */
 
 #define MLFF_MAX_LAYERS 8
 
@@ -79,6 +80,26 @@ typedef struct {
     const float *head_w2, *head_b2; /* energy_head.2 [H/4,H/2], [H/4] */
     const float *head_w3, *head_b3; /* energy_head.4 [1,H/4], [1] */
 } mlff_params;
+
+/* Float32 parameter gradients, one device pointer per state_dict tensor
+ * (same order and shapes as mlff_params); a NULL entry is skipped. */
+typedef struct {
+    float *embedding;
+    float *rbf_centers; /* not trained (buffers of the reference); left untouched */
+    float *rbf_widths;
+    float *filter_w1[MLFF_MAX_LAYERS];
+    float *filter_b1[MLFF_MAX_LAYERS];
+    float *filter_w2[MLFF_MAX_LAYERS];
+    float *filter_b2[MLFF_MAX_LAYERS];
+    float *mixing[MLFF_MAX_LAYERS];
+    float *update_w1[MLFF_MAX_LAYERS];
+    float *update_b1[MLFF_MAX_LAYERS];
+    float *update_w2[MLFF_MAX_LAYERS];
+    float *update_b2[MLFF_MAX_LAYERS];
+    float *head_w1, *head_b1;
+    float *head_w2, *head_b2;
+    float *head_w3, *head_b3;
+} mlff_grads;
 
 /* A ragged batch of structures (ase_calculator.py:647-706 _prepare_batch):
  * structure m owns atoms mol_ptr[m] .. mol_ptr[m+1]-1.  Edges never cross
@@ -181,6 +202,24 @@ int mlff_verlet_steps(const mlff_dims *dims, const void *packed, const mlff_syst
                       int64_t edge_capacity, int32_t path, mlff_md_state *state, double dt,
                       int32_t n_steps, void *workspace, size_t workspace_bytes,
                       mlff_stream_t stream);
+
+/* Parameter gradients for training: grads <- sum_b w_b dE_b/dtheta for
+ * every state_dict tensor, with w (device, double [B]) the derivative of
+ * the loss with respect to each structure's energy (the energy term of
+ * ForceFieldLoss, training/losses.py:106-246, e.g. w_b = 2 (E_b - E_ref_b)
+ * / B for a mean-squared energy error).  Replaces the parameter part of
+ * loss.backward() in Trainer.train_epoch (training/trainer.py:288-393) for
+ * the energy loss.  Runs the plain FP32 path forward (energies into
+ * out->energy) and its hand-written reverse pass with the weight-gradient
+ * reductions added; out->forces (optional) receives -sum_b w_b dE_b/dpos.
+ * The weight-gradient reductions add in a fixed order; the plain path's
+ * message scatter-adds are float atomics (as index_add_ on a GPU), so
+ * repeated calls agree to rounding, not bit for bit.
+ * Workspace: mlff_workspace_size(..., MLFF_PATH_TRAIN). */
+int mlff_param_grads(const mlff_dims *dims, const void *packed, const mlff_system *sys,
+                     int64_t edge_capacity, const double *energy_weights, const mlff_grads *grads,
+                     const mlff_outputs *out, void *workspace, size_t workspace_bytes,
+                     mlff_stream_t stream);
 
 /* Kernel timing for benchmarks (no counterpart in the reference, whose
  * timers wrap whole Python calls: cuda/benchmark_utils.py:147-194).

@@ -81,7 +81,7 @@ WsLayout ws_layout(const mlff_dims& d, int32_t n_atoms, int32_t n_mol, int64_t c
     L.e_atom = take(sizeof(float) * N);
     L.md_pos32 = take(sizeof(float) * 3 * N);
     if (path == MLFF_PATH_TUNED_TC) L.geo = take(sizeof(float4) * cap);
-    if (path == MLFF_PATH_PLAIN_FP32) {
+    if (path == MLFF_PATH_PLAIN_FP32 || path == MLFF_PATH_TRAIN) {
         L.geo = take(sizeof(float4) * cap);
         L.erbf = take(sizeof(float) * cap * RMAX);
         L.erbf_d = take(sizeof(float) * cap * RMAX);
@@ -92,6 +92,12 @@ WsLayout ws_layout(const mlff_dims& d, int32_t n_atoms, int32_t n_mol, int64_t c
         L.comb = take(sizeof(float) * N * 2 * H);
         L.uh = take(sizeof(float) * N * H);
         L.abar = take(sizeof(float) * N * H3);
+    }
+    if (path == MLFF_PATH_TRAIN) {
+        L.gcomb = take(sizeof(float) * N * 2 * H);
+        L.ghead = take(sizeof(float) * N * 193);
+        L.gpart = take(sizeof(float) * GRAD_SPLIT * H3 * H);
+        L.gmix = take(sizeof(float) * GRAD_MIX_BLOCKS * 9);
     }
     L.total = p;
     return L;
@@ -126,7 +132,8 @@ static int check_sys(const mlff_system* s, int64_t cap) {
 }
 
 static int check_path(int32_t path) {
-    if (path != MLFF_PATH_PLAIN_FP32 && path != MLFF_PATH_TUNED_TC && path != MLFF_PATH_TUNED_FP32) {
+    if (path != MLFF_PATH_PLAIN_FP32 && path != MLFF_PATH_TUNED_TC && path != MLFF_PATH_TUNED_FP32 &&
+        path != MLFF_PATH_TRAIN) {
         set_error("unknown path %d", path);
         return MLFF_ERR_INVALID;
     }
@@ -147,7 +154,7 @@ int energy_forces_impl(const mlff_dims& d, const void* packed, const mlff_system
     int r = launch_neighbors(d, sys, L, ws, st);
     if (r) return r;
     const float* P = static_cast<const float*>(packed);
-    if (path == MLFF_PATH_PLAIN_FP32) return run_plain(d, P, po, sys, L, ws, out, st);
+    if (path == MLFF_PATH_PLAIN_FP32 || path == MLFF_PATH_TRAIN) return run_plain(d, P, po, sys, L, ws, out, st);
     return run_tuned(d, P, po, sys, L, ws, out, path, st);
 }
 int md_kick_drift(const WsLayout& L, void* ws, mlff_md_state* s, double dt, cudaStream_t st);
@@ -282,6 +289,25 @@ int mlff_verlet_steps(const mlff_dims* dims, const void* packed, const mlff_syst
         }
     }
     return MLFF_OK;
+}
+
+int mlff_param_grads(const mlff_dims* dims, const void* packed, const mlff_system* sys, int64_t edge_capacity,
+                     const double* energy_weights, const mlff_grads* grads, const mlff_outputs* out, void* workspace,
+                     size_t workspace_bytes, mlff_stream_t stream) {
+    WsLayout L;
+    int r = prepare(dims, sys, edge_capacity, MLFF_PATH_TRAIN, workspace, workspace_bytes, L);
+    if (r) return r;
+    if (!packed || !energy_weights || !grads || !out || !out->energy) {
+        set_error("packed weights, energy_weights, grads and out->energy are required");
+        return MLFF_ERR_INVALID;
+    }
+    if (out->virial) { set_error("the training path returns no virial"); return MLFF_ERR_INVALID; }
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    MLFF_CUDA(cudaMemsetAsync(ws_ptr<Status>(workspace, L.status), 0, sizeof(Status), st));
+    if ((r = launch_neighbors(*dims, *sys, L, workspace, st))) return r;
+    PackedOffsets po = packed_offsets(*dims);
+    GradCtx g{energy_weights, *grads};
+    return run_plain(*dims, static_cast<const float*>(packed), po, *sys, L, workspace, *out, st, &g);
 }
 
 int mlff_read_status(const void* workspace, int32_t* code, int64_t* n_edges, int32_t* where, mlff_stream_t stream) {

@@ -1,0 +1,317 @@
+// Parameter gradients of sum_b w_b E_b for training (the parameter part of
+// loss.backward() in Trainer.train_epoch, training/trainer.py:288-393, for
+// the energy term of ForceFieldLoss, training/losses.py:106-246).
+//
+// They hang off the plain FP32 path's reverse pass (plain.cu), which keeps
+// every per-op intermediate the reductions need: the readout adjoint is
+// scaled per structure by w_b, and at each layer the weight gradients are
+// reductions over atoms or edges of an adjoint times a forward activation:
+//   filter   dW2 = sum_e fbar_e (x) silu(z_e)   db2 = sum_e fbar_e
+//            dW1 = sum_e zbar_e (x) rbf_e        db1 = sum_e zbar_e
+//   update   dU2 = sum_a abar_a (x) silu(uz_a)  dc2 = sum_a abar_a
+//            dU1 = sum_a zbar_a (x) [s, |v|]_a   dc1 = sum_a zbar_a
+//            dM_ij = sum_a,c xbar'_{v_i,c} g2_c v_{j,c}
+//   readout  the three Linear layers of energy_head, per atom
+//   embedding dEmb[z] = sum_{a: Z_a = z} dE/ds_a of the layer-0 input.
+// Every reduction here adds in a fixed order (fixed row splits, partial
+// sums written to a scratch buffer and added in split order); the inputs
+// come from the plain path, whose message scatter-adds are float atomics.
+#include "common.cuh"
+#include "workspace.h"
+#include "profile.h"
+
+namespace mlff {
+
+// ------------------------------------------------ generic A^T B reduction
+// partial[split][m][k] = sum over rows n of split: A[n][m] * op(B[n][k]),
+// op = identity (BOP 0), silu (BOP 1) or 1 (BOP 2: column sums of A, K = 1).
+// 32 x 32 output tile per block, 2 x 2 per thread, rows staged 32 at a time.
+template <int BOP>
+__global__ void __launch_bounds__(256) wgrad_partial_kernel(const float* __restrict__ A, int lda,
+                                                            const float* __restrict__ B, int ldb, int M, int K,
+                                                            int64_t n_static, const int32_t* __restrict__ n_dev,
+                                                            float* __restrict__ partial, const Status* st) {
+    __shared__ float As[32][33];
+    __shared__ float Bs[32][33];
+    if (st->code != 0) return;
+    const int64_t n = n_dev ? (int64_t)(*n_dev) : n_static;
+    const int tiles_k = (K + 31) / 32;
+    const int m0 = (blockIdx.x / tiles_k) * 32, k0 = (blockIdx.x % tiles_k) * 32;
+    const int split = blockIdx.y;
+    const int64_t per = (n + GRAD_SPLIT - 1) / GRAD_SPLIT;
+    const int64_t r0 = split * per, r1 = min(n, r0 + per);
+    const int t = threadIdx.x, tm = t >> 4, tk = t & 15;
+    float acc[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+    for (int64_t n0 = r0; n0 < r1; n0 += 32) {
+        for (int i = t; i < 32 * 32; i += 256) {
+            const int rr = i >> 5, cc = i & 31;
+            const int64_t row = n0 + rr;
+            const bool okr = row < r1;
+            As[rr][cc] = (okr && m0 + cc < M) ? A[row * lda + m0 + cc] : 0.f;
+            float b = 0.f;
+            if (okr && k0 + cc < K) {
+                if (BOP == 2) b = 1.f;
+                else {
+                    b = B[row * ldb + k0 + cc];
+                    if (BOP == 1) b = silu_f(b);
+                }
+            }
+            Bs[rr][cc] = b;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int i = 0; i < 32; ++i) {
+            const float a0 = As[i][2 * tm], a1 = As[i][2 * tm + 1];
+            const float b0 = Bs[i][2 * tk], b1 = Bs[i][2 * tk + 1];
+            acc[0][0] = fmaf(a0, b0, acc[0][0]);
+            acc[0][1] = fmaf(a0, b1, acc[0][1]);
+            acc[1][0] = fmaf(a1, b0, acc[1][0]);
+            acc[1][1] = fmaf(a1, b1, acc[1][1]);
+        }
+        __syncthreads();
+    }
+    float* out = partial + (int64_t)split * M * K;
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const int m = m0 + 2 * tm + i, k = k0 + 2 * tk + j;
+            if (m < M && k < K) out[(int64_t)m * K + k] = acc[i][j];
+        }
+}
+
+__global__ void wgrad_reduce_kernel(const float* __restrict__ partial, int64_t MK, float* __restrict__ out,
+                                    const Status* st) {
+    if (st->code != 0) return;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < MK; i += (int64_t)gridDim.x * blockDim.x) {
+        float s = 0.f;
+        for (int sp = 0; sp < GRAD_SPLIT; ++sp) s += partial[(int64_t)sp * MK + i];
+        out[i] = s;
+    }
+}
+
+// out[M][K] = sum_n A[n][m] op(B[n][k]) (out NULL: nothing to do)
+template <int BOP>
+static int wgrad(const float* A, int lda, const float* B, int ldb, int M, int K, int64_t n, const int32_t* n_dev,
+                 float* out, const WsLayout& L, void* ws, cudaStream_t st) {
+    if (!out) return MLFF_OK;
+    float* part = ws_ptr<float>(ws, L.gpart);
+    const Status* status = ws_ptr<Status>(ws, L.status);
+    dim3 grid(((M + 31) / 32) * ((K + 31) / 32), GRAD_SPLIT);
+    wgrad_partial_kernel<BOP><<<grid, 256, 0, st>>>(A, lda, B, ldb, M, K, n, n_dev, part, status);
+    MLFF_LAUNCH_CHECK("wgrad_partial");
+    const int64_t MK = (int64_t)M * K;
+    wgrad_reduce_kernel<<<(int)std::min<int64_t>((MK + 255) / 256, 152 * 4), 256, 0, st>>>(part, MK, out, status);
+    MLFF_LAUNCH_CHECK("wgrad_reduce");
+    return MLFF_OK;
+}
+
+// ------------------------------------------------------------- readout
+// Per atom (one thread per hidden unit, RO_G atoms per block): recompute
+// z1 = W1 s + b1, z2 = W2 silu(z1) + b2 and the adjoints for the seed
+// w = w_b of the atom's structure: ebar = w, a2bar = w w3 silu'(z2),
+// a1bar = (W2^T a2bar) silu'(z1); store h1, a1bar, h2, a2bar, ebar, and scale
+// the unit-seed adjoint dE_a/ds (xbar, written by the readout) by w.
+constexpr int RO_G = 8;
+__global__ void __launch_bounds__(128) readout_grad_kernel(const float* __restrict__ P, PackedOffsets po,
+                                                           const float* __restrict__ X, const int32_t* __restrict__ atom_mol,
+                                                           const double* __restrict__ w, int32_t n_atoms,
+                                                           float* __restrict__ ghead, float* __restrict__ xbar,
+                                                           const Status* st) {
+    __shared__ float s_in[RO_G][H];
+    __shared__ float z1[RO_G][64];
+    __shared__ float z2[RO_G][32];
+    __shared__ float g2[RO_G][32];
+    if (st->code != 0) return;
+    const int t = threadIdx.x;
+    for (int a0 = blockIdx.x * RO_G; a0 < n_atoms; a0 += gridDim.x * RO_G) {
+        for (int q = 0; q < RO_G; ++q) {
+            const int a = a0 + q;
+            s_in[q][t] = a < n_atoms ? X[(int64_t)a * 4 * H + t] : 0.0f;
+        }
+        __syncthreads();
+        if (t < 64) {
+            for (int q = 0; q < RO_G; ++q) {
+                float acc = P[po.head_b1 + t];
+                for (int i = 0; i < H; ++i) acc = fmaf(P[po.head_w1t + i * 64 + t], s_in[q][i], acc);
+                z1[q][t] = acc;
+            }
+        }
+        __syncthreads();
+        if (t < 32) {
+            for (int q = 0; q < RO_G; ++q) {
+                float acc = P[po.head_b2 + t];
+                for (int i = 0; i < 64; ++i) acc = fmaf(P[po.head_w2t + i * 32 + t], silu_f(z1[q][i]), acc);
+                z2[q][t] = acc;
+                const int a = a0 + q;
+                const float wq = a < n_atoms ? (float)w[atom_mol[a]] : 0.f;
+                g2[q][t] = wq * P[po.head_w3 + t] * dsilu_f(acc);
+            }
+        }
+        __syncthreads();
+        for (int q = 0; q < RO_G; ++q) {
+            const int a = a0 + q;
+            if (a >= n_atoms) continue;
+            float* gh = ghead + (int64_t)a * 193;
+            if (t < 64) {
+                float acc = 0.f;
+                for (int j = 0; j < 32; ++j) acc = fmaf(P[po.head_w2 + j * 64 + t], g2[q][j], acc);
+                gh[t] = silu_f(z1[q][t]);
+                gh[64 + t] = acc * dsilu_f(z1[q][t]);
+            } else if (t < 96) {
+                gh[128 + (t - 64)] = silu_f(z2[q][t - 64]);
+                gh[160 + (t - 64)] = g2[q][t - 64];
+            } else if (t == 96) {
+                gh[192] = (float)w[atom_mol[a]];
+            }
+            const float wq = (float)w[atom_mol[a]];
+            xbar[(int64_t)a * 4 * H + t] *= wq;
+        }
+        __syncthreads();
+    }
+}
+
+// ----------------------------------------------------------- embedding
+// dEmb[z][c] = sum over atoms of species z of xbar0[a][c] (s part), in atom
+// order; one block per species.
+__global__ void embed_grad_kernel(const int64_t* __restrict__ Z, const float* __restrict__ xbar0, int32_t n_atoms,
+                                  int32_t n_species, float* __restrict__ out, const Status* st) {
+    if (st->code != 0) return;
+    for (int z = blockIdx.x; z < n_species; z += gridDim.x) {
+        float acc = 0.f;
+        for (int a = 0; a < n_atoms; ++a)
+            if (Z[a] == z) acc += xbar0[(int64_t)a * 4 * H + threadIdx.x];
+        out[(int64_t)z * H + threadIdx.x] = acc;
+    }
+}
+
+// -------------------------------------------------------------- mixing
+// v' = v g1 + (M v) g2 (student_model.py:452-468): dM_ij = sum_a,c
+// xbar'_{v_i}[a][c] g2[a][c] v_j[a][c]; per-block partials, then a
+// fixed-order sum.
+__global__ void __launch_bounds__(256) mix_grad_partial_kernel(const float* __restrict__ Xt,
+                                                               const float* __restrict__ ua,
+                                                               const float* __restrict__ xbo, int32_t n_atoms,
+                                                               float* __restrict__ part, const Status* st) {
+    __shared__ float red[9][256];
+    if (st->code != 0) return;
+    float acc[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    const int64_t total = (int64_t)n_atoms * H;
+    for (int64_t i = blockIdx.x * 256 + threadIdx.x; i < total; i += (int64_t)gridDim.x * 256) {
+        const int64_t a = i / H;
+        const int c = (int)(i % H);
+        const float g2 = ua[a * H3 + 2 * H + c];
+        const float* x = Xt + a * 4 * H;
+        const float* xb = xbo + a * 4 * H;
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) acc[3 * r + j] = fmaf(xb[(1 + r) * H + c] * g2, x[(1 + j) * H + c], acc[3 * r + j]);
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) red[k][threadIdx.x] = acc[k];
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o)
+#pragma unroll
+            for (int k = 0; k < 9; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x < 9) part[blockIdx.x * 9 + threadIdx.x] = red[threadIdx.x][0];
+}
+
+__global__ void mix_grad_reduce_kernel(const float* __restrict__ part, float* __restrict__ out, const Status* st) {
+    if (st->code != 0) return;
+    if (threadIdx.x < 9) {
+        float s = 0.f;
+        for (int b = 0; b < GRAD_MIX_BLOCKS; ++b) s += part[b * 9 + threadIdx.x];
+        out[threadIdx.x] = s;
+    }
+}
+
+// ------------------------------------------------------------ launchers
+int grad_readout(const mlff_dims& d, const float* P, const PackedOffsets& po, const mlff_system& sys,
+                 const WsLayout& L, void* ws, const double* w, const mlff_grads& g, cudaStream_t st) {
+    ProfScope prof(PK_OTHER, st);
+    const int N = sys.n_atoms;
+    const float* XL = ws_ptr<float>(ws, L.X) + (int64_t)d.n_layers * N * 4 * H;
+    float* gh = ws_ptr<float>(ws, L.ghead);
+    float* xbar0 = ws_ptr<float>(ws, L.xbar);
+    const Status* status = ws_ptr<Status>(ws, L.status);
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((N + RO_G - 1) / RO_G, 152 * 8));
+    readout_grad_kernel<<<blocks, 128, 0, st>>>(P, po, XL, ws_ptr<int32_t>(ws, L.atom_mol), w, N, gh, xbar0, status);
+    MLFF_LAUNCH_CHECK("readout_grad");
+    int r;
+    // energy_head.0: [64][128] = sum a1bar (x) s ; energy_head.2: [32][64] = sum a2bar (x) h1 ; .4: [1][32]
+    if ((r = wgrad<0>(gh + 64, 193, XL, 4 * H, 64, H, N, nullptr, g.head_w1, L, ws, st))) return r;
+    if ((r = wgrad<2>(gh + 64, 193, nullptr, 0, 64, 1, N, nullptr, g.head_b1, L, ws, st))) return r;
+    if ((r = wgrad<0>(gh + 160, 193, gh, 193, 32, 64, N, nullptr, g.head_w2, L, ws, st))) return r;
+    if ((r = wgrad<2>(gh + 160, 193, nullptr, 0, 32, 1, N, nullptr, g.head_b2, L, ws, st))) return r;
+    if ((r = wgrad<0>(gh + 192, 193, gh + 128, 193, 1, 32, N, nullptr, g.head_w3, L, ws, st))) return r;
+    return wgrad<2>(gh + 192, 193, nullptr, 0, 1, 1, N, nullptr, g.head_b3, L, ws, st);
+}
+
+// after the update reverse prologue: abar = dE/d(ds, g1, g2) [N][3H]
+int grad_update_out(const WsLayout& L, void* ws, int l, const float* xbo, const mlff_grads& g, cudaStream_t st) {
+    ProfScope prof(PK_OTHER, st);
+    const int N = L.N;
+    const float* abar = ws_ptr<float>(ws, L.abar);
+    const float* uz = ws_ptr<float>(ws, L.uz) + (int64_t)l * N * H;
+    const float* ua = ws_ptr<float>(ws, L.ua) + (int64_t)l * N * H3;
+    const float* Xt = ws_ptr<float>(ws, L.Xt) + (int64_t)l * N * 4 * H;
+    int r;
+    if ((r = wgrad<1>(abar, H3, uz, H, H3, H, N, nullptr, g.update_w2[l], L, ws, st))) return r;
+    if ((r = wgrad<2>(abar, H3, nullptr, 0, H3, 1, N, nullptr, g.update_b2[l], L, ws, st))) return r;
+    if (g.mixing[l]) {
+        const Status* status = ws_ptr<Status>(ws, L.status);
+        float* part = ws_ptr<float>(ws, L.gmix);
+        mix_grad_partial_kernel<<<GRAD_MIX_BLOCKS, 256, 0, st>>>(Xt, ua, xbo, N, part, status);
+        MLFF_LAUNCH_CHECK("mix_grad");
+        mix_grad_reduce_kernel<<<1, 32, 0, st>>>(part, g.mixing[l], status);
+        MLFF_LAUNCH_CHECK("mix_grad_reduce");
+    }
+    return MLFF_OK;
+}
+
+// after zbar_u = (abar U2) silu'(uz) is in uh [N][H]; comb_l = [s, |v|] of Xt_l in gcomb
+int grad_update_in(const WsLayout& L, void* ws, int l, const float* zbar_u, const float* comb_l,
+                   const mlff_grads& g, cudaStream_t st) {
+    ProfScope prof(PK_OTHER, st);
+    const int N = L.N;
+    int r;
+    if ((r = wgrad<0>(zbar_u, H, comb_l, 2 * H, H, 2 * H, N, nullptr, g.update_w1[l], L, ws, st))) return r;
+    return wgrad<2>(zbar_u, H, nullptr, 0, H, 1, N, nullptr, g.update_b1[l], L, ws, st);
+}
+
+// after the message reverse: fbar [cap][3H]; z of layer l in fz
+int grad_filter_out(const WsLayout& L, void* ws, int l, const int32_t* E_dev, const mlff_grads& g, cudaStream_t st) {
+    ProfScope prof(PK_OTHER, st);
+    const float* fbar = ws_ptr<float>(ws, L.fbar);
+    const float* z = ws_ptr<float>(ws, L.fz) + (int64_t)l * L.cap * H;
+    int r;
+    if ((r = wgrad<1>(fbar, H3, z, H, H3, H, L.cap, E_dev, g.filter_w2[l], L, ws, st))) return r;
+    return wgrad<2>(fbar, H3, nullptr, 0, H3, 1, L.cap, E_dev, g.filter_b2[l], L, ws, st);
+}
+
+// after zbar_f = (fbar W2) silu'(z) is in fh [cap][H]
+int grad_filter_in(const mlff_dims& d, const WsLayout& L, void* ws, int l, const int32_t* E_dev, const mlff_grads& g,
+                   cudaStream_t st) {
+    ProfScope prof(PK_OTHER, st);
+    const float* zbar = ws_ptr<float>(ws, L.fh);
+    const float* erbf = ws_ptr<float>(ws, L.erbf);
+    int r;
+    if ((r = wgrad<0>(zbar, H, erbf, RMAX, H, d.n_rbf, L.cap, E_dev, g.filter_w1[l], L, ws, st))) return r;
+    return wgrad<2>(zbar, H, nullptr, 0, H, 1, L.cap, E_dev, g.filter_b1[l], L, ws, st);
+}
+
+int grad_embedding(const mlff_dims& d, const mlff_system& sys, const WsLayout& L, void* ws, const float* xbar0,
+                   const mlff_grads& g, cudaStream_t st) {
+    if (!g.embedding) return MLFF_OK;
+    ProfScope prof(PK_OTHER, st);
+    embed_grad_kernel<<<std::min(d.n_species, 152 * 4), H, 0, st>>>(sys.Z, xbar0, sys.n_atoms, d.n_species,
+                                                                     g.embedding, ws_ptr<Status>(ws, L.status));
+    MLFF_LAUNCH_CHECK("embed_grad");
+    return MLFF_OK;
+}
+
+}  // namespace mlff

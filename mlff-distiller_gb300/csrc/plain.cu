@@ -339,7 +339,7 @@ __global__ void copy_kernel(const float* __restrict__ src, float* __restrict__ d
 }
 
 int run_plain(const mlff_dims& d, const float* P, const PackedOffsets& po, const mlff_system& sys,
-              const WsLayout& L, void* ws, const mlff_outputs& out, cudaStream_t st) {
+              const WsLayout& L, void* ws, const mlff_outputs& out, cudaStream_t st, const GradCtx* grad) {
     const int N = sys.n_atoms;
     const int64_t NX = (int64_t)N * 4 * H;
     const int64_t cap = L.cap;
@@ -409,9 +409,11 @@ int run_plain(const mlff_dims& d, const float* P, const PackedOffsets& po, const
             MLFF_LAUNCH_CHECK("pl_update_post");
         }
     }
-    const bool want_grad = out.forces != nullptr || out.virial != nullptr;
+    const bool want_grad = out.forces != nullptr || out.virial != nullptr || grad != nullptr;
     if ((r = launch_readout(d, P, po, sys, L, ws, out, want_grad ? 1 : 0, st))) return r;
     if (!want_grad) return MLFF_OK;
+    // training: head gradients, and the adjoint seeded with dL/dE_b
+    if (grad && (r = grad_readout(d, P, po, sys, L, ws, grad->w, grad->g, st))) return r;
 
     MLFF_CUDA(cudaMemsetAsync(eacc, 0, sizeof(float4) * cap, st));
     prof_launch(PK_OTHER);   // the memset above
@@ -426,8 +428,15 @@ int run_plain(const mlff_dims& d, const float* P, const PackedOffsets& po, const
                                                               xbo, N, abar, xtb, status);
             MLFF_LAUNCH_CHECK("pl_update_bwd_pre");
         }
+        if (grad && (r = grad_update_out(L, ws, l, xbo, grad->g, st))) return r;
         if ((r = sgemm<2>(abar, P + lo.u2, nullptr, uh, nullptr, uz + (int64_t)l * N * H, N, nullptr, H, H3, status,
                           st))) return r;
+        if (grad) {
+            float* gcomb = ws_ptr<float>(ws, L.gcomb);
+            pl_update_pre_kernel<<<nblocks, 256, 0, st>>>(Xt + l * NX, N, gcomb, status);
+            MLFF_LAUNCH_CHECK("pl_update_pre");
+            if ((r = grad_update_in(L, ws, l, uh, gcomb, grad->g, st))) return r;
+        }
         if ((r = sgemm<0>(uh, P + lo.u1, nullptr, comb, nullptr, nullptr, N, nullptr, 2 * H, H, status, st))) return r;
         {
             ProfScope prof(PK_UPDATE_BWD, st);
@@ -444,9 +453,11 @@ int run_plain(const mlff_dims& d, const float* P, const PackedOffsets& po, const
                                                            E_dev, xtb, xbo, fbar, eacc, status);
             MLFF_LAUNCH_CHECK("pl_message_bwd");
         }
+        if (grad && (r = grad_filter_out(L, ws, l, E_dev, grad->g, st))) return r;
         // filter reverse: hbar = fbar W2, zbar = hbar silu'(z), ebar = zbar W1
         if ((r = sgemm<2>(fbar, P + lo.w2, nullptr, fh, nullptr, fz + (int64_t)l * cap * H, cap, E_dev, H, H3, status,
                           st))) return r;
+        if (grad && (r = grad_filter_in(d, L, ws, l, E_dev, grad->g, st))) return r;
         if ((r = sgemm<0>(fh, P + lo.w1, nullptr, fbar, nullptr, nullptr, cap, E_dev, RMAX, H, status, st))) return r;
         {
             ProfScope prof(PK_PLAIN_EDGE, st);
@@ -454,6 +465,8 @@ int run_plain(const mlff_dims& d, const float* P, const PackedOffsets& po, const
             MLFF_LAUNCH_CHECK("pl_dd");
         }
     }
+    if (grad && (r = grad_embedding(d, sys, L, ws, xbo, grad->g, st))) return r;
+    if (!out.forces && !out.virial) return MLFF_OK;
     return launch_forces(d, sys, L, ws, out, st);
 }
 

@@ -7,6 +7,9 @@
 
 namespace mlff {
 
+constexpr int GRAD_SPLIT = 64;        // row splits of the weight-gradient reductions
+constexpr int GRAD_MIX_BLOCKS = 304;  // blocks of the mixing-matrix gradient
+
 struct WsLayout {
     int32_t N, B, L, P;        // atoms, structures, layers, persistent CTAs
     int64_t cap;               // edge capacity
@@ -44,6 +47,11 @@ struct WsLayout {
     size_t comb;               // float [N][2H]
     size_t uh;                 // float [N][H]
     size_t abar;               // float [N][3H]
+    // parameter-gradient path only
+    size_t gcomb;              // float [N][2H]   update-MLP input recomputed per layer
+    size_t ghead;              // float [N][193]  readout: h1 (64), a1bar (64), h2 (32), a2bar (32), ebar (1)
+    size_t gpart;              // float [GRAD_SPLIT][3H*H] partial weight gradients
+    size_t gmix;               // float [GRAD_MIX_BLOCKS][9] partial mixing-matrix gradients
     size_t total;
 };
 
@@ -87,9 +95,24 @@ int launch_readout(const mlff_dims& d, const float* packed, const PackedOffsets&
                    int want_grad, cudaStream_t st);
 int launch_forces(const mlff_dims& d, const mlff_system& sys, const WsLayout& L, void* ws,
                   const mlff_outputs& out, cudaStream_t st);
+// Training: per-structure loss weights dL/dE_b and the gradient outputs.
+struct GradCtx {
+    const double* w;
+    mlff_grads g;
+};
 int run_plain(const mlff_dims& d, const float* packed, const PackedOffsets& po,
               const mlff_system& sys, const WsLayout& L, void* ws, const mlff_outputs& out,
-              cudaStream_t st);
+              cudaStream_t st, const GradCtx* grad = nullptr);
+int grad_readout(const mlff_dims& d, const float* P, const PackedOffsets& po, const mlff_system& sys,
+                 const WsLayout& L, void* ws, const double* w, const mlff_grads& g, cudaStream_t st);
+int grad_update_out(const WsLayout& L, void* ws, int l, const float* xbo, const mlff_grads& g, cudaStream_t st);
+int grad_update_in(const WsLayout& L, void* ws, int l, const float* zbar_u, const float* comb_l,
+                   const mlff_grads& g, cudaStream_t st);
+int grad_filter_out(const WsLayout& L, void* ws, int l, const int32_t* E_dev, const mlff_grads& g, cudaStream_t st);
+int grad_filter_in(const mlff_dims& d, const WsLayout& L, void* ws, int l, const int32_t* E_dev, const mlff_grads& g,
+                   cudaStream_t st);
+int grad_embedding(const mlff_dims& d, const mlff_system& sys, const WsLayout& L, void* ws, const float* xbar0,
+                   const mlff_grads& g, cudaStream_t st);
 int run_tuned(const mlff_dims& d, const float* packed, const PackedOffsets& po,
               const mlff_system& sys, const WsLayout& L, void* ws, const mlff_outputs& out,
               int path, cudaStream_t st);

@@ -27,6 +27,7 @@ ERR_WORKSPACE = 8
 PATH_PLAIN_FP32 = 0
 PATH_TUNED_TC = 1
 PATH_TUNED_FP32 = 2
+PATH_TRAIN = 3
 
 PATHS = {"plain": PATH_PLAIN_FP32, "fp32": PATH_PLAIN_FP32, "plain_fp32": PATH_PLAIN_FP32,
          "fp16x3": PATH_TUNED_TC, "tc": PATH_TUNED_TC, "tuned": PATH_TUNED_TC,
@@ -40,7 +41,7 @@ ERROR_NAMES = {ERR_INVALID: "invalid argument", ERR_CAPACITY: "edge capacity exc
 EXPORTS = ["mlff_version", "mlff_last_error_string", "mlff_packed_weights_size", "mlff_pack_weights",
            "mlff_workspace_size", "mlff_build_neighbors", "mlff_copy_neighbors", "mlff_energy_forces",
            "mlff_read_status", "mlff_clear_status", "mlff_verlet_steps", "mlff_profile_begin",
-           "mlff_profile_end", "mlff_radius_graph_noalloc"]
+           "mlff_profile_end", "mlff_radius_graph_noalloc", "mlff_param_grads"]
 
 PROFILE_KINDS = ["neighbors", "edge_fwd", "edge_bwd", "update_fwd", "update_bwd", "readout", "forces",
                  "plain_gemm", "plain_edge", "other", "md"]
@@ -61,6 +62,11 @@ class Params(ctypes.Structure):
                 ("mixing", _PL), ("update_w1", _PL), ("update_b1", _PL), ("update_w2", _PL),
                 ("update_b2", _PL), ("head_w1", _P), ("head_b1", _P), ("head_w2", _P),
                 ("head_b2", _P), ("head_w3", _P), ("head_b3", _P)]
+
+
+class Grads(ctypes.Structure):
+    """mlff_grads: gradient output pointers, same layout as Params."""
+    _fields_ = Params._fields_
 
 
 class System(ctypes.Structure):
@@ -135,6 +141,9 @@ def load(build_if_missing: bool = True):
         lib.mlff_profile_begin.restype = ctypes.c_int
         lib.mlff_profile_end.restype = ctypes.c_int
         lib.mlff_profile_end.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(i64), i32]
+        lib.mlff_param_grads.restype = ctypes.c_int
+        lib.mlff_param_grads.argtypes = [ctypes.POINTER(Dims), _P, ctypes.POINTER(System), i64, _P,
+                                         ctypes.POINTER(Grads), ctypes.POINTER(Outputs), _P, sz, _P]
         lib.mlff_radius_graph_noalloc.restype = ctypes.c_int
         lib.mlff_radius_graph_noalloc.argtypes = [ctypes.POINTER(System), ctypes.c_float, i64, _P, _P, _P, _P]
         _lib = lib

@@ -133,3 +133,32 @@ def stress_voigt(dEde: np.ndarray, box: np.ndarray) -> np.ndarray:
     xx, yy, zz, yz, xz, xy (ase_calculator.py:578-583 uses that order)."""
     s = 0.5 * (dEde + dEde.T) / float(np.prod(box))
     return np.array([s[0, 0], s[1, 1], s[2, 2], s[1, 2], s[0, 2], s[0, 1]])
+
+
+def param_grads(params, Z, pos, mol_ptr, weights, cutoff=5.0, box=None, pbc=None, dtype=torch.float64):
+    """sum_b w_b dE_b/dtheta for every tensor of the state_dict except the
+    RBF buffers, by autograd through `energy` (the parameter gradients
+    loss.backward() gives the reference's Trainer, training/trainer.py:
+    288-393, for an energy loss with dL/dE_b = w_b)."""
+    from . import nbr
+    pos_np = np.asarray(pos)
+    mol_ptr = np.asarray(mol_ptr, dtype=np.int64)
+    n_mol = len(mol_ptr) - 1
+    src, dst, shift = nbr.radius_graph(pos_np.astype(np.float32), mol_ptr, cutoff, box, pbc)
+    p = params_to(params, dtype)
+    train = [k for k in p if not k.startswith("rbf.")]
+    for k in train:
+        p[k].requires_grad_(True)
+    mol = torch.repeat_interleave(torch.arange(n_mol), torch.as_tensor(np.diff(mol_ptr)))
+    src_t = torch.as_tensor(np.asarray(src), dtype=torch.long)
+    dst_t = torch.as_tensor(np.asarray(dst), dtype=torch.long)
+    boxes = torch.zeros(n_mol, 3, dtype=dtype) if box is None else torch.as_tensor(
+        np.asarray(box, dtype=np.float64).reshape(n_mol, 3), dtype=dtype)
+    shift_t = torch.as_tensor(np.asarray(shift), dtype=dtype) * boxes[mol[dst_t]]
+    x = torch.as_tensor(pos_np, dtype=dtype)
+    E = energy(p, torch.as_tensor(np.asarray(Z), dtype=torch.long), x, src_t, dst_t, shift_t, mol, n_mol, cutoff)
+    w = torch.as_tensor(np.asarray(weights), dtype=dtype)
+    # the last layer's mixing matrix only moves vector features the readout
+    # never reads: its gradient is exactly zero
+    g = torch.autograd.grad((E * w).sum(), [p[k] for k in train], allow_unused=True)
+    return E.detach(), {k: (torch.zeros_like(p[k]) if gi is None else gi).detach() for k, gi in zip(train, g)}

@@ -113,3 +113,33 @@ def test_virial_matches_finite_difference():
         if vals:
             fd = (vals[0] - vals[1]) / (2 * h)
             assert abs(fd - float(V[0, a, b])) < 1e-5 * max(1.0, abs(fd))
+
+
+def test_oracle_param_grads_match_finite_differences(weights_bias):
+    """The oracle's parameter gradients (autograd) against central
+    differences of its float64 energy, a few entries of every kind of
+    tensor, on a small molecule."""
+    from mlff_gb300 import systems
+    s = systems.lattice_molecule(12, seed=5)
+    pos = s.pos.astype(np.float32).astype(np.float64)
+    w = np.array([0.7])
+    _, g = painn.param_grads(weights_bias, s.Z, pos, s.mol_ptr, w)
+    rng = np.random.default_rng(3)
+    for key in ["embedding.weight", "interactions.0.message.rbf_to_scalar.0.weight",
+                "interactions.1.message.rbf_to_scalar.2.bias", "interactions.2.update.mixing_matrix",
+                "interactions.0.update.update_mlp.0.weight", "energy_head.2.weight", "energy_head.4.bias"]:
+        shape = weights_bias[key].shape
+        for _ in range(2):
+            idx = tuple(int(rng.integers(0, n)) for n in shape)
+            if key == "embedding.weight":
+                idx = (int(s.Z[0]),) + idx[1:]
+            h = 1e-5
+            vals = []
+            for sgn in (1, -1):
+                W = {k: v.copy() for k, v in weights_bias.items()}
+                W[key] = W[key].astype(np.float64)
+                W[key][idx] += sgn * h
+                E, _ = painn.energy_forces(W, s.Z, pos, s.mol_ptr)
+                vals.append(float(E[0]) * w[0])
+            fd = (vals[0] - vals[1]) / (2 * h)
+            assert abs(fd - float(g[key][idx])) <= 1e-6 + 1e-5 * abs(fd), (key, idx, fd, float(g[key][idx]))
