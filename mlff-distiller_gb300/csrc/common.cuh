@@ -88,10 +88,12 @@ struct LayerOffsets {
     int64_t u2t;    // [H][H3]     update Linear(H->3H), transposed
     int64_t u2;     // [H3][H]
     int64_t c2;     // [H3]
-    int64_t w1_bf;  // bf16 hi/lo tiles for the tensor-core filter (bytes offset / 4)
+    int64_t w1_bf;  // split-fp16 hi/lo tiles for the tensor-core filter (bytes offset / 4)
     int64_t w2_bf;
-    int64_t u1_bf;
-    int64_t u2_bf;
+    int64_t u1_tc;  // split-fp16 A-operand tile pairs of the tensor-core update MLP:
+    int64_t u2_tc;  //   U1 [H][2H] and U2 [3H][H] (forward),
+    int64_t u2t_tc; //   U2^T [H][3H] and U1^T [2H][H] (reverse)
+    int64_t u1t_tc;
 };
 
 struct PackedOffsets {
@@ -118,6 +120,7 @@ PackedOffsets packed_offsets(const mlff_dims& d);
 namespace mlff {
 void set_error(const char* fmt, ...);
 int cuda_status(cudaError_t e, const char* what);
+int num_sms();   // streaming multiprocessors of the current device (cached)
 void prof_count_launch();   // profile.cu: one kernel launch of the current kind
 }
 

@@ -51,12 +51,15 @@ PackedOffsets packed_offsets(const mlff_dims& d) {
         L.u2t = take(H * H3);
         L.u2 = take(H3 * H);
         L.c2 = take(H3);
-        // split-BF16 operand tiles for the tensor-core filter: hi and lo
-        // copies of W1 (H x RMAX) and W2 (H3 x H), 2 bytes per value
+        // split-fp16 operand tiles (hi and lo, 2 bytes per value) for the
+        // tensor-core filter, W1 (H x RMAX) and W2 (H3 x H), and update MLP,
+        // U1 and U2 in both orientations
         L.w1_bf = take(2 * H * RMAX / 2);
         L.w2_bf = take(2 * H3 * H / 2);
-        L.u1_bf = take(2 * H * 2 * H / 2);
-        L.u2_bf = take(2 * H3 * H / 2);
+        L.u1_tc = take(2 * H * 2 * H / 2);
+        L.u2_tc = take(2 * H3 * H / 2);
+        L.u2t_tc = take(2 * H3 * H / 2);
+        L.u1t_tc = take(2 * H * 2 * H / 2);
     }
     o.total = p;
     return o;

@@ -31,16 +31,12 @@
 #include "edge_common.cuh"
 #include "profile.h"
 #include "tc_ptx.cuh"
+#include "tc_layout.cuh"
 
 namespace mlff {
 using namespace tc;
 
 // ----------------------------------------------------- operand layouts
-// A operand (weights): 128 rows x 16 K fp16, K-major, no swizzle:
-//   off(m, k) = (k / 8) * 2048 + (m / 8) * 128 + (m % 8) * 16 + (k % 8) * 2
-constexpr uint32_t A_TILE = 4096;
-constexpr uint32_t A_LBO = 2048;
-constexpr uint32_t A_SBO = 128;
 constexpr uint32_t SLAB = 2 * A_TILE;         // hi + lo of one 128 x 16 block (W1)
 constexpr int W2_TILES = 24;                  // 3 channel chunks x 8 K-steps, q = g * 8 + s
 constexpr uint32_t W1_BYTES = 2 * SLAB;       // 2 K-steps
@@ -54,30 +50,6 @@ constexpr int NSLOT = 8;                      // ring: the 8 lo tiles of W2 chun
 constexpr uint32_t TM_W2LO = 0;
 constexpr uint32_t TM_F = 128;
 constexpr uint32_t TM_Z = 384;
-
-__host__ __device__ constexpr uint32_t a_off(int m, int k) {
-    return (uint32_t)((k >> 3) * 2048 + (m >> 3) * 128 + (m & 7) * 16 + (k & 7) * 2);
-}
-
-// B operand (edge rows x K, fp16) in the K-major 128-byte-swizzle layout:
-// K-blocks of 64 columns, each n_rows x 128 bytes; inside a block, 8-row
-// groups of 1024 bytes, and row r's 16-byte chunk j (columns 8j..8j+7) sits
-// at chunk position j ^ (r % 8).  A warp storing 32 consecutive columns of
-// one row touches one 128-byte line, and the MMA reads whole lines.
-__host__ __device__ constexpr uint32_t b_block(int n_rows) { return (uint32_t)n_rows * 128; }
-__device__ __forceinline__ uint32_t b_off(int n_rows, int row, int k) {
-    return (uint32_t)((k >> 6) * b_block(n_rows) + (row >> 3) * 1024 + (row & 7) * 128 +
-                      ((((k >> 3) & 7) ^ (row & 7)) << 4) + (k & 7) * 2);
-}
-// descriptor start offset of K-step s (columns 16s..16s+15)
-__host__ __device__ constexpr uint32_t b_kstep_off(int n_rows, int s) {
-    return (uint32_t)((s >> 2) * b_block(n_rows) + (s & 3) * 32);
-}
-__device__ __forceinline__ uint64_t sdesc_b(uint32_t saddr) {
-    return sdesc(saddr, 16, 1024) | ((uint64_t)2 << 61);   // layout 2: 128-byte swizzle
-}
-
-constexpr uint32_t align1k(uint32_t x) { return (x + 1023u) & ~1023u; }
 
 // ------------------------------------------------------------- packing
 // W1 [H][RMAX] -> 2 K-step blocks (hi, lo); W2 [3H][H] -> 24 hi tiles
@@ -102,6 +74,8 @@ __global__ void pack_tc_kernel(const float* __restrict__ w1, const float* __rest
     }
 }
 
+int pack_update_tc(const mlff_dims& d, float* out, const PackedOffsets& o, cudaStream_t st);
+
 int pack_bf16(const mlff_dims& d, float* out, const PackedOffsets& o, cudaStream_t st) {
     for (int l = 0; l < d.n_layers; ++l) {
         const LayerOffsets& L = o.layer[l];
@@ -109,11 +83,10 @@ int pack_bf16(const mlff_dims& d, float* out, const PackedOffsets& o, cudaStream
                                            reinterpret_cast<unsigned char*>(out + L.w2_bf));
         MLFF_LAUNCH_CHECK("pack_tc");
     }
-    return MLFF_OK;
+    return pack_update_tc(d, out, o, st);
 }
 
 // -------------------------------------------------------- shared pieces
-constexpr long long WAIT_BUDGET = 1LL << 32;   // ~2 s at 2 GHz
 constexpr int NT = 512;                        // threads per CTA (16 warps)
 
 __device__ __forceinline__ void signal_timeout(const EdgeArgs& a, volatile int* abort_flag, int where) {
@@ -159,10 +132,6 @@ __device__ __forceinline__ void load_w2_hi(unsigned char* dst, const unsigned ch
     for (int i = 0; i < 6; ++i) bulk_g2s(dst + i * (W2_HALF / 6), w2hi + i * (W2_HALF / 6), W2_HALF / 6, bar);
 }
 
-// sigmoid via the fast exponential and reciprocal; silu = z s,
-// silu' = s (1 + z (1 - s)).  Both are exact in the limits z -> +-inf.
-__device__ __forceinline__ float fast_sigmoid(float z) { return __fdividef(1.0f, 1.0f + __expf(-z)); }
-
 // rbf(d)_r * fc(d) for r in [r0, r0 + 16) (0 beyond R or for padding edges)
 __device__ __forceinline__ void rbf16(float d, bool valid, int r0, int R, const float* cent, const float* gam,
                                       float rc, float (&out)[16]) {
@@ -185,42 +154,6 @@ __device__ __forceinline__ void rbf16_d(float d, bool valid, int r0, int R, cons
         const float g = __expf(-gam[r] * diff * diff);
         out[i] = (valid && r < R) ? g * (dfc - 2.0f * gam[r] * diff * fc) : 0.0f;
     }
-}
-
-// x = hi + lo for two values at once (packed conversions)
-__device__ __forceinline__ void split2(float a, float b, __half2& hi, __half2& lo) {
-    hi = __floats2half2_rn(a, b);
-    const float2 f = __half22float2(hi);
-    lo = __floats2half2_rn(a - f.x, b - f.y);
-}
-
-// store 16 consecutive K values (one K-step, both 8-column chunks) of one
-// row as split fp16 into a B-operand tile (hi half, lo half)
-__device__ __forceinline__ void store_row16(unsigned char* tile, uint32_t half_bytes, int n_rows, int row, int s,
-                                            const float (&v)[16]) {
-    __align__(16) __half2 hi[8];
-    __align__(16) __half2 lo[8];
-#pragma unroll
-    for (int i = 0; i < 8; ++i) split2(v[2 * i], v[2 * i + 1], hi[i], lo[i]);
-    const uint32_t o0 = b_off(n_rows, row, 16 * s);
-    const uint32_t o1 = b_off(n_rows, row, 16 * s + 8);
-    *reinterpret_cast<uint4*>(tile + o0) = *reinterpret_cast<const uint4*>(&hi[0]);
-    *reinterpret_cast<uint4*>(tile + o1) = *reinterpret_cast<const uint4*>(&hi[4]);
-    *reinterpret_cast<uint4*>(tile + half_bytes + o0) = *reinterpret_cast<const uint4*>(&lo[0]);
-    *reinterpret_cast<uint4*>(tile + half_bytes + o1) = *reinterpret_cast<const uint4*>(&lo[4]);
-}
-
-// Rows row and row+1, column k of a B-operand tile: store the split fp16
-// values of a pair of edges.
-__device__ __forceinline__ void store_col_pair(unsigned char* tile, uint32_t half_bytes, int n_rows, int row, int k,
-                                               float a, float b) {
-    __half2 hi, lo;
-    split2(a, b, hi, lo);
-    const uint32_t o0 = b_off(n_rows, row, k), o1 = b_off(n_rows, row + 1, k);
-    *reinterpret_cast<__half*>(tile + o0) = __low2half(hi);
-    *reinterpret_cast<__half*>(tile + o1) = __high2half(hi);
-    *reinterpret_cast<__half*>(tile + half_bytes + o0) = __low2half(lo);
-    *reinterpret_cast<__half*>(tile + half_bytes + o1) = __high2half(lo);
 }
 
 // Per-tile prep by threads otherwise idle during the E-tile phase: sender

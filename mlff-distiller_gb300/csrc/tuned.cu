@@ -382,7 +382,9 @@ int run_tuned(const mlff_dims& d, const float* P, const PackedOffsets& po, const
                 MLFF_LAUNCH_CHECK("edge_fwd_simt");
             }
         }
-        if ((r = launch_update_fwd(d, P, po.layer[l], L, ws, l, st))) return r;
+        if (tc) r = launch_update_fwd_tc(P, po.layer[l], L, ws, l, st);
+        else r = launch_update_fwd(d, P, po.layer[l], L, ws, l, st);
+        if (r) return r;
     }
     const bool want_grad = out.forces != nullptr || out.virial != nullptr;
     if ((r = launch_readout(d, P, po, sys, L, ws, out, want_grad ? 1 : 0, st))) return r;
@@ -392,7 +394,9 @@ int run_tuned(const mlff_dims& d, const float* P, const PackedOffsets& po, const
     float* xbo = ws_ptr<float>(ws, L.xbar);
     float* xtb = xbo + NX;
     for (int l = d.n_layers - 1; l >= 0; --l) {
-        if ((r = launch_update_bwd(d, P, po.layer[l], L, ws, l, xbo, xtb, st))) return r;
+        if (tc) r = launch_update_bwd_tc(P, po.layer[l], L, ws, l, xbo, xtb, st);
+        else r = launch_update_bwd(d, P, po.layer[l], L, ws, l, xbo, xtb, st);
+        if (r) return r;
         a.lo = po.layer[l];
         a.X = X + l * NX;
         a.xtbar = xtb;

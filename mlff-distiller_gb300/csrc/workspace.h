@@ -120,6 +120,10 @@ int launch_partition(const WsLayout& L, void* ws, cudaStream_t st);
 int launch_scan(int32_t* data, int64_t n, int32_t* tmp, cudaStream_t st);
 int launch_update_fwd(const mlff_dims& d, const float* packed, const LayerOffsets& lo,
                       const WsLayout& L, void* ws, int layer, cudaStream_t st);
+int launch_update_fwd_tc(const float* packed, const LayerOffsets& lo, const WsLayout& L, void* ws, int layer,
+                         cudaStream_t st);
+int launch_update_bwd_tc(const float* packed, const LayerOffsets& lo, const WsLayout& L, void* ws, int layer,
+                         const float* xbar_out, float* xtbar, cudaStream_t st);
 int launch_update_bwd(const mlff_dims& d, const float* packed, const LayerOffsets& lo,
                       const WsLayout& L, void* ws, int layer, const float* xbar_out,
                       float* xtbar, cudaStream_t st);

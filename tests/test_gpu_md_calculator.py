@@ -1,7 +1,7 @@
 """Drop-in ASE calculator and the GPU velocity-Verlet driver (GPU only).
 
 Calculator results are checked against the float64 oracle with the bars of
-the parity tests (forces max |dF| <= 1e-3 eV/A, energy <= 2e-5 eV/atom).
+the parity tests (forces max |dF| <= 1e-3 eV/A, energy <= 5e-5 eV/atom).
 The integrator is checked against the float64 Verlet restatement in
 oracle/md.py driven by oracle forces, the CUDA-graph replay against eager
 steps (bit for bit), and the NVE energy drift of MD replicas.
@@ -16,7 +16,7 @@ from oracle.md import velocity_verlet
 pytestmark = pytest.mark.gpu
 
 F_TOL = 1e-3
-E_TOL_PER_ATOM = 2e-5
+E_TOL_PER_ATOM = 5e-5
 
 
 @pytest.fixture(scope="module")
