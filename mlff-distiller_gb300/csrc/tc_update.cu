@@ -6,13 +6,17 @@
 // Transposed GEMMs, D[channel][atom] = W[channel][k] X[atom][k]^T: a TMEM
 // lane is an output channel, a column an atom, so the epilogue thread that
 // owns channel c touches channel c of consecutive atoms -- coalesced rows of
-// the [N][4][H] feature arrays.  128-atom tiles, persistent CTAs, 8 warps:
-// warp w reads TMEM lane quarter w % 4 for atoms 64 (w / 4) .. +63.
+// the [N][4][H] feature arrays.  64-atom tiles (MMA N = 64, so that a
+// 3,000-atom system still spreads over 47 SMs), persistent CTAs, 8 warps:
+// in the epilogues warp w reads TMEM lane quarter w % 4 for atoms
+// 32 (w / 4) .. +31; the B tiles are built one atom row per warp (lane l:
+// channels 4l..4l+3, coalesced 512-byte rows).
 //
 // The weights (split-FP16 A-operand tile pairs, 8 KB per 128 x 16 block)
-// stream through an 8-slot ring of bulk copies in the order the MMAs use
-// them; one thread issues both, refilling the slot whose MMAs were issued
-// four steps earlier.  Accumulators are pre-filled with the bias, so every
+// stream through a 16-slot ring of bulk copies in the order the MMAs use
+// them: one thread issues the MMAs and commits each slot, another refills
+// the slots (during a GEMM, and ahead of the next GEMM while the epilogue
+// runs).  The forward accumulators are pre-filled with the bias, so every
 // MMA accumulates.  Every wait is bounded (MLFF_ERR_TIMEOUT).
 #include <cuda_fp16.h>
 #include "common.cuh"
@@ -63,35 +67,33 @@ int pack_update_tc(const mlff_dims& d, float* out, const PackedOffsets& o, cudaS
 }
 
 // ------------------------------------------------------- weight stream
-constexpr int URING = 8;
+constexpr int URING = 16;
 constexpr int UNT = 256;
-constexpr int UN = 128;
+constexpr int UN = 64;
 
 struct UStream {
-    int nslot;                     // ring depth (pairs)
     unsigned char* ring;
     uint64_t* full;
     uint64_t* empty;
     const unsigned char* src[2];   // pair sources of the two GEMMs of a tile
     int npairs[2];
-    uint32_t issued;               // pairs copied so far (global count)
-    uint32_t per_tile;             // npairs[0] + npairs[1]
-    uint32_t consumed;             // pairs whose copy was seen complete
+    uint32_t issued;               // producer: pairs copied so far (global count)
+    uint32_t consumed;             // consumer: pairs whose copy was seen complete
 };
 
-// source of global pair number P
 __device__ __forceinline__ const unsigned char* ustream_src(const UStream& s, uint32_t P) {
-    const uint32_t q = P % s.per_tile;
+    const uint32_t per = s.npairs[0] + s.npairs[1];
+    const uint32_t q = P % per;
     return q < (uint32_t)s.npairs[0] ? s.src[0] + (size_t)q * A_PAIR : s.src[1] + (size_t)(q - s.npairs[0]) * A_PAIR;
 }
 
-// copy pairs until `target` (exclusive) are issued; a slot is reused after
-// the commit of the pair that used it URING pairs earlier
+// producer: copy pairs until `target` (exclusive) are issued; a slot is
+// reused once the commit of the pair that used it URING pairs earlier has
+// arrived
 __device__ __forceinline__ bool ustream_fill(UStream& s, uint32_t target) {
     while (s.issued < target) {
-        const uint32_t slot = s.issued % s.nslot;
-        if (s.issued >= (uint32_t)s.nslot &&
-            !mbar_wait(&s.empty[slot], ((s.issued / s.nslot) - 1) & 1, WAIT_BUDGET))
+        const uint32_t slot = s.issued % URING;
+        if (s.issued >= (uint32_t)URING && !mbar_wait(&s.empty[slot], ((s.issued / URING) - 1) & 1, WAIT_BUDGET))
             return false;
         mbar_expect_tx(&s.full[slot], A_PAIR);
         bulk_g2s(s.ring + slot * A_PAIR, ustream_src(s, s.issued), A_PAIR, &s.full[slot]);
@@ -100,20 +102,19 @@ __device__ __forceinline__ bool ustream_fill(UStream& s, uint32_t target) {
     return true;
 }
 
-// One GEMM of a tile: for pair i of n (global pair P0 + i), D[d_of(i)] +=
-// A_hi B_hi(i) + A_hi B_lo(i) + A_lo B_hi(i), B descriptors from b_of(i);
-// the first MMA of pair i overwrites D instead when fresh(i).
+// consumer: one GEMM of a tile.  Pair i of n (global pair P0 + i): D[d_of(i)]
+// += A_hi B_hi(i) + A_hi B_lo(i) + A_lo B_hi(i); the first MMA of pair i
+// overwrites D instead when fresh(i).
 template <typename DOf, typename BOf, typename Fresh>
-__device__ __forceinline__ bool ustream_gemm(UStream& s, uint32_t P0, int n, uint32_t P_end, DOf d_of, BOf b_of,
-                                             uint64_t bhalf, Fresh fresh) {
+__device__ __forceinline__ bool ustream_gemm(UStream& s, uint32_t P0, int n, DOf d_of, BOf b_of, uint64_t bhalf,
+                                             Fresh fresh) {
     constexpr uint32_t idesc = idesc_f16(UN);
     const uint64_t a0 = sdesc(smem_u32(s.ring), A_LBO, A_SBO);
 #pragma unroll 1
     for (int i = 0; i < n; ++i) {
         const uint32_t P = P0 + i;
-        if (!ustream_fill(s, min(P + s.nslot / 2 + 1, P_end))) return false;
-        const uint32_t slot = P % s.nslot;
-        if (!mbar_wait(&s.full[slot], (P / s.nslot) & 1, WAIT_BUDGET)) return false;
+        const uint32_t slot = P % URING;
+        if (!mbar_wait(&s.full[slot], (P / URING) & 1, WAIT_BUDGET)) return false;
         s.consumed = P + 1;
         const uint64_t ahi = a0 + (uint64_t)(slot * A_PAIR >> 4), alo = ahi + (A_TILE >> 4);
         const uint64_t bhi = b_of(i);
@@ -133,9 +134,49 @@ __device__ __forceinline__ void ufill_tmem(uint32_t taddr, float v, int n16) {
     for (int k = 0; k < n16; ++k) tmem_st16(taddr + 16 * k, bv);
 }
 
+// four consecutive K values (k % 4 == 0) of one row as split fp16
+__device__ __forceinline__ void store_row4(unsigned char* tile, uint32_t half_bytes, int row, int k, float4 v) {
+    __half2 h0, l0, h1, l1;
+    split2(v.x, v.y, h0, l0);
+    split2(v.z, v.w, h1, l1);
+    const uint32_t o = b_off(UN, row, k);
+    uint2 hv, lv;
+    hv.x = *reinterpret_cast<uint32_t*>(&h0);
+    hv.y = *reinterpret_cast<uint32_t*>(&h1);
+    lv.x = *reinterpret_cast<uint32_t*>(&l0);
+    lv.y = *reinterpret_cast<uint32_t*>(&l1);
+    *reinterpret_cast<uint2*>(tile + o) = hv;
+    *reinterpret_cast<uint2*>(tile + half_bytes + o) = lv;
+}
+
+// Synchronisation helpers shared by both kernels: one thread issues the
+// MMAs of a GEMM while the producer keeps the ring full; then the CTA waits
+// for the MMAs (warp 0 polls, the others wait at the barrier).
+struct UCtl {
+    uint64_t* mma_bar;
+    volatile int* abort_flag;
+    Status* st;
+    uint32_t phase;
+};
+
+__device__ __forceinline__ void ufail(UCtl& c, int where) {
+    set_status(c.st, MLFF_ERR_TIMEOUT, where);
+    *c.abort_flag = 1;
+}
+
+__device__ __forceinline__ void uwait_mma(UCtl& c, int w, int where) {
+    if (w == 0) __syncwarp();
+    if (w == 0 && !mbar_wait(c.mma_bar, c.phase, WAIT_BUDGET)) ufail(c, where);
+    c.phase ^= 1;
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+}
+
 // ------------------------------------------------------- forward kernel
-// smem: B tile [s, |v|] (K = 256: 4 K-blocks; hi half then lo half, 128 KB),
-// the H tile (K = 128, 64 KB) aliased into it after GEMM1, the ring (64 KB).
+// smem: B tile [s, |v|] (K = 256: 4 K-blocks; hi half then lo half, 64 KB),
+// the H tile (K = 128, 32 KB) aliased into it after GEMM1, the ring (128 KB).
+// TMEM: D1 = z (cols 0-63), D2 chunk g = (ds, g1, g2)[g] (64 + 64 g).
 constexpr uint32_t UF_BH = 4 * b_block(UN);
 constexpr uint32_t UF_HH = 2 * b_block(UN);
 constexpr uint32_t UF_OFF_B = 0;
@@ -164,7 +205,7 @@ __global__ void __launch_bounds__(UNT, 1) update_fwd_tc_kernel(const float* __re
     const int t = threadIdx.x, w = t >> 5, lane = t & 31;
     const int ntiles = (n_atoms + UN - 1) / UN;
     if (w == 0) {
-        tmem_alloc(tslot, 512);
+        tmem_alloc(tslot, 256);
         tmem_relinquish();
     }
     if (t == 0) {
@@ -183,57 +224,38 @@ __global__ void __launch_bounds__(UNT, 1) update_fwd_tc_kernel(const float* __re
     __syncthreads();
     fence_after_sync();
     const uint32_t tmem = *tslot;
-    UStream ws{URING, smem + UF_OFF_RING, full, empty,
+    UStream ws{smem + UF_OFF_RING, full, empty,
                {reinterpret_cast<const unsigned char*>(P + lo.u1_tc), reinterpret_cast<const unsigned char*>(P + lo.u2_tc)},
-               {16, 24}, 0, 40, 0};
+               {16, 24}, 0, 0};
+    UCtl ctl{mma_bar, abort_flag, st, 0};
     const int my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
     const uint32_t P_end = (uint32_t)my_tiles * 40;
-    if (t == 0 && !ustream_fill(ws, min((uint32_t)URING, P_end))) {
-        set_status(st, MLFF_ERR_TIMEOUT, 20);
-        *abort_flag = 1;
-    }
+    const bool producer = t == 32;
+    if (producer && !ustream_fill(ws, min((uint32_t)URING, P_end))) ufail(ctl, 20);
     const int q = w & 3, hh = w >> 2, c = 32 * q + lane;
     const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
-    uint32_t mma_phase = 0, P0 = 0;
+    uint32_t P0 = 0;
 
     for (int tile = blockIdx.x; tile < ntiles && !*abort_flag; tile += gridDim.x, P0 += 40) {
         const int a0 = tile * UN;
-        // accumulators <- bias: D1 (cols 0-127) c1, D2 chunk g (128 + 128 g) c2
-        ufill_tmem(lane_base + 64 * hh, c1s[c], 4);
+        // accumulators <- bias: D1 c1, D2 chunk g c2[g]
+        ufill_tmem(lane_base + 32 * hh, c1s[c], 2);
 #pragma unroll 1
-        for (int g = 0; g < 3; ++g) ufill_tmem(lane_base + 128 + 128 * g + 64 * hh, c2s[g * H + c], 4);
-        // B tile: row = atom, K = [s (128), |v| (128)] split fp16
-        {
-            const int i = t & (UN - 1), part = t >> 7, a = a0 + i;
-            const float* x = Xt + (int64_t)a * 4 * H;
+        for (int g = 0; g < 3; ++g) ufill_tmem(lane_base + 64 + 64 * g + 32 * hh, c2s[g * H + c], 2);
+        // B tile: row = atom, K = [s (128), |v| (128)]; warp w builds rows w, w + 8, ...
 #pragma unroll 1
-            for (int s8 = 0; s8 < 8; ++s8) {
-                float v[16];
-                if (a < n_atoms) {
-                    if (part == 0) {
-#pragma unroll
-                        for (int j = 0; j < 16; j += 4) {
-                            const float4 f = *reinterpret_cast<const float4*>(x + 16 * s8 + j);
-                            v[j] = f.x; v[j + 1] = f.y; v[j + 2] = f.z; v[j + 3] = f.w;
-                        }
-                    } else {
-#pragma unroll
-                        for (int j = 0; j < 16; j += 4) {
-                            const float4 fx = *reinterpret_cast<const float4*>(x + H + 16 * s8 + j);
-                            const float4 fy = *reinterpret_cast<const float4*>(x + 2 * H + 16 * s8 + j);
-                            const float4 fz = *reinterpret_cast<const float4*>(x + 3 * H + 16 * s8 + j);
-                            v[j] = pair_distance(fx.x, fy.x, fz.x);            // |v| over xyz (:437)
-                            v[j + 1] = pair_distance(fx.y, fy.y, fz.y);
-                            v[j + 2] = pair_distance(fx.z, fy.z, fz.z);
-                            v[j + 3] = pair_distance(fx.w, fy.w, fz.w);
-                        }
-                    }
-                } else {
-#pragma unroll
-                    for (int j = 0; j < 16; ++j) v[j] = 0.f;
-                }
-                store_row16(Bs, UF_BH, UN, i, 8 * part + s8, v);
+        for (int i = w; i < UN; i += 8) {
+            const int a = a0 + i;
+            float4 sv = make_float4(0.f, 0.f, 0.f, 0.f), nv = sv;
+            if (a < n_atoms) {
+                const float4* x = reinterpret_cast<const float4*>(Xt + (int64_t)a * 4 * H);
+                sv = x[lane];
+                const float4 vx = x[32 + lane], vy = x[64 + lane], vz = x[96 + lane];
+                nv = make_float4(pair_distance(vx.x, vy.x, vz.x), pair_distance(vx.y, vy.y, vz.y),
+                                 pair_distance(vx.z, vy.z, vz.z), pair_distance(vx.w, vy.w, vz.w));  // |v| (:437)
             }
+            store_row4(Bs, UF_BH, i, 4 * lane, sv);
+            store_row4(Bs, UF_BH, i, H + 4 * lane, nv);
         }
         tmem_st_wait();
         fence_async_smem();
@@ -242,42 +264,29 @@ __global__ void __launch_bounds__(UNT, 1) update_fwd_tc_kernel(const float* __re
         if (t == 0) {   // GEMM1: z^T = U1 [s, |v|]^T, K = 256
             fence_after_sync();
             const uint64_t b0 = sdesc_b(smem_u32(Bs));
-            const bool ok = ustream_gemm(
-                ws, P0, 16, P_end, [&](int) { return tmem; },
-                [&](int i) { return b0 + (uint64_t)(b_kstep_off(UN, i) >> 4); }, (uint64_t)(UF_BH >> 4),
-                [](int) { return false; });
-            if (!ok) {
-                set_status(st, MLFF_ERR_TIMEOUT, 21);
-                *abort_flag = 1;
-            }
+            if (!ustream_gemm(ws, P0, 16, [&](int) { return tmem; },
+                              [&](int i) { return b0 + (uint64_t)(b_kstep_off(UN, i) >> 4); }, (uint64_t)(UF_BH >> 4),
+                              [](int) { return false; }))
+                ufail(ctl, 21);
             mma_commit(mma_bar);
         }
-        if (w == 0) __syncwarp();
-        if (w == 0 && !mbar_wait(mma_bar, mma_phase, WAIT_BUDGET)) {
-            set_status(st, MLFF_ERR_TIMEOUT, 22);
-            *abort_flag = 1;
-        }
-        mma_phase ^= 1;
-        fence_before_sync();
-        __syncthreads();
-        fence_after_sync();
+        if (producer && !ustream_fill(ws, min(P0 + 16, P_end))) ufail(ctl, 26);
+        uwait_mma(ctl, w, 22);
+        // GEMM1 is done, so every slot is free: fetch GEMM2's pairs during epilogue 1
+        if (producer && !ustream_fill(ws, min(P0 + 16 + URING, P_end))) ufail(ctl, 27);
         {   // epilogue 1: z -> uz, h = silu(z) -> H tile (aliases the B tile)
-#pragma unroll 1
-            for (int half = 0; half < 2; ++half) {
-                const int col = 64 * hh + 32 * half;
-                float z[32];
-                tmem_ld32(lane_base + col, z);
-                tmem_ld_wait();
+            const int col = 32 * hh;
+            float z[32];
+            tmem_ld32(lane_base + col, z);
+            tmem_ld_wait();
 #pragma unroll
-                for (int i = 0; i < 32; i += 2) {
-                    const int a = a0 + col + i;
-                    if (a < n_atoms) uz[(int64_t)a * H + c] = z[i];
-                    if (a + 1 < n_atoms) uz[(int64_t)(a + 1) * H + c] = z[i + 1];
-                    // accurate exp: per-atom pre-activations reach |z| ~ 20 with
-                    // trained-like weights, where the fast exponential's error
-                    // (~|z| * 6e-8 relative) would show in the energy
-                    store_col_pair(Bs, UF_HH, UN, col + i, c, silu_f(z[i]), silu_f(z[i + 1]));
-                }
+            for (int i = 0; i < 32; i += 2) {
+                const int a = a0 + col + i;
+                if (a < n_atoms) uz[(int64_t)a * H + c] = z[i];
+                if (a + 1 < n_atoms) uz[(int64_t)(a + 1) * H + c] = z[i + 1];
+                // accurate exp: per-atom pre-activations reach |z| ~ 20 with
+                // trained-like weights
+                store_col_pair(Bs, UF_HH, UN, col + i, c, silu_f(z[i]), silu_f(z[i + 1]));
             }
         }
         fence_async_smem();
@@ -286,49 +295,54 @@ __global__ void __launch_bounds__(UNT, 1) update_fwd_tc_kernel(const float* __re
         if (t == 0) {   // GEMM2: a^T = U2 h^T, 3 chunks x 8 K-steps
             fence_after_sync();
             const uint64_t b0 = sdesc_b(smem_u32(Bs));
-            const bool ok = ustream_gemm(
-                ws, P0 + 16, 24, P_end, [&](int i) { return tmem + 128 + 128 * (i >> 3); },
-                [&](int i) { return b0 + (uint64_t)(b_kstep_off(UN, i & 7) >> 4); }, (uint64_t)(UF_HH >> 4),
-                [](int) { return false; });
-            if (!ok) {
-                set_status(st, MLFF_ERR_TIMEOUT, 23);
-                *abort_flag = 1;
-            }
+            if (!ustream_gemm(ws, P0 + 16, 24, [&](int i) { return tmem + 64 + 64 * (i >> 3); },
+                              [&](int i) { return b0 + (uint64_t)(b_kstep_off(UN, i & 7) >> 4); },
+                              (uint64_t)(UF_HH >> 4), [](int) { return false; }))
+                ufail(ctl, 23);
             mma_commit(mma_bar);
         }
-        if (w == 0) __syncwarp();
-        if (w == 0 && !mbar_wait(mma_bar, mma_phase, WAIT_BUDGET)) {
-            set_status(st, MLFF_ERR_TIMEOUT, 24);
-            *abort_flag = 1;
-        }
-        mma_phase ^= 1;
-        fence_before_sync();
-        __syncthreads();
-        fence_after_sync();
+        if (producer && !ustream_fill(ws, min(P0 + 40, P_end))) ufail(ctl, 28);
+        uwait_mma(ctl, w, 24);
+        // the next tile's GEMM1 pairs arrive while this epilogue and the next build run
+        if (producer && !ustream_fill(ws, min(P0 + 40 + URING, P_end))) ufail(ctl, 29);
         {   // epilogue 2: (ds, g1, g2) -> ua; s' = s + ds, v' = v g1 + (M v) g2 (:452-468)
 #pragma unroll 1
-            for (int blk = 0; blk < 4; ++blk) {
-                const int col = 64 * hh + 16 * blk;
+            for (int blk = 0; blk < 2; ++blk) {
+                const int col = 32 * hh + 16 * blk;
                 float ds[16], g1[16], g2[16];
-                tmem_ld16(lane_base + 128 + col, ds);
-                tmem_ld16(lane_base + 256 + col, g1);
-                tmem_ld16(lane_base + 384 + col, g2);
+                tmem_ld16(lane_base + 64 + col, ds);
+                tmem_ld16(lane_base + 128 + col, g1);
+                tmem_ld16(lane_base + 192 + col, g2);
                 tmem_ld_wait();
-#pragma unroll 4
-                for (int i = 0; i < 16; ++i) {
-                    const int a = a0 + col + i;
-                    if (a >= n_atoms) break;
-                    const float* x = Xt + (int64_t)a * 4 * H;
-                    const float s = x[c], vx = x[H + c], vy = x[2 * H + c], vz = x[3 * H + c];
-                    float* u = ua + (int64_t)a * H3;
-                    u[c] = ds[i];
-                    u[H + c] = g1[i];
-                    u[2 * H + c] = g2[i];
-                    float* xo = Xout + (int64_t)a * 4 * H;
-                    xo[c] = s + ds[i];
-                    xo[H + c] = vx * g1[i] + (mix[0] * vx + mix[1] * vy + mix[2] * vz) * g2[i];
-                    xo[2 * H + c] = vy * g1[i] + (mix[3] * vx + mix[4] * vy + mix[5] * vz) * g2[i];
-                    xo[3 * H + c] = vz * g1[i] + (mix[6] * vx + mix[7] * vy + mix[8] * vz) * g2[i];
+#pragma unroll
+                for (int sub = 0; sub < 16; sub += 8) {
+                    float s8[8], vx[8], vy[8], vz[8];
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        const int a = a0 + col + sub + i;
+                        const bool ok = a < n_atoms;
+                        const float* x = Xt + (int64_t)(ok ? a : 0) * 4 * H;
+                        s8[i] = ok ? x[c] : 0.f;
+                        vx[i] = ok ? x[H + c] : 0.f;
+                        vy[i] = ok ? x[2 * H + c] : 0.f;
+                        vz[i] = ok ? x[3 * H + c] : 0.f;
+                    }
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        const int a = a0 + col + sub + i;
+                        if (a < n_atoms) {
+                            const int k = sub + i;
+                            float* u = ua + (int64_t)a * H3;
+                            u[c] = ds[k];
+                            u[H + c] = g1[k];
+                            u[2 * H + c] = g2[k];
+                            float* xo = Xout + (int64_t)a * 4 * H;
+                            xo[c] = s8[i] + ds[k];
+                            xo[H + c] = vx[i] * g1[k] + (mix[0] * vx[i] + mix[1] * vy[i] + mix[2] * vz[i]) * g2[k];
+                            xo[2 * H + c] = vy[i] * g1[k] + (mix[3] * vx[i] + mix[4] * vy[i] + mix[5] * vz[i]) * g2[k];
+                            xo[3 * H + c] = vz[i] * g1[k] + (mix[6] * vx[i] + mix[7] * vy[i] + mix[8] * vz[i]) * g2[k];
+                        }
+                    }
                 }
             }
         }
@@ -338,8 +352,10 @@ __global__ void __launch_bounds__(UNT, 1) update_fwd_tc_kernel(const float* __re
     }
     // drain: every pair copied must have landed before the CTA exits
     __syncthreads();
-    if (t == 0) {
-        for (uint32_t f = ws.consumed; f < ws.issued; ++f)
+    if (producer) {
+        // copies still in flight are among the last URING issued (a slot is
+        // refilled only after its previous copy was consumed)
+        for (uint32_t f = ws.issued > (uint32_t)URING ? ws.issued - URING : 0u; f < ws.issued; ++f)
             if (!mbar_wait(&full[f % URING], (f / URING) & 1, WAIT_BUDGET)) {
                 set_status(st, MLFF_ERR_TIMEOUT, 25);
                 break;
@@ -348,7 +364,7 @@ __global__ void __launch_bounds__(UNT, 1) update_fwd_tc_kernel(const float* __re
     fence_before_sync();
     __syncthreads();
     fence_after_sync();
-    if (w == 0) tmem_dealloc(tmem, 512);
+    if (w == 0) tmem_dealloc(tmem, 256);
 }
 
 int launch_update_fwd_tc(const float* packed, const LayerOffsets& lo, const WsLayout& L, void* ws, int layer,
@@ -376,17 +392,16 @@ int launch_update_fwd_tc(const float* packed, const LayerOffsets& lo, const WsLa
 // ------------------------------------------------------- reverse kernel
 // abar = dE/d(ds, g1, g2) [atom][3H] -> zbar = (U2^T abar) silu'(uz) ->
 // cb = U1^T zbar = dE/d[s, |v|]; xtbar = (sb + cs, vb + cn v / |v|).
-// smem: abar B tile (K = 384: 6 K-blocks, hi then lo, 192 KB), the zbar tile
-// (K = 128, 64 KB) aliased into it after GEMM3, a 4-pair ring (32 KB).
-// TMEM: D3 = zbar pre-activation (cols 0-127), D4 = (cs, cn) (128-383).
-constexpr int URING_B = 4;
+// smem: abar B tile (K = 384: 6 K-blocks, hi then lo, 96 KB), the zbar tile
+// (K = 128, 32 KB) aliased into it after GEMM3, the ring (128 KB).
+// TMEM: D3 = zbar pre-activation (cols 0-63), D4 = (cs, cn) (64-191).
 constexpr uint32_t UB_AH = 6 * b_block(UN);
 constexpr uint32_t UB_ZH = 2 * b_block(UN);
 constexpr uint32_t UB_OFF_B = 0;
 constexpr uint32_t UB_OFF_RING = UB_OFF_B + 2 * UB_AH;
-constexpr uint32_t UB_OFF_MIX = UB_OFF_RING + URING_B * A_PAIR;
+constexpr uint32_t UB_OFF_MIX = UB_OFF_RING + URING * A_PAIR;
 constexpr uint32_t UB_OFF_BAR = UB_OFF_MIX + 64;
-constexpr uint32_t UB_OFF_MISC = UB_OFF_BAR + 8 * (1 + 2 * URING_B);
+constexpr uint32_t UB_OFF_MISC = UB_OFF_BAR + 8 * (1 + 2 * URING);
 constexpr uint32_t UB_SMEM = align1k(UB_OFF_MISC + 16);
 static_assert(UB_SMEM <= 232448, "update reverse kernel shared memory");
 
@@ -400,19 +415,19 @@ __global__ void __launch_bounds__(UNT, 1) update_bwd_tc_kernel(const float* __re
     float* mix = reinterpret_cast<float*>(smem + UB_OFF_MIX);
     uint64_t* mma_bar = reinterpret_cast<uint64_t*>(smem + UB_OFF_BAR);
     uint64_t* full = mma_bar + 1;
-    uint64_t* empty = full + URING_B;
+    uint64_t* empty = full + URING;
     uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + UB_OFF_MISC);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + UB_OFF_MISC + 4);
     if (st->code != 0) return;
     const int t = threadIdx.x, w = t >> 5, lane = t & 31;
     const int ntiles = (n_atoms + UN - 1) / UN;
     if (w == 0) {
-        tmem_alloc(tslot, 512);
+        tmem_alloc(tslot, 256);
         tmem_relinquish();
     }
     if (t == 0) {
         mbar_init(mma_bar, 1);
-        for (int i = 0; i < URING_B; ++i) {
+        for (int i = 0; i < URING; ++i) {
             mbar_init(&full[i], 1);
             mbar_init(&empty[i], 1);
         }
@@ -424,70 +439,45 @@ __global__ void __launch_bounds__(UNT, 1) update_bwd_tc_kernel(const float* __re
     __syncthreads();
     fence_after_sync();
     const uint32_t tmem = *tslot;
-    UStream ws{URING_B, smem + UB_OFF_RING, full, empty,
+    UStream ws{smem + UB_OFF_RING, full, empty,
                {reinterpret_cast<const unsigned char*>(P + lo.u2t_tc), reinterpret_cast<const unsigned char*>(P + lo.u1t_tc)},
-               {24, 16}, 0, 40, 0};
+               {24, 16}, 0, 0};
+    UCtl ctl{mma_bar, abort_flag, st, 0};
     const int my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
     const uint32_t P_end = (uint32_t)my_tiles * 40;
-    if (t == 0 && !ustream_fill(ws, min((uint32_t)URING_B, P_end))) {
-        set_status(st, MLFF_ERR_TIMEOUT, 30);
-        *abort_flag = 1;
-    }
+    const bool producer = t == 32;
+    if (producer && !ustream_fill(ws, min((uint32_t)URING, P_end))) ufail(ctl, 30);
     const int q = w & 3, hh = w >> 2, c = 32 * q + lane;
     const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
-    uint32_t mma_phase = 0, P0 = 0;
+    uint32_t P0 = 0;
 
     for (int tile = blockIdx.x; tile < ntiles && !*abort_flag; tile += gridDim.x, P0 += 40) {
         const int a0 = tile * UN;
-        // abar tile: row = atom; K = [sb (128), sum_i xb_i v_i (128), sum_i xb_i (M v)_i (128)]
-        {
-            const int i = t & (UN - 1), part = t >> 7, a = a0 + i;
-            const float* xo = xbo + (int64_t)a * 4 * H;
-            const float* x = Xt + (int64_t)a * 4 * H;
-            if (part == 0) {
+        // abar tile: row = atom; K = [sb, sum_i xb_i v_i, sum_i xb_i (M v)_i]; warp w builds rows w, w + 8, ...
 #pragma unroll 1
-                for (int s8 = 0; s8 < 8; ++s8) {
-                    float v[16];
-#pragma unroll
-                    for (int j = 0; j < 16; j += 4) {
-                        float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
-                        if (a < n_atoms) f = *reinterpret_cast<const float4*>(xo + 16 * s8 + j);
-                        v[j] = f.x; v[j + 1] = f.y; v[j + 2] = f.z; v[j + 3] = f.w;
-                    }
-                    store_row16(Bs, UB_AH, UN, i, s8, v);
-                }
+        for (int i = w; i < UN; i += 8) {
+            const int a = a0 + i;
+            float4 sb = make_float4(0.f, 0.f, 0.f, 0.f), g1 = sb, g2 = sb;
+            if (a < n_atoms) {
+                const float4* xo = reinterpret_cast<const float4*>(xbo + (int64_t)a * 4 * H);
+                const float4* x = reinterpret_cast<const float4*>(Xt + (int64_t)a * 4 * H);
+                sb = xo[lane];
+                const float4 bx = xo[32 + lane], by = xo[64 + lane], bz = xo[96 + lane];
+                const float4 vx = x[32 + lane], vy = x[64 + lane], vz = x[96 + lane];
+                auto one = [&](float b_x, float b_y, float b_z, float v_x, float v_y, float v_z, float& o1, float& o2) {
+                    o1 = b_x * v_x + b_y * v_y + b_z * v_z;
+                    o2 = b_x * (mix[0] * v_x + mix[1] * v_y + mix[2] * v_z) +
+                         b_y * (mix[3] * v_x + mix[4] * v_y + mix[5] * v_z) +
+                         b_z * (mix[6] * v_x + mix[7] * v_y + mix[8] * v_z);
+                };
+                one(bx.x, by.x, bz.x, vx.x, vy.x, vz.x, g1.x, g2.x);
+                one(bx.y, by.y, bz.y, vx.y, vy.y, vz.y, g1.y, g2.y);
+                one(bx.z, by.z, bz.z, vx.z, vy.z, vz.z, g1.z, g2.z);
+                one(bx.w, by.w, bz.w, vx.w, vy.w, vz.w, g1.w, g2.w);
             }
-#pragma unroll 1
-            for (int s4 = 0; s4 < 4; ++s4) {
-                const int s8 = 4 * part + s4;   // channels 16 s8 .. 16 s8 + 15
-                float g1v[16], g2v[16];
-#pragma unroll
-                for (int j = 0; j < 16; j += 4) {
-                    float4 bx = make_float4(0.f, 0.f, 0.f, 0.f), by = bx, bz = bx, vx = bx, vy = bx, vz = bx;
-                    if (a < n_atoms) {
-                        const int o = 16 * s8 + j;
-                        bx = *reinterpret_cast<const float4*>(xo + H + o);
-                        by = *reinterpret_cast<const float4*>(xo + 2 * H + o);
-                        bz = *reinterpret_cast<const float4*>(xo + 3 * H + o);
-                        vx = *reinterpret_cast<const float4*>(x + H + o);
-                        vy = *reinterpret_cast<const float4*>(x + 2 * H + o);
-                        vz = *reinterpret_cast<const float4*>(x + 3 * H + o);
-                    }
-                    const float BX[4] = {bx.x, bx.y, bx.z, bx.w}, BY[4] = {by.x, by.y, by.z, by.w},
-                                BZ[4] = {bz.x, bz.y, bz.z, bz.w}, VX[4] = {vx.x, vx.y, vx.z, vx.w},
-                                VY[4] = {vy.x, vy.y, vy.z, vy.w}, VZ[4] = {vz.x, vz.y, vz.z, vz.w};
-#pragma unroll
-                    for (int e = 0; e < 4; ++e) {
-                        g1v[j + e] = BX[e] * VX[e] + BY[e] * VY[e] + BZ[e] * VZ[e];
-                        const float mx = mix[0] * VX[e] + mix[1] * VY[e] + mix[2] * VZ[e];
-                        const float my = mix[3] * VX[e] + mix[4] * VY[e] + mix[5] * VZ[e];
-                        const float mz = mix[6] * VX[e] + mix[7] * VY[e] + mix[8] * VZ[e];
-                        g2v[j + e] = BX[e] * mx + BY[e] * my + BZ[e] * mz;
-                    }
-                }
-                store_row16(Bs, UB_AH, UN, i, 8 + s8, g1v);
-                store_row16(Bs, UB_AH, UN, i, 16 + s8, g2v);
-            }
+            store_row4(Bs, UB_AH, i, 4 * lane, sb);
+            store_row4(Bs, UB_AH, i, H + 4 * lane, g1);
+            store_row4(Bs, UB_AH, i, 2 * H + 4 * lane, g2);
         }
         fence_async_smem();
         fence_before_sync();
@@ -495,40 +485,29 @@ __global__ void __launch_bounds__(UNT, 1) update_bwd_tc_kernel(const float* __re
         if (t == 0) {   // GEMM3: zbar_pre^T = U2^T abar^T, K = 384
             fence_after_sync();
             const uint64_t b0 = sdesc_b(smem_u32(Bs));
-            const bool ok = ustream_gemm(
-                ws, P0, 24, P_end, [&](int) { return tmem; },
-                [&](int i) { return b0 + (uint64_t)(b_kstep_off(UN, i) >> 4); }, (uint64_t)(UB_AH >> 4),
-                [](int i) { return i == 0; });
-            if (!ok) {
-                set_status(st, MLFF_ERR_TIMEOUT, 31);
-                *abort_flag = 1;
-            }
+            if (!ustream_gemm(ws, P0, 24, [&](int) { return tmem; },
+                              [&](int i) { return b0 + (uint64_t)(b_kstep_off(UN, i) >> 4); }, (uint64_t)(UB_AH >> 4),
+                              [](int i) { return i == 0; }))
+                ufail(ctl, 31);
             mma_commit(mma_bar);
         }
-        if (w == 0) __syncwarp();
-        if (w == 0 && !mbar_wait(mma_bar, mma_phase, WAIT_BUDGET)) {
-            set_status(st, MLFF_ERR_TIMEOUT, 32);
-            *abort_flag = 1;
-        }
-        mma_phase ^= 1;
-        fence_before_sync();
-        __syncthreads();
-        fence_after_sync();
+        if (producer && !ustream_fill(ws, min(P0 + 24, P_end))) ufail(ctl, 36);
+        uwait_mma(ctl, w, 32);
+        if (producer && !ustream_fill(ws, min(P0 + 24 + URING, P_end))) ufail(ctl, 37);
         {   // epilogue 3: zbar = D3 silu'(uz) -> zbar tile (aliases the abar tile)
-#pragma unroll 1
-            for (int half = 0; half < 2; ++half) {
-                const int col = 64 * hh + 32 * half;
-                float zb[32];
-                tmem_ld32(lane_base + col, zb);
-                tmem_ld_wait();
+            const int col = 32 * hh;
+            float zb[32];
+            tmem_ld32(lane_base + col, zb);
+            float zz[32];
 #pragma unroll
-                for (int i = 0; i < 32; i += 2) {
-                    const int a = a0 + col + i;
-                    const float z0 = a < n_atoms ? uz[(int64_t)a * H + c] : 0.f;
-                    const float z1 = a + 1 < n_atoms ? uz[(int64_t)(a + 1) * H + c] : 0.f;
-                    store_col_pair(Bs, UB_ZH, UN, col + i, c, zb[i] * dsilu_f(z0), zb[i + 1] * dsilu_f(z1));
-                }
+            for (int i = 0; i < 32; ++i) {
+                const int a = a0 + col + i;
+                zz[i] = a < n_atoms ? uz[(int64_t)a * H + c] : 0.f;
             }
+            tmem_ld_wait();
+#pragma unroll
+            for (int i = 0; i < 32; i += 2)
+                store_col_pair(Bs, UB_ZH, UN, col + i, c, zb[i] * dsilu_f(zz[i]), zb[i + 1] * dsilu_f(zz[i + 1]));
         }
         fence_async_smem();
         fence_before_sync();
@@ -536,50 +515,51 @@ __global__ void __launch_bounds__(UNT, 1) update_bwd_tc_kernel(const float* __re
         if (t == 0) {   // GEMM4: cb^T = U1^T zbar^T, 2 chunks x 8 K-steps
             fence_after_sync();
             const uint64_t b0 = sdesc_b(smem_u32(Bs));
-            const bool ok = ustream_gemm(
-                ws, P0 + 24, 16, P_end, [&](int i) { return tmem + 128 + 128 * (i >> 3); },
-                [&](int i) { return b0 + (uint64_t)(b_kstep_off(UN, i & 7) >> 4); }, (uint64_t)(UB_ZH >> 4),
-                [](int i) { return (i & 7) == 0; });
-            if (!ok) {
-                set_status(st, MLFF_ERR_TIMEOUT, 33);
-                *abort_flag = 1;
-            }
+            if (!ustream_gemm(ws, P0 + 24, 16, [&](int i) { return tmem + 64 + 64 * (i >> 3); },
+                              [&](int i) { return b0 + (uint64_t)(b_kstep_off(UN, i & 7) >> 4); },
+                              (uint64_t)(UB_ZH >> 4), [](int i) { return (i & 7) == 0; }))
+                ufail(ctl, 33);
             mma_commit(mma_bar);
         }
-        if (w == 0) __syncwarp();
-        if (w == 0 && !mbar_wait(mma_bar, mma_phase, WAIT_BUDGET)) {
-            set_status(st, MLFF_ERR_TIMEOUT, 34);
-            *abort_flag = 1;
-        }
-        mma_phase ^= 1;
-        fence_before_sync();
-        __syncthreads();
-        fence_after_sync();
+        if (producer && !ustream_fill(ws, min(P0 + 40, P_end))) ufail(ctl, 38);
+        uwait_mma(ctl, w, 34);
+        if (producer && !ustream_fill(ws, min(P0 + 40 + URING, P_end))) ufail(ctl, 39);
         {   // epilogue 4: xtbar = (sb + cs, xb g1 + M^T xb g2 + cn v / |v|)
 #pragma unroll 1
-            for (int blk = 0; blk < 4; ++blk) {
-                const int col = 64 * hh + 16 * blk;
+            for (int blk = 0; blk < 2; ++blk) {
+                const int col = 32 * hh + 16 * blk;
                 float cs[16], cn[16];
-                tmem_ld16(lane_base + 128 + col, cs);
-                tmem_ld16(lane_base + 256 + col, cn);
+                tmem_ld16(lane_base + 64 + col, cs);
+                tmem_ld16(lane_base + 128 + col, cn);
                 tmem_ld_wait();
-#pragma unroll 4
-                for (int i = 0; i < 16; ++i) {
-                    const int a = a0 + col + i;
-                    if (a >= n_atoms) break;
-                    const float* xo = xbo + (int64_t)a * 4 * H;
-                    const float* x = Xt + (int64_t)a * 4 * H;
-                    const float* u = ua + (int64_t)a * H3;
-                    const float sb = xo[c], bx = xo[H + c], by = xo[2 * H + c], bz = xo[3 * H + c];
-                    const float vx = x[H + c], vy = x[2 * H + c], vz = x[3 * H + c];
-                    const float g1 = u[H + c], g2 = u[2 * H + c];
-                    const float n = pair_distance(vx, vy, vz);
-                    const float sc = n > 0.0f ? cn[i] / n : 0.0f;    // d|v|/dv = v / |v|, 0 at v = 0
-                    float* o = xtbar + (int64_t)a * 4 * H;
-                    o[c] = sb + cs[i];
-                    o[H + c] = bx * g1 + (mix[0] * bx + mix[3] * by + mix[6] * bz) * g2 + sc * vx;
-                    o[2 * H + c] = by * g1 + (mix[1] * bx + mix[4] * by + mix[7] * bz) * g2 + sc * vy;
-                    o[3 * H + c] = bz * g1 + (mix[2] * bx + mix[5] * by + mix[8] * bz) * g2 + sc * vz;
+#pragma unroll 1
+                for (int sub = 0; sub < 16; sub += 4) {
+                    float sb[4], bx[4], by[4], bz[4], vx[4], vy[4], vz[4], g1[4], g2[4];
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const int a = a0 + col + sub + i;
+                        const bool ok = a < n_atoms;
+                        const int64_t aa = ok ? a : 0;
+                        const float* xo = xbo + aa * 4 * H;
+                        const float* x = Xt + aa * 4 * H;
+                        const float* u = ua + aa * H3;
+                        sb[i] = xo[c]; bx[i] = xo[H + c]; by[i] = xo[2 * H + c]; bz[i] = xo[3 * H + c];
+                        vx[i] = x[H + c]; vy[i] = x[2 * H + c]; vz[i] = x[3 * H + c];
+                        g1[i] = u[H + c]; g2[i] = u[2 * H + c];
+                    }
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const int a = a0 + col + sub + i;
+                        if (a >= n_atoms) continue;
+                        const int k = sub + i;
+                        const float n = pair_distance(vx[i], vy[i], vz[i]);
+                        const float sc = n > 0.0f ? cn[k] / n : 0.0f;    // d|v|/dv = v / |v|, 0 at v = 0
+                        float* o = xtbar + (int64_t)a * 4 * H;
+                        o[c] = sb[i] + cs[k];
+                        o[H + c] = bx[i] * g1[i] + (mix[0] * bx[i] + mix[3] * by[i] + mix[6] * bz[i]) * g2[i] + sc * vx[i];
+                        o[2 * H + c] = by[i] * g1[i] + (mix[1] * bx[i] + mix[4] * by[i] + mix[7] * bz[i]) * g2[i] + sc * vy[i];
+                        o[3 * H + c] = bz[i] * g1[i] + (mix[2] * bx[i] + mix[5] * by[i] + mix[8] * bz[i]) * g2[i] + sc * vz[i];
+                    }
                 }
             }
         }
@@ -588,9 +568,11 @@ __global__ void __launch_bounds__(UNT, 1) update_bwd_tc_kernel(const float* __re
         fence_after_sync();
     }
     __syncthreads();
-    if (t == 0) {
-        for (uint32_t f = ws.consumed; f < ws.issued; ++f)
-            if (!mbar_wait(&full[f % URING_B], (f / URING_B) & 1, WAIT_BUDGET)) {
+    if (producer) {
+        // copies still in flight are among the last URING issued (a slot is
+        // refilled only after its previous copy was consumed)
+        for (uint32_t f = ws.issued > (uint32_t)URING ? ws.issued - URING : 0u; f < ws.issued; ++f)
+            if (!mbar_wait(&full[f % URING], (f / URING) & 1, WAIT_BUDGET)) {
                 set_status(st, MLFF_ERR_TIMEOUT, 35);
                 break;
             }
@@ -598,7 +580,7 @@ __global__ void __launch_bounds__(UNT, 1) update_bwd_tc_kernel(const float* __re
     fence_before_sync();
     __syncthreads();
     fence_after_sync();
-    if (w == 0) tmem_dealloc(tmem, 512);
+    if (w == 0) tmem_dealloc(tmem, 256);
 }
 
 int launch_update_bwd_tc(const float* packed, const LayerOffsets& lo, const WsLayout& L, void* ws, int layer,
