@@ -242,20 +242,26 @@ __global__ void __launch_bounds__(UNT, 1) update_fwd_tc_kernel(const float* __re
         ufill_tmem(lane_base + 32 * hh, c1s[c], 2);
 #pragma unroll 1
         for (int g = 0; g < 3; ++g) ufill_tmem(lane_base + 64 + 64 * g + 32 * hh, c2s[g * H + c], 2);
-        // B tile: row = atom, K = [s (128), |v| (128)]; warp w builds rows w, w + 8, ...
+        // B tile: row = atom, K = [s (128), |v| (128)]; warp w builds rows w, w + 8, ...,
+        // two rows per step so that their loads overlap
 #pragma unroll 1
-        for (int i = w; i < UN; i += 8) {
-            const int a = a0 + i;
-            float4 sv = make_float4(0.f, 0.f, 0.f, 0.f), nv = sv;
-            if (a < n_atoms) {
-                const float4* x = reinterpret_cast<const float4*>(Xt + (int64_t)a * 4 * H);
-                sv = x[lane];
-                const float4 vx = x[32 + lane], vy = x[64 + lane], vz = x[96 + lane];
-                nv = make_float4(pair_distance(vx.x, vy.x, vz.x), pair_distance(vx.y, vy.y, vz.y),
-                                 pair_distance(vx.z, vy.z, vz.z), pair_distance(vx.w, vy.w, vz.w));  // |v| (:437)
+        for (int i0 = w; i0 < UN; i0 += 16) {
+            float4 r[2][4];
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const int a = a0 + i0 + 8 * k;
+                const float4* x = reinterpret_cast<const float4*>(Xt + (int64_t)(a < n_atoms ? a : 0) * 4 * H);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) r[k][j] = a < n_atoms ? x[32 * j + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
             }
-            store_row4(Bs, UF_BH, i, 4 * lane, sv);
-            store_row4(Bs, UF_BH, i, H + 4 * lane, nv);
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const float4 vx = r[k][1], vy = r[k][2], vz = r[k][3];
+                const float4 nv = make_float4(pair_distance(vx.x, vy.x, vz.x), pair_distance(vx.y, vy.y, vz.y),
+                                              pair_distance(vx.z, vy.z, vz.z), pair_distance(vx.w, vy.w, vz.w));  // |v| (:437)
+                store_row4(Bs, UF_BH, i0 + 8 * k, 4 * lane, r[k][0]);
+                store_row4(Bs, UF_BH, i0 + 8 * k, H + 4 * lane, nv);
+            }
         }
         tmem_st_wait();
         fence_async_smem();
@@ -305,45 +311,70 @@ __global__ void __launch_bounds__(UNT, 1) update_fwd_tc_kernel(const float* __re
         uwait_mma(ctl, w, 24);
         // the next tile's GEMM1 pairs arrive while this epilogue and the next build run
         if (producer && !ustream_fill(ws, min(P0 + 40 + URING, P_end))) ufail(ctl, 29);
-        {   // epilogue 2: (ds, g1, g2) -> ua; s' = s + ds, v' = v g1 + (M v) g2 (:452-468)
+        {   // epilogue 2: (ds, g1, g2) -> ua; s' = s + ds, v' = v g1 + (M v) g2 (:452-468).
+            // The TMEM owner of channel c writes (ds, g1, g2) of 32 atoms to
+            // shared memory (the B tile is free), then each warp handles
+            // whole atom rows with 128-bit accesses; two passes of 32 atoms.
+            float* T = reinterpret_cast<float*>(Bs);      // [3][32 atoms][H]
 #pragma unroll 1
-            for (int blk = 0; blk < 2; ++blk) {
-                const int col = 32 * hh + 16 * blk;
-                float ds[16], g1[16], g2[16];
-                tmem_ld16(lane_base + 64 + col, ds);
-                tmem_ld16(lane_base + 128 + col, g1);
-                tmem_ld16(lane_base + 192 + col, g2);
-                tmem_ld_wait();
+            for (int pass = 0; pass < 2; ++pass) {
+                if (hh == pass) {
+#pragma unroll 1
+                    for (int g = 0; g < 3; ++g) {
+                        float v[32];
+                        tmem_ld32(lane_base + 64 + 64 * g + 32 * pass, v);
+                        tmem_ld_wait();
 #pragma unroll
-                for (int sub = 0; sub < 16; sub += 8) {
-                    float s8[8], vx[8], vy[8], vz[8];
-#pragma unroll
-                    for (int i = 0; i < 8; ++i) {
-                        const int a = a0 + col + sub + i;
-                        const bool ok = a < n_atoms;
-                        const float* x = Xt + (int64_t)(ok ? a : 0) * 4 * H;
-                        s8[i] = ok ? x[c] : 0.f;
-                        vx[i] = ok ? x[H + c] : 0.f;
-                        vy[i] = ok ? x[2 * H + c] : 0.f;
-                        vz[i] = ok ? x[3 * H + c] : 0.f;
-                    }
-#pragma unroll
-                    for (int i = 0; i < 8; ++i) {
-                        const int a = a0 + col + sub + i;
-                        if (a < n_atoms) {
-                            const int k = sub + i;
-                            float* u = ua + (int64_t)a * H3;
-                            u[c] = ds[k];
-                            u[H + c] = g1[k];
-                            u[2 * H + c] = g2[k];
-                            float* xo = Xout + (int64_t)a * 4 * H;
-                            xo[c] = s8[i] + ds[k];
-                            xo[H + c] = vx[i] * g1[k] + (mix[0] * vx[i] + mix[1] * vy[i] + mix[2] * vz[i]) * g2[k];
-                            xo[2 * H + c] = vy[i] * g1[k] + (mix[3] * vx[i] + mix[4] * vy[i] + mix[5] * vz[i]) * g2[k];
-                            xo[3 * H + c] = vz[i] * g1[k] + (mix[6] * vx[i] + mix[7] * vy[i] + mix[8] * vz[i]) * g2[k];
-                        }
+                        for (int i = 0; i < 32; ++i) T[(g * 32 + i) * H + c] = v[i];
                     }
                 }
+                __syncthreads();
+#pragma unroll 1
+                for (int i0 = w; i0 < 32; i0 += 16) {
+                    float4 x[2][4];
+#pragma unroll
+                    for (int k = 0; k < 2; ++k) {
+                        const int a = a0 + 32 * pass + i0 + 8 * k;
+                        const float4* xr = reinterpret_cast<const float4*>(Xt + (int64_t)(a < n_atoms ? a : 0) * 4 * H);
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) x[k][j] = a < n_atoms ? xr[32 * j + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+                    }
+#pragma unroll
+                    for (int k = 0; k < 2; ++k) {
+                        const int i = i0 + 8 * k, a = a0 + 32 * pass + i;
+                        if (a >= n_atoms) continue;
+                        const float4 ds = reinterpret_cast<const float4*>(T + (0 * 32 + i) * H)[lane];
+                        const float4 g1 = reinterpret_cast<const float4*>(T + (1 * 32 + i) * H)[lane];
+                        const float4 g2 = reinterpret_cast<const float4*>(T + (2 * 32 + i) * H)[lane];
+                        float4* u = reinterpret_cast<float4*>(ua + (int64_t)a * H3);
+                        u[lane] = ds;
+                        u[32 + lane] = g1;
+                        u[64 + lane] = g2;
+                        const float4 sv = x[k][0], vx = x[k][1], vy = x[k][2], vz = x[k][3];
+                        auto vnew = [&](float px, float py, float pz, float pc, float a1, float a2, int r) {
+                            return pc * a1 + (mix[3 * r] * px + mix[3 * r + 1] * py + mix[3 * r + 2] * pz) * a2;
+                        };
+                        float4 ox, oy, oz;
+                        ox.x = vnew(vx.x, vy.x, vz.x, vx.x, g1.x, g2.x, 0);
+                        ox.y = vnew(vx.y, vy.y, vz.y, vx.y, g1.y, g2.y, 0);
+                        ox.z = vnew(vx.z, vy.z, vz.z, vx.z, g1.z, g2.z, 0);
+                        ox.w = vnew(vx.w, vy.w, vz.w, vx.w, g1.w, g2.w, 0);
+                        oy.x = vnew(vx.x, vy.x, vz.x, vy.x, g1.x, g2.x, 1);
+                        oy.y = vnew(vx.y, vy.y, vz.y, vy.y, g1.y, g2.y, 1);
+                        oy.z = vnew(vx.z, vy.z, vz.z, vy.z, g1.z, g2.z, 1);
+                        oy.w = vnew(vx.w, vy.w, vz.w, vy.w, g1.w, g2.w, 1);
+                        oz.x = vnew(vx.x, vy.x, vz.x, vz.x, g1.x, g2.x, 2);
+                        oz.y = vnew(vx.y, vy.y, vz.y, vz.y, g1.y, g2.y, 2);
+                        oz.z = vnew(vx.z, vy.z, vz.z, vz.z, g1.z, g2.z, 2);
+                        oz.w = vnew(vx.w, vy.w, vz.w, vz.w, g1.w, g2.w, 2);
+                        float4* xo = reinterpret_cast<float4*>(Xout + (int64_t)a * 4 * H);
+                        xo[lane] = make_float4(sv.x + ds.x, sv.y + ds.y, sv.z + ds.z, sv.w + ds.w);
+                        xo[32 + lane] = ox;
+                        xo[64 + lane] = oy;
+                        xo[96 + lane] = oz;
+                    }
+                }
+                __syncthreads();
             }
         }
         fence_before_sync();
@@ -453,31 +484,40 @@ __global__ void __launch_bounds__(UNT, 1) update_bwd_tc_kernel(const float* __re
 
     for (int tile = blockIdx.x; tile < ntiles && !*abort_flag; tile += gridDim.x, P0 += 40) {
         const int a0 = tile * UN;
-        // abar tile: row = atom; K = [sb, sum_i xb_i v_i, sum_i xb_i (M v)_i]; warp w builds rows w, w + 8, ...
+        // abar tile: row = atom; K = [sb, sum_i xb_i v_i, sum_i xb_i (M v)_i]; warp w builds
+        // rows w, w + 8, ..., two rows per step so that their loads overlap
+        auto gpart = [&](float b_x, float b_y, float b_z, float v_x, float v_y, float v_z, float& o1, float& o2) {
+            o1 = b_x * v_x + b_y * v_y + b_z * v_z;
+            o2 = b_x * (mix[0] * v_x + mix[1] * v_y + mix[2] * v_z) + b_y * (mix[3] * v_x + mix[4] * v_y + mix[5] * v_z) +
+                 b_z * (mix[6] * v_x + mix[7] * v_y + mix[8] * v_z);
+        };
 #pragma unroll 1
-        for (int i = w; i < UN; i += 8) {
-            const int a = a0 + i;
-            float4 sb = make_float4(0.f, 0.f, 0.f, 0.f), g1 = sb, g2 = sb;
-            if (a < n_atoms) {
-                const float4* xo = reinterpret_cast<const float4*>(xbo + (int64_t)a * 4 * H);
-                const float4* x = reinterpret_cast<const float4*>(Xt + (int64_t)a * 4 * H);
-                sb = xo[lane];
-                const float4 bx = xo[32 + lane], by = xo[64 + lane], bz = xo[96 + lane];
-                const float4 vx = x[32 + lane], vy = x[64 + lane], vz = x[96 + lane];
-                auto one = [&](float b_x, float b_y, float b_z, float v_x, float v_y, float v_z, float& o1, float& o2) {
-                    o1 = b_x * v_x + b_y * v_y + b_z * v_z;
-                    o2 = b_x * (mix[0] * v_x + mix[1] * v_y + mix[2] * v_z) +
-                         b_y * (mix[3] * v_x + mix[4] * v_y + mix[5] * v_z) +
-                         b_z * (mix[6] * v_x + mix[7] * v_y + mix[8] * v_z);
-                };
-                one(bx.x, by.x, bz.x, vx.x, vy.x, vz.x, g1.x, g2.x);
-                one(bx.y, by.y, bz.y, vx.y, vy.y, vz.y, g1.y, g2.y);
-                one(bx.z, by.z, bz.z, vx.z, vy.z, vz.z, g1.z, g2.z);
-                one(bx.w, by.w, bz.w, vx.w, vy.w, vz.w, g1.w, g2.w);
+        for (int i0 = w; i0 < UN; i0 += 16) {
+            float4 r[2][7];
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const int a = a0 + i0 + 8 * k;
+                const int64_t aa = a < n_atoms ? a : 0;
+                const float4* xo = reinterpret_cast<const float4*>(xbo + aa * 4 * H);
+                const float4* x = reinterpret_cast<const float4*>(Xt + aa * 4 * H);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) r[k][j] = a < n_atoms ? xo[32 * j + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                for (int j = 1; j < 4; ++j) r[k][3 + j] = a < n_atoms ? x[32 * j + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
             }
-            store_row4(Bs, UB_AH, i, 4 * lane, sb);
-            store_row4(Bs, UB_AH, i, H + 4 * lane, g1);
-            store_row4(Bs, UB_AH, i, 2 * H + 4 * lane, g2);
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const float4 bx = r[k][1], by = r[k][2], bz = r[k][3], vx = r[k][4], vy = r[k][5], vz = r[k][6];
+                float4 g1, g2;
+                gpart(bx.x, by.x, bz.x, vx.x, vy.x, vz.x, g1.x, g2.x);
+                gpart(bx.y, by.y, bz.y, vx.y, vy.y, vz.y, g1.y, g2.y);
+                gpart(bx.z, by.z, bz.z, vx.z, vy.z, vz.z, g1.z, g2.z);
+                gpart(bx.w, by.w, bz.w, vx.w, vy.w, vz.w, g1.w, g2.w);
+                const int i = i0 + 8 * k;
+                store_row4(Bs, UB_AH, i, 4 * lane, r[k][0]);
+                store_row4(Bs, UB_AH, i, H + 4 * lane, g1);
+                store_row4(Bs, UB_AH, i, 2 * H + 4 * lane, g2);
+            }
         }
         fence_async_smem();
         fence_before_sync();
@@ -524,42 +564,63 @@ __global__ void __launch_bounds__(UNT, 1) update_bwd_tc_kernel(const float* __re
         if (producer && !ustream_fill(ws, min(P0 + 40, P_end))) ufail(ctl, 38);
         uwait_mma(ctl, w, 34);
         if (producer && !ustream_fill(ws, min(P0 + 40 + URING, P_end))) ufail(ctl, 39);
-        {   // epilogue 4: xtbar = (sb + cs, xb g1 + M^T xb g2 + cn v / |v|)
+        {   // epilogue 4: xtbar = (sb + cs, xb g1 + M^T xb g2 + cn v / |v|).  The
+            // TMEM owner of channel c writes (cs, cn) of its 32 atoms to shared
+            // memory (the abar tile is free), then each warp handles whole atom
+            // rows with 128-bit accesses.
+            float* T = reinterpret_cast<float*>(Bs);      // [2][UN atoms][H]
 #pragma unroll 1
-            for (int blk = 0; blk < 2; ++blk) {
-                const int col = 32 * hh + 16 * blk;
-                float cs[16], cn[16];
-                tmem_ld16(lane_base + 64 + col, cs);
-                tmem_ld16(lane_base + 128 + col, cn);
+            for (int g = 0; g < 2; ++g) {
+                float v[32];
+                tmem_ld32(lane_base + 64 + 64 * g + 32 * hh, v);
                 tmem_ld_wait();
+#pragma unroll
+                for (int i = 0; i < 32; ++i) T[(g * UN + 32 * hh + i) * H + c] = v[i];
+            }
+            __syncthreads();
 #pragma unroll 1
-                for (int sub = 0; sub < 16; sub += 4) {
-                    float sb[4], bx[4], by[4], bz[4], vx[4], vy[4], vz[4], g1[4], g2[4];
+            for (int i0 = w; i0 < UN; i0 += 16) {
+                float4 r[2][9];
 #pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        const int a = a0 + col + sub + i;
-                        const bool ok = a < n_atoms;
-                        const int64_t aa = ok ? a : 0;
-                        const float* xo = xbo + aa * 4 * H;
-                        const float* x = Xt + aa * 4 * H;
-                        const float* u = ua + aa * H3;
-                        sb[i] = xo[c]; bx[i] = xo[H + c]; by[i] = xo[2 * H + c]; bz[i] = xo[3 * H + c];
-                        vx[i] = x[H + c]; vy[i] = x[2 * H + c]; vz[i] = x[3 * H + c];
-                        g1[i] = u[H + c]; g2[i] = u[2 * H + c];
-                    }
+                for (int k = 0; k < 2; ++k) {
+                    const int a = a0 + i0 + 8 * k;
+                    const int64_t aa = a < n_atoms ? a : 0;
+                    const float4* xo = reinterpret_cast<const float4*>(xbo + aa * 4 * H);
+                    const float4* x = reinterpret_cast<const float4*>(Xt + aa * 4 * H);
+                    const float4* u = reinterpret_cast<const float4*>(ua + aa * H3);
 #pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        const int a = a0 + col + sub + i;
-                        if (a >= n_atoms) continue;
-                        const int k = sub + i;
-                        const float n = pair_distance(vx[i], vy[i], vz[i]);
-                        const float sc = n > 0.0f ? cn[k] / n : 0.0f;    // d|v|/dv = v / |v|, 0 at v = 0
-                        float* o = xtbar + (int64_t)a * 4 * H;
-                        o[c] = sb[i] + cs[k];
-                        o[H + c] = bx[i] * g1[i] + (mix[0] * bx[i] + mix[3] * by[i] + mix[6] * bz[i]) * g2[i] + sc * vx[i];
-                        o[2 * H + c] = by[i] * g1[i] + (mix[1] * bx[i] + mix[4] * by[i] + mix[7] * bz[i]) * g2[i] + sc * vy[i];
-                        o[3 * H + c] = bz[i] * g1[i] + (mix[2] * bx[i] + mix[5] * by[i] + mix[8] * bz[i]) * g2[i] + sc * vz[i];
-                    }
+                    for (int j = 0; j < 4; ++j) r[k][j] = xo[32 * j + lane];
+#pragma unroll
+                    for (int j = 1; j < 4; ++j) r[k][3 + j] = x[32 * j + lane];
+                    r[k][7] = u[32 + lane];
+                    r[k][8] = u[64 + lane];
+                }
+#pragma unroll
+                for (int k = 0; k < 2; ++k) {
+                    const int i = i0 + 8 * k, a = a0 + i;
+                    if (a >= n_atoms) continue;
+                    const float4 cs = reinterpret_cast<const float4*>(T + i * H)[lane];
+                    const float4 cn = reinterpret_cast<const float4*>(T + (UN + i) * H)[lane];
+                    const float4 sb = r[k][0], bx = r[k][1], by = r[k][2], bz = r[k][3];
+                    const float4 vx = r[k][4], vy = r[k][5], vz = r[k][6], g1 = r[k][7], g2 = r[k][8];
+                    float4* o = reinterpret_cast<float4*>(xtbar + (int64_t)a * 4 * H);
+                    o[lane] = make_float4(sb.x + cs.x, sb.y + cs.y, sb.z + cs.z, sb.w + cs.w);
+                    float4 ox, oy, oz;
+                    auto one = [&](float b_x, float b_y, float b_z, float v_x, float v_y, float v_z, float a1, float a2,
+                                   float n_c, float& px, float& py, float& pz) {
+                        const float nn = pair_distance(v_x, v_y, v_z);
+                        const float sc = nn > 0.0f ? n_c / nn : 0.0f;   // d|v|/dv = v / |v|, 0 at v = 0
+                        px = b_x * a1 + (mix[0] * b_x + mix[3] * b_y + mix[6] * b_z) * a2 + sc * v_x;
+                        py = b_y * a1 + (mix[1] * b_x + mix[4] * b_y + mix[7] * b_z) * a2 + sc * v_y;
+                        pz = b_z * a1 + (mix[2] * b_x + mix[5] * b_y + mix[8] * b_z) * a2 + sc * v_z;
+                    };
+                    one(bx.x, by.x, bz.x, vx.x, vy.x, vz.x, g1.x, g2.x, cn.x, ox.x, oy.x, oz.x);
+                    one(bx.y, by.y, bz.y, vx.y, vy.y, vz.y, g1.y, g2.y, cn.y, ox.y, oy.y, oz.y);
+                    one(bx.z, by.z, bz.z, vx.z, vy.z, vz.z, g1.z, g2.z, cn.z, ox.z, oy.z, oz.z);
+                    one(bx.w, by.w, bz.w, vx.w, vy.w, vz.w, g1.w, g2.w, cn.w, ox.w, oy.w, oz.w);
+                    o[32 + lane] = ox;
+                    o[64 + lane] = oy;
+                    o[96 + lane] = oz;
                 }
             }
         }
