@@ -80,7 +80,15 @@ WsLayout ws_layout(const mlff_dims& d, int32_t n_atoms, int32_t n_mol, int64_t c
     L.xbar = take(sizeof(float) * 2 * N * 4 * H);
     L.e_atom = take(sizeof(float) * N);
     L.md_pos32 = take(sizeof(float) * 3 * N);
-    if (path == MLFF_PATH_TUNED_TC) L.geo = take(sizeof(float4) * cap);
+    if (path == MLFF_PATH_TUNED_TC) {
+        L.geo = take(sizeof(float4) * cap);
+        // per-partition tiles: at most cap / tile + one partial tile per partition
+        L.n_etile_f = cap / 128 + L.P + 1;
+        L.n_etile_b = cap / 64 + L.P + 1;
+        L.etile_base = take(4 * 2 * ((size_t)L.P + 1));
+        L.etile_f = take((size_t)L.n_etile_f * 16384);
+        L.etile_b = take((size_t)L.n_etile_b * 16384);
+    }
     if (path == MLFF_PATH_PLAIN_FP32 || path == MLFF_PATH_TRAIN) {
         L.geo = take(sizeof(float4) * cap);
         L.erbf = take(sizeof(float) * cap * RMAX);

@@ -9,6 +9,8 @@ constexpr float PI_FC = 3.14159265358979f;
 struct EdgeArgs {
     const float4* pos4;
     const float4* geo;        // optional per-edge (u_x, u_y, u_z, d), computed once per call
+    const unsigned char* etile;       // tensor-core path: precomputed E tiles of this pass
+    const int32_t* etile_base;        // first tile of each partition
     const int32_t* atom_mol;
     const float* box;
     const uint8_t* pbc;

@@ -156,6 +156,102 @@ __device__ __forceinline__ void rbf16_d(float d, bool valid, int r0, int R, cons
     }
 }
 
+// ------------------------------------------------------ E tiles (per call)
+// The RBF x cutoff rows of every edge tile as split fp16 in the K-major
+// no-swizzle layout (16-byte core matrices: K-step s at 4096 s, its second 8
+// columns 2048 further, 8-row groups 128 apart; the hi image, then the lo
+// image 8 KB later), computed once per call for all layers: forward tiles of
+// 128 edges, reverse tiles of 64 edges with the d-derivative rows 64-127.
+// Tiles follow the receiver partitions, so tile k of partition p is the k-th
+// tile its CTA processes.
+constexpr uint32_t ET_BYTES = 16384, ET_HALF = 8192;
+__device__ __forceinline__ uint32_t et_off(int row, int k) {
+    return (uint32_t)((k >> 4) * 4096 + ((k >> 3) & 1) * 2048 + (row >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+__global__ void etile_index_kernel(const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ part, int P,
+                                   int32_t* __restrict__ base) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int bf = 0, bb = 0;
+    for (int p = 0; p < P; ++p) {
+        base[p] = bf;
+        base[P + 1 + p] = bb;
+        const int E = row_ptr[part[p + 1]] - row_ptr[part[p]];
+        bf += (E + 127) / 128;
+        bb += (E + 63) / 64;
+    }
+    base[P] = bf;
+    base[2 * P + 1] = bb;
+}
+
+template <bool REV>
+__global__ void __launch_bounds__(256) etile_fill_kernel(EdgeArgs a, const int32_t* __restrict__ base,
+                                                         unsigned char* __restrict__ out) {
+    __shared__ float cent[RMAX], gam[RMAX];
+    if (threadIdx.x < RMAX) {
+        cent[threadIdx.x] = a.centers[threadIdx.x];
+        gam[threadIdx.x] = a.gamma[threadIdx.x];
+    }
+    __syncthreads();
+    if (a.st->code != 0) return;
+    constexpr int TN = REV ? 64 : 128;
+    const int t = threadIdx.x;
+    const int row = t & (TN - 1), s = (t / TN) & 1, which = REV ? (t >> 7) : 0;
+    for (int p = blockIdx.x; p < a.nparts; p += gridDim.x) {
+        const int e0 = a.row_ptr[a.part[p]], e1 = a.row_ptr[a.part[p + 1]];
+        const int b0 = base[(REV ? a.nparts + 1 : 0) + p];
+        for (int k = blockIdx.y; e0 + k * TN < e1; k += gridDim.y) {
+            const int e = e0 + k * TN + row;
+            const bool valid = e < e1;
+            const float d = valid ? a.geo[e].w : 0.f;
+            float v[16];
+            if (which == 0) rbf16(d, valid, 16 * s, a.R, cent, gam, a.cutoff, v);
+            else rbf16_d(d, valid, 16 * s, a.R, cent, gam, a.cutoff, v);
+            __align__(16) __half2 hi[8];
+            __align__(16) __half2 lo[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) split2(v[2 * i], v[2 * i + 1], hi[i], lo[i]);
+            unsigned char* tile = out + (size_t)(b0 + k) * ET_BYTES;
+            const int trow = which * 64 + row;
+            *reinterpret_cast<uint4*>(tile + et_off(trow, 16 * s)) = *reinterpret_cast<const uint4*>(&hi[0]);
+            *reinterpret_cast<uint4*>(tile + et_off(trow, 16 * s + 8)) = *reinterpret_cast<const uint4*>(&hi[4]);
+            *reinterpret_cast<uint4*>(tile + ET_HALF + et_off(trow, 16 * s)) = *reinterpret_cast<const uint4*>(&lo[0]);
+            *reinterpret_cast<uint4*>(tile + ET_HALF + et_off(trow, 16 * s + 8)) = *reinterpret_cast<const uint4*>(&lo[4]);
+        }
+    }
+}
+
+int launch_etiles(const EdgeArgs& a, int32_t* base, unsigned char* fwd, unsigned char* rev, cudaStream_t st) {
+    etile_index_kernel<<<1, 32, 0, st>>>(a.row_ptr, a.part, a.nparts, base);
+    MLFF_LAUNCH_CHECK("etile_index");
+    // tiles of a partition spread over gridDim.y blocks
+    etile_fill_kernel<false><<<dim3(a.nparts, 16), 256, 0, st>>>(a, base, fwd);
+    MLFF_LAUNCH_CHECK("etile_fill_fwd");
+    if (rev) {
+        etile_fill_kernel<true><<<dim3(a.nparts, 32), 256, 0, st>>>(a, base, rev);
+        MLFF_LAUNCH_CHECK("etile_fill_rev");
+    }
+    return MLFF_OK;
+}
+
+// Per-edge arrays of a tile, fetched asynchronously for the next tile while
+// the current one runs: (u, d), sender, receiver (padding: 0, 0, -1).
+__device__ __forceinline__ void fetch_tile_edges(const EdgeArgs& a, int t, int tn, int t0, int n, float4* us,
+                                                 int* src_s, int* rcv_s) {
+    if (t < tn) {
+        if (t < n) {
+            cp_async16(us + t, a.geo + t0 + t);
+            cp_async4(src_s + t, a.col + t0 + t);
+            cp_async4(rcv_s + t, a.erecv + t0 + t);
+        } else {
+            us[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+            src_s[t] = 0;
+            rcv_s[t] = -1;
+        }
+    }
+    cp_async_commit();
+}
+
 // Per-tile prep by threads otherwise idle during the E-tile phase: sender
 // (and receiver) row offsets, u components, and a bitmask of the edges whose
 // receiver differs from the previous edge's (edge 0 compares with prev).
@@ -251,26 +347,28 @@ __device__ __forceinline__ void zero_empty_rows(float* out, const int32_t* row_p
 
 // ------------------------------------------------------- forward kernel
 constexpr int FN = 128;                                   // edges per tile
-constexpr uint32_t F_EH = b_block(FN);                    // E tile, one half (K = 32 in one K-block)
 constexpr uint32_t F_HH = 2 * b_block(FN);                // H tile, one half (K = 128)
 static_assert(F_HH == HALF128, "GEMM2 B layout");
 constexpr uint32_t F_OFF_W1 = 0;
 constexpr uint32_t F_OFF_W2H = F_OFF_W1 + W1_BYTES;
 constexpr uint32_t F_OFF_H = align1k(F_OFF_W2H + W2_HALF);     // H tile; the E tile shares its start
 constexpr uint32_t F_OFF_RING = align1k(F_OFF_H + 2 * F_HH);
-constexpr uint32_t F_OFF_US = F_OFF_RING + NSLOT * A_TILE;
-constexpr uint32_t F_OFF_SRC = F_OFF_US + FN * 16;
-constexpr uint32_t F_OFF_RCV = F_OFF_SRC + FN * 4;
-constexpr uint32_t F_OFF_B1 = F_OFF_RCV + FN * 4;
+// per-tile edge arrays, two buffers: (u, d), sender, receiver, sender row
+// offset, u components, receiver-change bits
+constexpr uint32_t F_SB_US = 0;
+constexpr uint32_t F_SB_SRC = F_SB_US + FN * 16;
+constexpr uint32_t F_SB_RCV = F_SB_SRC + FN * 4;
+constexpr uint32_t F_SB_SOFF = F_SB_RCV + FN * 4;
+constexpr uint32_t F_SB_UC = F_SB_SOFF + FN * 4;
+constexpr uint32_t F_SB_CHG = F_SB_UC + 3 * FN * 4;
+constexpr uint32_t F_SB_BYTES = F_SB_CHG + (FN / 32) * 4;
+constexpr uint32_t F_OFF_SB = F_OFF_RING + NSLOT * A_TILE;
+constexpr uint32_t F_OFF_B1 = F_OFF_SB + 2 * F_SB_BYTES;
 constexpr uint32_t F_OFF_B2 = F_OFF_B1 + H * 4;
-constexpr uint32_t F_OFF_CG = F_OFF_B2 + H3 * 4;
-constexpr uint32_t F_OFF_SOFF = F_OFF_CG + 2 * RMAX * 4;
-constexpr uint32_t F_OFF_UC = F_OFF_SOFF + FN * 4;
-constexpr uint32_t F_OFF_CHG = F_OFF_UC + 3 * FN * 4;
-constexpr uint32_t F_OFF_BAR = F_OFF_CHG + (FN / 32) * 4 + 16;
-constexpr uint32_t F_OFF_MISC = F_OFF_BAR + 8 * (2 + NSLOT);
+constexpr uint32_t F_OFF_BAR = F_OFF_B2 + H3 * 4;
+constexpr uint32_t F_OFF_MISC = F_OFF_BAR + 8 * (3 + NSLOT);
 constexpr uint32_t F_SMEM = align1k(F_OFF_MISC + 16);
-static_assert(2 * F_EH <= 2 * F_HH, "E tile fits in the H tile's space");
+static_assert(ET_BYTES <= 2 * F_HH, "E tile fits in the H tile's space");
 static_assert(F_SMEM <= 232448, "forward kernel shared memory");
 
 // 16 warps.  Epilogue roles: warp w reads TMEM lane quarter q = w % 4
@@ -282,22 +380,14 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
     unsigned char* w1s = smem + F_OFF_W1;
     unsigned char* w2h = smem + F_OFF_W2H;
     unsigned char* Hs = smem + F_OFF_H;
-    unsigned char* Es = smem + F_OFF_H;            // E tile lives in the H tile's space
+    unsigned char* Es = smem + F_OFF_H;            // E tile (bulk-copied) lives in the H tile's space
     unsigned char* ring = smem + F_OFF_RING;
-    float4* us = reinterpret_cast<float4*>(smem + F_OFF_US);
-    int* src_s = reinterpret_cast<int*>(smem + F_OFF_SRC);
-    int* rcv_s = reinterpret_cast<int*>(smem + F_OFF_RCV);
     float* b1s = reinterpret_cast<float*>(smem + F_OFF_B1);
     float* b2s = reinterpret_cast<float*>(smem + F_OFF_B2);
-    float* cent = reinterpret_cast<float*>(smem + F_OFF_CG);
-    float* gam = cent + RMAX;
-    int* soff = reinterpret_cast<int*>(smem + F_OFF_SOFF);
-    float* uc = reinterpret_cast<float*>(smem + F_OFF_UC);
-    uint32_t* chg = reinterpret_cast<uint32_t*>(smem + F_OFF_CHG);
-    int* prev_s = reinterpret_cast<int*>(smem + F_OFF_CHG + (FN / 32) * 4);
     uint64_t* mma_bar = reinterpret_cast<uint64_t*>(smem + F_OFF_BAR);
     uint64_t* w2h_bar = mma_bar + 1;
-    uint64_t* full = mma_bar + 2;
+    uint64_t* e_bar = mma_bar + 2;
+    uint64_t* full = mma_bar + 3;
     uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + F_OFF_MISC);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + F_OFF_MISC + 4);
     uint32_t* ccount_s = reinterpret_cast<uint32_t*>(smem + F_OFF_MISC + 8);
@@ -312,6 +402,7 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
     if (t == 0) {
         mbar_init(mma_bar, 1);
         mbar_init(w2h_bar, 1);
+        mbar_init(e_bar, 1);
         for (int i = 0; i < NSLOT; ++i) mbar_init(&full[i], 1);
         fence_mbar_init();
         *abort_flag = 0;
@@ -321,10 +412,6 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
         reinterpret_cast<uint4*>(w1s)[i] = reinterpret_cast<const uint4*>(w1g)[i];
     if (t < H) b1s[t] = a.P[a.lo.b1 + t];
     for (int i = t; i < H3; i += NT) b2s[i] = a.P[a.lo.b2 + i];
-    if (t < RMAX) {
-        cent[t] = a.centers[t];
-        gam[t] = a.gamma[t];
-    }
     fence_async_smem();
     fence_before_sync();
     __syncthreads();
@@ -352,29 +439,44 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
     fence_after_sync();
 
     bool aborted = false;
+    uint32_t e_phase = 0, e_issued = 0;   // E-tile copies: barrier phase, copies issued (thread 32)
     for (int p = blockIdx.x; p < a.nparts && !aborted; p += gridDim.x) {
         const int j0 = a.part[p], j1 = a.part[p + 1];
         if (j0 >= j1) continue;
         const int e0 = a.row_ptr[j0], e1 = a.row_ptr[j1];
+        const int ntl = (e1 - e0 + FN - 1) / FN;
+        const unsigned char* etiles = a.etile + (size_t)a.etile_base[p] * ET_BYTES;
         zero_empty_rows(a.Xt, a.row_ptr, j0, j1, w, lane);
         int cur = j0;
         float acc = 0.f, accu = 0.f;   // x * phi and u * phi_v2 parts of the current receiver's sum
-        for (int t0 = e0; t0 < e1; t0 += FN) {
-            const int n = min(FN, e1 - t0);
-            if (t < FN) load_edge(a, t0, t, n, us, src_s, rcv_s);
-            if (t == FN) *prev_s = cur;   // receiver before this tile
-            __syncthreads();
-            if (t < 2 * FN) {   // E tile: edge row, 16 RBF columns (one K-step) per thread
-                const int e = t & (FN - 1), s = t >> 7;
-                float v[16];
-                rbf16(us[e].w, e < n, 16 * s, a.R, cent, gam, a.cutoff, v);
-                store_row16(Es, F_EH, FN, e, s, v);
-            } else if (t < 3 * FN) {
-                tile_prep<FN>(t - 2 * FN, n, *prev_s, src_s, rcv_s, us, soff, nullptr, uc, chg);
+        if (ntl > 0) {   // the partition's first tile: edge arrays and E tile
+            unsigned char* sb = smem + F_OFF_SB;
+            fetch_tile_edges(a, t, FN, e0, min(FN, e1 - e0), reinterpret_cast<float4*>(sb + F_SB_US),
+                             reinterpret_cast<int*>(sb + F_SB_SRC), reinterpret_cast<int*>(sb + F_SB_RCV));
+            if (t == 32) {
+                mbar_expect_tx(e_bar, ET_BYTES);
+                bulk_g2s(Es, etiles, ET_BYTES, e_bar);
+                ++e_issued;
             }
-            fence_async_smem();
+            cp_async_wait_all();
             __syncthreads();
-            if (t == 0) {   // GEMM1: z^T = W1 e^T
+            if (t < FN)
+                tile_prep<FN>(t, min(FN, e1 - e0), j0, reinterpret_cast<int*>(sb + F_SB_SRC),
+                              reinterpret_cast<int*>(sb + F_SB_RCV), reinterpret_cast<float4*>(sb + F_SB_US),
+                              reinterpret_cast<int*>(sb + F_SB_SOFF), nullptr, reinterpret_cast<float*>(sb + F_SB_UC),
+                              reinterpret_cast<uint32_t*>(sb + F_SB_CHG));
+            __syncthreads();
+        }
+        for (int k = 0; k < ntl; ++k) {
+            const int t0 = e0 + k * FN, n = min(FN, e1 - t0), buf = k & 1;
+            unsigned char* sb = smem + F_OFF_SB + buf * F_SB_BYTES;
+            unsigned char* sbn = smem + F_OFF_SB + (buf ^ 1) * F_SB_BYTES;
+            const int* rcv_s = reinterpret_cast<const int*>(sb + F_SB_RCV);
+            const int* soff = reinterpret_cast<const int*>(sb + F_SB_SOFF);
+            const float* uc = reinterpret_cast<const float*>(sb + F_SB_UC);
+            const uint32_t* chg = reinterpret_cast<const uint32_t*>(sb + F_SB_CHG);
+            if (t == 0) {   // GEMM1: z^T = W1 e^T on the bulk-copied E tile
+                if (!mbar_wait(e_bar, e_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 8);
                 fence_after_sync();
                 constexpr uint32_t idesc = idesc_f16(FN);
 #pragma unroll
@@ -383,11 +485,12 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                     for (int pr = 0; pr < 3; ++pr) {
                         const uint32_t ahl = pr == 2 ? 1 : 0, bhl = pr == 1 ? 1 : 0;
                         const uint64_t ad = sdesc(smem_u32(w1s + s * SLAB + ahl * A_TILE), A_LBO, A_SBO);
-                        const uint64_t bd = sdesc_b(smem_u32(Es + bhl * F_EH + b_kstep_off(FN, s)));
+                        const uint64_t bd = sdesc(smem_u32(Es + bhl * ET_HALF + s * 4096), 2048, 128);
                         mma_f16(tmem + TM_Z, ad, bd, idesc, (s | pr) != 0);
                     }
                 mma_commit(mma_bar);
             }
+            e_phase ^= 1;
             if (w == 0) __syncwarp();
             // only warp 0 polls the MMA barrier; the others wait at the CTA
             // barrier instead of spinning on shared memory the MMAs read from
@@ -450,6 +553,18 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                 fill_lo_ring(ring, w2lo, full);
                 pcount += NSLOT;
             }
+            // ... and the H tile is free: the next tile's E tile and edge arrays
+            // arrive while epilogue 2 runs
+            const bool more = k + 1 < ntl && !*abort_flag;
+            if (more) {
+                fetch_tile_edges(a, t, FN, t0 + FN, min(FN, e1 - t0 - FN), reinterpret_cast<float4*>(sbn + F_SB_US),
+                                 reinterpret_cast<int*>(sbn + F_SB_SRC), reinterpret_cast<int*>(sbn + F_SB_RCV));
+                if (t == 32) {
+                    mbar_expect_tx(e_bar, ET_BYTES);
+                    bulk_g2s(Es, etiles + (size_t)(k + 1) * ET_BYTES, ET_BYTES, e_bar);
+                    ++e_issued;
+                }
+            }
             if (w == 1) __syncwarp();
             {   // epilogue 2: component r of the message sums, segmented by receiver;
                 // 16-edge blocks, the next block's gathers in flight.  Padding
@@ -509,12 +624,18 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                     process16(xn, col + 16);
                 }
             }
+            cp_async_wait_all();
             fence_before_sync();
             __syncthreads();
             if (*abort_flag) {
                 aborted = true;
                 break;
             }
+            if (more && t < FN)
+                tile_prep<FN>(t, min(FN, e1 - t0 - FN), rcv_s[FN - 1], reinterpret_cast<int*>(sbn + F_SB_SRC),
+                              reinterpret_cast<int*>(sbn + F_SB_RCV), reinterpret_cast<float4*>(sbn + F_SB_US),
+                              reinterpret_cast<int*>(sbn + F_SB_SOFF), nullptr, reinterpret_cast<float*>(sbn + F_SB_UC),
+                              reinterpret_cast<uint32_t*>(sbn + F_SB_CHG));
         }
         if (!aborted) a.Xt[(int64_t)cur * 4 * H + fidx] = acc + accu;
     }
@@ -523,6 +644,9 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
     __syncthreads();
     if (t == 32) {
         if (!mbar_wait(w2h_bar, 0, WAIT_BUDGET)) set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 7);
+        // an E-tile copy issued for a tile that never ran (abort) must land first
+        if (e_issued > 0 && !mbar_wait(e_bar, (e_issued - 1) & 1, WAIT_BUDGET))
+            set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 9);
         const uint32_t used = *ccount_s;
         for (uint32_t f = used; f < pcount; ++f)
             if (!mbar_wait(&full[f % NSLOT], (f / NSLOT) & 1, WAIT_BUDGET)) {
@@ -542,28 +666,28 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
 // [0,64) z^T, [64,128) z'^T, and per chunk g at 128 + 128 g: [0,64) f^T,
 // [64,128) f'^T.
 constexpr int BN = 64;
-constexpr uint32_t B_EH = b_block(2 * BN);
 constexpr uint32_t B_HH = 2 * b_block(2 * BN);
 static_assert(B_HH == HALF128, "GEMM2 B layout");
 constexpr uint32_t B_OFF_W1 = 0;
 constexpr uint32_t B_OFF_W2H = B_OFF_W1 + W1_BYTES;
 constexpr uint32_t B_OFF_H = align1k(B_OFF_W2H + W2_HALF);     // [H; H'] tile; the [E; E'] tile shares its start
 constexpr uint32_t B_OFF_RING = align1k(B_OFF_H + 2 * B_HH);
-constexpr uint32_t B_OFF_US = B_OFF_RING + NSLOT * A_TILE;
-constexpr uint32_t B_OFF_SRC = B_OFF_US + BN * 16;
-constexpr uint32_t B_OFF_RCV = B_OFF_SRC + BN * 4;
-constexpr uint32_t B_OFF_B1 = B_OFF_RCV + BN * 4;
+constexpr uint32_t B_SB_US = 0;
+constexpr uint32_t B_SB_SRC = B_SB_US + BN * 16;
+constexpr uint32_t B_SB_RCV = B_SB_SRC + BN * 4;
+constexpr uint32_t B_SB_SOFF = B_SB_RCV + BN * 4;
+constexpr uint32_t B_SB_ROFF = B_SB_SOFF + BN * 4;
+constexpr uint32_t B_SB_UC = B_SB_ROFF + BN * 4;
+constexpr uint32_t B_SB_CHG = B_SB_UC + 3 * BN * 4;
+constexpr uint32_t B_SB_BYTES = B_SB_CHG + 16;
+constexpr uint32_t B_OFF_SB = B_OFF_RING + NSLOT * A_TILE;
+constexpr uint32_t B_OFF_B1 = B_OFF_SB + 2 * B_SB_BYTES;
 constexpr uint32_t B_OFF_B2 = B_OFF_B1 + H * 4;
-constexpr uint32_t B_OFF_CG = B_OFF_B2 + H3 * 4;
-constexpr uint32_t B_OFF_SOFF = B_OFF_CG + 2 * RMAX * 4;
-constexpr uint32_t B_OFF_ROFF = B_OFF_SOFF + BN * 4;
-constexpr uint32_t B_OFF_UC = B_OFF_ROFF + BN * 4;
-constexpr uint32_t B_OFF_CHG = B_OFF_UC + 3 * BN * 4;
-constexpr uint32_t B_OFF_RED = B_OFF_CHG + (BN / 32) * 4 + 16;
+constexpr uint32_t B_OFF_RED = B_OFF_B2 + H3 * 4;
 constexpr uint32_t B_OFF_BAR = B_OFF_RED + 16 * BN * 2 * 4;
-constexpr uint32_t B_OFF_MISC = B_OFF_BAR + 8 * (2 + NSLOT);
+constexpr uint32_t B_OFF_MISC = B_OFF_BAR + 8 * (3 + NSLOT);
 constexpr uint32_t B_SMEM = align1k(B_OFF_MISC + 16);
-static_assert(2 * B_EH <= 2 * B_HH, "E tile fits in the H tile's space");
+static_assert(ET_BYTES <= 2 * B_HH, "E tile fits in the H tile's space");
 static_assert(B_SMEM <= 232448, "reverse kernel shared memory");
 
 __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const unsigned char* __restrict__ w1g,
@@ -572,24 +696,15 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
     unsigned char* w1s = smem + B_OFF_W1;
     unsigned char* w2h = smem + B_OFF_W2H;
     unsigned char* Hs = smem + B_OFF_H;            // [H; H'] hi, then lo
-    unsigned char* Es = smem + B_OFF_H;            // [E; E'] hi, then lo, before H is written
+    unsigned char* Es = smem + B_OFF_H;            // [E; E'] tile (bulk-copied), before H is written
     unsigned char* ring = smem + B_OFF_RING;
-    float4* us = reinterpret_cast<float4*>(smem + B_OFF_US);
-    int* src_s = reinterpret_cast<int*>(smem + B_OFF_SRC);
-    int* rcv_s = reinterpret_cast<int*>(smem + B_OFF_RCV);
     float* b1s = reinterpret_cast<float*>(smem + B_OFF_B1);
     float* b2s = reinterpret_cast<float*>(smem + B_OFF_B2);
-    float* cent = reinterpret_cast<float*>(smem + B_OFF_CG);
-    float* gam = cent + RMAX;
     float* red = reinterpret_cast<float*>(smem + B_OFF_RED);   // [16 warps][BN][2]
-    int* soff = reinterpret_cast<int*>(smem + B_OFF_SOFF);
-    int* roff = reinterpret_cast<int*>(smem + B_OFF_ROFF);
-    float* uc = reinterpret_cast<float*>(smem + B_OFF_UC);
-    uint32_t* chg = reinterpret_cast<uint32_t*>(smem + B_OFF_CHG);
-    int* prev_s = reinterpret_cast<int*>(smem + B_OFF_CHG + (BN / 32) * 4);
     uint64_t* mma_bar = reinterpret_cast<uint64_t*>(smem + B_OFF_BAR);
     uint64_t* w2h_bar = mma_bar + 1;
-    uint64_t* full = mma_bar + 2;
+    uint64_t* e_bar = mma_bar + 2;
+    uint64_t* full = mma_bar + 3;
     uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + B_OFF_MISC);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + B_OFF_MISC + 4);
     uint32_t* ccount_s = reinterpret_cast<uint32_t*>(smem + B_OFF_MISC + 8);
@@ -604,6 +719,7 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
     if (t == 0) {
         mbar_init(mma_bar, 1);
         mbar_init(w2h_bar, 1);
+        mbar_init(e_bar, 1);
         for (int i = 0; i < NSLOT; ++i) mbar_init(&full[i], 1);
         fence_mbar_init();
         *abort_flag = 0;
@@ -613,10 +729,6 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
         reinterpret_cast<uint4*>(w1s)[i] = reinterpret_cast<const uint4*>(w1g)[i];
     if (t < H) b1s[t] = a.P[a.lo.b1 + t];
     for (int i = t; i < H3; i += NT) b2s[i] = a.P[a.lo.b2 + i];
-    if (t < RMAX) {
-        cent[t] = a.centers[t];
-        gam[t] = a.gamma[t];
-    }
     fence_async_smem();
     fence_before_sync();
     __syncthreads();
@@ -644,30 +756,48 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
     const int rs_idx = reduce_scatter8_index(lane);
 
     bool aborted = false;
+    uint32_t e_phase = 0, e_issued = 0;   // E-tile copies: barrier phase, copies issued (thread 32)
+    auto prep = [&](unsigned char* sbx, int nn, int prev) {
+        if (t < BN)
+            tile_prep<BN>(t, nn, prev, reinterpret_cast<int*>(sbx + B_SB_SRC), reinterpret_cast<int*>(sbx + B_SB_RCV),
+                          reinterpret_cast<float4*>(sbx + B_SB_US), reinterpret_cast<int*>(sbx + B_SB_SOFF),
+                          reinterpret_cast<int*>(sbx + B_SB_ROFF), reinterpret_cast<float*>(sbx + B_SB_UC),
+                          reinterpret_cast<uint32_t*>(sbx + B_SB_CHG));
+    };
     for (int p = blockIdx.x; p < a.nparts && !aborted; p += gridDim.x) {
         const int j0 = a.part[p], j1 = a.part[p + 1];
         if (j0 >= j1) continue;
         const int e0 = a.row_ptr[j0], e1 = a.row_ptr[j1];
+        const int ntl = (e1 - e0 + BN - 1) / BN;
+        const unsigned char* etiles = a.etile + (size_t)a.etile_base[p] * ET_BYTES;
         if (a.write_nodes) zero_empty_rows(a.xbar, a.row_ptr, j0, j1, w, lane);
         int cur = j0;
         float acc = 0.f;
-        for (int t0 = e0; t0 < e1; t0 += BN) {
-            const int n = min(BN, e1 - t0);
-            if (t < BN) load_edge(a, t0, t, n, us, src_s, rcv_s);
-            if (t == BN) *prev_s = cur;   // receiver before this tile
-            __syncthreads();
-            if (t < 4 * BN) {   // E (rbf * fc) rows 0-63 and E' (its d-derivative) rows 64-127
-                const int e = t & (BN - 1), s = (t >> 6) & 1, which = t >> 7;
-                float v[16];
-                if (which == 0) rbf16(us[e].w, e < n, 16 * s, a.R, cent, gam, a.cutoff, v);
-                else rbf16_d(us[e].w, e < n, 16 * s, a.R, cent, gam, a.cutoff, v);
-                store_row16(Es, B_EH, 2 * BN, which * BN + e, s, v);
-            } else if (t < 5 * BN) {
-                tile_prep<BN>(t - 4 * BN, n, *prev_s, src_s, rcv_s, us, soff, roff, uc, chg);
+        if (ntl > 0) {   // the partition's first tile: edge arrays and [E; E'] tile
+            unsigned char* sb = smem + B_OFF_SB;
+            fetch_tile_edges(a, t, BN, e0, min(BN, e1 - e0), reinterpret_cast<float4*>(sb + B_SB_US),
+                             reinterpret_cast<int*>(sb + B_SB_SRC), reinterpret_cast<int*>(sb + B_SB_RCV));
+            if (t == 32) {
+                mbar_expect_tx(e_bar, ET_BYTES);
+                bulk_g2s(Es, etiles, ET_BYTES, e_bar);
+                ++e_issued;
             }
-            fence_async_smem();
+            cp_async_wait_all();
             __syncthreads();
-            if (t == 0) {   // [z; z']^T = W1 [e; e']^T
+            prep(sb, min(BN, e1 - e0), j0);
+            __syncthreads();
+        }
+        for (int k = 0; k < ntl; ++k) {
+            const int t0 = e0 + k * BN, n = min(BN, e1 - t0), buf = k & 1;
+            unsigned char* sb = smem + B_OFF_SB + buf * B_SB_BYTES;
+            unsigned char* sbn = smem + B_OFF_SB + (buf ^ 1) * B_SB_BYTES;
+            const int* rcv_s = reinterpret_cast<const int*>(sb + B_SB_RCV);
+            const int* soff = reinterpret_cast<const int*>(sb + B_SB_SOFF);
+            const int* roff = reinterpret_cast<const int*>(sb + B_SB_ROFF);
+            const float* uc = reinterpret_cast<const float*>(sb + B_SB_UC);
+            const uint32_t* chg = reinterpret_cast<const uint32_t*>(sb + B_SB_CHG);
+            if (t == 0) {   // [z; z']^T = W1 [e; e']^T on the bulk-copied tile
+                if (!mbar_wait(e_bar, e_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 18);
                 fence_after_sync();
                 constexpr uint32_t idesc = idesc_f16(2 * BN);
 #pragma unroll
@@ -676,11 +806,12 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                     for (int pr = 0; pr < 3; ++pr) {
                         const uint32_t ahl = pr == 2 ? 1 : 0, bhl = pr == 1 ? 1 : 0;
                         const uint64_t ad = sdesc(smem_u32(w1s + s * SLAB + ahl * A_TILE), A_LBO, A_SBO);
-                        const uint64_t bd = sdesc_b(smem_u32(Es + bhl * B_EH + b_kstep_off(2 * BN, s)));
+                        const uint64_t bd = sdesc(smem_u32(Es + bhl * ET_HALF + s * 4096), 2048, 128);
                         mma_f16(tmem + TM_Z, ad, bd, idesc, (s | pr) != 0);
                     }
                 mma_commit(mma_bar);
             }
+            e_phase ^= 1;
             if (w == 0) __syncwarp();
             // only warp 0 polls the MMA barrier; the others wait at the CTA
             // barrier instead of spinning on shared memory the MMAs read from
@@ -750,6 +881,18 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
             if (t == 32 && !*abort_flag) {
                 fill_lo_ring(ring, w2lo, full);
                 pcount += NSLOT;
+            }
+            // the H tile is free too: the next tile's [E; E'] tile and edge
+            // arrays arrive while epilogue 2 runs
+            const bool more = k + 1 < ntl && !*abort_flag;
+            if (more) {
+                fetch_tile_edges(a, t, BN, t0 + BN, min(BN, e1 - t0 - BN), reinterpret_cast<float4*>(sbn + B_SB_US),
+                                 reinterpret_cast<int*>(sbn + B_SB_SRC), reinterpret_cast<int*>(sbn + B_SB_RCV));
+                if (t == 32) {
+                    mbar_expect_tx(e_bar, ET_BYTES);
+                    bulk_g2s(Es, etiles + (size_t)(k + 1) * ET_BYTES, ET_BYTES, e_bar);
+                    ++e_issued;
+                }
             }
             if (w == 1) __syncwarp();
             {   // epilogue 2: component r of the node adjoints (gathered from the
@@ -846,17 +989,21 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                 ea.w += du[2];
                 a.eacc[t0 + t] = ea;
             }
+            cp_async_wait_all();
             __syncthreads();
             if (*abort_flag) {
                 aborted = true;
                 break;
             }
+            if (more) prep(sbn, min(BN, e1 - t0 - BN), rcv_s[BN - 1]);
         }
         if (!aborted && a.write_nodes) a.xbar[(int64_t)cur * 4 * H + fidx] = acc;
     }
     __syncthreads();
     if (t == 32) {
         if (!mbar_wait(w2h_bar, 0, WAIT_BUDGET)) set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 17);
+        if (e_issued > 0 && !mbar_wait(e_bar, (e_issued - 1) & 1, WAIT_BUDGET))
+            set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 19);
         const uint32_t used = *ccount_s;
         for (uint32_t f = used; f < pcount; ++f)
             if (!mbar_wait(&full[f % NSLOT], (f / NSLOT) & 1, WAIT_BUDGET)) {

@@ -294,6 +294,7 @@ __global__ void __launch_bounds__(128) edge_bwd_simt_kernel(EdgeArgs a) {
 
 int launch_edge_fwd_tc(const EdgeArgs& a, int layer, cudaStream_t st);
 int launch_edge_bwd_tc(const EdgeArgs& a, int layer, cudaStream_t st);
+int launch_etiles(const EdgeArgs& a, int32_t* base, unsigned char* fwd, unsigned char* rev, cudaStream_t st);
 
 // dst += src over n4 float4 elements (the tensor-core edge kernels write
 // per-receiver sums only; the per-atom term is added here)
@@ -367,6 +368,12 @@ int run_tuned(const mlff_dims& d, const float* P, const PackedOffsets& po, const
         edge_geom_kernel<<<blocks, 256, 0, st>>>(a, geo);
         MLFF_LAUNCH_CHECK("edge_geom");
         a.geo = geo;
+        // RBF x cutoff tiles for every edge tile of every layer (and their
+        // d-derivative for the reverse pass when forces are asked for)
+        const bool rev = out.forces != nullptr || out.virial != nullptr;
+        if ((r = launch_etiles(a, ws_ptr<int32_t>(ws, L.etile_base), ws_ptr<unsigned char>(ws, L.etile_f),
+                               rev ? ws_ptr<unsigned char>(ws, L.etile_b) : nullptr, st)))
+            return r;
     }
     for (int l = 0; l < d.n_layers; ++l) {
         a.lo = po.layer[l];
@@ -375,6 +382,8 @@ int run_tuned(const mlff_dims& d, const float* P, const PackedOffsets& po, const
         {
             ProfScope prof(PK_EDGE_FWD, st);
             if (tc) {
+                a.etile = ws_ptr<unsigned char>(ws, L.etile_f);
+                a.etile_base = ws_ptr<int32_t>(ws, L.etile_base);
                 if ((r = launch_edge_fwd_tc(a, l, st))) return r;
                 if ((r = add_rows(a.Xt, a.X, NX, a.st, st))) return r;
             } else {
@@ -405,6 +414,8 @@ int run_tuned(const mlff_dims& d, const float* P, const PackedOffsets& po, const
         {
             ProfScope prof(PK_EDGE_BWD, st);
             if (tc) {
+                a.etile = ws_ptr<unsigned char>(ws, L.etile_b);
+                a.etile_base = ws_ptr<int32_t>(ws, L.etile_base) + L.P + 1;
                 if ((r = launch_edge_bwd_tc(a, l, st))) return r;
                 if (l > 0 && (r = add_rows(xbo, xtb, NX, a.st, st))) return r;
             } else {

@@ -38,6 +38,10 @@ struct WsLayout {
     size_t md_pos32;           // float [N][3]  positions the integrator hands to the force call
     // plain path (materialised per-edge tensors, like the reference's graph)
     size_t geo;                // float4 [cap] (u_x, u_y, u_z, d)
+    size_t etile_base;         // int32 [2][P+1] first E tile of each partition (forward, reverse)
+    size_t etile_f;            // forward E tiles: 128 edges x K 32, split fp16, 16 KB each
+    size_t etile_b;            // reverse [E; E'] tiles: 64 edges, 16 KB each
+    int64_t n_etile_f, n_etile_b;
     size_t erbf;               // float [cap][RMAX]
     size_t erbf_d;             // float [cap][RMAX]
     size_t fz;                 // float [L][cap][H]
