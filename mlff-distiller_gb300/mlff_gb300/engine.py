@@ -179,6 +179,19 @@ class Engine:
             return E, F, V, A
         return E, F, V
 
+    def capture(self, batch: Batch, path: int = _lib.PATH_TUNED_TC, forces: bool = True):
+        """One energy_forces call captured in a CUDA graph, for repeated
+        evaluation of a fixed batch (the edge capacity must already be known:
+        call energy_forces once first).  Returns (replay, E, F): replay()
+        launches the graph on the current stream and refreshes E and F."""
+        self.energy_forces(batch, path, forces=forces)   # sizes capacity and workspace, loads kernels
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            E, F, _ = self.energy_forces(batch, path, forces=forces, check=False)
+        self._graph_keep = g
+        return g.replay, E, F
+
     def neighbors(self, batch: Batch):
         """CSR (row_ptr, col) of the radius graph, for tests and tools."""
         N, B = batch.n_atoms, batch.n_mol
