@@ -178,6 +178,7 @@ __global__ void __launch_bounds__(128) readout_kernel(const float* __restrict__ 
                                                       int want_grad, const Status* st) {
     __shared__ float s_in[RO_ATOMS][H];
     __shared__ float z1[RO_ATOMS][64];
+    __shared__ float h1[RO_ATOMS][64];
     __shared__ float z2[RO_ATOMS][32];
     __shared__ float g2[RO_ATOMS][32];
     __shared__ float g1[RO_ATOMS][64];
@@ -203,7 +204,10 @@ __global__ void __launch_bounds__(128) readout_kernel(const float* __restrict__ 
                 for (int q = 0; q < RO_ATOMS; ++q) acc[q] = fmaf(w, s_in[q][i], acc[q]);
             }
 #pragma unroll
-            for (int q = 0; q < RO_ATOMS; ++q) z1[q][t] = acc[q];
+            for (int q = 0; q < RO_ATOMS; ++q) {
+                z1[q][t] = acc[q];
+                h1[q][t] = silu_f(acc[q]);
+            }
         }
         __syncthreads();
         if (t < 32) {
@@ -213,7 +217,7 @@ __global__ void __launch_bounds__(128) readout_kernel(const float* __restrict__ 
             for (int i = 0; i < 64; ++i) {
                 float w = W2t[i * 32 + t];
 #pragma unroll
-                for (int q = 0; q < RO_ATOMS; ++q) acc[q] = fmaf(w, silu_f(z1[q][i]), acc[q]);
+                for (int q = 0; q < RO_ATOMS; ++q) acc[q] = fmaf(w, h1[q][i], acc[q]);
             }
 #pragma unroll
             for (int q = 0; q < RO_ATOMS; ++q) z2[q][t] = acc[q];
@@ -320,6 +324,19 @@ __device__ __forceinline__ float3 edge_grad(float4 acc, float3 r) {
                        acc.x * r.z * inv_d + acc.w * inv_de - c * r.z);
 }
 
+// One warp per receiver atom: lane l takes edges l, l + 32, ... of the row
+// (independent loads across lanes), then a fixed-order shuffle reduction.
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
 __global__ void forces_kernel(const float4* __restrict__ pos4, const int32_t* __restrict__ atom_mol,
                               const float* __restrict__ box, const uint8_t* __restrict__ pbc,
                               const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
@@ -327,7 +344,9 @@ __global__ void forces_kernel(const float4* __restrict__ pos4, const int32_t* __
                               int32_t n_atoms, float* __restrict__ forces, double* __restrict__ vir_atom,
                               const Status* st) {
     if (st->code != 0) return;
-    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < n_atoms; a += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; a < n_atoms; a += nw) {
         const int m = atom_mol[a];
         Box b;
         b.periodic = (pbc != nullptr && box != nullptr && pbc[m]) ? 1 : 0;
@@ -338,7 +357,7 @@ __global__ void forces_kernel(const float4* __restrict__ pos4, const int32_t* __
         const float4 pa = pos4[a];
         float fx = 0.f, fy = 0.f, fz = 0.f;
         double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-        for (int k = row_ptr[a]; k < row_ptr[a + 1]; ++k) {
+        for (int k = row_ptr[a] + lane; k < row_ptr[a + 1]; k += 32) {
             const int bb = col[k];
             const float3 r = edge_vector(pos4[bb], pa, b);         // sender bb -> receiver a
             const float3 g = edge_grad(acc[k], r);
@@ -354,13 +373,20 @@ __global__ void forces_kernel(const float4* __restrict__ pos4, const int32_t* __
                     for (int j = 0; j < 3; ++j) v[3 * i + j] += (double)gg[i] * (double)rr[j];
             }
         }
-        if (forces) {
+        fx = warp_sum(fx);
+        fy = warp_sum(fy);
+        fz = warp_sum(fz);
+        if (forces && lane == 0) {
             forces[3 * a] = fx;
             forces[3 * a + 1] = fy;
             forces[3 * a + 2] = fz;
         }
-        if (vir_atom)
-            for (int i = 0; i < 9; ++i) vir_atom[(int64_t)9 * a + i] = v[i];
+        if (vir_atom) {
+#pragma unroll
+            for (int i = 0; i < 9; ++i) v[i] = warp_sum_d(v[i]);
+            if (lane == 0)
+                for (int i = 0; i < 9; ++i) vir_atom[(int64_t)9 * a + i] = v[i];
+        }
     }
 }
 
@@ -391,7 +417,7 @@ int launch_forces(const mlff_dims& d, const mlff_system& sys, const WsLayout& L,
     // per-atom virial scratch reuses the second adjoint buffer (free by now)
     double* vir_atom = out.virial ? reinterpret_cast<double*>(ws_ptr<float>(ws, L.xbar) + (int64_t)sys.n_atoms * 4 * H)
                                   : nullptr;
-    int blocks = (int)std::min<int64_t>((sys.n_atoms + 127) / 128, 152 * 8);
+    int blocks = (int)std::min<int64_t>((sys.n_atoms + 3) / 4, 152 * 16);   // 4 atoms (warps) per block
     forces_kernel<<<std::max(blocks, 1), 128, 0, st>>>(
         ws_ptr<float4>(ws, L.pos4), ws_ptr<int32_t>(ws, L.atom_mol), sys.box, sys.pbc,
         ws_ptr<int32_t>(ws, L.row_ptr), ws_ptr<int32_t>(ws, L.col), ws_ptr<int32_t>(ws, L.rev),

@@ -169,19 +169,49 @@ __device__ __forceinline__ uint32_t et_off(int row, int k) {
     return (uint32_t)((k >> 4) * 4096 + ((k >> 3) & 1) * 2048 + (row >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
 }
 
-__global__ void etile_index_kernel(const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ part, int P,
-                                   int32_t* __restrict__ base) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    int bf = 0, bb = 0;
-    for (int p = 0; p < P; ++p) {
-        base[p] = bf;
-        base[P + 1 + p] = bb;
-        const int E = row_ptr[part[p + 1]] - row_ptr[part[p]];
-        bf += (E + 127) / 128;
-        bb += (E + 63) / 64;
+// tile counts of all partitions, then an exclusive scan (one block, the
+// partitions taken 1024 at a time)
+__global__ void __launch_bounds__(1024) etile_index_kernel(const int32_t* __restrict__ row_ptr,
+                                                           const int32_t* __restrict__ part, int P,
+                                                           int32_t* __restrict__ base) {
+    __shared__ int cf[1024], cb[1024];
+    __shared__ int carry[2];
+    const int t = threadIdx.x;
+    if (t == 0) carry[0] = carry[1] = 0;
+    __syncthreads();
+    for (int p0 = 0; p0 < P; p0 += 1024) {
+        const int p = p0 + t;
+        int nf = 0, nb = 0;
+        if (p < P) {
+            const int E = row_ptr[part[p + 1]] - row_ptr[part[p]];
+            nf = (E + 127) / 128;
+            nb = (E + 63) / 64;
+        }
+        cf[t] = nf;
+        cb[t] = nb;
+        __syncthreads();
+        for (int o = 1; o < 1024; o <<= 1) {   // inclusive scan (Hillis-Steele)
+            const int xf = t >= o ? cf[t - o] : 0, xb = t >= o ? cb[t - o] : 0;
+            __syncthreads();
+            cf[t] += xf;
+            cb[t] += xb;
+            __syncthreads();
+        }
+        if (p < P) {
+            base[p] = carry[0] + cf[t] - nf;
+            base[P + 1 + p] = carry[1] + cb[t] - nb;
+        }
+        __syncthreads();
+        if (t == 1023) {
+            carry[0] += cf[1023];
+            carry[1] += cb[1023];
+        }
+        __syncthreads();
     }
-    base[P] = bf;
-    base[2 * P + 1] = bb;
+    if (t == 0) {
+        base[P] = carry[0];
+        base[2 * P + 1] = carry[1];
+    }
 }
 
 template <bool REV>
@@ -222,7 +252,7 @@ __global__ void __launch_bounds__(256) etile_fill_kernel(EdgeArgs a, const int32
 }
 
 int launch_etiles(const EdgeArgs& a, int32_t* base, unsigned char* fwd, unsigned char* rev, cudaStream_t st) {
-    etile_index_kernel<<<1, 32, 0, st>>>(a.row_ptr, a.part, a.nparts, base);
+    etile_index_kernel<<<1, 1024, 0, st>>>(a.row_ptr, a.part, a.nparts, base);
     MLFF_LAUNCH_CHECK("etile_index");
     // tiles of a partition spread over gridDim.y blocks
     etile_fill_kernel<false><<<dim3(a.nparts, 16), 256, 0, st>>>(a, base, fwd);
@@ -337,12 +367,19 @@ __device__ __forceinline__ bool issue_gemm2(uint32_t tmem, const unsigned char* 
     return true;
 }
 
-// Receivers in [j0, j1) without edges get a zero row (the epilogues store
-// one value per receiver that has edges).
+// out = base + (sum over the receiver's edges): receivers in [j0, j1)
+// without edges get the base row (the epilogues store base + sum once per
+// receiver that has edges).
 __device__ __forceinline__ void zero_empty_rows(float* out, const int32_t* row_ptr, int j0, int j1, int w, int lane) {
     for (int j = j0 + w; j < j1; j += NT / 32)
         if (row_ptr[j] == row_ptr[j + 1])
             for (int k = lane; k < 4 * H; k += 32) out[(int64_t)j * 4 * H + k] = 0.0f;
+}
+__device__ __forceinline__ void copy_empty_rows(float* out, const float* base, const int32_t* row_ptr, int j0, int j1,
+                                                int w, int lane) {
+    for (int j = j0 + w; j < j1; j += NT / 32)
+        if (row_ptr[j] == row_ptr[j + 1])
+            for (int k = lane; k < 4 * H; k += 32) out[(int64_t)j * 4 * H + k] = base[(int64_t)j * 4 * H + k];
 }
 
 // ------------------------------------------------------- forward kernel
@@ -446,9 +483,12 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
         const int e0 = a.row_ptr[j0], e1 = a.row_ptr[j1];
         const int ntl = (e1 - e0 + FN - 1) / FN;
         const unsigned char* etiles = a.etile + (size_t)a.etile_base[p] * ET_BYTES;
-        zero_empty_rows(a.Xt, a.row_ptr, j0, j1, w, lane);
+        copy_empty_rows(a.Xt, a.X, a.row_ptr, j0, j1, w, lane);
         int cur = j0;
         float acc = 0.f, accu = 0.f;   // x * phi and u * phi_v2 parts of the current receiver's sum
+        // X of the current receiver (the residual term of Xt), loaded when the
+        // receiver starts so that the load is long done when its sum is stored
+        float base = a.X[(int64_t)cur * 4 * H + fidx];
         if (ntl > 0) {   // the partition's first tile: edge arrays and E tile
             unsigned char* sb = smem + F_OFF_SB;
             fetch_tile_edges(a, t, FN, e0, min(FN, e1 - e0), reinterpret_cast<float4*>(sb + F_SB_US),
@@ -571,7 +611,8 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                 // edges gather 0 (and have u = 0), so they add nothing.
                 const float* ur = uc + (r == 0 ? 0 : (r - 1) * FN);
                 const uint32_t f1col = r == 0 ? 128 : 256;
-                float* out = a.Xt + fidx;
+                float* out = a.Xt + fidx;          // Xt = X + message sum (student_model.py:359-385)
+                const float* xin = a.X + fidx;
                 float xa[16], xn[16];
                 auto gather16 = [&](float (&x)[16], int col) {
 #pragma unroll
@@ -605,8 +646,9 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
 #pragma unroll
                         for (int i = 0; i < 16; ++i) {
                             if (mask & (1u << i)) {
-                                out[(int64_t)cur * 4 * H] = acc + accu;
+                                out[(int64_t)cur * 4 * H] = base + (acc + accu);
                                 cur = rcv_s[col + i];
+                                base = xin[(int64_t)cur * 4 * H];
                                 acc = 0.f;
                                 accu = 0.f;
                             }
@@ -637,7 +679,7 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                               reinterpret_cast<int*>(sbn + F_SB_SOFF), nullptr, reinterpret_cast<float*>(sbn + F_SB_UC),
                               reinterpret_cast<uint32_t*>(sbn + F_SB_CHG));
         }
-        if (!aborted) a.Xt[(int64_t)cur * 4 * H + fidx] = acc + accu;
+        if (!aborted) a.Xt[(int64_t)cur * 4 * H + fidx] = base + (acc + accu);
     }
     // drain: the resident-tile load and every ring fill issued must have
     // landed before the CTA exits
@@ -901,7 +943,7 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                 // flight.  Padding edges gather 0, so they add nothing.
                 const uint32_t f1col = r == 0 ? 128 : 256, d1col = f1col + BN;
                 const float* ur = uc + (r == 0 ? 0 : (r - 1) * BN);
-                float* out = a.xbar + fidx;
+                float* out = a.xbar + fidx;        // gathered adjoint; dE/dXt is added afterwards
                 float tba[8], xba[8], tra[8], tbn[8], xbn[8], trn[8];
                 auto gather8 = [&](float (&tb)[8], float (&xb)[8], float (&tr)[8], int col) {
 #pragma unroll

@@ -296,30 +296,6 @@ int launch_edge_fwd_tc(const EdgeArgs& a, int layer, cudaStream_t st);
 int launch_edge_bwd_tc(const EdgeArgs& a, int layer, cudaStream_t st);
 int launch_etiles(const EdgeArgs& a, int32_t* base, unsigned char* fwd, unsigned char* rev, cudaStream_t st);
 
-// dst += src over n4 float4 elements (the tensor-core edge kernels write
-// per-receiver sums only; the per-atom term is added here)
-__global__ void add_rows_kernel(float4* __restrict__ dst, const float4* __restrict__ src, int64_t n4,
-                                const Status* st) {
-    if (st->code != 0) return;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n4; i += (int64_t)gridDim.x * blockDim.x) {
-        float4 d = dst[i];
-        const float4 v = src[i];
-        d.x += v.x;
-        d.y += v.y;
-        d.z += v.z;
-        d.w += v.w;
-        dst[i] = d;
-    }
-}
-
-static int add_rows(float* dst, const float* src, int64_t n, const Status* st, cudaStream_t s) {
-    const int64_t n4 = n / 4;
-    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((n4 + 255) / 256, 152 * 8));
-    add_rows_kernel<<<blocks, 256, 0, s>>>(reinterpret_cast<float4*>(dst), reinterpret_cast<const float4*>(src), n4,
-                                           st);
-    MLFF_LAUNCH_CHECK("add_rows");
-    return MLFF_OK;
-}
 
 __global__ void edge_geom_kernel(EdgeArgs a, float4* __restrict__ geo) {
     if (a.st->code != 0) return;
@@ -331,6 +307,31 @@ __global__ void edge_geom_kernel(EdgeArgs a, float4* __restrict__ geo) {
         load_edge(a, t0, threadIdx.x, n, us, src_s, rcv_s);
         if ((int)threadIdx.x < n) geo[t0 + threadIdx.x] = us[threadIdx.x];
     }
+}
+
+// dst += src over n4 float4 elements (the reverse tensor-core edge kernel
+// writes the gathered part of dE/dX only)
+__global__ void add_rows_kernel(float4* __restrict__ dst, const float4* __restrict__ src, int64_t n4,
+                                const Status* st) {
+    if (st->code != 0) return;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n4; i += (int64_t)gridDim.x * blockDim.x) {
+        float4 d = dst[i];
+        const float4 s = src[i];
+        d.x += s.x;
+        d.y += s.y;
+        d.z += s.z;
+        d.w += s.w;
+        dst[i] = d;
+    }
+}
+
+static int add_rows(float* dst, const float* src, int64_t n, const Status* st, cudaStream_t s) {
+    const int64_t n4 = n / 4;
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((n4 + 255) / 256, 152 * 8));
+    add_rows_kernel<<<blocks, 256, 0, s>>>(reinterpret_cast<float4*>(dst), reinterpret_cast<const float4*>(src), n4,
+                                           st);
+    MLFF_LAUNCH_CHECK("add_rows");
+    return MLFF_OK;
 }
 
 int run_tuned(const mlff_dims& d, const float* P, const PackedOffsets& po, const mlff_system& sys,
@@ -384,8 +385,7 @@ int run_tuned(const mlff_dims& d, const float* P, const PackedOffsets& po, const
             if (tc) {
                 a.etile = ws_ptr<unsigned char>(ws, L.etile_f);
                 a.etile_base = ws_ptr<int32_t>(ws, L.etile_base);
-                if ((r = launch_edge_fwd_tc(a, l, st))) return r;
-                if ((r = add_rows(a.Xt, a.X, NX, a.st, st))) return r;
+                if ((r = launch_edge_fwd_tc(a, l, st))) return r;   // writes Xt = X + messages
             } else {
                 edge_fwd_simt_kernel<<<L.P, 128, 0, st>>>(a);
                 MLFF_LAUNCH_CHECK("edge_fwd_simt");
@@ -417,7 +417,7 @@ int run_tuned(const mlff_dims& d, const float* P, const PackedOffsets& po, const
                 a.etile = ws_ptr<unsigned char>(ws, L.etile_b);
                 a.etile_base = ws_ptr<int32_t>(ws, L.etile_base) + L.P + 1;
                 if ((r = launch_edge_bwd_tc(a, l, st))) return r;
-                if (l > 0 && (r = add_rows(xbo, xtb, NX, a.st, st))) return r;
+                if (l > 0 && (r = add_rows(xbo, xtb, NX, a.st, st))) return r;   // dE/dX = dE/dXt + gathered part
             } else {
                 edge_bwd_simt_kernel<<<L.P, 128, 0, st>>>(a);
                 MLFF_LAUNCH_CHECK("edge_bwd_simt");
