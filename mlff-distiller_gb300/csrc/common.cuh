@@ -90,6 +90,7 @@ struct LayerOffsets {
     int64_t c2;     // [H3]
     int64_t w1_bf;  // split-fp16 hi/lo tiles for the tensor-core filter (bytes offset / 4)
     int64_t w2_bf;
+    int64_t w2_tm;  // lo halves of W2 rows [0,2H) as the TMEM image of the filter kernels ([4][32][H] u32)
     int64_t u1_tc;  // split-fp16 A-operand tile pairs of the tensor-core update MLP:
     int64_t u2_tc;  //   U1 [H][2H] and U2 [3H][H] (forward),
     int64_t u2t_tc; //   U2^T [H][3H] and U1^T [2H][H] (reverse)

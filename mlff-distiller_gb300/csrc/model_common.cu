@@ -56,6 +56,7 @@ PackedOffsets packed_offsets(const mlff_dims& d) {
         // U1 and U2 in both orientations
         L.w1_bf = take(2 * H * RMAX / 2);
         L.w2_bf = take(2 * H3 * H / 2);
+        L.w2_tm = take(4 * 32 * H);
         L.u1_tc = take(2 * H * 2 * H / 2);
         L.u2_tc = take(2 * H3 * H / 2);
         L.u2t_tc = take(2 * H3 * H / 2);

@@ -55,7 +55,8 @@ constexpr uint32_t TM_Z = 384;
 // W1 [H][RMAX] -> 2 K-step blocks (hi, lo); W2 [3H][H] -> 24 hi tiles
 // followed by the 24 matching lo tiles.
 __global__ void pack_tc_kernel(const float* __restrict__ w1, const float* __restrict__ w2,
-                               unsigned char* __restrict__ w1_out, unsigned char* __restrict__ w2_out) {
+                               unsigned char* __restrict__ w1_out, unsigned char* __restrict__ w2_out,
+                               uint32_t* __restrict__ w2_tm) {
     const int stride = gridDim.x * blockDim.x;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 2 * 128 * 16; i += stride) {
         const int s = i / 2048, m = (i / 16) % 128, kk = i % 16;
@@ -72,6 +73,19 @@ __global__ void pack_tc_kernel(const float* __restrict__ w1, const float* __rest
         *reinterpret_cast<__half*>(w2_out + q * A_TILE + a_off(m, kk)) = hi;
         *reinterpret_cast<__half*>(w2_out + W2_HALF + q * A_TILE + a_off(m, kk)) = lo;
     }
+    // TMEM image of the lo halves of chunks 0 and 1: word (r, v, m) is TMEM
+    // lane m, column 32 r + v, holding k = 2 (v % 8), 2 (v % 8) + 1 of
+    // K-step 4 r + v / 8 (low half first)
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 4 * 32 * 128; i += stride) {
+        const int m = i % 128, v = (i / 128) % 32, r = i / (32 * 128);
+        const int ks = 4 * r + v / 8, g = ks >> 3, s = ks & 7, j = v % 8;
+        const float* row = w2 + (size_t)(g * 128 + m) * H + 16 * s;
+        __half hi0, lo0, hi1, lo1;
+        split_f16(row[2 * j], hi0, lo0);
+        split_f16(row[2 * j + 1], hi1, lo1);
+        __half2 pr = __halves2half2(lo0, lo1);
+        w2_tm[i] = *reinterpret_cast<uint32_t*>(&pr);
+    }
 }
 
 int pack_update_tc(const mlff_dims& d, float* out, const PackedOffsets& o, cudaStream_t st);
@@ -80,7 +94,8 @@ int pack_bf16(const mlff_dims& d, float* out, const PackedOffsets& o, cudaStream
     for (int l = 0; l < d.n_layers; ++l) {
         const LayerOffsets& L = o.layer[l];
         pack_tc_kernel<<<64, 256, 0, st>>>(out + L.w1, out + L.w2, reinterpret_cast<unsigned char*>(out + L.w1_bf),
-                                           reinterpret_cast<unsigned char*>(out + L.w2_bf));
+                                           reinterpret_cast<unsigned char*>(out + L.w2_bf),
+                                           reinterpret_cast<uint32_t*>(out + L.w2_tm));
         MLFF_LAUNCH_CHECK("pack_tc");
     }
     return pack_update_tc(d, out, o, st);
@@ -104,24 +119,13 @@ __device__ __forceinline__ void fill_lo_ring(unsigned char* ring, const unsigned
     }
 }
 
-// Lo halves of W2 chunks 0 and 1 into TMEM columns [0,128), as A operands:
-// warp (q, r) writes rows 32q..32q+31 (its TMEM lane quarter), K-steps
-// 4r..4r+3 of the 16 (chunk (4r) / 8), i.e. columns 32r..32r+31.
-__device__ __forceinline__ void load_w2_lo_tmem(uint32_t lane_base, const float* w2, int r, int m) {
+// Lo halves of W2 chunks 0 and 1 into TMEM columns [0,128), as A operands,
+// from their packed TMEM image: warp (q, r) writes rows 32q..32q+31 (its
+// TMEM lane quarter), columns 32r..32r+31 (K-steps 4r..4r+3 of the 16).
+__device__ __forceinline__ void load_w2_lo_tmem(uint32_t lane_base, const uint32_t* w2tm, int r, int m) {
     uint32_t v[32];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const int ks = 4 * r + i, g = ks >> 3, s = ks & 7;
-        const float* row = w2 + (size_t)(g * 128 + m) * H + 16 * s;
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            __half hi0, lo0, hi1, lo1;
-            split_f16(row[2 * j], hi0, lo0);
-            split_f16(row[2 * j + 1], hi1, lo1);
-            __half2 pr = __halves2half2(lo0, lo1);
-            v[8 * i + j] = *reinterpret_cast<uint32_t*>(&pr);
-        }
-    }
+    for (int i = 0; i < 32; ++i) v[i] = __ldg(w2tm + (r * 32 + i) * 128 + m);
     tmem_st32u(lane_base + TM_W2LO + 32 * r, v);
 }
 
@@ -469,7 +473,7 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
     const int c = 32 * q + lane;
     const int fidx = r * H + c;                      // this thread's feature element in a [4][H] row
     const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
-    load_w2_lo_tmem(lane_base, a.P + a.lo.w2, r, c);
+    load_w2_lo_tmem(lane_base, reinterpret_cast<const uint32_t*>(a.P + a.lo.w2_tm), r, c);
     tmem_st_wait();
     fence_before_sync();
     __syncthreads();
@@ -790,7 +794,7 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
     const int c = 32 * q + lane;
     const int fidx = r * H + c;
     const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
-    load_w2_lo_tmem(lane_base, a.P + a.lo.w2, r, c);
+    load_w2_lo_tmem(lane_base, reinterpret_cast<const uint32_t*>(a.P + a.lo.w2_tm), r, c);
     tmem_st_wait();
     fence_before_sync();
     __syncthreads();
