@@ -3,6 +3,7 @@
 #include <cstdint>
 #include <cstddef>
 #include <cuda_runtime.h>
+#include <utility>
 #include "../../include/mlff_gb300.h"
 
 namespace mlff {
@@ -28,6 +29,21 @@ struct Status {
 __device__ __forceinline__ void set_status(Status* st, int code, int where) {
     if (atomicCAS(&st->code, 0, code) == 0) st->where = where;
 }
+
+// Programmatic dependent launch.  A kernel launched by MLFF_LAUNCH_PDL may be
+// scheduled while the kernel before it in the stream is still running, as
+// soon as that kernel has executed pdl_trigger() in every CTA (or exited).
+// Rules every such kernel follows:
+//  * pdl_wait() in every thread before it reads or writes any buffer an
+//    earlier kernel of the stream touches (the status word included) and
+//    before it can return; only packed weights and shared memory come before
+//    it, so that the prologue overlaps the previous kernel;
+//  * pdl_trigger() only after pdl_wait() and, in kernels that own tensor
+//    memory, only after the allocation (a dependent CTA then never holds
+//    columns a CTA of this kernel still waits for).
+// Both are no-ops in a kernel launched without the attribute.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
 __device__ __forceinline__ float silu_f(float x) {
     return x / (1.0f + expf(-x));
@@ -129,6 +145,34 @@ void prof_count_launch();   // profile.cu: one kernel launch of the current kind
     do {                                                                    \
         cudaError_t _e = (call);                                            \
         if (_e != cudaSuccess) return mlff::cuda_status(_e, #call);         \
+    } while (0)
+
+namespace mlff {
+bool pdl_enabled();   // programmatic dependent launch (on unless MLFF_PDL=0)
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                       Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = pdl_enabled() ? 1 : 0;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+}  // namespace mlff
+
+// Launch of a kernel that follows the pdl_wait / pdl_trigger rules, with the
+// same accounting and error check as MLFF_LAUNCH_CHECK.
+#define MLFF_LAUNCH_PDL(what, kernel, grid, block, smem, st, ...)                      \
+    do {                                                                              \
+        cudaError_t _e = mlff::launch_pdl(kernel, grid, block, smem, st, __VA_ARGS__); \
+        mlff::prof_count_launch();                                                    \
+        if (_e != cudaSuccess) return mlff::cuda_status(_e, what);                    \
     } while (0)
 
 // Every kernel launch is followed by this check (it also counts the launch

@@ -30,6 +30,7 @@ struct EdgeArgs {
     const float* xtbar;       // reverse: dE/dXt
     float* xbar;              // reverse: dE/dX
     float4* eacc;             // reverse: per-edge (dE/dd, dE/du)
+    int32_t eacc_init;        // reverse: 1 = first layer processed, eacc is written rather than added to
     int32_t write_nodes;      // reverse: also produce dE/dX (unused for the first layer)
     int32_t n_atoms;
     const Status* st;

@@ -12,6 +12,8 @@ namespace mlff {
 __global__ void kick_drift_kernel(double* __restrict__ pos, double* __restrict__ vel,
                                   const double* __restrict__ inv_mass, const float* __restrict__ F, double dt,
                                   int32_t n_atoms, float* __restrict__ pos32, const Status* st) {
+    pdl_wait();
+    pdl_trigger();
     if (st->code != 0) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 3 * n_atoms; i += gridDim.x * blockDim.x) {
         const int a = i / 3;
@@ -25,6 +27,8 @@ __global__ void kick_drift_kernel(double* __restrict__ pos, double* __restrict__
 
 __global__ void kick_kernel(double* __restrict__ vel, const double* __restrict__ inv_mass,
                             const float* __restrict__ F, double dt, int32_t n_atoms, const Status* st) {
+    pdl_wait();
+    pdl_trigger();
     if (st->code != 0) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 3 * n_atoms; i += gridDim.x * blockDim.x)
         vel[i] += 0.5 * dt * (double)F[i] * inv_mass[i / 3];
@@ -33,6 +37,8 @@ __global__ void kick_kernel(double* __restrict__ vel, const double* __restrict__
 // kinetic energy 1/2 m v^2 per structure (fixed-order tree)
 __global__ void kinetic_kernel(const double* __restrict__ vel, const double* __restrict__ inv_mass,
                                const int64_t* __restrict__ mol_ptr, int32_t n_mol, double* __restrict__ ke) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ double red[256];
     for (int m = blockIdx.x; m < n_mol; m += gridDim.x) {
         double s = 0.0;
@@ -54,9 +60,8 @@ __global__ void kinetic_kernel(const double* __restrict__ vel, const double* __r
 int md_kick_drift(const WsLayout& L, void* ws, mlff_md_state* s, double dt, cudaStream_t st) {
     ProfScope prof(PK_MD, st);
     const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((3LL * L.N + 255) / 256, 152 * 8));
-    kick_drift_kernel<<<blocks, 256, 0, st>>>(s->pos, s->vel, s->inv_mass, s->forces, dt, L.N,
+    MLFF_LAUNCH_PDL("kick_drift", kick_drift_kernel, blocks, 256, 0, st, s->pos, s->vel, s->inv_mass, s->forces, dt, L.N,
                                               ws_ptr<float>(ws, L.md_pos32), ws_ptr<Status>(ws, L.status));
-    MLFF_LAUNCH_CHECK("kick_drift");
     return MLFF_OK;
 }
 
@@ -64,12 +69,10 @@ int md_kick(const WsLayout& L, void* ws, mlff_md_state* s, double dt, const int6
             bool kinetic, cudaStream_t st) {
     ProfScope prof(PK_MD, st);
     const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((3LL * L.N + 255) / 256, 152 * 8));
-    kick_kernel<<<blocks, 256, 0, st>>>(s->vel, s->inv_mass, s->forces, dt, L.N, ws_ptr<Status>(ws, L.status));
-    MLFF_LAUNCH_CHECK("kick");
+    MLFF_LAUNCH_PDL("kick", kick_kernel, blocks, 256, 0, st, s->vel, s->inv_mass, s->forces, dt, L.N, ws_ptr<Status>(ws, L.status));
     if (kinetic && s->kinetic) {
-        kinetic_kernel<<<std::min(std::max(n_mol, 1), 152 * 8), 256, 0, st>>>(s->vel, s->inv_mass, mol_ptr, n_mol,
+        MLFF_LAUNCH_PDL("kinetic", kinetic_kernel, std::min(std::max(n_mol, 1), 152 * 8), 256, 0, st, s->vel, s->inv_mass, mol_ptr, n_mol,
                                                                               s->kinetic);
-        MLFF_LAUNCH_CHECK("kinetic");
     }
     return MLFF_OK;
 }

@@ -10,6 +10,7 @@
 //   energy_head + sum     :599-605, :734-757
 //   forces = -dE/dpos     :759-795
 #include <cstdio>
+#include <mutex>
 #include "common.cuh"
 #include "workspace.h"
 #include "profile.h"
@@ -142,6 +143,8 @@ int pack_fp32(const mlff_dims& d, const mlff_params& p, float* out, const Packed
 // ------------------------------------------------------------- embedding
 __global__ void embed_kernel(const float* __restrict__ emb, const int64_t* __restrict__ Z, int32_t n_atoms,
                              int32_t n_species, float* __restrict__ X, Status* st) {
+    pdl_wait();
+    pdl_trigger();
     // X[a] = (emb[Z[a]], 0, 0, 0)
     const int64_t total = (int64_t)n_atoms * 4 * H;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
@@ -163,110 +166,168 @@ __global__ void embed_kernel(const float* __restrict__ emb, const int64_t* __res
 int launch_embed(const mlff_dims& d, const float* packed, const PackedOffsets& po, const mlff_system& sys,
                  const WsLayout& L, void* ws, cudaStream_t st) {
     ProfScope prof(PK_OTHER, st);
-    embed_kernel<<<152 * 8, 256, 0, st>>>(packed + po.emb, sys.Z, sys.n_atoms, d.n_species,
+    MLFF_LAUNCH_PDL("embed", embed_kernel, 152 * 8, 256, 0, st, packed + po.emb, sys.Z, sys.n_atoms, d.n_species,
                                           ws_ptr<float>(ws, L.X), ws_ptr<Status>(ws, L.status));
-    MLFF_LAUNCH_CHECK("embed");
     return MLFF_OK;
 }
 
 // ---------------------------------------------------------------- readout
 // Per atom: E_a = w3 . silu(W2 silu(W1 s + b1) + b2) + b3 and, when
 // requested, dE_a/ds written as the adjoint seed (v adjoint = 0).
-constexpr int RO_ATOMS = 8;
-__global__ void __launch_bounds__(128) readout_kernel(const float* __restrict__ P, PackedOffsets po,
-                                                      const float* __restrict__ X, int32_t n_atoms,
-                                                      float* __restrict__ e_atom, float* __restrict__ xbar,
-                                                      int want_grad, const Status* st) {
-    __shared__ float s_in[RO_ATOMS][H];
-    __shared__ float z1[RO_ATOMS][64];
-    __shared__ float h1[RO_ATOMS][64];
-    __shared__ float z2[RO_ATOMS][32];
-    __shared__ float g2[RO_ATOMS][32];
-    __shared__ float g1[RO_ATOMS][64];
-    if (st->code != 0) return;
+// One CTA of 256 threads per SM walks groups of RO_ATOMS atoms; the head's
+// four weight matrices (80 KB) are staged in shared memory once per CTA with
+// independent 128-bit loads, so the dot products read shared memory only.
+constexpr int RO_ATOMS = 32;
+constexpr int RO_NT = 256;
+constexpr int RO_W1T = 0;                       // [H][64]
+constexpr int RO_W2T = RO_W1T + H * 64;         // [64][32]
+constexpr int RO_W2 = RO_W2T + 64 * 32;         // [32][64]
+constexpr int RO_W1 = RO_W2 + 32 * 64;          // [64][H]
+constexpr int RO_S = RO_W1 + 64 * H;            // [RO_ATOMS][H]     s
+constexpr int RO_Z1 = RO_S + RO_ATOMS * H;      // [RO_ATOMS][64]    z1
+constexpr int RO_H1 = RO_Z1 + RO_ATOMS * 64;    // [RO_ATOMS][64]    silu(z1)
+constexpr int RO_G1 = RO_H1 + RO_ATOMS * 64;    // [RO_ATOMS][64]    dE/dz1
+constexpr int RO_Z2 = RO_G1 + RO_ATOMS * 64;    // [RO_ATOMS][32]    z2
+constexpr int RO_G2 = RO_Z2 + RO_ATOMS * 32;    // [RO_ATOMS][32]    dE/dz2
+constexpr int RO_FLOATS = RO_G2 + RO_ATOMS * 32;
+constexpr size_t RO_SMEM = sizeof(float) * RO_FLOATS;
+
+__device__ __forceinline__ void ro_stage(float* dst, const float* __restrict__ src, int n) {
+    const float4* s4 = reinterpret_cast<const float4*>(src);
+    float4* d4 = reinterpret_cast<float4*>(dst);
+    for (int i = threadIdx.x; i < n / 4; i += RO_NT) d4[i] = __ldg(s4 + i);
+}
+
+__global__ void __launch_bounds__(RO_NT) readout_kernel(const float* __restrict__ P, PackedOffsets po,
+                                                        const float* __restrict__ X, int32_t n_atoms,
+                                                        float* __restrict__ e_atom, float* __restrict__ xbar,
+                                                        int want_grad, const Status* st) {
+    extern __shared__ __align__(16) float ro[];
     const int t = threadIdx.x;
-    const float* W1t = P + po.head_w1t;  // [H][64]
-    const float* W1 = P + po.head_w1;    // [64][H]
-    const float* W2t = P + po.head_w2t;  // [64][32]
-    const float* W2 = P + po.head_w2;    // [32][64]
+    ro_stage(ro + RO_W1T, P + po.head_w1t, H * 64);
+    ro_stage(ro + RO_W2T, P + po.head_w2t, 64 * 32);
+    if (want_grad) {
+        ro_stage(ro + RO_W2, P + po.head_w2, 32 * 64);
+        ro_stage(ro + RO_W1, P + po.head_w1, 64 * H);
+    }
+    pdl_wait();   // the weights above overlap the previous kernel
+    pdl_trigger();
+    if (st->code != 0) return;
+    float* S = ro + RO_S;
+    float* Z1 = ro + RO_Z1;
+    float* H1 = ro + RO_H1;
+    float* G1 = ro + RO_G1;
+    float* Z2 = ro + RO_Z2;
+    float* G2 = ro + RO_G2;
     for (int a0 = blockIdx.x * RO_ATOMS; a0 < n_atoms; a0 += gridDim.x * RO_ATOMS) {
-        for (int q = 0; q < RO_ATOMS; ++q) {
-            int a = a0 + q;
-            s_in[q][t] = a < n_atoms ? X[(int64_t)a * 4 * H + t] : 0.0f;
+        // s rows of the group (128-bit, one warp per atom row)
+        for (int i = t; i < RO_ATOMS * (H / 4); i += RO_NT) {
+            const int q = i / (H / 4), k = i % (H / 4), a = a0 + q;
+            reinterpret_cast<float4*>(S + q * H)[k] =
+                a < n_atoms ? __ldg(reinterpret_cast<const float4*>(X + (int64_t)a * 4 * H) + k)
+                            : make_float4(0.f, 0.f, 0.f, 0.f);
         }
         __syncthreads();
-        if (t < 64) {
-            float acc[RO_ATOMS];
+        {   // z1 = W1 s + b1: thread -> output o, atoms 8 (t / 64) .. + 8
+            const int o = t & 63, q0 = (t >> 6) * 8;
+            float acc[8];
+            const float b = P[po.head_b1 + o];
 #pragma unroll
-            for (int q = 0; q < RO_ATOMS; ++q) acc[q] = P[po.head_b1 + t];
-            for (int i = 0; i < H; ++i) {
-                float w = W1t[i * 64 + t];
+            for (int q = 0; q < 8; ++q) acc[q] = b;
+#pragma unroll 4
+            for (int i = 0; i < H; i += 4) {
+                const float w0 = ro[RO_W1T + (i + 0) * 64 + o], w1 = ro[RO_W1T + (i + 1) * 64 + o];
+                const float w2 = ro[RO_W1T + (i + 2) * 64 + o], w3 = ro[RO_W1T + (i + 3) * 64 + o];
 #pragma unroll
-                for (int q = 0; q < RO_ATOMS; ++q) acc[q] = fmaf(w, s_in[q][i], acc[q]);
+                for (int q = 0; q < 8; ++q) {
+                    const float4 x = *reinterpret_cast<const float4*>(S + (q0 + q) * H + i);
+                    acc[q] = fmaf(w3, x.w, fmaf(w2, x.z, fmaf(w1, x.y, fmaf(w0, x.x, acc[q]))));
+                }
             }
 #pragma unroll
-            for (int q = 0; q < RO_ATOMS; ++q) {
-                z1[q][t] = acc[q];
-                h1[q][t] = silu_f(acc[q]);
+            for (int q = 0; q < 8; ++q) {
+                Z1[(q0 + q) * 64 + o] = acc[q];
+                H1[(q0 + q) * 64 + o] = silu_f(acc[q]);
             }
         }
         __syncthreads();
-        if (t < 32) {
-            float acc[RO_ATOMS];
+        {   // z2 = W2 h1 + b2: thread -> output o, atoms 4 (t / 32) .. + 4
+            const int o = t & 31, q0 = (t >> 5) * 4;
+            float acc[4];
+            const float b = P[po.head_b2 + o];
 #pragma unroll
-            for (int q = 0; q < RO_ATOMS; ++q) acc[q] = P[po.head_b2 + t];
-            for (int i = 0; i < 64; ++i) {
-                float w = W2t[i * 32 + t];
+            for (int q = 0; q < 4; ++q) acc[q] = b;
+#pragma unroll 4
+            for (int i = 0; i < 64; i += 4) {
+                const float w0 = ro[RO_W2T + (i + 0) * 32 + o], w1 = ro[RO_W2T + (i + 1) * 32 + o];
+                const float w2 = ro[RO_W2T + (i + 2) * 32 + o], w3 = ro[RO_W2T + (i + 3) * 32 + o];
 #pragma unroll
-                for (int q = 0; q < RO_ATOMS; ++q) acc[q] = fmaf(w, h1[q][i], acc[q]);
+                for (int q = 0; q < 4; ++q) {
+                    const float4 h = *reinterpret_cast<const float4*>(H1 + (q0 + q) * 64 + i);
+                    acc[q] = fmaf(w3, h.w, fmaf(w2, h.z, fmaf(w1, h.y, fmaf(w0, h.x, acc[q]))));
+                }
             }
 #pragma unroll
-            for (int q = 0; q < RO_ATOMS; ++q) z2[q][t] = acc[q];
+            for (int q = 0; q < 4; ++q) {
+                Z2[(q0 + q) * 32 + o] = acc[q];
+                // adjoint seed of the last layer: dE/dz2 = w3 * silu'(z2)
+                G2[(q0 + q) * 32 + o] = P[po.head_w3 + o] * dsilu_f(acc[q]);
+            }
         }
         __syncthreads();
-        if (t < RO_ATOMS) {
-            int a = a0 + t;
-            float e = P[po.head_b3];
-            for (int i = 0; i < 32; ++i) e = fmaf(P[po.head_w3 + i], silu_f(z2[t][i]), e);
-            if (a < n_atoms) e_atom[a] = e;
+        {   // E_a = w3 . silu(z2) + b3: warp w -> atoms 4w .. 4w + 3, lanes over the 32 inputs
+            const int w = t >> 5, lane = t & 31;
+            const float w3 = P[po.head_w3 + lane];
+#pragma unroll
+            for (int q = 4 * w; q < 4 * w + 4; ++q) {
+                float e = w3 * silu_f(Z2[q * 32 + lane]);
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) e += __shfl_xor_sync(0xffffffffu, e, off);
+                if (lane == 0 && a0 + q < n_atoms) e_atom[a0 + q] = e + P[po.head_b3];
+            }
         }
         if (want_grad) {
-            // adjoints: dE/dz2 = w3 * silu'(z2); dE/dz1 = (W2^T dz2) * silu'(z1); dE/ds = W1^T dz1
-            if (t < 32) {
+            {   // dE/dz1 = (W2^T g2) * silu'(z1): thread -> output o, atoms 8 (t / 64) .. + 8
+                const int o = t & 63, q0 = (t >> 6) * 8;
+                float acc[8];
 #pragma unroll
-                for (int q = 0; q < RO_ATOMS; ++q) g2[q][t] = P[po.head_w3 + t] * dsilu_f(z2[q][t]);
-            }
-            __syncthreads();
-            if (t < 64) {
-                float acc[RO_ATOMS];
-#pragma unroll
-                for (int q = 0; q < RO_ATOMS; ++q) acc[q] = 0.0f;
+                for (int q = 0; q < 8; ++q) acc[q] = 0.0f;
+#pragma unroll 4
                 for (int j = 0; j < 32; ++j) {
-                    float w = W2[j * 64 + t];
+                    const float w = ro[RO_W2 + j * 64 + o];
 #pragma unroll
-                    for (int q = 0; q < RO_ATOMS; ++q) acc[q] = fmaf(w, g2[q][j], acc[q]);
+                    for (int q = 0; q < 8; ++q) acc[q] = fmaf(w, G2[(q0 + q) * 32 + j], acc[q]);
                 }
 #pragma unroll
-                for (int q = 0; q < RO_ATOMS; ++q) g1[q][t] = acc[q] * dsilu_f(z1[q][t]);
+                for (int q = 0; q < 8; ++q) G1[(q0 + q) * 64 + o] = acc[q] * dsilu_f(Z1[(q0 + q) * 64 + o]);
             }
             __syncthreads();
-            float acc[RO_ATOMS];
+            {   // dE/ds = W1^T g1: thread -> output o, atoms 16 (t / 128) .. + 16
+                const int o = t & 127, q0 = (t >> 7) * 16;
+                float acc[16];
 #pragma unroll
-            for (int q = 0; q < RO_ATOMS; ++q) acc[q] = 0.0f;
-            for (int j = 0; j < 64; ++j) {
-                float w = W1[j * H + t];
+                for (int q = 0; q < 16; ++q) acc[q] = 0.0f;
+#pragma unroll 2
+                for (int j = 0; j < 64; j += 4) {
+                    const float w0 = ro[RO_W1 + (j + 0) * H + o], w1 = ro[RO_W1 + (j + 1) * H + o];
+                    const float w2 = ro[RO_W1 + (j + 2) * H + o], w3 = ro[RO_W1 + (j + 3) * H + o];
 #pragma unroll
-                for (int q = 0; q < RO_ATOMS; ++q) acc[q] = fmaf(w, g1[q][j], acc[q]);
-            }
-            for (int q = 0; q < RO_ATOMS; ++q) {
-                int a = a0 + q;
-                if (a < n_atoms) {
-                    float* xb = xbar + (int64_t)a * 4 * H;
-                    xb[t] = acc[q];
-                    xb[H + t] = 0.0f;
-                    xb[2 * H + t] = 0.0f;
-                    xb[3 * H + t] = 0.0f;
+                    for (int q = 0; q < 16; ++q) {
+                        const float4 g = *reinterpret_cast<const float4*>(G1 + (q0 + q) * 64 + j);
+                        acc[q] = fmaf(w3, g.w, fmaf(w2, g.z, fmaf(w1, g.y, fmaf(w0, g.x, acc[q]))));
+                    }
                 }
+#pragma unroll
+                for (int q = 0; q < 16; ++q) {
+                    const int a = a0 + q0 + q;
+                    if (a < n_atoms) xbar[(int64_t)a * 4 * H + o] = acc[q];
+                }
+            }
+            // the vector part of the seed is zero
+            for (int i = t; i < RO_ATOMS * (3 * H / 4); i += RO_NT) {
+                const int q = i / (3 * H / 4), k = i % (3 * H / 4), a = a0 + q;
+                if (a < n_atoms)
+                    reinterpret_cast<float4*>(xbar + (int64_t)a * 4 * H + H)[k] = make_float4(0.f, 0.f, 0.f, 0.f);
             }
         }
         __syncthreads();
@@ -276,6 +337,8 @@ __global__ void __launch_bounds__(128) readout_kernel(const float* __restrict__ 
 // FP64 per-structure sums of per-atom energies (fixed-order tree)
 __global__ void energy_sum_kernel(const float* __restrict__ e_atom, const int64_t* __restrict__ mol_ptr,
                                   int32_t n_mol, double* __restrict__ energy, const Status* st) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ double red[256];
     for (int m = blockIdx.x; m < n_mol; m += gridDim.x) {
         int64_t a0 = mol_ptr[m], a1 = mol_ptr[m + 1];
@@ -299,12 +362,17 @@ int launch_readout(const mlff_dims& d, const float* packed, const PackedOffsets&
     float* e_atom = ws_ptr<float>(ws, L.e_atom);
     float* xbar = ws_ptr<float>(ws, L.xbar);  // buffer 0
     const Status* status = ws_ptr<Status>(ws, L.status);
-    int blocks = (int)std::min<int64_t>((sys.n_atoms + RO_ATOMS - 1) / RO_ATOMS, 152 * 8);
-    readout_kernel<<<std::max(blocks, 1), 128, 0, st>>>(packed, po, X, sys.n_atoms, e_atom, xbar, want_grad, status);
-    MLFF_LAUNCH_CHECK("readout");
-    energy_sum_kernel<<<std::min(std::max(sys.n_mol, 1), 152 * 8), 256, 0, st>>>(e_atom, sys.mol_ptr, sys.n_mol,
+    static std::once_flag once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(once, [] {
+        attr_err = cudaFuncSetAttribute(readout_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RO_SMEM);
+    });
+    if (attr_err != cudaSuccess) return cuda_status(attr_err, "readout smem attribute");
+    const int blocks = (int)std::min<int64_t>((sys.n_atoms + RO_ATOMS - 1) / RO_ATOMS, num_sms());
+    MLFF_LAUNCH_PDL("readout", readout_kernel, std::max(blocks, 1), RO_NT, RO_SMEM, st, packed, po, X, sys.n_atoms,
+                    e_atom, xbar, want_grad, status);
+    MLFF_LAUNCH_PDL("energy_sum", energy_sum_kernel, std::min(std::max(sys.n_mol, 1), 152 * 8), 256, 0, st, e_atom, sys.mol_ptr, sys.n_mol,
                                                                                  out.energy, status);
-    MLFF_LAUNCH_CHECK("energy_sum");
     if (out.atom_energy)
         MLFF_CUDA(cudaMemcpyAsync(out.atom_energy, e_atom, sizeof(float) * sys.n_atoms, cudaMemcpyDeviceToDevice, st));
     return MLFF_OK;
@@ -344,6 +412,8 @@ __global__ void forces_kernel(const float4* __restrict__ pos4, const int32_t* __
                               const int32_t* __restrict__ rev, const float4* __restrict__ acc,
                               int32_t n_atoms, float* __restrict__ forces, double* __restrict__ vir_atom,
                               const Status* st) {
+    pdl_wait();
+    pdl_trigger();
     if (st->code != 0) return;
     const int lane = threadIdx.x & 31;
     const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -393,6 +463,8 @@ __global__ void forces_kernel(const float4* __restrict__ pos4, const int32_t* __
 
 __global__ void virial_sum_kernel(const double* __restrict__ vir_atom, const int64_t* __restrict__ mol_ptr,
                                   int32_t n_mol, double* __restrict__ virial, const Status* st) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ double red[9][128];
     for (int m = blockIdx.x; m < n_mol; m += gridDim.x) {
         double s[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -419,15 +491,13 @@ int launch_forces(const mlff_dims& d, const mlff_system& sys, const WsLayout& L,
     double* vir_atom = out.virial ? reinterpret_cast<double*>(ws_ptr<float>(ws, L.xbar) + (int64_t)sys.n_atoms * 4 * H)
                                   : nullptr;
     int blocks = (int)std::min<int64_t>((sys.n_atoms + 3) / 4, 152 * 16);   // 4 atoms (warps) per block
-    forces_kernel<<<std::max(blocks, 1), 128, 0, st>>>(
+    MLFF_LAUNCH_PDL("forces", forces_kernel, std::max(blocks, 1), 128, 0, st, 
         ws_ptr<float4>(ws, L.pos4), ws_ptr<int32_t>(ws, L.atom_mol), sys.box, sys.pbc,
         ws_ptr<int32_t>(ws, L.row_ptr), ws_ptr<int32_t>(ws, L.col), ws_ptr<int32_t>(ws, L.rev),
         ws_ptr<float4>(ws, L.edge_acc), sys.n_atoms, out.forces, vir_atom, status);
-    MLFF_LAUNCH_CHECK("forces");
     if (out.virial) {
-        virial_sum_kernel<<<std::min(std::max(sys.n_mol, 1), 152 * 8), 128, 0, st>>>(vir_atom, sys.mol_ptr, sys.n_mol,
+        MLFF_LAUNCH_PDL("virial_sum", virial_sum_kernel, std::min(std::max(sys.n_mol, 1), 152 * 8), 128, 0, st, vir_atom, sys.mol_ptr, sys.n_mol,
                                                                                       out.virial, status);
-        MLFF_LAUNCH_CHECK("virial_sum");
     }
     return MLFF_OK;
 }

@@ -24,6 +24,8 @@ constexpr int ROW_CAP = 512;        // neighbours one periodic row can hold
 
 // ------------------------------------------------------------------ scan
 __global__ void scan_local_kernel(int32_t* __restrict__ data, int64_t n, int32_t* __restrict__ sums) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ int32_t warp_tot[8];
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     const int64_t base = (int64_t)blockIdx.x * 1024 + (int64_t)t * 4;
@@ -64,6 +66,8 @@ __global__ void scan_local_kernel(int32_t* __restrict__ data, int64_t n, int32_t
 
 // exclusive scan of sums[0..nb) by one block; sums[nb] receives the total
 __global__ void scan_blocks_kernel(int32_t* __restrict__ sums, int64_t nb) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ int32_t warp_tot[32];
     __shared__ int32_t carry;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
@@ -100,6 +104,8 @@ __global__ void scan_blocks_kernel(int32_t* __restrict__ sums, int64_t nb) {
 }
 
 __global__ void scan_add_kernel(int32_t* __restrict__ data, int64_t n, const int32_t* __restrict__ sums) {
+    pdl_wait();
+    pdl_trigger();
     const int64_t base = (int64_t)blockIdx.x * 1024;
     const int32_t add = sums[blockIdx.x];
     for (int i = threadIdx.x; i < 1024; i += blockDim.x) {
@@ -112,13 +118,10 @@ __global__ void scan_add_kernel(int32_t* __restrict__ data, int64_t n, const int
 int launch_scan(int32_t* data, int64_t n, int32_t* tmp, cudaStream_t st) {
     if (n <= 0) return MLFF_OK;
     int64_t nb = (n + 1023) / 1024;
-    scan_local_kernel<<<(unsigned)nb, 256, 0, st>>>(data, n, tmp);
-    MLFF_LAUNCH_CHECK("scan_local");
-    scan_blocks_kernel<<<1, 1024, 0, st>>>(tmp, nb);
-    MLFF_LAUNCH_CHECK("scan_blocks");
+    MLFF_LAUNCH_PDL("scan_local", scan_local_kernel, (unsigned)nb, 256, 0, st, data, n, tmp);
+    MLFF_LAUNCH_PDL("scan_blocks", scan_blocks_kernel, 1, 1024, 0, st, tmp, nb);
     if (nb > 1) {
-        scan_add_kernel<<<(unsigned)nb, 256, 0, st>>>(data, n, tmp);
-        MLFF_LAUNCH_CHECK("scan_add");
+        MLFF_LAUNCH_PDL("scan_add", scan_add_kernel, (unsigned)nb, 256, 0, st, data, n, tmp);
     }
     return MLFF_OK;
 }
@@ -127,6 +130,8 @@ int launch_scan(int32_t* data, int64_t n, int32_t* tmp, cudaStream_t st) {
 __global__ void prep_atoms_kernel(const float* __restrict__ pos, const int64_t* __restrict__ mol_ptr,
                                   int32_t n_mol, int32_t n_atoms, float4* __restrict__ pos4,
                                   int32_t* __restrict__ atom_mol) {
+    pdl_wait();
+    pdl_trigger();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_atoms; i += gridDim.x * blockDim.x) {
         pos4[i] = make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0.0f);
         // last m with mol_ptr[m] <= i
@@ -144,6 +149,8 @@ __global__ void prep_atoms_kernel(const float* __restrict__ pos, const int64_t* 
 __global__ void mol_grid_kernel(const int64_t* __restrict__ mol_ptr, const float* __restrict__ box,
                                 const uint8_t* __restrict__ pbc, int32_t n_mol, float cutoff,
                                 int4* __restrict__ grid, Status* st) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ int32_t warp_tot[32];
     __shared__ int32_t carry;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
@@ -222,6 +229,8 @@ __global__ void cell_count_kernel(const float4* __restrict__ pos4, const int32_t
                                   const float* __restrict__ box, const uint8_t* __restrict__ pbc,
                                   const int4* __restrict__ grid, int32_t n_atoms,
                                   int32_t* __restrict__ atom_cell, int32_t* __restrict__ cell_count) {
+    pdl_wait();
+    pdl_trigger();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_atoms; i += gridDim.x * blockDim.x) {
         int m = atom_mol[i];
         if (!mol_periodic(pbc, box, m)) { atom_cell[i] = -1; continue; }
@@ -240,6 +249,8 @@ __global__ void cell_count_kernel(const float4* __restrict__ pos4, const int32_t
 __global__ void cell_fill_kernel(const int32_t* __restrict__ atom_cell, const int32_t* __restrict__ cell_start,
                                  int32_t n_atoms, int32_t* __restrict__ cell_fill,
                                  int32_t* __restrict__ cell_atoms) {
+    pdl_wait();
+    pdl_trigger();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_atoms; i += gridDim.x * blockDim.x) {
         int c = atom_cell[i];
         if (c < 0) continue;
@@ -270,6 +281,8 @@ struct NbrArgs {
 
 template <bool FILL>
 __global__ void __launch_bounds__(NBR_WARPS * 32) nbr_rows_kernel(NbrArgs a) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ int32_t sbuf[FILL ? NBR_WARPS : 1][FILL ? ROW_CAP : 1];
     if (FILL && a.st->code != 0) return;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -365,6 +378,8 @@ __global__ void __launch_bounds__(NBR_WARPS * 32) nbr_rows_kernel(NbrArgs a) {
 
 __global__ void check_edges_kernel(const int32_t* __restrict__ row_ptr, int32_t n_atoms, int64_t cap,
                                    const int32_t* __restrict__ counts_total, Status* st) {
+    pdl_wait();
+    pdl_trigger();
     int64_t e = (int64_t)(uint32_t)row_ptr[n_atoms];
     st->n_edges = (int32_t)(e & 0x7fffffff);
     st->n_edges_hi = (int32_t)(e >> 31);
@@ -376,6 +391,8 @@ __global__ void check_edges_kernel(const int32_t* __restrict__ row_ptr, int32_t 
 __global__ void rev_kernel(const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
                            const int32_t* __restrict__ erecv, int32_t n_atoms,
                            int32_t* __restrict__ rev, Status* st) {
+    pdl_wait();
+    pdl_trigger();
     if (st->code != 0) return;
     const int32_t E = row_ptr[n_atoms];
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < E; k += gridDim.x * blockDim.x) {
@@ -396,6 +413,8 @@ __global__ void rev_kernel(const int32_t* __restrict__ row_ptr, const int32_t* _
 // receiver whose row starts at or after p*E/P
 __global__ void partition_kernel(const int32_t* __restrict__ row_ptr, int32_t n_atoms, int32_t P,
                                  int32_t* __restrict__ part) {
+    pdl_wait();
+    pdl_trigger();
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p > P) return;
     const int64_t E = row_ptr[n_atoms];
@@ -412,9 +431,8 @@ __global__ void partition_kernel(const int32_t* __restrict__ row_ptr, int32_t n_
 
 int launch_partition(const WsLayout& L, void* ws, cudaStream_t st) {
     ProfScope prof(PK_NEIGHBORS, st);
-    partition_kernel<<<(L.P + 1 + 255) / 256, 256, 0, st>>>(ws_ptr<int32_t>(ws, L.row_ptr), L.N, L.P,
+    MLFF_LAUNCH_PDL("partition", partition_kernel, (L.P + 1 + 255) / 256, 256, 0, st, ws_ptr<int32_t>(ws, L.row_ptr), L.N, L.P,
                                                             ws_ptr<int32_t>(ws, L.part));
-    MLFF_LAUNCH_CHECK("partition");
     return MLFF_OK;
 }
 
@@ -430,25 +448,21 @@ int launch_neighbors(const mlff_dims& d, const mlff_system& sys, const WsLayout&
     const bool any_pbc = sys.pbc != nullptr && sys.box != nullptr;
     const int tb = 256;
     const int gb = (int)std::min<int64_t>((N + tb - 1) / tb, 152 * 16);
-    prep_atoms_kernel<<<std::max(gb, 1), tb, 0, st>>>(sys.pos, sys.mol_ptr, sys.n_mol, N, pos4, atom_mol);
-    MLFF_LAUNCH_CHECK("prep_atoms");
+    MLFF_LAUNCH_PDL("prep_atoms", prep_atoms_kernel, std::max(gb, 1), tb, 0, st, sys.pos, sys.mol_ptr, sys.n_mol, N, pos4, atom_mol);
     int4* grid = ws_ptr<int4>(ws, L.mol_grid);
     int32_t* cell_count = ws_ptr<int32_t>(ws, L.cell_count);
     int32_t* cell_fill = ws_ptr<int32_t>(ws, L.cell_fill);
     int32_t* cell_atoms = ws_ptr<int32_t>(ws, L.cell_atoms);
     int32_t* atom_cell = ws_ptr<int32_t>(ws, L.atom_cell);
     if (any_pbc) {
-        mol_grid_kernel<<<1, 1024, 0, st>>>(sys.mol_ptr, sys.box, sys.pbc, sys.n_mol, d.cutoff, grid, status);
-        MLFF_LAUNCH_CHECK("mol_grid");
+        MLFF_LAUNCH_PDL("mol_grid", mol_grid_kernel, 1, 1024, 0, st, sys.mol_ptr, sys.box, sys.pbc, sys.n_mol, d.cutoff, grid, status);
         MLFF_CUDA(cudaMemsetAsync(cell_count, 0, sizeof(int32_t) * (L.ncell_cap + 1), st));
         MLFF_CUDA(cudaMemsetAsync(cell_fill, 0, sizeof(int32_t) * L.ncell_cap, st));
-        cell_count_kernel<<<std::max(gb, 1), tb, 0, st>>>(pos4, atom_mol, sys.box, sys.pbc, grid, N,
+        MLFF_LAUNCH_PDL("cell_count", cell_count_kernel, std::max(gb, 1), tb, 0, st, pos4, atom_mol, sys.box, sys.pbc, grid, N,
                                                           atom_cell, cell_count);
-        MLFF_LAUNCH_CHECK("cell_count");
         int r = launch_scan(cell_count, L.ncell_cap + 1, scan_tmp, st);
         if (r) return r;
-        cell_fill_kernel<<<std::max(gb, 1), tb, 0, st>>>(atom_cell, cell_count, N, cell_fill, cell_atoms);
-        MLFF_LAUNCH_CHECK("cell_fill");
+        MLFF_LAUNCH_PDL("cell_fill", cell_fill_kernel, std::max(gb, 1), tb, 0, st, atom_cell, cell_count, N, cell_fill, cell_atoms);
     }
     NbrArgs a;
     a.pos4 = pos4; a.atom_mol = atom_mol; a.mol_ptr = sys.mol_ptr; a.box = sys.box; a.pbc = sys.pbc;
@@ -457,17 +471,13 @@ int launch_neighbors(const mlff_dims& d, const mlff_system& sys, const WsLayout&
     a.col = ws_ptr<int32_t>(ws, L.col); a.erecv = ws_ptr<int32_t>(ws, L.erecv); a.st = status;
     const int rows_blocks = (int)std::max<int64_t>(1, std::min<int64_t>((N + NBR_WARPS - 1) / NBR_WARPS, 152 * 32));
     MLFF_CUDA(cudaMemsetAsync(row_ptr + N, 0, sizeof(int32_t), st));
-    nbr_rows_kernel<false><<<rows_blocks, NBR_WARPS * 32, 0, st>>>(a);
-    MLFF_LAUNCH_CHECK("nbr_count");
+    MLFF_LAUNCH_PDL("nbr_count", nbr_rows_kernel<false>, rows_blocks, NBR_WARPS * 32, 0, st, a);
     int r = launch_scan(row_ptr, (int64_t)N + 1, scan_tmp, st);
     if (r) return r;
-    check_edges_kernel<<<1, 1, 0, st>>>(row_ptr, N, L.cap, nullptr, status);
-    MLFF_LAUNCH_CHECK("check_edges");
-    nbr_rows_kernel<true><<<rows_blocks, NBR_WARPS * 32, 0, st>>>(a);
-    MLFF_LAUNCH_CHECK("nbr_fill");
+    MLFF_LAUNCH_PDL("check_edges", check_edges_kernel, 1, 1, 0, st, row_ptr, N, L.cap, nullptr, status);
+    MLFF_LAUNCH_PDL("nbr_fill", nbr_rows_kernel<true>, rows_blocks, NBR_WARPS * 32, 0, st, a);
     const int eb = (int)std::min<int64_t>((L.cap + 255) / 256, 152 * 16);
-    rev_kernel<<<std::max(eb, 1), 256, 0, st>>>(row_ptr, a.col, a.erecv, N, ws_ptr<int32_t>(ws, L.rev), status);
-    MLFF_LAUNCH_CHECK("rev");
+    MLFF_LAUNCH_PDL("rev", rev_kernel, std::max(eb, 1), 256, 0, st, row_ptr, a.col, a.erecv, N, ws_ptr<int32_t>(ws, L.rev), status);
     return MLFF_OK;
 }
 
@@ -483,20 +493,16 @@ int launch_neighbors_into(const mlff_dims& d, const mlff_system& sys, const NbrB
     const bool any_pbc = sys.pbc != nullptr && sys.box != nullptr;
     const int tb = 256;
     const int gb = (int)std::max<int64_t>(1, std::min<int64_t>((N + tb - 1) / tb, 152 * 16));
-    prep_atoms_kernel<<<gb, tb, 0, st>>>(sys.pos, sys.mol_ptr, sys.n_mol, N, b.pos4, b.atom_mol);
-    MLFF_LAUNCH_CHECK("prep_atoms");
+    MLFF_LAUNCH_PDL("prep_atoms", prep_atoms_kernel, gb, tb, 0, st, sys.pos, sys.mol_ptr, sys.n_mol, N, b.pos4, b.atom_mol);
     if (any_pbc) {
-        mol_grid_kernel<<<1, 1024, 0, st>>>(sys.mol_ptr, sys.box, sys.pbc, sys.n_mol, d.cutoff, b.mol_grid, b.status);
-        MLFF_LAUNCH_CHECK("mol_grid");
+        MLFF_LAUNCH_PDL("mol_grid", mol_grid_kernel, 1, 1024, 0, st, sys.mol_ptr, sys.box, sys.pbc, sys.n_mol, d.cutoff, b.mol_grid, b.status);
         MLFF_CUDA(cudaMemsetAsync(b.cell_count, 0, sizeof(int32_t) * (b.ncell_cap + 1), st));
         MLFF_CUDA(cudaMemsetAsync(b.cell_fill, 0, sizeof(int32_t) * b.ncell_cap, st));
-        cell_count_kernel<<<gb, tb, 0, st>>>(b.pos4, b.atom_mol, sys.box, sys.pbc, b.mol_grid, N, b.atom_cell,
+        MLFF_LAUNCH_PDL("cell_count", cell_count_kernel, gb, tb, 0, st, b.pos4, b.atom_mol, sys.box, sys.pbc, b.mol_grid, N, b.atom_cell,
                                              b.cell_count);
-        MLFF_LAUNCH_CHECK("cell_count");
         int r = launch_scan(b.cell_count, b.ncell_cap + 1, b.scan_tmp, st);
         if (r) return r;
-        cell_fill_kernel<<<gb, tb, 0, st>>>(b.atom_cell, b.cell_count, N, b.cell_fill, b.cell_atoms);
-        MLFF_LAUNCH_CHECK("cell_fill");
+        MLFF_LAUNCH_PDL("cell_fill", cell_fill_kernel, gb, tb, 0, st, b.atom_cell, b.cell_count, N, b.cell_fill, b.cell_atoms);
     }
     NbrArgs a;
     a.pos4 = b.pos4; a.atom_mol = b.atom_mol; a.mol_ptr = sys.mol_ptr; a.box = sys.box; a.pbc = sys.pbc;
@@ -505,14 +511,11 @@ int launch_neighbors_into(const mlff_dims& d, const mlff_system& sys, const NbrB
     a.col = b.col; a.erecv = b.erecv; a.st = b.status;
     const int rows_blocks = (int)std::max<int64_t>(1, std::min<int64_t>((N + NBR_WARPS - 1) / NBR_WARPS, 152 * 32));
     MLFF_CUDA(cudaMemsetAsync(b.row_ptr + N, 0, sizeof(int32_t), st));
-    nbr_rows_kernel<false><<<rows_blocks, NBR_WARPS * 32, 0, st>>>(a);
-    MLFF_LAUNCH_CHECK("nbr_count");
+    MLFF_LAUNCH_PDL("nbr_count", nbr_rows_kernel<false>, rows_blocks, NBR_WARPS * 32, 0, st, a);
     int r = launch_scan(b.row_ptr, (int64_t)N + 1, b.scan_tmp, st);
     if (r) return r;
-    check_edges_kernel<<<1, 1, 0, st>>>(b.row_ptr, N, b.cap, nullptr, b.status);
-    MLFF_LAUNCH_CHECK("check_edges");
-    nbr_rows_kernel<true><<<rows_blocks, NBR_WARPS * 32, 0, st>>>(a);
-    MLFF_LAUNCH_CHECK("nbr_fill");
+    MLFF_LAUNCH_PDL("check_edges", check_edges_kernel, 1, 1, 0, st, b.row_ptr, N, b.cap, nullptr, b.status);
+    MLFF_LAUNCH_PDL("nbr_fill", nbr_rows_kernel<true>, rows_blocks, NBR_WARPS * 32, 0, st, a);
     return MLFF_OK;
 }
 

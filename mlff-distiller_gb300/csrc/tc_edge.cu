@@ -178,6 +178,8 @@ __device__ __forceinline__ uint32_t et_off(int row, int k) {
 __global__ void __launch_bounds__(1024) etile_index_kernel(const int32_t* __restrict__ row_ptr,
                                                            const int32_t* __restrict__ part, int P,
                                                            int32_t* __restrict__ base) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ int cf[1024], cb[1024];
     __shared__ int carry[2];
     const int t = threadIdx.x;
@@ -221,6 +223,8 @@ __global__ void __launch_bounds__(1024) etile_index_kernel(const int32_t* __rest
 template <bool REV>
 __global__ void __launch_bounds__(256) etile_fill_kernel(EdgeArgs a, const int32_t* __restrict__ base,
                                                          unsigned char* __restrict__ out) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ float cent[RMAX], gam[RMAX];
     if (threadIdx.x < RMAX) {
         cent[threadIdx.x] = a.centers[threadIdx.x];
@@ -256,14 +260,11 @@ __global__ void __launch_bounds__(256) etile_fill_kernel(EdgeArgs a, const int32
 }
 
 int launch_etiles(const EdgeArgs& a, int32_t* base, unsigned char* fwd, unsigned char* rev, cudaStream_t st) {
-    etile_index_kernel<<<1, 1024, 0, st>>>(a.row_ptr, a.part, a.nparts, base);
-    MLFF_LAUNCH_CHECK("etile_index");
+    MLFF_LAUNCH_PDL("etile_index", etile_index_kernel, 1, 1024, 0, st, a.row_ptr, a.part, a.nparts, base);
     // tiles of a partition spread over gridDim.y blocks
-    etile_fill_kernel<false><<<dim3(a.nparts, 16), 256, 0, st>>>(a, base, fwd);
-    MLFF_LAUNCH_CHECK("etile_fill_fwd");
+    MLFF_LAUNCH_PDL("etile_fill_fwd", etile_fill_kernel<false>, dim3(a.nparts, 16), 256, 0, st, a, base, fwd);
     if (rev) {
-        etile_fill_kernel<true><<<dim3(a.nparts, 32), 256, 0, st>>>(a, base, rev);
-        MLFF_LAUNCH_CHECK("etile_fill_rev");
+        MLFF_LAUNCH_PDL("etile_fill_rev", etile_fill_kernel<true>, dim3(a.nparts, 32), 256, 0, st, a, base, rev);
     }
     return MLFF_OK;
 }
@@ -433,6 +434,9 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
     volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + F_OFF_MISC + 4);
     uint32_t* ccount_s = reinterpret_cast<uint32_t*>(smem + F_OFF_MISC + 8);
 
+    // waits for the previous kernel at entry: reading the status word first
+    // and returning early keeps the main loop's register allocation lean
+    pdl_wait();
     if (a.st->code != 0) return;
     const int t = threadIdx.x, w = t >> 5, lane = t & 31;
     const unsigned char* w2lo = w2g + W2_HALF;
@@ -478,6 +482,7 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
     fence_before_sync();
     __syncthreads();
     fence_after_sync();
+    pdl_trigger();   // after the TMEM allocation
 
     bool aborted = false;
     uint32_t e_phase = 0, e_issued = 0;   // E-tile copies: barrier phase, copies issued (thread 32)
@@ -755,6 +760,9 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
     volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + B_OFF_MISC + 4);
     uint32_t* ccount_s = reinterpret_cast<uint32_t*>(smem + B_OFF_MISC + 8);
 
+    // waits for the previous kernel at entry: reading the status word first
+    // and returning early keeps the main loop's register allocation lean
+    pdl_wait();
     if (a.st->code != 0) return;
     const int t = threadIdx.x, w = t >> 5, lane = t & 31;
     const unsigned char* w2lo = w2g + W2_HALF;
@@ -799,6 +807,7 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
     fence_before_sync();
     __syncthreads();
     fence_after_sync();
+    pdl_trigger();   // after the TMEM allocation
     const int rs_idx = reduce_scatter8_index(lane);
 
     bool aborted = false;
@@ -1028,7 +1037,7 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                     dd += rr[0];
                     if (ww >= 4) du[(ww >> 2) - 1] += rr[1];
                 }
-                float4 ea = a.eacc[t0 + t];
+                float4 ea = a.eacc_init ? make_float4(0.f, 0.f, 0.f, 0.f) : a.eacc[t0 + t];
                 ea.x += dd;
                 ea.y += du[0];
                 ea.z += du[1];
@@ -1085,8 +1094,7 @@ int launch_edge_fwd_tc(const EdgeArgs& a, int layer, cudaStream_t st) {
     if (attr_err != cudaSuccess) return cuda_status(attr_err, "edge_fwd_tc smem attribute");
     const unsigned char* w1 = reinterpret_cast<const unsigned char*>(a.P + a.lo.w1_bf);
     const unsigned char* w2 = reinterpret_cast<const unsigned char*>(a.P + a.lo.w2_bf);
-    edge_fwd_tc_kernel<<<tc_grid(a.nparts), NT, F_SMEM, st>>>(a, w1, w2);
-    MLFF_LAUNCH_CHECK("edge_fwd_tc");
+    MLFF_LAUNCH_PDL("edge_fwd_tc", edge_fwd_tc_kernel, tc_grid(a.nparts), NT, F_SMEM, st, a, w1, w2);
     return MLFF_OK;
 }
 
@@ -1100,8 +1108,7 @@ int launch_edge_bwd_tc(const EdgeArgs& a, int layer, cudaStream_t st) {
     if (attr_err != cudaSuccess) return cuda_status(attr_err, "edge_bwd_tc smem attribute");
     const unsigned char* w1 = reinterpret_cast<const unsigned char*>(a.P + a.lo.w1_bf);
     const unsigned char* w2 = reinterpret_cast<const unsigned char*>(a.P + a.lo.w2_bf);
-    edge_bwd_tc_kernel<<<tc_grid(a.nparts), NT, B_SMEM, st>>>(a, w1, w2);
-    MLFF_LAUNCH_CHECK("edge_bwd_tc");
+    MLFF_LAUNCH_PDL("edge_bwd_tc", edge_bwd_tc_kernel, tc_grid(a.nparts), NT, B_SMEM, st, a, w1, w2);
     return MLFF_OK;
 }
 

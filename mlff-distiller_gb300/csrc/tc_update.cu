@@ -201,7 +201,6 @@ __global__ void __launch_bounds__(UNT, 1) update_fwd_tc_kernel(const float* __re
     uint64_t* empty = full + URING;
     uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + UF_OFF_MISC);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + UF_OFF_MISC + 4);
-    if (st->code != 0) return;
     const int t = threadIdx.x, w = t >> 5, lane = t & 31;
     const int ntiles = (n_atoms + UN - 1) / UN;
     if (w == 0) {
@@ -232,6 +231,11 @@ __global__ void __launch_bounds__(UNT, 1) update_fwd_tc_kernel(const float* __re
     const uint32_t P_end = (uint32_t)my_tiles * 40;
     const bool producer = t == 32;
     if (producer && !ustream_fill(ws, min((uint32_t)URING, P_end))) ufail(ctl, 20);
+    // everything above reads packed weights only and overlaps the previous kernel
+    pdl_wait();
+    if (t == 0 && st->code != 0) *abort_flag = 1;
+    __syncthreads();
+    pdl_trigger();
     const int q = w & 3, hh = w >> 2, c = 32 * q + lane;
     const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
     uint32_t P0 = 0;
@@ -415,8 +419,8 @@ int launch_update_fwd_tc(const float* packed, const LayerOffsets& lo, const WsLa
     float* ua = ws_ptr<float>(ws, L.ua) + (int64_t)layer * L.N * H3;
     const int ntiles = (L.N + UN - 1) / UN;
     const int grid = std::max(1, std::min(ntiles, num_sms()));
-    update_fwd_tc_kernel<<<grid, UNT, UF_SMEM, st>>>(packed, lo, Xt, L.N, Xout, uz, ua, ws_ptr<Status>(ws, L.status));
-    MLFF_LAUNCH_CHECK("update_fwd_tc");
+    MLFF_LAUNCH_PDL("update_fwd_tc", update_fwd_tc_kernel, grid, UNT, UF_SMEM, st, packed, lo, Xt, L.N, Xout, uz, ua,
+                    ws_ptr<Status>(ws, L.status));
     return MLFF_OK;
 }
 
@@ -449,7 +453,6 @@ __global__ void __launch_bounds__(UNT, 1) update_bwd_tc_kernel(const float* __re
     uint64_t* empty = full + URING;
     uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + UB_OFF_MISC);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + UB_OFF_MISC + 4);
-    if (st->code != 0) return;
     const int t = threadIdx.x, w = t >> 5, lane = t & 31;
     const int ntiles = (n_atoms + UN - 1) / UN;
     if (w == 0) {
@@ -478,6 +481,11 @@ __global__ void __launch_bounds__(UNT, 1) update_bwd_tc_kernel(const float* __re
     const uint32_t P_end = (uint32_t)my_tiles * 40;
     const bool producer = t == 32;
     if (producer && !ustream_fill(ws, min((uint32_t)URING, P_end))) ufail(ctl, 30);
+    // everything above reads packed weights only and overlaps the previous kernel
+    pdl_wait();
+    if (t == 0 && st->code != 0) *abort_flag = 1;
+    __syncthreads();
+    pdl_trigger();
     const int q = w & 3, hh = w >> 2, c = 32 * q + lane;
     const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
     uint32_t P0 = 0;
@@ -660,9 +668,8 @@ int launch_update_bwd_tc(const float* packed, const LayerOffsets& lo, const WsLa
     const float* ua = ws_ptr<float>(ws, L.ua) + (int64_t)layer * L.N * H3;
     const int ntiles = (L.N + UN - 1) / UN;
     const int grid = std::max(1, std::min(ntiles, num_sms()));
-    update_bwd_tc_kernel<<<grid, UNT, UB_SMEM, st>>>(packed, lo, Xt, uz, ua, xbar_out, L.N, xtbar,
-                                                     ws_ptr<Status>(ws, L.status));
-    MLFF_LAUNCH_CHECK("update_bwd_tc");
+    MLFF_LAUNCH_PDL("update_bwd_tc", update_bwd_tc_kernel, grid, UNT, UB_SMEM, st, packed, lo, Xt, uz, ua, xbar_out,
+                    L.N, xtbar, ws_ptr<Status>(ws, L.status));
     return MLFF_OK;
 }
 

@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(128) edge_bwd_simt_kernel(EdgeArgs a) {
             }
             __syncthreads();
             if (t < n) {
-                float4 acc = a.eacc[t0 + t];
+                float4 acc = a.eacc_init ? make_float4(0.f, 0.f, 0.f, 0.f) : a.eacc[t0 + t];
                 acc.x += red[0][t][0] + red[1][t][0] + red[2][t][0] + red[3][t][0];
                 acc.y += red[0][t][1] + red[1][t][1] + red[2][t][1] + red[3][t][1];
                 acc.z += red[0][t][2] + red[1][t][2] + red[2][t][2] + red[3][t][2];
@@ -298,6 +298,8 @@ int launch_etiles(const EdgeArgs& a, int32_t* base, unsigned char* fwd, unsigned
 
 
 __global__ void edge_geom_kernel(EdgeArgs a, float4* __restrict__ geo) {
+    pdl_wait();
+    pdl_trigger();
     if (a.st->code != 0) return;
     const int n_edges = a.row_ptr[a.n_atoms];
     __shared__ float4 us[256];
@@ -313,6 +315,8 @@ __global__ void edge_geom_kernel(EdgeArgs a, float4* __restrict__ geo) {
 // writes the gathered part of dE/dX only)
 __global__ void add_rows_kernel(float4* __restrict__ dst, const float4* __restrict__ src, int64_t n4,
                                 const Status* st) {
+    pdl_wait();
+    pdl_trigger();
     if (st->code != 0) return;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n4; i += (int64_t)gridDim.x * blockDim.x) {
         float4 d = dst[i];
@@ -328,9 +332,8 @@ __global__ void add_rows_kernel(float4* __restrict__ dst, const float4* __restri
 static int add_rows(float* dst, const float* src, int64_t n, const Status* st, cudaStream_t s) {
     const int64_t n4 = n / 4;
     const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((n4 + 255) / 256, 152 * 8));
-    add_rows_kernel<<<blocks, 256, 0, s>>>(reinterpret_cast<float4*>(dst), reinterpret_cast<const float4*>(src), n4,
+    MLFF_LAUNCH_PDL("add_rows", add_rows_kernel, blocks, 256, 0, s, reinterpret_cast<float4*>(dst), reinterpret_cast<const float4*>(src), n4,
                                            st);
-    MLFF_LAUNCH_CHECK("add_rows");
     return MLFF_OK;
 }
 
@@ -366,8 +369,7 @@ int run_tuned(const mlff_dims& d, const float* P, const PackedOffsets& po, const
         float4* geo = ws_ptr<float4>(ws, L.geo);
         ProfScope prof(PK_NEIGHBORS, st);
         const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((L.cap + 255) / 256, 152 * 8));
-        edge_geom_kernel<<<blocks, 256, 0, st>>>(a, geo);
-        MLFF_LAUNCH_CHECK("edge_geom");
+        MLFF_LAUNCH_PDL("edge_geom", edge_geom_kernel, blocks, 256, 0, st, a, geo);
         a.geo = geo;
         // RBF x cutoff tiles for every edge tile of every layer (and their
         // d-derivative for the reverse pass when forces are asked for)
@@ -398,8 +400,6 @@ int run_tuned(const mlff_dims& d, const float* P, const PackedOffsets& po, const
     const bool want_grad = out.forces != nullptr || out.virial != nullptr;
     if ((r = launch_readout(d, P, po, sys, L, ws, out, want_grad ? 1 : 0, st))) return r;
     if (!want_grad) return MLFF_OK;
-    MLFF_CUDA(cudaMemsetAsync(a.eacc, 0, sizeof(float4) * L.cap, st));
-    prof_launch(PK_OTHER);   // the memset above
     float* xbo = ws_ptr<float>(ws, L.xbar);
     float* xtb = xbo + NX;
     for (int l = d.n_layers - 1; l >= 0; --l) {
@@ -411,6 +411,7 @@ int run_tuned(const mlff_dims& d, const float* P, const PackedOffsets& po, const
         a.xtbar = xtb;
         a.xbar = xbo;
         a.write_nodes = l > 0 ? 1 : 0;
+        a.eacc_init = l == d.n_layers - 1 ? 1 : 0;
         {
             ProfScope prof(PK_EDGE_BWD, st);
             if (tc) {
