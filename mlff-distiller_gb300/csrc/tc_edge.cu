@@ -13,17 +13,23 @@
 //     coalesced gathers of the senders' feature rows;
 //   * split-FP16 operands: x = hi + lo (both fp16), three MMAs per K-step
 //     (hi*hi + hi*lo + lo*hi) with FP32 accumulation in TMEM;
-//   * W1 (128 x 32) and the hi half of W2 (384 x 128) stay in shared
-//     memory; the lo half of W2 streams through a ring of 4 KB tiles filled
-//     by cp.async.bulk and recycled by tcgen05.commit on per-slot mbarriers
-//     (one SM's bulk stream, ~27 B/clk, cannot feed the whole of W2 per
-//     tile at MMA speed, half of it it can);
+//   * operands resident for the whole launch: W1 (128 x 32), the hi half
+//     of W2 (384 x 128) and the lo half of W2's third chunk in shared
+//     memory, the lo halves of chunks 0 and 1 in TMEM (A operands of
+//     tcgen05.mma with A in tensor memory);
+//   * the E tiles (RBF x cutoff, split fp16) are computed once per call for
+//     all layers and bulk-copied per edge tile; per-tile edge arrays are
+//     fetched with cp.async while the previous tile's epilogue runs;
+//   * GEMM2's three 128-channel chunks are issued by three threads: a thread
+//     stalls on tcgen05.mma issue while the tensor core is busy (about one
+//     MMA per 50 cycles from one thread), three keep it saturated;
 //   * every wait is bounded (clock64 budget); on expiry the kernel records
 //     MLFF_ERR_TIMEOUT, drains its own copies, frees TMEM and returns.
 //
-// Forward: 128-edge tiles, TMEM columns [0,128) = z^T, [128,512) = f^T.
-// Reverse: 64-edge tiles, TMEM columns [0,64) z^T, [64,128) z'^T,
-// [128,320) f^T, [320,512) f'^T (f' = df/dd, forward mode).
+// TMEM (512 columns): [0,128) lo halves of W2 chunks 0 and 1; [128,512) the
+// GEMM2 accumulators (forward: 128-edge tiles, chunk g at 128 + 128 g;
+// reverse: 64-edge tiles with [f | f'] per chunk, f' = df/dd in forward
+// mode); GEMM1's z (and z') alias chunk 2 until epilogue 1 has read them.
 #include <cuda_fp16.h>
 #include <mutex>
 #include "common.cuh"
@@ -41,7 +47,7 @@ constexpr uint32_t SLAB = 2 * A_TILE;         // hi + lo of one 128 x 16 block (
 constexpr int W2_TILES = 24;                  // 3 channel chunks x 8 K-steps, q = g * 8 + s
 constexpr uint32_t W1_BYTES = 2 * SLAB;       // 2 K-steps
 constexpr uint32_t W2_HALF = W2_TILES * A_TILE;   // all hi tiles (96 KB), then all lo tiles
-constexpr int NSLOT = 8;                      // ring: the 8 lo tiles of W2 chunk 2, one round per edge tile
+constexpr uint32_t W2L_BYTES = 8 * A_TILE;    // lo tiles of W2 chunk 2 (resident in shared memory)
 
 // TMEM columns (512 allocated): [0,128) the lo halves of W2 chunks 0 and 1
 // as MMA A operands (chunk g, K-step s at 64 g + 8 s); [128,512) the GEMM2
@@ -109,16 +115,6 @@ __device__ __forceinline__ void signal_timeout(const EdgeArgs& a, volatile int* 
     *abort_flag = 1;
 }
 
-// Ring producer: the 8 lo tiles of W2 chunk 2 (tiles 16..23), one per slot.
-// Called once the MMAs of the previous edge tile have completed.
-__device__ __forceinline__ void fill_lo_ring(unsigned char* ring, const unsigned char* w2lo, uint64_t* full) {
-#pragma unroll 1
-    for (int slot = 0; slot < NSLOT; ++slot) {
-        mbar_expect_tx(&full[slot], A_TILE);
-        bulk_g2s(ring + slot * A_TILE, w2lo + (size_t)(16 + slot) * A_TILE, A_TILE, &full[slot]);
-    }
-}
-
 // Lo halves of W2 chunks 0 and 1 into TMEM columns [0,128), as A operands,
 // from their packed TMEM image: warp (q, r) writes rows 32q..32q+31 (its
 // TMEM lane quarter), columns 32r..32r+31 (K-steps 4r..4r+3 of the 16).
@@ -129,11 +125,15 @@ __device__ __forceinline__ void load_w2_lo_tmem(uint32_t lane_base, const uint32
     tmem_st32u(lane_base + TM_W2LO + 32 * r, v);
 }
 
-// Resident hi half of W2: six 16 KB bulk copies on one mbarrier.
-__device__ __forceinline__ void load_w2_hi(unsigned char* dst, const unsigned char* w2hi, uint64_t* bar) {
-    mbar_expect_tx(bar, W2_HALF);
+// Resident W2 operands on one mbarrier: all 24 hi tiles (six 16 KB bulk
+// copies), then the 8 lo tiles of chunk 2 (the lo tiles of chunks 0 and 1 are
+// TMEM operands).
+__device__ __forceinline__ void load_w2_resident(unsigned char* hi, unsigned char* lo2, const unsigned char* w2g,
+                                                 uint64_t* bar) {
+    mbar_expect_tx(bar, W2_HALF + W2L_BYTES);
 #pragma unroll
-    for (int i = 0; i < 6; ++i) bulk_g2s(dst + i * (W2_HALF / 6), w2hi + i * (W2_HALF / 6), W2_HALF / 6, bar);
+    for (int i = 0; i < 6; ++i) bulk_g2s(hi + i * (W2_HALF / 6), w2g + i * (W2_HALF / 6), W2_HALF / 6, bar);
+    bulk_g2s(lo2, w2g + W2_HALF + 16 * A_TILE, W2L_BYTES, bar);
 }
 
 // rbf(d)_r * fc(d) for r in [r0, r0 + 16) (0 beyond R or for padding edges)
@@ -337,39 +337,33 @@ __device__ __forceinline__ int reduce_scatter8_index(int lane) {
     return ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
 }
 
-// GEMM2 of one tile, issued by one thread: D chunk g (TMEM columns
-// 128 + 128 g) += W2[g] B^T with B a 128-row split-fp16 tile at Hs (hi half,
-// then lo half HALF128 bytes later).  Per K-step and chunk: the resident hi
-// tile (shared memory) times both halves of B, then the lo tile times the hi
-// half -- from TMEM for chunks 0 and 1, from the ring slot for chunk 2.  Every
-// MMA accumulates (the epilogue filled TMEM with the bias).  `round` is the
-// ring round of this tile.  Returns false on a ring timeout.
+// Chunk g of GEMM2 for one 128-row B tile: D (TMEM columns 128 + 128 g) +=
+// W2[g] B^T with B the split-fp16 tile at Hs (hi half, then lo half HALF128
+// bytes later).  Per K-step: the resident hi tile times both halves of B,
+// then the lo tile (TMEM for chunks 0 and 1, shared memory for chunk 2)
+// times the hi half.  Every MMA accumulates (the epilogue filled TMEM with
+// the bias).  The three chunks are issued by three threads in parallel: a
+// thread issues about one MMA per 50 cycles and stalls while the tensor core
+// is busy, so one issuer adds its own latency to every MMA; each chunk keeps
+// a fixed accumulation order.
 constexpr uint32_t HALF128 = 2 * b_block(128);   // K = 128: two K-blocks
-__device__ __forceinline__ bool issue_gemm2(uint32_t tmem, const unsigned char* w2h, const unsigned char* ring,
-                                            const unsigned char* Hs, uint64_t* full, uint32_t round) {
+__device__ __forceinline__ void issue_gemm2_chunk(int g, uint32_t tmem, const unsigned char* w2h,
+                                                  const unsigned char* w2l, const unsigned char* Hs) {
     constexpr uint32_t idesc = idesc_f16(128);
     constexpr uint64_t DA = A_TILE >> 4, DH = HALF128 >> 4;
-    const uint64_t a_hi = sdesc(smem_u32(w2h), A_LBO, A_SBO);
-    const uint64_t a_lo = sdesc(smem_u32(ring), A_LBO, A_SBO);
+    const uint64_t a_hi = sdesc(smem_u32(w2h), A_LBO, A_SBO) + (uint64_t)(8 * g) * DA;
+    const uint64_t a_lo = sdesc(smem_u32(w2l), A_LBO, A_SBO);
     const uint64_t b0 = sdesc_b(smem_u32(Hs));
+    const uint32_t d = tmem + TM_F + 128 * g;
 #pragma unroll 1
     for (int s = 0; s < 8; ++s) {
         const uint64_t bh = b0 + (uint64_t)(b_kstep_off(128, s) >> 4);
         const uint64_t ah = a_hi + (uint64_t)s * DA;
-#pragma unroll
-        for (int g = 0; g < 2; ++g) {
-            const uint32_t d = tmem + TM_F + 128 * g;
-            mma_f16(d, ah + (uint64_t)(8 * g) * DA, bh, idesc, 1);
-            mma_f16(d, ah + (uint64_t)(8 * g) * DA, bh + DH, idesc, 1);
-            mma_f16_ts(d, tmem + TM_W2LO + 64 * g + 8 * s, bh, idesc, 1);
-        }
-        const uint32_t d2 = tmem + TM_F + 256;
-        mma_f16(d2, ah + 16 * DA, bh, idesc, 1);
-        mma_f16(d2, ah + 16 * DA, bh + DH, idesc, 1);
-        if (!mbar_wait(&full[s], round & 1, WAIT_BUDGET)) return false;
-        mma_f16(d2, a_lo + (uint64_t)s * DA, bh, idesc, 1);
+        mma_f16(d, ah, bh, idesc, 1);
+        mma_f16(d, ah, bh + DH, idesc, 1);
+        if (g < 2) mma_f16_ts(d, tmem + TM_W2LO + 64 * g + 8 * s, bh, idesc, 1);
+        else mma_f16(d, a_lo + (uint64_t)s * DA, bh, idesc, 1);
     }
-    return true;
 }
 
 // out = base + (sum over the receiver's edges): receivers in [j0, j1)
@@ -404,11 +398,11 @@ constexpr uint32_t F_SB_SOFF = F_SB_RCV + FN * 4;
 constexpr uint32_t F_SB_UC = F_SB_SOFF + FN * 4;
 constexpr uint32_t F_SB_CHG = F_SB_UC + 3 * FN * 4;
 constexpr uint32_t F_SB_BYTES = F_SB_CHG + (FN / 32) * 4;
-constexpr uint32_t F_OFF_SB = F_OFF_RING + NSLOT * A_TILE;
+constexpr uint32_t F_OFF_SB = F_OFF_RING + W2L_BYTES;
 constexpr uint32_t F_OFF_B1 = F_OFF_SB + 2 * F_SB_BYTES;
 constexpr uint32_t F_OFF_B2 = F_OFF_B1 + H * 4;
 constexpr uint32_t F_OFF_BAR = F_OFF_B2 + H3 * 4;
-constexpr uint32_t F_OFF_MISC = F_OFF_BAR + 8 * (3 + NSLOT);
+constexpr uint32_t F_OFF_MISC = F_OFF_BAR + 8 * 4;
 constexpr uint32_t F_SMEM = align1k(F_OFF_MISC + 16);
 static_assert(ET_BYTES <= 2 * F_HH, "E tile fits in the H tile's space");
 static_assert(F_SMEM <= 232448, "forward kernel shared memory");
@@ -423,23 +417,21 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
     unsigned char* w2h = smem + F_OFF_W2H;
     unsigned char* Hs = smem + F_OFF_H;
     unsigned char* Es = smem + F_OFF_H;            // E tile (bulk-copied) lives in the H tile's space
-    unsigned char* ring = smem + F_OFF_RING;
+    unsigned char* w2l = smem + F_OFF_RING;        // resident lo tiles of W2 chunk 2
     float* b1s = reinterpret_cast<float*>(smem + F_OFF_B1);
     float* b2s = reinterpret_cast<float*>(smem + F_OFF_B2);
     uint64_t* mma_bar = reinterpret_cast<uint64_t*>(smem + F_OFF_BAR);
     uint64_t* w2h_bar = mma_bar + 1;
     uint64_t* e_bar = mma_bar + 2;
-    uint64_t* full = mma_bar + 3;
+    uint64_t* g2_bar = mma_bar + 3;                 // GEMM2: one commit per chunk issuer
     uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + F_OFF_MISC);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + F_OFF_MISC + 4);
-    uint32_t* ccount_s = reinterpret_cast<uint32_t*>(smem + F_OFF_MISC + 8);
 
     // waits for the previous kernel at entry: reading the status word first
     // and returning early keeps the main loop's register allocation lean
     pdl_wait();
     if (a.st->code != 0) return;
     const int t = threadIdx.x, w = t >> 5, lane = t & 31;
-    const unsigned char* w2lo = w2g + W2_HALF;
     if (w == 0) {
         tmem_alloc(tslot, 512);
         tmem_relinquish();
@@ -448,10 +440,9 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
         mbar_init(mma_bar, 1);
         mbar_init(w2h_bar, 1);
         mbar_init(e_bar, 1);
-        for (int i = 0; i < NSLOT; ++i) mbar_init(&full[i], 1);
+        mbar_init(g2_bar, 3);
         fence_mbar_init();
         *abort_flag = 0;
-        *ccount_s = 0;
     }
     for (int i = t; i < (int)(W1_BYTES / 16); i += NT)
         reinterpret_cast<uint4*>(w1s)[i] = reinterpret_cast<const uint4*>(w1g)[i];
@@ -463,15 +454,9 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
     fence_after_sync();
     const uint32_t tmem = *tslot;
 
-    uint32_t mma_phase = 0;
-    uint32_t pcount = 0, ccount = 0;   // ring fills (thread 32) / uses (thread 0), NSLOT per edge tile
-    uint32_t tiles = 0;
-    bool w2h_ready = false;
-    if (t == 32) {
-        load_w2_hi(w2h, w2g, w2h_bar);
-        fill_lo_ring(ring, w2lo, full);
-        pcount += NSLOT;
-    }
+    uint32_t mma_phase = 0, g2_phase = 0;   // GEMM1 / GEMM2 barrier phases
+    bool w2h_ready = false;                 // (GEMM2 issuers)
+    if (t == 32) load_w2_resident(w2h, w2l, w2g, w2h_bar);
 
     const int q = w & 3, r = w >> 2;
     const int c = 32 * q + lane;
@@ -577,31 +562,23 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
             fence_async_smem();
             fence_before_sync();
             __syncthreads();
-            if (w == 0 && lane == 0) {   // GEMM2: f^T = W2 h^T
+            if (w < 3 && lane == 0) {   // GEMM2: f^T = W2 h^T, chunk w issued by warp w
                 fence_after_sync();
                 if (!w2h_ready) {
                     if (!mbar_wait(w2h_bar, 0, WAIT_BUDGET)) signal_timeout(a, abort_flag, 6);
                     w2h_ready = true;
                 }
-                if (issue_gemm2(tmem, w2h, ring, Hs, full, tiles)) ccount += NSLOT;
-                else signal_timeout(a, abort_flag, 2);
-                mma_commit(mma_bar);
-                *ccount_s = ccount;
+                issue_gemm2_chunk(w, tmem, w2h, w2l, Hs);
+                mma_commit(g2_bar);
             }
-            if (w == 0) __syncwarp();   // lanes 1-31 of the issuing warp wait here, not in a spin loop
+            if (w < 3) __syncwarp();   // lanes 1-31 of the issuing warps wait here, not in a spin loop
             // only warp 0 polls the MMA barrier; the others wait at the CTA
             // barrier instead of spinning on shared memory the MMAs read from
-            if (w == 0 && !mbar_wait(mma_bar, mma_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 4);
-            mma_phase ^= 1;
+            if (w == 0 && !mbar_wait(g2_bar, g2_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 4);
+            g2_phase ^= 1;
             fence_before_sync();
             __syncthreads();
             fence_after_sync();
-            ++tiles;
-            if (t == 32 && !*abort_flag) {
-                // this tile's MMAs are done, so the ring is free: fetch the next tile's lo tiles
-                fill_lo_ring(ring, w2lo, full);
-                pcount += NSLOT;
-            }
             // ... and the H tile is free: the next tile's E tile and edge arrays
             // arrive while epilogue 2 runs
             const bool more = k + 1 < ntl && !*abort_flag;
@@ -690,7 +667,7 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
         }
         if (!aborted) a.Xt[(int64_t)cur * 4 * H + fidx] = base + (acc + accu);
     }
-    // drain: the resident-tile load and every ring fill issued must have
+    // drain: the resident-weight load and any E-tile copy issued must have
     // landed before the CTA exits
     __syncthreads();
     if (t == 32) {
@@ -698,12 +675,6 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
         // an E-tile copy issued for a tile that never ran (abort) must land first
         if (e_issued > 0 && !mbar_wait(e_bar, (e_issued - 1) & 1, WAIT_BUDGET))
             set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 9);
-        const uint32_t used = *ccount_s;
-        for (uint32_t f = used; f < pcount; ++f)
-            if (!mbar_wait(&full[f % NSLOT], (f / NSLOT) & 1, WAIT_BUDGET)) {
-                set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 5);
-                break;
-            }
     }
     fence_before_sync();
     __syncthreads();
@@ -731,12 +702,12 @@ constexpr uint32_t B_SB_ROFF = B_SB_SOFF + BN * 4;
 constexpr uint32_t B_SB_UC = B_SB_ROFF + BN * 4;
 constexpr uint32_t B_SB_CHG = B_SB_UC + 3 * BN * 4;
 constexpr uint32_t B_SB_BYTES = B_SB_CHG + 16;
-constexpr uint32_t B_OFF_SB = B_OFF_RING + NSLOT * A_TILE;
+constexpr uint32_t B_OFF_SB = B_OFF_RING + W2L_BYTES;
 constexpr uint32_t B_OFF_B1 = B_OFF_SB + 2 * B_SB_BYTES;
 constexpr uint32_t B_OFF_B2 = B_OFF_B1 + H * 4;
 constexpr uint32_t B_OFF_RED = B_OFF_B2 + H3 * 4;
 constexpr uint32_t B_OFF_BAR = B_OFF_RED + 16 * BN * 2 * 4;
-constexpr uint32_t B_OFF_MISC = B_OFF_BAR + 8 * (3 + NSLOT);
+constexpr uint32_t B_OFF_MISC = B_OFF_BAR + 8 * 4;
 constexpr uint32_t B_SMEM = align1k(B_OFF_MISC + 16);
 static_assert(ET_BYTES <= 2 * B_HH, "E tile fits in the H tile's space");
 static_assert(B_SMEM <= 232448, "reverse kernel shared memory");
@@ -748,24 +719,22 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
     unsigned char* w2h = smem + B_OFF_W2H;
     unsigned char* Hs = smem + B_OFF_H;            // [H; H'] hi, then lo
     unsigned char* Es = smem + B_OFF_H;            // [E; E'] tile (bulk-copied), before H is written
-    unsigned char* ring = smem + B_OFF_RING;
+    unsigned char* w2l = smem + B_OFF_RING;        // resident lo tiles of W2 chunk 2
     float* b1s = reinterpret_cast<float*>(smem + B_OFF_B1);
     float* b2s = reinterpret_cast<float*>(smem + B_OFF_B2);
     float* red = reinterpret_cast<float*>(smem + B_OFF_RED);   // [16 warps][BN][2]
     uint64_t* mma_bar = reinterpret_cast<uint64_t*>(smem + B_OFF_BAR);
     uint64_t* w2h_bar = mma_bar + 1;
     uint64_t* e_bar = mma_bar + 2;
-    uint64_t* full = mma_bar + 3;
+    uint64_t* g2_bar = mma_bar + 3;                 // GEMM2: one commit per chunk issuer
     uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + B_OFF_MISC);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + B_OFF_MISC + 4);
-    uint32_t* ccount_s = reinterpret_cast<uint32_t*>(smem + B_OFF_MISC + 8);
 
     // waits for the previous kernel at entry: reading the status word first
     // and returning early keeps the main loop's register allocation lean
     pdl_wait();
     if (a.st->code != 0) return;
     const int t = threadIdx.x, w = t >> 5, lane = t & 31;
-    const unsigned char* w2lo = w2g + W2_HALF;
     if (w == 0) {
         tmem_alloc(tslot, 512);
         tmem_relinquish();
@@ -774,10 +743,9 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
         mbar_init(mma_bar, 1);
         mbar_init(w2h_bar, 1);
         mbar_init(e_bar, 1);
-        for (int i = 0; i < NSLOT; ++i) mbar_init(&full[i], 1);
+        mbar_init(g2_bar, 3);
         fence_mbar_init();
         *abort_flag = 0;
-        *ccount_s = 0;
     }
     for (int i = t; i < (int)(W1_BYTES / 16); i += NT)
         reinterpret_cast<uint4*>(w1s)[i] = reinterpret_cast<const uint4*>(w1g)[i];
@@ -789,15 +757,9 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
     fence_after_sync();
     const uint32_t tmem = *tslot;
 
-    uint32_t mma_phase = 0;
-    uint32_t pcount = 0, ccount = 0;   // ring fills (thread 32) / uses (thread 0), NSLOT per edge tile
-    uint32_t tiles = 0;
-    bool w2h_ready = false;
-    if (t == 32) {
-        load_w2_hi(w2h, w2g, w2h_bar);
-        fill_lo_ring(ring, w2lo, full);
-        pcount += NSLOT;
-    }
+    uint32_t mma_phase = 0, g2_phase = 0;   // GEMM1 / GEMM2 barrier phases
+    bool w2h_ready = false;                 // (GEMM2 issuers)
+    if (t == 32) load_w2_resident(w2h, w2l, w2g, w2h_bar);
     const int q = w & 3, r = w >> 2;
     const int c = 32 * q + lane;
     const int fidx = r * H + c;
@@ -913,30 +875,23 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
             fence_async_smem();
             fence_before_sync();
             __syncthreads();
-            if (w == 0 && lane == 0) {   // [f; f']^T = W2 [h; h']^T
+            if (w < 3 && lane == 0) {   // [f; f']^T = W2 [h; h']^T, chunk w issued by warp w
                 fence_after_sync();
                 if (!w2h_ready) {
                     if (!mbar_wait(w2h_bar, 0, WAIT_BUDGET)) signal_timeout(a, abort_flag, 16);
                     w2h_ready = true;
                 }
-                if (issue_gemm2(tmem, w2h, ring, Hs, full, tiles)) ccount += NSLOT;
-                else signal_timeout(a, abort_flag, 12);
-                mma_commit(mma_bar);
-                *ccount_s = ccount;
+                issue_gemm2_chunk(w, tmem, w2h, w2l, Hs);
+                mma_commit(g2_bar);
             }
-            if (w == 0) __syncwarp();   // lanes 1-31 of the issuing warp wait here, not in a spin loop
+            if (w < 3) __syncwarp();   // lanes 1-31 of the issuing warps wait here, not in a spin loop
             // only warp 0 polls the MMA barrier; the others wait at the CTA
             // barrier instead of spinning on shared memory the MMAs read from
-            if (w == 0 && !mbar_wait(mma_bar, mma_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 14);
-            mma_phase ^= 1;
+            if (w == 0 && !mbar_wait(g2_bar, g2_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 14);
+            g2_phase ^= 1;
             fence_before_sync();
             __syncthreads();
             fence_after_sync();
-            ++tiles;
-            if (t == 32 && !*abort_flag) {
-                fill_lo_ring(ring, w2lo, full);
-                pcount += NSLOT;
-            }
             // the H tile is free too: the next tile's [E; E'] tile and edge
             // arrays arrive while epilogue 2 runs
             const bool more = k + 1 < ntl && !*abort_flag;
@@ -1059,12 +1014,6 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
         if (!mbar_wait(w2h_bar, 0, WAIT_BUDGET)) set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 17);
         if (e_issued > 0 && !mbar_wait(e_bar, (e_issued - 1) & 1, WAIT_BUDGET))
             set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 19);
-        const uint32_t used = *ccount_s;
-        for (uint32_t f = used; f < pcount; ++f)
-            if (!mbar_wait(&full[f % NSLOT], (f / NSLOT) & 1, WAIT_BUDGET)) {
-                set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 15);
-                break;
-            }
     }
     fence_before_sync();
     __syncthreads();
