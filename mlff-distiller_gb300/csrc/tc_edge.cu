@@ -110,6 +110,9 @@ int pack_bf16(const mlff_dims& d, float* out, const PackedOffsets& o, cudaStream
 // -------------------------------------------------------- shared pieces
 constexpr int NT = 512;                        // threads per CTA (16 warps)
 
+// Barrier 1 over the first n threads (whole warps) of the CTA.
+__device__ __forceinline__ void bar_sync_first(int n) { asm volatile("bar.sync 1, %0;" ::"r"(n) : "memory"); }
+
 __device__ __forceinline__ void signal_timeout(const EdgeArgs& a, volatile int* abort_flag, int where) {
     set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, where);
     *abort_flag = 1;
@@ -270,14 +273,17 @@ int launch_etiles(const EdgeArgs& a, int32_t* base, unsigned char* fwd, unsigned
 }
 
 // Per-edge arrays of a tile, fetched asynchronously for the next tile while
-// the current one runs: (u, d), sender, receiver (padding: 0, 0, -1).
+// the current one runs: (u, d), sender, receiver (padding: 0, 0, -1) and,
+// when ea is given, the edges' accumulated (dE/dd, dE/du) of the layers
+// processed so far.
 __device__ __forceinline__ void fetch_tile_edges(const EdgeArgs& a, int t, int tn, int t0, int n, float4* us,
-                                                 int* src_s, int* rcv_s) {
+                                                 int* src_s, int* rcv_s, float4* ea = nullptr) {
     if (t < tn) {
         if (t < n) {
             cp_async16(us + t, a.geo + t0 + t);
             cp_async4(src_s + t, a.col + t0 + t);
             cp_async4(rcv_s + t, a.erecv + t0 + t);
+            if (ea) cp_async16(ea + t, a.eacc + t0 + t);
         } else {
             us[t] = make_float4(0.f, 0.f, 0.f, 0.f);
             src_s[t] = 0;
@@ -701,7 +707,8 @@ constexpr uint32_t B_SB_SOFF = B_SB_RCV + BN * 4;
 constexpr uint32_t B_SB_ROFF = B_SB_SOFF + BN * 4;
 constexpr uint32_t B_SB_UC = B_SB_ROFF + BN * 4;
 constexpr uint32_t B_SB_CHG = B_SB_UC + 3 * BN * 4;
-constexpr uint32_t B_SB_BYTES = B_SB_CHG + 16;
+constexpr uint32_t B_SB_EACC = B_SB_CHG + 16;
+constexpr uint32_t B_SB_BYTES = B_SB_EACC + BN * 16;
 constexpr uint32_t B_OFF_SB = B_OFF_RING + W2L_BYTES;
 constexpr uint32_t B_OFF_B1 = B_OFF_SB + 2 * B_SB_BYTES;
 constexpr uint32_t B_OFF_B2 = B_OFF_B1 + H * 4;
@@ -793,7 +800,8 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
         if (ntl > 0) {   // the partition's first tile: edge arrays and [E; E'] tile
             unsigned char* sb = smem + B_OFF_SB;
             fetch_tile_edges(a, t, BN, e0, min(BN, e1 - e0), reinterpret_cast<float4*>(sb + B_SB_US),
-                             reinterpret_cast<int*>(sb + B_SB_SRC), reinterpret_cast<int*>(sb + B_SB_RCV));
+                             reinterpret_cast<int*>(sb + B_SB_SRC), reinterpret_cast<int*>(sb + B_SB_RCV),
+                             a.eacc_init ? nullptr : reinterpret_cast<float4*>(sb + B_SB_EACC));
             if (t == 32) {
                 mbar_expect_tx(e_bar, ET_BYTES);
                 bulk_g2s(Es, etiles, ET_BYTES, e_bar);
@@ -897,7 +905,8 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
             const bool more = k + 1 < ntl && !*abort_flag;
             if (more) {
                 fetch_tile_edges(a, t, BN, t0 + BN, min(BN, e1 - t0 - BN), reinterpret_cast<float4*>(sbn + B_SB_US),
-                                 reinterpret_cast<int*>(sbn + B_SB_SRC), reinterpret_cast<int*>(sbn + B_SB_RCV));
+                                 reinterpret_cast<int*>(sbn + B_SB_SRC), reinterpret_cast<int*>(sbn + B_SB_RCV),
+                                 a.eacc_init ? nullptr : reinterpret_cast<float4*>(sbn + B_SB_EACC));
                 if (t == 32) {
                     mbar_expect_tx(e_bar, ET_BYTES);
                     bulk_g2s(Es, etiles + (size_t)(k + 1) * ET_BYTES, ET_BYTES, e_bar);
@@ -982,6 +991,11 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                     process8(tbn, xbn, trn, col + 8);
                 }
             }
+            if (more && t < BN) {   // the next tile's prep, by the two warps that fetched it
+                cp_async_wait_all();
+                bar_sync_first(BN);
+                prep(sbn, min(BN, e1 - t0 - BN), rcv_s[BN - 1]);
+            }
             fence_before_sync();
             __syncthreads();
             if (t < n) {
@@ -992,20 +1006,18 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                     dd += rr[0];
                     if (ww >= 4) du[(ww >> 2) - 1] += rr[1];
                 }
-                float4 ea = a.eacc_init ? make_float4(0.f, 0.f, 0.f, 0.f) : a.eacc[t0 + t];
+                float4 ea = a.eacc_init ? make_float4(0.f, 0.f, 0.f, 0.f)
+                                        : reinterpret_cast<const float4*>(sb + B_SB_EACC)[t];
                 ea.x += dd;
                 ea.y += du[0];
                 ea.z += du[1];
                 ea.w += du[2];
                 a.eacc[t0 + t] = ea;
             }
-            cp_async_wait_all();
-            __syncthreads();
             if (*abort_flag) {
                 aborted = true;
                 break;
             }
-            if (more) prep(sbn, min(BN, e1 - t0 - BN), rcv_s[BN - 1]);
         }
         if (!aborted && a.write_nodes) a.xbar[(int64_t)cur * 4 * H + fidx] = acc;
     }
