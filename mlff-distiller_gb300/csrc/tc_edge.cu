@@ -568,6 +568,21 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
             fence_async_smem();
             fence_before_sync();
             __syncthreads();
+            // epilogue 2's first two 16-edge blocks of sender features are
+            // gathered while GEMM2 runs
+            float xa[16], xn[16];
+            auto gather16 = [&](float (&x)[16], int col) {
+#pragma unroll
+                for (int i = 0; i < 16; i += 4) {
+                    const int4 so = *reinterpret_cast<const int4*>(soff + col + i);
+                    x[i] = col + i < n ? __ldg(a.X + so.x + fidx) : 0.f;
+                    x[i + 1] = col + i + 1 < n ? __ldg(a.X + so.y + fidx) : 0.f;
+                    x[i + 2] = col + i + 2 < n ? __ldg(a.X + so.z + fidx) : 0.f;
+                    x[i + 3] = col + i + 3 < n ? __ldg(a.X + so.w + fidx) : 0.f;
+                }
+            };
+            gather16(xa, 0);
+            if (16 < n) gather16(xn, 16);
             if (w < 3 && lane == 0) {   // GEMM2: f^T = W2 h^T, chunk w issued by warp w
                 fence_after_sync();
                 if (!w2h_ready) {
@@ -605,17 +620,6 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                 const uint32_t f1col = r == 0 ? 128 : 256;
                 float* out = a.Xt + fidx;          // Xt = X + message sum (student_model.py:359-385)
                 const float* xin = a.X + fidx;
-                float xa[16], xn[16];
-                auto gather16 = [&](float (&x)[16], int col) {
-#pragma unroll
-                    for (int i = 0; i < 16; i += 4) {
-                        const int4 so = *reinterpret_cast<const int4*>(soff + col + i);
-                        x[i] = col + i < n ? __ldg(a.X + so.x + fidx) : 0.f;
-                        x[i + 1] = col + i + 1 < n ? __ldg(a.X + so.y + fidx) : 0.f;
-                        x[i + 2] = col + i + 2 < n ? __ldg(a.X + so.z + fidx) : 0.f;
-                        x[i + 3] = col + i + 3 < n ? __ldg(a.X + so.w + fidx) : 0.f;
-                    }
-                };
                 auto process16 = [&](const float (&x)[16], int col) {
                     float f1[16], f2[16];
                     tmem_ld16(lane_base + f1col + col, f1);
@@ -649,13 +653,12 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                         }
                     }
                 };
-                gather16(xa, 0);
-                for (int col = 0; col < n; col += 32) {
-                    if (col + 16 < n) gather16(xn, col + 16);
+                for (int col = 0; col < n; col += 32) {   // blocks col and col + 16 are in flight
                     process16(xa, col);
                     if (col + 16 >= n) break;
                     if (col + 32 < n) gather16(xa, col + 32);
                     process16(xn, col + 16);
+                    if (col + 48 < n) gather16(xn, col + 48);
                 }
             }
             cp_async_wait_all();
@@ -883,6 +886,25 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
             fence_async_smem();
             fence_before_sync();
             __syncthreads();
+            // epilogue 2's first two 8-edge blocks of gathers are issued while GEMM2 runs
+            float tba[8], xba[8], tra[8], tbn[8], xbn[8], trn[8];
+            auto gather8 = [&](float (&tb)[8], float (&xb)[8], float (&tr)[8], int col) {
+#pragma unroll
+                for (int i = 0; i < 8; i += 4) {
+                    const int4 so = *reinterpret_cast<const int4*>(soff + col + i);
+                    const int4 ro = *reinterpret_cast<const int4*>(roff + col + i);
+                    const int sv[4] = {so.x, so.y, so.z, so.w}, rv[4] = {ro.x, ro.y, ro.z, ro.w};
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const bool ok = col + i + k < n;
+                        tb[i + k] = ok ? __ldg(a.xtbar + sv[k] + fidx) : 0.f;
+                        xb[i + k] = ok ? __ldg(a.X + sv[k] + fidx) : 0.f;
+                        tr[i + k] = ok ? __ldg(a.xtbar + rv[k] + fidx) : 0.f;
+                    }
+                }
+            };
+            gather8(tba, xba, tra, 0);
+            if (8 < n) gather8(tbn, xbn, trn, 8);
             if (w < 3 && lane == 0) {   // [f; f']^T = W2 [h; h']^T, chunk w issued by warp w
                 fence_after_sync();
                 if (!w2h_ready) {
@@ -921,22 +943,6 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                 const uint32_t f1col = r == 0 ? 128 : 256, d1col = f1col + BN;
                 const float* ur = uc + (r == 0 ? 0 : (r - 1) * BN);
                 float* out = a.xbar + fidx;        // gathered adjoint; dE/dXt is added afterwards
-                float tba[8], xba[8], tra[8], tbn[8], xbn[8], trn[8];
-                auto gather8 = [&](float (&tb)[8], float (&xb)[8], float (&tr)[8], int col) {
-#pragma unroll
-                    for (int i = 0; i < 8; i += 4) {
-                        const int4 so = *reinterpret_cast<const int4*>(soff + col + i);
-                        const int4 ro = *reinterpret_cast<const int4*>(roff + col + i);
-                        const int sv[4] = {so.x, so.y, so.z, so.w}, rv[4] = {ro.x, ro.y, ro.z, ro.w};
-#pragma unroll
-                        for (int k = 0; k < 4; ++k) {
-                            const bool ok = col + i + k < n;
-                            tb[i + k] = ok ? __ldg(a.xtbar + sv[k] + fidx) : 0.f;
-                            xb[i + k] = ok ? __ldg(a.X + sv[k] + fidx) : 0.f;
-                            tr[i + k] = ok ? __ldg(a.xtbar + rv[k] + fidx) : 0.f;
-                        }
-                    }
-                };
                 auto process8 = [&](const float (&tb)[8], const float (&xb)[8], const float (&tr)[8], int col) {
                     float f1[8], f2[8], d1[8], d2[8];
                     tmem_ld8(lane_base + f1col + col, f1);   // phi_s or phi_v1 (bias included)
@@ -982,13 +988,12 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                         rr[1] = s1;
                     }
                 };
-                gather8(tba, xba, tra, 0);
-                for (int col = 0; col < n; col += 16) {
-                    if (col + 8 < n) gather8(tbn, xbn, trn, col + 8);
+                for (int col = 0; col < n; col += 16) {   // blocks col and col + 8 are in flight
                     process8(tba, xba, tra, col);
                     if (col + 8 >= n) break;
                     if (col + 16 < n) gather8(tba, xba, tra, col + 16);
                     process8(tbn, xbn, trn, col + 8);
+                    if (col + 24 < n) gather8(tbn, xbn, trn, col + 24);
                 }
             }
             if (more && t < BN) {   // the next tile's prep, by the two warps that fetched it
