@@ -385,7 +385,9 @@ def main():
     if not args.no_e2e:
         Zh = torch.from_numpy(sysm.Z.astype(np.int64)).pin_memory()
         Ph = torch.from_numpy(sysm.pos.astype(np.float32)).pin_memory()
-        bh = torch.from_numpy(np.repeat(np.arange(sysm.n_mol), np.diff(sysm.mol_ptr)).astype(np.int64)).pin_memory()
+        # structure index, cell and pbc are host-side metadata, as the calculator passes them;
+        # the model turns them into molecule offsets / boxes and copies those
+        bh = torch.from_numpy(np.repeat(np.arange(sysm.n_mol), np.diff(sysm.mol_ptr)).astype(np.int64))
         cell = pbc = None
         if sysm.pbc.any():
             cell = torch.from_numpy(np.diag(sysm.box[0]).astype(np.float32))
@@ -394,9 +396,7 @@ def main():
         def e2e_step():
             Z = Zh.to("cuda", non_blocking=True)
             P = Ph.to("cuda", non_blocking=True)
-            b = bh.to("cuda", non_blocking=True)
-            E, F = model.energy_and_forces(Z, P, batch=b if sysm.n_mol > 1 else None,
-                                           cell=None if cell is None else cell.cuda(), pbc=pbc)
+            E, F = model.energy_and_forces(Z, P, batch=bh if sysm.n_mol > 1 else None, cell=cell, pbc=pbc)
             return E.cpu(), F.cpu()
         for _ in range(2):
             e2e_step()
@@ -410,7 +410,7 @@ def main():
             t = torch.tensor([el], device="cuda")
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             el = float(t.item())
-        h2d = Zh.numel() * 8 + Ph.numel() * 4 + bh.numel() * 8
+        h2d = Zh.numel() * 8 + Ph.numel() * 4 + (sysm.n_mol + 1) * 8 + (sysm.n_mol * 13 if cell is not None else 0)
         d2h = sysm.n_mol * 8 + sysm.n_atoms * 12
         e2e = {"value": atoms_all * args.steps / el, "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h}

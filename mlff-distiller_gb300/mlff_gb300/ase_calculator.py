@@ -125,8 +125,9 @@ class StudentForceFieldCalculator(Calculator):
         z = torch.as_tensor(np.asarray(numbers, dtype=np.int64), device=dev)
         x = torch.as_tensor(np.asarray(positions, dtype=np.float32), device=dev)
         periodic = bool(np.asarray(pbc).any())
-        c = torch.as_tensor(np.asarray(cell, dtype=np.float32).reshape(3, 3), device=dev) if periodic else None
-        p = torch.as_tensor(np.asarray(pbc, dtype=bool), device=dev) if periodic else None
+        # cell and pbc stay on the host: the model checks them there without a device sync
+        c = torch.as_tensor(np.asarray(cell, dtype=np.float32).reshape(3, 3)) if periodic else None
+        p = torch.as_tensor(np.asarray(pbc, dtype=bool)) if periodic else None
         return z, x, c, p
 
     # -------------------------------------------------------------- calculate
@@ -200,12 +201,12 @@ class StudentForceFieldCalculator(Calculator):
             dev = self.device
             z = torch.as_tensor(np.concatenate(num).astype(np.int64), device=dev)
             x = torch.as_tensor(np.concatenate(pos).astype(np.float32), device=dev)
-            bidx = torch.repeat_interleave(torch.arange(len(atoms_list), device=dev),
-                                           torch.as_tensor(counts, device=dev))
+            # structure index, cells and pbc flags on the host (checked there, no device sync)
+            bidx = torch.as_tensor(np.repeat(np.arange(len(atoms_list), dtype=np.int64), counts))
             c = p = None
             if all(periodic):
-                c = torch.as_tensor(np.stack(cells).astype(np.float32), device=dev)
-                p = torch.as_tensor(np.stack(pbcs), device=dev)
+                c = torch.as_tensor(np.stack(cells).astype(np.float32))
+                p = torch.as_tensor(np.stack(pbcs))
             E, F = self.model.energy_and_forces(z, x, bidx, c, p)
             E = E.detach().cpu().numpy()
             F = F.detach().cpu().numpy().astype(np.float64)

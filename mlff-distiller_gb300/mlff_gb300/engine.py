@@ -4,7 +4,10 @@ C-ABI calls, on the current torch CUDA stream.
 ``Engine.energy_forces`` is the single entry the module, the calculator,
 the MD driver and the benchmark use.  It grows the edge capacity and the
 workspace when the neighbour build reports that they were too small and
-re-runs the call.
+re-runs the call.  Calls whose shape repeats (same atom and structure
+counts, path and outputs) replay a cached CUDA graph of the whole step: the
+inputs are copied into the graph's own buffers, one graph launch replaces
+the ~40 kernel launches, and the outputs are copied out.
 """
 from __future__ import annotations
 
@@ -17,6 +20,7 @@ import torch
 from . import _lib
 
 DEFAULT_EDGES_PER_ATOM = 64
+GRAPH_CACHE_SIZE = 4
 
 
 def _stream_handle() -> int:
@@ -89,6 +93,8 @@ class Engine:
         self.workspace: Optional[torch.Tensor] = None
         self.edge_capacity: Dict[int, int] = {}
         self._param_version = None
+        self.use_graphs = True          # replay cached CUDA graphs for repeated shapes
+        self._graphs: Dict[tuple, dict] = {}
 
     # -------------------------------------------------------------- weights
     def pack(self, sd: Dict[str, torch.Tensor]):
@@ -143,9 +149,24 @@ class Engine:
 
     # ---------------------------------------------------------------- calls
     def energy_forces(self, batch: Batch, path: int = _lib.PATH_TUNED_TC, forces: bool = True,
-                      virial: bool = False, atom_energy: bool = False, check: bool = True
+                      virial: bool = False, atom_energy: bool = False, check: bool = True,
+                      graph: Optional[bool] = None
                       ) -> Tuple[torch.Tensor, Optional[torch.Tensor], Optional[torch.Tensor]]:
-        """Energies [B] (float64), forces [N,3] (float32), dE/dstrain [B,3,3]."""
+        """Energies [B] (float64), forces [N,3] (float32), dE/dstrain [B,3,3].
+
+        ``graph`` (default: ``self.use_graphs``) replays a cached CUDA graph
+        when a call of the same shape was seen before; the first call of a
+        shape runs eagerly and captures the graph for the next one.  The
+        batch's ``mol_ptr``, ``box`` and ``pbc`` tensors are taken as
+        immutable: passing the same tensor object again skips its copy."""
+        use_graph = self.use_graphs if graph is None else graph
+        if use_graph and check and not torch.cuda.is_current_stream_capturing():
+            res = self._graph_call(batch, path, forces, virial, atom_energy)
+            if res is not None:
+                return res
+        return self._eager_call(batch, path, forces, virial, atom_energy, check)
+
+    def _eager_call(self, batch: Batch, path: int, forces: bool, virial: bool, atom_energy: bool, check: bool):
         N, B = batch.n_atoms, batch.n_mol
         dev = self.device
         E = torch.empty(B, dtype=torch.float64, device=dev)
@@ -179,16 +200,69 @@ class Engine:
             return E, F, V, A
         return E, F, V
 
+    def _graph_call(self, batch: Batch, path: int, forces: bool, virial: bool, atom_energy: bool):
+        """Replay (or, on the first call of a shape, run eagerly and capture)
+        a CUDA graph of one energy_forces call.  Returns None when the graph
+        must be rebuilt and the call redone eagerly."""
+        N, B = batch.n_atoms, batch.n_mol
+        key = (N, B, path, forces, virial, atom_energy, batch.box is not None, batch.pbc is not None)
+        ent = self._graphs.get(key)
+        cap = self.capacity(N, path)
+        ws_ptr = None if self.workspace is None else self.workspace.data_ptr()
+        if ent is not None and (ent["cap"] != cap or ent["ws"] != ws_ptr):
+            del self._graphs[key]
+            ent = None
+        if ent is None:
+            res = self._eager_call(batch, path, forces, virial, atom_energy, True)
+            self._capture_call(key, batch, path, forces, virial, atom_energy)
+            return res
+        st, src = ent["batch"], ent["src"]
+        st.Z.copy_(batch.Z, non_blocking=True)
+        st.pos.copy_(batch.pos, non_blocking=True)
+        # molecule offsets and boxes are usually the caller's cached tensors:
+        # copied only when a different tensor comes in
+        for name in ("mol_ptr", "box", "pbc"):
+            t = getattr(batch, name)
+            if t is not None and src.get(name) is not t:
+                getattr(st, name).copy_(t, non_blocking=True)
+                src[name] = t
+        ent["graph"].replay()
+        code, n_edges, where = self.status()
+        if code == _lib.ERR_CAPACITY:
+            self.edge_capacity[path] = int(n_edges * 1.25) + 1024
+            del self._graphs[key]
+            return None
+        if code != _lib.OK:
+            raise _lib.MLFFError(code, f"device status {code} at index {where}")
+        self.edge_capacity[path] = max(self.edge_capacity.get(path, 0), int(n_edges * 1.15) + 1024)
+        return tuple(None if t is None else t.clone() for t in ent["out"])
+
+    def _capture_call(self, key, batch: Batch, path: int, forces: bool, virial: bool, atom_energy: bool):
+        N, B = batch.n_atoms, batch.n_mol
+        cap = self.capacity(N, path)
+        self.workspace_for(N, B, cap, path)          # sized before capture: no allocation inside it
+        st = Batch(batch.Z.clone(), batch.pos.clone(), batch.mol_ptr.clone(),
+                   None if batch.box is None else batch.box.clone(),
+                   None if batch.pbc is None else batch.pbc.clone())
+        torch.cuda.current_stream().synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            out = self._eager_call(st, path, forces, virial, atom_energy, False)
+        while len(self._graphs) >= GRAPH_CACHE_SIZE:
+            self._graphs.pop(next(iter(self._graphs)))
+        self._graphs[key] = {"graph": g, "batch": st, "out": out, "cap": cap, "ws": self.workspace.data_ptr(),
+                             "src": {"mol_ptr": batch.mol_ptr, "box": batch.box, "pbc": batch.pbc}}
+
     def capture(self, batch: Batch, path: int = _lib.PATH_TUNED_TC, forces: bool = True):
         """One energy_forces call captured in a CUDA graph, for repeated
         evaluation of a fixed batch (the edge capacity must already be known:
         call energy_forces once first).  Returns (replay, E, F): replay()
         launches the graph on the current stream and refreshes E and F."""
-        self.energy_forces(batch, path, forces=forces)   # sizes capacity and workspace, loads kernels
+        self.energy_forces(batch, path, forces=forces, graph=False)   # sizes capacity and workspace
         torch.cuda.synchronize()
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):
-            E, F, _ = self.energy_forces(batch, path, forces=forces, check=False)
+            E, F, _ = self.energy_forces(batch, path, forces=forces, check=False, graph=False)
         self._graph_keep = g
         return g.replay, E, F
 

@@ -162,6 +162,9 @@ class StudentForceField(nn.Module):
                                          nn.Linear(hidden_dim // 4, 1))
         self._initialize_parameters()
         self._engine: Optional[Engine] = None
+        self._single_ptr: Dict[int, torch.Tensor] = {}   # device [0, N] offsets of single-structure calls
+        self._cell_cache = None                            # last host cell -> checked device box / pbc
+        self._batch_cache = None                           # last host structure index -> device offsets
         self._packed_version = None
 
     def _initialize_parameters(self):
@@ -204,15 +207,38 @@ class StudentForceField(nn.Module):
     def _engine_call(self, batch: Batch, forces: bool = True, virial: bool = False):
         return self.engine().energy_forces(batch, self.path, forces=forces, virial=virial)
 
-    def _make_batch(self, atomic_numbers, positions, cell, pbc, batch):
+    def _make_batch(self, atomic_numbers, positions, cell, pbc, batch, need_index: bool = True):
+        """Device Batch of one call.  A ``batch`` index or ``cell`` given on
+        the host (as the calculator passes them) is validated and turned into
+        molecule offsets on the host, with no device synchronisation; device
+        tensors are validated on the device."""
         dev = self.embedding.weight.device
+        if dev.type != "cuda" or not torch.cuda.is_available():
+            raise RuntimeError("mlff_gb300 needs a CUDA device (GB300, sm_103a): move the model to cuda")
         if positions.device != dev:
             raise RuntimeError(f"positions on {positions.device} but model on {dev}")
         N = int(atomic_numbers.shape[0])
         if batch is None:
-            mol_ptr = torch.tensor([0, N], dtype=torch.int64, device=dev)
-            mol_index = torch.zeros(N, dtype=torch.int64, device=dev)
+            mol_ptr = self._single_ptr.get(N)   # device [0, N], reused (the engine skips re-copying it)
+            if mol_ptr is None:
+                mol_ptr = torch.tensor([0, N], dtype=torch.int64, device=dev)
+                self._single_ptr = {N: mol_ptr}
+            mol_index = torch.zeros(N, dtype=torch.int64, device=dev) if need_index else None
             n_mol = 1
+        elif batch.device.type == "cpu":
+            b = batch.to(torch.int64)
+            hit = self._batch_cache is not None and torch.equal(self._batch_cache[0], b)
+            if hit:   # the same structure index as the last call: reuse its device offsets
+                n_mol, mol_ptr = self._batch_cache[1], self._batch_cache[2]
+            else:
+                if N and bool((b[1:] < b[:-1]).any()):
+                    raise ValueError("batch indices must be non-decreasing (atoms grouped by structure)")
+                n_mol = int(b[-1]) + 1 if N else 0
+                mp = torch.zeros(n_mol + 1, dtype=torch.int64)
+                mp[1:] = torch.cumsum(torch.bincount(b, minlength=n_mol), 0)
+                mol_ptr = mp.pin_memory().to(dev, non_blocking=True)
+                self._batch_cache = (b.clone(), n_mol, mol_ptr)
+            mol_index = b.to(dev, non_blocking=True) if need_index else None
         else:
             b = batch.to(torch.int64)
             if N and bool((b[1:] < b[:-1]).any()):
@@ -224,8 +250,17 @@ class StudentForceField(nn.Module):
             mol_index = b
         box = pbc_t = None
         if self.periodic and pbc is not None and cell is not None and bool(torch.as_tensor(pbc).any()):
-            cell_t = torch.as_tensor(cell, dtype=torch.float32, device=dev).reshape(-1, 3, 3)
-            pbc_b = torch.as_tensor(pbc, device=dev).reshape(-1, 3).to(torch.bool)
+            on_host = not (isinstance(cell, torch.Tensor) and cell.device.type != "cpu")
+            if on_host:   # the same host cell as the last call: reuse its checked device copies
+                ck = (n_mol, np.asarray(cell, dtype=np.float32).tobytes(), np.asarray(pbc, dtype=bool).tobytes())
+                if self._cell_cache is not None and self._cell_cache[0] == ck:
+                    box, pbc_t = self._cell_cache[1]
+                    bt = Batch(atomic_numbers.to(torch.int64).contiguous(),
+                               positions.detach().to(torch.float32).contiguous(), mol_ptr, box, pbc_t)
+                    return bt, mol_index, n_mol
+            vdev = torch.device("cpu") if on_host else dev   # where the cell is checked
+            cell_t = torch.as_tensor(cell, dtype=torch.float32, device=vdev).reshape(-1, 3, 3)
+            pbc_b = torch.as_tensor(pbc, device=vdev).reshape(-1, 3).to(torch.bool)
             if cell_t.shape[0] == 1 and n_mol > 1:
                 cell_t = cell_t.expand(n_mol, 3, 3)
                 pbc_b = pbc_b.expand(n_mol, 3)
@@ -237,6 +272,10 @@ class StudentForceField(nn.Module):
                 raise NotImplementedError("periodicity must be on all three axes or none")
             box = torch.diagonal(cell_t, dim1=1, dim2=2).contiguous()
             pbc_t = pbc_b.all(dim=1).to(torch.uint8).contiguous()
+            if on_host:
+                box = box.pin_memory().to(dev, non_blocking=True)
+                pbc_t = pbc_t.pin_memory().to(dev, non_blocking=True)
+                self._cell_cache = (ck, (box, pbc_t))
         bt = Batch(atomic_numbers.to(torch.int64).contiguous(),
                    positions.detach().to(torch.float32).contiguous(), mol_ptr, box, pbc_t)
         return bt, mol_index, n_mol
@@ -270,7 +309,7 @@ class StudentForceField(nn.Module):
         """Batched (energies [B] float64, forces [N,3] float32) in one call,
         without autograd -- the batched calculator path
         (ase_calculator.py:708-770)."""
-        bt, _, _ = self._make_batch(atomic_numbers, positions, cell, pbc, batch)
+        bt, _, _ = self._make_batch(atomic_numbers, positions, cell, pbc, batch, need_index=False)
         E, F, _ = self._engine_call(bt, forces=True)
         return E, F
 
