@@ -1,0 +1,60 @@
+"""The engine's cached CUDA graphs of repeated call shapes (GPU only).
+
+A call whose shape was seen before replays a captured graph of the whole
+step on copies of the inputs; its results must equal an eager call bit for
+bit, for changing positions, for structure indices and cells given on the
+host, and across an edge-capacity overflow (the graph is dropped, the call
+redone eagerly with a larger capacity and captured again).
+"""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def model(weights_bias):
+    from mlff_gb300.student_model import StudentForceField
+    m = StudentForceField()
+    m.load_state_dict({k: torch.tensor(v) for k, v in weights_bias.items()})
+    return m.cuda()
+
+
+def _eager(model, Z, P, batch=None, cell=None, pbc=None):
+    eng = model.engine()
+    bt, _, _ = model._make_batch(Z, P, cell, pbc, batch, need_index=False)
+    E, F, _ = eng.energy_forces(bt, model.path, forces=True, graph=False)
+    return E, F
+
+
+def test_graph_replay_equals_eager_batch(model):
+    from mlff_gb300 import systems
+    s = systems.molecule_batch(12, 10, 60, seed=5)
+    Z = torch.as_tensor(s.Z, dtype=torch.int64, device="cuda")
+    b = torch.as_tensor(np.repeat(np.arange(s.n_mol), np.diff(s.mol_ptr)))   # host index
+    rng = np.random.default_rng(0)
+    for it in range(4):   # call 1 captures, calls 2-4 replay
+        pos = s.pos + 0.01 * it * rng.standard_normal(s.pos.shape)
+        P = torch.as_tensor(pos, dtype=torch.float32, device="cuda")
+        E, F = model.energy_and_forces(Z, P, batch=b)
+        E0, F0 = _eager(model, Z, P, batch=b)
+        assert torch.equal(E, E0) and torch.equal(F, F0)
+    assert len(model.engine()._graphs) >= 1
+
+
+def test_graph_replay_equals_eager_periodic_and_capacity(model):
+    from mlff_gb300 import systems
+    s = systems.water_box(150, 15.0, 2.5, seed=4)
+    Z = torch.as_tensor(s.Z, dtype=torch.int64, device="cuda")
+    cell = torch.as_tensor(np.diag(s.box[0]).astype(np.float32))   # host cell
+    pbc = torch.ones(3, dtype=torch.bool)
+    eng = model.engine()
+    for scale in (1.0, 1.0, 1.0, 0.9, 0.9):   # the compressed box needs more edges than captured
+        P = torch.as_tensor(s.pos * scale, dtype=torch.float32, device="cuda")
+        c = cell * scale
+        E, F = model.energy_and_forces(Z, P, cell=c, pbc=pbc)
+        E0, F0 = _eager(model, Z, P, cell=c, pbc=pbc)
+        assert torch.equal(E, E0) and torch.equal(F, F0)
+        assert torch.isfinite(F).all()
+    assert eng.status()[0] == 0
