@@ -125,6 +125,21 @@ class VelocityVerletGPU:
             v = zero_rotation(self.positions(), v, self.masses, self.mol_ptr_np)
         self.set_velocities(v)
 
+    def snapshot(self) -> Dict[str, torch.Tensor]:
+        """Device copies of the integrator state (positions, velocities,
+        forces, energies, step count) for restore()."""
+        return {"pos": self.pos.clone(), "vel": self.vel.clone(), "forces": self.forces.clone(),
+                "energy": self.energy.clone(), "kinetic": self.kinetic.clone(), "steps_done": self.steps_done,
+                "forces_valid": self._forces_valid}
+
+    def restore(self, snap: Dict[str, torch.Tensor]):
+        """Put a snapshot() back in place (the captured graphs keep working:
+        the state tensors are updated in place)."""
+        for k in ("pos", "vel", "forces", "energy", "kinetic"):
+            getattr(self, k).copy_(snap[k])
+        self.steps_done = snap["steps_done"]
+        self._forces_valid = snap["forces_valid"]
+
     def positions(self) -> np.ndarray:
         return self.pos.cpu().numpy()
 
