@@ -293,7 +293,7 @@ __device__ __forceinline__ void fetch_tile_edges(const EdgeArgs& a, int t, int t
     cp_async_commit();
 }
 
-// Per-tile prep by threads otherwise idle during the E-tile phase: sender
+// Per-tile prep by the threads that fetched the tile's edge arrays: sender
 // (and receiver) row offsets, u components, and a bitmask of the edges whose
 // receiver differs from the previous edge's (edge 0 compares with prev).
 template <int N>
@@ -394,7 +394,7 @@ static_assert(F_HH == HALF128, "GEMM2 B layout");
 constexpr uint32_t F_OFF_W1 = 0;
 constexpr uint32_t F_OFF_W2H = F_OFF_W1 + W1_BYTES;
 constexpr uint32_t F_OFF_H = align1k(F_OFF_W2H + W2_HALF);     // H tile; the E tile shares its start
-constexpr uint32_t F_OFF_RING = align1k(F_OFF_H + 2 * F_HH);
+constexpr uint32_t F_OFF_W2L = align1k(F_OFF_H + 2 * F_HH);
 // per-tile edge arrays, two buffers: (u, d), sender, receiver, sender row
 // offset, u components, receiver-change bits
 constexpr uint32_t F_SB_US = 0;
@@ -404,7 +404,7 @@ constexpr uint32_t F_SB_SOFF = F_SB_RCV + FN * 4;
 constexpr uint32_t F_SB_UC = F_SB_SOFF + FN * 4;
 constexpr uint32_t F_SB_CHG = F_SB_UC + 3 * FN * 4;
 constexpr uint32_t F_SB_BYTES = F_SB_CHG + (FN / 32) * 4;
-constexpr uint32_t F_OFF_SB = F_OFF_RING + W2L_BYTES;
+constexpr uint32_t F_OFF_SB = F_OFF_W2L + W2L_BYTES;
 constexpr uint32_t F_OFF_B1 = F_OFF_SB + 2 * F_SB_BYTES;
 constexpr uint32_t F_OFF_B2 = F_OFF_B1 + H * 4;
 constexpr uint32_t F_OFF_BAR = F_OFF_B2 + H3 * 4;
@@ -423,7 +423,7 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
     unsigned char* w2h = smem + F_OFF_W2H;
     unsigned char* Hs = smem + F_OFF_H;
     unsigned char* Es = smem + F_OFF_H;            // E tile (bulk-copied) lives in the H tile's space
-    unsigned char* w2l = smem + F_OFF_RING;        // resident lo tiles of W2 chunk 2
+    unsigned char* w2l = smem + F_OFF_W2L;        // resident lo tiles of W2 chunk 2
     float* b1s = reinterpret_cast<float*>(smem + F_OFF_B1);
     float* b2s = reinterpret_cast<float*>(smem + F_OFF_B2);
     uint64_t* mma_bar = reinterpret_cast<uint64_t*>(smem + F_OFF_BAR);
@@ -702,7 +702,7 @@ static_assert(B_HH == HALF128, "GEMM2 B layout");
 constexpr uint32_t B_OFF_W1 = 0;
 constexpr uint32_t B_OFF_W2H = B_OFF_W1 + W1_BYTES;
 constexpr uint32_t B_OFF_H = align1k(B_OFF_W2H + W2_HALF);     // [H; H'] tile; the [E; E'] tile shares its start
-constexpr uint32_t B_OFF_RING = align1k(B_OFF_H + 2 * B_HH);
+constexpr uint32_t B_OFF_W2L = align1k(B_OFF_H + 2 * B_HH);
 constexpr uint32_t B_SB_US = 0;
 constexpr uint32_t B_SB_SRC = B_SB_US + BN * 16;
 constexpr uint32_t B_SB_RCV = B_SB_SRC + BN * 4;
@@ -712,7 +712,7 @@ constexpr uint32_t B_SB_UC = B_SB_ROFF + BN * 4;
 constexpr uint32_t B_SB_CHG = B_SB_UC + 3 * BN * 4;
 constexpr uint32_t B_SB_EACC = B_SB_CHG + 16;
 constexpr uint32_t B_SB_BYTES = B_SB_EACC + BN * 16;
-constexpr uint32_t B_OFF_SB = B_OFF_RING + W2L_BYTES;
+constexpr uint32_t B_OFF_SB = B_OFF_W2L + W2L_BYTES;
 constexpr uint32_t B_OFF_B1 = B_OFF_SB + 2 * B_SB_BYTES;
 constexpr uint32_t B_OFF_B2 = B_OFF_B1 + H * 4;
 constexpr uint32_t B_OFF_RED = B_OFF_B2 + H3 * 4;
@@ -729,7 +729,7 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
     unsigned char* w2h = smem + B_OFF_W2H;
     unsigned char* Hs = smem + B_OFF_H;            // [H; H'] hi, then lo
     unsigned char* Es = smem + B_OFF_H;            // [E; E'] tile (bulk-copied), before H is written
-    unsigned char* w2l = smem + B_OFF_RING;        // resident lo tiles of W2 chunk 2
+    unsigned char* w2l = smem + B_OFF_W2L;        // resident lo tiles of W2 chunk 2
     float* b1s = reinterpret_cast<float*>(smem + B_OFF_B1);
     float* b2s = reinterpret_cast<float*>(smem + B_OFF_B2);
     float* red = reinterpret_cast<float*>(smem + B_OFF_RED);   // [16 warps][BN][2]
