@@ -196,12 +196,31 @@ typedef struct {
     double *kinetic;
     double *energy_trace;
     double *kinetic_trace;
+    int64_t *step_counter; /* device int64: steps taken; keys the Langevin draws (required
+                              by mlff_langevin_steps, optional here); +1 per step */
 } mlff_md_state;
 
 int mlff_verlet_steps(const mlff_dims *dims, const void *packed, const mlff_system *sys,
                       int64_t edge_capacity, int32_t path, mlff_md_state *state, double dt,
                       int32_t n_steps, void *workspace, size_t workspace_bytes,
                       mlff_stream_t stream);
+
+/* Langevin (NVT) steps in float64 state, BAOAB splitting (Leimkuhler and
+ * Matthews, J. Chem. Phys. 138, 174102 (2013)): per step
+ *   v += dt/2 F/m; r += dt/2 v; v = c1 v + sqrt((1 - c1^2) kT/m) xi;
+ *   r += dt/2 v; F = F(r); v += dt/2 F/m,   c1 = exp(-friction dt),
+ * with xi standard normals drawn by Box-Muller from Philox4x32-10 (Salmon
+ * et al., SC'11) keyed by (seed, *step_counter, atom) -- reproducible and
+ * independent of launch shape; the counter lives in device memory so a
+ * captured graph draws new numbers on every replay.  Replaces ASE's
+ * Langevin in the reference's NVT protocol (benchmarks/md_trajectory.py:
+ * 400-413).  Units as mlff_verlet_steps: dt and 1/friction in ASE time units
+ * (Angstrom sqrt(amu/eV)), kT in eV.  Same state, traces and workspace as
+ * mlff_verlet_steps; state->step_counter is required. */
+int mlff_langevin_steps(const mlff_dims *dims, const void *packed, const mlff_system *sys,
+                        int64_t edge_capacity, int32_t path, mlff_md_state *state, double dt,
+                        double friction, double kT, uint64_t seed, int32_t n_steps, void *workspace,
+                        size_t workspace_bytes, mlff_stream_t stream);
 
 /* Parameter gradients for training: grads <- sum_b w_b dE_b/dtheta for
  * every state_dict tensor, with w (device, double [B]) the derivative of

@@ -176,6 +176,8 @@ int energy_forces_impl(const mlff_dims& d, const void* packed, const mlff_system
     return run_tuned(d, P, po, sys, L, ws, out, path, st);
 }
 int md_kick_drift(const WsLayout& L, void* ws, mlff_md_state* s, double dt, cudaStream_t st);
+int md_langevin_baoa(const WsLayout& L, void* ws, mlff_md_state* s, double dt, double friction, double kT,
+                     uint64_t seed, cudaStream_t st);
 int md_kick(const WsLayout& L, void* ws, mlff_md_state* s, double dt, const int64_t* mol_ptr, int32_t n_mol,
             bool kinetic, cudaStream_t st);
 }  // namespace mlff
@@ -265,14 +267,19 @@ int mlff_energy_forces(const mlff_dims* dims, const void* packed, const mlff_sys
     return energy_forces_impl(*dims, packed, *sys, L, path, *out, workspace, st);
 }
 
-int mlff_verlet_steps(const mlff_dims* dims, const void* packed, const mlff_system* sys, int64_t edge_capacity,
-                      int32_t path, mlff_md_state* state, double dt, int32_t n_steps, void* workspace,
-                      size_t workspace_bytes, mlff_stream_t stream) {
+// One integrator for both entry points: Verlet (langevin false) or BAOAB.
+static int md_steps(const mlff_dims* dims, const void* packed, const mlff_system* sys, int64_t edge_capacity,
+                    int32_t path, mlff_md_state* state, double dt, bool langevin, double friction, double kT,
+                    uint64_t seed, int32_t n_steps, void* workspace, size_t workspace_bytes, mlff_stream_t stream) {
     if (!sys || !state || !state->pos || !state->vel || !state->inv_mass || !state->forces || !state->energy) {
         set_error("system and md state (pos, vel, inv_mass, forces, energy) are required");
         return MLFF_ERR_INVALID;
     }
     if (n_steps < 0 || !(dt > 0.0)) { set_error("n_steps >= 0 and dt > 0 required"); return MLFF_ERR_INVALID; }
+    if (langevin && (!state->step_counter || !(friction >= 0.0) || !(kT >= 0.0))) {
+        set_error("Langevin steps need state->step_counter, friction >= 0 and kT >= 0");
+        return MLFF_ERR_INVALID;
+    }
     if (!packed) { set_error("packed weights are required"); return MLFF_ERR_INVALID; }
     mlff_system s2 = *sys;
     WsLayout L;
@@ -293,7 +300,9 @@ int mlff_verlet_steps(const mlff_dims* dims, const void* packed, const mlff_syst
                          nullptr, nullptr};
         mlff_md_state ks = *state;
         if (state->kinetic_trace) ks.kinetic = state->kinetic_trace + s * B;
-        if ((r = md_kick_drift(L, workspace, state, dt, st))) return r;
+        r = langevin ? md_langevin_baoa(L, workspace, state, dt, friction, kT, seed, st)
+                     : md_kick_drift(L, workspace, state, dt, st);
+        if (r) return r;
         if ((r = energy_forces_impl(*dims, packed, s2, L, path, out, workspace, st))) return r;
         if ((r = md_kick(L, workspace, &ks, dt, sys->mol_ptr, sys->n_mol, last || state->kinetic_trace, st)))
             return r;
@@ -307,6 +316,20 @@ int mlff_verlet_steps(const mlff_dims* dims, const void* packed, const mlff_syst
         }
     }
     return MLFF_OK;
+}
+
+int mlff_verlet_steps(const mlff_dims* dims, const void* packed, const mlff_system* sys, int64_t edge_capacity,
+                      int32_t path, mlff_md_state* state, double dt, int32_t n_steps, void* workspace,
+                      size_t workspace_bytes, mlff_stream_t stream) {
+    return md_steps(dims, packed, sys, edge_capacity, path, state, dt, false, 0.0, 0.0, 0, n_steps, workspace,
+                    workspace_bytes, stream);
+}
+
+int mlff_langevin_steps(const mlff_dims* dims, const void* packed, const mlff_system* sys, int64_t edge_capacity,
+                        int32_t path, mlff_md_state* state, double dt, double friction, double kT, uint64_t seed,
+                        int32_t n_steps, void* workspace, size_t workspace_bytes, mlff_stream_t stream) {
+    return md_steps(dims, packed, sys, edge_capacity, path, state, dt, true, friction, kT, seed, n_steps, workspace,
+                    workspace_bytes, stream);
 }
 
 int mlff_param_grads(const mlff_dims* dims, const void* packed, const mlff_system* sys, int64_t edge_capacity,

@@ -40,7 +40,7 @@ ERROR_NAMES = {ERR_INVALID: "invalid argument", ERR_CAPACITY: "edge capacity exc
 
 EXPORTS = ["mlff_version", "mlff_last_error_string", "mlff_packed_weights_size", "mlff_pack_weights",
            "mlff_workspace_size", "mlff_build_neighbors", "mlff_copy_neighbors", "mlff_energy_forces",
-           "mlff_read_status", "mlff_clear_status", "mlff_verlet_steps", "mlff_profile_begin",
+           "mlff_read_status", "mlff_clear_status", "mlff_verlet_steps", "mlff_langevin_steps", "mlff_profile_begin",
            "mlff_profile_end", "mlff_radius_graph_noalloc", "mlff_param_grads"]
 
 PROFILE_KINDS = ["neighbors", "edge_fwd", "edge_bwd", "update_fwd", "update_bwd", "readout", "forces",
@@ -80,7 +80,7 @@ class Outputs(ctypes.Structure):
 
 class MDState(ctypes.Structure):
     _fields_ = [("pos", _P), ("vel", _P), ("inv_mass", _P), ("forces", _P), ("energy", _P),
-                ("kinetic", _P), ("energy_trace", _P), ("kinetic_trace", _P)]
+                ("kinetic", _P), ("energy_trace", _P), ("kinetic_trace", _P), ("step_counter", _P)]
 
 
 class MLFFError(RuntimeError):
@@ -138,6 +138,10 @@ def load(build_if_missing: bool = True):
         lib.mlff_verlet_steps.restype = ctypes.c_int
         lib.mlff_verlet_steps.argtypes = [ctypes.POINTER(Dims), _P, ctypes.POINTER(System), i64, i32,
                                           ctypes.POINTER(MDState), ctypes.c_double, i32, _P, sz, _P]
+        lib.mlff_langevin_steps.restype = ctypes.c_int
+        lib.mlff_langevin_steps.argtypes = [ctypes.POINTER(Dims), _P, ctypes.POINTER(System), i64, i32,
+                                            ctypes.POINTER(MDState), ctypes.c_double, ctypes.c_double,
+                                            ctypes.c_double, ctypes.c_uint64, i32, _P, sz, _P]
         lib.mlff_profile_begin.restype = ctypes.c_int
         lib.mlff_profile_end.restype = ctypes.c_int
         lib.mlff_profile_end.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(i64), i32]

@@ -8,6 +8,11 @@ the per-structure potential and kinetic energy recorded on the device.
 Blocks of steps are captured once in a CUDA graph and replayed, so a step
 costs no host round trip.
 
+``set_langevin`` (or ``LangevinGPU``) switches the same driver to Langevin
+NVT dynamics (BAOAB splitting, ``mlff_langevin_steps``), the protocol the
+reference's MD benchmark runs through ASE's Langevin
+(benchmarks/md_trajectory.py:400-413).
+
 ``NVEMDHarness`` mirrors the reference's harness
 (testing/nve_harness.py:57-380: Maxwell-Boltzmann start at T, zero
 centre-of-mass momentum and angular momentum, VelocityVerlet at dt fs,
@@ -110,6 +115,20 @@ class VelocityVerletGPU:
         self.steps_done = 0
         self._graphs: Dict[int, Any] = {}
         self._forces_valid = False
+        self.step_counter = torch.zeros(1, dtype=torch.int64, device=d)   # keys the Langevin draws
+        self.thermostat: Optional[Dict[str, float]] = None
+
+    def set_langevin(self, temperature_K: float, friction: float = 0.01, seed: int = 0):
+        """Langevin NVT from now on: ``friction`` in inverse ASE time units
+        (the reference's NVT protocol uses 0.01), target temperature in K;
+        ``None`` temperature switches back to NVE."""
+        if temperature_K is None:
+            self.thermostat = None
+            return
+        if friction < 0 or temperature_K < 0:
+            raise ValueError("friction and temperature must be non-negative")
+        self.thermostat = {"friction": float(friction), "kT": float(units.kB * temperature_K),
+                           "seed": int(seed) & 0xFFFFFFFFFFFFFFFF}
 
     # state
     def set_velocities(self, vel):
@@ -130,12 +149,12 @@ class VelocityVerletGPU:
         forces, energies, step count) for restore()."""
         return {"pos": self.pos.clone(), "vel": self.vel.clone(), "forces": self.forces.clone(),
                 "energy": self.energy.clone(), "kinetic": self.kinetic.clone(), "steps_done": self.steps_done,
-                "forces_valid": self._forces_valid}
+                "forces_valid": self._forces_valid, "step_counter": self.step_counter.clone()}
 
     def restore(self, snap: Dict[str, torch.Tensor]):
         """Put a snapshot() back in place (the captured graphs keep working:
         the state tensors are updated in place)."""
-        for k in ("pos", "vel", "forces", "energy", "kinetic"):
+        for k in ("pos", "vel", "forces", "energy", "kinetic", "step_counter"):
             getattr(self, k).copy_(snap[k])
         self.steps_done = snap["steps_done"]
         self._forces_valid = snap["forces_valid"]
@@ -171,11 +190,20 @@ class VelocityVerletGPU:
         st.inv_mass, st.forces = self.inv_mass.data_ptr(), self.forces.data_ptr()
         st.energy, st.kinetic = self.energy.data_ptr(), self.kinetic.data_ptr()
         st.energy_trace, st.kinetic_trace = _lib.ptr(e_trace), _lib.ptr(k_trace)
+        st.step_counter = self.step_counter.data_ptr()
         sysd = self._batch_sys
-        _lib.check(self.lib.mlff_verlet_steps(ctypes.byref(self.engine.dims), self.engine.packed.data_ptr(),
-                                              ctypes.byref(sysd), cap, self.path, ctypes.byref(st),
-                                              ctypes.c_double(self.dt), n_steps, ws.data_ptr(), ws.numel(),
-                                              _stream_handle()))
+        th = self.thermostat
+        if th is None:
+            _lib.check(self.lib.mlff_verlet_steps(ctypes.byref(self.engine.dims), self.engine.packed.data_ptr(),
+                                                  ctypes.byref(sysd), cap, self.path, ctypes.byref(st),
+                                                  ctypes.c_double(self.dt), n_steps, ws.data_ptr(), ws.numel(),
+                                                  _stream_handle()))
+        else:
+            _lib.check(self.lib.mlff_langevin_steps(ctypes.byref(self.engine.dims), self.engine.packed.data_ptr(),
+                                                    ctypes.byref(sysd), cap, self.path, ctypes.byref(st),
+                                                    ctypes.c_double(self.dt), ctypes.c_double(th["friction"]),
+                                                    ctypes.c_double(th["kT"]), ctypes.c_uint64(th["seed"]), n_steps,
+                                                    ws.data_ptr(), ws.numel(), _stream_handle()))
 
     def _capacity(self) -> int:
         return max(self.engine.capacity(self.N, self.path),
@@ -220,7 +248,8 @@ class VelocityVerletGPU:
 
     def _graph(self, k: int, cap: int, record: bool):
         ws = self.engine.workspace_for(self.N, self.B, cap, self.path)
-        key = (k, cap, record, ws.data_ptr())
+        th = self.thermostat
+        key = (k, cap, record, ws.data_ptr(), None if th is None else (th["friction"], th["kT"], th["seed"]))
         if key in self._graphs:
             return self._graphs[key]
         # a graph holds the workspace address it was captured with
@@ -234,6 +263,17 @@ class VelocityVerletGPU:
             self._call(k, cap, e, kk)
         self._graphs[key] = {"graph": g, "e": e, "k": kk, "ws": ws}
         return self._graphs[key]
+
+
+class LangevinGPU(VelocityVerletGPU):
+    """Langevin NVT driver with ASE Langevin's arguments (timestep in fs,
+    temperature_K, friction in inverse ASE time units): the reference's NVT
+    protocol (benchmarks/md_trajectory.py:408-413) on the fused GPU step."""
+
+    def __init__(self, model, numbers, positions, mol_ptr, temperature_K: float, friction: float = 0.01,
+                 seed: int = 0, timestep_fs: float = 0.5, **kwargs):
+        super().__init__(model, numbers, positions, mol_ptr, timestep_fs=timestep_fs, **kwargs)
+        self.set_langevin(temperature_K, friction, seed)
 
 
 # ----------------------------------------------------------------- harness

@@ -146,3 +146,35 @@ def test_oracle_verlet_harmonic():
         e = ep[:, 0] + ek[:, 0]
         assert np.ptp(e) < 1e-3
     assert 3.5 < errs[0] / errs[1] < 4.5
+
+
+def test_oracle_philox_known_answers():
+    """Philox4x32-10 against the known-answer vectors published with the
+    generator's reference implementation (counter, key -> output)."""
+    from oracle.philox import philox4x32_10
+    kat = [((0, 0, 0, 0), (0, 0), (0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8)),
+           ((0xffffffff,) * 4, (0xffffffff,) * 2, (0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd)),
+           ((0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344), (0xa4093822, 0x299f31d0),
+            (0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1))]
+    for ctr, key, out in kat:
+        got = philox4x32_10(np.array(ctr, np.uint32), np.array(key, np.uint32))
+        assert tuple(int(x) for x in got) == out
+
+
+def test_oracle_langevin_normals_and_equipartition():
+    """The Box-Muller normals are standard normal, and BAOAB of free
+    particles relaxes the kinetic energy to 3/2 kT per atom."""
+    from oracle.md import langevin_baoab
+    from oracle.philox import langevin_normals
+    xi = np.concatenate([langevin_normals(7, s, 2000) for s in range(5)])
+    assert abs(xi.mean()) < 0.02 and abs(xi.std() - 1.0) < 0.02
+    n, kT = 500, units.kB * 300.0
+    m = np.full(n, 12.0)
+
+    def free(r):
+        return np.zeros(1), np.zeros_like(r)
+
+    r, v, F, ep, ek = langevin_baoab(np.zeros((n, 3)), np.zeros((n, 3)), m, free, 1.0 * units.fs, 0.05 / units.fs,
+                                     kT, 3, 0, 400, np.array([0, n]))
+    T_kin = ek[200:, 0].mean() / (1.5 * n * kT)
+    assert abs(T_kin - 1.0) < 0.05
