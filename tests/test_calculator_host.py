@@ -178,3 +178,31 @@ def test_oracle_langevin_normals_and_equipartition():
                                      kT, 3, 0, 400, np.array([0, n]))
     T_kin = ek[200:, 0].mean() / (1.5 * n * kT)
     assert abs(T_kin - 1.0) < 0.05
+
+
+def test_student_calculator_contract(tmp_path):
+    """Generic StudentCalculator: constructor errors as the reference's, and a
+    foreign dict-in/dict-out module evaluated as the reference does."""
+    from mlff_gb300.student_calculator import StudentCalculator
+    with pytest.raises(ValueError):
+        StudentCalculator(device="cpu")
+    with pytest.raises(FileNotFoundError):
+        StudentCalculator(model_path=tmp_path / "missing.pth", device="cpu")
+    with pytest.raises(ValueError):
+        StudentCalculator(model=lambda: 3, device="cpu")
+
+    class Toy(torch.nn.Module):   # energy = sum |r|^2, forces = -2 r
+        def forward(self, inp):
+            r = inp["positions"]
+            return {"energy": (r * r).sum().reshape(1), "forces": -2.0 * r}
+
+    calc = StudentCalculator(model=Toy(), device="cpu")
+    a = Atoms(numbers=[1, 8], positions=[[0.0, 0, 0], [1.0, 2.0, 0]])
+    a.calc = calc
+    assert abs(a.get_potential_energy() - 5.0) < 1e-6
+    np.testing.assert_allclose(a.get_forces(), [[0, 0, 0], [-2.0, -4.0, 0]], atol=1e-6)
+    assert calc.n_calls >= 1
+    # a state_dict that is not a StudentForceField needs model_class
+    torch.save({"model_state_dict": Toy().state_dict()}, tmp_path / "toy.pth")
+    with pytest.raises(RuntimeError):
+        StudentCalculator(model_path=tmp_path / "toy.pth", device="cpu")

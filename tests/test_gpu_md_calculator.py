@@ -192,3 +192,21 @@ def test_harness_interface(ckpt):
         assert k in res
     with pytest.raises(ValueError):
         h.run_simulation(steps=0)
+
+
+def test_student_calculator_equals_force_field_calculator(ckpt):
+    """The generic dict-in/dict-out StudentCalculator on a StudentForceField
+    checkpoint gives the drop-in calculator's results (molecule and
+    periodic box with stress)."""
+    from mlff_gb300 import systems
+    from mlff_gb300.ase_calculator import StudentForceFieldCalculator
+    from mlff_gb300.student_calculator import StudentCalculator
+    gen = StudentCalculator(model_path=ckpt)
+    ref = StudentForceFieldCalculator(ckpt, enable_stress=True)
+    for s in (systems.lattice_molecule(60, seed=0), systems.water_box(n_water=50, L=11.0, seed=3)):
+        a, b = _atoms(s), _atoms(s)
+        a.calc, b.calc = gen, ref
+        assert a.get_potential_energy() == b.get_potential_energy()
+        np.testing.assert_array_equal(a.get_forces(), b.get_forces())
+        if s.pbc is not None and bool(np.asarray(s.pbc).any()):
+            np.testing.assert_allclose(a.get_stress(), b.get_stress(), rtol=1e-12, atol=1e-12)
