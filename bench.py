@@ -258,8 +258,13 @@ def run_md(args, world, rank, local):
     # energy drift over --md-steps steps from the initial state (not timed)
     drift = None
     if args.md_steps > 0:
+        from mlff_gb300.energy_metrics import replica_energy_stats
         drv.restore(init)
-        tr = drv.run(args.md_steps, graph=True, block=MD_BLOCK)
+        trd = drv.run(args.md_steps, graph=True, block=MD_BLOCK, to_host=False)
+        dst = replica_energy_stats(trd["potential_energy"], trd["kinetic_energy"], 0.5e-3,
+                                   mol_ptr=torch.as_tensor(sysm.mol_ptr), epot0=torch.as_tensor(E0),
+                                   ekin0=torch.as_tensor(K0))
+        tr = {k: v.cpu().numpy() for k, v in trd.items()}
         rel, ab = replica_drift(tr["potential_energy"], tr["kinetic_energy"], E0, K0)
         n_per = np.diff(sysm.mol_ptr)
         mev = 1000.0 * ab / n_per
@@ -269,7 +274,9 @@ def run_md(args, world, rank, local):
                  "abs_drift_mev_per_atom_median": float(np.median(mev)),
                  "abs_drift_mev_per_atom_max_abs": float(np.abs(mev).max()),
                  "max_excursion_mev_per_atom": float(1000.0 * (np.abs(et - (E0 + K0)[None, :]) / n_per).max()),
-                 "edges_at_end": int(drv.engine.status()[1])}
+                 "edges_at_end": int(drv.engine.status()[1]),
+                 "device_stats_median": {k: float(dst[k].median()) for k in (
+                     "conservation_ratio", "drift_rate", "r_squared", "avg_temperature", "std_temperature")}}
     if rank != 0:
         return
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

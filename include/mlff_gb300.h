@@ -222,6 +222,24 @@ int mlff_langevin_steps(const mlff_dims *dims, const void *packed, const mlff_sy
                         double friction, double kT, uint64_t seed, int32_t n_steps, void *workspace,
                         size_t workspace_bytes, mlff_stream_t stream);
 
+/* Per-replica energy-conservation statistics of an MD energy trace, the
+ * report of testing/energy_metrics.py:48-357 (compute_energy_drift,
+ * compute_energy_conservation_ratio, compute_energy_fluctuations,
+ * compute_kinetic_potential_stability, compute_time_resolved_drift with a
+ * linear fit) for every replica at once, on the device.  epot and ekin are
+ * [n_samples][n_mol] (eV, e.g. the traces of mlff_verlet_steps with the
+ * initial energies prepended), samples dt_ps apart; mol_ptr (optional,
+ * [n_mol + 1]) gives atom counts for the temperature.  out [n_mol][20]:
+ *  0 E_0, 1 E_final, 2 drift % (relative), 3 max deviation %, 4 mean E,
+ *  5 std E, 6 range E, 7 mean |E - mean|, 8 conservation ratio,
+ *  9 mean KE, 10 std KE, 11 mean PE, 12 std PE, 13 KE-PE correlation,
+ *  14 <KE>/|<PE>|, 15 drift rate eV/ps (linear fit), 16 R^2 of the fit,
+ *  17 standard error of the rate, 18 mean T (K), 19 std T (K).
+ * Fixed-order reductions: identical results on every run. */
+#define MLFF_ENERGY_STATS 20
+int mlff_md_energy_stats(const double *epot, const double *ekin, int32_t n_samples, int32_t n_mol,
+                         const int64_t *mol_ptr, double dt_ps, double *out, mlff_stream_t stream);
+
 /* Parameter gradients for training: grads <- sum_b w_b dE_b/dtheta for
  * every state_dict tensor, with w (device, double [B]) the derivative of
  * the loss with respect to each structure's energy (the energy term of

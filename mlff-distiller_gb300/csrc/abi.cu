@@ -178,6 +178,8 @@ int energy_forces_impl(const mlff_dims& d, const void* packed, const mlff_system
 int md_kick_drift(const WsLayout& L, void* ws, mlff_md_state* s, double dt, cudaStream_t st);
 int md_langevin_baoa(const WsLayout& L, void* ws, mlff_md_state* s, double dt, double friction, double kT,
                      uint64_t seed, cudaStream_t st);
+int md_energy_stats(const double* epot, const double* ekin, int32_t n, int32_t B, const int64_t* mol_ptr,
+                    double dt_ps, double* out, cudaStream_t st);
 int md_kick(const WsLayout& L, void* ws, mlff_md_state* s, double dt, const int64_t* mol_ptr, int32_t n_mol,
             bool kinetic, cudaStream_t st);
 }  // namespace mlff
@@ -330,6 +332,14 @@ int mlff_langevin_steps(const mlff_dims* dims, const void* packed, const mlff_sy
                         int32_t n_steps, void* workspace, size_t workspace_bytes, mlff_stream_t stream) {
     return md_steps(dims, packed, sys, edge_capacity, path, state, dt, true, friction, kT, seed, n_steps, workspace,
                     workspace_bytes, stream);
+}
+
+int mlff_md_energy_stats(const double* epot, const double* ekin, int32_t n_samples, int32_t n_mol,
+                         const int64_t* mol_ptr, double dt_ps, double* out, mlff_stream_t stream) {
+    if (!epot || !ekin || !out) { set_error("epot, ekin and out are required"); return MLFF_ERR_INVALID; }
+    if (n_samples < 1 || n_mol < 1) { set_error("n_samples >= 1 and n_mol >= 1 required"); return MLFF_ERR_INVALID; }
+    if (!(dt_ps > 0.0)) { set_error("dt_ps > 0 required"); return MLFF_ERR_INVALID; }
+    return md_energy_stats(epot, ekin, n_samples, n_mol, mol_ptr, dt_ps, out, reinterpret_cast<cudaStream_t>(stream));
 }
 
 int mlff_param_grads(const mlff_dims* dims, const void* packed, const mlff_system* sys, int64_t edge_capacity,

@@ -153,4 +153,139 @@ int md_kick(const WsLayout& L, void* ws, mlff_md_state* s, double dt, const int6
     return MLFF_OK;
 }
 
+
+// --------------------------------------------------- energy statistics
+// Per-replica NVE statistics of an energy trace, the quantities of the
+// reference's energy-conservation report (testing/energy_metrics.py:48-357):
+// drift, fluctuations, conservation ratio, kinetic/potential stability,
+// linear-fit drift rate, temperature.  One block per replica, every sum a
+// fixed-order strided accumulation followed by a fixed tree: the result
+// does not depend on the launch and is the same on every run.
+constexpr int ES_NT = 256;
+
+__device__ double es_block_sum(double v, double* red) {
+    red[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = ES_NT / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    const double r = red[0];
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(ES_NT) energy_stats_kernel(const double* __restrict__ epot,
+                                                            const double* __restrict__ ekin, int32_t n, int32_t B,
+                                                            const int64_t* __restrict__ mol_ptr, double dt_ps,
+                                                            double* __restrict__ out) {
+    pdl_wait();
+    pdl_trigger();
+    __shared__ double red[ES_NT];
+    for (int b = blockIdx.x; b < B; b += gridDim.x) {
+        auto et = [&](int i) { return epot[(int64_t)i * B + b] + ekin[(int64_t)i * B + b]; };
+        double se = 0.0, sk = 0.0, sp = 0.0;
+        for (int i = threadIdx.x; i < n; i += ES_NT) {
+            se += et(i);
+            sk += ekin[(int64_t)i * B + b];
+            sp += epot[(int64_t)i * B + b];
+        }
+        const double me = es_block_sum(se, red) / n, mk = es_block_sum(sk, red) / n, mp = es_block_sum(sp, red) / n;
+        const double tm = 0.5 * (n - 1) * dt_ps;   // mean sample time
+        double see = 0.0, sad = 0.0, skk = 0.0, spp = 0.0, skp = 0.0, stt = 0.0, ste = 0.0, smax = 0.0;
+        double emin = 1e300, emax = -1e300;
+        const double e0 = et(0);
+        for (int i = threadIdx.x; i < n; i += ES_NT) {
+            const double e = et(i), de = e - me;
+            const double dk = ekin[(int64_t)i * B + b] - mk, dp = epot[(int64_t)i * B + b] - mp;
+            const double dt = i * dt_ps - tm;
+            see += de * de;
+            sad += fabs(de);
+            skk += dk * dk;
+            spp += dp * dp;
+            skp += dk * dp;
+            stt += dt * dt;
+            ste += dt * de;
+            smax = fmax(smax, fabs(e - e0));
+            emin = fmin(emin, e);
+            emax = fmax(emax, e);
+        }
+        see = es_block_sum(see, red);
+        sad = es_block_sum(sad, red);
+        skk = es_block_sum(skk, red);
+        spp = es_block_sum(spp, red);
+        skp = es_block_sum(skp, red);
+        stt = es_block_sum(stt, red);
+        ste = es_block_sum(ste, red);
+        // maxima and minima by the same fixed tree
+        red[threadIdx.x] = smax;
+        __syncthreads();
+        for (int o = ES_NT / 2; o > 0; o >>= 1) {
+            if (threadIdx.x < o) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + o]);
+            __syncthreads();
+        }
+        smax = red[0];
+        __syncthreads();
+        red[threadIdx.x] = emax;
+        __syncthreads();
+        for (int o = ES_NT / 2; o > 0; o >>= 1) {
+            if (threadIdx.x < o) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + o]);
+            __syncthreads();
+        }
+        emax = red[0];
+        __syncthreads();
+        red[threadIdx.x] = emin;
+        __syncthreads();
+        for (int o = ES_NT / 2; o > 0; o >>= 1) {
+            if (threadIdx.x < o) red[threadIdx.x] = fmin(red[threadIdx.x], red[threadIdx.x + o]);
+            __syncthreads();
+        }
+        emin = red[0];
+        __syncthreads();
+        // residual sum of squares of the linear fit E = a + r t
+        const double rate = stt > 0.0 ? ste / stt : 0.0;
+        double srr = 0.0;
+        for (int i = threadIdx.x; i < n; i += ES_NT) {
+            const double res = et(i) - me - rate * (i * dt_ps - tm);
+            srr += res * res;
+        }
+        srr = es_block_sum(srr, red);
+        if (threadIdx.x == 0) {
+            const double ef = et(n - 1);
+            const double sd = sqrt(see / n), sdk = sqrt(skk / n), sdp = sqrt(spp / n);
+            const double na = mol_ptr ? (double)(mol_ptr[b + 1] - mol_ptr[b]) : 0.0;
+            const double kTconv = na > 0 ? 2.0 / (3.0 * na * 8.617333262e-5) : 0.0;   // K per eV of kinetic energy
+            double* o = out + (int64_t)b * 20;
+            o[0] = e0;
+            o[1] = ef;
+            o[2] = fabs(e0) >= 1e-10 ? 100.0 * (ef - e0) / fabs(e0) : 0.0;   // drift %
+            o[3] = fabs(e0) >= 1e-10 ? 100.0 * smax / fabs(e0) : 0.0;        // max deviation %
+            o[4] = me;
+            o[5] = sd;                                                        // std
+            o[6] = emax - emin;                                               // range
+            o[7] = sad / n;                                                   // mean absolute deviation
+            o[8] = fabs(me) >= 1e-10 ? fmax(0.0, 1.0 - sd / fabs(me)) : 1.0;  // conservation ratio
+            o[9] = mk;
+            o[10] = sdk;
+            o[11] = mp;
+            o[12] = sdp;
+            o[13] = (sdk > 0.0 && sdp > 0.0) ? (skp / n) / (sdk * sdp) : 0.0;  // KE-PE correlation
+            o[14] = fabs(mp) > 1e-10 ? mk / fabs(mp) : 0.0;                   // partition ratio
+            o[15] = rate;                                                     // drift rate (eV/ps)
+            o[16] = see > 1e-10 ? 1.0 - srr / see : 1.0;                      // R^2
+            const double st = sqrt(stt / n);
+            o[17] = st > 1e-10 ? sqrt(srr / n) / (st * sqrt((double)n)) : 0.0;   // drift-rate standard error
+            o[18] = mk * kTconv;                                              // mean temperature (K)
+            o[19] = sdk * kTconv;                                             // temperature std (K)
+        }
+        __syncthreads();
+    }
+}
+
+int md_energy_stats(const double* epot, const double* ekin, int32_t n, int32_t B, const int64_t* mol_ptr,
+                    double dt_ps, double* out, cudaStream_t st) {
+    MLFF_LAUNCH_PDL("energy_stats", energy_stats_kernel, std::min(std::max(B, 1), 152 * 8), ES_NT, 0, st, epot,
+                    ekin, n, B, mol_ptr, dt_ps, out);
+    return MLFF_OK;
+}
 }  // namespace mlff

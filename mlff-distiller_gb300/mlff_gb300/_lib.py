@@ -40,7 +40,8 @@ ERROR_NAMES = {ERR_INVALID: "invalid argument", ERR_CAPACITY: "edge capacity exc
 
 EXPORTS = ["mlff_version", "mlff_last_error_string", "mlff_packed_weights_size", "mlff_pack_weights",
            "mlff_workspace_size", "mlff_build_neighbors", "mlff_copy_neighbors", "mlff_energy_forces",
-           "mlff_read_status", "mlff_clear_status", "mlff_verlet_steps", "mlff_langevin_steps", "mlff_profile_begin",
+           "mlff_read_status", "mlff_clear_status", "mlff_verlet_steps", "mlff_langevin_steps", "mlff_md_energy_stats",
+           "mlff_profile_begin",
            "mlff_profile_end", "mlff_radius_graph_noalloc", "mlff_param_grads"]
 
 PROFILE_KINDS = ["neighbors", "edge_fwd", "edge_bwd", "update_fwd", "update_bwd", "readout", "forces",
@@ -142,6 +143,8 @@ def load(build_if_missing: bool = True):
         lib.mlff_langevin_steps.argtypes = [ctypes.POINTER(Dims), _P, ctypes.POINTER(System), i64, i32,
                                             ctypes.POINTER(MDState), ctypes.c_double, ctypes.c_double,
                                             ctypes.c_double, ctypes.c_uint64, i32, _P, sz, _P]
+        lib.mlff_md_energy_stats.restype = ctypes.c_int
+        lib.mlff_md_energy_stats.argtypes = [_P, _P, i32, i32, _P, ctypes.c_double, _P, _P]
         lib.mlff_profile_begin.restype = ctypes.c_int
         lib.mlff_profile_end.restype = ctypes.c_int
         lib.mlff_profile_end.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(i64), i32]

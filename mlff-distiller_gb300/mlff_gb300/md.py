@@ -209,9 +209,11 @@ class VelocityVerletGPU:
         return max(self.engine.capacity(self.N, self.path),
                    int(self.engine.edge_capacity.get(self.path, 0) * self.headroom) + 1024)
 
-    def run(self, n_steps: int, graph: bool = True, block: int = 50, record: bool = True) -> Dict[str, np.ndarray]:
+    def run(self, n_steps: int, graph: bool = True, block: int = 50, record: bool = True,
+            to_host: bool = True) -> Dict[str, np.ndarray]:
         """Advance n_steps.  Returns per-step potential / kinetic energy per
-        structure, shape [n_steps, B] (eV), when record is set."""
+        structure, shape [n_steps, B] (eV), when record is set -- as device
+        tensors with to_host=False (e.g. for energy_metrics.replica_energy_stats)."""
         if not self._forces_valid:
             self.compute_forces()
         cap = self._capacity()
@@ -244,6 +246,8 @@ class VelocityVerletGPU:
         self.steps_done += n_steps
         if not record:
             return {}
+        if not to_host:
+            return {"potential_energy": epot, "kinetic_energy": ekin}
         return {"potential_energy": epot.cpu().numpy(), "kinetic_energy": ekin.cpu().numpy()}
 
     def _graph(self, k: int, cap: int, record: bool):
