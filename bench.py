@@ -214,6 +214,7 @@ def run_md(args, world, rank, local):
     steps), so timing later steps would measure a sparser system."""
     from mlff_gb300 import _lib, systems
     from mlff_gb300.md import VelocityVerletGPU, kinetic_energy, replica_drift
+    from mlff_gb300.replicas import aggregate_throughput
     sysm = systems.workload(args.workload)
     model = seed_model(args.path).cuda().eval()
     drv = VelocityVerletGPU(model, sysm.Z, sysm.pos, sysm.mol_ptr, timestep_fs=0.5)
@@ -248,13 +249,9 @@ def run_md(args, world, rank, local):
     if code != _lib.OK:
         raise RuntimeError(f"device status {code} during the timed MD region")
     blk_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
-    total_s = sum(blk_ms) / 1000.0
-    if world > 1:
-        t = torch.tensor([total_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(t.item())
     n_md = args.steps * MD_TIME_BLOCK
-    value = sysm.n_atoms * world * n_md / total_s
+    # atom-steps of all ranks / the slowest rank's timed region
+    _, total_s, value = aggregate_throughput(sysm.n_atoms * n_md, sum(blk_ms) / 1000.0, device="cuda")
     # energy drift over --md-steps steps from the initial state (not timed)
     drift = None
     if args.md_steps > 0:
@@ -312,6 +309,7 @@ def main():
         return
     from mlff_gb300 import _lib, systems
     from mlff_gb300.engine import make_batch
+    from mlff_gb300.replicas import aggregate_throughput
 
     sysm = systems.workload(args.workload)
     model = seed_model(args.path).cuda().eval()
@@ -362,13 +360,8 @@ def main():
             eng.energy_forces(batch, path, check=False)
         barrier()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_s = sum(step_ms) / 1000.0
-    if world > 1:
-        t = torch.tensor([total_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(t.item())
     atoms_all = sysm.n_atoms * world
-    value = atoms_all * args.steps / total_s
+    _, total_s, value = aggregate_throughput(sysm.n_atoms * args.steps, sum(step_ms) / 1000.0, device="cuda")
 
     # dominant kernel and its roofline (algorithmic GEMM FLOPs of the filter MLP)
     L = model.num_interactions
@@ -422,11 +415,7 @@ def main():
         for _ in range(args.steps):
             e2e_step()
         barrier()
-        el = time.perf_counter() - t0
-        if world > 1:
-            t = torch.tensor([el], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            el = float(t.item())
+        _, el, _ = aggregate_throughput(sysm.n_atoms * args.steps, time.perf_counter() - t0, device="cuda")
         h2d = Zh.numel() * 8 + Ph.numel() * 4 + (sysm.n_mol + 1) * 8 + (sysm.n_mol * 13 if cell is not None else 0)
         d2h = sysm.n_mol * 8 + sysm.n_atoms * 12
         e2e = {"value": atoms_all * args.steps / el, "unit": UNIT, "h2d_bytes_per_step": h2d,
