@@ -545,10 +545,11 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                 float z[32];
                 tmem_ld32(lane_base + TM_Z + col, z);
                 tmem_ld_wait();
+                const BColumn hc(Hs, F_HH, FN, col, k);
 #pragma unroll
                 for (int i = 0; i < 32; i += 2) {
                     const float z0 = z[i] + bias, z1 = z[i + 1] + bias;
-                    store_col_pair(Hs, F_HH, FN, col + i, k, z0 * fast_sigmoid(z0), z1 * fast_sigmoid(z1));
+                    hc.put_pair(i, z0 * fast_sigmoid(z0), z1 * fast_sigmoid(z1));
                 }
                 // GEMM2 accumulates onto b2[g * 128 + channel]: this warp refills
                 // the 32 chunk-2 cells it has just read, and 64 columns of
@@ -856,13 +857,13 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                 tmem_ld16(lane_base + TM_Z + col, z);
                 tmem_ld16(lane_base + TM_Z + BN + col, zd);
                 tmem_ld_wait();
+                const BColumn hc(Hs, B_HH, 2 * BN, col, k), hdc(Hs, B_HH, 2 * BN, BN + col, k);
 #pragma unroll
                 for (int i = 0; i < 16; i += 2) {
                     const float z0 = z[i] + bias, z1 = z[i + 1] + bias;
                     const float s0 = fast_sigmoid(z0), s1 = fast_sigmoid(z1);
-                    store_col_pair(Hs, B_HH, 2 * BN, col + i, k, z0 * s0, z1 * s1);
-                    store_col_pair(Hs, B_HH, 2 * BN, BN + col + i, k, s0 * (1.0f + z0 * (1.0f - s0)) * zd[i],
-                                   s1 * (1.0f + z1 * (1.0f - s1)) * zd[i + 1]);
+                    hc.put_pair(i, z0 * s0, z1 * s1);
+                    hdc.put_pair(i, s0 * (1.0f + z0 * (1.0f - s0)) * zd[i], s1 * (1.0f + z1 * (1.0f - s1)) * zd[i + 1]);
                 }
                 // f = W2 h accumulates onto b2 and f' = W2 h' onto 0 (each chunk:
                 // 64 columns f^T, then 64 columns f'^T).  This warp refills the

@@ -82,5 +82,28 @@ __device__ __forceinline__ void store_col_pair(unsigned char* tile, uint32_t hal
     *reinterpret_cast<__half*>(tile + half_bytes + o1) = __high2half(lo);
 }
 
+// Column k of a B tile written by the thread that owns it, rows row0 + i
+// with row0 a multiple of 8 (then row0 + i sits i * 128 bytes further and
+// its swizzle key is i % 8): the k-dependent part of b_off is computed once,
+// each pair store costs an add and an xor when i is a compile-time constant.
+struct BColumn {
+    unsigned char* base;   // tile + K-block of k + row0 * 128 + (k % 8) * 2
+    uint32_t half_bytes;
+    uint32_t kj;           // 16-byte chunk of k within its 128-byte row
+    __device__ __forceinline__ BColumn(unsigned char* tile, uint32_t half, int n_rows, int row0, int k)
+        : base(tile + (k >> 6) * b_block(n_rows) + row0 * 128 + (k & 7) * 2), half_bytes(half), kj((k >> 3) & 7) {}
+    // rows row0 + i and row0 + i + 1: the split fp16 values of a and b
+    __device__ __forceinline__ void put_pair(int i, float a, float b) const {
+        __half2 hi, lo;
+        split2(a, b, hi, lo);
+        const uint32_t o0 = (uint32_t)i * 128 + ((kj ^ (uint32_t)(i & 7)) << 4);
+        const uint32_t o1 = (uint32_t)(i + 1) * 128 + ((kj ^ (uint32_t)((i + 1) & 7)) << 4);
+        *reinterpret_cast<__half*>(base + o0) = __low2half(hi);
+        *reinterpret_cast<__half*>(base + o1) = __high2half(hi);
+        *reinterpret_cast<__half*>(base + half_bytes + o0) = __low2half(lo);
+        *reinterpret_cast<__half*>(base + half_bytes + o1) = __high2half(lo);
+    }
+};
+
 }  // namespace tc
 }  // namespace mlff

@@ -289,6 +289,7 @@ __global__ void __launch_bounds__(UNT, 1) update_fwd_tc_kernel(const float* __re
             float z[32];
             tmem_ld32(lane_base + col, z);
             tmem_ld_wait();
+            const BColumn hcol(Bs, UF_HH, UN, col, c);
 #pragma unroll
             for (int i = 0; i < 32; i += 2) {
                 const int a = a0 + col + i;
@@ -296,7 +297,7 @@ __global__ void __launch_bounds__(UNT, 1) update_fwd_tc_kernel(const float* __re
                 if (a + 1 < n_atoms) uz[(int64_t)(a + 1) * H + c] = z[i + 1];
                 // accurate exp: per-atom pre-activations reach |z| ~ 20 with
                 // trained-like weights
-                store_col_pair(Bs, UF_HH, UN, col + i, c, silu_f(z[i]), silu_f(z[i + 1]));
+                hcol.put_pair(i, silu_f(z[i]), silu_f(z[i + 1]));
             }
         }
         fence_async_smem();
@@ -553,9 +554,9 @@ __global__ void __launch_bounds__(UNT, 1) update_bwd_tc_kernel(const float* __re
                 zz[i] = a < n_atoms ? uz[(int64_t)a * H + c] : 0.f;
             }
             tmem_ld_wait();
+            const BColumn zcol(Bs, UB_ZH, UN, col, c);
 #pragma unroll
-            for (int i = 0; i < 32; i += 2)
-                store_col_pair(Bs, UB_ZH, UN, col + i, c, zb[i] * dsilu_f(zz[i]), zb[i + 1] * dsilu_f(zz[i + 1]));
+            for (int i = 0; i < 32; i += 2) zcol.put_pair(i, zb[i] * dsilu_f(zz[i]), zb[i + 1] * dsilu_f(zz[i + 1]));
         }
         fence_async_smem();
         fence_before_sync();
