@@ -29,7 +29,10 @@
 // TMEM (512 columns): [0,128) lo halves of W2 chunks 0 and 1; [128,512) the
 // GEMM2 accumulators (forward: 128-edge tiles, chunk g at 128 + 128 g;
 // reverse: 64-edge tiles with [f | f'] per chunk, f' = df/dd in forward
-// mode); GEMM1's z (and z') alias chunk 2 until epilogue 1 has read them.
+// mode); GEMM1's output aliases one chunk until epilogue 1 has read it:
+// chunk 0 in the forward kernel (read by the scalar warps only, so the next
+// tile's GEMM1 is issued while the vector warps finish epilogue 2), chunk 2
+// ([z; z']) in the reverse kernel.
 #include <cuda_fp16.h>
 #include <mutex>
 #include "common.cuh"
@@ -51,8 +54,9 @@ constexpr uint32_t W2L_BYTES = 8 * A_TILE;    // lo tiles of W2 chunk 2 (residen
 
 // TMEM columns (512 allocated): [0,128) the lo halves of W2 chunks 0 and 1
 // as MMA A operands (chunk g, K-step s at 64 g + 8 s); [128,512) the GEMM2
-// accumulators, chunk g at 128 + 128 g; GEMM1 writes z into chunk 2's
-// columns, which epilogue 1 reads before it refills them with the bias.
+// accumulators, chunk g at 128 + 128 g; GEMM1 writes z into the columns
+// of chunk 0 (forward) or 2 (reverse, TM_Z), which epilogue 1 reads before
+// it refills them with the bias.
 constexpr uint32_t TM_W2LO = 0;
 constexpr uint32_t TM_F = 128;
 constexpr uint32_t TM_Z = 384;
@@ -477,6 +481,23 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
 
     bool aborted = false;
     uint32_t e_phase = 0, e_issued = 0;   // E-tile copies: barrier phase, copies issued (thread 32)
+    // GEMM1: z^T = W1 e^T on the bulk-copied E tile, into chunk 0's columns
+    auto issue_gemm1 = [&]() {
+        if (!mbar_wait(e_bar, e_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 8);
+        fence_after_sync();
+        constexpr uint32_t idesc = idesc_f16(FN);
+#pragma unroll
+        for (int s = 0; s < 2; ++s)
+#pragma unroll
+            for (int pr = 0; pr < 3; ++pr) {
+                const uint32_t ahl = pr == 2 ? 1 : 0, bhl = pr == 1 ? 1 : 0;
+                const uint64_t ad = sdesc(smem_u32(w1s + s * SLAB + ahl * A_TILE), A_LBO, A_SBO);
+                const uint64_t bd = sdesc(smem_u32(Es + bhl * ET_HALF + s * 4096), 2048, 128);
+                mma_f16(tmem + TM_F, ad, bd, idesc, (s | pr) != 0);
+            }
+        mma_commit(mma_bar);
+    };
+    bool g1_issued = false;   // GEMM1 of the current tile already issued (at the end of the previous tile)
     for (int p = blockIdx.x; p < a.nparts && !aborted; p += gridDim.x) {
         const int j0 = a.part[p], j1 = a.part[p + 1];
         if (j0 >= j1) continue;
@@ -515,21 +536,8 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
             const int* soff = reinterpret_cast<const int*>(sb + F_SB_SOFF);
             const float* uc = reinterpret_cast<const float*>(sb + F_SB_UC);
             const uint32_t* chg = reinterpret_cast<const uint32_t*>(sb + F_SB_CHG);
-            if (t == 0) {   // GEMM1: z^T = W1 e^T on the bulk-copied E tile
-                if (!mbar_wait(e_bar, e_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 8);
-                fence_after_sync();
-                constexpr uint32_t idesc = idesc_f16(FN);
-#pragma unroll
-                for (int s = 0; s < 2; ++s)
-#pragma unroll
-                    for (int pr = 0; pr < 3; ++pr) {
-                        const uint32_t ahl = pr == 2 ? 1 : 0, bhl = pr == 1 ? 1 : 0;
-                        const uint64_t ad = sdesc(smem_u32(w1s + s * SLAB + ahl * A_TILE), A_LBO, A_SBO);
-                        const uint64_t bd = sdesc(smem_u32(Es + bhl * ET_HALF + s * 4096), 2048, 128);
-                        mma_f16(tmem + TM_Z, ad, bd, idesc, (s | pr) != 0);
-                    }
-                mma_commit(mma_bar);
-            }
+            if (t == 0 && !g1_issued) issue_gemm1();
+            g1_issued = false;
             e_phase ^= 1;
             if (w == 0) __syncwarp();
             // only warp 0 polls the MMA barrier; the others wait at the CTA
@@ -543,7 +551,7 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                 const int k = c, col = 32 * r;
                 const float bias = b1s[k];
                 float z[32];
-                tmem_ld32(lane_base + TM_Z + col, z);
+                tmem_ld32(lane_base + TM_F + col, z);
                 tmem_ld_wait();
                 const BColumn hc(Hs, F_HH, FN, col, k);
 #pragma unroll
@@ -552,18 +560,18 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                     hc.put_pair(i, z0 * fast_sigmoid(z0), z1 * fast_sigmoid(z1));
                 }
                 // GEMM2 accumulates onto b2[g * 128 + channel]: this warp refills
-                // the 32 chunk-2 cells it has just read, and 64 columns of
-                // chunks 0 and 1 (warps r = 0, 1: chunk 0; r = 2, 3: chunk 1)
+                // the 32 chunk-0 cells it has just read, and 64 columns of
+                // chunks 1 and 2 (warps r = 0, 1: chunk 1; r = 2, 3: chunk 2)
                 float bv[16];
-                const float b2c = b2s[2 * H + c], b01 = b2s[(r >> 1) * H + c];
+                const float b0c = b2s[c], b12 = b2s[(1 + (r >> 1)) * H + c];
 #pragma unroll
-                for (int i = 0; i < 16; ++i) bv[i] = b2c;
-                tmem_st16(lane_base + TM_Z + col, bv);
-                tmem_st16(lane_base + TM_Z + col + 16, bv);
+                for (int i = 0; i < 16; ++i) bv[i] = b0c;
+                tmem_st16(lane_base + TM_F + col, bv);
+                tmem_st16(lane_base + TM_F + col + 16, bv);
 #pragma unroll
-                for (int i = 0; i < 16; ++i) bv[i] = b01;
+                for (int i = 0; i < 16; ++i) bv[i] = b12;
 #pragma unroll
-                for (int kk = 0; kk < 4; ++kk) tmem_st16(lane_base + TM_F + 64 * r + 16 * kk, bv);
+                for (int kk = 0; kk < 4; ++kk) tmem_st16(lane_base + TM_F + 128 + 64 * r + 16 * kk, bv);
                 tmem_st_wait();
             }
             fence_async_smem();
@@ -662,6 +670,16 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                     if (col + 48 < n) gather16(xn, col + 48);
                 }
             }
+            // chunk 0 is read by the scalar warps only (r = 0, warps 0-3): once
+            // all four are through epilogue 2, the next tile's GEMM1 can write z
+            // there while the vector warps finish
+            if (more && r == 0) {
+                tmem_ld_wait();
+                fence_before_sync();
+                bar_sync_first(4 * 32);
+                if (t == 0) issue_gemm1();
+            }
+            g1_issued = more;
             cp_async_wait_all();
             fence_before_sync();
             __syncthreads();
@@ -677,9 +695,11 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
         }
         if (!aborted) a.Xt[(int64_t)cur * 4 * H + fidx] = base + (acc + accu);
     }
-    // drain: the resident-weight load and any E-tile copy issued must have
-    // landed before the CTA exits
+    // drain: the resident-weight load, any E-tile copy and a GEMM1 issued
+    // for a tile that never ran (abort) must be complete before the CTA exits
     __syncthreads();
+    if (t == 0 && g1_issued && !mbar_wait(mma_bar, mma_phase, WAIT_BUDGET))
+        set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 3);
     if (t == 32) {
         if (!mbar_wait(w2h_bar, 0, WAIT_BUDGET)) set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 7);
         // an E-tile copy issued for a tile that never ran (abort) must land first
