@@ -1,8 +1,8 @@
 """ORACLE -- test infrastructure only.
 
 The reference's energy-conservation metrics (src/mlff_distiller/testing/
-energy_metrics.py) restated in numpy, as the checker of the device
-statistics kernel (mlff_md_energy_stats):
+energy_metrics.py) restated in numpy; the tests compare the device
+statistics kernel (mlff_md_energy_stats) with it:
   drift (relative / max deviation)           energy_metrics.py:48-94
   conservation ratio 1 - std/|mean|          :97-157
   fluctuations (std, range, mean abs dev)    :160-200

@@ -1,7 +1,7 @@
 /*
  * ORACLE -- test infrastructure only. Nothing in the product path links,
  * loads or calls this file; tests/, __graft_entry__.smoke() and bench.py's
- * CPU-baseline leg use it as the checker.
+ * CPU-baseline leg use it to check results.
  *
  * CPU restatement of the reference's radius-graph decision
  * (src/mlff_distiller/models/student_model.py:63-109, radius_graph_native):
