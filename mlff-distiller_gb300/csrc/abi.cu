@@ -66,6 +66,10 @@ WsLayout ws_layout(const mlff_dims& d, int32_t n_atoms, int32_t n_mol, int64_t c
         return r;
     };
     const int64_t N = n_atoms, B = n_mol, Ly = d.n_layers;
+    // the tangent pass of the force-loss gradient keeps (value, tangent)
+    // pairs in the plain path's float arrays
+    const bool dual = path == MLFF_PATH_TRAIN_FORCES;
+    const size_t fs = dual ? 2 * sizeof(float) : sizeof(float);
     const int64_t scan_n = std::max<int64_t>(N + 1, L.ncell_cap + 1);
     L.status = take(sizeof(Status));
     L.pos4 = take(sizeof(float4) * N);
@@ -82,12 +86,12 @@ WsLayout ws_layout(const mlff_dims& d, int32_t n_atoms, int32_t n_mol, int64_t c
     L.cell_atoms = take(4 * N);
     L.atom_cell = take(4 * N);
     L.part = take(4 * (L.P + 1));
-    L.X = take(sizeof(float) * (Ly + 1) * N * 4 * H);
-    L.Xt = take(sizeof(float) * Ly * N * 4 * H);
-    L.uz = take(sizeof(float) * Ly * N * H);
-    L.ua = take(sizeof(float) * Ly * N * H3);
+    L.X = take(fs * (Ly + 1) * N * 4 * H);
+    L.Xt = take(fs * Ly * N * 4 * H);
+    L.uz = take(fs * Ly * N * H);
+    L.ua = take(fs * Ly * N * H3);
     // two adjoint buffers; the second also holds the per-atom virial (9 doubles)
-    L.xbar = take(sizeof(float) * 2 * N * 4 * H);
+    L.xbar = take(fs * 2 * N * 4 * H);
     L.e_atom = take(sizeof(float) * N);
     L.md_pos32 = take(sizeof(float) * 3 * N);
     if (path == MLFF_PATH_TUNED_TC) {
@@ -99,23 +103,23 @@ WsLayout ws_layout(const mlff_dims& d, int32_t n_atoms, int32_t n_mol, int64_t c
         L.etile_f = take((size_t)L.n_etile_f * 16384);
         L.etile_b = take((size_t)L.n_etile_b * 16384);
     }
-    if (path == MLFF_PATH_PLAIN_FP32 || path == MLFF_PATH_TRAIN) {
-        L.geo = take(sizeof(float4) * cap);
-        L.erbf = take(sizeof(float) * cap * RMAX);
-        L.erbf_d = take(sizeof(float) * cap * RMAX);
-        L.fz = take(sizeof(float) * Ly * cap * H);
-        L.ff = take(sizeof(float) * Ly * cap * H3);
-        L.fh = take(sizeof(float) * cap * H);
-        L.fbar = take(sizeof(float) * cap * H3);
-        L.comb = take(sizeof(float) * N * 2 * H);
-        L.uh = take(sizeof(float) * N * H);
-        L.abar = take(sizeof(float) * N * H3);
+    if (path == MLFF_PATH_PLAIN_FP32 || path == MLFF_PATH_TRAIN || dual) {
+        L.geo = take(4 * fs * cap);
+        L.erbf = take(fs * cap * RMAX);
+        L.erbf_d = take(fs * cap * RMAX);
+        L.fz = take(fs * Ly * cap * H);
+        L.ff = take(fs * Ly * cap * H3);
+        L.fh = take(fs * cap * H);
+        L.fbar = take(fs * cap * H3);
+        L.comb = take(fs * N * 2 * H);
+        L.uh = take(fs * N * H);
+        L.abar = take(fs * N * H3);
     }
-    if (path == MLFF_PATH_TRAIN) {
-        L.gcomb = take(sizeof(float) * N * 2 * H);
-        L.ghead = take(sizeof(float) * N * 193);
-        L.gpart = take(sizeof(float) * GRAD_SPLIT * H3 * H);
-        L.gmix = take(sizeof(float) * GRAD_MIX_BLOCKS * 9);
+    if (path == MLFF_PATH_TRAIN || dual) {
+        L.gcomb = take(fs * N * 2 * H);
+        L.ghead = take(fs * N * 193);
+        L.gpart = take(fs * GRAD_SPLIT * H3 * H);
+        L.gmix = take(fs * GRAD_MIX_BLOCKS * 9);
     }
     L.total = p;
     return L;
@@ -151,7 +155,7 @@ static int check_sys(const mlff_system* s, int64_t cap) {
 
 static int check_path(int32_t path) {
     if (path != MLFF_PATH_PLAIN_FP32 && path != MLFF_PATH_TUNED_TC && path != MLFF_PATH_TUNED_FP32 &&
-        path != MLFF_PATH_TRAIN) {
+        path != MLFF_PATH_TRAIN && path != MLFF_PATH_TRAIN_FORCES) {
         set_error("unknown path %d", path);
         return MLFF_ERR_INVALID;
     }
@@ -172,7 +176,8 @@ int energy_forces_impl(const mlff_dims& d, const void* packed, const mlff_system
     int r = launch_neighbors(d, sys, L, ws, st);
     if (r) return r;
     const float* P = static_cast<const float*>(packed);
-    if (path == MLFF_PATH_PLAIN_FP32 || path == MLFF_PATH_TRAIN) return run_plain(d, P, po, sys, L, ws, out, st);
+    if (path == MLFF_PATH_PLAIN_FP32 || path == MLFF_PATH_TRAIN || path == MLFF_PATH_TRAIN_FORCES)
+        return run_plain(d, P, po, sys, L, ws, out, st);
     return run_tuned(d, P, po, sys, L, ws, out, path, st);
 }
 int md_kick_drift(const WsLayout& L, void* ws, mlff_md_state* s, double dt, cudaStream_t st);
@@ -359,6 +364,24 @@ int mlff_param_grads(const mlff_dims* dims, const void* packed, const mlff_syste
     PackedOffsets po = packed_offsets(*dims);
     GradCtx g{energy_weights, *grads};
     return run_plain(*dims, static_cast<const float*>(packed), po, *sys, L, workspace, *out, st, &g);
+}
+
+int mlff_param_grads_forces(const mlff_dims* dims, const void* packed, const mlff_system* sys, int64_t edge_capacity,
+                            const float* force_weights, const mlff_grads* grads, void* workspace,
+                            size_t workspace_bytes, mlff_stream_t stream) {
+    WsLayout L;
+    int r = prepare(dims, sys, edge_capacity, MLFF_PATH_TRAIN_FORCES, workspace, workspace_bytes, L);
+    if (r) return r;
+    if (!packed || !force_weights || !grads) {
+        set_error("packed weights, force_weights and grads are required");
+        return MLFF_ERR_INVALID;
+    }
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    MLFF_CUDA(cudaMemsetAsync(ws_ptr<Status>(workspace, L.status), 0, sizeof(Status), st));
+    if ((r = launch_neighbors(*dims, *sys, L, workspace, st))) return r;
+    PackedOffsets po = packed_offsets(*dims);
+    GradCtx g{nullptr, *grads};
+    return run_plain_tangent(*dims, static_cast<const float*>(packed), po, *sys, L, workspace, st, g, force_weights);
 }
 
 int mlff_read_status(const void* workspace, int32_t* code, int64_t* n_edges, int32_t* where, mlff_stream_t stream) {

@@ -51,7 +51,8 @@ struct WsLayout {
     size_t comb;               // float [N][2H]
     size_t uh;                 // float [N][H]
     size_t abar;               // float [N][3H]
-    // parameter-gradient path only
+    // parameter-gradient paths only (float arrays of the plain path hold
+    // (value, tangent) pairs, twice the size, on MLFF_PATH_TRAIN_FORCES)
     size_t gcomb;              // float [N][2H]   update-MLP input recomputed per layer
     size_t ghead;              // float [N][193]  readout: h1 (64), a1bar (64), h2 (32), a2bar (32), ebar (1)
     size_t gpart;              // float [GRAD_SPLIT][3H*H] partial weight gradients
@@ -107,15 +108,29 @@ struct GradCtx {
 int run_plain(const mlff_dims& d, const float* packed, const PackedOffsets& po,
               const mlff_system& sys, const WsLayout& L, void* ws, const mlff_outputs& out,
               cudaStream_t st, const GradCtx* grad = nullptr);
+// Pass of the plain path over (value, tangent) pairs with position
+// direction pos_t [N][3]: subtracts d/deps grad_theta sum_b E_b(r + eps pos_t)
+// from every non-NULL gradient in grad.g (grad.w unused).
+int run_plain_tangent(const mlff_dims& d, const float* packed, const PackedOffsets& po,
+                      const mlff_system& sys, const WsLayout& L, void* ws, cudaStream_t st,
+                      const GradCtx& grad, const float* pos_t);
+// Weight-gradient reductions of the plain path's reverse pass, over float
+// or Dual scalars (instantiated in grads.cu).
+template <class T>
 int grad_readout(const mlff_dims& d, const float* P, const PackedOffsets& po, const mlff_system& sys,
                  const WsLayout& L, void* ws, const double* w, const mlff_grads& g, cudaStream_t st);
-int grad_update_out(const WsLayout& L, void* ws, int l, const float* xbo, const mlff_grads& g, cudaStream_t st);
-int grad_update_in(const WsLayout& L, void* ws, int l, const float* zbar_u, const float* comb_l,
+template <class T>
+int grad_update_out(const WsLayout& L, void* ws, int l, const T* xbo, const mlff_grads& g, cudaStream_t st);
+template <class T>
+int grad_update_in(const WsLayout& L, void* ws, int l, const T* zbar_u, const T* comb_l,
                    const mlff_grads& g, cudaStream_t st);
+template <class T>
 int grad_filter_out(const WsLayout& L, void* ws, int l, const int32_t* E_dev, const mlff_grads& g, cudaStream_t st);
+template <class T>
 int grad_filter_in(const mlff_dims& d, const WsLayout& L, void* ws, int l, const int32_t* E_dev, const mlff_grads& g,
                    cudaStream_t st);
-int grad_embedding(const mlff_dims& d, const mlff_system& sys, const WsLayout& L, void* ws, const float* xbar0,
+template <class T>
+int grad_embedding(const mlff_dims& d, const mlff_system& sys, const WsLayout& L, void* ws, const T* xbar0,
                    const mlff_grads& g, cudaStream_t st);
 int run_tuned(const mlff_dims& d, const float* packed, const PackedOffsets& po,
               const mlff_system& sys, const WsLayout& L, void* ws, const mlff_outputs& out,

@@ -28,6 +28,7 @@ PATH_PLAIN_FP32 = 0
 PATH_TUNED_TC = 1
 PATH_TUNED_FP32 = 2
 PATH_TRAIN = 3
+PATH_TRAIN_FORCES = 4
 
 PATHS = {"plain": PATH_PLAIN_FP32, "fp32": PATH_PLAIN_FP32, "plain_fp32": PATH_PLAIN_FP32,
          "fp16x3": PATH_TUNED_TC, "tc": PATH_TUNED_TC, "tuned": PATH_TUNED_TC,
@@ -42,7 +43,7 @@ EXPORTS = ["mlff_version", "mlff_last_error_string", "mlff_packed_weights_size",
            "mlff_workspace_size", "mlff_build_neighbors", "mlff_copy_neighbors", "mlff_energy_forces",
            "mlff_read_status", "mlff_clear_status", "mlff_verlet_steps", "mlff_langevin_steps", "mlff_md_energy_stats",
            "mlff_profile_begin",
-           "mlff_profile_end", "mlff_radius_graph_noalloc", "mlff_param_grads"]
+           "mlff_profile_end", "mlff_radius_graph_noalloc", "mlff_param_grads", "mlff_param_grads_forces"]
 
 PROFILE_KINDS = ["neighbors", "edge_fwd", "edge_bwd", "update_fwd", "update_bwd", "readout", "forces",
                  "plain_gemm", "plain_edge", "other", "md"]
@@ -151,6 +152,9 @@ def load(build_if_missing: bool = True):
         lib.mlff_param_grads.restype = ctypes.c_int
         lib.mlff_param_grads.argtypes = [ctypes.POINTER(Dims), _P, ctypes.POINTER(System), i64, _P,
                                          ctypes.POINTER(Grads), ctypes.POINTER(Outputs), _P, sz, _P]
+        lib.mlff_param_grads_forces.restype = ctypes.c_int
+        lib.mlff_param_grads_forces.argtypes = [ctypes.POINTER(Dims), _P, ctypes.POINTER(System), i64, _P,
+                                                ctypes.POINTER(Grads), _P, sz, _P]
         lib.mlff_radius_graph_noalloc.restype = ctypes.c_int
         lib.mlff_radius_graph_noalloc.argtypes = [ctypes.POINTER(System), ctypes.c_float, i64, _P, _P, _P, _P]
         _lib = lib

@@ -1,21 +1,27 @@
 """Training of the StudentForceField on the GPU with the library's own
 forward and reverse kernels.
 
-``param_grads`` returns sum_b w_b dE_b/dtheta for every trainable tensor
-of the state_dict from one call of ``mlff_param_grads`` (plain FP32 path:
-per-op forward, hand-written reverse pass with the weight-gradient
-reductions), the parameter part of ``loss.backward()`` in
-Trainer.train_epoch (training/trainer.py:288-393) for an energy loss.
+``param_grads`` returns the parameter part of ``loss.backward()`` in
+Trainer.train_epoch (training/trainer.py:288-393) for every trainable
+tensor of the state_dict, given the loss's derivatives with respect to the
+predictions: w_b = dL/dE_b (one call of ``mlff_param_grads``: plain FP32
+path forward, hand-written reverse pass with the weight-gradient
+reductions) and, for a loss on forces, G_i = dL/dF_i (one call of
+``mlff_param_grads_forces``: the same path in forward mode over the reverse
+pass, which adds sum_i G_i . dF_i/dtheta -- what the reference gets by
+taking forces with create_graph=True and differentiating again).
 
-``EnergyTrainer`` is the optimisation step around it with the reference's
-defaults (configs/train_student.yaml: AdamW, lr 1e-3, weight decay 1e-5,
-betas (0.9, 0.999), eps 1e-8, gradient-norm clip 1.0) and the energy
-term of ForceFieldLoss (training/losses.py:106-246: mean squared error of
-the per-structure energies).  The force term of that loss needs the
-gradient of the forces with respect to the parameters (a second-order
-reverse pass) and is not part of this module.
+``ForceFieldLoss`` restates the reference's loss (training/losses.py:15-
+246: energy, force and angular terms with mse / mae / huber components);
+the trainers evaluate it with torch on the predicted energies and forces
+only, to get w and G.  ``ForceFieldTrainer`` is the optimisation step with
+the reference's defaults (configs/train_student.yaml: energy weight 1,
+force weight 100, angular weight 10, AdamW lr 1e-3, weight decay 1e-5,
+betas (0.9, 0.999), eps 1e-8, gradient-norm clip 1.0); ``EnergyTrainer``
+the energy-only step.
 """
 import ctypes
+import warnings
 from typing import Dict, Optional, Tuple
 
 import numpy as np
@@ -40,19 +46,7 @@ def trainable_names(model) -> list:
     return [n for n, p in model.named_parameters() if p.requires_grad]
 
 
-def param_grads(model, batch: Batch, weights: torch.Tensor, forces: bool = False
-                ) -> Tuple[torch.Tensor, Dict[str, torch.Tensor], Optional[torch.Tensor]]:
-    """Energies [B] (float64), {name: sum_b w_b dE_b/d(name)} for every
-    trainable parameter (float32, state_dict shapes) and, if asked,
-    -sum_b w_b dE_b/dpos."""
-    eng = model.engine()
-    dev = eng.device
-    N, B = batch.n_atoms, batch.n_mol
-    w = torch.as_tensor(weights, dtype=torch.float64, device=dev).contiguous()
-    if w.shape != (B,):
-        raise ValueError(f"weights must have shape ({B},), got {tuple(w.shape)}")
-    params = dict(model.named_parameters())
-    grads = {n: torch.zeros_like(p, dtype=torch.float32, device=dev) for n, p in params.items() if p.requires_grad}
+def _grads_struct(model, grads: Dict[str, torch.Tensor]):
     g = _lib.Grads()
     g.embedding = _lib.ptr(grads.get("embedding.weight"))
     for l in range(model.num_interactions):
@@ -60,15 +54,42 @@ def param_grads(model, batch: Batch, weights: torch.Tensor, forces: bool = False
             getattr(g, field)[l] = _lib.ptr(grads.get(f"interactions.{l}.{key}"))
     for field, key in _HEAD_KEYS.items():
         setattr(g, field, _lib.ptr(grads.get(key)))
+    return g
+
+
+def param_grads(model, batch: Batch, weights: torch.Tensor, forces: bool = False,
+                force_weights: Optional[torch.Tensor] = None
+                ) -> Tuple[torch.Tensor, Dict[str, torch.Tensor], Optional[torch.Tensor]]:
+    """Energies [B] (float64), {name: dL/d(name)} for every trainable
+    parameter (float32, state_dict shapes) and, if asked, the forces
+    -sum_b w_b dE_b/dpos.
+
+    dL/dtheta = sum_b w_b dE_b/dtheta (weights: w = dL/dE, [B]) plus, when
+    force_weights G = dL/dF [N,3] is given, sum_i G_i . dF_i/dtheta."""
+    eng = model.engine()
+    dev = eng.device
+    N, B = batch.n_atoms, batch.n_mol
+    w = torch.as_tensor(weights, dtype=torch.float64, device=dev).contiguous()
+    if w.shape != (B,):
+        raise ValueError(f"weights must have shape ({B},), got {tuple(w.shape)}")
+    G = None
+    if force_weights is not None:
+        G = torch.as_tensor(force_weights, dtype=torch.float32, device=dev).contiguous()
+        if G.shape != (N, 3):
+            raise ValueError(f"force_weights must have shape ({N}, 3), got {tuple(G.shape)}")
+    params = dict(model.named_parameters())
+    grads = {n: torch.zeros_like(p, dtype=torch.float32, device=dev) for n, p in params.items() if p.requires_grad}
+    g = _grads_struct(model, grads)
     E = torch.empty(B, dtype=torch.float64, device=dev)
     F = torch.empty(N, 3, dtype=torch.float32, device=dev) if forces else None
     out = _lib.Outputs()
     out.energy, out.forces, out.virial, out.atom_energy = E.data_ptr(), _lib.ptr(F), None, None
     sysd = batch.system()
     path = _lib.PATH_TRAIN
+    ws_path = _lib.PATH_TRAIN if G is None else _lib.PATH_TRAIN_FORCES
     for _ in range(4):
         cap = eng.capacity(N, path)
-        ws = eng.workspace_for(N, B, cap, path)
+        ws = eng.workspace_for(N, B, cap, ws_path)
         _lib.check(eng.lib.mlff_param_grads(ctypes.byref(eng.dims), eng.packed.data_ptr(), ctypes.byref(sysd), cap,
                                             w.data_ptr(), ctypes.byref(g), ctypes.byref(out), ws.data_ptr(),
                                             ws.numel(), _stream_handle()))
@@ -82,7 +103,167 @@ def param_grads(model, batch: Batch, weights: torch.Tensor, forces: bool = False
         break
     else:
         raise _lib.MLFFError(_lib.ERR_CAPACITY, "edge capacity did not converge")
+    if G is not None:
+        # same structures, same capacity: the edge list fits
+        _lib.check(eng.lib.mlff_param_grads_forces(ctypes.byref(eng.dims), eng.packed.data_ptr(), ctypes.byref(sysd),
+                                                   cap, G.data_ptr(), ctypes.byref(g), ws.data_ptr(), ws.numel(),
+                                                   _stream_handle()))
+        code, _, where = eng.status()
+        if code != _lib.OK:
+            raise _lib.MLFFError(code, f"device status {code} at index {where}")
     return E, grads, F
+
+
+class ForceFieldLoss:
+    """Weighted energy / force / angular loss on predicted energies [B] and
+    forces [N,3] (ForceFieldLoss, training/losses.py:15-246): each term is an
+    mse, mae or huber loss with the given reduction; the angular term is
+    1 - cos between predicted and target force vectors (norms clamped at
+    1e-8).  Stress enters only when both dicts hold it.  Returns the
+    reference's dict of terms and monitoring metrics."""
+
+    def __init__(self, energy_weight: float = 1.0, force_weight: float = 100.0, stress_weight: float = 0.1,
+                 angular_weight: float = 10.0, energy_loss_type: str = "mse", force_loss_type: str = "mse",
+                 stress_loss_type: str = "mse", huber_delta: float = 1.0, reduction: str = "mean"):
+        self.energy_weight, self.force_weight = energy_weight, force_weight
+        self.stress_weight, self.angular_weight = stress_weight, angular_weight
+        self.energy_loss_type, self.force_loss_type = energy_loss_type, force_loss_type
+        self.stress_loss_type = stress_loss_type
+        self.huber_delta, self.reduction = huber_delta, reduction
+        if force_weight > 0 and energy_weight > 0 and force_weight < energy_weight:
+            warnings.warn(f"Force weight ({force_weight}) < energy weight ({energy_weight}). "
+                          "For MD stability, forces should be weighted higher than energy.", UserWarning)
+
+    def _component(self, pred, target, kind: str):
+        import torch.nn.functional as tf
+        if kind == "mse":
+            return tf.mse_loss(pred, target, reduction=self.reduction)
+        if kind == "mae":
+            return tf.l1_loss(pred, target, reduction=self.reduction)
+        if kind == "huber":
+            return tf.huber_loss(pred, target, delta=self.huber_delta, reduction=self.reduction)
+        raise ValueError(f"Unknown loss type: {kind}")
+
+    def __call__(self, predictions: Dict[str, torch.Tensor], targets: Dict[str, torch.Tensor],
+                 mask: Optional[Dict[str, torch.Tensor]] = None) -> Dict[str, torch.Tensor]:
+        import torch.nn.functional as tf
+        out: Dict[str, torch.Tensor] = {}
+        total = 0.0
+
+        def pair(key):
+            p, t = predictions[key], targets[key]
+            if mask is not None and key in mask:
+                p, t = p[mask[key]], t[mask[key]]
+            return p, t
+
+        if "energy" in predictions and "energy" in targets and self.energy_weight > 0:
+            p, t = pair("energy")
+            out["energy"] = self._component(p, t, self.energy_loss_type)
+            total = total + self.energy_weight * out["energy"]
+            with torch.no_grad():
+                out["energy_rmse"] = torch.sqrt(tf.mse_loss(p, t))
+                out["energy_mae"] = tf.l1_loss(p, t)
+        if "forces" in predictions and "forces" in targets and self.force_weight > 0:
+            p, t = pair("forces")
+            out["force"] = self._component(p, t, self.force_loss_type)
+            total = total + self.force_weight * out["force"]
+            if self.angular_weight > 0:
+                pn = p / torch.norm(p, dim=-1, keepdim=True).clamp(min=1e-8)
+                tn = t / torch.norm(t, dim=-1, keepdim=True).clamp(min=1e-8)
+                cos = (pn * tn).sum(dim=-1)
+                ang = 1.0 - cos
+                out["angular"] = ang.mean() if self.reduction == "mean" else (
+                    ang.sum() if self.reduction == "sum" else ang)
+                total = total + self.angular_weight * out["angular"]
+                with torch.no_grad():
+                    deg = torch.acos(torch.clamp(cos, -1.0, 1.0)) * (180.0 / 3.14159265)
+                    out["angular_error_mean_deg"], out["angular_error_max_deg"] = deg.mean(), deg.max()
+            with torch.no_grad():
+                out["force_rmse"] = torch.sqrt(tf.mse_loss(p, t))
+                out["force_mae"] = tf.l1_loss(p, t)
+                if p.dim() >= 2 and p.shape[-1] == 3:
+                    sq = (p - t) ** 2
+                    for i, ax in enumerate("xyz"):
+                        out[f"force_rmse_{ax}"] = torch.sqrt(sq[..., i].mean())
+        if "stress" in predictions and "stress" in targets and self.stress_weight > 0:
+            p, t = pair("stress")
+            out["stress"] = self._component(p, t, self.stress_loss_type)
+            total = total + self.stress_weight * out["stress"]
+            with torch.no_grad():
+                out["stress_rmse"] = torch.sqrt(tf.mse_loss(p, t))
+                out["stress_mae"] = tf.l1_loss(p, t)
+        out["total"] = total
+        return out
+
+    def derivatives(self, E: torch.Tensor, F: torch.Tensor, E_ref: torch.Tensor, F_ref: torch.Tensor,
+                    mask: Optional[Dict[str, torch.Tensor]] = None):
+        """(loss dict, dL/dE [B] float64, dL/dF [N,3] float32 or None): the
+        loss differentiated with respect to the predictions only."""
+        Ed = E.detach().to(torch.float64).requires_grad_(True)
+        Fd = F.detach().to(torch.float64).requires_grad_(True)
+        out = self({"energy": Ed, "forces": Fd},
+                   {"energy": E_ref.to(torch.float64), "forces": F_ref.to(torch.float64)}, mask)
+        total = out["total"]
+        if not torch.is_tensor(total) or not total.requires_grad:
+            return out, torch.zeros_like(Ed), None
+        gE, gF = torch.autograd.grad(total, [Ed, Fd], allow_unused=True)
+        gE = torch.zeros_like(Ed) if gE is None else gE.detach()
+        gF = None if gF is None else gF.detach().to(torch.float32)
+        return out, gE, gF
+
+
+def _adamw(model, lr, weight_decay, betas, eps):
+    return torch.optim.AdamW([p for p in model.parameters() if p.requires_grad], lr=lr,
+                             weight_decay=weight_decay, betas=betas, eps=eps)
+
+
+def _apply(model, opt, grads, grad_clip):
+    for n, p in model.named_parameters():
+        if p.requires_grad:
+            p.grad = grads[n].to(p.dtype)
+    if grad_clip:
+        torch.nn.utils.clip_grad_norm_(model.parameters(), grad_clip)
+    opt.step()
+    opt.zero_grad(set_to_none=True)
+
+
+class ForceFieldTrainer:
+    """One optimisation step per call on energies and forces: forward and
+    forces on the plain FP32 path, the loss and its derivatives w = dL/dE,
+    G = dL/dF (``ForceFieldLoss``), parameter gradients from the CUDA
+    reverse pass and its forward-mode derivative (``param_grads``),
+    gradient clipping and AdamW."""
+
+    def __init__(self, model, loss: Optional[ForceFieldLoss] = None, lr: float = 1e-3, weight_decay: float = 1e-5,
+                 betas=(0.9, 0.999), eps: float = 1e-8, grad_clip: float = 1.0):
+        self.model = model
+        self.loss_fn = loss if loss is not None else ForceFieldLoss()
+        self.opt = _adamw(model, lr, weight_decay, betas, eps)
+        self.grad_clip = grad_clip
+        self.steps = 0
+
+    def _predict(self, batch: Batch):
+        E, F, _ = self.model.engine().energy_forces(batch, _lib.PATH_PLAIN_FP32, forces=True)
+        return E, F
+
+    def step(self, batch: Batch, E_ref, F_ref) -> Dict[str, float]:
+        dev = batch.Z.device
+        E_ref = torch.as_tensor(E_ref, dtype=torch.float64, device=dev)
+        F_ref = torch.as_tensor(F_ref, dtype=torch.float64, device=dev)
+        E, F = self._predict(batch)
+        out, w, G = self.loss_fn.derivatives(E, F, E_ref, F_ref)
+        _, grads, _ = param_grads(self.model, batch, w, force_weights=G)
+        _apply(self.model, self.opt, grads, self.grad_clip)
+        self.steps += 1
+        return {k: float(v.item()) for k, v in out.items() if torch.is_tensor(v) and v.numel() == 1}
+
+    def evaluate(self, batch: Batch, E_ref, F_ref) -> Dict[str, float]:
+        dev = batch.Z.device
+        E, F = self._predict(batch)
+        out = self.loss_fn({"energy": E.to(torch.float64), "forces": F.to(torch.float64)},
+                           {"energy": torch.as_tensor(E_ref, dtype=torch.float64, device=dev),
+                            "forces": torch.as_tensor(F_ref, dtype=torch.float64, device=dev)})
+        return {k: float(v.item()) for k, v in out.items() if torch.is_tensor(v) and v.numel() == 1}
 
 
 class EnergyTrainer:
@@ -92,8 +273,7 @@ class EnergyTrainer:
     def __init__(self, model, lr: float = 1e-3, weight_decay: float = 1e-5, betas=(0.9, 0.999),
                  eps: float = 1e-8, grad_clip: float = 1.0, per_atom: bool = False):
         self.model = model
-        self.opt = torch.optim.AdamW([p for p in model.parameters() if p.requires_grad], lr=lr,
-                                     weight_decay=weight_decay, betas=betas, eps=eps)
+        self.opt = _adamw(model, lr, weight_decay, betas, eps)
         self.grad_clip = grad_clip
         self.per_atom = per_atom
         self.steps = 0
@@ -115,13 +295,7 @@ class EnergyTrainer:
         E0, _, _ = self.model.engine().energy_forces(batch, _lib.PATH_PLAIN_FP32, forces=False)
         loss, w = self.loss_weights(E0, E_ref, n_atoms)
         E, grads, _ = param_grads(self.model, batch, w)
-        for n, p in self.model.named_parameters():
-            if p.requires_grad:
-                p.grad = grads[n].to(p.dtype)
-        if self.grad_clip:
-            torch.nn.utils.clip_grad_norm_(self.model.parameters(), self.grad_clip)
-        self.opt.step()
-        self.opt.zero_grad(set_to_none=True)
+        _apply(self.model, self.opt, grads, self.grad_clip)
         self.steps += 1
         return float(loss.item())
 
@@ -135,4 +309,4 @@ class EnergyTrainer:
         return float(loss.item())
 
 
-__all__ = ["param_grads", "EnergyTrainer", "trainable_names", "make_batch"]
+__all__ = ["param_grads", "ForceFieldLoss", "ForceFieldTrainer", "EnergyTrainer", "trainable_names", "make_batch"]

@@ -135,11 +135,7 @@ def stress_voigt(dEde: np.ndarray, box: np.ndarray) -> np.ndarray:
     return np.array([s[0, 0], s[1, 1], s[2, 2], s[1, 2], s[0, 2], s[0, 1]])
 
 
-def param_grads(params, Z, pos, mol_ptr, weights, cutoff=5.0, box=None, pbc=None, dtype=torch.float64):
-    """sum_b w_b dE_b/dtheta for every tensor of the state_dict except the
-    RBF buffers, by autograd through `energy` (the parameter gradients
-    loss.backward() gives the reference's Trainer, training/trainer.py:
-    288-393, for an energy loss with dL/dE_b = w_b)."""
+def _train_setup(params, Z, pos, mol_ptr, cutoff, box, pbc, dtype):
     from . import nbr
     pos_np = np.asarray(pos)
     mol_ptr = np.asarray(mol_ptr, dtype=np.int64)
@@ -155,10 +151,43 @@ def param_grads(params, Z, pos, mol_ptr, weights, cutoff=5.0, box=None, pbc=None
     boxes = torch.zeros(n_mol, 3, dtype=dtype) if box is None else torch.as_tensor(
         np.asarray(box, dtype=np.float64).reshape(n_mol, 3), dtype=dtype)
     shift_t = torch.as_tensor(np.asarray(shift), dtype=dtype) * boxes[mol[dst_t]]
-    x = torch.as_tensor(pos_np, dtype=dtype)
-    E = energy(p, torch.as_tensor(np.asarray(Z), dtype=torch.long), x, src_t, dst_t, shift_t, mol, n_mol, cutoff)
-    w = torch.as_tensor(np.asarray(weights), dtype=dtype)
+    Zt = torch.as_tensor(np.asarray(Z), dtype=torch.long)
+
+    def energy_of(x):
+        return energy(p, Zt, x, src_t, dst_t, shift_t, mol, n_mol, cutoff)
+
+    return p, train, energy_of, torch.as_tensor(pos_np, dtype=dtype)
+
+
+def _grads_of(obj, p, train):
     # the last layer's mixing matrix only moves vector features the readout
     # never reads: its gradient is exactly zero
-    g = torch.autograd.grad((E * w).sum(), [p[k] for k in train], allow_unused=True)
-    return E.detach(), {k: (torch.zeros_like(p[k]) if gi is None else gi).detach() for k, gi in zip(train, g)}
+    g = torch.autograd.grad(obj, [p[k] for k in train], allow_unused=True)
+    return {k: (torch.zeros_like(p[k]) if gi is None else gi).detach() for k, gi in zip(train, g)}
+
+
+def param_grads(params, Z, pos, mol_ptr, weights, cutoff=5.0, box=None, pbc=None, dtype=torch.float64):
+    """sum_b w_b dE_b/dtheta for every tensor of the state_dict except the
+    RBF buffers, by autograd through `energy` (the parameter gradients
+    loss.backward() gives the reference's Trainer, training/trainer.py:
+    288-393, for an energy loss with dL/dE_b = w_b)."""
+    p, train, energy_of, x = _train_setup(params, Z, pos, mol_ptr, cutoff, box, pbc, dtype)
+    E = energy_of(x)
+    w = torch.as_tensor(np.asarray(weights), dtype=dtype)
+    return E.detach(), _grads_of((E * w).sum(), p, train)
+
+
+def param_grads_forces(params, Z, pos, mol_ptr, energy_weights, force_weights, cutoff=5.0, box=None, pbc=None,
+                       dtype=torch.float64):
+    """sum_b w_b dE_b/dtheta + sum_i G_i . dF_i/dtheta, F = -dE/dpos taken
+    with create_graph=True (predict_energy_and_forces, student_model.py:
+    759-795, in training mode) and differentiated again: the parameter
+    gradients loss.backward() gives the reference's Trainer for a loss with
+    dL/dE_b = w_b and dL/dF_i = G_i.  Returns (E, F, grads)."""
+    p, train, energy_of, x = _train_setup(params, Z, pos, mol_ptr, cutoff, box, pbc, dtype)
+    x = x.clone().requires_grad_(True)
+    E = energy_of(x)
+    F = -torch.autograd.grad(E.sum(), x, create_graph=True)[0]
+    w = torch.as_tensor(np.asarray(energy_weights), dtype=dtype)
+    G = torch.as_tensor(np.asarray(force_weights), dtype=dtype)
+    return E.detach(), F.detach(), _grads_of((E * w).sum() + (F * G).sum(), p, train)

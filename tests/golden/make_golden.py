@@ -18,6 +18,15 @@ seeded inputs in float32 (the reference's own dtype) and float64
                              float32 and float64, for seed and biased weights
 * golden_norm.npz         -- float32 vectors with |d| near 5 A and the
                              reference's torch.norm decision |d| <= 5
+* golden_train.npz        -- one training step's parameter gradients: the
+                             reference model (biased weights, float64) with
+                             forces taken with create_graph=True, the
+                             reference's ForceFieldLoss (training/losses.py,
+                             configs/train_student.yaml weights) and
+                             loss.backward(); per tensor the gradient's norm
+                             and its values at seeded sample indices
+
+``--train-only`` rewrites golden_train.npz alone.
 """
 from __future__ import annotations
 
@@ -50,6 +59,55 @@ def load_reference(ref_root: str):
     return mod
 
 
+def load_reference_losses(ref_root: str):
+    path = os.path.join(ref_root, "src", "mlff_distiller", "training", "losses.py")
+    spec = importlib.util.spec_from_file_location("mlff_distiller_training_losses", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+TRAIN_SAMPLES = 64   # sampled gradient entries per tensor
+
+
+def sample_indices(name: str, numel: int) -> np.ndarray:
+    """Seeded flat indices of the gradient entries recorded for one tensor."""
+    seed = sum(ord(c) * (i + 1) for i, c in enumerate(name))
+    k = min(TRAIN_SAMPLES, numel)
+    return np.sort(np.random.default_rng(seed).choice(numel, size=k, replace=False))
+
+
+def make_train_golden(sm, ref_root: str, sd, pert):
+    losses = load_reference_losses(ref_root)
+    model = sm.StudentForceField(use_torch_cluster=False)
+    model.load_state_dict({k: torch.tensor(sd[k] + pert[k]) if k in pert else torch.tensor(sd[k]) for k in sd})
+    model = model.double()
+    model.train()
+    sysm = systems.molecule_batch(3, 12, 30, seed=31)
+    batch = np.repeat(np.arange(sysm.n_mol), np.diff(sysm.mol_ptr))
+    pos32 = sysm.pos.astype(np.float32)
+    x = torch.tensor(pos32.astype(np.float64)).requires_grad_(True)
+    E = model(torch.tensor(sysm.Z, dtype=torch.long), x, batch=torch.tensor(batch, dtype=torch.long))
+    F = -torch.autograd.grad(E, x, grad_outputs=torch.ones_like(E), create_graph=True)[0]
+    g = np.random.default_rng(77)
+    E_ref = E.detach().numpy() + g.normal(0.0, 0.5, size=E.shape)
+    F_ref = F.detach().numpy() + g.normal(0.0, 0.3, size=F.shape)
+    loss_fn = losses.ForceFieldLoss(energy_weight=1.0, force_weight=100.0, stress_weight=0.1, angular_weight=10.0)
+    out = loss_fn({"energy": E, "forces": F}, {"energy": torch.tensor(E_ref), "forces": torch.tensor(F_ref)})
+    out["total"].backward()
+    rec = {"Z": sysm.Z, "pos": pos32, "mol_ptr": sysm.mol_ptr, "E_ref": E_ref, "F_ref": F_ref,
+           "E": E.detach().numpy(), "F": F.detach().numpy(), "loss": np.float64(out["total"].item()),
+           "loss_energy": np.float64(out["energy"].item()), "loss_force": np.float64(out["force"].item()),
+           "loss_angular": np.float64(out["angular"].item())}
+    for name, prm in model.named_parameters():
+        gr = torch.zeros_like(prm) if prm.grad is None else prm.grad
+        flat = gr.detach().reshape(-1).numpy()
+        rec[f"grad/{name}/norm"] = np.float64(np.linalg.norm(flat))
+        rec[f"grad/{name}/idx"] = sample_indices(name, flat.size)
+        rec[f"grad/{name}/val"] = flat[rec[f"grad/{name}/idx"]]
+    np.savez_compressed(os.path.join(HERE, "golden_train.npz"), **rec)
+
+
 def ref_eval(model, Z, pos, batch=None, dtype=torch.float32):
     m = model.to(dtype)
     x = torch.tensor(pos, dtype=dtype).requires_grad_(True)
@@ -60,8 +118,14 @@ def ref_eval(model, Z, pos, batch=None, dtype=torch.float32):
     return np.atleast_1d(E.detach().numpy()).astype(np.float64), F.detach().numpy().astype(np.float64)
 
 
-def main(ref_root: str):
+def main(ref_root: str, train_only: bool = False):
     sm = load_reference(ref_root)
+    if train_only:
+        sd = dict(np.load(os.path.join(HERE, "weights_seed0.npz")))
+        pert = dict(np.load(os.path.join(HERE, "bias_perturbation.npz")))
+        make_train_golden(sm, ref_root, sd, pert)
+        print("wrote golden_train.npz")
+        return
     torch.manual_seed(0)
     model = sm.StudentForceField(use_torch_cluster=False)
     model.eval()
@@ -125,8 +189,10 @@ def main(ref_root: str):
     dist = torch.norm(torch.tensor(vec), dim=1).numpy()
     np.savez_compressed(os.path.join(HERE, "golden_norm.npz"), vec=vec, dist=dist,
                         keep=(dist <= 5.0))
+    make_train_golden(sm, ref_root, sd, pert)
     print("wrote", sorted(os.listdir(HERE)))
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    main(args[0] if args else "/root/reference", train_only="--train-only" in sys.argv)

@@ -39,6 +39,10 @@ def test_size_queries_without_gpu():
     ws_plain = lib.mlff_workspace_size(ctypes.byref(d), 1000, 4, 64_000, _lib.PATH_PLAIN_FP32)
     ws_tuned = lib.mlff_workspace_size(ctypes.byref(d), 1000, 4, 64_000, _lib.PATH_TUNED_TC)
     assert ws_plain > ws_tuned > 0
+    ws_train = lib.mlff_workspace_size(ctypes.byref(d), 1000, 4, 64_000, _lib.PATH_TRAIN)
+    ws_force = lib.mlff_workspace_size(ctypes.byref(d), 1000, 4, 64_000, _lib.PATH_TRAIN_FORCES)
+    # the tangent pass keeps (value, tangent) pairs: about twice the training workspace
+    assert 1.8 * ws_train < ws_force < 2.1 * ws_train
 
 
 def test_unsupported_shape_is_reported():
@@ -101,3 +105,33 @@ def test_model_refuses_cpu_compute(weights_seed0):
     m = StudentForceField()
     with pytest.raises(RuntimeError, match="CUDA"):
         m(torch.tensor([1, 1]), torch.tensor([[0.0, 0, 0], [1.0, 0, 0]]))
+
+
+def test_force_loss_gradient_arguments_checked_on_host():
+    """mlff_param_grads_forces validates its arguments before any device
+    work: a NULL direction, a NULL workspace and a short workspace."""
+    import ctypes
+    from mlff_gb300 import _lib
+    from mlff_gb300.engine import dims_of
+    lib = _lib.load()
+    d = dims_of(128, 20, 3, 119, 5.0)
+    pos = (ctypes.c_float * 6)()
+    Z = (ctypes.c_int64 * 2)(1, 1)
+    ptr = (ctypes.c_int64 * 2)(0, 2)
+    s = _lib.System()
+    s.n_atoms, s.n_mol = 2, 1
+    s.pos = ctypes.cast(pos, ctypes.c_void_p).value
+    s.Z = ctypes.cast(Z, ctypes.c_void_p).value
+    s.mol_ptr = ctypes.cast(ptr, ctypes.c_void_p).value
+    g = _lib.Grads()
+    need = lib.mlff_workspace_size(ctypes.byref(d), 2, 1, 1024, _lib.PATH_TRAIN_FORCES)
+    fake = ctypes.c_void_p(256)   # never dereferenced: every call below fails on the host
+    r = lib.mlff_param_grads_forces(ctypes.byref(d), fake, ctypes.byref(s), 1024, None, ctypes.byref(g), fake,
+                                    need, None)
+    assert r == _lib.ERR_INVALID and b"force_weights" in lib.mlff_last_error_string()
+    r = lib.mlff_param_grads_forces(ctypes.byref(d), fake, ctypes.byref(s), 1024, fake, ctypes.byref(g), None,
+                                    need, None)
+    assert r == _lib.ERR_INVALID and b"workspace" in lib.mlff_last_error_string()
+    r = lib.mlff_param_grads_forces(ctypes.byref(d), fake, ctypes.byref(s), 1024, fake, ctypes.byref(g), fake,
+                                    need - 1, None)
+    assert r == _lib.ERR_WORKSPACE

@@ -1,8 +1,11 @@
 """Training path (GPU only): parameter gradients of sum_b w_b E_b from the
 CUDA reverse pass against float64 autograd through the oracle, determinism,
-and what training buys: the network fitted to a teacher's energies on
-training molecules predicts held-out molecules far better than the same
-network before training.
+the force-loss term (sum_i G_i . dF_i/dtheta, forward mode over the reverse
+pass) against float64 double backward through the oracle and against the
+reference's own recorded training step, and what training buys: the
+network fitted to a teacher's energies (and forces) on training molecules
+predicts held-out molecules far better than the same network before
+training.
 """
 import numpy as np
 import pytest
@@ -97,3 +100,107 @@ def test_training_gain_over_untrained(weights_seed0, weights_bias):
     assert losses[-1] < 0.1 * losses[0]
     assert after < 0.1 * before
     assert mse_inf < 0.1 * before
+
+
+def _compare_grads(grads, ref, tol):
+    worst = 0.0
+    for k, r in ref.items():
+        got = grads[k].double().cpu()
+        scale = max(float(r.abs().max()), 1e-6)
+        err = float((got - r).abs().max()) / scale
+        worst = max(worst, err)
+        assert err < tol, (k, err)
+    return worst
+
+
+@pytest.mark.parametrize("wname", ["seed", "bias"])
+def test_force_loss_grads_vs_oracle(weights_seed0, weights_bias, wname):
+    """sum_b w_b dE_b/dtheta + sum_i G_i . dF_i/dtheta from the library
+    (reverse pass + its forward-mode derivative along G, float32) against
+    float64 double backward through the oracle."""
+    from mlff_gb300 import systems
+    from mlff_gb300.training import param_grads
+    W = weights_seed0 if wname == "seed" else weights_bias
+    s = systems.molecule_batch(4, 10, 40, seed=13)
+    rng = np.random.default_rng(2)
+    w = rng.normal(size=s.n_mol)
+    G = (0.2 * rng.normal(size=(s.n_atoms, 3))).astype(np.float32)
+    m = _model(W)
+    E, grads, F = param_grads(m, _batch(s), torch.tensor(w), forces=True, force_weights=torch.tensor(G))
+    pos = s.pos.astype(np.float32).astype(np.float64)
+    E0, F0, g0 = painn.param_grads_forces(W, s.Z, pos, s.mol_ptr, w, G.astype(np.float64))
+    assert np.abs(E.cpu().numpy() - E0.numpy()).max() <= 2e-5 * s.n_atoms
+    # the float pass still returns -sum_b w_b dE_b/dpos
+    _, Fa = painn.energy_forces(W, s.Z, pos, s.mol_ptr)
+    Fw = Fa.numpy() * np.repeat(w, np.diff(s.mol_ptr))[:, None]
+    assert np.abs(F.cpu().numpy() - Fw).max() <= 1e-3 * max(1.0, np.abs(Fw).max())
+    assert set(grads) == set(g0)
+    worst = _compare_grads(grads, g0, 2e-4)
+    # the force term alone (w = 0) against the oracle
+    _, gf, _ = param_grads(m, _batch(s), torch.zeros(s.n_mol), force_weights=torch.tensor(G))
+    _, _, gf0 = painn.param_grads_forces(W, s.Z, pos, s.mol_ptr, np.zeros(s.n_mol), G.astype(np.float64))
+    worst_f = _compare_grads(gf, gf0, 2e-4)
+    print(f"worst relative max error: energy+force {worst:.2e}, force term {worst_f:.2e}")
+
+
+def test_force_loss_grads_vs_reference_training_step(weights_bias):
+    """The reference's own training step (golden_train.npz: its model in
+    float64, forces with create_graph=True, ForceFieldLoss with energy 1 /
+    force 100 / angular 10, loss.backward()) against the library's
+    gradients for the loss derivatives of the same predictions."""
+    import os
+    from conftest import GOLDEN
+    from mlff_gb300.engine import make_batch
+    from mlff_gb300.training import ForceFieldLoss, param_grads
+    g = np.load(os.path.join(GOLDEN, "golden_train.npz"))
+    loss = ForceFieldLoss(energy_weight=1.0, force_weight=100.0, stress_weight=0.1, angular_weight=10.0)
+    _, w, G = loss.derivatives(torch.tensor(g["E"]), torch.tensor(g["F"]), torch.tensor(g["E_ref"]),
+                               torch.tensor(g["F_ref"]))
+    m = _model(weights_bias)
+    _, grads, _ = param_grads(m, make_batch(g["Z"], g["pos"], g["mol_ptr"]), w, force_weights=G)
+    worst = 0.0
+    for k in grads:
+        got = grads[k].double().cpu().reshape(-1).numpy()
+        ref_norm = float(g[f"grad/{k}/norm"])
+        val = g[f"grad/{k}/val"]
+        scale = max(np.abs(val).max(), ref_norm / np.sqrt(got.size), 1e-9)
+        err = np.abs(got[g[f"grad/{k}/idx"]] - val).max() / scale
+        worst = max(worst, err)
+        assert err < 2e-4, (k, err)
+        assert abs(np.linalg.norm(got) - ref_norm) <= 2e-4 * ref_norm + 1e-9, k
+    print(f"worst relative error vs the reference's training step: {worst:.2e}")
+
+
+def test_force_training_gain(weights_seed0, weights_bias):
+    """Energy + force training (ForceFieldTrainer, the reference's loss
+    weights) on a teacher's float64 energies and forces: held-out force
+    RMSE and loss drop well below the untrained network's, and the trained
+    weights predict better forces on the tensor-core inference path too."""
+    from mlff_gb300 import systems
+    from mlff_gb300.training import ForceFieldLoss, ForceFieldTrainer
+    train = systems.molecule_batch(32, 10, 40, seed=41)
+    test = systems.molecule_batch(12, 10, 40, seed=42)
+
+    def teacher(s):
+        E, F = painn.energy_forces(weights_bias, s.Z, s.pos.astype(np.float32).astype(np.float64), s.mol_ptr)
+        return E.numpy(), F.numpy()
+
+    (Et, Ft), (Ev, Fv) = teacher(train), teacher(test)
+    m = _model(weights_seed0)
+    tr = ForceFieldTrainer(m, ForceFieldLoss(energy_weight=1.0, force_weight=100.0, angular_weight=0.0), lr=2e-3)
+    bt, bv = _batch(train), _batch(test)
+    before = tr.evaluate(bv, Ev, Fv)
+    hist = [tr.step(bt, Et, Ft) for _ in range(60)]
+    after = tr.evaluate(bv, Ev, Fv)
+    from mlff_gb300.student_model import StudentForceField
+    inf = StudentForceField(precision="fp16x3").to("cuda")
+    inf.load_state_dict(m.state_dict())
+    _, F_inf = inf.energy_and_forces(bv.Z, bv.pos, torch.repeat_interleave(
+        torch.arange(test.n_mol, device="cuda"), torch.as_tensor(np.diff(test.mol_ptr), device="cuda")))
+    rmse_inf = float(np.sqrt(np.mean((F_inf.cpu().numpy() - Fv) ** 2)))
+    print(f"held-out force RMSE: untrained {before['force_rmse']:.3e}, trained {after['force_rmse']:.3e} "
+          f"(fp16x3 {rmse_inf:.3e}); total loss {before['total']:.3e} -> {after['total']:.3e}; "
+          f"train loss {hist[0]['total']:.3e} -> {hist[-1]['total']:.3e}")
+    assert hist[-1]["total"] < 0.5 * hist[0]["total"]
+    assert after["force_rmse"] < 0.7 * before["force_rmse"]
+    assert rmse_inf < 0.7 * before["force_rmse"]

@@ -1,9 +1,11 @@
 """The oracle (CPU restatement) against golden vectors written by the
 reference implementation itself (tests/golden/make_golden.py)."""
+import os
+
 import numpy as np
 import pytest
 
-from conftest import case_names
+from conftest import GOLDEN, case_names
 from oracle import nbr, painn
 
 CASES = ["batch6", "cutoff_edge", "methane", "molecule60", "water"]
@@ -143,3 +145,35 @@ def test_oracle_param_grads_match_finite_differences(weights_bias):
                 vals.append(float(E[0]) * w[0])
             fd = (vals[0] - vals[1]) / (2 * h)
             assert abs(fd - float(g[key][idx])) <= 1e-6 + 1e-5 * abs(fd), (key, idx, fd, float(g[key][idx]))
+
+
+def test_force_loss_grads_match_reference_training_step(weights_bias):
+    """One training step of the reference (its model in float64, forces
+    with create_graph=True, its ForceFieldLoss with the train_student.yaml
+    weights, loss.backward()) recorded in golden_train.npz, against the
+    restated loss (mlff_gb300.training.ForceFieldLoss: values and the
+    derivatives dL/dE, dL/dF) and the oracle's second-order parameter
+    gradients for those derivatives."""
+    import torch
+    from mlff_gb300.training import ForceFieldLoss
+    g = np.load(os.path.join(GOLDEN, "golden_train.npz"))
+    E, F = torch.tensor(g["E"]), torch.tensor(g["F"])
+    loss = ForceFieldLoss(energy_weight=1.0, force_weight=100.0, stress_weight=0.1, angular_weight=10.0)
+    out, w, G = loss.derivatives(E, F, torch.tensor(g["E_ref"]), torch.tensor(g["F_ref"]))
+    for key in ["loss", "loss_energy", "loss_force", "loss_angular"]:
+        name = "total" if key == "loss" else key.split("_", 1)[1]
+        assert abs(float(out[name].detach()) - float(g[key])) <= 1e-12 * max(1.0, abs(float(g[key]))), key
+    E0, F0, grads = painn.param_grads_forces(weights_bias, g["Z"], g["pos"].astype(np.float64), g["mol_ptr"],
+                                             w.numpy(), G.double().numpy())
+    assert np.abs(E0.numpy() - g["E"]).max() < 1e-10
+    assert np.abs(F0.numpy() - g["F"]).max() < 1e-10
+    names = sorted(k.split("/")[1] for k in g.files if k.startswith("grad/") and k.endswith("/norm"))
+    assert set(names) == set(grads), set(names) ^ set(grads)
+    for k in names:
+        ref_norm = float(g[f"grad/{k}/norm"])
+        got = grads[k].reshape(-1).numpy()
+        # G is rounded to float32 (the library's input type): relative 1e-6
+        assert abs(np.linalg.norm(got) - ref_norm) <= 1e-6 * ref_norm + 1e-12, k
+        val = g[f"grad/{k}/val"]
+        err = np.abs(got[g[f"grad/{k}/idx"]] - val).max()
+        assert err <= 1e-6 * max(np.abs(val).max(), ref_norm / np.sqrt(got.size)) + 1e-12, (k, err)
