@@ -83,7 +83,7 @@ WsLayout ws_layout(const mlff_dims& d, int32_t n_atoms, int32_t n_mol, int64_t c
     L.mol_grid = take(sizeof(int4) * B);
     L.cell_count = take(4 * (L.ncell_cap + 1));
     L.cell_fill = take(4 * L.ncell_cap);
-    L.cell_atoms = take(4 * N);
+    L.cell_pos = take(sizeof(float4) * N);
     L.atom_cell = take(4 * N);
     L.part = take(4 * (L.P + 1));
     L.X = take(fs * (Ly + 1) * N * 4 * H);

@@ -10,9 +10,13 @@
 //
 // Open structures: every atom pair of the structure is tested (one warp per
 // row, warp-ballot compaction keeps the ascending order).  Periodic boxes:
-// atoms are binned into cells of edge >= cutoff, each row gathers
-// candidates from the 27 (or fewer, for small grids) neighbouring cells,
-// compacts hits with a warp ballot into shared memory and rank-sorts them.
+// atoms are binned into cells of edge >= cutoff and copied in cell order
+// (position and atom index in one float4, so a cell's candidates are
+// contiguous); a row's warp looks up its 27 (or fewer, for small grids)
+// neighbouring cells in one step -- one cell per lane, a warp scan of their
+// sizes -- and walks the concatenated candidates 32 at a time, each lane
+// finding its cell by a binary search over the scan; hits are compacted
+// with a warp ballot into shared memory and rank-sorted.
 #include "common.cuh"
 #include "workspace.h"
 #include "profile.h"
@@ -114,6 +118,57 @@ __global__ void scan_add_kernel(int32_t* __restrict__ data, int64_t n, const int
     }
 }
 
+// One block for small inputs: exclusive scan of data[0..n_in), data[n_in] =
+// total.  Each of the 1024 threads owns a contiguous run of ceil(n_in/1024)
+// values (read twice: once to sum, once to write).  With st non-NULL the
+// total is the edge count: it is recorded in the status word and checked
+// against the edge capacity.
+constexpr int64_t SCAN1_MAX = 8192;
+__global__ void __launch_bounds__(1024) scan_single_kernel(int32_t* __restrict__ data, int64_t n_in,
+                                                           Status* st, int64_t cap) {
+    pdl_wait();
+    pdl_trigger();
+    __shared__ int32_t warp_tot[32];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const int64_t per = (n_in + 1023) / 1024;
+    const int64_t b0 = min((int64_t)t * per, n_in), b1 = min(b0 + per, n_in);
+    int32_t s = 0;
+    for (int64_t k = b0; k < b1; ++k) s += data[k];
+    int32_t x = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int32_t wt = warp_tot[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int32_t y = __shfl_up_sync(0xffffffffu, wt, o);
+            if (lane >= o) wt += y;
+        }
+        warp_tot[lane] = wt;
+    }
+    __syncthreads();
+    int32_t run = x - s + (w > 0 ? warp_tot[w - 1] : 0);
+    for (int64_t k = b0; k < b1; ++k) {
+        const int32_t v = data[k];
+        data[k] = run;
+        run += v;
+    }
+    if (t == 1023) {
+        data[n_in] = run;
+        if (st) {
+            const int64_t e = (int64_t)(uint32_t)run;
+            st->n_edges = (int32_t)(e & 0x7fffffff);
+            st->n_edges_hi = (int32_t)(e >> 31);
+            if (e > cap) set_status(st, MLFF_ERR_CAPACITY, -1);
+        }
+    }
+}
+
 // In-place exclusive scan of n int32 values; tmp holds ceil(n/1024)+1 ints.
 int launch_scan(int32_t* data, int64_t n, int32_t* tmp, cudaStream_t st) {
     if (n <= 0) return MLFF_OK;
@@ -146,14 +201,20 @@ __global__ void prep_atoms_kernel(const float* __restrict__ pos, const int64_t* 
 
 // One block: per periodic structure choose the cell grid (cells of edge
 // >= cutoff, at most max(n_atoms, 27) cells) and the first cell index.
+// It also zeroes the cell counters (ncell_cap + 1) and fill cursors.
 __global__ void mol_grid_kernel(const int64_t* __restrict__ mol_ptr, const float* __restrict__ box,
                                 const uint8_t* __restrict__ pbc, int32_t n_mol, float cutoff,
-                                int4* __restrict__ grid, Status* st) {
+                                int4* __restrict__ grid, int32_t* __restrict__ cell_count,
+                                int32_t* __restrict__ cell_fill, int64_t ncell_cap, Status* st) {
     pdl_wait();
     pdl_trigger();
     __shared__ int32_t warp_tot[32];
     __shared__ int32_t carry;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    for (int64_t k = t; k <= ncell_cap; k += blockDim.x) {
+        cell_count[k] = 0;
+        if (k < ncell_cap) cell_fill[k] = 0;
+    }
     if (t == 0) carry = 0;
     __syncthreads();
     for (int c0 = 0; c0 < n_mol; c0 += 1024) {
@@ -247,15 +308,16 @@ __global__ void cell_count_kernel(const float4* __restrict__ pos4, const int32_t
 }
 
 __global__ void cell_fill_kernel(const int32_t* __restrict__ atom_cell, const int32_t* __restrict__ cell_start,
-                                 int32_t n_atoms, int32_t* __restrict__ cell_fill,
-                                 int32_t* __restrict__ cell_atoms) {
+                                 const float4* __restrict__ pos4, int32_t n_atoms, int32_t* __restrict__ cell_fill,
+                                 float4* __restrict__ cell_pos) {
     pdl_wait();
     pdl_trigger();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_atoms; i += gridDim.x * blockDim.x) {
         int c = atom_cell[i];
         if (c < 0) continue;
         int slot = atomicAdd(&cell_fill[c], 1);
-        cell_atoms[cell_start[c] + slot] = i;
+        const float4 p = pos4[i];
+        cell_pos[cell_start[c] + slot] = make_float4(p.x, p.y, p.z, __int_as_float(i));
     }
 }
 
@@ -268,7 +330,7 @@ struct NbrArgs {
     const uint8_t* pbc;
     const int4* grid;
     const int32_t* cell_start;
-    const int32_t* cell_atoms;
+    const float4* cell_pos;
     const int32_t* atom_cell;
     int32_t n_atoms;
     float cutoff;
@@ -285,6 +347,8 @@ __global__ void __launch_bounds__(NBR_WARPS * 32) nbr_rows_kernel(NbrArgs a) {
     pdl_trigger();
     __shared__ int32_t sbuf[FILL ? NBR_WARPS : 1][FILL ? ROW_CAP : 1];
     if (FILL && a.st->code != 0) return;
+    // the count pass zeroes the entry after the last row: the scan's total lands there
+    if (!FILL && blockIdx.x == 0 && threadIdx.x == 0) a.counts[a.n_atoms] = 0;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int nwarps = gridDim.x * NBR_WARPS;
     const unsigned lt_mask = (1u << lane) - 1u;
@@ -317,41 +381,64 @@ __global__ void __launch_bounds__(NBR_WARPS * 32) nbr_rows_kernel(NbrArgs a) {
             const int ci = a.atom_cell[i] - g.w;
             const int cc[3] = {ci / (g.y * g.z), (ci / g.z) % g.y, ci % g.z};
             const int ncs[3] = {g.x, g.y, g.z};
-            int lo[3], hi[3];
-#pragma unroll
-            for (int ax = 0; ax < 3; ++ax) {
-                if (ncs[ax] >= 3) { lo[ax] = -1; hi[ax] = 1; }
-                else { lo[ax] = 0; hi[ax] = ncs[ax] - 1; }
-            }
             bool overflow = false;
-            for (int ox = lo[0]; ox <= hi[0]; ++ox)
-            for (int oy = lo[1]; oy <= hi[1]; ++oy)
-            for (int oz = lo[2]; oz <= hi[2]; ++oz) {
+            // lane k < 27 looks up neighbour cell (k / 9, k / 3 % 3, k % 3) - 1 (wrapped); on an
+            // axis with fewer than 3 cells the offsets 0 .. nc-1 name its cells directly
+            int c0 = 0, len = 0;
+            if (lane < 27) {
+                const int o[3] = {lane / 9, (lane / 3) % 3, lane % 3};
+                bool keep = true;
                 int q[3];
-                const int o[3] = {ox, oy, oz};
 #pragma unroll
-                for (int ax = 0; ax < 3; ++ax)
-                    q[ax] = ncs[ax] >= 3 ? ((cc[ax] + o[ax]) % ncs[ax] + ncs[ax]) % ncs[ax] : o[ax];
-                const int qc = g.w + (q[0] * g.y + q[1]) * g.z + q[2];
-                const int t0 = a.cell_start[qc], t1 = a.cell_start[qc + 1];
-                for (int t = t0; t < t1; t += 32) {
-                    bool ok = false;
-                    int j = -1;
-                    if (t + lane < t1) {
-                        j = a.cell_atoms[t + lane];
-                        if (j != i) {
-                            float4 pj = a.pos4[j];
-                            float3 r = edge_vector(pj, pi, b);
-                            ok = pair_distance(r.x, r.y, r.z) <= a.cutoff;
-                        }
+                for (int ax = 0; ax < 3; ++ax) {
+                    if (ncs[ax] >= 3) {
+                        q[ax] = (cc[ax] + o[ax] - 1 + ncs[ax]) % ncs[ax];
+                    } else {
+                        keep = keep && o[ax] < ncs[ax];
+                        q[ax] = o[ax];
                     }
-                    const unsigned mask = __ballot_sync(0xffffffffu, ok);
-                    if (FILL) {
-                        const int slot = cnt + __popc(mask & lt_mask);
-                        if (ok && slot < ROW_CAP) sbuf[wib][slot] = j;
-                    }
-                    cnt += __popc(mask);
                 }
+                if (keep) {
+                    const int qc = g.w + (q[0] * g.y + q[1]) * g.z + q[2];
+                    c0 = a.cell_start[qc];
+                    len = a.cell_start[qc + 1] - c0;
+                }
+            }
+            int incl = len;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            const int excl = incl - len;
+            for (int t = 0; t < total; t += 32) {
+                const int c = t + lane;
+                // cell of candidate c: the number of lanes whose cells end at or before c
+                int k = 0;
+#pragma unroll
+                for (int bit = 16; bit > 0; bit >>= 1) {
+                    const int v = __shfl_sync(0xffffffffu, incl, k + bit - 1);
+                    if (v <= c) k += bit;
+                }
+                const int kb = __shfl_sync(0xffffffffu, c0, k);
+                const int ke = __shfl_sync(0xffffffffu, excl, k);
+                bool ok = false;
+                int j = -1;
+                if (c < total) {
+                    const float4 pj = a.cell_pos[kb + c - ke];
+                    j = __float_as_int(pj.w);
+                    if (j != i) {
+                        float3 r = edge_vector(pj, pi, b);
+                        ok = pair_distance(r.x, r.y, r.z) <= a.cutoff;
+                    }
+                }
+                const unsigned mask = __ballot_sync(0xffffffffu, ok);
+                if (FILL) {
+                    const int slot = cnt + __popc(mask & lt_mask);
+                    if (ok && slot < ROW_CAP) sbuf[wib][slot] = j;
+                }
+                cnt += __popc(mask);
             }
             if (cnt > ROW_CAP) overflow = true;
             if (FILL) {
@@ -436,86 +523,75 @@ int launch_partition(const WsLayout& L, void* ws, cudaStream_t st) {
     return MLFF_OK;
 }
 
-int launch_neighbors(const mlff_dims& d, const mlff_system& sys, const WsLayout& L, void* ws,
-                     cudaStream_t st) {
-    ProfScope prof(PK_NEIGHBORS, st);
-    const int N = sys.n_atoms;
-    Status* status = ws_ptr<Status>(ws, L.status);
-    float4* pos4 = ws_ptr<float4>(ws, L.pos4);
-    int32_t* atom_mol = ws_ptr<int32_t>(ws, L.atom_mol);
-    int32_t* row_ptr = ws_ptr<int32_t>(ws, L.row_ptr);
-    int32_t* scan_tmp = ws_ptr<int32_t>(ws, L.scan_tmp);
-    const bool any_pbc = sys.pbc != nullptr && sys.box != nullptr;
-    const int tb = 256;
-    const int gb = (int)std::min<int64_t>((N + tb - 1) / tb, 152 * 16);
-    MLFF_LAUNCH_PDL("prep_atoms", prep_atoms_kernel, std::max(gb, 1), tb, 0, st, sys.pos, sys.mol_ptr, sys.n_mol, N, pos4, atom_mol);
-    int4* grid = ws_ptr<int4>(ws, L.mol_grid);
-    int32_t* cell_count = ws_ptr<int32_t>(ws, L.cell_count);
-    int32_t* cell_fill = ws_ptr<int32_t>(ws, L.cell_fill);
-    int32_t* cell_atoms = ws_ptr<int32_t>(ws, L.cell_atoms);
-    int32_t* atom_cell = ws_ptr<int32_t>(ws, L.atom_cell);
-    if (any_pbc) {
-        MLFF_LAUNCH_PDL("mol_grid", mol_grid_kernel, 1, 1024, 0, st, sys.mol_ptr, sys.box, sys.pbc, sys.n_mol, d.cutoff, grid, status);
-        MLFF_CUDA(cudaMemsetAsync(cell_count, 0, sizeof(int32_t) * (L.ncell_cap + 1), st));
-        MLFF_CUDA(cudaMemsetAsync(cell_fill, 0, sizeof(int32_t) * L.ncell_cap, st));
-        MLFF_LAUNCH_PDL("cell_count", cell_count_kernel, std::max(gb, 1), tb, 0, st, pos4, atom_mol, sys.box, sys.pbc, grid, N,
-                                                          atom_cell, cell_count);
-        int r = launch_scan(cell_count, L.ncell_cap + 1, scan_tmp, st);
-        if (r) return r;
-        MLFF_LAUNCH_PDL("cell_fill", cell_fill_kernel, std::max(gb, 1), tb, 0, st, atom_cell, cell_count, N, cell_fill, cell_atoms);
+// Exclusive scan of data[0..n_in) with the total written to data[n_in]
+// (which must hold 0 for the multi-block form); with st the total is the
+// edge count, recorded and checked against cap.
+static int scan_with_total(int32_t* data, int64_t n_in, int32_t* tmp, Status* st, int64_t cap, cudaStream_t s) {
+    if (n_in + 1 <= SCAN1_MAX) {
+        MLFF_LAUNCH_PDL("scan_single", scan_single_kernel, 1, 1024, 0, s, data, n_in, st, cap);
+        return MLFF_OK;
     }
-    NbrArgs a;
-    a.pos4 = pos4; a.atom_mol = atom_mol; a.mol_ptr = sys.mol_ptr; a.box = sys.box; a.pbc = sys.pbc;
-    a.grid = grid; a.cell_start = cell_count; a.cell_atoms = cell_atoms; a.atom_cell = atom_cell;
-    a.n_atoms = N; a.cutoff = d.cutoff; a.cap = L.cap; a.counts = row_ptr;
-    a.col = ws_ptr<int32_t>(ws, L.col); a.erecv = ws_ptr<int32_t>(ws, L.erecv); a.st = status;
-    const int rows_blocks = (int)std::max<int64_t>(1, std::min<int64_t>((N + NBR_WARPS - 1) / NBR_WARPS, 152 * 32));
-    MLFF_CUDA(cudaMemsetAsync(row_ptr + N, 0, sizeof(int32_t), st));
-    MLFF_LAUNCH_PDL("nbr_count", nbr_rows_kernel<false>, rows_blocks, NBR_WARPS * 32, 0, st, a);
-    int r = launch_scan(row_ptr, (int64_t)N + 1, scan_tmp, st);
+    int r = launch_scan(data, n_in + 1, tmp, s);
     if (r) return r;
-    MLFF_LAUNCH_PDL("check_edges", check_edges_kernel, 1, 1, 0, st, row_ptr, N, L.cap, nullptr, status);
-    MLFF_LAUNCH_PDL("nbr_fill", nbr_rows_kernel<true>, rows_blocks, NBR_WARPS * 32, 0, st, a);
-    const int eb = (int)std::min<int64_t>((L.cap + 255) / 256, 152 * 16);
-    MLFF_LAUNCH_PDL("rev", rev_kernel, std::max(eb, 1), 256, 0, st, row_ptr, a.col, a.erecv, N, ws_ptr<int32_t>(ws, L.rev), status);
+    if (st) MLFF_LAUNCH_PDL("check_edges", check_edges_kernel, 1, 1, 0, s, data, (int32_t)n_in, cap, nullptr, st);
     return MLFF_OK;
 }
 
-}  // namespace mlff
-
-namespace mlff {
-
-// Same launch sequence as launch_neighbors (without the reversed-edge map
-// and the partition), on explicitly given buffers.  Used by the
-// allocation-free entry point in noalloc.cu.
+// Radius graph into explicit buffers: atom copies, cell lists (periodic
+// structures), row counts, their scan (row_ptr) and the rank-sorted rows.
 int launch_neighbors_into(const mlff_dims& d, const mlff_system& sys, const NbrBuffers& b, cudaStream_t st) {
     const int N = sys.n_atoms;
     const bool any_pbc = sys.pbc != nullptr && sys.box != nullptr;
     const int tb = 256;
     const int gb = (int)std::max<int64_t>(1, std::min<int64_t>((N + tb - 1) / tb, 152 * 16));
-    MLFF_LAUNCH_PDL("prep_atoms", prep_atoms_kernel, gb, tb, 0, st, sys.pos, sys.mol_ptr, sys.n_mol, N, b.pos4, b.atom_mol);
+    MLFF_LAUNCH_PDL("prep_atoms", prep_atoms_kernel, gb, tb, 0, st, sys.pos, sys.mol_ptr, sys.n_mol, N, b.pos4,
+                    b.atom_mol);
     if (any_pbc) {
-        MLFF_LAUNCH_PDL("mol_grid", mol_grid_kernel, 1, 1024, 0, st, sys.mol_ptr, sys.box, sys.pbc, sys.n_mol, d.cutoff, b.mol_grid, b.status);
-        MLFF_CUDA(cudaMemsetAsync(b.cell_count, 0, sizeof(int32_t) * (b.ncell_cap + 1), st));
-        MLFF_CUDA(cudaMemsetAsync(b.cell_fill, 0, sizeof(int32_t) * b.ncell_cap, st));
-        MLFF_LAUNCH_PDL("cell_count", cell_count_kernel, gb, tb, 0, st, b.pos4, b.atom_mol, sys.box, sys.pbc, b.mol_grid, N, b.atom_cell,
-                                             b.cell_count);
-        int r = launch_scan(b.cell_count, b.ncell_cap + 1, b.scan_tmp, st);
+        MLFF_LAUNCH_PDL("mol_grid", mol_grid_kernel, 1, 1024, 0, st, sys.mol_ptr, sys.box, sys.pbc, sys.n_mol, d.cutoff,
+                        b.mol_grid, b.cell_count, b.cell_fill, b.ncell_cap, b.status);
+        MLFF_LAUNCH_PDL("cell_count", cell_count_kernel, gb, tb, 0, st, b.pos4, b.atom_mol, sys.box, sys.pbc, b.mol_grid,
+                        N, b.atom_cell, b.cell_count);
+        int r = scan_with_total(b.cell_count, b.ncell_cap, b.scan_tmp, nullptr, 0, st);
         if (r) return r;
-        MLFF_LAUNCH_PDL("cell_fill", cell_fill_kernel, gb, tb, 0, st, b.atom_cell, b.cell_count, N, b.cell_fill, b.cell_atoms);
+        MLFF_LAUNCH_PDL("cell_fill", cell_fill_kernel, gb, tb, 0, st, b.atom_cell, b.cell_count, b.pos4, N, b.cell_fill,
+                        b.cell_pos);
     }
     NbrArgs a;
     a.pos4 = b.pos4; a.atom_mol = b.atom_mol; a.mol_ptr = sys.mol_ptr; a.box = sys.box; a.pbc = sys.pbc;
-    a.grid = b.mol_grid; a.cell_start = b.cell_count; a.cell_atoms = b.cell_atoms; a.atom_cell = b.atom_cell;
+    a.grid = b.mol_grid; a.cell_start = b.cell_count; a.cell_pos = b.cell_pos; a.atom_cell = b.atom_cell;
     a.n_atoms = N; a.cutoff = d.cutoff; a.cap = b.cap; a.counts = b.row_ptr;
     a.col = b.col; a.erecv = b.erecv; a.st = b.status;
     const int rows_blocks = (int)std::max<int64_t>(1, std::min<int64_t>((N + NBR_WARPS - 1) / NBR_WARPS, 152 * 32));
-    MLFF_CUDA(cudaMemsetAsync(b.row_ptr + N, 0, sizeof(int32_t), st));
     MLFF_LAUNCH_PDL("nbr_count", nbr_rows_kernel<false>, rows_blocks, NBR_WARPS * 32, 0, st, a);
-    int r = launch_scan(b.row_ptr, (int64_t)N + 1, b.scan_tmp, st);
+    int r = scan_with_total(b.row_ptr, N, b.scan_tmp, b.status, b.cap, st);
     if (r) return r;
-    MLFF_LAUNCH_PDL("check_edges", check_edges_kernel, 1, 1, 0, st, b.row_ptr, N, b.cap, nullptr, b.status);
     MLFF_LAUNCH_PDL("nbr_fill", nbr_rows_kernel<true>, rows_blocks, NBR_WARPS * 32, 0, st, a);
+    return MLFF_OK;
+}
+
+int launch_neighbors(const mlff_dims& d, const mlff_system& sys, const WsLayout& L, void* ws,
+                     cudaStream_t st) {
+    ProfScope prof(PK_NEIGHBORS, st);
+    NbrBuffers b;
+    b.status = ws_ptr<Status>(ws, L.status);
+    b.pos4 = ws_ptr<float4>(ws, L.pos4);
+    b.atom_mol = ws_ptr<int32_t>(ws, L.atom_mol);
+    b.row_ptr = ws_ptr<int32_t>(ws, L.row_ptr);
+    b.col = ws_ptr<int32_t>(ws, L.col);
+    b.erecv = ws_ptr<int32_t>(ws, L.erecv);
+    b.scan_tmp = ws_ptr<int32_t>(ws, L.scan_tmp);
+    b.mol_grid = ws_ptr<int4>(ws, L.mol_grid);
+    b.cell_count = ws_ptr<int32_t>(ws, L.cell_count);
+    b.cell_fill = ws_ptr<int32_t>(ws, L.cell_fill);
+    b.cell_pos = ws_ptr<float4>(ws, L.cell_pos);
+    b.atom_cell = ws_ptr<int32_t>(ws, L.atom_cell);
+    b.ncell_cap = L.ncell_cap;
+    b.cap = L.cap;
+    int r = launch_neighbors_into(d, sys, b, st);
+    if (r) return r;
+    const int eb = (int)std::min<int64_t>((L.cap + 255) / 256, 152 * 16);
+    MLFF_LAUNCH_PDL("rev", rev_kernel, std::max(eb, 1), 256, 0, st, b.row_ptr, b.col, b.erecv, sys.n_atoms,
+                    ws_ptr<int32_t>(ws, L.rev), b.status);
     return MLFF_OK;
 }
 

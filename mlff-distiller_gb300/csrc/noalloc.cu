@@ -10,7 +10,7 @@
 //
 // Limits: at most NOALLOC_MAX_ATOMS atoms, NOALLOC_MAX_MOLS structures and
 // NOALLOC_MAX_EDGES directed edges per call; larger inputs are rejected.
-// The array is about 5.6 MB and stays resident on every device that has
+// The array is about 5.8 MB and stays resident on every device that has
 // loaded the library until the process exits.
 //
 // Every call shares the array and it keeps the last call's contents: the
@@ -41,8 +41,8 @@ constexpr int64_t kOffScan = align256(kOffErecv + 4 * NOALLOC_MAX_EDGES);
 constexpr int64_t kOffGrid = align256(kOffScan + 4 * ((kScanN + 1023) / 1024 + 2));
 constexpr int64_t kOffCellCount = align256(kOffGrid + 16 * NOALLOC_MAX_MOLS);
 constexpr int64_t kOffCellFill = align256(kOffCellCount + 4 * (kNcellCap + 1));
-constexpr int64_t kOffCellAtoms = align256(kOffCellFill + 4 * kNcellCap);
-constexpr int64_t kOffAtomCell = align256(kOffCellAtoms + 4 * NOALLOC_MAX_ATOMS);
+constexpr int64_t kOffCellPos = align256(kOffCellFill + 4 * kNcellCap);
+constexpr int64_t kOffAtomCell = align256(kOffCellPos + 16 * NOALLOC_MAX_ATOMS);
 constexpr int64_t kScratchBytes = align256(kOffAtomCell + 4 * NOALLOC_MAX_ATOMS);
 static_assert(kScratchBytes < 6 * 1024 * 1024, "static scratch must stay modest");
 }  // namespace
@@ -125,7 +125,7 @@ extern "C" int mlff_radius_graph_noalloc(const mlff_system* sys, float cutoff, i
     b.mol_grid = reinterpret_cast<int4*>(s + kOffGrid);
     b.cell_count = reinterpret_cast<int32_t*>(s + kOffCellCount);
     b.cell_fill = reinterpret_cast<int32_t*>(s + kOffCellFill);
-    b.cell_atoms = reinterpret_cast<int32_t*>(s + kOffCellAtoms);
+    b.cell_pos = reinterpret_cast<float4*>(s + kOffCellPos);
     b.atom_cell = reinterpret_cast<int32_t*>(s + kOffAtomCell);
     b.ncell_cap = (int64_t)sys->n_atoms + 27LL * sys->n_mol;
     b.cap = edge_capacity;

@@ -26,7 +26,7 @@ struct WsLayout {
     size_t mol_grid;           // int4 [B]  (ncx, ncy, ncz, first cell)
     size_t cell_count;         // int32 [ncell_cap + 1]
     size_t cell_fill;          // int32 [ncell_cap]
-    size_t cell_atoms;         // int32 [N]
+    size_t cell_pos;           // float4 [N]  atoms in cell order: x, y, z, atom index (int bits)
     size_t atom_cell;          // int32 [N]
     size_t part;               // int32 [P + 1] receiver partition
     size_t X;                  // float [L+1][N][4][H]  layer inputs (s, v_x, v_y, v_z)
@@ -83,7 +83,7 @@ struct NbrBuffers {
     int4* mol_grid;         // [B]
     int32_t* cell_count;    // [ncell_cap + 1]
     int32_t* cell_fill;     // [ncell_cap]
-    int32_t* cell_atoms;    // [N]
+    float4* cell_pos;       // [N] atoms in cell order (x, y, z, index bits)
     int32_t* atom_cell;     // [N]
     int64_t ncell_cap;      // N + 27 B
     int64_t cap;            // edge capacity

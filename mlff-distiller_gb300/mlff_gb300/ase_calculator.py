@@ -120,10 +120,26 @@ class StudentForceFieldCalculator(Calculator):
                 warnings.warn(f"Cell volume very small ({volume:.2e} A^3), may indicate degenerate cell",
                               stacklevel=3)
 
-    def _tensors(self, positions, numbers, cell, pbc):
+    def _host_inputs(self, numbers, positions):
+        """Atomic numbers and positions in pinned host buffers reused from
+        call to call (the model copies them straight into its CUDA graph's
+        input buffers)."""
+        n = len(numbers)
+        buf = getattr(self, "_pinned", None)
+        if buf is None or buf[0].shape[0] != n:
+            buf = (torch.empty(n, dtype=torch.int64).pin_memory(), torch.empty(n, 3, dtype=torch.float32).pin_memory())
+            self._pinned = buf
+        buf[0].numpy()[:] = np.asarray(numbers, dtype=np.int64)
+        buf[1].numpy()[:] = np.asarray(positions)
+        return buf
+
+    def _tensors(self, positions, numbers, cell, pbc, host: bool = False):
         dev = self.device
-        z = torch.as_tensor(np.asarray(numbers, dtype=np.int64), device=dev)
-        x = torch.as_tensor(np.asarray(positions, dtype=np.float32), device=dev)
+        if host and dev.type == "cuda":
+            z, x = self._host_inputs(numbers, positions)
+        else:
+            z = torch.as_tensor(np.asarray(numbers, dtype=np.int64), device=dev)
+            x = torch.as_tensor(np.asarray(positions, dtype=np.float32), device=dev)
         periodic = bool(np.asarray(pbc).any())
         # cell and pbc stay on the host: the model checks them there without a device sync
         c = torch.as_tensor(np.asarray(cell, dtype=np.float32).reshape(3, 3)) if periodic else None
@@ -142,8 +158,9 @@ class StudentForceFieldCalculator(Calculator):
             cell = np.asarray(atoms.get_cell())
             pbc = np.asarray(atoms.get_pbc())
             self._validate_inputs(positions, numbers, cell, pbc)
-            z, x, c, p = self._tensors(positions, numbers, cell, pbc)
             want_stress = "stress" in properties and self.enable_stress
+            # energy + forces: host buffers in, host results out (one synchronisation)
+            z, x, c, p = self._tensors(positions, numbers, cell, pbc, host=not want_stress)
             E, F, V = self.model.energy_forces_virial(z, x, c, p) if want_stress else \
                 (*self.model.energy_and_forces(z, x, None, c, p), None)
             results: Dict[str, Any] = {"energy": float(E.sum().item()),
@@ -198,9 +215,9 @@ class StudentForceFieldCalculator(Calculator):
             periodic = [bool(b.any()) for b in pbcs]
             if any(periodic) and not all(periodic):
                 raise ValueError("calculate_batch needs all structures periodic or all non-periodic")
-            dev = self.device
-            z = torch.as_tensor(np.concatenate(num).astype(np.int64), device=dev)
-            x = torch.as_tensor(np.concatenate(pos).astype(np.float32), device=dev)
+            z, x = self._host_inputs(np.concatenate(num), np.concatenate(pos)) if self.device.type == "cuda" else \
+                (torch.as_tensor(np.concatenate(num).astype(np.int64)),
+                 torch.as_tensor(np.concatenate(pos).astype(np.float32)))
             # structure index, cells and pbc flags on the host (checked there, no device sync)
             bidx = torch.as_tensor(np.repeat(np.arange(len(atoms_list), dtype=np.int64), counts))
             c = p = None

@@ -8,6 +8,12 @@ re-runs the call.  Calls whose shape repeats (same atom and structure
 counts, path and outputs) replay a cached CUDA graph of the whole step: the
 inputs are copied into the graph's own buffers, one graph launch replaces
 the ~40 kernel launches, and the outputs are copied out.
+
+Host inputs (``to_host=True``: Z and positions in host memory, ideally
+pinned) are copied straight into the graph's input buffers, and the
+outputs and the status word come back with asynchronous copies into pinned
+host buffers behind one stream synchronisation -- the call a host-side
+caller (the ASE calculator) makes once per step.
 """
 from __future__ import annotations
 
@@ -150,7 +156,7 @@ class Engine:
     # ---------------------------------------------------------------- calls
     def energy_forces(self, batch: Batch, path: int = _lib.PATH_TUNED_TC, forces: bool = True,
                       virial: bool = False, atom_energy: bool = False, check: bool = True,
-                      graph: Optional[bool] = None
+                      graph: Optional[bool] = None, to_host: bool = False
                       ) -> Tuple[torch.Tensor, Optional[torch.Tensor], Optional[torch.Tensor]]:
         """Energies [B] (float64), forces [N,3] (float32), dE/dstrain [B,3,3].
 
@@ -158,12 +164,20 @@ class Engine:
         when a call of the same shape was seen before; the first call of a
         shape runs eagerly and captures the graph for the next one.  The
         batch's ``mol_ptr``, ``box`` and ``pbc`` tensors are taken as
-        immutable: passing the same tensor object again skips its copy."""
+        immutable: passing the same tensor object again skips its copy.
+        ``to_host``: the batch's Z and positions may live in host memory and
+        the results are returned in host memory."""
         use_graph = self.use_graphs if graph is None else graph
         if use_graph and check and not torch.cuda.is_current_stream_capturing():
-            res = self._graph_call(batch, path, forces, virial, atom_energy)
+            res = self._graph_call(batch, path, forces, virial, atom_energy, to_host)
             if res is not None:
                 return res
+        if to_host:
+            dev = self.device
+            db = Batch(batch.Z.to(dev, non_blocking=True), batch.pos.to(dev, non_blocking=True), batch.mol_ptr,
+                       batch.box, batch.pbc)
+            res = self._eager_call(db, path, forces, virial, atom_energy, check)
+            return tuple(None if t is None else t.cpu() for t in res)
         return self._eager_call(batch, path, forces, virial, atom_energy, check)
 
     def _eager_call(self, batch: Batch, path: int, forces: bool, virial: bool, atom_energy: bool, check: bool):
@@ -200,7 +214,8 @@ class Engine:
             return E, F, V, A
         return E, F, V
 
-    def _graph_call(self, batch: Batch, path: int, forces: bool, virial: bool, atom_energy: bool):
+    def _graph_call(self, batch: Batch, path: int, forces: bool, virial: bool, atom_energy: bool,
+                    to_host: bool = False):
         """Replay (or, on the first call of a shape, run eagerly and capture)
         a CUDA graph of one energy_forces call.  Returns None when the graph
         must be rebuilt and the call redone eagerly."""
@@ -213,6 +228,12 @@ class Engine:
             del self._graphs[key]
             ent = None
         if ent is None:
+            if to_host:
+                dev = self.device
+                db = Batch(batch.Z.to(dev), batch.pos.to(dev), batch.mol_ptr, batch.box, batch.pbc)
+                res = self._eager_call(db, path, forces, virial, atom_energy, True)
+                self._capture_call(key, db, path, forces, virial, atom_energy)
+                return tuple(None if t is None else t.cpu() for t in res)
             res = self._eager_call(batch, path, forces, virial, atom_energy, True)
             self._capture_call(key, batch, path, forces, virial, atom_energy)
             return res
@@ -227,6 +248,8 @@ class Engine:
                 getattr(st, name).copy_(t, non_blocking=True)
                 src[name] = t
         ent["graph"].replay()
+        if to_host:
+            return self._host_results(key, ent, path)
         code, n_edges, where = self.status()
         if code == _lib.ERR_CAPACITY:
             self.edge_capacity[path] = int(n_edges * 1.25) + 1024
@@ -236,6 +259,31 @@ class Engine:
             raise _lib.MLFFError(code, f"device status {code} at index {where}")
         self.edge_capacity[path] = max(self.edge_capacity.get(path, 0), int(n_edges * 1.15) + 1024)
         return tuple(None if t is None else t.clone() for t in ent["out"])
+
+    def _host_results(self, key, ent, path: int):
+        """Status word and outputs of a replayed graph copied into pinned
+        host buffers behind one synchronisation; host copies returned."""
+        hb = ent.get("host")
+        if hb is None:
+            hb = ent["host"] = {"status": torch.empty(4, dtype=torch.int32).pin_memory(),
+                                "out": [None if t is None else torch.empty(t.shape, dtype=t.dtype).pin_memory()
+                                        for t in ent["out"]]}
+        # the status word sits at offset 0 of the workspace: code, n_edges (low 31 bits), where, n_edges >> 31
+        hb["status"].copy_(self.workspace[:16].view(torch.int32), non_blocking=True)
+        for t, h in zip(ent["out"], hb["out"]):
+            if t is not None:
+                h.copy_(t, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        code, lo, where, hi = hb["status"].tolist()
+        n_edges = (hi << 31) | (lo & 0x7FFFFFFF)
+        if code == _lib.ERR_CAPACITY:
+            self.edge_capacity[path] = int(n_edges * 1.25) + 1024
+            del self._graphs[key]
+            return None
+        if code != _lib.OK:
+            raise _lib.MLFFError(code, f"device status {code} at index {where}")
+        self.edge_capacity[path] = max(self.edge_capacity.get(path, 0), int(n_edges * 1.15) + 1024)
+        return tuple(None if h is None else h.clone() for h in hb["out"])
 
     def _capture_call(self, key, batch: Batch, path: int, forces: bool, virial: bool, atom_energy: bool):
         N, B = batch.n_atoms, batch.n_mol

@@ -119,9 +119,11 @@ class StudentCalculator(Calculator):
 
     def _fused(self, positions, numbers, cell, pbc, want_stress: bool) -> Dict[str, torch.Tensor]:
         dev = self.device
-        z = torch.as_tensor(np.asarray(numbers, dtype=np.int64), device=dev)
-        x = torch.as_tensor(np.asarray(positions, dtype=np.float32), device=dev)
         periodic = bool(pbc.any())
+        # energy + forces take host inputs and return host results (one synchronisation)
+        host = not (want_stress and periodic)
+        z = torch.as_tensor(np.asarray(numbers, dtype=np.int64), device="cpu" if host else dev)
+        x = torch.as_tensor(np.asarray(positions, dtype=np.float32), device="cpu" if host else dev)
         c = torch.as_tensor(cell.astype(np.float32).reshape(3, 3)) if periodic else None
         p = torch.as_tensor(pbc.astype(bool)) if periodic else None
         out: Dict[str, torch.Tensor] = {}

@@ -166,6 +166,7 @@ class StudentForceField(nn.Module):
         self._cell_cache = None                            # last host cell -> checked device box / pbc
         self._batch_cache = None                           # last host structure index -> device offsets
         self._packed_version = None
+        self._weight_slots = None                          # (tensor dict, name) of every parameter and buffer
 
     def _initialize_parameters(self):
         """Same initialisation as the reference (student_model.py:618-628)."""
@@ -188,7 +189,16 @@ class StudentForceField(nn.Module):
             raise ValueError(f"unknown precision {self.precision!r}; use one of {sorted(_lib.PATHS)}")
 
     def _weights_version(self):
-        return tuple((p.data_ptr(), p._version) for p in self.state_dict(keep_vars=True).values())
+        """(address, in-place version) of every parameter and buffer: changes
+        when a weight is updated in place, reassigned or moved.  The slots
+        are the modules' own parameter / buffer dicts, looked up once."""
+        slots = self._weight_slots
+        if slots is None:
+            slots = [(m._parameters, n) for m in self.modules() for n in m._parameters] + \
+                    [(m._buffers, n) for m in self.modules() for n in m._buffers]
+            self._weight_slots = slots
+        return tuple((t.data_ptr(), t._version) if t is not None else None
+                     for t in (d[n] for d, n in slots))
 
     def engine(self) -> Engine:
         dev = self.embedding.weight.device
@@ -204,18 +214,24 @@ class StudentForceField(nn.Module):
             self._packed_version = v
         return self._engine
 
-    def _engine_call(self, batch: Batch, forces: bool = True, virial: bool = False):
-        return self.engine().energy_forces(batch, self.path, forces=forces, virial=virial)
+    def _engine_call(self, batch: Batch, forces: bool = True, virial: bool = False, to_host: bool = False):
+        return self.engine().energy_forces(batch, self.path, forces=forces, virial=virial, to_host=to_host)
 
-    def _make_batch(self, atomic_numbers, positions, cell, pbc, batch, need_index: bool = True):
+    def _make_batch(self, atomic_numbers, positions, cell, pbc, batch, need_index: bool = True,
+                    host_inputs: bool = False):
         """Device Batch of one call.  A ``batch`` index or ``cell`` given on
         the host (as the calculator passes them) is validated and turned into
         molecule offsets on the host, with no device synchronisation; device
-        tensors are validated on the device."""
+        tensors are validated on the device.  ``host_inputs``: atomic numbers
+        and positions stay in host memory (the engine copies them into its
+        graph's input buffers)."""
         dev = self.embedding.weight.device
         if dev.type != "cuda" or not torch.cuda.is_available():
             raise RuntimeError("mlff_gb300 needs a CUDA device (GB300, sm_103a): move the model to cuda")
-        if positions.device != dev:
+        if host_inputs:
+            if positions.device.type != "cpu" or atomic_numbers.device.type != "cpu":
+                raise RuntimeError("host_inputs needs atomic numbers and positions in host memory")
+        elif positions.device != dev:
             raise RuntimeError(f"positions on {positions.device} but model on {dev}")
         N = int(atomic_numbers.shape[0])
         if batch is None:
@@ -308,9 +324,14 @@ class StudentForceField(nn.Module):
                           ) -> Tuple[torch.Tensor, torch.Tensor]:
         """Batched (energies [B] float64, forces [N,3] float32) in one call,
         without autograd -- the batched calculator path
-        (ase_calculator.py:708-770)."""
-        bt, _, _ = self._make_batch(atomic_numbers, positions, cell, pbc, batch, need_index=False)
-        E, F, _ = self._engine_call(bt, forces=True)
+        (ase_calculator.py:708-770).  Atomic numbers and positions in host
+        memory (pinned for asynchronous copies) give results in host memory:
+        the inputs go straight into the cached CUDA graph's buffers and the
+        results and status come back behind one synchronisation."""
+        host = positions.device.type == "cpu" and atomic_numbers.device.type == "cpu"
+        bt, _, _ = self._make_batch(atomic_numbers, positions, cell, pbc, batch, need_index=False,
+                                    host_inputs=host)
+        E, F, _ = self._engine_call(bt, forces=True, to_host=host)
         return E, F
 
     def energy_forces_virial(self, atomic_numbers, positions, cell=None, pbc=None, batch=None):

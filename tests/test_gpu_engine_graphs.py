@@ -4,7 +4,9 @@ A call whose shape was seen before replays a captured graph of the whole
 step on copies of the inputs; its results must equal an eager call bit for
 bit, for changing positions, for structure indices and cells given on the
 host, and across an edge-capacity overflow (the graph is dropped, the call
-redone eagerly with a larger capacity and captured again).
+redone eagerly with a larger capacity and captured again).  Host inputs
+(pinned host Z and positions, results returned in host memory) give the same
+bits as device inputs, through capture, replay and a capacity overflow.
 """
 import numpy as np
 import pytest
@@ -58,3 +60,31 @@ def test_graph_replay_equals_eager_periodic_and_capacity(model):
         assert torch.equal(E, E0) and torch.equal(F, F0)
         assert torch.isfinite(F).all()
     assert eng.status()[0] == 0
+
+
+def test_host_buffers_equal_device_call(model):
+    """energy_and_forces with host Z/positions: first call eager + capture,
+    later calls copy straight into the graph's inputs and read results and
+    status back behind one synchronisation; a compressed box overflows the
+    captured edge capacity on the host path and is redone."""
+    from mlff_gb300 import systems
+    s = systems.water_box(150, 15.0, 2.5, seed=6)
+    Zh = torch.as_tensor(s.Z, dtype=torch.int64).pin_memory()
+    Zd = Zh.cuda()
+    cell = torch.as_tensor(np.diag(s.box[0]).astype(np.float32))
+    pbc = torch.ones(3, dtype=torch.bool)
+    for scale in (1.0, 1.0, 1.0, 0.88, 0.88, 0.88):
+        Ph = torch.as_tensor(s.pos * scale, dtype=torch.float32).pin_memory()
+        E, F = model.energy_and_forces(Zh, Ph, cell=cell * scale, pbc=pbc)
+        assert E.device.type == "cpu" and F.device.type == "cpu"
+        E0, F0 = _eager(model, Zd, Ph.cuda(), cell=cell * scale, pbc=pbc)
+        assert torch.equal(E, E0.cpu()) and torch.equal(F, F0.cpu())
+    # a ragged batch with a host structure index, pageable host inputs
+    m = systems.molecule_batch(8, 10, 50, seed=9)
+    b = torch.as_tensor(np.repeat(np.arange(m.n_mol), np.diff(m.mol_ptr)))
+    Z = torch.as_tensor(m.Z, dtype=torch.int64)
+    for it in range(3):
+        P = torch.as_tensor(m.pos + 0.01 * it, dtype=torch.float32)
+        E, F = model.energy_and_forces(Z, P, batch=b)
+        E0, F0 = _eager(model, Z.cuda(), P.cuda(), batch=b)
+        assert torch.equal(E, E0.cpu()) and torch.equal(F, F0.cpu())
