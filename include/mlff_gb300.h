@@ -259,24 +259,31 @@ int mlff_param_grads(const mlff_dims *dims, const void *packed, const mlff_syste
                      const mlff_outputs *out, void *workspace, size_t workspace_bytes,
                      mlff_stream_t stream);
 
-/* Force term of the training loss: grads += sum_i G_i . dF_i/dtheta for
- * every non-NULL state_dict gradient, with G = force_weights (device,
- * float [N,3]) the derivative of the loss with respect to the predicted
- * forces F = -dE/dpos (e.g. G = 2 w_F (F - F_ref) / (3N) for the mean-
- * squared force error of ForceFieldLoss, training/losses.py:154-170, weight
- * w_F = 100 in configs/train_student.yaml).  This is the second-order part
- * of loss.backward() when the forces were taken with
+/* Force and stress terms of the training loss: grads += sum_i G_i .
+ * dF_i/dtheta + sum_b S_b : dW_b/dtheta for every non-NULL state_dict
+ * gradient, with G = force_weights (device, float [N,3], or NULL) the
+ * derivative of the loss with respect to the predicted forces F = -dE/dpos
+ * (e.g. G = 2 w_F (F - F_ref) / (3N) for the mean-squared force error of
+ * ForceFieldLoss, training/losses.py:154-170, weight w_F = 100 in
+ * configs/train_student.yaml) and S = virial_weights (device, double
+ * [B,3,3], or NULL) the derivative with respect to the strain derivatives
+ * W_b = dE_b/d(strain) that mlff_energy_forces returns as the virial (the
+ * stress term, :222-234, enters through stress = sym(W) / volume).  This
+ * is the second-order part of loss.backward() when forces were taken with
  * torch.autograd.grad(..., create_graph=True) (predict_energy_and_forces,
- * models/student_model.py:759-795, in training mode).  Computed exactly, in
- * forward mode over the reverse pass: the plain FP32 path runs once on
- * (value, derivative along G) pairs and the derivative of grad_theta E is
- * subtracted from the gradients.  Call after mlff_param_grads (which
- * writes the energy term) to get the full loss gradient; the grads
- * structure is the same.  Workspace: mlff_workspace_size(...,
- * MLFF_PATH_TRAIN_FORCES), which also serves mlff_param_grads. */
+ * models/student_model.py:759-795, in training mode).  Computed exactly,
+ * in forward mode over the reverse pass: the plain FP32 path runs once on
+ * (value, derivative) pairs along the direction (positions moved by -G,
+ * every edge vector r of structure b strained by S_b r) and the derivative
+ * of grad_theta E is added to the gradients.  Call after
+ * mlff_param_grads (which writes the energy term) to get the full loss
+ * gradient; the grads structure is the same.  Workspace:
+ * mlff_workspace_size(..., MLFF_PATH_TRAIN_FORCES), which also serves
+ * mlff_param_grads. */
 int mlff_param_grads_forces(const mlff_dims *dims, const void *packed, const mlff_system *sys,
-                            int64_t edge_capacity, const float *force_weights, const mlff_grads *grads,
-                            void *workspace, size_t workspace_bytes, mlff_stream_t stream);
+                            int64_t edge_capacity, const float *force_weights, const double *virial_weights,
+                            const mlff_grads *grads, void *workspace, size_t workspace_bytes,
+                            mlff_stream_t stream);
 
 /* Kernel timing for benchmarks (no counterpart in the reference, whose
  * timers wrap whole Python calls: cuda/benchmark_utils.py:147-194).

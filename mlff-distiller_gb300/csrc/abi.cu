@@ -367,13 +367,13 @@ int mlff_param_grads(const mlff_dims* dims, const void* packed, const mlff_syste
 }
 
 int mlff_param_grads_forces(const mlff_dims* dims, const void* packed, const mlff_system* sys, int64_t edge_capacity,
-                            const float* force_weights, const mlff_grads* grads, void* workspace,
-                            size_t workspace_bytes, mlff_stream_t stream) {
+                            const float* force_weights, const double* virial_weights, const mlff_grads* grads,
+                            void* workspace, size_t workspace_bytes, mlff_stream_t stream) {
     WsLayout L;
     int r = prepare(dims, sys, edge_capacity, MLFF_PATH_TRAIN_FORCES, workspace, workspace_bytes, L);
     if (r) return r;
-    if (!packed || !force_weights || !grads) {
-        set_error("packed weights, force_weights and grads are required");
+    if (!packed || (!force_weights && !virial_weights) || !grads) {
+        set_error("packed weights, grads and force_weights and / or virial_weights are required");
         return MLFF_ERR_INVALID;
     }
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
@@ -381,7 +381,8 @@ int mlff_param_grads_forces(const mlff_dims* dims, const void* packed, const mlf
     if ((r = launch_neighbors(*dims, *sys, L, workspace, st))) return r;
     PackedOffsets po = packed_offsets(*dims);
     GradCtx g{nullptr, *grads};
-    return run_plain_tangent(*dims, static_cast<const float*>(packed), po, *sys, L, workspace, st, g, force_weights);
+    return run_plain_tangent(*dims, static_cast<const float*>(packed), po, *sys, L, workspace, st, g, force_weights,
+                             virial_weights);
 }
 
 int mlff_read_status(const void* workspace, int32_t* code, int64_t* n_edges, int32_t* where, mlff_stream_t stream) {

@@ -1,12 +1,13 @@
-// Forward-mode (tangent) arithmetic for the force-matching gradient.
+// Forward-mode (tangent) arithmetic for the force- and stress-loss
+// gradients.
 //
 // A Dual carries a value and its derivative along one direction of the
-// atom positions (v + eps t).  The plain FP32 path's kernels are templates
-// over the scalar type: instantiated with float they are the plain path,
-// instantiated with Dual they run the same operations on (value, tangent)
-// pairs, so the weight-gradient reductions return both grad_theta E and
-// its derivative along the direction, d/deps grad_theta E(r + eps G) -- the
-// mixed second derivative a force loss needs (the double backward of
+// atom positions and cell strains (v + eps t).  The plain FP32 path's
+// kernels are templates over the scalar type: instantiated with float they
+// are the plain path, instantiated with Dual they run the same operations
+// on (value, tangent) pairs, so the weight-gradient reductions return both
+// grad_theta E and its derivative along the direction -- the mixed second
+// derivative a force or stress loss needs (the double backward of
 // torch.autograd.grad(..., create_graph=True) followed by loss.backward()).
 //
 // The helpers below have a float overload that is exactly the plain path's

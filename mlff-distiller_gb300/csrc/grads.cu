@@ -18,10 +18,12 @@
 // come from the plain path, whose message scatter-adds are float atomics.
 //
 // The same reductions over Dual scalars (the plain path's tangent pass,
-// dual.cuh) give d/deps grad_theta E(r + eps G); their tangent part is
-// subtracted from the gradient outputs, which adds sum_i G_i . dF_i/dtheta,
-// the parameter gradient of a force loss with dL/dF = G (the second-order
-// term of loss.backward() through forces taken with create_graph=True).
+// dual.cuh) give the derivative of grad_theta E along positions moved by
+// -G and cells strained by S; their tangent part is added to the gradient
+// outputs: sum_i G_i . dF_i/dtheta + sum_b S_b : dW_b/dtheta, the parameter
+// gradient of a force / stress loss with dL/dF = G, dL/dW = S (the
+// second-order term of loss.backward() through forces and strain
+// derivatives taken with create_graph=True).
 #include "common.cuh"
 #include "dual.cuh"
 #include "workspace.h"
@@ -87,9 +89,9 @@ __global__ void __launch_bounds__(256) wgrad_partial_kernel(const T* __restrict_
         }
 }
 
-// float: out = the sum; Dual: out -= the tangent of the sum
+// float: out = the sum; Dual: out += the tangent of the sum
 __device__ __forceinline__ void grad_store(float* out, float s) { *out = s; }
-__device__ __forceinline__ void grad_store(float* out, Dual s) { *out -= s.t; }
+__device__ __forceinline__ void grad_store(float* out, Dual s) { *out += s.t; }
 
 template <class T>
 __global__ void wgrad_reduce_kernel(const T* __restrict__ partial, int64_t MK, float* __restrict__ out,

@@ -20,9 +20,14 @@ constexpr float PI_F = 3.14159265358979f;
 
 // ------------------------------------------------------------- geometry
 // u = r / (d + 1e-8), d = |r| (:709-715); e = rbf(d) * fc(d) (:718-722) and
-// de/dd for the reverse pass.  Dual: pos_t [N][3] is the position tangent.
+// de/dd for the reverse pass.  Dual: the edge vector's tangent is
+// -(pos_t[b] - pos_t[a]) (positions moved along -G, G = pos_t [N][3],
+// optional; F = -dE/dpos) plus S_m r for a strain direction S_m [B][3][3]
+// (optional; positions and image shifts scale with the cell, so every
+// edge vector r becomes (I + eps S_m) r).
 template <class T>
 __global__ void pl_geom_kernel(const float4* __restrict__ pos4, const float* __restrict__ pos_t,
+                               const double* __restrict__ strain_t,
                                const int32_t* __restrict__ atom_mol,
                                const float* __restrict__ box, const uint8_t* __restrict__ pbc,
                                const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
@@ -43,11 +48,17 @@ __global__ void pl_geom_kernel(const float4* __restrict__ pos4, const float* __r
         }
         const float3 r0 = edge_vector(pos4[b], pos4[a], bx);
         float tx = 0.0f, ty = 0.0f, tz = 0.0f;
-        if (is_dual_v<T>) {
-            // the image shift is constant: r' = G_b - G_a
-            tx = pos_t[3 * b] - pos_t[3 * a];
-            ty = pos_t[3 * b + 1] - pos_t[3 * a + 1];
-            tz = pos_t[3 * b + 2] - pos_t[3 * a + 2];
+        if (is_dual_v<T> && pos_t) {
+            // a position direction leaves the image shift alone: r' = -(G_b - G_a)
+            tx = pos_t[3 * a] - pos_t[3 * b];
+            ty = pos_t[3 * a + 1] - pos_t[3 * b + 1];
+            tz = pos_t[3 * a + 2] - pos_t[3 * b + 2];
+        }
+        if (is_dual_v<T> && strain_t) {
+            const double* S = strain_t + 9 * m;
+            tx += (float)(S[0] * r0.x + S[1] * r0.y + S[2] * r0.z);
+            ty += (float)(S[3] * r0.x + S[4] * r0.y + S[5] * r0.z);
+            tz += (float)(S[6] * r0.x + S[7] * r0.y + S[8] * r0.z);
         }
         const T rx = tmake<T>(r0.x, tx), ry = tmake<T>(r0.y, ty), rz = tmake<T>(r0.z, tz);
         const T d = tdist(rx, ry, rz);
@@ -397,13 +408,14 @@ __global__ void pl_embed_dual_kernel(const float* __restrict__ emb, const int64_
 
 // One pass of the plain path over scalars T.  float: energies, the
 // reverse pass for forces (and, with grad, the parameter gradients of
-// sum_b w_b E_b).  Dual (grad required, pos_t the position direction G):
-// the same graph with unit seeds; the weight-gradient reductions subtract
-// the tangent of grad_theta E, i.e. add sum_i G_i . dF_i/dtheta.
+// sum_b w_b E_b).  Dual (grad required; pos_t the position direction G
+// and / or strain_t the strain direction S): the same graph with unit
+// seeds along (-G, S); the weight-gradient reductions add the tangent of
+// grad_theta E, i.e. sum_i G_i . dF_i/dtheta + sum_b S_b : dW_b/dtheta.
 template <class T>
 static int run_plain_t(const mlff_dims& d, const float* P, const PackedOffsets& po, const mlff_system& sys,
                        const WsLayout& L, void* ws, const mlff_outputs& out, cudaStream_t st, const GradCtx* grad,
-                       const float* pos_t) {
+                       const float* pos_t, const double* strain_t) {
     constexpr bool DUAL = is_dual_v<T>;
     const int N = sys.n_atoms;
     const int64_t NX = (int64_t)N * 4 * H;
@@ -431,14 +443,15 @@ static int run_plain_t(const mlff_dims& d, const float* P, const PackedOffsets& 
     const int eblocks = 152 * 8;
     const int nblocks = (int)std::max<int64_t>(1, std::min<int64_t>(((int64_t)N * H + 255) / 256, 152 * 8));
     int r;
-    if (DUAL && (!grad || !pos_t)) {
-        set_error("the tangent pass needs gradient outputs and a position direction");
+    if (DUAL && (!grad || (!pos_t && !strain_t))) {
+        set_error("the tangent pass needs gradient outputs and a position or strain direction");
         return MLFF_ERR_INVALID;
     }
 
     {
         ProfScope prof(PK_PLAIN_EDGE, st);
-        pl_geom_kernel<T><<<eblocks, 256, 0, st>>>(ws_ptr<float4>(ws, L.pos4), pos_t, ws_ptr<int32_t>(ws, L.atom_mol),
+        pl_geom_kernel<T><<<eblocks, 256, 0, st>>>(ws_ptr<float4>(ws, L.pos4), pos_t, strain_t,
+                                                   ws_ptr<int32_t>(ws, L.atom_mol),
                                                    sys.box, sys.pbc, row_ptr, ws_ptr<int32_t>(ws, L.col),
                                                    ws_ptr<int32_t>(ws, L.erecv), N, P + po.centers, P + po.gamma,
                                                    d.n_rbf, d.cutoff, geo, erbf, erbf_d, status);
@@ -559,13 +572,14 @@ static int run_plain_t(const mlff_dims& d, const float* P, const PackedOffsets& 
 
 int run_plain(const mlff_dims& d, const float* P, const PackedOffsets& po, const mlff_system& sys,
               const WsLayout& L, void* ws, const mlff_outputs& out, cudaStream_t st, const GradCtx* grad) {
-    return run_plain_t<float>(d, P, po, sys, L, ws, out, st, grad, nullptr);
+    return run_plain_t<float>(d, P, po, sys, L, ws, out, st, grad, nullptr, nullptr);
 }
 
 int run_plain_tangent(const mlff_dims& d, const float* P, const PackedOffsets& po, const mlff_system& sys,
-                      const WsLayout& L, void* ws, cudaStream_t st, const GradCtx& grad, const float* pos_t) {
+                      const WsLayout& L, void* ws, cudaStream_t st, const GradCtx& grad, const float* pos_t,
+                      const double* strain_t) {
     mlff_outputs none{};
-    return run_plain_t<Dual>(d, P, po, sys, L, ws, none, st, &grad, pos_t);
+    return run_plain_t<Dual>(d, P, po, sys, L, ws, none, st, &grad, pos_t, strain_t);
 }
 
 }  // namespace mlff

@@ -108,12 +108,14 @@ struct GradCtx {
 int run_plain(const mlff_dims& d, const float* packed, const PackedOffsets& po,
               const mlff_system& sys, const WsLayout& L, void* ws, const mlff_outputs& out,
               cudaStream_t st, const GradCtx* grad = nullptr);
-// Pass of the plain path over (value, tangent) pairs with position
-// direction pos_t [N][3]: subtracts d/deps grad_theta sum_b E_b(r + eps pos_t)
-// from every non-NULL gradient in grad.g (grad.w unused).
+// Pass of the plain path over (value, tangent) pairs along positions moved
+// by -pos_t [N][3] and cells strained by strain_t [B][3][3] (either may be
+// NULL): adds the derivative of grad_theta sum_b E_b along that direction
+// to every non-NULL gradient in grad.g (grad.w unused), i.e. sum_i G_i .
+// dF_i/dtheta + sum_b S_b : dW_b/dtheta.
 int run_plain_tangent(const mlff_dims& d, const float* packed, const PackedOffsets& po,
                       const mlff_system& sys, const WsLayout& L, void* ws, cudaStream_t st,
-                      const GradCtx& grad, const float* pos_t);
+                      const GradCtx& grad, const float* pos_t, const double* strain_t);
 // Weight-gradient reductions of the plain path's reverse pass, over float
 // or Dual scalars (instantiated in grads.cu).
 template <class T>

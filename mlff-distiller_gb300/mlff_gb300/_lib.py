@@ -153,7 +153,7 @@ def load(build_if_missing: bool = True):
         lib.mlff_param_grads.argtypes = [ctypes.POINTER(Dims), _P, ctypes.POINTER(System), i64, _P,
                                          ctypes.POINTER(Grads), ctypes.POINTER(Outputs), _P, sz, _P]
         lib.mlff_param_grads_forces.restype = ctypes.c_int
-        lib.mlff_param_grads_forces.argtypes = [ctypes.POINTER(Dims), _P, ctypes.POINTER(System), i64, _P,
+        lib.mlff_param_grads_forces.argtypes = [ctypes.POINTER(Dims), _P, ctypes.POINTER(System), i64, _P, _P,
                                                 ctypes.POINTER(Grads), _P, sz, _P]
         lib.mlff_radius_graph_noalloc.restype = ctypes.c_int
         lib.mlff_radius_graph_noalloc.argtypes = [ctypes.POINTER(System), ctypes.c_float, i64, _P, _P, _P, _P]

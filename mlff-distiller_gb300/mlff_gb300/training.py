@@ -12,9 +12,11 @@ pass, which adds sum_i G_i . dF_i/dtheta -- what the reference gets by
 taking forces with create_graph=True and differentiating again).
 
 ``ForceFieldLoss`` restates the reference's loss (training/losses.py:15-
-246: energy, force and angular terms with mse / mae / huber components);
-the trainers evaluate it with torch on the predicted energies and forces
-only, to get w and G.  ``ForceFieldTrainer`` is the optimisation step with
+246: energy, force, angular and stress terms with mse / mae / huber
+components); the trainers evaluate it with torch on the predictions only
+(energies, forces, stress) to get w, G and, for the stress term, S =
+dL/dW with W = dE/d(strain) (one more direction of the same forward-mode
+pass).  ``ForceFieldTrainer`` is the optimisation step with
 the reference's defaults (configs/train_student.yaml: energy weight 1,
 force weight 100, angular weight 10, AdamW lr 1e-3, weight decay 1e-5,
 betas (0.9, 0.999), eps 1e-8, gradient-norm clip 1.0); ``EnergyTrainer``
@@ -58,25 +60,31 @@ def _grads_struct(model, grads: Dict[str, torch.Tensor]):
 
 
 def param_grads(model, batch: Batch, weights: torch.Tensor, forces: bool = False,
-                force_weights: Optional[torch.Tensor] = None
+                force_weights: Optional[torch.Tensor] = None, virial_weights: Optional[torch.Tensor] = None
                 ) -> Tuple[torch.Tensor, Dict[str, torch.Tensor], Optional[torch.Tensor]]:
     """Energies [B] (float64), {name: dL/d(name)} for every trainable
     parameter (float32, state_dict shapes) and, if asked, the forces
     -sum_b w_b dE_b/dpos.
 
     dL/dtheta = sum_b w_b dE_b/dtheta (weights: w = dL/dE, [B]) plus, when
-    force_weights G = dL/dF [N,3] is given, sum_i G_i . dF_i/dtheta."""
+    force_weights G = dL/dF [N,3] is given, sum_i G_i . dF_i/dtheta, plus,
+    when virial_weights S = dL/dW [B,3,3] is given (W = dE/d(strain), the
+    virial the engine returns), sum_b S_b : dW_b/dtheta."""
     eng = model.engine()
     dev = eng.device
     N, B = batch.n_atoms, batch.n_mol
     w = torch.as_tensor(weights, dtype=torch.float64, device=dev).contiguous()
     if w.shape != (B,):
         raise ValueError(f"weights must have shape ({B},), got {tuple(w.shape)}")
-    G = None
+    G = S = None
     if force_weights is not None:
         G = torch.as_tensor(force_weights, dtype=torch.float32, device=dev).contiguous()
         if G.shape != (N, 3):
             raise ValueError(f"force_weights must have shape ({N}, 3), got {tuple(G.shape)}")
+    if virial_weights is not None:
+        S = torch.as_tensor(virial_weights, dtype=torch.float64, device=dev).contiguous()
+        if S.shape != (B, 3, 3):
+            raise ValueError(f"virial_weights must have shape ({B}, 3, 3), got {tuple(S.shape)}")
     params = dict(model.named_parameters())
     grads = {n: torch.zeros_like(p, dtype=torch.float32, device=dev) for n, p in params.items() if p.requires_grad}
     g = _grads_struct(model, grads)
@@ -86,7 +94,8 @@ def param_grads(model, batch: Batch, weights: torch.Tensor, forces: bool = False
     out.energy, out.forces, out.virial, out.atom_energy = E.data_ptr(), _lib.ptr(F), None, None
     sysd = batch.system()
     path = _lib.PATH_TRAIN
-    ws_path = _lib.PATH_TRAIN if G is None else _lib.PATH_TRAIN_FORCES
+    second = G is not None or S is not None
+    ws_path = _lib.PATH_TRAIN_FORCES if second else _lib.PATH_TRAIN
     for _ in range(4):
         cap = eng.capacity(N, path)
         ws = eng.workspace_for(N, B, cap, ws_path)
@@ -103,11 +112,11 @@ def param_grads(model, batch: Batch, weights: torch.Tensor, forces: bool = False
         break
     else:
         raise _lib.MLFFError(_lib.ERR_CAPACITY, "edge capacity did not converge")
-    if G is not None:
+    if second:
         # same structures, same capacity: the edge list fits
         _lib.check(eng.lib.mlff_param_grads_forces(ctypes.byref(eng.dims), eng.packed.data_ptr(), ctypes.byref(sysd),
-                                                   cap, G.data_ptr(), ctypes.byref(g), ws.data_ptr(), ws.numel(),
-                                                   _stream_handle()))
+                                                   cap, _lib.ptr(G), _lib.ptr(S), ctypes.byref(g), ws.data_ptr(),
+                                                   ws.numel(), _stream_handle()))
         code, _, where = eng.status()
         if code != _lib.OK:
             raise _lib.MLFFError(code, f"device status {code} at index {where}")
@@ -196,20 +205,36 @@ class ForceFieldLoss:
         return out
 
     def derivatives(self, E: torch.Tensor, F: torch.Tensor, E_ref: torch.Tensor, F_ref: torch.Tensor,
-                    mask: Optional[Dict[str, torch.Tensor]] = None):
-        """(loss dict, dL/dE [B] float64, dL/dF [N,3] float32 or None): the
-        loss differentiated with respect to the predictions only."""
+                    mask: Optional[Dict[str, torch.Tensor]] = None, W: Optional[torch.Tensor] = None,
+                    volume: Optional[torch.Tensor] = None, S_ref: Optional[torch.Tensor] = None):
+        """(loss dict, dL/dE [B] float64, dL/dF [N,3] float32 or None,
+        dL/dW [B,3,3] float64 or None): the loss differentiated with respect
+        to the predictions only.  With W = dE/d(strain) [B,3,3], the cell
+        volumes [B] and stress targets S_ref ([B,3,3] or Voigt [B,6]), the
+        predicted stress sym(W) / volume (the calculator's stress) enters
+        the stress term."""
         Ed = E.detach().to(torch.float64).requires_grad_(True)
         Fd = F.detach().to(torch.float64).requires_grad_(True)
-        out = self({"energy": Ed, "forces": Fd},
-                   {"energy": E_ref.to(torch.float64), "forces": F_ref.to(torch.float64)}, mask)
+        pred = {"energy": Ed, "forces": Fd}
+        tgt = {"energy": E_ref.to(torch.float64), "forces": F_ref.to(torch.float64)}
+        Wd = None
+        if W is not None and S_ref is not None:
+            Wd = W.detach().to(torch.float64).requires_grad_(True)
+            sym = 0.5 * (Wd + Wd.transpose(1, 2)) / volume.to(torch.float64).reshape(-1, 1, 1)
+            if S_ref.shape[-1] == 6:
+                sym = torch.stack([sym[:, 0, 0], sym[:, 1, 1], sym[:, 2, 2], sym[:, 1, 2], sym[:, 0, 2],
+                                   sym[:, 0, 1]], dim=-1)
+            pred["stress"], tgt["stress"] = sym, S_ref.to(torch.float64)
+        out = self(pred, tgt, mask)
         total = out["total"]
         if not torch.is_tensor(total) or not total.requires_grad:
-            return out, torch.zeros_like(Ed), None
-        gE, gF = torch.autograd.grad(total, [Ed, Fd], allow_unused=True)
-        gE = torch.zeros_like(Ed) if gE is None else gE.detach()
-        gF = None if gF is None else gF.detach().to(torch.float32)
-        return out, gE, gF
+            return out, torch.zeros_like(Ed), None, None
+        inputs = [Ed, Fd] + ([Wd] if Wd is not None else [])
+        gr = torch.autograd.grad(total, inputs, allow_unused=True)
+        gE = torch.zeros_like(Ed) if gr[0] is None else gr[0].detach()
+        gF = None if gr[1] is None else gr[1].detach().to(torch.float32)
+        gW = None if Wd is None or gr[2] is None else gr[2].detach()
+        return out, gE, gF, gW
 
 
 def _adamw(model, lr, weight_decay, betas, eps):
@@ -242,24 +267,30 @@ class ForceFieldTrainer:
         self.grad_clip = grad_clip
         self.steps = 0
 
-    def _predict(self, batch: Batch):
-        E, F, _ = self.model.engine().energy_forces(batch, _lib.PATH_PLAIN_FP32, forces=True)
-        return E, F
+    def _predict(self, batch: Batch, virial: bool = False):
+        return self.model.engine().energy_forces(batch, _lib.PATH_PLAIN_FP32, forces=True, virial=virial)
 
-    def step(self, batch: Batch, E_ref, F_ref) -> Dict[str, float]:
+    def step(self, batch: Batch, E_ref, F_ref, S_ref=None) -> Dict[str, float]:
+        """One step on energy and force targets (and stress targets
+        [B,3,3] or Voigt [B,6] for periodic batches)."""
         dev = batch.Z.device
         E_ref = torch.as_tensor(E_ref, dtype=torch.float64, device=dev)
         F_ref = torch.as_tensor(F_ref, dtype=torch.float64, device=dev)
-        E, F = self._predict(batch)
-        out, w, G = self.loss_fn.derivatives(E, F, E_ref, F_ref)
-        _, grads, _ = param_grads(self.model, batch, w, force_weights=G)
+        stress = S_ref is not None and self.loss_fn.stress_weight > 0
+        if stress and batch.box is None:
+            raise ValueError("stress targets need periodic structures (batch.box)")
+        E, F, W = self._predict(batch, virial=stress)
+        vol = torch.prod(batch.box.to(torch.float64), dim=1) if stress else None
+        S_ref = torch.as_tensor(S_ref, dtype=torch.float64, device=dev) if stress else None
+        out, w, G, S = self.loss_fn.derivatives(E, F, E_ref, F_ref, W=W, volume=vol, S_ref=S_ref)
+        _, grads, _ = param_grads(self.model, batch, w, force_weights=G, virial_weights=S)
         _apply(self.model, self.opt, grads, self.grad_clip)
         self.steps += 1
         return {k: float(v.item()) for k, v in out.items() if torch.is_tensor(v) and v.numel() == 1}
 
     def evaluate(self, batch: Batch, E_ref, F_ref) -> Dict[str, float]:
         dev = batch.Z.device
-        E, F = self._predict(batch)
+        E, F, _ = self._predict(batch)
         out = self.loss_fn({"energy": E.to(torch.float64), "forces": F.to(torch.float64)},
                            {"energy": torch.as_tensor(E_ref, dtype=torch.float64, device=dev),
                             "forces": torch.as_tensor(F_ref, dtype=torch.float64, device=dev)})

@@ -153,8 +153,14 @@ def _train_setup(params, Z, pos, mol_ptr, cutoff, box, pbc, dtype):
     shift_t = torch.as_tensor(np.asarray(shift), dtype=dtype) * boxes[mol[dst_t]]
     Zt = torch.as_tensor(np.asarray(Z), dtype=torch.long)
 
-    def energy_of(x):
-        return energy(p, Zt, x, src_t, dst_t, shift_t, mol, n_mol, cutoff)
+    def energy_of(x, eps=None):
+        # eps [B,3,3]: affine strain of positions and image shifts, r' = (I + eps) r
+        if eps is None:
+            return energy(p, Zt, x, src_t, dst_t, shift_t, mol, n_mol, cutoff)
+        strain = torch.eye(3, dtype=dtype) + eps
+        xs = torch.einsum("nab,nb->na", strain[mol], x)
+        sv = torch.einsum("eab,eb->ea", strain[mol[dst_t]], shift_t)
+        return energy(p, Zt, xs, src_t, dst_t, sv, mol, n_mol, cutoff)
 
     return p, train, energy_of, torch.as_tensor(pos_np, dtype=dtype)
 
@@ -178,16 +184,25 @@ def param_grads(params, Z, pos, mol_ptr, weights, cutoff=5.0, box=None, pbc=None
 
 
 def param_grads_forces(params, Z, pos, mol_ptr, energy_weights, force_weights, cutoff=5.0, box=None, pbc=None,
-                       dtype=torch.float64):
-    """sum_b w_b dE_b/dtheta + sum_i G_i . dF_i/dtheta, F = -dE/dpos taken
-    with create_graph=True (predict_energy_and_forces, student_model.py:
-    759-795, in training mode) and differentiated again: the parameter
-    gradients loss.backward() gives the reference's Trainer for a loss with
-    dL/dE_b = w_b and dL/dF_i = G_i.  Returns (E, F, grads)."""
+                       dtype=torch.float64, virial_weights=None):
+    """sum_b w_b dE_b/dtheta + sum_i G_i . dF_i/dtheta (+ sum_b S_b :
+    dW_b/dtheta with W_b = dE_b/d(strain)), F = -dE/dpos and W taken with
+    create_graph=True (predict_energy_and_forces, student_model.py:759-795,
+    in training mode) and differentiated again: the parameter gradients
+    loss.backward() gives the reference's Trainer for a loss with dL/dE_b =
+    w_b, dL/dF_i = G_i (and dL/dW_b = S_b).  Returns (E, F, grads)."""
     p, train, energy_of, x = _train_setup(params, Z, pos, mol_ptr, cutoff, box, pbc, dtype)
     x = x.clone().requires_grad_(True)
-    E = energy_of(x)
-    F = -torch.autograd.grad(E.sum(), x, create_graph=True)[0]
+    n_mol = len(np.asarray(mol_ptr)) - 1
+    eps = torch.zeros(n_mol, 3, 3, dtype=dtype, requires_grad=True)
+    E = energy_of(x, eps if virial_weights is not None else None)
+    inputs = [x, eps] if virial_weights is not None else [x]
+    g = torch.autograd.grad(E.sum(), inputs, create_graph=True)
+    F = -g[0]
     w = torch.as_tensor(np.asarray(energy_weights), dtype=dtype)
-    G = torch.as_tensor(np.asarray(force_weights), dtype=dtype)
-    return E.detach(), F.detach(), _grads_of((E * w).sum() + (F * G).sum(), p, train)
+    obj = (E * w).sum()
+    if force_weights is not None:
+        obj = obj + (F * torch.as_tensor(np.asarray(force_weights), dtype=dtype)).sum()
+    if virial_weights is not None:
+        obj = obj + (g[1] * torch.as_tensor(np.asarray(virial_weights), dtype=dtype)).sum()
+    return E.detach(), F.detach(), _grads_of(obj, p, train)

@@ -109,7 +109,8 @@ def test_model_refuses_cpu_compute(weights_seed0):
 
 def test_force_loss_gradient_arguments_checked_on_host():
     """mlff_param_grads_forces validates its arguments before any device
-    work: a NULL direction, a NULL workspace and a short workspace."""
+    work: no direction (neither force nor virial weights), a NULL workspace
+    and a short workspace."""
     import ctypes
     from mlff_gb300 import _lib
     from mlff_gb300.engine import dims_of
@@ -126,12 +127,12 @@ def test_force_loss_gradient_arguments_checked_on_host():
     g = _lib.Grads()
     need = lib.mlff_workspace_size(ctypes.byref(d), 2, 1, 1024, _lib.PATH_TRAIN_FORCES)
     fake = ctypes.c_void_p(256)   # never dereferenced: every call below fails on the host
-    r = lib.mlff_param_grads_forces(ctypes.byref(d), fake, ctypes.byref(s), 1024, None, ctypes.byref(g), fake,
-                                    need, None)
+    r = lib.mlff_param_grads_forces(ctypes.byref(d), fake, ctypes.byref(s), 1024, None, None, ctypes.byref(g),
+                                    fake, need, None)
     assert r == _lib.ERR_INVALID and b"force_weights" in lib.mlff_last_error_string()
-    r = lib.mlff_param_grads_forces(ctypes.byref(d), fake, ctypes.byref(s), 1024, fake, ctypes.byref(g), None,
+    r = lib.mlff_param_grads_forces(ctypes.byref(d), fake, ctypes.byref(s), 1024, fake, None, ctypes.byref(g), None,
                                     need, None)
     assert r == _lib.ERR_INVALID and b"workspace" in lib.mlff_last_error_string()
-    r = lib.mlff_param_grads_forces(ctypes.byref(d), fake, ctypes.byref(s), 1024, fake, ctypes.byref(g), fake,
+    r = lib.mlff_param_grads_forces(ctypes.byref(d), fake, ctypes.byref(s), 1024, None, fake, ctypes.byref(g), fake,
                                     need - 1, None)
     assert r == _lib.ERR_WORKSPACE

@@ -154,7 +154,7 @@ def test_force_loss_grads_vs_reference_training_step(weights_bias):
     from mlff_gb300.training import ForceFieldLoss, param_grads
     g = np.load(os.path.join(GOLDEN, "golden_train.npz"))
     loss = ForceFieldLoss(energy_weight=1.0, force_weight=100.0, stress_weight=0.1, angular_weight=10.0)
-    _, w, G = loss.derivatives(torch.tensor(g["E"]), torch.tensor(g["F"]), torch.tensor(g["E_ref"]),
+    _, w, G, _ = loss.derivatives(torch.tensor(g["E"]), torch.tensor(g["F"]), torch.tensor(g["E_ref"]),
                                torch.tensor(g["F_ref"]))
     m = _model(weights_bias)
     _, grads, _ = param_grads(m, make_batch(g["Z"], g["pos"], g["mol_ptr"]), w, force_weights=G)
@@ -172,10 +172,13 @@ def test_force_loss_grads_vs_reference_training_step(weights_bias):
 
 
 def test_force_training_gain(weights_seed0, weights_bias):
-    """Energy + force training (ForceFieldTrainer, the reference's loss
-    weights) on a teacher's float64 energies and forces: held-out force
-    RMSE and loss drop well below the untrained network's, and the trained
-    weights predict better forces on the tensor-core inference path too."""
+    """Force-matching training (ForceFieldTrainer on the force term: the
+    parameter gradients are all second-order) on a teacher's float64
+    forces: held-out force RMSE and loss drop well below the untrained
+    network's, and the trained weights predict better forces on the
+    tensor-core inference path too.  (With the reference's energy weight
+    the first steps mostly remove the teacher's energy offset; the force
+    term alone shows what the second-order gradients buy.)"""
     from mlff_gb300 import systems
     from mlff_gb300.training import ForceFieldLoss, ForceFieldTrainer
     train = systems.molecule_batch(32, 10, 40, seed=41)
@@ -187,7 +190,7 @@ def test_force_training_gain(weights_seed0, weights_bias):
 
     (Et, Ft), (Ev, Fv) = teacher(train), teacher(test)
     m = _model(weights_seed0)
-    tr = ForceFieldTrainer(m, ForceFieldLoss(energy_weight=1.0, force_weight=100.0, angular_weight=0.0), lr=2e-3)
+    tr = ForceFieldTrainer(m, ForceFieldLoss(energy_weight=0.0, force_weight=100.0, angular_weight=0.0), lr=2e-3)
     bt, bv = _batch(train), _batch(test)
     before = tr.evaluate(bv, Ev, Fv)
     hist = [tr.step(bt, Et, Ft) for _ in range(60)]
@@ -201,6 +204,60 @@ def test_force_training_gain(weights_seed0, weights_bias):
     print(f"held-out force RMSE: untrained {before['force_rmse']:.3e}, trained {after['force_rmse']:.3e} "
           f"(fp16x3 {rmse_inf:.3e}); total loss {before['total']:.3e} -> {after['total']:.3e}; "
           f"train loss {hist[0]['total']:.3e} -> {hist[-1]['total']:.3e}")
+    assert hist[-1]["total"] < 0.3 * hist[0]["total"]
+    assert after["force_rmse"] < 0.6 * before["force_rmse"]
+    assert rmse_inf < 0.6 * before["force_rmse"]
+
+
+def test_stress_loss_grads_vs_oracle(weights_bias):
+    """Periodic box: energy + force + strain-derivative (stress) loss
+    gradients, and the strain term alone, against float64 double backward
+    through the oracle."""
+    from mlff_gb300 import systems
+    from mlff_gb300.engine import make_batch
+    from mlff_gb300.training import param_grads
+    s = systems.water_box(n_water=60, L=11.5, d_oo=2.2, seed=8)
+    pos32 = s.pos.astype(np.float32)
+    rng = np.random.default_rng(6)
+    w = rng.normal(size=1)
+    G = (0.2 * rng.normal(size=(s.n_atoms, 3))).astype(np.float32)
+    S = rng.normal(size=(1, 3, 3))
+    m = _model(weights_bias)
+    b = make_batch(s.Z, pos32, s.mol_ptr, s.box, s.pbc)
+    pos = pos32.astype(np.float64)
+    _, grads, _ = param_grads(m, b, torch.tensor(w), force_weights=torch.tensor(G), virial_weights=torch.tensor(S))
+    _, _, g0 = painn.param_grads_forces(weights_bias, s.Z, pos, s.mol_ptr, w, G.astype(np.float64), box=s.box,
+                                        pbc=s.pbc, virial_weights=S)
+    worst = _compare_grads(grads, g0, 2e-4)
+    _, gs, _ = param_grads(m, b, torch.zeros(1), virial_weights=torch.tensor(S))
+    _, _, gs0 = painn.param_grads_forces(weights_bias, s.Z, pos, s.mol_ptr, np.zeros(1), None, box=s.box,
+                                         pbc=s.pbc, virial_weights=S)
+    worst_s = _compare_grads(gs, gs0, 2e-4)
+    print(f"worst relative max error: energy+force+strain {worst:.2e}, strain term {worst_s:.2e}")
+
+
+def test_force_field_trainer_with_stress(weights_seed0, weights_bias):
+    """ForceFieldTrainer on periodic boxes with energy, force and stress
+    targets (teacher: float64 oracle with the perturbed weights): the
+    stress term is part of the loss and falls with training."""
+    from mlff_gb300 import systems
+    from mlff_gb300.engine import make_batch
+    from mlff_gb300.training import ForceFieldLoss, ForceFieldTrainer
+    boxes = [systems.water_box(n_water=50, L=11.5, d_oo=2.2, seed=20 + k) for k in range(4)]
+    s = systems.concat(boxes)
+    pos32 = s.pos.astype(np.float32)
+    E0, F0, V0 = painn.energy_forces(weights_bias, s.Z, pos32.astype(np.float64), s.mol_ptr, box=s.box, pbc=s.pbc,
+                                     virial=True)
+    vol = np.prod(s.box, axis=1)
+    sym = 0.5 * (V0.numpy() + V0.numpy().transpose(0, 2, 1)) / vol[:, None, None]
+    S_ref = np.stack([sym[:, 0, 0], sym[:, 1, 1], sym[:, 2, 2], sym[:, 1, 2], sym[:, 0, 2], sym[:, 0, 1]], axis=1)
+    m = _model(weights_seed0)
+    loss = ForceFieldLoss(energy_weight=1.0, force_weight=100.0, stress_weight=1000.0, angular_weight=0.0)
+    tr = ForceFieldTrainer(m, loss, lr=2e-3)
+    b = make_batch(s.Z, pos32, s.mol_ptr, s.box, s.pbc)
+    hist = [tr.step(b, E0.numpy(), F0.numpy(), S_ref) for _ in range(25)]
+    print(f"stress term {hist[0]['stress']:.3e} -> {hist[-1]['stress']:.3e}; "
+          f"total {hist[0]['total']:.3e} -> {hist[-1]['total']:.3e}")
+    assert "stress" in hist[0]
     assert hist[-1]["total"] < 0.5 * hist[0]["total"]
-    assert after["force_rmse"] < 0.7 * before["force_rmse"]
-    assert rmse_inf < 0.7 * before["force_rmse"]
+    assert hist[-1]["stress"] < hist[0]["stress"]

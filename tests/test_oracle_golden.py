@@ -159,7 +159,7 @@ def test_force_loss_grads_match_reference_training_step(weights_bias):
     g = np.load(os.path.join(GOLDEN, "golden_train.npz"))
     E, F = torch.tensor(g["E"]), torch.tensor(g["F"])
     loss = ForceFieldLoss(energy_weight=1.0, force_weight=100.0, stress_weight=0.1, angular_weight=10.0)
-    out, w, G = loss.derivatives(E, F, torch.tensor(g["E_ref"]), torch.tensor(g["F_ref"]))
+    out, w, G, _ = loss.derivatives(E, F, torch.tensor(g["E_ref"]), torch.tensor(g["F_ref"]))
     for key in ["loss", "loss_energy", "loss_force", "loss_angular"]:
         name = "total" if key == "loss" else key.split("_", 1)[1]
         assert abs(float(out[name].detach()) - float(g[key])) <= 1e-12 * max(1.0, abs(float(g[key]))), key
@@ -177,3 +177,29 @@ def test_force_loss_grads_match_reference_training_step(weights_bias):
         val = g[f"grad/{k}/val"]
         err = np.abs(got[g[f"grad/{k}/idx"]] - val).max()
         assert err <= 1e-6 * max(np.abs(val).max(), ref_norm / np.sqrt(got.size)) + 1e-12, (k, err)
+
+
+def test_oracle_strain_second_order_matches_finite_differences(weights_bias):
+    """The oracle's stress-loss parameter gradients sum_ab S_ab dW_ab/dtheta
+    (W = dE/d(strain) taken with create_graph=True) against central
+    differences of S : W over a few parameters, on a small periodic box."""
+    from mlff_gb300 import systems
+    s = systems.water_box(n_water=40, L=11.0, d_oo=2.2, seed=3)
+    pos = s.pos.astype(np.float32).astype(np.float64)
+    S = np.random.default_rng(4).normal(size=(1, 3, 3))
+    _, _, g = painn.param_grads_forces(weights_bias, s.Z, pos, s.mol_ptr, np.zeros(1), None, box=s.box,
+                                       pbc=s.pbc, virial_weights=S)
+    rng = np.random.default_rng(5)
+    for key in ["interactions.0.message.rbf_to_scalar.0.weight", "interactions.2.update.update_mlp.2.bias",
+                "energy_head.0.weight"]:
+        idx = tuple(int(rng.integers(0, n)) for n in weights_bias[key].shape)
+        h = 1e-5
+        vals = []
+        for sgn in (1, -1):
+            W = {k: v.copy() for k, v in weights_bias.items()}
+            W[key] = W[key].astype(np.float64)
+            W[key][idx] += sgn * h
+            _, _, V = painn.energy_forces(W, s.Z, pos, s.mol_ptr, box=s.box, pbc=s.pbc, virial=True)
+            vals.append(float((V.numpy() * S).sum()))
+        fd = (vals[0] - vals[1]) / (2 * h)
+        assert abs(fd - float(g[key][idx])) <= 1e-6 + 1e-5 * abs(fd), (key, idx, fd, float(g[key][idx]))
