@@ -223,6 +223,46 @@ int mlff_langevin_steps(const mlff_dims *dims, const void *packed, const mlff_sy
                         double friction, double kT, uint64_t seed, int32_t n_steps, void *workspace,
                         size_t workspace_bytes, mlff_stream_t stream);
 
+/* NPT state beyond mlff_md_state, per structure (all device memory):
+ * box float64 [B,3] edge lengths and box32 float32 [B,3] (the copy the
+ * force call reads; both updated every step), zeta [B] thermostat rate,
+ * eta [B,3] diagonal barostat strain rate (1 / ASE time unit), xi [B] the
+ * time integral of zeta (for the conserved quantity), virial [B,3,3]
+ * dE/d(strain) at the current positions (in and out, like forces). */
+typedef struct {
+    double *box;
+    float *box32;
+    double *zeta;
+    double *eta;
+    double *xi;
+    double *virial;
+} mlff_npt_state;
+
+/* NPT steps (isothermal-isobaric) with the equations of motion of ASE's NPT
+ * (Nose-Hoover thermostat + Parrinello-Rahman barostat, Melchionna et al.,
+ * Mol. Phys. 78, 533 (1993)) that the reference's NPT protocol runs
+ * (benchmarks/md_trajectory.py:415-424: ttime 25 fs, pfactor 75 fs^2,
+ * externalstress 0), for orthorhombic periodic boxes (diagonal strain
+ * rate):
+ *   dr/dt = v + eta (r - R_com),  dv/dt = F/m - (zeta + eta) v,
+ *   dzeta/dt = (2 K / (3 n kT) - 1) / ttime^2,
+ *   deta/dt = V / pfactor (diag(sum m v v - W) / V - pressure),
+ *   dL/dt = eta L,
+ * integrated by a time-reversible splitting (half step of zeta and eta,
+ * velocity scaling and half kick, exact drift of positions and box, force
+ * and virial, half kick and scaling, half step of zeta and eta).  Conserved:
+ *   E + K + pressure V + 3 n kT (ttime^2 zeta^2 / 2 + xi) + pfactor |eta|^2 / 2.
+ * ttime = 0 turns the thermostat off, pfactor = 0 the barostat.  Units as
+ * mlff_verlet_steps (ttime in ASE time units, pfactor in eV (ASE time)^2 /
+ * A^3 -- ASE's pfactor -- pressure in eV/A^3, kT in eV).  sys->pbc must mark
+ * every structure periodic; the force call reads npt->box32 (sys->box is
+ * ignored).  Traces, workspace and status as mlff_verlet_steps.  Parity with
+ * ASE's own discretisation is not claimed (ASE is not vendored). */
+int mlff_npt_steps(const mlff_dims *dims, const void *packed, const mlff_system *sys, int64_t edge_capacity,
+                   int32_t path, mlff_md_state *state, mlff_npt_state *npt, double dt, double kT, double ttime,
+                   double pfactor, double pressure, int32_t n_steps, void *workspace, size_t workspace_bytes,
+                   mlff_stream_t stream);
+
 /* Per-replica energy-conservation statistics of an MD energy trace, the
  * report of testing/energy_metrics.py:48-357 (compute_energy_drift,
  * compute_energy_conservation_ratio, compute_energy_fluctuations,

@@ -5,6 +5,7 @@
 #include <cstring>
 #include <algorithm>
 #include <cstdlib>
+#include <cmath>
 #include "common.cuh"
 #include "workspace.h"
 
@@ -187,6 +188,11 @@ int md_energy_stats(const double* epot, const double* ekin, int32_t n, int32_t B
                     double dt_ps, double* out, cudaStream_t st);
 int md_kick(const WsLayout& L, void* ws, mlff_md_state* s, double dt, const int64_t* mol_ptr, int32_t n_mol,
             bool kinetic, cudaStream_t st);
+int md_npt_open(const WsLayout& L, void* ws, const mlff_md_state* s, const mlff_npt_state* n, double dt, double kT,
+                double ttime, double pfactor, double pext, const int64_t* mol_ptr, int32_t n_mol, cudaStream_t st);
+int md_npt_close(const WsLayout& L, void* ws, const mlff_md_state* s, const mlff_npt_state* n, double dt, double kT,
+                 double ttime, double pfactor, double pext, const int64_t* mol_ptr, int32_t n_mol, double* kinetic,
+                 cudaStream_t st);
 }  // namespace mlff
 
 using namespace mlff;
@@ -337,6 +343,63 @@ int mlff_langevin_steps(const mlff_dims* dims, const void* packed, const mlff_sy
                         int32_t n_steps, void* workspace, size_t workspace_bytes, mlff_stream_t stream) {
     return md_steps(dims, packed, sys, edge_capacity, path, state, dt, true, friction, kT, seed, n_steps, workspace,
                     workspace_bytes, stream);
+}
+
+int mlff_npt_steps(const mlff_dims* dims, const void* packed, const mlff_system* sys, int64_t edge_capacity,
+                   int32_t path, mlff_md_state* state, mlff_npt_state* npt, double dt, double kT, double ttime,
+                   double pfactor, double pressure, int32_t n_steps, void* workspace, size_t workspace_bytes,
+                   mlff_stream_t stream) {
+    if (!sys || !state || !state->pos || !state->vel || !state->inv_mass || !state->forces || !state->energy) {
+        set_error("system and md state (pos, vel, inv_mass, forces, energy) are required");
+        return MLFF_ERR_INVALID;
+    }
+    if (!npt || !npt->box || !npt->box32 || !npt->zeta || !npt->eta || !npt->xi || !npt->virial || !sys->pbc) {
+        set_error("NPT state (box, box32, zeta, eta, xi, virial) and periodic flags are required");
+        return MLFF_ERR_INVALID;
+    }
+    if (n_steps < 0 || !(dt > 0.0) || !(ttime >= 0.0) || !(pfactor >= 0.0) || !(kT >= 0.0) ||
+        (ttime > 0.0 && !(kT > 0.0)) || !std::isfinite(pressure)) {
+        set_error("NPT needs n_steps >= 0, dt > 0, ttime >= 0, pfactor >= 0, kT > 0 with a thermostat, "
+                  "finite pressure");
+        return MLFF_ERR_INVALID;
+    }
+    if (!packed) { set_error("packed weights are required"); return MLFF_ERR_INVALID; }
+    mlff_system s2 = *sys;
+    s2.box = npt->box32;
+    WsLayout L;
+    {
+        const float* keep = s2.pos;
+        s2.pos = reinterpret_cast<const float*>(workspace);   // placeholder for the check
+        int r = prepare(dims, &s2, edge_capacity, path, workspace, workspace_bytes, L);
+        s2.pos = keep;
+        if (r) return r;
+    }
+    s2.pos = ws_ptr<float>(workspace, L.md_pos32);
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    MLFF_CUDA(cudaMemsetAsync(ws_ptr<Status>(workspace, L.status), 0, sizeof(Status), st));
+    const int64_t B = sys->n_mol;
+    int r;
+    for (int s = 0; s < n_steps; ++s) {
+        const bool last = s == n_steps - 1;
+        mlff_outputs out{state->energy_trace && !last ? state->energy_trace + s * B : state->energy, state->forces,
+                         npt->virial, nullptr};
+        double* ke = state->kinetic_trace ? state->kinetic_trace + s * B : state->kinetic;
+        if ((r = md_npt_open(L, workspace, state, npt, dt, kT, ttime, pfactor, pressure, sys->mol_ptr, sys->n_mol, st)))
+            return r;
+        if ((r = energy_forces_impl(*dims, packed, s2, L, path, out, workspace, st))) return r;
+        if ((r = md_npt_close(L, workspace, state, npt, dt, kT, ttime, pfactor, pressure, sys->mol_ptr, sys->n_mol,
+                              (last || state->kinetic_trace) ? ke : nullptr, st)))
+            return r;
+        if (last) {
+            if (state->energy_trace)
+                MLFF_CUDA(cudaMemcpyAsync(state->energy_trace + s * B, state->energy, sizeof(double) * B,
+                                          cudaMemcpyDeviceToDevice, st));
+            if (state->kinetic_trace && state->kinetic)
+                MLFF_CUDA(cudaMemcpyAsync(state->kinetic, state->kinetic_trace + s * B, sizeof(double) * B,
+                                          cudaMemcpyDeviceToDevice, st));
+        }
+    }
+    return MLFF_OK;
 }
 
 int mlff_md_energy_stats(const double* epot, const double* ekin, int32_t n_samples, int32_t n_mol,

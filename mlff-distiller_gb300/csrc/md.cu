@@ -1,5 +1,5 @@
-// Velocity-Verlet NVE and Langevin (BAOAB) NVT integrator kernels, float64
-// state.  One Verlet step is
+// Velocity-Verlet NVE, Langevin (BAOAB) NVT and Nose-Hoover /
+// Parrinello-Rahman NPT integrator kernels, float64 state.  One Verlet step is
 //   v += dt/2 F/m ; r += dt v ; (float32 copy of r) -> F(r) ; v += dt/2 F/m
 // which is what ASE's VelocityVerlet does per step when driven by
 // NVEMDHarness.run_simulation (src/mlff_distiller/testing/nve_harness.py:
@@ -153,6 +153,218 @@ int md_kick(const WsLayout& L, void* ws, mlff_md_state* s, double dt, const int6
     return MLFF_OK;
 }
 
+
+// ----------------------------------------------------------------- NPT
+// Isothermal-isobaric dynamics with the equations of motion of ASE's NPT
+// (Nose-Hoover thermostat and Parrinello-Rahman barostat, Melchionna,
+// Ciccotti and Holian, Mol. Phys. 78, 533 (1993)), for orthorhombic boxes
+// (diagonal strain rate eta), per structure:
+//   dr/dt = v + eta (r - R0)        R0 = centre of mass
+//   dv/dt = F/m - (zeta + eta) v
+//   dzeta/dt = (2 K / (g kT) - 1) / ttime^2           g = 3 n
+//   deta_a/dt = V / pfactor (P_aa - P_ext),  P_aa = (sum m v_a^2 - W_aa) / V
+//   dL_a/dt = eta_a L_a
+// with W = dE/d(strain), the virial the force call returns.  These conserve
+//   H = E + K + P_ext V + g kT (ttime^2 zeta^2 / 2 + xi) + pfactor |eta|^2 / 2,
+// dxi/dt = zeta.  Time-reversible splitting per step: half step of zeta,
+// eta (and xi); v scaled by exp(-(zeta + eta) dt/2) and half-kicked; the
+// drift solved exactly for constant v (positions relative to the moving
+// centre of mass scale by exp(eta dt), boxes too); forces and virial; half
+// kick, scaling and half step of the extended variables with the new
+// kinetic tensor and virial.  ttime = 0 switches the thermostat off,
+// pfactor = 0 the barostat.  One block per structure, fixed-order sums.
+constexpr int NPT_NT = 256;
+
+struct NptArgs {
+    double* pos;
+    double* vel;
+    const double* inv_mass;
+    const float* F;
+    const double* virial;    // [B][9]
+    double* box;             // [B][3] float64 master copy
+    float* box32;            // [B][3] what the force call reads
+    double* zeta;            // [B]
+    double* eta;             // [B][3]
+    double* xi;              // [B]
+    double* kinetic;         // [B] or NULL
+    const int64_t* mol_ptr;
+    int32_t n_mol;
+    double dt, kT, ttime, pfactor, pext;
+    float* pos32;
+    Status* st;
+};
+
+__device__ double npt_block_sum(double v, double* red) {
+    red[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = NPT_NT / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    const double r = red[0];
+    __syncthreads();
+    return r;
+}
+
+// kinetic tensor diagonal sum m v_a^2 of structure m's atoms [a0, a1)
+__device__ void npt_kinetic_diag(const NptArgs& a, int64_t a0, int64_t a1, double* red, double K[3]) {
+    double k[3] = {0.0, 0.0, 0.0};
+    for (int64_t i = a0 + threadIdx.x; i < a1; i += NPT_NT) {
+        const double m = 1.0 / a.inv_mass[i];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) k[d] += m * a.vel[3 * i + d] * a.vel[3 * i + d];
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) K[d] = npt_block_sum(k[d], red);
+}
+
+// half step of zeta and eta from the kinetic tensor K and virial W (thread 0)
+__device__ void npt_half_extended(const NptArgs& a, int m, const double K[3], double n_atoms) {
+    const double* L = a.box + 3 * m;
+    const double V = L[0] * L[1] * L[2];
+    const double h = 0.5 * a.dt;
+    if (a.ttime > 0.0) {
+        const double g = 3.0 * n_atoms;
+        a.zeta[m] += h * ((K[0] + K[1] + K[2]) / (g * a.kT) - 1.0) / (a.ttime * a.ttime);
+    }
+    if (a.pfactor > 0.0) {
+        const double* W = a.virial + 9 * m;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) a.eta[3 * m + d] += h * (V / a.pfactor) * ((K[d] - W[4 * d]) / V - a.pext);
+    }
+}
+
+// exp(x) - 1 over x, 1 at x = 0
+__device__ __forceinline__ double expm1_over(double x) { return fabs(x) < 1e-12 ? 1.0 + 0.5 * x : expm1(x) / x; }
+
+// extended half step, thermostat/barostat scaling, half kick, exact drift
+__global__ void __launch_bounds__(NPT_NT) npt_open_kernel(NptArgs a) {
+    pdl_wait();
+    pdl_trigger();
+    __shared__ double red[NPT_NT];
+    __shared__ double sh[8];
+    if (a.st->code != 0) return;
+    for (int m = blockIdx.x; m < a.n_mol; m += gridDim.x) {
+        const int64_t a0 = a.mol_ptr[m], a1 = a.mol_ptr[m + 1];
+        double K[3];
+        npt_kinetic_diag(a, a0, a1, red, K);
+        if (threadIdx.x == 0) {
+            npt_half_extended(a, m, K, (double)(a1 - a0));
+            a.xi[m] += 0.5 * a.dt * a.zeta[m];
+            sh[0] = a.zeta[m];
+            sh[1] = a.eta[3 * m];
+            sh[2] = a.eta[3 * m + 1];
+            sh[3] = a.eta[3 * m + 2];
+        }
+        __syncthreads();
+        const double zeta = sh[0], eta[3] = {sh[1], sh[2], sh[3]};
+        double scale[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) scale[d] = exp(-0.5 * a.dt * (zeta + eta[d]));
+        // scaled, half-kicked velocities; mass-weighted sums of positions and velocities
+        double s[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        for (int64_t i = a0 + threadIdx.x; i < a1; i += NPT_NT) {
+            const double m_i = 1.0 / a.inv_mass[i];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const double v = a.vel[3 * i + d] * scale[d] + 0.5 * a.dt * (double)a.F[3 * i + d] * a.inv_mass[i];
+                a.vel[3 * i + d] = v;
+                s[d] += m_i * a.pos[3 * i + d];
+                s[3 + d] += m_i * v;
+            }
+            s[6] += m_i;
+        }
+        double t[7];
+#pragma unroll
+        for (int k = 0; k < 7; ++k) t[k] = npt_block_sum(s[k], red);
+        const double R0[3] = {t[0] / t[6], t[1] / t[6], t[2] / t[6]};
+        const double vc[3] = {t[3] / t[6], t[4] / t[6], t[5] / t[6]};
+        double ex[3], ph[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            ex[d] = exp(eta[d] * a.dt);
+            ph[d] = a.dt * expm1_over(eta[d] * a.dt);
+        }
+        // r - R0(t) scales by exp(eta dt) while moving with v - v_com; R0 moves with v_com
+        for (int64_t i = a0 + threadIdx.x; i < a1; i += NPT_NT) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const double r = R0[d] + vc[d] * a.dt + ex[d] * (a.pos[3 * i + d] - R0[d]) +
+                                 (a.vel[3 * i + d] - vc[d]) * ph[d];
+                a.pos[3 * i + d] = r;
+                a.pos32[3 * i + d] = (float)r;
+            }
+        }
+        if (threadIdx.x < 3) {
+            const double Lb = a.box[3 * m + threadIdx.x] * ex[threadIdx.x];
+            a.box[3 * m + threadIdx.x] = Lb;
+            a.box32[3 * m + threadIdx.x] = (float)Lb;
+            // a box that changes by more than 20 % in one step (or stops being finite) means the
+            // barostat has run away (pfactor far too small for the system): stop with an error
+            if (!(fabs(eta[threadIdx.x] * a.dt) < 0.2) || !isfinite(Lb)) set_status(a.st, MLFF_ERR_BOX, m);
+        }
+        __syncthreads();
+    }
+}
+
+// half kick, scaling, extended half step with the new virial; kinetic energy
+__global__ void __launch_bounds__(NPT_NT) npt_close_kernel(NptArgs a) {
+    pdl_wait();
+    pdl_trigger();
+    __shared__ double red[NPT_NT];
+    if (a.st->code != 0) return;
+    for (int m = blockIdx.x; m < a.n_mol; m += gridDim.x) {
+        const int64_t a0 = a.mol_ptr[m], a1 = a.mol_ptr[m + 1];
+        const double zeta = a.zeta[m];
+        double scale[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) scale[d] = exp(-0.5 * a.dt * (zeta + a.eta[3 * m + d]));
+        for (int64_t i = a0 + threadIdx.x; i < a1; i += NPT_NT) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+                a.vel[3 * i + d] = (a.vel[3 * i + d] + 0.5 * a.dt * (double)a.F[3 * i + d] * a.inv_mass[i]) * scale[d];
+        }
+        __syncthreads();
+        double K[3];
+        npt_kinetic_diag(a, a0, a1, red, K);
+        if (threadIdx.x == 0) {
+            a.xi[m] += 0.5 * a.dt * a.zeta[m];
+            npt_half_extended(a, m, K, (double)(a1 - a0));
+            if (a.kinetic) a.kinetic[m] = 0.5 * (K[0] + K[1] + K[2]);
+        }
+        __syncthreads();
+    }
+}
+
+static NptArgs npt_args(const WsLayout& L, void* ws, const mlff_md_state* s, const mlff_npt_state* n, double dt,
+                        double kT, double ttime, double pfactor, double pext, const int64_t* mol_ptr, int32_t n_mol,
+                        double* kinetic) {
+    NptArgs a;
+    a.pos = s->pos; a.vel = s->vel; a.inv_mass = s->inv_mass; a.F = s->forces;
+    a.virial = n->virial; a.box = n->box; a.box32 = n->box32; a.zeta = n->zeta; a.eta = n->eta; a.xi = n->xi;
+    a.kinetic = kinetic; a.mol_ptr = mol_ptr; a.n_mol = n_mol;
+    a.dt = dt; a.kT = kT; a.ttime = ttime; a.pfactor = pfactor; a.pext = pext;
+    a.pos32 = ws_ptr<float>(ws, L.md_pos32);
+    a.st = ws_ptr<Status>(ws, L.status);
+    return a;
+}
+
+int md_npt_open(const WsLayout& L, void* ws, const mlff_md_state* s, const mlff_npt_state* n, double dt, double kT,
+                double ttime, double pfactor, double pext, const int64_t* mol_ptr, int32_t n_mol, cudaStream_t st) {
+    ProfScope prof(PK_MD, st);
+    NptArgs a = npt_args(L, ws, s, n, dt, kT, ttime, pfactor, pext, mol_ptr, n_mol, nullptr);
+    MLFF_LAUNCH_PDL("npt_open", npt_open_kernel, std::min(std::max(n_mol, 1), 152 * 8), NPT_NT, 0, st, a);
+    return MLFF_OK;
+}
+
+int md_npt_close(const WsLayout& L, void* ws, const mlff_md_state* s, const mlff_npt_state* n, double dt, double kT,
+                 double ttime, double pfactor, double pext, const int64_t* mol_ptr, int32_t n_mol, double* kinetic,
+                 cudaStream_t st) {
+    ProfScope prof(PK_MD, st);
+    NptArgs a = npt_args(L, ws, s, n, dt, kT, ttime, pfactor, pext, mol_ptr, n_mol, kinetic);
+    MLFF_LAUNCH_PDL("npt_close", npt_close_kernel, std::min(std::max(n_mol, 1), 152 * 8), NPT_NT, 0, st, a);
+    return MLFF_OK;
+}
 
 // --------------------------------------------------- energy statistics
 // Per-replica NVE statistics of an energy trace, the quantities of the

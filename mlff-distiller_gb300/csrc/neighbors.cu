@@ -233,6 +233,8 @@ __global__ void mol_grid_kernel(const int64_t* __restrict__ mol_ptr, const float
                 nc[0] = nc[1] = nc[2] = 1;
             }
             int lim = max(n_m, 27);
+            // no axis needs more cells than lim; this also keeps the product below 2^63 for huge boxes
+            for (int a = 0; a < 3; ++a) nc[a] = min(nc[a], lim);
             while ((long long)nc[0] * nc[1] * nc[2] > lim) {
                 int a = (nc[0] >= nc[1] && nc[0] >= nc[2]) ? 0 : (nc[1] >= nc[2] ? 1 : 2);
                 nc[a] -= 1;

@@ -41,7 +41,8 @@ ERROR_NAMES = {ERR_INVALID: "invalid argument", ERR_CAPACITY: "edge capacity exc
 
 EXPORTS = ["mlff_version", "mlff_last_error_string", "mlff_packed_weights_size", "mlff_pack_weights",
            "mlff_workspace_size", "mlff_build_neighbors", "mlff_copy_neighbors", "mlff_energy_forces",
-           "mlff_read_status", "mlff_clear_status", "mlff_verlet_steps", "mlff_langevin_steps", "mlff_md_energy_stats",
+           "mlff_read_status", "mlff_clear_status", "mlff_verlet_steps", "mlff_langevin_steps", "mlff_npt_steps",
+           "mlff_md_energy_stats",
            "mlff_profile_begin",
            "mlff_profile_end", "mlff_radius_graph_noalloc", "mlff_param_grads", "mlff_param_grads_forces"]
 
@@ -83,6 +84,10 @@ class Outputs(ctypes.Structure):
 class MDState(ctypes.Structure):
     _fields_ = [("pos", _P), ("vel", _P), ("inv_mass", _P), ("forces", _P), ("energy", _P),
                 ("kinetic", _P), ("energy_trace", _P), ("kinetic_trace", _P), ("step_counter", _P)]
+
+
+class NPTState(ctypes.Structure):
+    _fields_ = [("box", _P), ("box32", _P), ("zeta", _P), ("eta", _P), ("xi", _P), ("virial", _P)]
 
 
 class MLFFError(RuntimeError):
@@ -144,6 +149,11 @@ def load(build_if_missing: bool = True):
         lib.mlff_langevin_steps.argtypes = [ctypes.POINTER(Dims), _P, ctypes.POINTER(System), i64, i32,
                                             ctypes.POINTER(MDState), ctypes.c_double, ctypes.c_double,
                                             ctypes.c_double, ctypes.c_uint64, i32, _P, sz, _P]
+        lib.mlff_npt_steps.restype = ctypes.c_int
+        lib.mlff_npt_steps.argtypes = [ctypes.POINTER(Dims), _P, ctypes.POINTER(System), i64, i32,
+                                       ctypes.POINTER(MDState), ctypes.POINTER(NPTState), ctypes.c_double,
+                                       ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, i32, _P,
+                                       sz, _P]
         lib.mlff_md_energy_stats.restype = ctypes.c_int
         lib.mlff_md_energy_stats.argtypes = [_P, _P, i32, i32, _P, ctypes.c_double, _P, _P]
         lib.mlff_profile_begin.restype = ctypes.c_int

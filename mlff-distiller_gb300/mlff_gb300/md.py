@@ -11,7 +11,10 @@ costs no host round trip.
 ``set_langevin`` (or ``LangevinGPU``) switches the same driver to Langevin
 NVT dynamics (BAOAB splitting, ``mlff_langevin_steps``), the protocol the
 reference's MD benchmark runs through ASE's Langevin
-(benchmarks/md_trajectory.py:400-413).
+(benchmarks/md_trajectory.py:400-413); ``set_npt`` (or ``NPTGPU``) to NPT
+with the equations of motion of ASE's NPT (Nose-Hoover thermostat,
+Parrinello-Rahman barostat; ``mlff_npt_steps``), the reference's NPT
+protocol (:415-424), on orthorhombic periodic boxes.
 
 ``NVEMDHarness`` mirrors the reference's harness
 (testing/nve_harness.py:57-380: Maxwell-Boltzmann start at T, zero
@@ -117,6 +120,8 @@ class VelocityVerletGPU:
         self._forces_valid = False
         self.step_counter = torch.zeros(1, dtype=torch.int64, device=d)   # keys the Langevin draws
         self.thermostat: Optional[Dict[str, float]] = None
+        self.npt: Optional[Dict[str, float]] = None
+        self.box64 = self.zeta = self.eta = self.xi = self.virial = None
 
     def set_langevin(self, temperature_K: float, friction: float = 0.01, seed: int = 0):
         """Langevin NVT from now on: ``friction`` in inverse ASE time units
@@ -127,8 +132,51 @@ class VelocityVerletGPU:
             return
         if friction < 0 or temperature_K < 0:
             raise ValueError("friction and temperature must be non-negative")
+        self.npt = None
         self.thermostat = {"friction": float(friction), "kT": float(units.kB * temperature_K),
                            "seed": int(seed) & 0xFFFFFFFFFFFFFFFF}
+
+    def set_npt(self, temperature_K: Optional[float], externalstress: float = 0.0, ttime: float = 25.0 * units.fs,
+                pfactor: float = 75.0 * units.fs ** 2):
+        """NPT from now on, with ASE NPT's arguments (the reference's NPT
+        protocol: ttime 25 fs, pfactor 75 fs^2, externalstress 0): ttime
+        (ASE time units; 0 = no thermostat), pfactor (eV (ASE time)^2 / A^3;
+        0 = no barostat), externalstress a scalar pressure in eV/A^3.  Every
+        structure must be an orthorhombic periodic box.  ``None``
+        temperature switches back to NVE (the box keeps its size)."""
+        if temperature_K is None:
+            self.npt = None
+            return
+        if self.box is None or self.pbc is None or not bool(self.pbc.bool().all()):
+            raise ValueError("NPT needs every structure periodic (box and pbc)")
+        if temperature_K < 0 or ttime < 0 or pfactor < 0 or (ttime > 0 and temperature_K <= 0):
+            raise ValueError("NPT needs ttime >= 0, pfactor >= 0 and a positive temperature with a thermostat")
+        self.thermostat = None
+        self.npt = {"kT": float(units.kB * temperature_K), "ttime": float(ttime), "pfactor": float(pfactor),
+                    "pressure": float(externalstress)}
+        if self.box64 is None:
+            d = self.dev
+            self.box64 = self.box.to(torch.float64).clone()
+            self.zeta = torch.zeros(self.B, dtype=torch.float64, device=d)
+            self.eta = torch.zeros(self.B, 3, dtype=torch.float64, device=d)
+            self.xi = torch.zeros(self.B, dtype=torch.float64, device=d)
+            self.virial = torch.zeros(self.B, 3, 3, dtype=torch.float64, device=d)
+        self._forces_valid = False   # the first NPT step needs the virial
+
+    def volumes(self) -> np.ndarray:
+        """Box volumes [B] (A^3)."""
+        b = self.box64 if self.box64 is not None else self.box.to(torch.float64)
+        return torch.prod(b, dim=1).cpu().numpy()
+
+    def npt_conserved(self) -> np.ndarray:
+        """Per structure E + K + P V + 3 n kT (ttime^2 zeta^2 / 2 + xi) +
+        pfactor |eta|^2 / 2, the quantity the NPT equations conserve."""
+        p = self.npt
+        n = np.diff(self.mol_ptr_np).astype(np.float64)
+        zeta, xi, eta = self.zeta.cpu().numpy(), self.xi.cpu().numpy(), self.eta.cpu().numpy()
+        return (self.energy.cpu().numpy() + self.kinetic.cpu().numpy() + p["pressure"] * self.volumes() +
+                3.0 * n * p["kT"] * (0.5 * p["ttime"] ** 2 * zeta ** 2 + xi) +
+                0.5 * p["pfactor"] * (eta * eta).sum(axis=1))
 
     # state
     def set_velocities(self, vel):
@@ -147,15 +195,22 @@ class VelocityVerletGPU:
     def snapshot(self) -> Dict[str, torch.Tensor]:
         """Device copies of the integrator state (positions, velocities,
         forces, energies, step count) for restore()."""
-        return {"pos": self.pos.clone(), "vel": self.vel.clone(), "forces": self.forces.clone(),
+        snap = {"pos": self.pos.clone(), "vel": self.vel.clone(), "forces": self.forces.clone(),
                 "energy": self.energy.clone(), "kinetic": self.kinetic.clone(), "steps_done": self.steps_done,
                 "forces_valid": self._forces_valid, "step_counter": self.step_counter.clone()}
+        for k in self._NPT_KEYS:
+            if getattr(self, k) is not None:
+                snap[k] = getattr(self, k).clone()
+        return snap
+
+    _NPT_KEYS = ("box", "box64", "zeta", "eta", "xi", "virial")
 
     def restore(self, snap: Dict[str, torch.Tensor]):
         """Put a snapshot() back in place (the captured graphs keep working:
         the state tensors are updated in place)."""
-        for k in ("pos", "vel", "forces", "energy", "kinetic", "step_counter"):
-            getattr(self, k).copy_(snap[k])
+        for k in ("pos", "vel", "forces", "energy", "kinetic", "step_counter") + self._NPT_KEYS:
+            if k in snap and getattr(self, k) is not None:
+                getattr(self, k).copy_(snap[k])
         self.steps_done = snap["steps_done"]
         self._forces_valid = snap["forces_valid"]
 
@@ -174,9 +229,11 @@ class VelocityVerletGPU:
     def compute_forces(self):
         """Energy and forces at the current positions (eager, with the
         edge-capacity check), the start of a trajectory."""
-        E, F, _ = self.engine.energy_forces(self._batch(), self.path, forces=True)
+        E, F, V = self.engine.energy_forces(self._batch(), self.path, forces=True, virial=self.npt is not None)
         self.energy.copy_(E)
         self.forces.copy_(F)
+        if V is not None:
+            self.virial.copy_(V)
         self.kinetic.copy_(torch.as_tensor(kinetic_energy(self.velocities(), self.masses, self.mol_ptr_np),
                                            device=self.dev))
         self._forces_valid = True
@@ -193,7 +250,19 @@ class VelocityVerletGPU:
         st.step_counter = self.step_counter.data_ptr()
         sysd = self._batch_sys
         th = self.thermostat
-        if th is None:
+        if self.npt is not None:
+            p = self.npt
+            ns = _lib.NPTState()
+            ns.box, ns.box32 = self.box64.data_ptr(), self.box.data_ptr()
+            ns.zeta, ns.eta, ns.xi, ns.virial = (self.zeta.data_ptr(), self.eta.data_ptr(), self.xi.data_ptr(),
+                                                 self.virial.data_ptr())
+            _lib.check(self.lib.mlff_npt_steps(ctypes.byref(self.engine.dims), self.engine.packed.data_ptr(),
+                                               ctypes.byref(sysd), cap, self.path, ctypes.byref(st), ctypes.byref(ns),
+                                               ctypes.c_double(self.dt), ctypes.c_double(p["kT"]),
+                                               ctypes.c_double(p["ttime"]), ctypes.c_double(p["pfactor"]),
+                                               ctypes.c_double(p["pressure"]), n_steps, ws.data_ptr(), ws.numel(),
+                                               _stream_handle()))
+        elif th is None:
             _lib.check(self.lib.mlff_verlet_steps(ctypes.byref(self.engine.dims), self.engine.packed.data_ptr(),
                                                   ctypes.byref(sysd), cap, self.path, ctypes.byref(st),
                                                   ctypes.c_double(self.dt), n_steps, ws.data_ptr(), ws.numel(),
@@ -253,7 +322,8 @@ class VelocityVerletGPU:
     def _graph(self, k: int, cap: int, record: bool):
         ws = self.engine.workspace_for(self.N, self.B, cap, self.path)
         th = self.thermostat
-        key = (k, cap, record, ws.data_ptr(), None if th is None else (th["friction"], th["kT"], th["seed"]))
+        key = (k, cap, record, ws.data_ptr(), None if th is None else (th["friction"], th["kT"], th["seed"]),
+               None if self.npt is None else tuple(sorted(self.npt.items())))
         if key in self._graphs:
             return self._graphs[key]
         # a graph holds the workspace address it was captured with
@@ -278,6 +348,21 @@ class LangevinGPU(VelocityVerletGPU):
                  seed: int = 0, timestep_fs: float = 0.5, **kwargs):
         super().__init__(model, numbers, positions, mol_ptr, timestep_fs=timestep_fs, **kwargs)
         self.set_langevin(temperature_K, friction, seed)
+
+
+class NPTGPU(VelocityVerletGPU):
+    """NPT driver with ASE NPT's arguments (timestep in fs, temperature_K,
+    externalstress in eV/A^3, ttime, pfactor): the reference's NPT protocol
+    (benchmarks/md_trajectory.py:415-424) on the fused GPU step, for
+    orthorhombic periodic boxes (box [B,3])."""
+
+    def __init__(self, model, numbers, positions, mol_ptr, box, temperature_K: float, externalstress: float = 0.0,
+                 ttime: float = 25.0 * units.fs, pfactor: float = 75.0 * units.fs ** 2, timestep_fs: float = 0.5,
+                 **kwargs):
+        B = len(np.asarray(mol_ptr)) - 1
+        super().__init__(model, numbers, positions, mol_ptr, box=box, pbc=np.ones(B, bool), timestep_fs=timestep_fs,
+                         **kwargs)
+        self.set_npt(temperature_K, externalstress, ttime, pfactor)
 
 
 # ----------------------------------------------------------------- harness

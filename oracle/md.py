@@ -68,3 +68,74 @@ def langevin_baoab(pos: np.ndarray, vel: np.ndarray, masses: np.ndarray,
         epot[s] = e
         ekin[s] = [ke[mol_ptr[b]:mol_ptr[b + 1]].sum() for b in range(B)]
     return r, v, F, epot, ekin
+
+
+def npt_melchionna(pos: np.ndarray, vel: np.ndarray, masses: np.ndarray, box: np.ndarray,
+                   force_fn: Callable[[np.ndarray, np.ndarray], Tuple[float, np.ndarray, np.ndarray]], dt: float,
+                   kT: float, ttime: float, pfactor: float, pressure: float, n_steps: int,
+                   zeta: float = 0.0, eta=None, xi: float = 0.0):
+    """Float64 NPT for one orthorhombic periodic structure with the
+    equations of motion of ASE's NPT (Melchionna, Ciccotti and Holian, Mol.
+    Phys. 78, 533 (1993); diagonal strain rate):
+        dr/dt = v + eta (r - R_com),  dv/dt = F/m - (zeta + eta) v,
+        dzeta/dt = (2K / (3 n kT) - 1) / ttime^2,
+        deta/dt = V / pfactor (diag(sum m v v - W) / V - pressure),  dL/dt = eta L,
+    W = dE/d(strain), and the time-reversible splitting the GPU integrator
+    uses: half step of zeta (then xi += dt/2 zeta) and eta; v scaled by
+    exp(-(zeta + eta) dt/2) and half-kicked; exact drift for constant v of
+    positions relative to the moving centre of mass and of the box; force
+    and virial; half kick and scaling; xi += dt/2 zeta, half step of zeta
+    and eta.  force_fn(pos, box) -> (E, F [n,3], W [3,3]).  Returns the
+    final state and per-step potential energy, kinetic energy, volume,
+    zeta, eta and xi."""
+    r = np.array(pos, dtype=np.float64)
+    v = np.array(vel, dtype=np.float64)
+    L = np.array(box, dtype=np.float64).reshape(3)
+    m = np.asarray(masses, dtype=np.float64)[:, None]
+    eta = np.zeros(3) if eta is None else np.array(eta, dtype=np.float64)
+    n = r.shape[0]
+    g = 3.0 * n
+    E, F, W = force_fn(r, L)
+    out = {"epot": np.zeros(n_steps), "ekin": np.zeros(n_steps), "volume": np.zeros(n_steps),
+           "zeta_t": np.zeros(n_steps), "eta_t": np.zeros((n_steps, 3)), "xi_t": np.zeros(n_steps)}
+
+    def half(zeta, eta, K):
+        V = float(np.prod(L))
+        if ttime > 0:
+            zeta = zeta + 0.5 * dt * (K.sum() / (g * kT) - 1.0) / ttime ** 2
+        if pfactor > 0:
+            eta = eta + 0.5 * dt * (V / pfactor) * ((K - np.diag(W)) / V - pressure)
+        return zeta, eta
+
+    for s in range(n_steps):
+        K = (m * v * v).sum(axis=0)
+        zeta, eta = half(zeta, eta, K)
+        xi += 0.5 * dt * zeta
+        v = v * np.exp(-0.5 * dt * (zeta + eta)) + 0.5 * dt * F / m
+        M = m.sum()
+        R0 = (m * r).sum(axis=0) / M
+        vc = (m * v).sum(axis=0) / M
+        x = eta * dt
+        ph = dt * np.where(np.abs(x) < 1e-12, 1.0 + 0.5 * x, np.expm1(x) / np.where(x == 0, 1.0, x))
+        r = R0 + vc * dt + np.exp(x) * (r - R0) + (v - vc) * ph
+        L = L * np.exp(x)
+        E, F, W = force_fn(r, L)
+        v = (v + 0.5 * dt * F / m) * np.exp(-0.5 * dt * (zeta + eta))
+        K = (m * v * v).sum(axis=0)
+        xi += 0.5 * dt * zeta
+        zeta, eta = half(zeta, eta, K)
+        out["epot"][s] = E
+        out["ekin"][s] = 0.5 * K.sum()
+        out["volume"][s] = np.prod(L)
+        out["zeta_t"][s], out["eta_t"][s], out["xi_t"][s] = zeta, eta, xi
+    out.update(pos=r, vel=v, box=L, zeta=zeta, eta=eta, xi=xi, forces=F, virial=W)
+    return out
+
+
+def npt_conserved(epot: float, ekin: float, volume: float, n_atoms: int, kT: float, ttime: float, pfactor: float,
+                  pressure: float, zeta: float, eta: np.ndarray, xi: float) -> float:
+    """E + K + P V + 3 n kT (ttime^2 zeta^2 / 2 + xi) + pfactor |eta|^2 / 2,
+    conserved by the NPT equations of motion above."""
+    g = 3.0 * n_atoms
+    return (epot + ekin + pressure * volume + g * kT * (0.5 * ttime ** 2 * zeta ** 2 + xi) +
+            0.5 * pfactor * float(np.dot(eta, eta)))

@@ -206,3 +206,55 @@ def test_student_calculator_contract(tmp_path):
     torch.save({"model_state_dict": Toy().state_dict()}, tmp_path / "toy.pth")
     with pytest.raises(RuntimeError):
         StudentCalculator(model_path=tmp_path / "toy.pth", device="cpu")
+
+
+def _soft_pairs(n_side=3, a=2.0, seed=0):
+    """Periodic soft Gaussian pair potential (E = sum exp(-d^2/2)), its
+    forces and strain derivative, for the NPT oracle checks."""
+    rng = np.random.default_rng(seed)
+    g = np.stack(np.meshgrid(*[np.arange(n_side)] * 3, indexing="ij"), -1).reshape(-1, 3) * a
+    pos = g + 0.3 * rng.normal(size=g.shape)
+
+    def ff(r, L):
+        d = r[:, None, :] - r[None, :, :]
+        d -= L * np.round(d / L)
+        e = np.exp(-0.5 * (d * d).sum(-1))
+        np.fill_diagonal(e, 0.0)
+        return 0.5 * e.sum(), (e[:, :, None] * d).sum(1), -0.5 * np.einsum("ij,ija,ijb->ab", e, d, d)
+
+    return pos, ff
+
+
+def test_oracle_npt_conserves_extended_energy():
+    """The NPT restatement (thermostat and barostat on) conserves E + K +
+    P V + 3 n kT (ttime^2 zeta^2 / 2 + xi) + pfactor |eta|^2 / 2 to the
+    accuracy of its splitting, while the box changes."""
+    from oracle.md import npt_conserved, npt_melchionna
+    pos, ff = _soft_pairs()
+    n = pos.shape[0]
+    L0 = np.full(3, 6.0)
+    m = np.ones(n)
+    v = 0.3 * np.random.default_rng(1).normal(size=pos.shape)
+    kT, tt, pf, P = 0.05, 0.5, 200.0, 0.01
+    E, F, W = ff(pos, L0)
+    H0 = npt_conserved(E, 0.5 * (v * v).sum(), 216.0, n, kT, tt, pf, P, 0.0, np.zeros(3), 0.0)
+    o = npt_melchionna(pos, v, m, L0, ff, 0.01, kT, tt, pf, P, 300)
+    H1 = npt_conserved(o["epot"][-1], o["ekin"][-1], o["volume"][-1], n, kT, tt, pf, P, o["zeta"], o["eta"],
+                       o["xi"])
+    assert abs(o["volume"][-1] - 216.0) > 1.0
+    assert abs(H1 - H0) < 1e-3, (H0, H1)
+
+
+def test_oracle_npt_strain_derivative_is_the_energy_change_under_strain():
+    """The force field's W (used by the barostat) is dE/d(strain):
+    E((1 + e) r, (1 + e) L) against central differences."""
+    pos, ff = _soft_pairs(seed=2)
+    L = np.full(3, 6.0)
+    _, _, W = ff(pos, L)
+    for a in range(3):
+        h = 1e-6
+        S = np.zeros((3, 3))
+        S[a, a] = h
+        ep = ff(pos @ (np.eye(3) + S).T, L * (1 + np.diag(S)))[0]
+        em = ff(pos @ (np.eye(3) - S).T, L * (1 - np.diag(S)))[0]
+        assert abs((ep - em) / (2 * h) - W[a, a]) < 1e-6
