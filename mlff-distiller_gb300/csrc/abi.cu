@@ -59,7 +59,8 @@ WsLayout ws_layout(const mlff_dims& d, int32_t n_atoms, int32_t n_mol, int64_t c
     L.L = d.n_layers;
     L.P = persistent_ctas(path);
     L.cap = cap;
-    L.ncell_cap = (int64_t)n_atoms + 27LL * n_mol;
+    // Morton code spaces of the cell grids: under 8 x max(n_atoms, 27) per structure
+    L.ncell_cap = 8LL * ((int64_t)n_atoms + 27LL * n_mol);
     size_t p = 0;
     auto take = [&](size_t bytes) {
         size_t r = p;
@@ -81,7 +82,7 @@ WsLayout ws_layout(const mlff_dims& d, int32_t n_atoms, int32_t n_mol, int64_t c
     L.rev = take(4 * cap);
     L.edge_acc = take(sizeof(float4) * cap);
     L.scan_tmp = take(4 * ((scan_n + 1023) / 1024 + 2));
-    L.mol_grid = take(sizeof(int4) * B);
+    L.mol_grid = take(sizeof(int4) * (B + 1));   // + the count of cell codes in use
     L.cell_count = take(4 * (L.ncell_cap + 1));
     L.cell_fill = take(4 * L.ncell_cap);
     L.cell_pos = take(sizeof(float4) * N);

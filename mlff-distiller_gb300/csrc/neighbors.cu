@@ -10,9 +10,11 @@
 //
 // Open structures: every atom pair of the structure is tested (one warp per
 // row, warp-ballot compaction keeps the ascending order).  Periodic boxes:
-// atoms are binned into cells of edge >= cutoff and copied in cell order
-// (position and atom index in one float4, so a cell's candidates are
-// contiguous); a row's warp looks up its 27 (or fewer, for small grids)
+// atoms are binned into cells of edge >= cutoff, the cells numbered along a
+// Morton (Z-order) curve, and the atoms copied in that order (position and
+// atom index in one float4, so a cell's candidates are contiguous and
+// neighbouring cells lie close in memory); a row's warp looks up its 27 (or
+// fewer, for small grids)
 // neighbouring cells in one step -- one cell per lane, a warp scan of their
 // sizes -- and walks the concatenated candidates 32 at a time, each lane
 // finding its cell by a binary search over the scan; hits are compacted
@@ -119,17 +121,21 @@ __global__ void scan_add_kernel(int32_t* __restrict__ data, int64_t n, const int
 }
 
 // One block for small inputs: exclusive scan of data[0..n_in), data[n_in] =
-// total.  Each of the 1024 threads owns a contiguous run of ceil(n_in/1024)
-// values (read twice: once to sum, once to write).  With st non-NULL the
-// total is the edge count: it is recorded in the status word and checked
-// against the edge capacity.
+// total, with n_in = n_max or the device-side count *n_dev (at most n_max).
+// Each of the 1024 threads owns a contiguous run of ceil(n_in/1024) values
+// (read twice: once to sum, once to write).  With st non-NULL the total is
+// the edge count: it is recorded in the status word and checked against the
+// edge capacity.
 constexpr int64_t SCAN1_MAX = 8192;
-__global__ void __launch_bounds__(1024) scan_single_kernel(int32_t* __restrict__ data, int64_t n_in,
-                                                           Status* st, int64_t cap) {
+__global__ void __launch_bounds__(1024) scan_single_kernel(int32_t* __restrict__ data, int64_t n_max,
+                                                           const int32_t* __restrict__ n_dev, Status* st,
+                                                           int64_t cap) {
     pdl_wait();
     pdl_trigger();
     __shared__ int32_t warp_tot[32];
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    // the count of values: n_max, or the smaller device-side count when given
+    const int64_t n_in = n_dev ? min((int64_t)max(*n_dev, 0), n_max) : n_max;
     const int64_t per = (n_in + 1023) / 1024;
     const int64_t b0 = min((int64_t)t * per, n_in), b1 = min(b0 + per, n_in);
     int32_t s = 0;
@@ -199,9 +205,28 @@ __global__ void prep_atoms_kernel(const float* __restrict__ pos, const int64_t* 
     }
 }
 
+// bits of a cell coordinate on an axis with nc cells
+__device__ __forceinline__ int cell_bits(int nc) { return nc > 1 ? 32 - __clz(nc - 1) : 0; }
+
+// Morton (Z-order) code of cell (x, y, z) on a grid with bx, by, bz bits per
+// axis: the coordinates' bits interleaved from the lowest level up, each axis
+// contributing while it still has bits -- a bijection onto [0, 2^(bx+by+bz)).
+__device__ __forceinline__ int morton3(int x, int y, int z, int bx, int by, int bz) {
+    int code = 0, pos = 0;
+    const int nb = max(bx, max(by, bz));
+    for (int b = 0; b < nb; ++b) {
+        if (b < bz) code |= ((z >> b) & 1) << pos++;
+        if (b < by) code |= ((y >> b) & 1) << pos++;
+        if (b < bx) code |= ((x >> b) & 1) << pos++;
+    }
+    return code;
+}
+
 // One block: per periodic structure choose the cell grid (cells of edge
-// >= cutoff, at most max(n_atoms, 27) cells) and the first cell index.
-// It also zeroes the cell counters (ncell_cap + 1) and fill cursors.
+// >= cutoff, at most max(n_atoms, 27) cells) and the first cell code (the
+// structure's Morton code space is under 8 times its cell count).
+// It also zeroes the counters and fill cursors of the codes in use and
+// writes their count to grid[n_mol].x.
 __global__ void mol_grid_kernel(const int64_t* __restrict__ mol_ptr, const float* __restrict__ box,
                                 const uint8_t* __restrict__ pbc, int32_t n_mol, float cutoff,
                                 int4* __restrict__ grid, int32_t* __restrict__ cell_count,
@@ -211,10 +236,6 @@ __global__ void mol_grid_kernel(const int64_t* __restrict__ mol_ptr, const float
     __shared__ int32_t warp_tot[32];
     __shared__ int32_t carry;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-    for (int64_t k = t; k <= ncell_cap; k += blockDim.x) {
-        cell_count[k] = 0;
-        if (k < ncell_cap) cell_fill[k] = 0;
-    }
     if (t == 0) carry = 0;
     __syncthreads();
     for (int c0 = 0; c0 < n_mol; c0 += 1024) {
@@ -239,7 +260,8 @@ __global__ void mol_grid_kernel(const int64_t* __restrict__ mol_ptr, const float
                 int a = (nc[0] >= nc[1] && nc[0] >= nc[2]) ? 0 : (nc[1] >= nc[2] ? 1 : 2);
                 nc[a] -= 1;
             }
-            ncell = nc[0] * nc[1] * nc[2];
+            // cells are numbered by their Morton code: the code space holds 2^(bits x + y + z)
+            ncell = 1 << (cell_bits(nc[0]) + cell_bits(nc[1]) + cell_bits(nc[2]));
         }
         int32_t x = ncell;
 #pragma unroll
@@ -264,6 +286,16 @@ __global__ void mol_grid_kernel(const int64_t* __restrict__ mol_ptr, const float
         __syncthreads();
         if (t == 1023) carry = excl + ncell;
         __syncthreads();
+    }
+    // the codes in use: [0, carry); zero their counters (and the total slot) and fill cursors
+    const int64_t used = min((int64_t)carry, ncell_cap);
+    for (int64_t k = t; k <= used; k += blockDim.x) {
+        cell_count[k] = 0;
+        if (k < used) cell_fill[k] = 0;
+    }
+    if (t == 0) {
+        if (carry > ncell_cap) set_status(st, MLFF_ERR_BOX, -1);
+        grid[n_mol] = make_int4((int)used, 0, 0, 0);
     }
 }
 
@@ -303,7 +335,7 @@ __global__ void cell_count_kernel(const float4* __restrict__ pos4, const int32_t
         int cx = cell_coord(p.x, b.L[0], b.invL[0], g.x);
         int cy = cell_coord(p.y, b.L[1], b.invL[1], g.y);
         int cz = cell_coord(p.z, b.L[2], b.invL[2], g.z);
-        int c = g.w + (cx * g.y + cy) * g.z + cz;
+        int c = g.w + morton3(cx, cy, cz, cell_bits(g.x), cell_bits(g.y), cell_bits(g.z));
         atom_cell[i] = c;
         atomicAdd(&cell_count[c], 1);
     }
@@ -380,9 +412,11 @@ __global__ void __launch_bounds__(NBR_WARPS * 32) nbr_rows_kernel(NbrArgs a) {
             }
         } else {
             const int4 g = a.grid[m];
-            const int ci = a.atom_cell[i] - g.w;
-            const int cc[3] = {ci / (g.y * g.z), (ci / g.z) % g.y, ci % g.z};
+            // the row atom's cell, computed as the binning did
+            const int cc[3] = {cell_coord(pi.x, b.L[0], b.invL[0], g.x), cell_coord(pi.y, b.L[1], b.invL[1], g.y),
+                               cell_coord(pi.z, b.L[2], b.invL[2], g.z)};
             const int ncs[3] = {g.x, g.y, g.z};
+            const int bits[3] = {cell_bits(g.x), cell_bits(g.y), cell_bits(g.z)};
             bool overflow = false;
             // lane k < 27 looks up neighbour cell (k / 9, k / 3 % 3, k % 3) - 1 (wrapped); on an
             // axis with fewer than 3 cells the offsets 0 .. nc-1 name its cells directly
@@ -401,7 +435,7 @@ __global__ void __launch_bounds__(NBR_WARPS * 32) nbr_rows_kernel(NbrArgs a) {
                     }
                 }
                 if (keep) {
-                    const int qc = g.w + (q[0] * g.y + q[1]) * g.z + q[2];
+                    const int qc = g.w + morton3(q[0], q[1], q[2], bits[0], bits[1], bits[2]);
                     c0 = a.cell_start[qc];
                     len = a.cell_start[qc + 1] - c0;
                 }
@@ -527,10 +561,12 @@ int launch_partition(const WsLayout& L, void* ws, cudaStream_t st) {
 
 // Exclusive scan of data[0..n_in) with the total written to data[n_in]
 // (which must hold 0 for the multi-block form); with st the total is the
-// edge count, recorded and checked against cap.
-static int scan_with_total(int32_t* data, int64_t n_in, int32_t* tmp, Status* st, int64_t cap, cudaStream_t s) {
-    if (n_in + 1 <= SCAN1_MAX) {
-        MLFF_LAUNCH_PDL("scan_single", scan_single_kernel, 1, 1024, 0, s, data, n_in, st, cap);
+// edge count, recorded and checked against cap.  With n_dev the count is
+// read on the device (at most n_in) and one block scans it.
+static int scan_with_total(int32_t* data, int64_t n_in, int32_t* tmp, Status* st, int64_t cap, cudaStream_t s,
+                           const int32_t* n_dev = nullptr) {
+    if (n_in + 1 <= SCAN1_MAX || n_dev) {
+        MLFF_LAUNCH_PDL("scan_single", scan_single_kernel, 1, 1024, 0, s, data, n_in, n_dev, st, cap);
         return MLFF_OK;
     }
     int r = launch_scan(data, n_in + 1, tmp, s);
@@ -553,7 +589,9 @@ int launch_neighbors_into(const mlff_dims& d, const mlff_system& sys, const NbrB
                         b.mol_grid, b.cell_count, b.cell_fill, b.ncell_cap, b.status);
         MLFF_LAUNCH_PDL("cell_count", cell_count_kernel, gb, tb, 0, st, b.pos4, b.atom_mol, sys.box, sys.pbc, b.mol_grid,
                         N, b.atom_cell, b.cell_count);
-        int r = scan_with_total(b.cell_count, b.ncell_cap, b.scan_tmp, nullptr, 0, st);
+        // the cell codes in use (grid[n_mol].x, at most ncell_cap), scanned by one block
+        int r = scan_with_total(b.cell_count, b.ncell_cap, b.scan_tmp, nullptr, 0, st,
+                                reinterpret_cast<const int32_t*>(b.mol_grid + sys.n_mol));
         if (r) return r;
         MLFF_LAUNCH_PDL("cell_fill", cell_fill_kernel, gb, tb, 0, st, b.atom_cell, b.cell_count, b.pos4, N, b.cell_fill,
                         b.cell_pos);

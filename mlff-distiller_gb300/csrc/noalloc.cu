@@ -10,7 +10,7 @@
 //
 // Limits: at most NOALLOC_MAX_ATOMS atoms, NOALLOC_MAX_MOLS structures and
 // NOALLOC_MAX_EDGES directed edges per call; larger inputs are rejected.
-// The array is about 5.8 MB and stays resident on every device that has
+// The array is about 12.6 MB and stays resident on every device that has
 // loaded the library until the process exits.
 //
 // Every call shares the array and it keeps the last call's contents: the
@@ -31,7 +31,7 @@ constexpr int64_t NOALLOC_MAX_EDGES = 1 << 20;
 
 namespace {
 constexpr int64_t align256(int64_t x) { return (x + 255) & ~int64_t(255); }
-constexpr int64_t kNcellCap = NOALLOC_MAX_ATOMS + 27 * NOALLOC_MAX_MOLS;
+constexpr int64_t kNcellCap = 8 * (NOALLOC_MAX_ATOMS + 27 * NOALLOC_MAX_MOLS);   // Morton code spaces
 constexpr int64_t kScanN = kNcellCap + 1;    // >= N + 1
 constexpr int64_t kOffStatus = 0;
 constexpr int64_t kOffPos4 = align256(kOffStatus + (int64_t)sizeof(Status));
@@ -39,12 +39,12 @@ constexpr int64_t kOffAtomMol = align256(kOffPos4 + 16 * NOALLOC_MAX_ATOMS);
 constexpr int64_t kOffErecv = align256(kOffAtomMol + 4 * NOALLOC_MAX_ATOMS);
 constexpr int64_t kOffScan = align256(kOffErecv + 4 * NOALLOC_MAX_EDGES);
 constexpr int64_t kOffGrid = align256(kOffScan + 4 * ((kScanN + 1023) / 1024 + 2));
-constexpr int64_t kOffCellCount = align256(kOffGrid + 16 * NOALLOC_MAX_MOLS);
+constexpr int64_t kOffCellCount = align256(kOffGrid + 16 * (NOALLOC_MAX_MOLS + 1));
 constexpr int64_t kOffCellFill = align256(kOffCellCount + 4 * (kNcellCap + 1));
 constexpr int64_t kOffCellPos = align256(kOffCellFill + 4 * kNcellCap);
 constexpr int64_t kOffAtomCell = align256(kOffCellPos + 16 * NOALLOC_MAX_ATOMS);
 constexpr int64_t kScratchBytes = align256(kOffAtomCell + 4 * NOALLOC_MAX_ATOMS);
-static_assert(kScratchBytes < 6 * 1024 * 1024, "static scratch must stay modest");
+static_assert(kScratchBytes < 14 * 1024 * 1024, "static scratch must stay modest");
 }  // namespace
 
 // The shared scratch of the allocation-free entry point.  In host code this
@@ -127,7 +127,7 @@ extern "C" int mlff_radius_graph_noalloc(const mlff_system* sys, float cutoff, i
     b.cell_fill = reinterpret_cast<int32_t*>(s + kOffCellFill);
     b.cell_pos = reinterpret_cast<float4*>(s + kOffCellPos);
     b.atom_cell = reinterpret_cast<int32_t*>(s + kOffAtomCell);
-    b.ncell_cap = (int64_t)sys->n_atoms + 27LL * sys->n_mol;
+    b.ncell_cap = 8LL * ((int64_t)sys->n_atoms + 27LL * sys->n_mol);
     b.cap = edge_capacity;
     // the status word keeps the previous call's value: clear it
     MLFF_CUDA(cudaMemsetAsync(b.status, 0, sizeof(Status), st));
