@@ -136,3 +136,36 @@ def test_force_loss_gradient_arguments_checked_on_host():
     r = lib.mlff_param_grads_forces(ctypes.byref(d), fake, ctypes.byref(s), 1024, None, fake, ctypes.byref(g), fake,
                                     need - 1, None)
     assert r == _lib.ERR_WORKSPACE
+
+
+def test_npt_arguments_checked_on_host():
+    """mlff_npt_steps validates its arguments before any device work: a
+    missing NPT state, missing periodic flags, a thermostat without a
+    temperature and a negative pfactor."""
+    import ctypes
+    from mlff_gb300 import _lib
+    from mlff_gb300.engine import dims_of
+    lib = _lib.load()
+    d = dims_of(128, 20, 3, 119, 5.0)
+    fake = ctypes.c_void_p(256)   # never dereferenced: every call below fails on the host
+    s = _lib.System()
+    s.n_atoms, s.n_mol = 3, 1
+    s.pos = s.Z = s.mol_ptr = fake.value
+    st = _lib.MDState()
+    st.pos = st.vel = st.inv_mass = st.forces = st.energy = fake.value
+    npt = _lib.NPTState()
+    npt.box = npt.box32 = npt.zeta = npt.eta = npt.xi = npt.virial = fake.value
+    dbl = ctypes.c_double
+
+    def call(state, flags, kT, ttime, pfactor):
+        s.box = s.pbc = flags
+        return lib.mlff_npt_steps(ctypes.byref(d), fake, ctypes.byref(s), 1024, _lib.PATH_TUNED_TC,
+                                  ctypes.byref(st), state, dbl(0.02), dbl(kT), dbl(ttime), dbl(pfactor), dbl(0.0),
+                                  1, fake, 1 << 30, None)
+
+    assert call(None, fake.value, 0.025, 2.5, 1.0) == _lib.ERR_INVALID
+    assert b"NPT state" in lib.mlff_last_error_string()
+    assert call(ctypes.byref(npt), None, 0.025, 2.5, 1.0) == _lib.ERR_INVALID
+    assert call(ctypes.byref(npt), fake.value, 0.0, 2.5, 1.0) == _lib.ERR_INVALID
+    assert call(ctypes.byref(npt), fake.value, 0.025, 2.5, -1.0) == _lib.ERR_INVALID
+    assert b"pfactor" in lib.mlff_last_error_string()
