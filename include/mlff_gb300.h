@@ -344,7 +344,7 @@ int mlff_profile_end(double *ms_by_kind, int64_t *launches_by_kind, int32_t n_ki
  * Same CSR as mlff_build_neighbors (row_ptr [N+1], col [edge_capacity],
  * caller-owned outputs) plus status [4] int32 (code, edges found, first
  * offending index, edges >> 31), all device pointers.  Scratch lives in one
- * file-scope device array of about 5.8 MB, so sizes are capped: n_atoms <=
+ * file-scope device array of about 13 MB, so sizes are capped: n_atoms <=
  * 16384, n_mol <= 4096, edge_capacity <= 1048576 (MLFF_ERR_INVALID above
  * that).  The first call on a device looks up the array's address; make it
  * before any stream capture.  Calls share the array: calls that overlap on

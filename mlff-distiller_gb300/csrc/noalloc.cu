@@ -10,7 +10,7 @@
 //
 // Limits: at most NOALLOC_MAX_ATOMS atoms, NOALLOC_MAX_MOLS structures and
 // NOALLOC_MAX_EDGES directed edges per call; larger inputs are rejected.
-// The array is about 12.6 MB and stays resident on every device that has
+// The array is about 13 MB and stays resident on every device that has
 // loaded the library until the process exits.
 //
 // Every call shares the array and it keeps the last call's contents: the
