@@ -23,7 +23,6 @@ from __future__ import annotations
 
 import logging
 import math
-import warnings
 from pathlib import Path
 from typing import Dict, Optional, Tuple, Union
 
@@ -135,6 +134,72 @@ class _EnergyForces(torch.autograd.Function):
             return None, None, None, None
         g = grad_E.to(torch.float32)[mol_index].unsqueeze(1)
         return (-F * g).to(grad_E.dtype), None, None, None
+
+
+def _trainable(model):
+    return [(n, p) for n, p in model.named_parameters() if p.requires_grad]
+
+
+class _EnergyTrain(torch.autograd.Function):
+    """Training-mode E = model(positions), differentiable in the parameters
+    to second order, on the plain FP32 path (the one with parameter
+    gradients).  backward(g): the position gradient sum_b g_b dE_b/dpos and
+    the parameter gradients sum_b g_b dE_b/dtheta (mlff_param_grads).  When
+    the backward itself is recorded (torch.autograd.grad(E, pos,
+    create_graph=True), the reference's forces in training mode,
+    student_model.py:759-795) the position gradient is a _ForceTerm node
+    instead, whose own backward gives the forces' parameter gradients; the
+    energy term's parameter gradients then come from the later
+    loss.backward()."""
+
+    @staticmethod
+    def forward(ctx, positions, model, batch, mol_index, *params):
+        from . import _lib
+        E, F, _ = model.engine().energy_forces(batch, _lib.PATH_PLAIN_FP32, forces=True)
+        ctx.model, ctx.batch = model, batch
+        ctx.save_for_backward(F, mol_index, *params)
+        return E.to(positions.dtype)
+
+    @staticmethod
+    def backward(ctx, grad_E):
+        F, mol_index, *params = ctx.saved_tensors
+        none = (None, None, None)
+        if torch.is_grad_enabled():
+            gpos = _ForceTerm.apply(grad_E, F, mol_index, ctx.model, ctx.batch, *params)
+            return (gpos,) + none + (None,) * len(params)
+        from .training import param_grads
+        g = grad_E.detach()
+        gpos = (-F * g.to(torch.float32)[mol_index].unsqueeze(1)).to(grad_E.dtype)
+        _, grads, _ = param_grads(ctx.model, ctx.batch, g.to(torch.float64))
+        return (gpos,) + none + tuple(grads[n].to(p.dtype) for (n, _), p in zip(_trainable(ctx.model), params))
+
+
+class _ForceTerm(torch.autograd.Function):
+    """sum_b g_b dE_b/dpos as a function of g and the parameters (the
+    recorded position gradient of _EnergyTrain).  backward(G): the parameter
+    gradients sum_i G'_i . d(dE/dpos_i)/dtheta with G'_i = g_b(i) G_i, by the
+    forward-mode pass over the reverse pass (mlff_param_grads_forces), and
+    dL/dg_b = sum over the atoms of b of G_i . dE/dpos_i.  The second
+    derivative in the positions (a Hessian-vector product) is not formed:
+    positions are training data."""
+
+    @staticmethod
+    def forward(ctx, grad_E, F, mol_index, model, batch, *params):
+        ctx.model, ctx.batch = model, batch
+        ctx.save_for_backward(grad_E, F, mol_index, *params)
+        return -F * grad_E.detach().to(torch.float32)[mol_index].unsqueeze(1)
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        grad_E, F, mol_index, *params = ctx.saved_tensors
+        from .training import force_term_grads
+        G = grad_out.detach().to(torch.float32)
+        Gp = G * grad_E.detach().to(torch.float32)[mol_index].unsqueeze(1)
+        # the output is +dE/dpos = -F: its weights enter the forces' gradient with a minus sign
+        grads = force_term_grads(ctx.model, ctx.batch, -Gp)
+        gE = torch.zeros_like(grad_E).index_add_(0, mol_index, -(G * F).sum(dim=1).to(grad_E.dtype))
+        return (gE, None, None, None, None) + tuple(grads[n].to(p.dtype)
+                                                    for (n, _), p in zip(_trainable(ctx.model), params))
 
 
 class StudentForceField(nn.Module):
@@ -303,10 +368,12 @@ class StudentForceField(nn.Module):
         """Total energy: 0-dim for one structure, [B] for a batch
         (student_model.py:634-757).  Differentiable w.r.t. positions."""
         bt, mol_index, n_mol = self._make_batch(atomic_numbers, positions, cell, pbc, batch)
-        if self.training and torch.is_grad_enabled() and any(p.requires_grad for p in self.parameters()):
-            warnings.warn("mlff_gb300.StudentForceField gives position gradients only; use "
-                          "mlff_gb300.training for parameter gradients", stacklevel=2)
-        E = _EnergyForces.apply(positions, self, bt, mol_index)
+        train = _trainable(self) if self.training and torch.is_grad_enabled() else []
+        if train:
+            # parameter gradients (to second order, for force losses) from the CUDA passes
+            E = _EnergyTrain.apply(positions, self, bt, mol_index, *[p for _, p in train])
+        else:
+            E = _EnergyForces.apply(positions, self, bt, mol_index)
         # one structure -> 0-dim, several -> [B]  (student_model.py:739-755)
         return E.sum() if n_mol <= 1 else E
 
@@ -314,7 +381,15 @@ class StudentForceField(nn.Module):
                                   cell: Optional[torch.Tensor] = None, pbc: Optional[torch.Tensor] = None
                                   ) -> Tuple[torch.Tensor, torch.Tensor]:
         """(energy, forces) with forces from the CUDA adjoint
-        (student_model.py:759-795)."""
+        (student_model.py:759-795).  In training mode with trainable
+        parameters the forces are -dE/dpos taken with create_graph=True, as
+        the reference does, so a loss on them back-propagates into the
+        parameters."""
+        if self.training and torch.is_grad_enabled() and _trainable(self):
+            x = positions if positions.requires_grad else positions.detach().requires_grad_(True)
+            E = self.forward(atomic_numbers, x, cell=cell, pbc=pbc)
+            F = -torch.autograd.grad(E, x, grad_outputs=torch.ones_like(E), create_graph=True)[0]
+            return E, F
         bt, _, _ = self._make_batch(atomic_numbers, positions, cell, pbc, None)
         E, F, _ = self._engine_call(bt, forces=True)
         return E[0].to(positions.dtype), F.to(positions.dtype)

@@ -123,6 +123,48 @@ def param_grads(model, batch: Batch, weights: torch.Tensor, forces: bool = False
     return E, grads, F
 
 
+def force_term_grads(model, batch: Batch, force_weights: torch.Tensor,
+                     virial_weights: Optional[torch.Tensor] = None) -> Dict[str, torch.Tensor]:
+    """{name: sum_i G_i . dF_i/dtheta (+ sum_b S_b : dW_b/dtheta)} for every
+    trainable parameter: the forward-mode pass alone (mlff_param_grads_forces
+    into zeroed gradients), without the energy term."""
+    eng = model.engine()
+    dev = eng.device
+    N, B = batch.n_atoms, batch.n_mol
+    G = None if force_weights is None else torch.as_tensor(force_weights, dtype=torch.float32,
+                                                          device=dev).contiguous()
+    S = None if virial_weights is None else torch.as_tensor(virial_weights, dtype=torch.float64,
+                                                            device=dev).contiguous()
+    if G is not None and G.shape != (N, 3):
+        raise ValueError(f"force_weights must have shape ({N}, 3), got {tuple(G.shape)}")
+    if S is not None and S.shape != (B, 3, 3):
+        raise ValueError(f"virial_weights must have shape ({B}, 3, 3), got {tuple(S.shape)}")
+    grads = {n: torch.zeros_like(p, dtype=torch.float32, device=dev)
+             for n, p in model.named_parameters() if p.requires_grad}
+    if G is None and S is None:
+        return grads
+    g = _grads_struct(model, grads)
+    sysd = batch.system()
+    path = _lib.PATH_TRAIN
+    for _ in range(4):
+        cap = eng.capacity(N, path)
+        ws = eng.workspace_for(N, B, cap, _lib.PATH_TRAIN_FORCES)
+        _lib.check(eng.lib.mlff_param_grads_forces(ctypes.byref(eng.dims), eng.packed.data_ptr(), ctypes.byref(sysd),
+                                                   cap, _lib.ptr(G), _lib.ptr(S), ctypes.byref(g), ws.data_ptr(),
+                                                   ws.numel(), _stream_handle()))
+        code, n_edges, where = eng.status()
+        if code == _lib.ERR_CAPACITY:
+            eng.edge_capacity[path] = int(n_edges * 1.25) + 1024
+            for t in grads.values():
+                t.zero_()
+            continue
+        if code != _lib.OK:
+            raise _lib.MLFFError(code, f"device status {code} at index {where}")
+        eng.edge_capacity[path] = max(eng.edge_capacity.get(path, 0), int(n_edges * 1.15) + 1024)
+        return grads
+    raise _lib.MLFFError(_lib.ERR_CAPACITY, "edge capacity did not converge")
+
+
 class ForceFieldLoss:
     """Weighted energy / force / angular loss on predicted energies [B] and
     forces [N,3] (ForceFieldLoss, training/losses.py:15-246): each term is an
@@ -340,4 +382,4 @@ class EnergyTrainer:
         return float(loss.item())
 
 
-__all__ = ["param_grads", "ForceFieldLoss", "ForceFieldTrainer", "EnergyTrainer", "trainable_names", "make_batch"]
+__all__ = ["param_grads", "force_term_grads", "ForceFieldLoss", "ForceFieldTrainer", "EnergyTrainer", "trainable_names", "make_batch"]

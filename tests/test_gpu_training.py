@@ -261,3 +261,47 @@ def test_force_field_trainer_with_stress(weights_seed0, weights_bias):
     assert "stress" in hist[0]
     assert hist[-1]["total"] < 0.5 * hist[0]["total"]
     assert hist[-1]["stress"] < hist[0]["stress"]
+
+
+def test_reference_training_loop_runs_on_the_cuda_gradients(weights_bias):
+    """The reference's own training step, unchanged: model in train mode,
+    E = model(Z, pos, batch), F = -autograd.grad(E, pos, create_graph=True),
+    ForceFieldLoss(E, F) and loss.backward().  The parameters' .grad come
+    from the library (energy term: reverse pass; force and angular terms:
+    forward mode over it) and match the reference's recorded step
+    (golden_train.npz) to float32 accuracy."""
+    import os
+    from conftest import GOLDEN
+    from mlff_gb300.training import ForceFieldLoss
+    g = np.load(os.path.join(GOLDEN, "golden_train.npz"))
+    m = _model(weights_bias)
+    m.train()
+    Z = torch.tensor(g["Z"], device="cuda")
+    x = torch.tensor(g["pos"], device="cuda", requires_grad=True)
+    b = torch.repeat_interleave(torch.arange(len(g["mol_ptr"]) - 1, device="cuda"),
+                                torch.as_tensor(np.diff(g["mol_ptr"]), device="cuda"))
+    E = m(Z, x, batch=b)
+    F = -torch.autograd.grad(E, x, grad_outputs=torch.ones_like(E), create_graph=True)[0]
+    loss = ForceFieldLoss(energy_weight=1.0, force_weight=100.0, stress_weight=0.1, angular_weight=10.0)
+    out = loss({"energy": E, "forces": F},
+               {"energy": torch.tensor(g["E_ref"], dtype=torch.float32, device="cuda"),
+                "forces": torch.tensor(g["F_ref"], dtype=torch.float32, device="cuda")})
+    assert abs(float(out["total"].detach()) - float(g["loss"])) <= 1e-4 * abs(float(g["loss"]))
+    out["total"].backward()
+    worst = 0.0
+    for k, p in m.named_parameters():
+        got = p.grad.double().cpu().reshape(-1).numpy()
+        ref_norm = float(g[f"grad/{k}/norm"])
+        val = g[f"grad/{k}/val"]
+        scale = max(np.abs(val).max(), ref_norm / np.sqrt(got.size), 1e-9)
+        err = np.abs(got[g[f"grad/{k}/idx"]] - val).max() / scale
+        worst = max(worst, err)
+        assert err < 1e-3, (k, err)
+    print(f"reference-style loss.backward(): worst relative error vs the reference's step {worst:.2e}")
+    # predict_energy_and_forces in training mode builds the same graph
+    m.zero_grad()
+    s0 = slice(int(g["mol_ptr"][0]), int(g["mol_ptr"][1]))
+    E1, F1 = m.predict_energy_and_forces(Z[s0], torch.tensor(g["pos"][s0], device="cuda"))
+    (F1 * F1).sum().backward()
+    assert all(p.grad is not None and torch.isfinite(p.grad).all() for p in m.parameters() if p.requires_grad)
+    assert float(m.energy_head[0].weight.grad.abs().sum()) > 0
