@@ -88,3 +88,22 @@ def test_host_buffers_equal_device_call(model):
         E, F = model.energy_and_forces(Z, P, batch=b)
         E0, F0 = _eager(model, Z.cuda(), P.cuda(), batch=b)
         assert torch.equal(E, E0.cpu()) and torch.equal(F, F0.cpu())
+
+
+def test_forward_autograd_equals_engine_forces(model):
+    """The reference API in inference (eval mode): E = model(Z, pos, batch),
+    forces by torch.autograd.grad(E.sum(), pos) through the CUDA adjoint,
+    equal to the engine's forces bit for bit; no parameter gradients."""
+    from mlff_gb300 import systems
+    model.eval()
+    s = systems.molecule_batch(5, 10, 40, seed=14)
+    Z = torch.as_tensor(s.Z, dtype=torch.int64, device="cuda")
+    x = torch.as_tensor(s.pos, dtype=torch.float32, device="cuda").requires_grad_(True)
+    b = torch.as_tensor(np.repeat(np.arange(s.n_mol), np.diff(s.mol_ptr)))
+    E = model(Z, x, batch=b)
+    assert E.shape == (s.n_mol,)
+    (gx,) = torch.autograd.grad(E.sum(), x)
+    E0, F0 = _eager(model, Z, x.detach(), batch=b)
+    assert torch.equal(E.detach().double(), E0.to(E.dtype).double())
+    assert torch.equal(-gx, F0)
+    assert all(p.grad is None for p in model.parameters())
