@@ -24,7 +24,9 @@ seeded inputs in float32 (the reference's own dtype) and float64
                              reference's ForceFieldLoss (training/losses.py,
                              configs/train_student.yaml weights) and
                              loss.backward(); per tensor the gradient's norm
-                             and its values at seeded sample indices
+                             and its values at seeded sample indices; and the
+                             loss with mae / huber components: its value and
+                             derivatives in the predicted energies and forces
 
 ``--train-only`` rewrites golden_train.npz alone.
 """
@@ -99,6 +101,17 @@ def make_train_golden(sm, ref_root: str, sd, pert):
            "E": E.detach().numpy(), "F": F.detach().numpy(), "loss": np.float64(out["total"].item()),
            "loss_energy": np.float64(out["energy"].item()), "loss_force": np.float64(out["force"].item()),
            "loss_angular": np.float64(out["angular"].item())}
+    # the loss alone for other component types: values and derivatives in E and F
+    for kind in ("mae", "huber"):
+        Ed = E.detach().clone().requires_grad_(True)
+        Fd = F.detach().clone().requires_grad_(True)
+        lf = losses.ForceFieldLoss(energy_weight=1.0, force_weight=100.0, stress_weight=0.1, angular_weight=10.0,
+                                   energy_loss_type=kind, force_loss_type=kind, huber_delta=0.2)
+        o = lf({"energy": Ed, "forces": Fd}, {"energy": torch.tensor(E_ref), "forces": torch.tensor(F_ref)})
+        gE, gF = torch.autograd.grad(o["total"], [Ed, Fd])
+        rec[f"{kind}/loss"] = np.float64(o["total"].item())
+        rec[f"{kind}/dE"] = gE.numpy()
+        rec[f"{kind}/dF"] = gF.numpy()
     for name, prm in model.named_parameters():
         gr = torch.zeros_like(prm) if prm.grad is None else prm.grad
         flat = gr.detach().reshape(-1).numpy()

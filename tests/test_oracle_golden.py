@@ -203,3 +203,21 @@ def test_oracle_strain_second_order_matches_finite_differences(weights_bias):
             vals.append(float((V.numpy() * S).sum()))
         fd = (vals[0] - vals[1]) / (2 * h)
         assert abs(fd - float(g[key][idx])) <= 1e-6 + 1e-5 * abs(fd), (key, idx, fd, float(g[key][idx]))
+
+
+@pytest.mark.parametrize("kind", ["mae", "huber"])
+def test_force_field_loss_components_match_reference(kind):
+    """The restated ForceFieldLoss with mae / huber components (delta 0.2)
+    against the reference's own loss on the same predictions: value and the
+    derivatives in the energies and forces (golden_train.npz)."""
+    import torch
+    from mlff_gb300.training import ForceFieldLoss
+    g = np.load(os.path.join(GOLDEN, "golden_train.npz"))
+    loss = ForceFieldLoss(energy_weight=1.0, force_weight=100.0, stress_weight=0.1, angular_weight=10.0,
+                          energy_loss_type=kind, force_loss_type=kind, huber_delta=0.2)
+    out, w, G, _ = loss.derivatives(torch.tensor(g["E"]), torch.tensor(g["F"]), torch.tensor(g["E_ref"]),
+                                    torch.tensor(g["F_ref"]))
+    assert abs(float(out["total"].detach()) - float(g[f"{kind}/loss"])) <= 1e-12 * abs(float(g[f"{kind}/loss"]))
+    np.testing.assert_allclose(w.numpy(), g[f"{kind}/dE"], rtol=1e-12, atol=1e-15)
+    # G is returned in float32 (the library's input type)
+    np.testing.assert_allclose(G.numpy(), g[f"{kind}/dF"], rtol=1e-6, atol=1e-9)
