@@ -365,7 +365,6 @@ struct NbrArgs {
     const int4* grid;
     const int32_t* cell_start;
     const float4* cell_pos;
-    const int32_t* atom_cell;
     int32_t n_atoms;
     float cutoff;
     int64_t cap;
@@ -499,15 +498,13 @@ __global__ void __launch_bounds__(NBR_WARPS * 32) nbr_rows_kernel(NbrArgs a) {
     }
 }
 
-__global__ void check_edges_kernel(const int32_t* __restrict__ row_ptr, int32_t n_atoms, int64_t cap,
-                                   const int32_t* __restrict__ counts_total, Status* st) {
+__global__ void check_edges_kernel(const int32_t* __restrict__ row_ptr, int32_t n_atoms, int64_t cap, Status* st) {
     pdl_wait();
     pdl_trigger();
     int64_t e = (int64_t)(uint32_t)row_ptr[n_atoms];
     st->n_edges = (int32_t)(e & 0x7fffffff);
     st->n_edges_hi = (int32_t)(e >> 31);
     if (e > cap) set_status(st, MLFF_ERR_CAPACITY, -1);
-    (void)counts_total;
 }
 
 // rev[k]: position of the reversed edge (row b, col a) for edge k = (row a, col b)
@@ -571,7 +568,7 @@ static int scan_with_total(int32_t* data, int64_t n_in, int32_t* tmp, Status* st
     }
     int r = launch_scan(data, n_in + 1, tmp, s);
     if (r) return r;
-    if (st) MLFF_LAUNCH_PDL("check_edges", check_edges_kernel, 1, 1, 0, s, data, (int32_t)n_in, cap, nullptr, st);
+    if (st) MLFF_LAUNCH_PDL("check_edges", check_edges_kernel, 1, 1, 0, s, data, (int32_t)n_in, cap, st);
     return MLFF_OK;
 }
 
@@ -598,7 +595,7 @@ int launch_neighbors_into(const mlff_dims& d, const mlff_system& sys, const NbrB
     }
     NbrArgs a;
     a.pos4 = b.pos4; a.atom_mol = b.atom_mol; a.mol_ptr = sys.mol_ptr; a.box = sys.box; a.pbc = sys.pbc;
-    a.grid = b.mol_grid; a.cell_start = b.cell_count; a.cell_pos = b.cell_pos; a.atom_cell = b.atom_cell;
+    a.grid = b.mol_grid; a.cell_start = b.cell_count; a.cell_pos = b.cell_pos;
     a.n_atoms = N; a.cutoff = d.cutoff; a.cap = b.cap; a.counts = b.row_ptr;
     a.col = b.col; a.erecv = b.erecv; a.st = b.status;
     const int rows_blocks = (int)std::max<int64_t>(1, std::min<int64_t>((N + NBR_WARPS - 1) / NBR_WARPS, 152 * 32));
