@@ -10,6 +10,16 @@ e2e figure goes through the public module API with host buffers (H2D of
 positions and numbers; D2H of energies, forces and the status word) inside
 the timed region.  An L2-sized buffer is rewritten between timed steps.
 
+Beside the headline the line carries, measured in the same run:
+  * ``vs_plain_fp32``: the tensor-core path against the plain FP32 CUDA path
+    on the 256-molecule batch and on the 3,000-atom periodic water box, both
+    paths timed the same way (CUDA-graph replays of one step, L2 flushed);
+  * ``accuracy``: energy and force errors of the timed path against the
+    float64 oracle (a checker, run after the timed regions);
+  * ``roofline``: the dominant kernel's algorithmic filter-MLP FLOPs over its
+    CUDA-event launch time against the measured bf16 burst peak, and the
+    whole step's GEMM FLOPs over the step time.
+
   python bench.py [--gpus N --steps K --warmup W] [--workload batch256]
                   [--path fp16x3|tuned_fp32|fp32] [--impl ours|reference]
 
@@ -59,6 +69,11 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--md-steps", type=int, default=0,
                     help="MD workloads: further untimed steps for the energy drift (20000 = 10 ps)")
+    ap.add_argument("--no-compare", action="store_true", help="skip the plain-FP32 / water-box comparison")
+    ap.add_argument("--compare-steps", type=int, default=10)
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the float64 oracle accuracy check")
+    ap.add_argument("--accuracy-structures", type=int, default=64,
+                    help="structures of a multi-structure workload checked against the float64 oracle")
     return ap.parse_args()
 
 
@@ -132,16 +147,9 @@ def seed_model(precision):
     return StudentForceField(precision=precision)
 
 
-def cpu_baseline(sysm, seconds, n_threads=None):
-    """Oracle port of the reference CPU path (float32 torch autograd, C
-    radius graph) on a bounded sample of the workload's molecules."""
+def _port_rate(W, sub, seconds):
+    """atom-steps/s of the oracle port (float32 torch autograd) on `sub`."""
     from oracle import painn
-    if n_threads:
-        torch.set_num_threads(n_threads)
-    model = seed_model("tuned_fp32")
-    W = {k: v.numpy() for k, v in model.state_dict().items()}
-    n_take = min(sysm.n_mol, 16)
-    sub = sysm.subset(list(range(n_take))) if sysm.n_mol > 1 else sysm
     pos = sub.pos.astype(np.float32).astype(np.float64)
     painn.energy_forces(W, sub.Z, pos, sub.mol_ptr, box=sub.box, pbc=sub.pbc, dtype=torch.float32)
     reps, t0 = 0, time.perf_counter()
@@ -151,9 +159,32 @@ def cpu_baseline(sysm, seconds, n_threads=None):
         el = time.perf_counter() - t0
         if (el >= seconds and reps >= 3) or el >= 4 * seconds:
             break
-    return {"value": sub.n_atoms * reps / el, "unit": UNIT, "cores": torch.get_num_threads(), "kind": "port",
+    return sub.n_atoms * reps / el, reps
+
+
+def cpu_baseline(sysm, seconds, n_threads=None, one_thread_seconds=3.0):
+    """Oracle port of the reference CPU path (float32 torch autograd, C
+    radius graph) on a bounded sample of the workload's molecules, with all
+    host threads and (value_1thread) with one."""
+    if n_threads:
+        torch.set_num_threads(n_threads)
+    W = W_SEED0()
+    n_take = min(sysm.n_mol, 16)
+    sub = sysm.subset(list(range(n_take))) if sysm.n_mol > 1 else sysm
+    v, reps = _port_rate(W, sub, seconds)
+    cores = torch.get_num_threads()
+    v1 = None
+    if one_thread_seconds > 0:
+        n1 = min(sysm.n_mol, 4)
+        sub1 = sysm.subset(list(range(n1))) if sysm.n_mol > 1 else sysm
+        torch.set_num_threads(1)
+        v1, _ = _port_rate(W, sub1, one_thread_seconds)
+        torch.set_num_threads(cores)
+    return {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+            "value_1thread": v1,
             "sample": f"{n_take} of {sysm.n_mol} structures ({sub.n_atoms} atoms), {reps} E+F evaluations, "
-                      f"float32 torch autograd on the host CPU"}
+                      f"float32 torch autograd on the host CPU"
+                      + (f"; value_1thread on the first {min(sysm.n_mol, 4)} structures" if v1 else "")}
 
 
 def read_traffic(kernel_kind, workload):
@@ -166,11 +197,60 @@ def read_traffic(kernel_kind, workload):
 
 
 def measured_peaks():
+    """bf16 burst TFLOP/s (the kernels are timed inside a few-ms step, not a
+    seconds-long loop) and HBM GB/s: measured on this GPU model if the
+    measurement file is present, else the fallback figures."""
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
         d = json.load(open(p))
-        return d.get("bf16_tflops_sustained", 1700.0), d.get("hbm_gbs", 6800.0), "measured"
-    return 1700.0, 6800.0, "fallback"
+        return d.get("bf16_tflops", 1900.0), d.get("hbm_gbs", 6800.0), "measured"
+    return 1900.0, 6800.0, "fallback"
+
+
+def step_gemm_flop(n_atoms, n_edges, n_layers=3):
+    """Algorithmic GEMM FLOPs of one E+F evaluation: forward plus the
+    input-gradient pass of the filter MLP per directed edge, the update MLP
+    per atom and layer, and the readout per atom."""
+    return 2 * (n_layers * (n_edges * GEMM_FLOP_PER_EDGE + n_atoms * 163_840) + n_atoms * 20_544)
+
+
+def accuracy_vs_oracle(sysm, E, F, max_structures):
+    """Checker, outside every timed region: energies [B] and forces [N,3] of
+    the timed path against the float64 oracle evaluated on the same float32
+    positions, on the first max_structures structures (structures are
+    independent, so a subset's results are exactly the full batch's)."""
+    from oracle import painn
+    take = min(sysm.n_mol, max_structures)
+    sub = sysm.subset(list(range(take))) if take < sysm.n_mol else sysm
+    n_sub = sub.n_atoms
+    t0 = time.perf_counter()
+    E0, F0 = painn.energy_forces(W_SEED0(), sub.Z, sub.pos.astype(np.float32).astype(np.float64), sub.mol_ptr,
+                                 box=sub.box, pbc=sub.pbc)
+    el = time.perf_counter() - t0
+    E0, F0 = E0.numpy(), F0.numpy()
+    Eg = np.asarray(E, dtype=np.float64)[:take]
+    Fg = np.asarray(F, dtype=np.float64)[:n_sub]
+    per_atom = np.abs(Eg - E0) / np.diff(sub.mol_ptr)
+    dF = Fg - F0
+    return {"reference": "float64 oracle (CPU) on the same float32 positions",
+            "structures": f"{take} of {sysm.n_mol}", "atoms": int(n_sub),
+            "energy_err_mev_per_atom_max": float(1000 * per_atom.max()),
+            "energy_err_mev_per_atom_mean": float(1000 * per_atom.mean()),
+            "force_err_max_ev_per_a": float(np.abs(dF).max()),
+            "force_err_rms_ev_per_a": float(np.sqrt((dF ** 2).mean())),
+            "force_rms_ev_per_a": float(np.sqrt((F0 ** 2).mean())),
+            "force_tol_ev_per_a": 1e-3, "within_tol": bool(np.abs(dF).max() <= 1e-3),
+            "oracle_seconds": round(el, 1)}
+
+
+_W0 = {}
+
+
+def W_SEED0():
+    """The seed-0 weights (the model every bench workload evaluates)."""
+    if not _W0:
+        _W0.update({k: v.numpy() for k, v in seed_model("tuned_fp32").state_dict().items()})
+    return _W0
 
 
 def run_reference(args, world, rank):
@@ -182,11 +262,11 @@ def run_reference(args, world, rank):
     torch.set_num_threads(n_thr)
     step_s = max(1.0, args.cpu_seconds / max(1, args.steps))
     for _ in range(args.warmup):
-        cpu_baseline(sysm, 0.0, n_thr)
+        cpu_baseline(sysm, 0.0, n_thr, one_thread_seconds=0)
     vals = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        vals.append(cpu_baseline(sysm, step_s, n_thr))
+        vals.append(cpu_baseline(sysm, step_s, n_thr, one_thread_seconds=0))
     total = time.perf_counter() - t0
     v = statistics.mean(x["value"] for x in vals)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
@@ -292,6 +372,64 @@ def run_md(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def time_replays(step, steps, flush):
+    """CUDA-event times (ms) of `steps` calls of step(), an L2-sized buffer
+    rewritten before each one."""
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    torch.cuda.synchronize()
+    for i in range(steps):
+        flush.fill_(float(i))
+        starts[i].record()
+        step()
+        ends[i].record()
+    torch.cuda.synchronize()
+    return [s.elapsed_time(e) for s, e in zip(starts, ends)]
+
+
+def graph_step(model, sysm, warmup):
+    """A CUDA graph of one E+F evaluation of the workload on the model's
+    path (edge capacity sized first); returns (replay, E, F, n_edges)."""
+    from mlff_gb300.engine import make_batch
+    eng = model.engine()
+    batch = make_batch(sysm.Z, sysm.pos, sysm.mol_ptr, sysm.box if sysm.pbc.any() else None,
+                       sysm.pbc if sysm.pbc.any() else None)
+    eng.energy_forces(batch, model.path)
+    _, n_edges, _ = eng.status()
+    step, E, F = eng.capture(batch, model.path)
+    for _ in range(max(3, warmup)):
+        step()
+    return step, E, F, n_edges, batch
+
+
+def compare_paths(args, path, flush):
+    """Tensor-core path vs plain FP32 on the 256-molecule batch and the
+    3,000-atom periodic water box: both timed as CUDA-graph replays of one
+    step with the L2 flushed between steps."""
+    from mlff_gb300 import _lib, systems
+    out = {}
+    for wl in ("batch256", "water3000"):
+        sysm = systems.workload(wl)
+        ms = {}
+        for prec in (path, "fp32"):
+            m = seed_model(prec).cuda().eval()
+            step, _, _, n_edges, _ = graph_step(m, sysm, args.warmup)
+            t = time_replays(step, args.compare_steps, flush)
+            code, _, _ = m.engine().status()
+            if code != _lib.OK:
+                raise RuntimeError(f"device status {code} in the {prec} comparison on {wl}")
+            ms[prec] = statistics.median(t)
+            del m, step
+            torch.cuda.empty_cache()
+        out[wl] = {"ratio": round(ms["fp32"] / ms[path], 3),
+                   "tuned_ms_per_step": round(ms[path], 4), "plain_fp32_ms_per_step": round(ms["fp32"], 4),
+                   "tuned_atom_steps_per_s": round(sysm.n_atoms / (ms[path] * 1e-3)),
+                   "plain_fp32_atom_steps_per_s": round(sysm.n_atoms / (ms["fp32"] * 1e-3)),
+                   "atoms": sysm.n_atoms, "directed_edges": int(n_edges)}
+    out["launch"] = "both paths: CUDA-graph replay of one step, median of %d, L2 flushed" % args.compare_steps
+    return out
+
+
 def main():
     args = parse()
     world, rank, local = dist_env()
@@ -333,12 +471,14 @@ def main():
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     if args.graph:
-        step, _, _ = eng.capture(batch, path)
+        step, E_out, F_out = eng.capture(batch, path)
         for _ in range(max(3, args.warmup)):
             step()
     else:
+        res = {}
+
         def step():
-            eng.energy_forces(batch, path, check=False)
+            res["E"], res["F"], _ = eng.energy_forces(batch, path, check=False)
     barrier()
     clocks.start()
     time.sleep(0.3)
@@ -352,6 +492,10 @@ def main():
     code, _, _ = eng.status()
     if code != _lib.OK:
         raise RuntimeError(f"device status {code} during the timed region")
+    if not args.graph:
+        E_out, F_out = res["E"], res["F"]
+    E_timed = E_out.cpu().numpy().copy()
+    F_timed = F_out.cpu().numpy().copy()
     # kernel split and launch count: the same steps again, eagerly, under the
     # library's CUDA-event profiler (not part of the timed region)
     with _lib.Profile() as prof:
@@ -360,8 +504,10 @@ def main():
             eng.energy_forces(batch, path, check=False)
         barrier()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    hbm_peak = int(torch.cuda.max_memory_allocated())    # the timed workload alone
     atoms_all = sysm.n_atoms * world
     _, total_s, value = aggregate_throughput(sysm.n_atoms * args.steps, sum(step_ms) / 1000.0, device="cuda")
+    ms_per_step = 1000 * total_s / args.steps
 
     # dominant kernel and its roofline (algorithmic GEMM FLOPs of the filter MLP)
     L = model.num_interactions
@@ -374,20 +520,21 @@ def main():
         flop = n_edges * GEMM_FLOP_PER_EDGE
     elif dom == "edge_bwd":
         flop = 2 * n_edges * GEMM_FLOP_PER_EDGE
-    elif dom == "plain_gemm":
-        # plain path GEMM launches: per layer 2 forward + 2 reverse filter GEMMs and 4 update GEMMs
-        flop = None
     else:
         flop = None
+    step_flop = step_gemm_flop(sysm.n_atoms, n_edges, L)
+    step_tf = step_flop / (ms_per_step * 1e-3) / 1e12
     roof = None
     if flop is not None:
         ach = flop / (avg_ms * 1e-3) / 1e12
         roof = {"bound": "tensor", "kernel": dom, "achieved": round(ach, 2), "peak": peak_tf, "unit": "TFLOP/s",
-                "frac": round(ach / peak_tf, 4), "peak_source": f"{peak_src} bf16 sustained",
+                "frac": round(ach / peak_tf, 4), "peak_source": f"{peak_src} bf16 burst",
                 "traffic": read_traffic(dom, args.workload), "avg_launch_ms": round(avg_ms, 4),
-                "flop_per_launch": flop,
+                "launches_per_step": launches / args.steps, "flop_per_launch": flop,
                 "mma_work_factor": (3.0 * (2 * (32 * 128 + 128 * 384)) / GEMM_FLOP_PER_EDGE
-                                    if path == _lib.PATH_TUNED_TC else None)}
+                                    if path == _lib.PATH_TUNED_TC else None),
+                "step": {"gemm_flop_per_step": step_flop, "achieved": round(step_tf, 2),
+                         "frac": round(step_tf / peak_tf, 4)}}
     gpu_launches = sum(prof.launches.values())
 
     # e2e through the public module API with host buffers
@@ -427,21 +574,31 @@ def main():
         if world > 1:
             torch.distributed.destroy_process_group()
         return
+    del model, eng
+    torch.cuda.empty_cache()
+    compare = None
+    if not args.no_compare and world == 1:
+        compare = compare_paths(args, args.path, flush)
+    acc = None
+    if not args.no_accuracy:
+        acc = accuracy_vs_oracle(sysm, E_timed, F_timed, args.accuracy_structures)
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(sysm, args.cpu_seconds, os.cpu_count())
     dtype = {"fp16x3": "fp16x3 (split-fp16 operands, fp32 accumulate)", "tuned_fp32": "f32", "fp32": "f32"}[args.path]
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000 * total_s / args.steps, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": dtype,
             "data": "synthetic (seeded), seed-0 weights",
             "config": {"workload": args.workload, "atoms": sysm.n_atoms, "structures": sysm.n_mol,
                        "directed_edges": n_edges, "path": args.path, "l2": "256 MiB buffer rewritten "
                        "between timed steps", "per_rank": "independent copy of the workload",
                        "launch": "CUDA graph of one step" if args.graph else "eager library call per step",
-                       "hbm_peak_bytes": int(torch.cuda.max_memory_allocated())},
+                       "hbm_peak_bytes": hbm_peak},
+            "vs_plain_fp32": compare, "accuracy": acc,
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches,
             "kernel_ms": {k: round(v, 3) for k, v in prof.ms.items() if v > 0},
+            "kernel_launches": {k: v for k, v in prof.launches.items() if v > 0},
             "clocks": ck}
     print(json.dumps(line), flush=True)
     if world > 1:

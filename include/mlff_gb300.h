@@ -5,7 +5,7 @@
  * The reference (MLFF-Distiller) is pure Python/PyTorch: it has no native
  * FFI.  Each entry point below replaces one Python call on the hot path; the
  * comment names that call (file:line inside the reference project).  The
- * Python package mlff_gb300 binds these with ctypes.
+ * Python package mlff_gb300 binds these with ctypes (mlff_gb300/_lib.py).
  *
  * Conventions
  *  - Every pointer to array data is a DEVICE pointer owned by the caller
@@ -337,6 +337,20 @@ int mlff_param_grads_forces(const mlff_dims *dims, const void *packed, const mlf
 #define MLFF_PROFILE_KINDS 11
 int mlff_profile_begin(void);
 int mlff_profile_end(double *ms_by_kind, int64_t *launches_by_kind, int32_t n_kinds);
+
+/* Test hook for the bounded device waits (no counterpart in the reference;
+ * the timeout path replaces a hang where the reference would block).  While
+ * bit 0 (forward) or bit 1 (reverse) of `kernels` is set, every CTA of the
+ * tensor-core edge kernels launched afterwards also waits, at its first
+ * main-loop wait, on an mbarrier that nothing arrives at, for about 65,000
+ * cycles; the wait runs out and the kernel takes the path of a real timeout:
+ * MLFF_ERR_TIMEOUT with index 99 in the status word, abort flag raised, its
+ * own copies and MMAs drained, tensor memory freed, return.  The kernels
+ * that follow see the status and do nothing.  0 (the default) turns it off.
+ * Kernel arguments are fixed when a CUDA graph is captured: the hook applies
+ * to eager calls and to graphs captured while it is set.  Not for use in
+ * production. */
+int mlff_debug_stall_test(int32_t kernels);
 
 /* Radius graph that allocates nothing.  No counterpart in the reference:
  * it exists for callers that cannot call cudaMalloc or hand over a

@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cmath>
+#include <atomic>
 #include "common.cuh"
 #include "workspace.h"
 
@@ -165,6 +166,7 @@ static int check_path(int32_t path) {
 }
 
 int pack_fp32(const mlff_dims& d, const mlff_params& p, float* out, const PackedOffsets& o, cudaStream_t st);
+extern std::atomic<int> g_stall_test;
 int pack_bf16(const mlff_dims& d, float* out, const PackedOffsets& o, cudaStream_t st);
 
 }  // namespace mlff
@@ -201,6 +203,15 @@ using namespace mlff;
 extern "C" {
 
 int mlff_version(void) { return 100; }
+
+int mlff_debug_stall_test(int32_t kernels) {
+    if (kernels < 0 || kernels > 3) {
+        set_error("stall test mask %d outside 0..3", kernels);
+        return MLFF_ERR_INVALID;
+    }
+    g_stall_test.store(kernels);
+    return MLFF_OK;
+}
 
 const char* mlff_last_error_string(void) { return g_err; }
 

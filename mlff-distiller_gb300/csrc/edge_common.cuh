@@ -33,6 +33,7 @@ struct EdgeArgs {
     int32_t eacc_init;        // reverse: 1 = first layer processed, eacc is written rather than added to
     int32_t write_nodes;      // reverse: also produce dE/dX (unused for the first layer)
     int32_t n_atoms;
+    int32_t stall_test;       // tensor-core kernels, test hook: time out at the first main-loop wait
     const Status* st;
 };
 

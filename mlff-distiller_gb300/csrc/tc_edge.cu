@@ -113,6 +113,11 @@ int pack_bf16(const mlff_dims& d, float* out, const PackedOffsets& o, cudaStream
 
 // -------------------------------------------------------- shared pieces
 constexpr int NT = 512;                        // threads per CTA (16 warps)
+// Test hook (EdgeArgs::stall_test): the first main-loop wait of a partition
+// also waits on an mbarrier that nothing arrives at, for STALL_BUDGET
+// cycles, and so takes the timeout path of a real stalled wait.
+constexpr long long STALL_BUDGET = 1LL << 16;
+constexpr int WHERE_STALL_TEST = 99;
 
 // Barrier 1 over the first n threads (whole warps) of the CTA.
 __device__ __forceinline__ void bar_sync_first(int n) { asm volatile("bar.sync 1, %0;" ::"r"(n) : "memory"); }
@@ -412,7 +417,7 @@ constexpr uint32_t F_OFF_SB = F_OFF_W2L + W2L_BYTES;
 constexpr uint32_t F_OFF_B1 = F_OFF_SB + 2 * F_SB_BYTES;
 constexpr uint32_t F_OFF_B2 = F_OFF_B1 + H * 4;
 constexpr uint32_t F_OFF_BAR = F_OFF_B2 + H3 * 4;
-constexpr uint32_t F_OFF_MISC = F_OFF_BAR + 8 * 4;
+constexpr uint32_t F_OFF_MISC = F_OFF_BAR + 8 * 5;
 constexpr uint32_t F_SMEM = align1k(F_OFF_MISC + 16);
 static_assert(ET_BYTES <= 2 * F_HH, "E tile fits in the H tile's space");
 static_assert(F_SMEM <= 232448, "forward kernel shared memory");
@@ -434,6 +439,7 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
     uint64_t* w2h_bar = mma_bar + 1;
     uint64_t* e_bar = mma_bar + 2;
     uint64_t* g2_bar = mma_bar + 3;                 // GEMM2: one commit per chunk issuer
+    uint64_t* never_bar = mma_bar + 4;              // test hook: nothing arrives here
     uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + F_OFF_MISC);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + F_OFF_MISC + 4);
 
@@ -451,6 +457,7 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
         mbar_init(w2h_bar, 1);
         mbar_init(e_bar, 1);
         mbar_init(g2_bar, 3);
+        mbar_init(never_bar, 1);
         fence_mbar_init();
         *abort_flag = 0;
     }
@@ -542,6 +549,8 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
             if (w == 0) __syncwarp();
             // only warp 0 polls the MMA barrier; the others wait at the CTA
             // barrier instead of spinning on shared memory the MMAs read from
+            if (w == 0 && (a.stall_test & 1) && k == 0 && !mbar_wait(never_bar, 0, STALL_BUDGET))
+                signal_timeout(a, abort_flag, WHERE_STALL_TEST);
             if (w == 0 && !mbar_wait(mma_bar, mma_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 1);
             mma_phase ^= 1;
             fence_before_sync();
@@ -698,8 +707,14 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
     // drain: the resident-weight load, any E-tile copy and a GEMM1 issued
     // for a tile that never ran (abort) must be complete before the CTA exits
     __syncthreads();
-    if (t == 0 && g1_issued && !mbar_wait(mma_bar, mma_phase, WAIT_BUDGET))
+    // the last GEMM1 and GEMM2 committed must be complete: a GEMM1 issued for
+    // a tile that never ran (abort), or MMAs whose wait timed out.  A wait on
+    // the parity of the phase before the current one returns at once, so
+    // these also hold when nothing was committed.
+    if (t == 0 && !mbar_wait(mma_bar, g1_issued ? mma_phase : (mma_phase ^ 1), WAIT_BUDGET))
         set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 3);
+    if (t == 0 && !mbar_wait(g2_bar, g2_phase ^ 1, WAIT_BUDGET))
+        set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 5);
     if (t == 32) {
         if (!mbar_wait(w2h_bar, 0, WAIT_BUDGET)) set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 7);
         // an E-tile copy issued for a tile that never ran (abort) must land first
@@ -738,7 +753,7 @@ constexpr uint32_t B_OFF_B1 = B_OFF_SB + 2 * B_SB_BYTES;
 constexpr uint32_t B_OFF_B2 = B_OFF_B1 + H * 4;
 constexpr uint32_t B_OFF_RED = B_OFF_B2 + H3 * 4;
 constexpr uint32_t B_OFF_BAR = B_OFF_RED + 16 * BN * 2 * 4;
-constexpr uint32_t B_OFF_MISC = B_OFF_BAR + 8 * 4;
+constexpr uint32_t B_OFF_MISC = B_OFF_BAR + 8 * 5;
 constexpr uint32_t B_SMEM = align1k(B_OFF_MISC + 16);
 static_assert(ET_BYTES <= 2 * B_HH, "E tile fits in the H tile's space");
 static_assert(B_SMEM <= 232448, "reverse kernel shared memory");
@@ -758,6 +773,7 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
     uint64_t* w2h_bar = mma_bar + 1;
     uint64_t* e_bar = mma_bar + 2;
     uint64_t* g2_bar = mma_bar + 3;                 // GEMM2: one commit per chunk issuer
+    uint64_t* never_bar = mma_bar + 4;              // test hook: nothing arrives here
     uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + B_OFF_MISC);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + B_OFF_MISC + 4);
 
@@ -775,6 +791,7 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
         mbar_init(w2h_bar, 1);
         mbar_init(e_bar, 1);
         mbar_init(g2_bar, 3);
+        mbar_init(never_bar, 1);
         fence_mbar_init();
         *abort_flag = 0;
     }
@@ -864,6 +881,8 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
             if (w == 0) __syncwarp();
             // only warp 0 polls the MMA barrier; the others wait at the CTA
             // barrier instead of spinning on shared memory the MMAs read from
+            if (w == 0 && (a.stall_test & 2) && k == 0 && !mbar_wait(never_bar, 0, STALL_BUDGET))
+                signal_timeout(a, abort_flag, WHERE_STALL_TEST);
             if (w == 0 && !mbar_wait(mma_bar, mma_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 11);
             mma_phase ^= 1;
             fence_before_sync();
@@ -1048,6 +1067,14 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
         if (!aborted && a.write_nodes) a.xbar[(int64_t)cur * 4 * H + fidx] = acc;
     }
     __syncthreads();
+    // after a timed-out wait the MMAs it waited for may still be running: the
+    // last GEMM1 and GEMM2 committed must be complete (a wait on the parity of
+    // the phase before the current one returns at once, so this also holds
+    // when nothing was committed)
+    if (t == 0) {
+        if (!mbar_wait(mma_bar, mma_phase ^ 1, WAIT_BUDGET)) set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 13);
+        if (!mbar_wait(g2_bar, g2_phase ^ 1, WAIT_BUDGET)) set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 15);
+    }
     if (t == 32) {
         if (!mbar_wait(w2h_bar, 0, WAIT_BUDGET)) set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 17);
         if (e_issued > 0 && !mbar_wait(e_bar, (e_issued - 1) & 1, WAIT_BUDGET))

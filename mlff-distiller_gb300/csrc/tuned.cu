@@ -22,12 +22,16 @@
 // so no filter activation is stored and no transposed filter GEMM is needed.
 // This file holds the FP32 CUDA-core version of those kernels and the
 // driver for the fused path; tc_edge.cu holds the tensor-core version.
+#include <atomic>
 #include "common.cuh"
 #include "workspace.h"
 #include "edge_common.cuh"
 #include "profile.h"
 
 namespace mlff {
+
+// mlff_debug_stall_test: kernels that time out on purpose (test hook)
+std::atomic<int> g_stall_test{0};
 
 constexpr int FT = 32;   // edges per tile, forward
 constexpr int BT = 16;   // edges per tile, reverse
@@ -362,6 +366,7 @@ int run_tuned(const mlff_dims& d, const float* P, const PackedOffsets& po, const
     a.n_atoms = N;
     a.st = ws_ptr<Status>(ws, L.status);
     a.eacc = ws_ptr<float4>(ws, L.edge_acc);
+    a.stall_test = g_stall_test.load();
     float* X = ws_ptr<float>(ws, L.X);
     float* Xt = ws_ptr<float>(ws, L.Xt);
     const bool tc = path == MLFF_PATH_TUNED_TC;
@@ -413,16 +418,19 @@ int run_tuned(const mlff_dims& d, const float* P, const PackedOffsets& po, const
         a.write_nodes = l > 0 ? 1 : 0;
         a.eacc_init = l == d.n_layers - 1 ? 1 : 0;
         {
-            ProfScope prof(PK_EDGE_BWD, st);
+            ProfScope prof(PK_EDGE_BWD, st);   // the reverse edge kernel alone
             if (tc) {
                 a.etile = ws_ptr<unsigned char>(ws, L.etile_b);
                 a.etile_base = ws_ptr<int32_t>(ws, L.etile_base) + L.P + 1;
                 if ((r = launch_edge_bwd_tc(a, l, st))) return r;
-                if (l > 0 && (r = add_rows(xbo, xtb, NX, a.st, st))) return r;   // dE/dX = dE/dXt + gathered part
             } else {
                 edge_bwd_simt_kernel<<<L.P, 128, 0, st>>>(a);
                 MLFF_LAUNCH_CHECK("edge_bwd_simt");
             }
+        }
+        if (tc && l > 0) {
+            ProfScope prof(PK_OTHER, st);
+            if ((r = add_rows(xbo, xtb, NX, a.st, st))) return r;   // dE/dX = dE/dXt + gathered part
         }
     }
     return launch_forces(d, sys, L, ws, out, st);

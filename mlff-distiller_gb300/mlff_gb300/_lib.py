@@ -44,7 +44,8 @@ EXPORTS = ["mlff_version", "mlff_last_error_string", "mlff_packed_weights_size",
            "mlff_read_status", "mlff_clear_status", "mlff_verlet_steps", "mlff_langevin_steps", "mlff_npt_steps",
            "mlff_md_energy_stats",
            "mlff_profile_begin",
-           "mlff_profile_end", "mlff_radius_graph_noalloc", "mlff_param_grads", "mlff_param_grads_forces"]
+           "mlff_profile_end", "mlff_radius_graph_noalloc", "mlff_param_grads", "mlff_param_grads_forces",
+           "mlff_debug_stall_test"]
 
 PROFILE_KINDS = ["neighbors", "edge_fwd", "edge_bwd", "update_fwd", "update_bwd", "readout", "forces",
                  "plain_gemm", "plain_edge", "other", "md"]
@@ -165,6 +166,8 @@ def load(build_if_missing: bool = True):
         lib.mlff_param_grads_forces.restype = ctypes.c_int
         lib.mlff_param_grads_forces.argtypes = [ctypes.POINTER(Dims), _P, ctypes.POINTER(System), i64, _P, _P,
                                                 ctypes.POINTER(Grads), _P, sz, _P]
+        lib.mlff_debug_stall_test.restype = ctypes.c_int
+        lib.mlff_debug_stall_test.argtypes = [i32]
         lib.mlff_radius_graph_noalloc.restype = ctypes.c_int
         lib.mlff_radius_graph_noalloc.argtypes = [ctypes.POINTER(System), ctypes.c_float, i64, _P, _P, _P, _P]
         _lib = lib

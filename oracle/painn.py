@@ -42,13 +42,32 @@ def _linear(x: Tensor, p: Dict[str, Tensor], key: str) -> Tensor:
     return x @ p[key + ".weight"].T + p[key + ".bias"]
 
 
+def _messages(s: Tensor, v: Tensor, e: Tensor, u: Tensor, src: Tensor, dst: Tensor, w1: Tensor, b1: Tensor,
+              w2: Tensor, b2: Tensor):
+    """(ds, dv) of one edge set: filter MLP (:350), split (:353-355), scalar
+    and vector messages summed at the receivers (:359-385)."""
+    H = s.shape[1]
+    f = _silu(e @ w1.T + b1) @ w2.T + b2
+    fs, fv1, fv2 = torch.split(f, H, dim=-1)
+    ds = torch.zeros_like(s).index_add_(0, dst, s[src] * fs)
+    dv = torch.zeros_like(v).index_add_(
+        0, dst, v[src] * fv1.unsqueeze(1) + u.unsqueeze(-1) * fv2.unsqueeze(1))
+    return ds, dv
+
+
 def energy(p: Dict[str, Tensor], Z: Tensor, pos: Tensor, src: Tensor, dst: Tensor,
-           shift_vec: Tensor, mol: Tensor, n_mol: int, cutoff: float = 5.0) -> Tensor:
+           shift_vec: Tensor, mol: Tensor, n_mol: int, cutoff: float = 5.0,
+           edge_chunk: Optional[int] = None) -> Tensor:
     """Per-molecule energies [n_mol] (StudentForceField.forward :634-757).
 
     shift_vec [E,3] is added to pos[src]-pos[dst] (zero for open molecules).
     Messages flow src -> dst (PaiNNMessage.forward :346-387); the update is
     PaiNNUpdate.forward :434-470 with the 3x3 mixing over the xyz axis.
+
+    edge_chunk: evaluate the messages over chunks of that many edges, each
+    recomputed in the backward pass (torch.utils.checkpoint), so that large
+    systems fit in host memory; the sums then add chunk by chunk (the same
+    result up to float64 rounding).  None: one pass over all edges.
     """
     H = p["embedding.weight"].shape[1]
     s = p["embedding.weight"][Z]                                  # :684
@@ -60,12 +79,23 @@ def energy(p: Dict[str, Tensor], Z: Tensor, pos: Tensor, src: Tensor, dst: Tenso
     n_layers = 1 + max(int(k.split(".")[1]) for k in p if k.startswith("interactions."))
     for l in range(n_layers):
         pre = f"interactions.{l}."
-        f = _linear(_silu(_linear(e, p, pre + "message.rbf_to_scalar.0")), p,
-                    pre + "message.rbf_to_scalar.2")              # :350
-        fs, fv1, fv2 = torch.split(f, H, dim=-1)                   # :353-355
-        ds = torch.zeros_like(s).index_add_(0, dst, s[src] * fs)   # :359-364
-        dv = torch.zeros_like(v).index_add_(
-            0, dst, v[src] * fv1.unsqueeze(1) + u.unsqueeze(-1) * fv2.unsqueeze(1))  # :370-385
+        if edge_chunk is None or src.shape[0] <= edge_chunk:
+            f = _linear(_silu(_linear(e, p, pre + "message.rbf_to_scalar.0")), p,
+                        pre + "message.rbf_to_scalar.2")              # :350
+            fs, fv1, fv2 = torch.split(f, H, dim=-1)                   # :353-355
+            ds = torch.zeros_like(s).index_add_(0, dst, s[src] * fs)   # :359-364
+            dv = torch.zeros_like(v).index_add_(
+                0, dst, v[src] * fv1.unsqueeze(1) + u.unsqueeze(-1) * fv2.unsqueeze(1))  # :370-385
+        else:
+            from torch.utils.checkpoint import checkpoint
+            wts = [p[pre + "message.rbf_to_scalar.0.weight"], p[pre + "message.rbf_to_scalar.0.bias"],
+                   p[pre + "message.rbf_to_scalar.2.weight"], p[pre + "message.rbf_to_scalar.2.bias"]]
+            ds, dv = torch.zeros_like(s), torch.zeros_like(v)
+            for c0 in range(0, src.shape[0], edge_chunk):
+                c = slice(c0, c0 + edge_chunk)
+                dsc, dvc = checkpoint(_messages, s, v, e[c], u[c], src[c], dst[c], *wts, use_reentrant=False)
+                ds = ds + dsc
+                dv = dv + dvc
         s = s + ds
         v = v + dv
         n = torch.linalg.vector_norm(v, dim=1)                     # :437
@@ -86,7 +116,7 @@ def params_to(p: Dict[str, Tensor], dtype=torch.float64) -> Dict[str, Tensor]:
 
 
 def energy_forces(params, Z, pos, mol_ptr, cutoff=5.0, box=None, pbc=None,
-                  edges=None, dtype=torch.float64, virial=False):
+                  edges=None, dtype=torch.float64, virial=False, edge_chunk=None):
     """Energies [B], forces [N,3] (= -dE/dpos) and optionally the strain
     derivative dE/d(eps) [B,3,3] for an affine strain of positions and cell.
 
@@ -119,7 +149,7 @@ def energy_forces(params, Z, pos, mol_ptr, cutoff=5.0, box=None, pbc=None,
         sv = torch.einsum("eab,eb->ea", strain[mol[dst_t]], shift_t)
     else:
         xs, sv = x, shift_t
-    E = energy(p, Zt, xs, src_t, dst_t, sv, mol, n_mol, cutoff)
+    E = energy(p, Zt, xs, src_t, dst_t, sv, mol, n_mol, cutoff, edge_chunk=edge_chunk)
     inputs = [x, eps] if virial else [x]
     grads = torch.autograd.grad(E.sum(), inputs)
     F = -grads[0]

@@ -208,4 +208,8 @@ def main(ref_root: str, train_only: bool = False):
 
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
-    main(args[0] if args else "/root/reference", train_only="--train-only" in sys.argv)
+    root = args[0] if args else os.environ.get("MLFF_REFERENCE_ROOT")
+    if not root:
+        sys.exit("usage: make_golden.py <reference checkout> [--train-only] "
+                 "(or set MLFF_REFERENCE_ROOT)")
+    main(root, train_only="--train-only" in sys.argv)

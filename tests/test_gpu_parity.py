@@ -124,12 +124,13 @@ def test_batch_equals_individual(golden_cases, weights_bias, path):
         assert np.abs(Fi - F[a:b]).max() <= 1e-4
 
 
-def test_forces_match_fd_of_oracle_energy(golden_cases, weights_bias):
+@pytest.mark.parametrize("path", ["tuned_fp32", "fp16x3"])
+def test_forces_match_fd_of_oracle_energy(golden_cases, weights_bias, path):
     """Central differences (step 1e-4 A) of the float64 model energy vs the
     device forces from the hand-written adjoint."""
     g = golden_cases
     Z, pos, mp = g["molecule60/Z"], g["molecule60/pos"].astype(np.float64), g["molecule60/mol_ptr"]
-    m = engine_for(weights_bias, "tuned_fp32")
+    m = engine_for(weights_bias, path)
     _, F, _ = run(m, Z, pos.astype(np.float32), mp)
     edges = nbr.radius_graph(pos.astype(np.float32), mp)
     h = 1e-4

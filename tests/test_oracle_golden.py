@@ -221,3 +221,17 @@ def test_force_field_loss_components_match_reference(kind):
     np.testing.assert_allclose(w.numpy(), g[f"{kind}/dE"], rtol=1e-12, atol=1e-15)
     # G is returned in float32 (the library's input type)
     np.testing.assert_allclose(G.numpy(), g[f"{kind}/dF"], rtol=1e-6, atol=1e-9)
+
+
+def test_oracle_edge_chunks_equal_single_pass(weights_bias):
+    """The oracle's checkpointed edge chunks (used for the benchmark-size
+    parity tests) give the single-pass result up to float64 rounding."""
+    from mlff_gb300 import systems
+    s = systems.water_box(n_water=40, L=10.5, d_oo=2.2, seed=9)
+    p = s.pos.astype(np.float32).astype(np.float64)
+    E1, F1, V1 = painn.energy_forces(weights_bias, s.Z, p, s.mol_ptr, box=s.box, pbc=s.pbc, virial=True)
+    E2, F2, V2 = painn.energy_forces(weights_bias, s.Z, p, s.mol_ptr, box=s.box, pbc=s.pbc, virial=True,
+                                     edge_chunk=1000)
+    assert abs(float(E1[0] - E2[0])) < 1e-10
+    assert float((F1 - F2).abs().max()) < 1e-11
+    assert float((V1 - V2).abs().max()) < 1e-10

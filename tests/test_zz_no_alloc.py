@@ -62,6 +62,30 @@ def test_noalloc_radius_graph_matches_workspace_entry_point():
 
 
 @pytest.mark.gpu
+def test_noalloc_radius_graph_above_8192_atoms_and_at_the_limit():
+    """Sizes whose row-pointer scan spans several blocks (the multi-block
+    scan keeps its partial sums in the shared array): a 9,000-atom water box
+    and a box of exactly MLFF_NOALLOC_MAX_ATOMS = 16,384 atoms, one call
+    after the other."""
+    from mlff_gb300 import _lib, systems
+    lib = _lib.load()
+    water = systems.water_box(n_water=3000, L=44.8, d_oo=2.5, seed=23)
+    box = systems.large_box(n_atoms=16384, seed=24)
+    assert water.n_atoms == 9000 and box.n_atoms == 16384
+    for s in (water, box):
+        batch = _system(s.Z, s.pos.astype(np.float32), s.mol_ptr, s.box, s.pbc)
+        ref_row, ref_col = _workspace_csr(batch)
+        n_edges = int(ref_row[-1])
+        cap = min(n_edges + 4096, 1 << 20)
+        assert n_edges < cap
+        row, col, st = _noalloc_csr(lib, batch, cap)
+        assert st[0] == 0, st
+        assert st[1] == n_edges
+        np.testing.assert_array_equal(row, ref_row)
+        np.testing.assert_array_equal(col[:n_edges], ref_col)
+
+
+@pytest.mark.gpu
 def test_noalloc_capacity_reported():
     from mlff_gb300 import _lib, systems
     lib = _lib.load()
