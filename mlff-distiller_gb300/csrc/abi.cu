@@ -48,9 +48,10 @@ int num_sms() {
 
 int persistent_ctas(int32_t path) {
     // Receiver partitions: the CUDA-core fused kernels run 4 CTAs of 128
-    // threads per SM; the tensor-core kernels run one CTA per SM, one
-    // partition each (fewer partial edge tiles).
-    return path == MLFF_PATH_TUNED_TC ? num_sms() : num_sms() * 4;
+    // threads per SM; the tensor-core kernels run one CTA per SM with two
+    // partitions each (the reverse kernel's two pipelines take one each,
+    // the forward kernel walks both as one receiver range).
+    return path == MLFF_PATH_TUNED_TC ? 2 * num_sms() : num_sms() * 4;
 }
 
 WsLayout ws_layout(const mlff_dims& d, int32_t n_atoms, int32_t n_mol, int64_t cap, int32_t path) {
@@ -99,12 +100,14 @@ WsLayout ws_layout(const mlff_dims& d, int32_t n_atoms, int32_t n_mol, int64_t c
     L.md_pos32 = take(sizeof(float) * 3 * N);
     if (path == MLFF_PATH_TUNED_TC) {
         L.geo = take(sizeof(float4) * cap);
-        // per-partition tiles: at most cap / tile + one partial tile per partition
-        L.n_etile_f = cap / 128 + L.P + 1;
-        L.n_etile_b = cap / 64 + L.P + 1;
+        // at most cap / tile + one partial tile per tiled range: forward
+        // tiles of 128 edges (16 KB) over ranges of two partitions, reverse
+        // tiles of 32 edges (8 KB) per partition
+        L.n_etile_f = cap / 128 + L.P / 2 + 2;
+        L.n_etile_b = cap / 32 + L.P + 1;
         L.etile_base = take(4 * 2 * ((size_t)L.P + 1));
         L.etile_f = take((size_t)L.n_etile_f * 16384);
-        L.etile_b = take((size_t)L.n_etile_b * 16384);
+        L.etile_b = take((size_t)L.n_etile_b * 8192);
     }
     if (path == MLFF_PATH_PLAIN_FP32 || path == MLFF_PATH_TRAIN || dual) {
         L.geo = take(4 * fs * cap);

@@ -28,11 +28,12 @@
 //
 // TMEM (512 columns): [0,128) lo halves of W2 chunks 0 and 1; [128,512) the
 // GEMM2 accumulators (forward: 128-edge tiles, chunk g at 128 + 128 g;
-// reverse: 64-edge tiles with [f | f'] per chunk, f' = df/dd in forward
-// mode); GEMM1's output aliases one chunk until epilogue 1 has read it:
-// chunk 0 in the forward kernel (read by the scalar warps only, so the next
-// tile's GEMM1 is issued while the vector warps finish epilogue 2), chunk 2
-// ([z; z']) in the reverse kernel.
+// reverse: two pipelines of 32-edge tiles, 192 columns each, with [f | f']
+// per chunk, f' = df/dd in forward mode); GEMM1's output aliases one chunk
+// until epilogue 1 has read it: chunk 0 in the forward kernel (read by the
+// scalar warps only, so the next tile's GEMM1 is issued while the vector
+// warps finish epilogue 2), chunk 2 ([z; z']) of the pipeline in the
+// reverse kernel.
 #include <cuda_fp16.h>
 #include <mutex>
 #include "common.cuh"
@@ -54,12 +55,11 @@ constexpr uint32_t W2L_BYTES = 8 * A_TILE;    // lo tiles of W2 chunk 2 (residen
 
 // TMEM columns (512 allocated): [0,128) the lo halves of W2 chunks 0 and 1
 // as MMA A operands (chunk g, K-step s at 64 g + 8 s); [128,512) the GEMM2
-// accumulators, chunk g at 128 + 128 g; GEMM1 writes z into the columns
-// of chunk 0 (forward) or 2 (reverse, TM_Z), which epilogue 1 reads before
-// it refills them with the bias.
+// accumulators (forward: chunk g at 128 + 128 g, GEMM1 writes z into chunk
+// 0's columns, which epilogue 1 reads before it refills them with the bias;
+// reverse: see the reverse kernel).
 constexpr uint32_t TM_W2LO = 0;
 constexpr uint32_t TM_F = 128;
-constexpr uint32_t TM_Z = 384;
 
 // ------------------------------------------------------------- packing
 // W1 [H][RMAX] -> 2 K-step blocks (hi, lo); W2 [3H][H] -> 24 hi tiles
@@ -174,19 +174,26 @@ __device__ __forceinline__ void rbf16_d(float d, bool valid, int r0, int R, cons
 
 // ------------------------------------------------------ E tiles (per call)
 // The RBF x cutoff rows of every edge tile as split fp16 in the K-major
-// no-swizzle layout (16-byte core matrices: K-step s at 4096 s, its second 8
-// columns 2048 further, 8-row groups 128 apart; the hi image, then the lo
-// image 8 KB later), computed once per call for all layers: forward tiles of
-// 128 edges, reverse tiles of 64 edges with the d-derivative rows 64-127.
-// Tiles follow the receiver partitions, so tile k of partition p is the k-th
-// tile its CTA processes.
-constexpr uint32_t ET_BYTES = 16384, ET_HALF = 8192;
-__device__ __forceinline__ uint32_t et_off(int row, int k) {
-    return (uint32_t)((k >> 4) * 4096 + ((k >> 3) & 1) * 2048 + (row >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+// no-swizzle layout (16-byte core matrices: K-step s at rows * 32 s, its
+// second 8 columns rows * 16 further, 8-row groups 128 apart; the hi image,
+// then the lo image rows * 64 further), computed once per call for all
+// layers.  Forward tiles: 128 edges, one row each, over receiver ranges of
+// two partitions (the forward kernel walks a CTA's two partitions as one
+// range).  Reverse tiles: 32 edges, rows 0-31 the RBF rows and rows 32-63
+// their d-derivatives, per partition.  Tile k of a range is the k-th tile
+// its kernel processes.
+constexpr uint32_t ET_BYTES = 16384, ET_HALF = 8192;     // forward: 128 rows
+constexpr uint32_t ETR_BYTES = 8192, ETR_HALF = 4096;    // reverse: 64 rows
+constexpr int FWD_GROUP = 2;                              // partitions per forward range
+__device__ __forceinline__ uint32_t et_off(int rows, int row, int k) {
+    return (uint32_t)((k >> 4) * rows * 32 + ((k >> 3) & 1) * rows * 16 + (row >> 3) * 128 + (row & 7) * 16 +
+                      (k & 7) * 2);
 }
+__host__ __device__ constexpr int fwd_ranges(int nparts) { return (nparts + FWD_GROUP - 1) / FWD_GROUP; }
 
-// tile counts of all partitions, then an exclusive scan (one block, the
-// partitions taken 1024 at a time)
+// Tile counts of all forward ranges and reverse partitions, then exclusive
+// scans (one block, 1024 at a time): forward bases at base[0..R], reverse
+// bases at base[P+1 .. 2P+1].
 __global__ void __launch_bounds__(1024) etile_index_kernel(const int32_t* __restrict__ row_ptr,
                                                            const int32_t* __restrict__ part, int P,
                                                            int32_t* __restrict__ base) {
@@ -195,15 +202,19 @@ __global__ void __launch_bounds__(1024) etile_index_kernel(const int32_t* __rest
     __shared__ int cf[1024], cb[1024];
     __shared__ int carry[2];
     const int t = threadIdx.x;
+    const int R = fwd_ranges(P);
     if (t == 0) carry[0] = carry[1] = 0;
     __syncthreads();
     for (int p0 = 0; p0 < P; p0 += 1024) {
         const int p = p0 + t;
         int nf = 0, nb = 0;
+        if (p < R) {
+            const int E = row_ptr[part[min(FWD_GROUP * p + FWD_GROUP, P)]] - row_ptr[part[FWD_GROUP * p]];
+            nf = (E + 127) / 128;
+        }
         if (p < P) {
             const int E = row_ptr[part[p + 1]] - row_ptr[part[p]];
-            nf = (E + 127) / 128;
-            nb = (E + 63) / 64;
+            nb = (E + 31) / 32;
         }
         cf[t] = nf;
         cb[t] = nb;
@@ -215,10 +226,8 @@ __global__ void __launch_bounds__(1024) etile_index_kernel(const int32_t* __rest
             cb[t] += xb;
             __syncthreads();
         }
-        if (p < P) {
-            base[p] = carry[0] + cf[t] - nf;
-            base[P + 1 + p] = carry[1] + cb[t] - nb;
-        }
+        if (p < R) base[p] = carry[0] + cf[t] - nf;
+        if (p < P) base[P + 1 + p] = carry[1] + cb[t] - nb;
         __syncthreads();
         if (t == 1023) {
             carry[0] += cf[1023];
@@ -227,7 +236,7 @@ __global__ void __launch_bounds__(1024) etile_index_kernel(const int32_t* __rest
         __syncthreads();
     }
     if (t == 0) {
-        base[P] = carry[0];
+        base[R] = carry[0];
         base[2 * P + 1] = carry[1];
     }
 }
@@ -244,14 +253,21 @@ __global__ void __launch_bounds__(256) etile_fill_kernel(EdgeArgs a, const int32
     }
     __syncthreads();
     if (a.st->code != 0) return;
-    constexpr int TN = REV ? 64 : 128;
-    const int t = threadIdx.x;
-    const int row = t & (TN - 1), s = (t / TN) & 1, which = REV ? (t >> 7) : 0;
-    for (int p = blockIdx.x; p < a.nparts; p += gridDim.x) {
-        const int e0 = a.row_ptr[a.part[p]], e1 = a.row_ptr[a.part[p + 1]];
+    constexpr int TE = REV ? 32 : 128;                  // edges per tile
+    constexpr int ROWS = REV ? 64 : 128;                // rows per tile
+    constexpr uint32_t BYTES = ROWS * 128, HALF = ROWS * 64;
+    constexpr int PER = 2 * ROWS;                       // threads per tile: (row, K-step)
+    constexpr int TPI = 256 / PER;                      // tiles per block iteration
+    const int t = threadIdx.x, sub = t / PER, loc = t % PER;
+    const int row = loc % ROWS, s = loc / ROWS;
+    const int which = REV ? (row >> 5) : 0, erow = REV ? (row & 31) : row;
+    const int nr = REV ? a.nparts : fwd_ranges(a.nparts);
+    for (int p = blockIdx.x; p < nr; p += gridDim.x) {
+        const int g0 = REV ? p : FWD_GROUP * p, g1 = REV ? p + 1 : min(FWD_GROUP * p + FWD_GROUP, a.nparts);
+        const int e0 = a.row_ptr[a.part[g0]], e1 = a.row_ptr[a.part[g1]];
         const int b0 = base[(REV ? a.nparts + 1 : 0) + p];
-        for (int k = blockIdx.y; e0 + k * TN < e1; k += gridDim.y) {
-            const int e = e0 + k * TN + row;
+        for (int k = blockIdx.y * TPI + sub; e0 + k * TE < e1; k += gridDim.y * TPI) {
+            const int e = e0 + k * TE + erow;
             const bool valid = e < e1;
             const float d = valid ? a.geo[e].w : 0.f;
             float v[16];
@@ -261,22 +277,23 @@ __global__ void __launch_bounds__(256) etile_fill_kernel(EdgeArgs a, const int32
             __align__(16) __half2 lo[8];
 #pragma unroll
             for (int i = 0; i < 8; ++i) split2(v[2 * i], v[2 * i + 1], hi[i], lo[i]);
-            unsigned char* tile = out + (size_t)(b0 + k) * ET_BYTES;
-            const int trow = which * 64 + row;
-            *reinterpret_cast<uint4*>(tile + et_off(trow, 16 * s)) = *reinterpret_cast<const uint4*>(&hi[0]);
-            *reinterpret_cast<uint4*>(tile + et_off(trow, 16 * s + 8)) = *reinterpret_cast<const uint4*>(&hi[4]);
-            *reinterpret_cast<uint4*>(tile + ET_HALF + et_off(trow, 16 * s)) = *reinterpret_cast<const uint4*>(&lo[0]);
-            *reinterpret_cast<uint4*>(tile + ET_HALF + et_off(trow, 16 * s + 8)) = *reinterpret_cast<const uint4*>(&lo[4]);
+            unsigned char* tile = out + (size_t)(b0 + k) * BYTES;
+            *reinterpret_cast<uint4*>(tile + et_off(ROWS, row, 16 * s)) = *reinterpret_cast<const uint4*>(&hi[0]);
+            *reinterpret_cast<uint4*>(tile + et_off(ROWS, row, 16 * s + 8)) = *reinterpret_cast<const uint4*>(&hi[4]);
+            *reinterpret_cast<uint4*>(tile + HALF + et_off(ROWS, row, 16 * s)) = *reinterpret_cast<const uint4*>(&lo[0]);
+            *reinterpret_cast<uint4*>(tile + HALF + et_off(ROWS, row, 16 * s + 8)) =
+                *reinterpret_cast<const uint4*>(&lo[4]);
         }
     }
 }
 
 int launch_etiles(const EdgeArgs& a, int32_t* base, unsigned char* fwd, unsigned char* rev, cudaStream_t st) {
     MLFF_LAUNCH_PDL("etile_index", etile_index_kernel, 1, 1024, 0, st, a.row_ptr, a.part, a.nparts, base);
-    // tiles of a partition spread over gridDim.y blocks
-    MLFF_LAUNCH_PDL("etile_fill_fwd", etile_fill_kernel<false>, dim3(a.nparts, 16), 256, 0, st, a, base, fwd);
+    // tiles of a range spread over gridDim.y blocks
+    MLFF_LAUNCH_PDL("etile_fill_fwd", etile_fill_kernel<false>, dim3(fwd_ranges(a.nparts), 16), 256, 0, st, a, base,
+                    fwd);
     if (rev) {
-        MLFF_LAUNCH_PDL("etile_fill_rev", etile_fill_kernel<true>, dim3(a.nparts, 32), 256, 0, st, a, base, rev);
+        MLFF_LAUNCH_PDL("etile_fill_rev", etile_fill_kernel<true>, dim3(a.nparts, 16), 256, 0, st, a, base, rev);
     }
     return MLFF_OK;
 }
@@ -352,27 +369,28 @@ __device__ __forceinline__ int reduce_scatter8_index(int lane) {
     return ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
 }
 
-// Chunk g of GEMM2 for one 128-row B tile: D (TMEM columns 128 + 128 g) +=
-// W2[g] B^T with B the split-fp16 tile at Hs (hi half, then lo half HALF128
-// bytes later).  Per K-step: the resident hi tile times both halves of B,
-// then the lo tile (TMEM for chunks 0 and 1, shared memory for chunk 2)
-// times the hi half.  Every MMA accumulates (the epilogue filled TMEM with
-// the bias).  The three chunks are issued by three threads in parallel: a
-// thread issues about one MMA per 50 cycles and stalls while the tensor core
-// is busy, so one issuer adds its own latency to every MMA; each chunk keeps
-// a fixed accumulation order.
+// Chunk g of GEMM2 for one B tile of NR rows: D (TMEM columns dcol) +=
+// W2[g] B^T with B the split-fp16 tile at Hs (hi half, then lo half
+// 2 * b_block(NR) bytes later).  Per K-step: the resident hi tile times both
+// halves of B, then the lo tile (TMEM for chunks 0 and 1, shared memory for
+// chunk 2) times the hi half.  Every MMA accumulates (the epilogue filled
+// TMEM with the bias).  The three chunks are issued by three threads in
+// parallel: a thread issues about one MMA per 50 cycles and stalls while the
+// tensor core is busy, so one issuer adds its own latency to every MMA; each
+// chunk keeps a fixed accumulation order.
 constexpr uint32_t HALF128 = 2 * b_block(128);   // K = 128: two K-blocks
-__device__ __forceinline__ void issue_gemm2_chunk(int g, uint32_t tmem, const unsigned char* w2h,
+template <int NR>
+__device__ __forceinline__ void issue_gemm2_chunk(int g, uint32_t tmem, uint32_t dcol, const unsigned char* w2h,
                                                   const unsigned char* w2l, const unsigned char* Hs) {
-    constexpr uint32_t idesc = idesc_f16(128);
-    constexpr uint64_t DA = A_TILE >> 4, DH = HALF128 >> 4;
+    constexpr uint32_t idesc = idesc_f16(NR);
+    constexpr uint64_t DA = A_TILE >> 4, DH = (2 * b_block(NR)) >> 4;
     const uint64_t a_hi = sdesc(smem_u32(w2h), A_LBO, A_SBO) + (uint64_t)(8 * g) * DA;
     const uint64_t a_lo = sdesc(smem_u32(w2l), A_LBO, A_SBO);
     const uint64_t b0 = sdesc_b(smem_u32(Hs));
-    const uint32_t d = tmem + TM_F + 128 * g;
+    const uint32_t d = tmem + dcol;
 #pragma unroll 1
     for (int s = 0; s < 8; ++s) {
-        const uint64_t bh = b0 + (uint64_t)(b_kstep_off(128, s) >> 4);
+        const uint64_t bh = b0 + (uint64_t)(b_kstep_off(NR, s) >> 4);
         const uint64_t ah = a_hi + (uint64_t)s * DA;
         mma_f16(d, ah, bh, idesc, 1);
         mma_f16(d, ah, bh + DH, idesc, 1);
@@ -384,8 +402,9 @@ __device__ __forceinline__ void issue_gemm2_chunk(int g, uint32_t tmem, const un
 // out = base + (sum over the receiver's edges): receivers in [j0, j1)
 // without edges get the base row (the epilogues store base + sum once per
 // receiver that has edges).
-__device__ __forceinline__ void zero_empty_rows(float* out, const int32_t* row_ptr, int j0, int j1, int w, int lane) {
-    for (int j = j0 + w; j < j1; j += NT / 32)
+__device__ __forceinline__ void zero_empty_rows(float* out, const int32_t* row_ptr, int j0, int j1, int w, int lane,
+                                                int nwarps = NT / 32) {
+    for (int j = j0 + w; j < j1; j += nwarps)
         if (row_ptr[j] == row_ptr[j + 1])
             for (int k = lane; k < 4 * H; k += 32) out[(int64_t)j * 4 * H + k] = 0.0f;
 }
@@ -505,8 +524,9 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
         mma_commit(mma_bar);
     };
     bool g1_issued = false;   // GEMM1 of the current tile already issued (at the end of the previous tile)
-    for (int p = blockIdx.x; p < a.nparts && !aborted; p += gridDim.x) {
-        const int j0 = a.part[p], j1 = a.part[p + 1];
+    // receiver ranges of FWD_GROUP consecutive partitions
+    for (int p = blockIdx.x; p < fwd_ranges(a.nparts) && !aborted; p += gridDim.x) {
+        const int j0 = a.part[FWD_GROUP * p], j1 = a.part[min(FWD_GROUP * p + FWD_GROUP, a.nparts)];
         if (j0 >= j1) continue;
         const int e0 = a.row_ptr[j0], e1 = a.row_ptr[j1];
         const int ntl = (e1 - e0 + FN - 1) / FN;
@@ -607,7 +627,7 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                     if (!mbar_wait(w2h_bar, 0, WAIT_BUDGET)) signal_timeout(a, abort_flag, 6);
                     w2h_ready = true;
                 }
-                issue_gemm2_chunk(w, tmem, w2h, w2l, Hs);
+                issue_gemm2_chunk<FN>(w, tmem, TM_F + 128 * w, w2h, w2l, Hs);
                 mma_commit(g2_bar);
             }
             if (w < 3) __syncwarp();   // lanes 1-31 of the issuing warps wait here, not in a spin loop
@@ -728,54 +748,105 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
 }
 
 // ------------------------------------------------------- reverse kernel
-// 64-edge tiles; E and E' (and then H and H') are stacked as rows 0-63 and
-// 64-127 of one 128-row B tile, so every MMA is N = 128: TMEM columns
-// [0,64) z^T, [64,128) z'^T, and per chunk g at 128 + 128 g: [0,64) f^T,
-// [64,128) f'^T.
-constexpr int BN = 64;
-constexpr uint32_t B_HH = 2 * b_block(2 * BN);
-static_assert(B_HH == HALF128, "GEMM2 B layout");
-constexpr uint32_t B_OFF_W1 = 0;
-constexpr uint32_t B_OFF_W2H = B_OFF_W1 + W1_BYTES;
-constexpr uint32_t B_OFF_H = align1k(B_OFF_W2H + W2_HALF);     // [H; H'] tile; the [E; E'] tile shares its start
-constexpr uint32_t B_OFF_W2L = align1k(B_OFF_H + 2 * B_HH);
-constexpr uint32_t B_SB_US = 0;
-constexpr uint32_t B_SB_SRC = B_SB_US + BN * 16;
-constexpr uint32_t B_SB_RCV = B_SB_SRC + BN * 4;
-constexpr uint32_t B_SB_SOFF = B_SB_RCV + BN * 4;
-constexpr uint32_t B_SB_ROFF = B_SB_SOFF + BN * 4;
-constexpr uint32_t B_SB_UC = B_SB_ROFF + BN * 4;
-constexpr uint32_t B_SB_CHG = B_SB_UC + 3 * BN * 4;
-constexpr uint32_t B_SB_EACC = B_SB_CHG + 16;
-constexpr uint32_t B_SB_BYTES = B_SB_EACC + BN * 16;
-constexpr uint32_t B_OFF_SB = B_OFF_W2L + W2L_BYTES;
-constexpr uint32_t B_OFF_B1 = B_OFF_SB + 2 * B_SB_BYTES;
-constexpr uint32_t B_OFF_B2 = B_OFF_B1 + H * 4;
-constexpr uint32_t B_OFF_RED = B_OFF_B2 + H3 * 4;
-constexpr uint32_t B_OFF_BAR = B_OFF_RED + 16 * BN * 2 * 4;
-constexpr uint32_t B_OFF_MISC = B_OFF_BAR + 8 * 5;
-constexpr uint32_t B_SMEM = align1k(B_OFF_MISC + 16);
-static_assert(ET_BYTES <= 2 * B_HH, "E tile fits in the H tile's space");
-static_assert(B_SMEM <= 232448, "reverse kernel shared memory");
+// Two independent pipelines per CTA, warps 0-7 and 8-15, each on its own
+// receiver partition (CTA b: partitions 2b and 2b + 1, then 2b + 2G ...),
+// so that one pipeline's MMAs, copies and barrier waits overlap the other
+// pipeline's CUDA-core epilogues.  A pipeline processes 32-edge tiles with
+// E and E' (then H and H') stacked as rows 0-31 / 32-63 of one 64-row B
+// tile: every MMA is 128 x 64 x 16 and one pass gives the filter f and its
+// d-derivative f' (forward mode, no transposed GEMM, no stored activation).
+//
+// TMEM (512 columns): [0,128) the lo halves of W2 chunks 0-1 (shared A
+// operands); pipeline p owns [128 + 192 p, 320 + 192 p): chunk g at
+// + 64 g with f in its first 32 columns and f' in the next 32; GEMM1's
+// [z | z'] output aliases chunk 2 until epilogue 1 has read it.
+//
+// Epilogue 2 roles: warp (q, h) of a pipeline reads TMEM lane quarter q
+// (channels 32q..32q+31) and handles two feature components of every edge
+// of the tile: h = 0 the scalar and v_x, h = 1 v_y and v_z.  Node adjoints
+// are gathered from the sender side (exact: f(d_ab) = f(d_ba)) and summed per
+// receiver in registers; each thread adds its two components' shares of
+// dE/dd (and its dE/du components) before the cross-lane reduction.
+// Padding edges of a partial tile get h = h' = 0 and a zero bias fill, so
+// their filter is exactly zero and every gather runs unpredicated (padding
+// gathers read row 0).
+constexpr int PN = 32;                               // edges per reverse tile
+constexpr int PT = 256;                              // threads per pipeline
+constexpr uint32_t P_HH = 2 * b_block(2 * PN);       // one half (hi or lo) of a [H; H'] tile: 16 KB
+constexpr uint32_t R_SB_US = 0;
+constexpr uint32_t R_SB_SRC = R_SB_US + PN * 16;
+constexpr uint32_t R_SB_RCV = R_SB_SRC + PN * 4;
+constexpr uint32_t R_SB_SOFF = R_SB_RCV + PN * 4;
+constexpr uint32_t R_SB_ROFF = R_SB_SOFF + PN * 4;
+constexpr uint32_t R_SB_UC = R_SB_ROFF + PN * 4;
+constexpr uint32_t R_SB_CHG = R_SB_UC + 3 * PN * 4;
+constexpr uint32_t R_SB_EACC = R_SB_CHG + 16;
+constexpr uint32_t R_SB_BYTES = R_SB_EACC + PN * 16;
+constexpr uint32_t R_OFF_W1 = 0;
+constexpr uint32_t R_OFF_W2H = R_OFF_W1 + W1_BYTES;
+constexpr uint32_t R_OFF_H = align1k(R_OFF_W2H + W2_HALF);   // pipeline p's [H; H'] tile at + 2 P_HH p
+constexpr uint32_t R_OFF_W2L = align1k(R_OFF_H + 4 * P_HH);
+constexpr uint32_t R_OFF_SB = R_OFF_W2L + W2L_BYTES;        // [pipeline][buffer] edge arrays
+constexpr uint32_t R_OFF_B1 = R_OFF_SB + 4 * R_SB_BYTES;
+constexpr uint32_t R_OFF_B2 = R_OFF_B1 + H * 4;
+constexpr uint32_t R_OFF_RED = R_OFF_B2 + H3 * 4;            // [pipeline][warp][edge][3] partial sums
+constexpr uint32_t R_RED_FLOATS = 8 * PN * 3;
+constexpr uint32_t R_OFF_BAR = R_OFF_RED + 2 * R_RED_FLOATS * 4;
+constexpr uint32_t R_OFF_MISC = R_OFF_BAR + 8 * 8;
+constexpr uint32_t R_SMEM = align1k(R_OFF_MISC + 16);
+static_assert(ETR_BYTES <= 2 * P_HH, "E tile fits in the H tile's space");
+static_assert(R_SB_EACC % 16 == 0 && R_SB_BYTES % 16 == 0, "edge array alignment");
+static_assert(R_SMEM <= 232448, "reverse kernel shared memory");
+
+__device__ __forceinline__ void pipe_sync(int pp) {
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + pp), "r"(PT) : "memory");
+}
+// Pipeline barrier that also ORs v over the pipeline's threads: every thread
+// gets the same answer.
+__device__ __forceinline__ bool pipe_sync_or(int pp, bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.or.pred q, %2, %3, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(1 + pp), "r"(PT)
+        : "memory");
+    return r != 0;
+}
+
+// Sum 4 per-lane values over the 32 lanes of a warp (reduce-scatter):
+// afterwards lanes with (lane & 7) == 0 hold the sum of value index
+// bits 4..3 of the lane id.
+__device__ __forceinline__ float warp_reduce_scatter4(const float (&v)[4], int lane) {
+    float w2[2];
+    const bool b16 = lane & 16, b8 = lane & 8;
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        const float send = b16 ? v[j] : v[j + 2];
+        const float keep = b16 ? v[j + 2] : v[j];
+        w2[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+    const float send = b8 ? w2[0] : w2[1];
+    const float keep = b8 ? w2[1] : w2[0];
+    float w1 = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    w1 += __shfl_xor_sync(0xffffffffu, w1, 4);
+    w1 += __shfl_xor_sync(0xffffffffu, w1, 2);
+    w1 += __shfl_xor_sync(0xffffffffu, w1, 1);
+    return w1;
+}
 
 __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const unsigned char* __restrict__ w1g,
                                                             const unsigned char* __restrict__ w2g) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char* w1s = smem + B_OFF_W1;
-    unsigned char* w2h = smem + B_OFF_W2H;
-    unsigned char* Hs = smem + B_OFF_H;            // [H; H'] hi, then lo
-    unsigned char* Es = smem + B_OFF_H;            // [E; E'] tile (bulk-copied), before H is written
-    unsigned char* w2l = smem + B_OFF_W2L;        // resident lo tiles of W2 chunk 2
-    float* b1s = reinterpret_cast<float*>(smem + B_OFF_B1);
-    float* b2s = reinterpret_cast<float*>(smem + B_OFF_B2);
-    float* red = reinterpret_cast<float*>(smem + B_OFF_RED);   // [16 warps][BN][2]
-    uint64_t* mma_bar = reinterpret_cast<uint64_t*>(smem + B_OFF_BAR);
-    uint64_t* w2h_bar = mma_bar + 1;
-    uint64_t* e_bar = mma_bar + 2;
-    uint64_t* g2_bar = mma_bar + 3;                 // GEMM2: one commit per chunk issuer
-    uint64_t* never_bar = mma_bar + 4;              // test hook: nothing arrives here
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + B_OFF_MISC);
-    volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + B_OFF_MISC + 4);
+    unsigned char* w1s = smem + R_OFF_W1;
+    unsigned char* w2h = smem + R_OFF_W2H;
+    unsigned char* w2l = smem + R_OFF_W2L;        // resident lo tiles of W2 chunk 2
+    float* b1s = reinterpret_cast<float*>(smem + R_OFF_B1);
+    float* b2s = reinterpret_cast<float*>(smem + R_OFF_B2);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + R_OFF_BAR);
+    uint64_t* w2h_bar = bars;                       // resident W2 operands
+    uint64_t* never_bar = bars + 1;                 // test hook: nothing arrives here
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + R_OFF_MISC);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + R_OFF_MISC + 4);
 
     // waits for the previous kernel at entry: reading the status word first
     // and returning early keeps the main loop's register allocation lean
@@ -787,11 +858,13 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
         tmem_relinquish();
     }
     if (t == 0) {
-        mbar_init(mma_bar, 1);
         mbar_init(w2h_bar, 1);
-        mbar_init(e_bar, 1);
-        mbar_init(g2_bar, 3);
         mbar_init(never_bar, 1);
+        for (int p = 0; p < 2; ++p) {
+            mbar_init(bars + 2 + 3 * p, 1);   // GEMM1
+            mbar_init(bars + 3 + 3 * p, 1);   // E tile
+            mbar_init(bars + 4 + 3 * p, 3);   // GEMM2: one commit per chunk issuer
+        }
         fence_mbar_init();
         *abort_flag = 0;
     }
@@ -804,279 +877,343 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
     __syncthreads();
     fence_after_sync();
     const uint32_t tmem = *tslot;
-
-    uint32_t mma_phase = 0, g2_phase = 0;   // GEMM1 / GEMM2 barrier phases
-    bool w2h_ready = false;                 // (GEMM2 issuers)
     if (t == 32) load_w2_resident(w2h, w2l, w2g, w2h_bar);
-    const int q = w & 3, r = w >> 2;
+    const int q = w & 3;
     const int c = 32 * q + lane;
-    const int fidx = r * H + c;
     const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
-    load_w2_lo_tmem(lane_base, reinterpret_cast<const uint32_t*>(a.P + a.lo.w2_tm), r, c);
+    load_w2_lo_tmem(lane_base, reinterpret_cast<const uint32_t*>(a.P + a.lo.w2_tm), w >> 2, c);
     tmem_st_wait();
     fence_before_sync();
     __syncthreads();
     fence_after_sync();
     pdl_trigger();   // after the TMEM allocation
-    const int rs_idx = reduce_scatter8_index(lane);
 
+    // ---- this thread's pipeline
+    const int pp = w >> 3, wl = w & 7, tp = t & (PT - 1), hh = wl >> 2;
+    const uint32_t TB = 128 + 192 * pp;             // the pipeline's TMEM columns
+    unsigned char* Hs = smem + R_OFF_H + pp * 2 * P_HH;   // [H; H'] hi, then lo
+    unsigned char* Es = Hs;                         // [E; E'] tile (bulk-copied) before H is written
+    uint64_t* mma_bar = bars + 2 + 3 * pp;
+    uint64_t* e_bar = bars + 3 + 3 * pp;
+    uint64_t* g2_bar = bars + 4 + 3 * pp;
+    float* red = reinterpret_cast<float*>(smem + R_OFF_RED) + pp * R_RED_FLOATS;
+    unsigned char* sbase = smem + R_OFF_SB + 2 * pp * R_SB_BYTES;
+    const int rs_idx = reduce_scatter8_index(lane);
+    const int rs4_idx = ((lane >> 4) & 1) * 2 + ((lane >> 3) & 1);
+    // components 2 hh and 2 hh + 1; the second sits H floats after the first
+    const int fidx0 = 2 * hh * H + c;
+    const float* xtb = a.xtbar + fidx0;
+    const float* xx = a.X + fidx0;
+    float* out = a.xbar + fidx0;
+
+    uint32_t mma_phase = 0, g2_phase = 0;   // GEMM1 / GEMM2 barrier phases
+    uint32_t e_phase = 0, e_issued = 0;     // E-tile copies: barrier phase, copies issued (thread tp 32)
+    bool w2h_ready = false;                 // (GEMM2 issuers)
     bool aborted = false;
-    uint32_t e_phase = 0, e_issued = 0;   // E-tile copies: barrier phase, copies issued (thread 32)
     auto prep = [&](unsigned char* sbx, int nn, int prev) {
-        if (t < BN)
-            tile_prep<BN>(t, nn, prev, reinterpret_cast<int*>(sbx + B_SB_SRC), reinterpret_cast<int*>(sbx + B_SB_RCV),
-                          reinterpret_cast<float4*>(sbx + B_SB_US), reinterpret_cast<int*>(sbx + B_SB_SOFF),
-                          reinterpret_cast<int*>(sbx + B_SB_ROFF), reinterpret_cast<float*>(sbx + B_SB_UC),
-                          reinterpret_cast<uint32_t*>(sbx + B_SB_CHG));
+        tile_prep<PN>(tp, nn, prev, reinterpret_cast<int*>(sbx + R_SB_SRC), reinterpret_cast<int*>(sbx + R_SB_RCV),
+                      reinterpret_cast<float4*>(sbx + R_SB_US), reinterpret_cast<int*>(sbx + R_SB_SOFF),
+                      reinterpret_cast<int*>(sbx + R_SB_ROFF), reinterpret_cast<float*>(sbx + R_SB_UC),
+                      reinterpret_cast<uint32_t*>(sbx + R_SB_CHG));
     };
-    for (int p = blockIdx.x; p < a.nparts && !aborted; p += gridDim.x) {
+    auto fetch = [&](unsigned char* sbx, int t0, int nn) {
+        fetch_tile_edges(a, tp, PN, t0, nn, reinterpret_cast<float4*>(sbx + R_SB_US),
+                         reinterpret_cast<int*>(sbx + R_SB_SRC), reinterpret_cast<int*>(sbx + R_SB_RCV),
+                         a.eacc_init ? nullptr : reinterpret_cast<float4*>(sbx + R_SB_EACC));
+    };
+    for (int p = 2 * blockIdx.x + pp; p < a.nparts && !aborted; p += 2 * gridDim.x) {
         const int j0 = a.part[p], j1 = a.part[p + 1];
         if (j0 >= j1) continue;
         const int e0 = a.row_ptr[j0], e1 = a.row_ptr[j1];
-        const int ntl = (e1 - e0 + BN - 1) / BN;
-        const unsigned char* etiles = a.etile + (size_t)a.etile_base[p] * ET_BYTES;
-        if (a.write_nodes) zero_empty_rows(a.xbar, a.row_ptr, j0, j1, w, lane);
+        const int ntl = (e1 - e0 + PN - 1) / PN;
+        const unsigned char* etiles = a.etile + (size_t)a.etile_base[p] * ETR_BYTES;
+        if (a.write_nodes) zero_empty_rows(a.xbar, a.row_ptr, j0, j1, wl, lane, PT / 32);
         int cur = j0;
-        float acc = 0.f;
+        float acc0 = 0.f, acc1 = 0.f;   // node adjoints of the current receiver, two components
         if (ntl > 0) {   // the partition's first tile: edge arrays and [E; E'] tile
-            unsigned char* sb = smem + B_OFF_SB;
-            fetch_tile_edges(a, t, BN, e0, min(BN, e1 - e0), reinterpret_cast<float4*>(sb + B_SB_US),
-                             reinterpret_cast<int*>(sb + B_SB_SRC), reinterpret_cast<int*>(sb + B_SB_RCV),
-                             a.eacc_init ? nullptr : reinterpret_cast<float4*>(sb + B_SB_EACC));
-            if (t == 32) {
-                mbar_expect_tx(e_bar, ET_BYTES);
-                bulk_g2s(Es, etiles, ET_BYTES, e_bar);
+            fetch(sbase, e0, min(PN, e1 - e0));
+            if (tp == 32) {
+                mbar_expect_tx(e_bar, ETR_BYTES);
+                bulk_g2s(Es, etiles, ETR_BYTES, e_bar);
                 ++e_issued;
             }
             cp_async_wait_all();
-            __syncthreads();
-            prep(sb, min(BN, e1 - e0), j0);
-            __syncthreads();
+            pipe_sync(pp);
+            if (tp < PN) prep(sbase, min(PN, e1 - e0), j0);
+            pipe_sync(pp);
         }
         for (int k = 0; k < ntl; ++k) {
-            const int t0 = e0 + k * BN, n = min(BN, e1 - t0), buf = k & 1;
-            unsigned char* sb = smem + B_OFF_SB + buf * B_SB_BYTES;
-            unsigned char* sbn = smem + B_OFF_SB + (buf ^ 1) * B_SB_BYTES;
-            const int* rcv_s = reinterpret_cast<const int*>(sb + B_SB_RCV);
-            const int* soff = reinterpret_cast<const int*>(sb + B_SB_SOFF);
-            const int* roff = reinterpret_cast<const int*>(sb + B_SB_ROFF);
-            const float* uc = reinterpret_cast<const float*>(sb + B_SB_UC);
-            const uint32_t* chg = reinterpret_cast<const uint32_t*>(sb + B_SB_CHG);
-            if (t == 0) {   // [z; z']^T = W1 [e; e']^T on the bulk-copied tile
+            const int t0 = e0 + k * PN, n = min(PN, e1 - t0), buf = k & 1;
+            unsigned char* sb = sbase + buf * R_SB_BYTES;
+            unsigned char* sbn = sbase + (buf ^ 1) * R_SB_BYTES;
+            const int* rcv_s = reinterpret_cast<const int*>(sb + R_SB_RCV);
+            const int* soff = reinterpret_cast<const int*>(sb + R_SB_SOFF);
+            const int* roff = reinterpret_cast<const int*>(sb + R_SB_ROFF);
+            const float* uc = reinterpret_cast<const float*>(sb + R_SB_UC);
+            if (tp == 0) {   // [z; z']^T = W1 [e; e']^T on the bulk-copied tile
                 if (!mbar_wait(e_bar, e_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 18);
                 fence_after_sync();
-                constexpr uint32_t idesc = idesc_f16(2 * BN);
+                constexpr uint32_t idesc = idesc_f16(2 * PN);
 #pragma unroll
                 for (int s = 0; s < 2; ++s)
 #pragma unroll
                     for (int pr = 0; pr < 3; ++pr) {
                         const uint32_t ahl = pr == 2 ? 1 : 0, bhl = pr == 1 ? 1 : 0;
                         const uint64_t ad = sdesc(smem_u32(w1s + s * SLAB + ahl * A_TILE), A_LBO, A_SBO);
-                        const uint64_t bd = sdesc(smem_u32(Es + bhl * ET_HALF + s * 4096), 2048, 128);
-                        mma_f16(tmem + TM_Z, ad, bd, idesc, (s | pr) != 0);
+                        const uint64_t bd = sdesc(smem_u32(Es + bhl * ETR_HALF + s * (2 * PN * 32)), 2 * PN * 16, 128);
+                        mma_f16(tmem + TB + 128, ad, bd, idesc, (s | pr) != 0);
                     }
                 mma_commit(mma_bar);
             }
             e_phase ^= 1;
-            if (w == 0) __syncwarp();
-            // only warp 0 polls the MMA barrier; the others wait at the CTA
-            // barrier instead of spinning on shared memory the MMAs read from
-            if (w == 0 && (a.stall_test & 2) && k == 0 && !mbar_wait(never_bar, 0, STALL_BUDGET))
-                signal_timeout(a, abort_flag, WHERE_STALL_TEST);
-            if (w == 0 && !mbar_wait(mma_bar, mma_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 11);
+            if (wl == 0) {
+                __syncwarp();
+                // one warp polls the MMA barrier; the others wait at the
+                // pipeline barrier instead of spinning
+                if ((a.stall_test & 2) && k == 0 && !mbar_wait(never_bar, 0, STALL_BUDGET))
+                    signal_timeout(a, abort_flag, WHERE_STALL_TEST);
+                if (!mbar_wait(mma_bar, mma_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 11);
+            }
             mma_phase ^= 1;
             fence_before_sync();
-            __syncthreads();
+            pipe_sync(pp);
             fence_after_sync();
-            {   // epilogue 1: h = silu(z + b1) (rows 0-63), h' = silu'(z + b1) z'
-                // (rows 64-127), 16 edges per warp
-                const int k = c, col = 16 * r;
-                const float bias = b1s[k];
+            {   // epilogue 1: h = silu(z + b1) (rows 0-31), h' = silu'(z + b1) z'
+                // (rows 32-63); warp (q, hh) takes hidden unit c of edges 16 hh..16 hh + 15
+                const int col = 16 * hh, nv = n - col;   // valid edges among this warp's 16
+                const float bias = b1s[c];
                 float z[16], zd[16];
-                tmem_ld16(lane_base + TM_Z + col, z);
-                tmem_ld16(lane_base + TM_Z + BN + col, zd);
+                tmem_ld16(lane_base + TB + 128 + col, z);
+                tmem_ld16(lane_base + TB + 128 + PN + col, zd);
                 tmem_ld_wait();
-                const BColumn hc(Hs, B_HH, 2 * BN, col, k), hdc(Hs, B_HH, 2 * BN, BN + col, k);
+                const BColumn hc(Hs, P_HH, 2 * PN, col, c), hdc(Hs, P_HH, 2 * PN, PN + col, c);
 #pragma unroll
                 for (int i = 0; i < 16; i += 2) {
                     const float z0 = z[i] + bias, z1 = z[i + 1] + bias;
                     const float s0 = fast_sigmoid(z0), s1 = fast_sigmoid(z1);
-                    hc.put_pair(i, z0 * s0, z1 * s1);
-                    hdc.put_pair(i, s0 * (1.0f + z0 * (1.0f - s0)) * zd[i], s1 * (1.0f + z1 * (1.0f - s1)) * zd[i + 1]);
+                    const bool v0 = i < nv, v1 = i + 1 < nv;
+                    hc.put_pair(i, v0 ? z0 * s0 : 0.f, v1 ? z1 * s1 : 0.f);
+                    hdc.put_pair(i, v0 ? s0 * (1.0f + z0 * (1.0f - s0)) * zd[i] : 0.f,
+                                 v1 ? s1 * (1.0f + z1 * (1.0f - s1)) * zd[i + 1] : 0.f);
                 }
-                // f = W2 h accumulates onto b2 and f' = W2 h' onto 0 (each chunk:
-                // 64 columns f^T, then 64 columns f'^T).  This warp refills the
-                // chunk-2 cells it has just read (f then f'), and 64 columns of
-                // chunks 0 and 1: r = 0 chunk 0 f, 1 chunk 0 f', 2 chunk 1 f, 3 chunk 1 f'.
-                float bv[16];
-                const float b2c = b2s[2 * H + c];
+                // f = W2 h accumulates onto b2 (0 for padding edges), f' = W2 h'
+                // onto 0: this warp refills the chunk-2 cells it has just read
+                // and chunk hh (f: 32 columns, f': 32 columns)
+                float bv[16], bz[16];
+                const float b2c = b2s[2 * H + c], bch = b2s[hh * H + c];
 #pragma unroll
-                for (int i = 0; i < 16; ++i) bv[i] = b2c;
-                tmem_st16(lane_base + TM_Z + col, bv);
+                for (int i = 0; i < 16; ++i) {
+                    bv[i] = i < nv ? b2c : 0.0f;
+                    bz[i] = 0.0f;
+                }
+                tmem_st16(lane_base + TB + 128 + col, bv);
+                tmem_st16(lane_base + TB + 128 + PN + col, bz);
 #pragma unroll
-                for (int i = 0; i < 16; ++i) bv[i] = 0.0f;
-                tmem_st16(lane_base + TM_Z + BN + col, bv);
-                const float b01 = (r & 1) ? 0.0f : b2s[(r >> 1) * H + c];
+                for (int i = 0; i < 16; ++i) bv[i] = i < n ? bch : 0.0f;
+                tmem_st16(lane_base + TB + 64 * hh, bv);
 #pragma unroll
-                for (int i = 0; i < 16; ++i) bv[i] = b01;
-#pragma unroll
-                for (int kk = 0; kk < 4; ++kk) tmem_st16(lane_base + TM_F + 64 * r + 16 * kk, bv);
+                for (int i = 0; i < 16; ++i) bv[i] = 16 + i < n ? bch : 0.0f;
+                tmem_st16(lane_base + TB + 64 * hh + 16, bv);
+                tmem_st16(lane_base + TB + 64 * hh + PN, bz);
+                tmem_st16(lane_base + TB + 64 * hh + PN + 16, bz);
                 tmem_st_wait();
             }
             fence_async_smem();
             fence_before_sync();
-            __syncthreads();
-            // epilogue 2's first two 8-edge blocks of gathers are issued while GEMM2 runs
-            float tba[8], xba[8], tra[8], tbn[8], xbn[8], trn[8];
-            auto gather8 = [&](float (&tb)[8], float (&xb)[8], float (&tr)[8], int col) {
+            pipe_sync(pp);
+            // epilogue 2's first two 4-edge blocks of gathers are issued while
+            // GEMM2 runs: the senders' dE/dXt and X rows, the receiver's dE/dXt
+            // row (once per block when no receiver starts inside it)
+            const uint32_t chw = *reinterpret_cast<const uint32_t*>(sb + R_SB_CHG);
+            float tba0[4], tba1[4], xba0[4], xba1[4], tra0[4], tra1[4];
+            float tbb0[4], tbb1[4], xbb0[4], xbb1[4], trb0[4], trb1[4];
+            auto gather4 = [&](float (&tb0)[4], float (&tb1)[4], float (&xb0)[4], float (&xb1)[4], float (&tr0)[4],
+                               float (&tr1)[4], int col) {
+                const int4 so = *reinterpret_cast<const int4*>(soff + col);
+                const int sv[4] = {so.x, so.y, so.z, so.w};
 #pragma unroll
-                for (int i = 0; i < 8; i += 4) {
-                    const int4 so = *reinterpret_cast<const int4*>(soff + col + i);
-                    const int4 ro = *reinterpret_cast<const int4*>(roff + col + i);
-                    const int sv[4] = {so.x, so.y, so.z, so.w}, rv[4] = {ro.x, ro.y, ro.z, ro.w};
+                for (int i = 0; i < 4; ++i) {
+                    tb0[i] = __ldg(xtb + sv[i]);
+                    tb1[i] = __ldg(xtb + sv[i] + H);
+                    xb0[i] = __ldg(xx + sv[i]);
+                    xb1[i] = __ldg(xx + sv[i] + H);
+                }
+                if (((chw >> col) & 0xEu) == 0) {   // one receiver for the whole block
+                    const int ro = roff[col];
+                    const float r0 = __ldg(xtb + ro), r1 = __ldg(xtb + ro + H);
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        const bool ok = col + i + k < n;
-                        tb[i + k] = ok ? __ldg(a.xtbar + sv[k] + fidx) : 0.f;
-                        xb[i + k] = ok ? __ldg(a.X + sv[k] + fidx) : 0.f;
-                        tr[i + k] = ok ? __ldg(a.xtbar + rv[k] + fidx) : 0.f;
+                    for (int i = 0; i < 4; ++i) {
+                        tr0[i] = r0;
+                        tr1[i] = r1;
+                    }
+                } else {
+                    const int4 ro = *reinterpret_cast<const int4*>(roff + col);
+                    const int rv[4] = {ro.x, ro.y, ro.z, ro.w};
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        tr0[i] = __ldg(xtb + rv[i]);
+                        tr1[i] = __ldg(xtb + rv[i] + H);
                     }
                 }
             };
-            gather8(tba, xba, tra, 0);
-            if (8 < n) gather8(tbn, xbn, trn, 8);
-            if (w < 3 && lane == 0) {   // [f; f']^T = W2 [h; h']^T, chunk w issued by warp w
+            gather4(tba0, tba1, xba0, xba1, tra0, tra1, 0);
+            if (4 < n) gather4(tbb0, tbb1, xbb0, xbb1, trb0, trb1, 4);
+            if (wl < 3 && lane == 0) {   // [f; f']^T = W2 [h; h']^T, chunk wl issued by warp wl
                 fence_after_sync();
                 if (!w2h_ready) {
                     if (!mbar_wait(w2h_bar, 0, WAIT_BUDGET)) signal_timeout(a, abort_flag, 16);
                     w2h_ready = true;
                 }
-                issue_gemm2_chunk(w, tmem, w2h, w2l, Hs);
+                issue_gemm2_chunk<2 * PN>(wl, tmem, TB + 64 * wl, w2h, w2l, Hs);
                 mma_commit(g2_bar);
             }
-            if (w < 3) __syncwarp();   // lanes 1-31 of the issuing warps wait here, not in a spin loop
-            // only warp 0 polls the MMA barrier; the others wait at the CTA
-            // barrier instead of spinning on shared memory the MMAs read from
-            if (w == 0 && !mbar_wait(g2_bar, g2_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 14);
+            if (wl < 3) __syncwarp();   // lanes 1-31 of the issuing warps wait here, not in a spin loop
+            if (wl == 0 && !mbar_wait(g2_bar, g2_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 14);
             g2_phase ^= 1;
             fence_before_sync();
-            __syncthreads();
+            // the abort decision is the same for every thread of the pipeline
+            const bool abort_now = pipe_sync_or(pp, *abort_flag != 0);
             fence_after_sync();
-            // the H tile is free too: the next tile's [E; E'] tile and edge
-            // arrays arrive while epilogue 2 runs
-            const bool more = k + 1 < ntl && !*abort_flag;
+            // the H tile is free: the next tile's [E; E'] tile and edge arrays
+            // arrive while epilogue 2 runs
+            const bool more = k + 1 < ntl && !abort_now;
             if (more) {
-                fetch_tile_edges(a, t, BN, t0 + BN, min(BN, e1 - t0 - BN), reinterpret_cast<float4*>(sbn + B_SB_US),
-                                 reinterpret_cast<int*>(sbn + B_SB_SRC), reinterpret_cast<int*>(sbn + B_SB_RCV),
-                                 a.eacc_init ? nullptr : reinterpret_cast<float4*>(sbn + B_SB_EACC));
-                if (t == 32) {
-                    mbar_expect_tx(e_bar, ET_BYTES);
-                    bulk_g2s(Es, etiles + (size_t)(k + 1) * ET_BYTES, ET_BYTES, e_bar);
+                fetch(sbn, t0 + PN, min(PN, e1 - t0 - PN));
+                if (tp == 32) {
+                    mbar_expect_tx(e_bar, ETR_BYTES);
+                    bulk_g2s(Es, etiles + (size_t)(k + 1) * ETR_BYTES, ETR_BYTES, e_bar);
                     ++e_issued;
                 }
             }
-            if (w == 1) __syncwarp();
-            {   // epilogue 2: component r of the node adjoints (gathered from the
-                // sender side, summed per receiver) and this component's share
-                // of dE/dd, dE/du; 8-edge blocks, the next block's gathers in
-                // flight.  Padding edges gather 0, so they add nothing.
-                const uint32_t f1col = r == 0 ? 128 : 256, d1col = f1col + BN;
-                const float* ur = uc + (r == 0 ? 0 : (r - 1) * BN);
-                float* out = a.xbar + fidx;        // gathered adjoint; dE/dXt is added afterwards
-                auto process8 = [&](const float (&tb)[8], const float (&xb)[8], const float (&tr)[8], int col) {
-                    float f1[8], f2[8], d1[8], d2[8];
-                    tmem_ld8(lane_base + f1col + col, f1);   // phi_s or phi_v1 (bias included)
-                    tmem_ld8(lane_base + d1col + col, d1);   // its d-derivative
-                    if (r != 0) {
-                        tmem_ld8(lane_base + 384 + col, f2);       // phi_v2 (bias included)
-                        tmem_ld8(lane_base + 384 + BN + col, d2);  // dphi_v2/dd
+            if (wl == 1) __syncwarp();
+            {   // epilogue 2 over 4-edge blocks, the next block's gathers in flight
+                auto process4 = [&](const float (&tb0)[4], const float (&tb1)[4], const float (&xb0)[4],
+                                    const float (&xb1)[4], const float (&tr0)[4], const float (&tr1)[4], int col) {
+                    float fa[4], da[4], f1[4], d1[4], f2[4], d2[4];
+                    if (hh == 0) {
+                        tmem_ld4(lane_base + TB + col, fa);        // phi_s (bias included)
+                        tmem_ld4(lane_base + TB + PN + col, da);   // dphi_s / dd
                     }
-                    const uint32_t mask = (chg[col >> 5] >> (col & 31)) & 0xFFu;
+                    tmem_ld4(lane_base + TB + 64 + col, f1);       // phi_v1
+                    tmem_ld4(lane_base + TB + 64 + PN + col, d1);
+                    tmem_ld4(lane_base + TB + 128 + col, f2);      // phi_v2
+                    tmem_ld4(lane_base + TB + 128 + PN + col, d2);
+                    const uint32_t m = (chw >> col) & 0xFu;
                     tmem_ld_wait();
-                    if (mask == 0) {
+                    if (hh != 0) {
 #pragma unroll
-                        for (int i = 0; i < 8; ++i) acc = fmaf(tb[i], f1[i], acc);
-                    } else {   // a receiver changes in this block: flush its finished sum
+                        for (int i = 0; i < 4; ++i) {
+                            fa[i] = f1[i];
+                            da[i] = d1[i];
+                        }
+                    }
+                    if (m == 0) {
 #pragma unroll
-                        for (int i = 0; i < 8; ++i) {
-                            if (mask & (1u << i)) {
-                                if (a.write_nodes) out[(int64_t)cur * 4 * H] = acc;
+                        for (int i = 0; i < 4; ++i) {
+                            acc0 = fmaf(tb0[i], fa[i], acc0);
+                            acc1 = fmaf(tb1[i], f1[i], acc1);
+                        }
+                    } else {   // a receiver starts in this block: store the finished sums
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) {
+                            if (m & (1u << i)) {
+                                if (a.write_nodes) {
+                                    out[(int64_t)cur * 4 * H] = acc0;
+                                    out[(int64_t)cur * 4 * H + H] = acc1;
+                                }
                                 cur = rcv_s[col + i];
-                                acc = 0.f;
+                                acc0 = 0.f;
+                                acc1 = 0.f;
                             }
-                            acc = fmaf(tb[i], f1[i], acc);
+                            acc0 = fmaf(tb0[i], fa[i], acc0);
+                            acc1 = fmaf(tb1[i], f1[i], acc1);
                         }
                     }
-                    float p0[8], p1[8];
-                    if (r == 0) {
+                    // this thread's shares of dE/dd and dE/du for the 4 edges
+                    float pv[8], p2[4];
+                    if (hh == 0) {   // scalar and v_x
+                        const float* ux = uc + col;
 #pragma unroll
-                        for (int i = 0; i < 8; ++i) p0[i] = (tr[i] * xb[i]) * d1[i];
-                    } else {
-                        const float* u = ur + col;
+                        for (int i = 0; i < 4; ++i) {
+                            pv[i] = fmaf(tr0[i] * xb0[i], da[i], tr1[i] * fmaf(xb1[i], d1[i], ux[i] * d2[i]));
+                            pv[4 + i] = tr1[i] * f2[i];
+                        }
+                    } else {         // v_y and v_z
+                        const float* uy = uc + PN + col;
+                        const float* uz = uc + 2 * PN + col;
 #pragma unroll
-                        for (int i = 0; i < 8; ++i) {
-                            p0[i] = tr[i] * fmaf(xb[i], d1[i], u[i] * d2[i]);
-                            p1[i] = tr[i] * f2[i];
+                        for (int i = 0; i < 4; ++i) {
+                            pv[i] = fmaf(tr0[i], fmaf(xb0[i], d1[i], uy[i] * d2[i]),
+                                         tr1[i] * fmaf(xb1[i], d1[i], uz[i] * d2[i]));
+                            pv[4 + i] = tr0[i] * f2[i];
+                            p2[i] = tr1[i] * f2[i];
                         }
                     }
-                    const float s0 = warp_reduce_scatter8(p0, lane);
-                    float s1 = 0.f;
-                    if (r != 0) s1 = warp_reduce_scatter8(p1, lane);
-                    if ((lane & 3) == 0) {
-                        float* rr = red + ((size_t)w * BN + col + rs_idx) * 2;
-                        rr[0] = s0;
-                        rr[1] = s1;
+                    const float s8 = warp_reduce_scatter8(pv, lane);
+                    if ((lane & 3) == 0) red[(wl * PN + col + (rs_idx & 3)) * 3 + (rs_idx >> 2)] = s8;
+                    if (hh != 0) {
+                        const float s4 = warp_reduce_scatter4(p2, lane);
+                        if ((lane & 7) == 0) red[(wl * PN + col + rs4_idx) * 3 + 2] = s4;
                     }
                 };
-                for (int col = 0; col < n; col += 16) {   // blocks col and col + 8 are in flight
-                    process8(tba, xba, tra, col);
-                    if (col + 8 >= n) break;
-                    if (col + 16 < n) gather8(tba, xba, tra, col + 16);
-                    process8(tbn, xbn, trn, col + 8);
-                    if (col + 24 < n) gather8(tbn, xbn, trn, col + 24);
+                for (int col = 0; col < n; col += 8) {   // blocks col and col + 4 are in flight
+                    process4(tba0, tba1, xba0, xba1, tra0, tra1, col);
+                    if (col + 4 >= n) break;
+                    if (col + 8 < n) gather4(tba0, tba1, xba0, xba1, tra0, tra1, col + 8);
+                    process4(tbb0, tbb1, xbb0, xbb1, trb0, trb1, col + 4);
+                    if (col + 12 < n) gather4(tbb0, tbb1, xbb0, xbb1, trb0, trb1, col + 12);
                 }
             }
-            if (more && t < BN) {   // the next tile's prep, by the two warps that fetched it
+            if (more && tp < PN) {   // the next tile's prep, by the warp that fetched it
                 cp_async_wait_all();
-                bar_sync_first(BN);
-                prep(sbn, min(BN, e1 - t0 - BN), rcv_s[BN - 1]);
+                __syncwarp();
+                prep(sbn, min(PN, e1 - t0 - PN), rcv_s[PN - 1]);
             }
             fence_before_sync();
-            __syncthreads();
-            if (t < n) {
-                float dd = 0.f, du[3] = {0.f, 0.f, 0.f};
+            pipe_sync(pp);
+            if (tp < n) {   // per-edge sums over the pipeline's 8 warps, fixed order
+                const float* rr = red + tp * 3;
+                float dd = 0.f, du0 = 0.f, du1 = 0.f, du2 = 0.f;
 #pragma unroll
-                for (int ww = 0; ww < 16; ++ww) {
-                    const float* rr = red + ((size_t)ww * BN + t) * 2;
-                    dd += rr[0];
-                    if (ww >= 4) du[(ww >> 2) - 1] += rr[1];
+                for (int ww = 0; ww < 8; ++ww) {
+                    const float* rw = rr + ww * PN * 3;
+                    dd += rw[0];
+                    if (ww < 4) du0 += rw[1];
+                    else {
+                        du1 += rw[1];
+                        du2 += rw[2];
+                    }
                 }
                 float4 ea = a.eacc_init ? make_float4(0.f, 0.f, 0.f, 0.f)
-                                        : reinterpret_cast<const float4*>(sb + B_SB_EACC)[t];
+                                        : reinterpret_cast<const float4*>(sb + R_SB_EACC)[tp];
                 ea.x += dd;
-                ea.y += du[0];
-                ea.z += du[1];
-                ea.w += du[2];
-                a.eacc[t0 + t] = ea;
+                ea.y += du0;
+                ea.z += du1;
+                ea.w += du2;
+                a.eacc[t0 + tp] = ea;
             }
-            if (*abort_flag) {
+            if (abort_now) {
                 aborted = true;
                 break;
             }
         }
-        if (!aborted && a.write_nodes) a.xbar[(int64_t)cur * 4 * H + fidx] = acc;
+        if (!aborted && a.write_nodes) {
+            out[(int64_t)cur * 4 * H] = acc0;
+            out[(int64_t)cur * 4 * H + H] = acc1;
+        }
     }
+    // drain: every MMA and copy this CTA issued must be complete before it
+    // frees its tensor memory and exits (after a timed-out wait the work it
+    // waited for may still be running).  A wait on the parity of the phase
+    // before the current one returns at once, so these also hold when
+    // nothing was issued.
     __syncthreads();
-    // after a timed-out wait the MMAs it waited for may still be running: the
-    // last GEMM1 and GEMM2 committed must be complete (a wait on the parity of
-    // the phase before the current one returns at once, so this also holds
-    // when nothing was committed)
-    if (t == 0) {
+    if (tp == 0) {
         if (!mbar_wait(mma_bar, mma_phase ^ 1, WAIT_BUDGET)) set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 13);
         if (!mbar_wait(g2_bar, g2_phase ^ 1, WAIT_BUDGET)) set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 15);
     }
-    if (t == 32) {
-        if (!mbar_wait(w2h_bar, 0, WAIT_BUDGET)) set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 17);
+    if (tp == 32) {
+        if (t == 32 && !mbar_wait(w2h_bar, 0, WAIT_BUDGET)) set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 17);
         if (e_issued > 0 && !mbar_wait(e_bar, (e_issued - 1) & 1, WAIT_BUDGET))
             set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 19);
     }
@@ -1108,7 +1245,7 @@ int launch_edge_fwd_tc(const EdgeArgs& a, int layer, cudaStream_t st) {
     if (attr_err != cudaSuccess) return cuda_status(attr_err, "edge_fwd_tc smem attribute");
     const unsigned char* w1 = reinterpret_cast<const unsigned char*>(a.P + a.lo.w1_bf);
     const unsigned char* w2 = reinterpret_cast<const unsigned char*>(a.P + a.lo.w2_bf);
-    MLFF_LAUNCH_PDL("edge_fwd_tc", edge_fwd_tc_kernel, tc_grid(a.nparts), NT, F_SMEM, st, a, w1, w2);
+    MLFF_LAUNCH_PDL("edge_fwd_tc", edge_fwd_tc_kernel, tc_grid(fwd_ranges(a.nparts)), NT, F_SMEM, st, a, w1, w2);
     return MLFF_OK;
 }
 
@@ -1117,12 +1254,13 @@ int launch_edge_bwd_tc(const EdgeArgs& a, int layer, cudaStream_t st) {
     static std::once_flag once;
     static cudaError_t attr_err = cudaSuccess;
     std::call_once(once, [] {
-        attr_err = cudaFuncSetAttribute(edge_bwd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, B_SMEM);
+        attr_err = cudaFuncSetAttribute(edge_bwd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, R_SMEM);
     });
     if (attr_err != cudaSuccess) return cuda_status(attr_err, "edge_bwd_tc smem attribute");
     const unsigned char* w1 = reinterpret_cast<const unsigned char*>(a.P + a.lo.w1_bf);
     const unsigned char* w2 = reinterpret_cast<const unsigned char*>(a.P + a.lo.w2_bf);
-    MLFF_LAUNCH_PDL("edge_bwd_tc", edge_bwd_tc_kernel, tc_grid(a.nparts), NT, B_SMEM, st, a, w1, w2);
+    // two pipelines (partitions) per CTA
+    MLFF_LAUNCH_PDL("edge_bwd_tc", edge_bwd_tc_kernel, tc_grid((a.nparts + 1) / 2), NT, R_SMEM, st, a, w1, w2);
     return MLFF_OK;
 }
 
