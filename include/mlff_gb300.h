@@ -338,6 +338,47 @@ int mlff_param_grads_forces(const mlff_dims *dims, const void *packed, const mlf
 int mlff_profile_begin(void);
 int mlff_profile_end(double *ms_by_kind, int64_t *launches_by_kind, int32_t n_kinds);
 
+/* Per-module blocks, any hidden width H and number of basis functions R:
+ * the reference's PaiNNMessage.forward (src/mlff_distiller/models/
+ * student_model.py:324-387) and PaiNNUpdate.forward (:418-470) and their
+ * reverse passes, for callers that use the blocks outside StudentForceField
+ * (the fused path does not call these).  FP32, float-atomic scatter as
+ * index_add_ on a GPU.  Layouts as the reference's tensors: scalar [N,H],
+ * vector [N,3,H], edge_index int64 [2,E] (row 0 senders, row 1
+ * receivers), edge_rbf [E,R], edge_vector [E,3], weights in nn.Linear's
+ * [out,in] layout, mixing [3,3].  Outputs must not alias inputs.  Each call
+ * needs a caller-owned workspace of *_workspace_size(..., with_backward)
+ * bytes (with_backward = 1 for the *_backward calls, which recompute the
+ * forward activations).  status (message calls): int32 [4] device; an
+ * out-of-range edge index gives MLFF_ERR_INVALID with the edge's position
+ * and the call stops after the residual copies. */
+size_t mlff_painn_message_workspace_size(int32_t hidden, int32_t n_rbf, int64_t n_edges, int32_t with_backward);
+int mlff_painn_message(int32_t hidden, int32_t n_rbf, int32_t n_atoms, int64_t n_edges, const float *scalar,
+                       const float *vector, const int64_t *edge_index, const float *edge_rbf,
+                       const float *edge_vector, const float *w1, const float *b1, const float *w2,
+                       const float *b2, float *scalar_out, float *vector_out, int32_t *status, void *workspace,
+                       size_t workspace_bytes, mlff_stream_t stream);
+/* grad_* = d(loss)/d(input or parameter) from grad_scalar_out / grad_vector_out */
+int mlff_painn_message_backward(int32_t hidden, int32_t n_rbf, int32_t n_atoms, int64_t n_edges,
+                                const float *scalar, const float *vector, const int64_t *edge_index,
+                                const float *edge_rbf, const float *edge_vector, const float *w1,
+                                const float *b1, const float *w2, const float *b2,
+                                const float *grad_scalar_out, const float *grad_vector_out, float *grad_scalar,
+                                float *grad_vector, float *grad_rbf, float *grad_edge_vector, float *grad_w1,
+                                float *grad_b1, float *grad_w2, float *grad_b2, int32_t *status,
+                                void *workspace, size_t workspace_bytes, mlff_stream_t stream);
+size_t mlff_painn_update_workspace_size(int32_t hidden, int32_t n_atoms, int32_t with_backward);
+int mlff_painn_update(int32_t hidden, int32_t n_atoms, const float *scalar, const float *vector,
+                      const float *w1, const float *b1, const float *w2, const float *b2, const float *mixing,
+                      float *scalar_out, float *vector_out, void *workspace, size_t workspace_bytes,
+                      mlff_stream_t stream);
+int mlff_painn_update_backward(int32_t hidden, int32_t n_atoms, const float *scalar, const float *vector,
+                               const float *w1, const float *b1, const float *w2, const float *b2,
+                               const float *mixing, const float *grad_scalar_out, const float *grad_vector_out,
+                               float *grad_scalar, float *grad_vector, float *grad_w1, float *grad_b1,
+                               float *grad_w2, float *grad_b2, float *grad_mixing, void *workspace,
+                               size_t workspace_bytes, mlff_stream_t stream);
+
 /* Test hook for the bounded device waits (no counterpart in the reference;
  * the timeout path replaces a hang where the reference would block).  While
  * bit 0 (forward) or bit 1 (reverse) of `kernels` is set, every CTA of the

@@ -570,6 +570,16 @@ static int run_plain_t(const mlff_dims& d, const float* P, const PackedOffsets& 
     return launch_forces(d, sys, L, ws, out, st);
 }
 
+// Float32 C[M][N] = A[M][K] B[K][N] (+ bias) for the per-module entry points
+// (modules.cu): mode 0 C = acc + bias; 1 also C2 = silu(C); 2 C = acc *
+// silu'(Z).
+int plain_sgemm(int mode, const float* A, const float* B, const float* bias, float* C, float* C2, const float* Z,
+                int64_t M, int N, int K, const Status* st, cudaStream_t s) {
+    if (mode == 0) return sgemm<0, float>(A, B, bias, C, C2, Z, M, nullptr, N, K, st, s);
+    if (mode == 1) return sgemm<1, float>(A, B, bias, C, C2, Z, M, nullptr, N, K, st, s);
+    return sgemm<2, float>(A, B, bias, C, C2, Z, M, nullptr, N, K, st, s);
+}
+
 int run_plain(const mlff_dims& d, const float* P, const PackedOffsets& po, const mlff_system& sys,
               const WsLayout& L, void* ws, const mlff_outputs& out, cudaStream_t st, const GradCtx* grad) {
     return run_plain_t<float>(d, P, po, sys, L, ws, out, st, grad, nullptr, nullptr);

@@ -45,7 +45,9 @@ EXPORTS = ["mlff_version", "mlff_last_error_string", "mlff_packed_weights_size",
            "mlff_md_energy_stats",
            "mlff_profile_begin",
            "mlff_profile_end", "mlff_radius_graph_noalloc", "mlff_param_grads", "mlff_param_grads_forces",
-           "mlff_debug_stall_test"]
+           "mlff_debug_stall_test", "mlff_painn_message_workspace_size", "mlff_painn_message",
+           "mlff_painn_message_backward", "mlff_painn_update_workspace_size", "mlff_painn_update",
+           "mlff_painn_update_backward"]
 
 PROFILE_KINDS = ["neighbors", "edge_fwd", "edge_bwd", "update_fwd", "update_bwd", "readout", "forces",
                  "plain_gemm", "plain_edge", "other", "md"]
@@ -166,6 +168,18 @@ def load(build_if_missing: bool = True):
         lib.mlff_param_grads_forces.restype = ctypes.c_int
         lib.mlff_param_grads_forces.argtypes = [ctypes.POINTER(Dims), _P, ctypes.POINTER(System), i64, _P, _P,
                                                 ctypes.POINTER(Grads), _P, sz, _P]
+        lib.mlff_painn_message_workspace_size.restype = sz
+        lib.mlff_painn_message_workspace_size.argtypes = [i32, i32, i64, i32]
+        lib.mlff_painn_message.restype = ctypes.c_int
+        lib.mlff_painn_message.argtypes = [i32, i32, i32, i64] + [_P] * 13 + [sz, _P]
+        lib.mlff_painn_message_backward.restype = ctypes.c_int
+        lib.mlff_painn_message_backward.argtypes = [i32, i32, i32, i64] + [_P] * 21 + [sz, _P]
+        lib.mlff_painn_update_workspace_size.restype = sz
+        lib.mlff_painn_update_workspace_size.argtypes = [i32, i32, i32]
+        lib.mlff_painn_update.restype = ctypes.c_int
+        lib.mlff_painn_update.argtypes = [i32, i32] + [_P] * 10 + [sz, _P]
+        lib.mlff_painn_update_backward.restype = ctypes.c_int
+        lib.mlff_painn_update_backward.argtypes = [i32, i32] + [_P] * 17 + [sz, _P]
         lib.mlff_debug_stall_test.restype = ctypes.c_int
         lib.mlff_debug_stall_test.argtypes = [i32]
         lib.mlff_radius_graph_noalloc.restype = ctypes.c_int

@@ -70,10 +70,125 @@ class CosineCutoff(nn.Module):
         return 0.5 * (torch.cos(math.pi * distances / self.cutoff) + 1.0) * (distances < self.cutoff).float()
 
 
+def _dev_f32(t: torch.Tensor, name: str) -> torch.Tensor:
+    if not t.is_cuda:
+        raise RuntimeError(f"{name} must be a CUDA tensor: mlff_gb300 has no CPU path")
+    return t.detach().to(torch.float32).contiguous()
+
+
+def _check_status(status: torch.Tensor, what: str):
+    code, where = (int(x) for x in status[:3:2].tolist())
+    if code == _lib.ERR_INVALID:
+        raise IndexError(f"{what}: edge_index entry of edge {where} is out of range")
+    if code != _lib.OK:
+        raise _lib.MLFFError(code, f"{what}: device status {code} at {where}")
+
+
+class _MessageFn(torch.autograd.Function):
+    """PaiNNMessage.forward on the library's per-module kernels; backward
+    returns the gradients of features, basis values, unit vectors and the
+    filter parameters (mlff_painn_message_backward)."""
+
+    @staticmethod
+    def forward(ctx, s, v, edge_index, rbf, evec, w1, b1, w2, b2):
+        lib = _lib.load()
+        N, H = s.shape
+        E, R = rbf.shape
+        if v.shape != (N, 3, H) or edge_index.shape != (2, E) or evec.shape != (E, 3):
+            raise ValueError(f"PaiNNMessage: inconsistent shapes scalar {tuple(s.shape)}, vector {tuple(v.shape)}, "
+                             f"edge_index {tuple(edge_index.shape)}, edge_rbf {tuple(rbf.shape)}, "
+                             f"edge_vector {tuple(evec.shape)}")
+        args = [_dev_f32(x, n) for x, n in ((s, "scalar_features"), (v, "vector_features"), (rbf, "edge_rbf"),
+                                            (evec, "edge_vector"), (w1, "weight"), (b1, "bias"), (w2, "weight"),
+                                            (b2, "bias"))]
+        ei = edge_index.detach().to(device=s.device, dtype=torch.int64).contiguous()
+        so = torch.empty(N, H, device=s.device)
+        vo = torch.empty(N, 3, H, device=s.device)
+        status = torch.zeros(4, dtype=torch.int32, device=s.device)
+        ws = torch.empty(lib.mlff_painn_message_workspace_size(H, R, E, 0), dtype=torch.uint8, device=s.device)
+        sf, vf, rf, ef, w1f, b1f, w2f, b2f = args
+        _lib.check(lib.mlff_painn_message(H, R, N, E, sf.data_ptr(), vf.data_ptr(), ei.data_ptr(), rf.data_ptr(),
+                                          ef.data_ptr(), w1f.data_ptr(), b1f.data_ptr(), w2f.data_ptr(),
+                                          b2f.data_ptr(), so.data_ptr(), vo.data_ptr(), status.data_ptr(),
+                                          ws.data_ptr(), ws.numel(), torch.cuda.current_stream().cuda_stream))
+        _check_status(status, "PaiNNMessage")
+        ctx.save_for_backward(sf, vf, ei, rf, ef, w1f, b1f, w2f, b2f)
+        ctx.dtypes = (s.dtype, v.dtype, rbf.dtype, evec.dtype, w1.dtype, b1.dtype, w2.dtype, b2.dtype)
+        return so.to(s.dtype), vo.to(v.dtype)
+
+    @staticmethod
+    def backward(ctx, gso, gvo):
+        lib = _lib.load()
+        sf, vf, ei, rf, ef, w1f, b1f, w2f, b2f = ctx.saved_tensors
+        N, H = sf.shape
+        E, R = rf.shape
+        dev = sf.device
+        gso = torch.zeros_like(sf) if gso is None else gso.to(torch.float32).contiguous()
+        gvo = torch.zeros_like(vf) if gvo is None else gvo.to(torch.float32).contiguous()
+        gs, gv = torch.empty_like(sf), torch.empty_like(vf)
+        grbf, gev = torch.empty_like(rf), torch.empty_like(ef)
+        gw1, gb1, gw2, gb2 = (torch.empty_like(w1f), torch.empty_like(b1f), torch.empty_like(w2f),
+                              torch.empty_like(b2f))
+        status = torch.zeros(4, dtype=torch.int32, device=dev)
+        ws = torch.empty(lib.mlff_painn_message_workspace_size(H, R, E, 1), dtype=torch.uint8, device=dev)
+        _lib.check(lib.mlff_painn_message_backward(
+            H, R, N, E, sf.data_ptr(), vf.data_ptr(), ei.data_ptr(), rf.data_ptr(), ef.data_ptr(), w1f.data_ptr(),
+            b1f.data_ptr(), w2f.data_ptr(), b2f.data_ptr(), gso.data_ptr(), gvo.data_ptr(), gs.data_ptr(),
+            gv.data_ptr(), grbf.data_ptr(), gev.data_ptr(), gw1.data_ptr(), gb1.data_ptr(), gw2.data_ptr(),
+            gb2.data_ptr(), status.data_ptr(), ws.data_ptr(), ws.numel(), torch.cuda.current_stream().cuda_stream))
+        _check_status(status, "PaiNNMessage backward")
+        d = ctx.dtypes
+        return (gs.to(d[0]), gv.to(d[1]), None, grbf.to(d[2]), gev.to(d[3]), gw1.to(d[4]), gb1.to(d[5]),
+                gw2.to(d[6]), gb2.to(d[7]))
+
+
+class _UpdateFn(torch.autograd.Function):
+    """PaiNNUpdate.forward on the library's per-module kernels, with its
+    reverse pass (mlff_painn_update_backward)."""
+
+    @staticmethod
+    def forward(ctx, s, v, w1, b1, w2, b2, mix):
+        lib = _lib.load()
+        N, H = s.shape
+        if v.shape != (N, 3, H):
+            raise ValueError(f"PaiNNUpdate: scalar {tuple(s.shape)} and vector {tuple(v.shape)} do not match")
+        sf, vf, w1f, b1f, w2f, b2f, mf = (_dev_f32(x, n) for x, n in (
+            (s, "scalar_features"), (v, "vector_features"), (w1, "weight"), (b1, "bias"), (w2, "weight"),
+            (b2, "bias"), (mix, "mixing_matrix")))
+        so = torch.empty(N, H, device=s.device)
+        vo = torch.empty(N, 3, H, device=s.device)
+        ws = torch.empty(lib.mlff_painn_update_workspace_size(H, N, 0), dtype=torch.uint8, device=s.device)
+        _lib.check(lib.mlff_painn_update(H, N, sf.data_ptr(), vf.data_ptr(), w1f.data_ptr(), b1f.data_ptr(),
+                                         w2f.data_ptr(), b2f.data_ptr(), mf.data_ptr(), so.data_ptr(), vo.data_ptr(),
+                                         ws.data_ptr(), ws.numel(), torch.cuda.current_stream().cuda_stream))
+        ctx.save_for_backward(sf, vf, w1f, b1f, w2f, b2f, mf)
+        ctx.dtypes = (s.dtype, v.dtype, w1.dtype, b1.dtype, w2.dtype, b2.dtype, mix.dtype)
+        return so.to(s.dtype), vo.to(v.dtype)
+
+    @staticmethod
+    def backward(ctx, gso, gvo):
+        lib = _lib.load()
+        sf, vf, w1f, b1f, w2f, b2f, mf = ctx.saved_tensors
+        N, H = sf.shape
+        dev = sf.device
+        gso = torch.zeros_like(sf) if gso is None else gso.to(torch.float32).contiguous()
+        gvo = torch.zeros_like(vf) if gvo is None else gvo.to(torch.float32).contiguous()
+        outs = [torch.empty_like(x) for x in (sf, vf, w1f, b1f, w2f, b2f, mf)]
+        ws = torch.empty(lib.mlff_painn_update_workspace_size(H, N, 1), dtype=torch.uint8, device=dev)
+        _lib.check(lib.mlff_painn_update_backward(
+            H, N, sf.data_ptr(), vf.data_ptr(), w1f.data_ptr(), b1f.data_ptr(), w2f.data_ptr(), b2f.data_ptr(),
+            mf.data_ptr(), gso.data_ptr(), gvo.data_ptr(), *[o.data_ptr() for o in outs], ws.data_ptr(),
+            ws.numel(), torch.cuda.current_stream().cuda_stream))
+        return tuple(o.to(d) for o, d in zip(outs, ctx.dtypes))
+
+
 class PaiNNMessage(nn.Module):
-    """Parameter container of the message block: ``rbf_to_scalar`` =
-    Linear(R, H) - SiLU - Linear(H, 3H) (student_model.py:297-322).  It is
-    evaluated only inside the fused edge kernels."""
+    """Message block: ``rbf_to_scalar`` = Linear(R, H) - SiLU - Linear(H, 3H)
+    (student_model.py:297-322).  Inside StudentForceField the fused edge
+    kernels evaluate it; called on its own (``forward``, student_model.py:
+    324-387: messages from edge_index[0] to edge_index[1] added to the input
+    features), it runs on the library's per-module kernels for any width,
+    with gradients."""
 
     def __init__(self, hidden_dim: int, num_rbf: int):
         super().__init__()
@@ -81,15 +196,17 @@ class PaiNNMessage(nn.Module):
         self.rbf_to_scalar = nn.Sequential(nn.Linear(num_rbf, hidden_dim), nn.SiLU(),
                                            nn.Linear(hidden_dim, hidden_dim * 3))
 
-    def forward(self, *args, **kwargs):
-        raise NotImplementedError("mlff_gb300 evaluates interaction blocks only inside StudentForceField "
-                                  "(fused CUDA edge kernels)")
+    def forward(self, scalar_features: torch.Tensor, vector_features: torch.Tensor, edge_index: torch.Tensor,
+                edge_rbf: torch.Tensor, edge_vector: torch.Tensor) -> Tuple[torch.Tensor, torch.Tensor]:
+        l1, l2 = self.rbf_to_scalar[0], self.rbf_to_scalar[2]
+        return _MessageFn.apply(scalar_features, vector_features, edge_index, edge_rbf, edge_vector,
+                                l1.weight, l1.bias, l2.weight, l2.bias)
 
 
 class PaiNNUpdate(nn.Module):
-    """Parameter container of the update block: ``update_mlp`` =
-    Linear(2H, H) - SiLU - Linear(H, 3H) and the 3x3 ``mixing_matrix``
-    over the xyz axis (student_model.py:390-416)."""
+    """Update block: ``update_mlp`` = Linear(2H, H) - SiLU - Linear(H, 3H)
+    and the 3x3 ``mixing_matrix`` over the xyz axis (student_model.py:
+    390-416).  ``forward`` (:418-470) runs on the per-module kernels."""
 
     def __init__(self, hidden_dim: int):
         super().__init__()
@@ -98,9 +215,11 @@ class PaiNNUpdate(nn.Module):
                                         nn.Linear(hidden_dim, hidden_dim * 3))
         self.mixing_matrix = nn.Parameter(torch.randn(3, 3) / np.sqrt(3))
 
-    def forward(self, *args, **kwargs):
-        raise NotImplementedError("mlff_gb300 evaluates interaction blocks only inside StudentForceField "
-                                  "(fused CUDA update kernels)")
+    def forward(self, scalar_features: torch.Tensor,
+                vector_features: torch.Tensor) -> Tuple[torch.Tensor, torch.Tensor]:
+        l1, l2 = self.update_mlp[0], self.update_mlp[2]
+        return _UpdateFn.apply(scalar_features, vector_features, l1.weight, l1.bias, l2.weight, l2.bias,
+                               self.mixing_matrix)
 
 
 class PaiNNInteraction(nn.Module):
@@ -111,8 +230,10 @@ class PaiNNInteraction(nn.Module):
         self.message = PaiNNMessage(hidden_dim, num_rbf)
         self.update = PaiNNUpdate(hidden_dim)
 
-    def forward(self, *args, **kwargs):
-        raise NotImplementedError("mlff_gb300 evaluates interaction blocks only inside StudentForceField")
+    def forward(self, scalar_features: torch.Tensor, vector_features: torch.Tensor, edge_index: torch.Tensor,
+                edge_rbf: torch.Tensor, edge_vector: torch.Tensor) -> Tuple[torch.Tensor, torch.Tensor]:
+        s, v = self.message(scalar_features, vector_features, edge_index, edge_rbf, edge_vector)
+        return self.update(s, v)
 
 
 class _EnergyForces(torch.autograd.Function):
@@ -142,8 +263,11 @@ def _trainable(model):
 
 class _EnergyTrain(torch.autograd.Function):
     """Training-mode E = model(positions), differentiable in the parameters
-    to second order, on the plain FP32 path (the one with parameter
-    gradients).  backward(g): the position gradient sum_b g_b dE_b/dpos and
+    to second order.  The forward value and forces come from the fused FP32
+    path (no per-edge activations are stored, so a forward-only call stays
+    small); the parameter gradients from the plain FP32 path's reverse
+    passes, recomputed in backward.  backward(g): the position gradient
+    sum_b g_b dE_b/dpos and
     the parameter gradients sum_b g_b dE_b/dtheta (mlff_param_grads).  When
     the backward itself is recorded (torch.autograd.grad(E, pos,
     create_graph=True), the reference's forces in training mode,
@@ -155,7 +279,7 @@ class _EnergyTrain(torch.autograd.Function):
     @staticmethod
     def forward(ctx, positions, model, batch, mol_index, *params):
         from . import _lib
-        E, F, _ = model.engine().energy_forces(batch, _lib.PATH_PLAIN_FP32, forces=True)
+        E, F, _ = model.engine().energy_forces(batch, _lib.PATH_TUNED_FP32, forces=True)
         ctx.model, ctx.batch = model, batch
         ctx.save_for_backward(F, mol_index, *params)
         return E.to(positions.dtype)
@@ -393,6 +517,21 @@ class StudentForceField(nn.Module):
         bt, _, _ = self._make_batch(atomic_numbers, positions, cell, pbc, None)
         E, F, _ = self._engine_call(bt, forces=True)
         return E[0].to(positions.dtype), F.to(positions.dtype)
+
+    def forward_with_analytical_forces(self, atomic_numbers: torch.Tensor, positions: torch.Tensor,
+                                       cell: Optional[torch.Tensor] = None, pbc: Optional[torch.Tensor] = None,
+                                       batch: Optional[torch.Tensor] = None
+                                       ) -> Tuple[torch.Tensor, torch.Tensor]:
+        """(energy, forces) without autograd (student_model.py:797-932, which
+        differentiates the radial basis and cutoff by hand and the rest by
+        autograd).  Here the whole reverse pass is hand-written: forces are
+        the library's CUDA adjoint.  energy is 0-dim for one structure and
+        [B] for a batch (as ``forward``); forces [N,3]; neither carries an
+        autograd graph."""
+        bt, _, n_mol = self._make_batch(atomic_numbers, positions, cell, pbc, batch, need_index=False)
+        E, F, _ = self._engine_call(bt, forces=True)
+        E = E.to(positions.dtype)
+        return (E.sum() if n_mol <= 1 else E), F.to(positions.dtype)
 
     def energy_and_forces(self, atomic_numbers: torch.Tensor, positions: torch.Tensor,
                           batch: Optional[torch.Tensor] = None, cell=None, pbc=None
