@@ -338,6 +338,24 @@ int mlff_param_grads_forces(const mlff_dims *dims, const void *packed, const mlf
 int mlff_profile_begin(void);
 int mlff_profile_end(double *ms_by_kind, int64_t *launches_by_kind, int32_t n_kinds);
 
+/* Force-accuracy statistics on the device (testing/force_metrics.py:46-384,
+ * whose functions take host arrays): pred and ref are double [n_vectors,3]
+ * device arrays; stats (double [MLFF_FORCE_STATS], device) receives
+ *   0 n, 1-3 sum of squared component errors (x, y, z), 4-6 sum of absolute
+ *   component errors, 7 sum of squared magnitude errors, 8 sum of absolute
+ *   magnitude errors, 9 sum of |magnitude error| / |ref| over vectors with
+ *   |ref| > 1e-6, 10 their count, 11 count of vectors with both magnitudes
+ *   > 1e-6, 12 sum of their cosines, 13-17 sums of p, r, p^2, r^2, p r over
+ *   all components, 18 largest absolute component error, 19 unused;
+ * per_vector (double [n_vectors,4], device, or NULL): per vector the RMSE
+ * and MAE over its components, |magnitude error| and the angle in degrees
+ * (NaN where a magnitude is <= 1e-6).  Sums are reduced in a fixed order.
+ * workspace: mlff_force_stats_workspace_size() bytes, device. */
+#define MLFF_FORCE_STATS 20
+size_t mlff_force_stats_workspace_size(void);
+int mlff_force_stats(const double *pred, const double *ref, int64_t n_vectors, double *stats,
+                     double *per_vector, void *workspace, size_t workspace_bytes, mlff_stream_t stream);
+
 /* Per-module blocks, any hidden width H and number of basis functions R:
  * the reference's PaiNNMessage.forward (src/mlff_distiller/models/
  * student_model.py:324-387) and PaiNNUpdate.forward (:418-470) and their

@@ -47,7 +47,7 @@ EXPORTS = ["mlff_version", "mlff_last_error_string", "mlff_packed_weights_size",
            "mlff_profile_end", "mlff_radius_graph_noalloc", "mlff_param_grads", "mlff_param_grads_forces",
            "mlff_debug_stall_test", "mlff_painn_message_workspace_size", "mlff_painn_message",
            "mlff_painn_message_backward", "mlff_painn_update_workspace_size", "mlff_painn_update",
-           "mlff_painn_update_backward"]
+           "mlff_painn_update_backward", "mlff_force_stats_workspace_size", "mlff_force_stats"]
 
 PROFILE_KINDS = ["neighbors", "edge_fwd", "edge_bwd", "update_fwd", "update_bwd", "readout", "forces",
                  "plain_gemm", "plain_edge", "other", "md"]
@@ -180,6 +180,10 @@ def load(build_if_missing: bool = True):
         lib.mlff_painn_update.argtypes = [i32, i32] + [_P] * 10 + [sz, _P]
         lib.mlff_painn_update_backward.restype = ctypes.c_int
         lib.mlff_painn_update_backward.argtypes = [i32, i32] + [_P] * 17 + [sz, _P]
+        lib.mlff_force_stats_workspace_size.restype = sz
+        lib.mlff_force_stats_workspace_size.argtypes = []
+        lib.mlff_force_stats.restype = ctypes.c_int
+        lib.mlff_force_stats.argtypes = [_P, _P, i64, _P, _P, _P, sz, _P]
         lib.mlff_debug_stall_test.restype = ctypes.c_int
         lib.mlff_debug_stall_test.argtypes = [i32]
         lib.mlff_radius_graph_noalloc.restype = ctypes.c_int

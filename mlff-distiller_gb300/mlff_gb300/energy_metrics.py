@@ -72,11 +72,24 @@ def compute_energy_drift(energies: np.ndarray, method: str = "relative") -> floa
     raise ValueError(f"Unknown drift method: {method}")
 
 
-def compute_energy_conservation_ratio(energies: np.ndarray) -> float:
-    """energy_metrics.py:97-157: 1 - std/|mean| (global form)."""
+def compute_energy_conservation_ratio(energies: np.ndarray, window: Optional[int] = None) -> float:
+    """energy_metrics.py:97-157: 1 - std/|mean|, clamped at 0, over the whole
+    trajectory or averaged over rolling windows of ``window`` samples
+    (windows whose mean is within 1e-10 of zero are skipped)."""
     if len(energies) < 2:
         raise ValueError(f"Need at least 2 energy values, got {len(energies)}")
-    return _one(energies)["conservation_ratio"]
+    if window is not None and window > len(energies):
+        window = None
+    if window is None:
+        return _one(energies)["conservation_ratio"]
+    e = torch.as_tensor(np.asarray(energies, np.float64), device="cuda")
+    w = e.unfold(0, int(window), 1)                  # [n - window + 1, window] rolling windows
+    mean = w.mean(dim=1)
+    std = w.std(dim=1, unbiased=False)
+    keep = mean.abs() > 1e-10
+    if not bool(keep.any()):
+        return 1.0
+    return float(torch.clamp(1.0 - std[keep] / mean[keep].abs(), min=0.0).mean())
 
 
 def compute_energy_fluctuations(energies: np.ndarray) -> Dict[str, float]:
@@ -101,13 +114,25 @@ def compute_kinetic_potential_stability(kinetic_energies: np.ndarray, potential_
                                     "energy_partition_ratio")}
 
 
-def compute_time_resolved_drift(times: np.ndarray, energies: np.ndarray) -> Dict[str, float]:
-    """energy_metrics.py:270-354, linear-fit method, uniformly spaced times."""
+def compute_time_resolved_drift(times: np.ndarray, energies: np.ndarray, method: str = "linear_fit") -> Dict[str, Any]:
+    """energy_metrics.py:270-354: 'linear_fit' (drift rate, its standard
+    error, R^2, total drift, fitted initial energy; uniformly spaced times) or
+    'cumulative' (average rate, total and largest drift from the first
+    sample, the drift series)."""
     if len(times) != len(energies):
         raise ValueError(f"Times and energies must have same length: {len(times)} vs {len(energies)}")
     if len(times) < 3:
         raise ValueError(f"Need at least 3 data points for drift analysis, got {len(times)}")
     t = np.asarray(times, np.float64)
+    if method == "cumulative":
+        e = torch.as_tensor(np.asarray(energies, np.float64), device="cuda")
+        cum = e - e[0]
+        span = float(t[-1] - t[0])
+        total = float(cum[-1])
+        return {"drift_rate": total / span if span > 1e-10 else 0.0, "total_drift": total,
+                "max_drift": float(cum.abs().max()), "cumulative_drift": cum.cpu().numpy()}
+    if method != "linear_fit":
+        raise ValueError(f"Unknown method: {method}")
     s = _one(energies, dt_ps=float(t[1] - t[0]))
     return {"drift_rate": s["drift_rate"], "drift_rate_std": s["drift_rate_std"], "r_squared": s["r_squared"],
             "total_drift": s["final_energy"] - s["initial_energy"],

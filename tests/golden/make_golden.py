@@ -28,7 +28,14 @@ seeded inputs in float32 (the reference's own dtype) and float64
                              loss with mae / huber components: its value and
                              derivatives in the predicted energies and forces
 
-``--train-only`` rewrites golden_train.npz alone.
+* golden_metrics.npz      -- the reference's own energy-conservation and
+                             force-accuracy metrics (testing/energy_metrics.py,
+                             testing/force_metrics.py, pure numpy) on seeded
+                             energy traces and force arrays: inputs and
+                             every returned value
+
+``--train-only`` rewrites golden_train.npz alone, ``--metrics-only``
+golden_metrics.npz alone.
 """
 from __future__ import annotations
 
@@ -203,7 +210,103 @@ def main(ref_root: str, train_only: bool = False):
     np.savez_compressed(os.path.join(HERE, "golden_norm.npz"), vec=vec, dist=dist,
                         keep=(dist <= 5.0))
     make_train_golden(sm, ref_root, sd, pert)
+    make_metrics_golden(ref_root)
     print("wrote", sorted(os.listdir(HERE)))
+
+
+def load_reference_testing(ref_root: str, name: str):
+    """testing/<name>.py by file path (numpy only; the package __init__
+    pulls in ASE, which is not needed by these modules)."""
+    path = os.path.join(ref_root, "src", "mlff_distiller", "testing", f"{name}.py")
+    spec = importlib.util.spec_from_file_location(f"mlff_distiller_testing_{name}", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def metric_traces():
+    """Seeded energy traces (kinetic, potential; 0.5 fs steps in ps): an
+    oscillating conserved trajectory, one with a linear drift, one noisy,
+    one short."""
+    g = np.random.default_rng(11)
+    out = []
+    for n, drift, noise in ((400, 0.0, 1e-4), (400, 2e-3, 1e-4), (250, -5e-4, 3e-3), (12, 0.0, 1e-3)):
+        t = np.arange(n) * 5e-4
+        k = 1.2 + 0.3 * np.sin(2 * np.pi * t / 0.02) + noise * g.standard_normal(n)
+        p = -40.0 - 0.3 * np.sin(2 * np.pi * t / 0.02) + drift * np.arange(n) + noise * g.standard_normal(n)
+        out.append((t, k, p))
+    return out
+
+
+def metric_forces():
+    """Seeded (predicted, reference) force arrays: [n_atoms, 3] with noise,
+    [frames, atoms, 3], and one with zero and near-zero vectors."""
+    g = np.random.default_rng(12)
+    ref = g.standard_normal((300, 3)) * 1.5
+    a = (ref + 0.05 * g.standard_normal(ref.shape), ref)
+    ref3 = g.standard_normal((5, 40, 3))
+    b = (ref3 + 0.2 * g.standard_normal(ref3.shape), ref3)
+    ref_z = g.standard_normal((60, 3))
+    pred_z = ref_z + 0.1 * g.standard_normal(ref_z.shape)
+    ref_z[:5] = 0.0
+    pred_z[5:8] = 1e-8
+    pred_z[8] = -ref_z[8]
+    c = (pred_z, ref_z)
+    return [a, b, c]
+
+
+def make_metrics_golden(ref_root: str):
+    em = load_reference_testing(ref_root, "energy_metrics")
+    fm = load_reference_testing(ref_root, "force_metrics")
+    out = {}
+    for i, (t, k, p) in enumerate(metric_traces()):
+        e = k + p
+        pre = f"e{i}/"
+        out[pre + "time"], out[pre + "kinetic"], out[pre + "potential"] = t, k, p
+        out[pre + "drift_relative"] = em.compute_energy_drift(e, "relative")
+        out[pre + "drift_absolute"] = em.compute_energy_drift(e, "absolute")
+        out[pre + "drift_max_deviation"] = em.compute_energy_drift(e, "max_deviation")
+        out[pre + "conservation_ratio"] = em.compute_energy_conservation_ratio(e)
+        out[pre + "conservation_ratio_w10"] = em.compute_energy_conservation_ratio(e, window=10)
+        for key, v in em.compute_energy_fluctuations(e).items():
+            out[pre + "fluct/" + key] = v
+        for key, v in em.compute_kinetic_potential_stability(k, p).items():
+            out[pre + "kp/" + key] = v
+        for key, v in em.compute_time_resolved_drift(t, e).items():
+            out[pre + "trd/" + key] = v
+        for key, v in em.compute_time_resolved_drift(t, e, method="cumulative").items():
+            out[pre + "trc/" + key] = v
+        a = em.assess_energy_conservation({"time": list(t), "total_energy": list(e), "kinetic_energy": list(k),
+                                           "potential_energy": list(p)}, verbose=False)
+        out[pre + "assess/passed"] = a["passed"]
+        for key in ("energy_drift_pct", "energy_drift_max_pct", "conservation_ratio"):
+            out[pre + "assess/" + key] = a[key]
+        for key, v in a["criteria"].items():
+            out[pre + "assess/criteria/" + key] = v
+    for i, (pred, ref) in enumerate(metric_forces()):
+        pre = f"f{i}/"
+        out[pre + "pred"], out[pre + "ref"] = pred, ref
+        out[pre + "rmse"] = fm.compute_force_rmse(pred, ref)
+        out[pre + "rmse_comp"] = fm.compute_force_rmse(pred, ref, per_component=True)
+        out[pre + "mae"] = fm.compute_force_mae(pred, ref)
+        out[pre + "mae_comp"] = fm.compute_force_mae(pred, ref, per_component=True)
+        for key, v in fm.compute_force_magnitude_error(pred, ref).items():
+            out[pre + "mag/" + key] = v
+        out[pre + "angular_median"] = fm.compute_angular_error(pred, ref)
+        out[pre + "angular_dist"] = fm.compute_angular_error(pred, ref, return_distribution=True)
+        for key, v in fm.compute_force_correlation(pred, ref).items():
+            out[pre + "corr/" + key] = v
+        if pred.ndim == 2:
+            for key, v in fm.compute_per_atom_force_errors(pred, ref).items():
+                out[pre + "atom/" + key] = v
+        a = fm.assess_force_accuracy(pred, ref, verbose=False)
+        out[pre + "assess/passed"] = a["passed"]
+        for key, v in a["angular_percentiles"].items():
+            out[pre + "assess/pct/" + key] = v
+        for key, v in a["criteria"].items():
+            out[pre + "assess/criteria/" + key] = v
+    np.savez_compressed(os.path.join(HERE, "golden_metrics.npz"), **{k: np.asarray(v) for k, v in out.items()})
+    print("wrote golden_metrics.npz with", len(out), "arrays")
 
 
 if __name__ == "__main__":
@@ -212,4 +315,7 @@ if __name__ == "__main__":
     if not root:
         sys.exit("usage: make_golden.py <reference checkout> [--train-only] "
                  "(or set MLFF_REFERENCE_ROOT)")
-    main(root, train_only="--train-only" in sys.argv)
+    if "--metrics-only" in sys.argv:
+        make_metrics_golden(root)
+    else:
+        main(root, train_only="--train-only" in sys.argv)

@@ -52,3 +52,72 @@ def test_reference_named_metrics():
             "potential_energy": list(-110.0 - 0.1 * np.sin(times))}
     a = em.assess_energy_conservation(traj, tolerance_pct=1.0)
     assert a["passed"] and abs(a["energy_drift_pct"]) < 1e-9
+
+
+def _golden():
+    import os
+    from conftest import GOLDEN
+    return np.load(os.path.join(GOLDEN, "golden_metrics.npz"))
+
+
+def test_energy_metrics_vs_reference_outputs():
+    """The reference-named functions against the reference's own
+    energy_metrics outputs (golden_metrics.npz)."""
+    from mlff_gb300 import energy_metrics as em
+    g = _golden()
+    close = lambda a, b, key: np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-12, err_msg=key)
+    for i in range(4):
+        pre = f"e{i}/"
+        t, k, p = g[pre + "time"], g[pre + "kinetic"], g[pre + "potential"]
+        e = k + p
+        close(em.compute_energy_drift(e, "relative"), g[pre + "drift_relative"], "relative")
+        close(em.compute_energy_drift(e, "absolute"), g[pre + "drift_absolute"], "absolute")
+        close(em.compute_energy_drift(e, "max_deviation"), g[pre + "drift_max_deviation"], "max_deviation")
+        close(em.compute_energy_conservation_ratio(e), g[pre + "conservation_ratio"], "ratio")
+        close(em.compute_energy_conservation_ratio(e, window=10), g[pre + "conservation_ratio_w10"], "ratio w10")
+        for key, v in em.compute_energy_fluctuations(e).items():
+            close(v, g[pre + "fluct/" + key], key)
+        for key, v in em.compute_kinetic_potential_stability(k, p).items():
+            close(v, g[pre + "kp/" + key], key)
+        for key, v in em.compute_time_resolved_drift(t, e).items():
+            close(v, g[pre + "trd/" + key], key)
+        for key, v in em.compute_time_resolved_drift(t, e, method="cumulative").items():
+            close(v, g[pre + "trc/" + key], key)
+        a = em.assess_energy_conservation({"time": t, "kinetic_energy": k, "potential_energy": p})
+        assert a["passed"] == bool(g[pre + "assess/passed"])
+        for key in ("energy_drift_pct", "energy_drift_max_pct", "conservation_ratio"):
+            close(a[key], g[pre + "assess/" + key], key)
+        for key, v in a["criteria"].items():
+            assert v == bool(g[pre + "assess/criteria/" + key]), key
+
+
+def test_force_metrics_vs_reference_outputs():
+    """Device force-accuracy statistics through the reference-named
+    functions against the reference's own force_metrics outputs."""
+    from mlff_gb300 import force_metrics as fm
+    g = _golden()
+    close = lambda a, b, key: np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-12, err_msg=key)
+    for i in range(3):
+        pre = f"f{i}/"
+        pred, ref = g[pre + "pred"], g[pre + "ref"]
+        close(fm.compute_force_rmse(pred, ref), g[pre + "rmse"], "rmse")
+        close(fm.compute_force_rmse(pred, ref, per_component=True), g[pre + "rmse_comp"], "rmse comp")
+        close(fm.compute_force_mae(pred, ref), g[pre + "mae"], "mae")
+        close(fm.compute_force_mae(pred, ref, per_component=True), g[pre + "mae_comp"], "mae comp")
+        for key, v in fm.compute_force_magnitude_error(pred, ref).items():
+            close(v, g[pre + "mag/" + key], key)
+        close(fm.compute_angular_error(pred, ref), g[pre + "angular_median"], "angle median")
+        close(fm.compute_angular_error(pred, ref, return_distribution=True), g[pre + "angular_dist"], "angles")
+        for key, v in fm.compute_force_correlation(pred, ref).items():
+            close(v, g[pre + "corr/" + key], key)
+        if pred.ndim == 2:
+            for key, v in fm.compute_per_atom_force_errors(pred, ref).items():
+                close(v, g[pre + "atom/" + key], key)
+        a = fm.assess_force_accuracy(torch.tensor(pred, device="cuda"), torch.tensor(ref), verbose=False)
+        assert a["passed"] == bool(g[pre + "assess/passed"])
+        for key, v in a["angular_percentiles"].items():
+            close(v, g[pre + "assess/pct/" + key], key)
+        for key, v in a["criteria"].items():
+            assert v == bool(g[pre + "assess/criteria/" + key]), key
+    with pytest.raises(ValueError):
+        fm.compute_force_rmse(np.zeros((4, 3)), np.zeros((5, 3)))

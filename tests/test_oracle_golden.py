@@ -235,3 +235,35 @@ def test_oracle_edge_chunks_equal_single_pass(weights_bias):
     assert abs(float(E1[0] - E2[0])) < 1e-10
     assert float((F1 - F2).abs().max()) < 1e-11
     assert float((V1 - V2).abs().max()) < 1e-10
+
+
+def _golden_metrics():
+    return np.load(os.path.join(GOLDEN, "golden_metrics.npz"))
+
+
+def test_energy_metrics_oracle_pinned_to_reference():
+    """oracle/energy_metrics.py against the reference's own energy_metrics
+    outputs on seeded traces (golden_metrics.npz, written by make_golden.py)."""
+    from oracle import energy_metrics
+    g = _golden_metrics()
+    for i in range(4):
+        pre = f"e{i}/"
+        t, k, p = g[pre + "time"], g[pre + "kinetic"], g[pre + "potential"]
+        s = energy_metrics.stats(k + p, k, p, float(t[1] - t[0]))
+        want = {2: "drift_relative", 3: "drift_max_deviation", 5: "fluct/std", 6: "fluct/range",
+                7: "fluct/mean_abs_dev", 8: "conservation_ratio", 9: "kp/ke_mean", 10: "kp/ke_std",
+                11: "kp/pe_mean", 12: "kp/pe_std", 13: "kp/ke_pe_correlation", 14: "kp/energy_partition_ratio",
+                15: "trd/drift_rate", 16: "trd/r_squared", 17: "trd/drift_rate_std"}
+        for j, key in want.items():
+            np.testing.assert_allclose(s[j], g[pre + key], rtol=1e-9, atol=1e-12, err_msg=pre + key)
+        np.testing.assert_allclose(s[1] - s[0], g[pre + "drift_absolute"], rtol=1e-9, atol=1e-12)
+
+
+def test_force_metrics_oracle_pinned_to_reference():
+    from oracle import force_metrics
+    g = _golden_metrics()
+    for i in range(3):
+        pre = f"f{i}/"
+        m = force_metrics.metrics(g[pre + "pred"], g[pre + "ref"])
+        for key, v in m.items():
+            np.testing.assert_allclose(v, g[pre + key], rtol=1e-9, atol=1e-12, err_msg=pre + key)
