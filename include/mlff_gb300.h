@@ -223,6 +223,23 @@ int mlff_langevin_steps(const mlff_dims *dims, const void *packed, const mlff_sy
                         double friction, double kT, uint64_t seed, int32_t n_steps, void *workspace,
                         size_t workspace_bytes, mlff_stream_t stream);
 
+/* Langevin NVT with the scheme of ASE's Langevin, the reference's NVT
+ * protocol (src/mlff_distiller/benchmarks/md_trajectory.py:407-413, ASE
+ * Langevin with friction 0.01 and its default fixcm=True): the propagator
+ * of Vanden-Eijnden and Ciccotti (Chem. Phys. Lett. 429, 310 (2006),
+ * Eq. 23), restated in the library's own kernels.  Same state and
+ * arguments as mlff_langevin_steps (friction in inverse ASE time units, kT
+ * in eV); fix_com = 1 keeps each structure's centre of mass in place and
+ * removes its centre-of-mass velocity every step, as ASE does by default.
+ * Six normals per atom and step (Philox4x32-10 keyed by seed and (step,
+ * atom, 1 or 2), Box-Muller).  ASE draws from numpy's generator instead,
+ * so trajectories agree with ASE's in distribution, not sample by sample.
+ * Graph-capturable like mlff_langevin_steps. */
+int mlff_langevin_ase_steps(const mlff_dims *dims, const void *packed, const mlff_system *sys,
+                            int64_t edge_capacity, int32_t path, mlff_md_state *state, double dt,
+                            double friction, double kT, uint64_t seed, int32_t fix_com, int32_t n_steps,
+                            void *workspace, size_t workspace_bytes, mlff_stream_t stream);
+
 /* NPT state beyond mlff_md_state, per structure (all device memory):
  * box float64 [B,3] edge lengths and box32 float32 [B,3] (the copy the
  * force call reads; both updated every step), zeta [B] thermostat rate,

@@ -98,6 +98,7 @@ WsLayout ws_layout(const mlff_dims& d, int32_t n_atoms, int32_t n_mol, int64_t c
     L.xbar = take(fs * 2 * N * 4 * H);
     L.e_atom = take(sizeof(float) * N);
     L.md_pos32 = take(sizeof(float) * 3 * N);
+    L.md_noise = take(sizeof(double) * 6 * N);
     if (path == MLFF_PATH_TUNED_TC) {
         L.geo = take(sizeof(float4) * cap);
         // at most cap / tile + one partial tile per tiled range: forward
@@ -190,6 +191,10 @@ int energy_forces_impl(const mlff_dims& d, const void* packed, const mlff_system
 int md_kick_drift(const WsLayout& L, void* ws, mlff_md_state* s, double dt, cudaStream_t st);
 int md_langevin_baoa(const WsLayout& L, void* ws, mlff_md_state* s, double dt, double friction, double kT,
                      uint64_t seed, cudaStream_t st);
+int md_vec_open(const WsLayout& L, void* ws, mlff_md_state* s, double dt, double friction, double kT, uint64_t seed,
+                int32_t fix_com, const int64_t* mol_ptr, int32_t n_mol, cudaStream_t st);
+int md_vec_close(const WsLayout& L, void* ws, mlff_md_state* s, double dt, double friction, double kT,
+                 int32_t fix_com, const int64_t* mol_ptr, int32_t n_mol, double* kinetic, cudaStream_t st);
 int md_energy_stats(const double* epot, const double* ekin, int32_t n, int32_t B, const int64_t* mol_ptr,
                     double dt_ps, double* out, cudaStream_t st);
 int md_kick(const WsLayout& L, void* ws, mlff_md_state* s, double dt, const int64_t* mol_ptr, int32_t n_mol,
@@ -296,9 +301,14 @@ int mlff_energy_forces(const mlff_dims* dims, const void* packed, const mlff_sys
 }
 
 // One integrator for both entry points: Verlet (langevin false) or BAOAB.
+// One integrator for three entry points: scheme 0 velocity Verlet, 1 BAOAB
+// Langevin, 2 ASE's Langevin (Vanden-Eijnden-Ciccotti; fix_com as ASE's fixcm).
+enum { MD_VERLET = 0, MD_BAOAB = 1, MD_VEC = 2 };
 static int md_steps(const mlff_dims* dims, const void* packed, const mlff_system* sys, int64_t edge_capacity,
-                    int32_t path, mlff_md_state* state, double dt, bool langevin, double friction, double kT,
-                    uint64_t seed, int32_t n_steps, void* workspace, size_t workspace_bytes, mlff_stream_t stream) {
+                    int32_t path, mlff_md_state* state, double dt, int scheme, double friction, double kT,
+                    uint64_t seed, int32_t fix_com, int32_t n_steps, void* workspace, size_t workspace_bytes,
+                    mlff_stream_t stream) {
+    const bool langevin = scheme != MD_VERLET;
     if (!sys || !state || !state->pos || !state->vel || !state->inv_mass || !state->forces || !state->energy) {
         set_error("system and md state (pos, vel, inv_mass, forces, energy) are required");
         return MLFF_ERR_INVALID;
@@ -328,12 +338,18 @@ static int md_steps(const mlff_dims* dims, const void* packed, const mlff_system
                          nullptr, nullptr};
         mlff_md_state ks = *state;
         if (state->kinetic_trace) ks.kinetic = state->kinetic_trace + s * B;
-        r = langevin ? md_langevin_baoa(L, workspace, state, dt, friction, kT, seed, st)
-                     : md_kick_drift(L, workspace, state, dt, st);
+        if (scheme == MD_VEC) r = md_vec_open(L, workspace, state, dt, friction, kT, seed, fix_com, sys->mol_ptr,
+                                              sys->n_mol, st);
+        else if (scheme == MD_BAOAB) r = md_langevin_baoa(L, workspace, state, dt, friction, kT, seed, st);
+        else r = md_kick_drift(L, workspace, state, dt, st);
         if (r) return r;
         if ((r = energy_forces_impl(*dims, packed, s2, L, path, out, workspace, st))) return r;
-        if ((r = md_kick(L, workspace, &ks, dt, sys->mol_ptr, sys->n_mol, last || state->kinetic_trace, st)))
-            return r;
+        if (scheme == MD_VEC)
+            r = md_vec_close(L, workspace, &ks, dt, friction, kT, fix_com, sys->mol_ptr, sys->n_mol,
+                             (last || state->kinetic_trace) ? ks.kinetic : nullptr, st);
+        else
+            r = md_kick(L, workspace, &ks, dt, sys->mol_ptr, sys->n_mol, last || state->kinetic_trace, st);
+        if (r) return r;
         if (last) {
             if (state->energy_trace)
                 MLFF_CUDA(cudaMemcpyAsync(state->energy_trace + s * B, state->energy, sizeof(double) * B,
@@ -349,15 +365,23 @@ static int md_steps(const mlff_dims* dims, const void* packed, const mlff_system
 int mlff_verlet_steps(const mlff_dims* dims, const void* packed, const mlff_system* sys, int64_t edge_capacity,
                       int32_t path, mlff_md_state* state, double dt, int32_t n_steps, void* workspace,
                       size_t workspace_bytes, mlff_stream_t stream) {
-    return md_steps(dims, packed, sys, edge_capacity, path, state, dt, false, 0.0, 0.0, 0, n_steps, workspace,
+    return md_steps(dims, packed, sys, edge_capacity, path, state, dt, MD_VERLET, 0.0, 0.0, 0, 0, n_steps, workspace,
                     workspace_bytes, stream);
 }
 
 int mlff_langevin_steps(const mlff_dims* dims, const void* packed, const mlff_system* sys, int64_t edge_capacity,
                         int32_t path, mlff_md_state* state, double dt, double friction, double kT, uint64_t seed,
                         int32_t n_steps, void* workspace, size_t workspace_bytes, mlff_stream_t stream) {
-    return md_steps(dims, packed, sys, edge_capacity, path, state, dt, true, friction, kT, seed, n_steps, workspace,
-                    workspace_bytes, stream);
+    return md_steps(dims, packed, sys, edge_capacity, path, state, dt, MD_BAOAB, friction, kT, seed, 0, n_steps,
+                    workspace, workspace_bytes, stream);
+}
+
+int mlff_langevin_ase_steps(const mlff_dims* dims, const void* packed, const mlff_system* sys, int64_t edge_capacity,
+                            int32_t path, mlff_md_state* state, double dt, double friction, double kT, uint64_t seed,
+                            int32_t fix_com, int32_t n_steps, void* workspace, size_t workspace_bytes,
+                            mlff_stream_t stream) {
+    return md_steps(dims, packed, sys, edge_capacity, path, state, dt, MD_VEC, friction, kT, seed, fix_com ? 1 : 0,
+                    n_steps, workspace, workspace_bytes, stream);
 }
 
 int mlff_npt_steps(const mlff_dims* dims, const void* packed, const mlff_system* sys, int64_t edge_capacity,

@@ -97,6 +97,205 @@ __global__ void langevin_baoa_kernel(double* __restrict__ pos, double* __restric
     }
 }
 
+// ------------------------------------------------- Langevin, ASE's scheme
+// The propagator of Vanden-Eijnden and Ciccotti (Chem. Phys. Lett. 429, 310
+// (2006), Eq. 23), the one ASE's Langevin integrates, with ASE's default of
+// a fixed centre of mass per structure.  Per step, with gamma the friction,
+// sigma = sqrt(2 kT gamma / m) and two standard-normal vectors xi, eta per
+// atom:
+//   v += c1 F/m - c2 v + c3 xi - c4 eta
+//   r += dt v + c5 eta    (then, with fix_com, every atom of a structure is
+//                          shifted back by its centre-of-mass change and v
+//                          takes that shift / dt: v = (r_new - r - c5 eta)/dt)
+//   F = F(r)
+//   v += c1 F/m - c2 v + c3 xi - c4 eta;  with fix_com v -= its centre-of-mass velocity
+// c1 = dt/2 - dt^2 gamma/8, c2 = gamma dt/2 - gamma^2 dt^2/8,
+// c3 = sqrt(dt) sigma/2 - dt^1.5 gamma sigma/8, c5 = dt^1.5 sigma/(2 sqrt 3),
+// c4 = gamma c5/2.  The six normals of an atom come from two Philox blocks
+// keyed by (seed; step, atom, 1) and (seed; step, atom, 2), Box-Muller on
+// consecutive uniform pairs; xi = the first three, eta = the next three.
+// The open kernel stores them for the close kernel, which advances the step
+// counter (no kernel reads and writes the counter).
+struct VecCoef {
+    double c1, c2, c3, c4, c5;
+};
+__device__ __forceinline__ VecCoef vec_coef(double dt, double gamma, double kT, double inv_m) {
+    const double sigma = sqrt(2.0 * kT * gamma * inv_m);
+    VecCoef c;
+    c.c1 = 0.5 * dt - dt * dt * gamma / 8.0;
+    c.c2 = 0.5 * gamma * dt - gamma * gamma * dt * dt / 8.0;
+    c.c3 = 0.5 * sqrt(dt) * sigma - dt * sqrt(dt) * gamma * sigma / 8.0;
+    c.c5 = dt * sqrt(dt) * sigma / (2.0 * sqrt(3.0));
+    c.c4 = 0.5 * gamma * c.c5;
+    return c;
+}
+__device__ __forceinline__ void box_muller4(uint4 x, double* n) {
+    const double u0 = ((double)x.x + 0.5) * 0x1p-32, u1 = ((double)x.y + 0.5) * 0x1p-32;
+    const double u2 = ((double)x.z + 0.5) * 0x1p-32, u3 = ((double)x.w + 0.5) * 0x1p-32;
+    const double r0 = sqrt(-2.0 * log(u0)), r1 = sqrt(-2.0 * log(u2));
+    double s0, k0, s1, k1;
+    sincospi(2.0 * u1, &s0, &k0);
+    sincospi(2.0 * u3, &s1, &k1);
+    n[0] = r0 * k0;
+    n[1] = r0 * s0;
+    n[2] = r1 * k1;
+    n[3] = r1 * s1;
+}
+
+constexpr int VEC_NT = 256;
+// sum of 8 doubles over the block, fixed tree; every thread gets the sums
+__device__ __forceinline__ void block_sum8(double (&v)[8], double (*red)[VEC_NT]) {
+    const int t = threadIdx.x;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) red[j][t] = v[j];
+    __syncthreads();
+    for (int o = VEC_NT / 2; o > 0; o >>= 1) {
+        if (t < o)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) red[j][t] += red[j][t + o];
+        __syncthreads();
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] = red[j][0];
+    __syncthreads();
+}
+
+// first half of a step and the drift, one block per structure
+__global__ void __launch_bounds__(VEC_NT) vec_open_kernel(double* __restrict__ pos, double* __restrict__ vel,
+                                                          const double* __restrict__ inv_mass,
+                                                          const float* __restrict__ F, double dt, double gamma,
+                                                          double kT, uint64_t seed,
+                                                          const int64_t* __restrict__ step_counter,
+                                                          const int64_t* __restrict__ mol_ptr, int32_t n_mol,
+                                                          int32_t fix_com, double* __restrict__ noise,
+                                                          float* __restrict__ pos32, const Status* st) {
+    __shared__ double red[8][VEC_NT];
+    pdl_wait();
+    pdl_trigger();
+    if (st->code != 0) return;
+    const uint64_t step = (uint64_t)*step_counter;
+    const uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
+    for (int m = blockIdx.x; m < n_mol; m += gridDim.x) {
+        const int64_t a0 = mol_ptr[m], a1 = mol_ptr[m + 1];
+        double acc[8] = {};   // sum m r_old (3), sum m r_new (3), total mass
+        for (int64_t a = a0 + threadIdx.x; a < a1; a += VEC_NT) {
+            double nz[8];
+            box_muller4(philox4x32_10(make_uint4((uint32_t)step, (uint32_t)(step >> 32), (uint32_t)a, 1u), key), nz);
+            box_muller4(philox4x32_10(make_uint4((uint32_t)step, (uint32_t)(step >> 32), (uint32_t)a, 2u), key),
+                        nz + 4);
+#pragma unroll
+            for (int j = 0; j < 6; ++j) noise[6 * a + j] = nz[j];
+            const double im = inv_mass[a], mass = 1.0 / im;
+            const VecCoef c = vec_coef(dt, gamma, kT, im);
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const int64_t i = 3 * a + d;
+                double v = vel[i];
+                v += c.c1 * (double)F[i] * im - c.c2 * v + c.c3 * nz[d] - c.c4 * nz[3 + d];
+                const double r0 = pos[i], r = r0 + dt * v + c.c5 * nz[3 + d];
+                vel[i] = v;
+                pos[i] = r;
+                acc[d] += mass * r0;
+                acc[3 + d] += mass * r;
+            }
+            acc[6] += mass;
+        }
+        if (fix_com) {
+            block_sum8(acc, red);
+            double sh[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) sh[d] = (acc[d] - acc[3 + d]) / acc[6];
+            for (int64_t a = a0 + threadIdx.x; a < a1; a += VEC_NT)
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    const int64_t i = 3 * a + d;
+                    const double r = pos[i] + sh[d];
+                    pos[i] = r;
+                    vel[i] += sh[d] / dt;
+                    pos32[i] = (float)r;
+                }
+        } else {
+            for (int64_t a = a0 + threadIdx.x; a < a1; a += VEC_NT)
+#pragma unroll
+                for (int d = 0; d < 3; ++d) pos32[3 * a + d] = (float)pos[3 * a + d];
+        }
+    }
+}
+
+// second half of a step at the new forces, centre-of-mass velocity removed,
+// kinetic energy per structure (when ke is given); advances the step counter
+__global__ void __launch_bounds__(VEC_NT) vec_close_kernel(double* __restrict__ vel, const double* __restrict__ inv_mass,
+                                                           const float* __restrict__ F, double dt, double gamma,
+                                                           double kT, const double* __restrict__ noise,
+                                                           const int64_t* __restrict__ mol_ptr, int32_t n_mol,
+                                                           int32_t fix_com, double* __restrict__ ke,
+                                                           int64_t* __restrict__ step_counter, const Status* st) {
+    __shared__ double red[8][VEC_NT];
+    pdl_wait();
+    pdl_trigger();
+    if (st->code != 0) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *step_counter += 1;
+    for (int m = blockIdx.x; m < n_mol; m += gridDim.x) {
+        const int64_t a0 = mol_ptr[m], a1 = mol_ptr[m + 1];
+        double acc[8] = {};   // sum m v (3), total mass, sum m v^2
+        for (int64_t a = a0 + threadIdx.x; a < a1; a += VEC_NT) {
+            const double im = inv_mass[a], mass = 1.0 / im;
+            const VecCoef c = vec_coef(dt, gamma, kT, im);
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const int64_t i = 3 * a + d;
+                double v = vel[i];
+                v += c.c1 * (double)F[i] * im - c.c2 * v + c.c3 * noise[6 * a + d] - c.c4 * noise[6 * a + 3 + d];
+                vel[i] = v;
+                acc[d] += mass * v;
+                acc[4] += mass * v * v;
+            }
+            acc[3] += mass;
+        }
+        if (fix_com || ke) block_sum8(acc, red);
+        if (fix_com) {
+            double vc[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) vc[d] = acc[d] / acc[3];
+            double k2[8] = {};
+            for (int64_t a = a0 + threadIdx.x; a < a1; a += VEC_NT) {
+                const double mass = 1.0 / inv_mass[a];
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    const int64_t i = 3 * a + d;
+                    const double v = vel[i] - vc[d];
+                    vel[i] = v;
+                    k2[0] += mass * v * v;
+                }
+            }
+            if (ke) {
+                block_sum8(k2, red);
+                if (threadIdx.x == 0) ke[m] = 0.5 * k2[0];
+            }
+        } else if (ke && threadIdx.x == 0) {
+            ke[m] = 0.5 * acc[4];
+        }
+    }
+}
+
+int md_vec_open(const WsLayout& L, void* ws, mlff_md_state* s, double dt, double friction, double kT, uint64_t seed,
+                int32_t fix_com, const int64_t* mol_ptr, int32_t n_mol, cudaStream_t st) {
+    ProfScope prof(PK_MD, st);
+    MLFF_LAUNCH_PDL("vec_open", vec_open_kernel, std::min(std::max(n_mol, 1), 152 * 8), VEC_NT, 0, st, s->pos,
+                    s->vel, s->inv_mass, s->forces, dt, friction, kT, seed, s->step_counter, mol_ptr, n_mol, fix_com,
+                    ws_ptr<double>(ws, L.md_noise), ws_ptr<float>(ws, L.md_pos32), ws_ptr<Status>(ws, L.status));
+    return MLFF_OK;
+}
+
+int md_vec_close(const WsLayout& L, void* ws, mlff_md_state* s, double dt, double friction, double kT,
+                 int32_t fix_com, const int64_t* mol_ptr, int32_t n_mol, double* kinetic, cudaStream_t st) {
+    ProfScope prof(PK_MD, st);
+    MLFF_LAUNCH_PDL("vec_close", vec_close_kernel, std::min(std::max(n_mol, 1), 152 * 8), VEC_NT, 0, st, s->vel,
+                    s->inv_mass, s->forces, dt, friction, kT, ws_ptr<double>(ws, L.md_noise), mol_ptr, n_mol,
+                    fix_com, kinetic, s->step_counter, ws_ptr<Status>(ws, L.status));
+    return MLFF_OK;
+}
+
 // kinetic energy 1/2 m v^2 per structure (fixed-order tree)
 __global__ void kinetic_kernel(const double* __restrict__ vel, const double* __restrict__ inv_mass,
                                const int64_t* __restrict__ mol_ptr, int32_t n_mol, double* __restrict__ ke) {

@@ -36,6 +36,7 @@ struct WsLayout {
     size_t xbar;               // float [2][N][4][H]    adjoints
     size_t e_atom;             // float [N]
     size_t md_pos32;           // float [N][3]  positions the integrator hands to the force call
+    size_t md_noise;           // double [N][6] Langevin normals of a step (ASE's scheme: xi, eta)
     // plain path (materialised per-edge tensors, like the reference's graph)
     size_t geo;                // float4 [cap] (u_x, u_y, u_z, d)
     size_t etile_base;         // int32 [2][P+1] first E tile of each partition (forward, reverse)

@@ -42,6 +42,7 @@ ERROR_NAMES = {ERR_INVALID: "invalid argument", ERR_CAPACITY: "edge capacity exc
 EXPORTS = ["mlff_version", "mlff_last_error_string", "mlff_packed_weights_size", "mlff_pack_weights",
            "mlff_workspace_size", "mlff_build_neighbors", "mlff_copy_neighbors", "mlff_energy_forces",
            "mlff_read_status", "mlff_clear_status", "mlff_verlet_steps", "mlff_langevin_steps", "mlff_npt_steps",
+           "mlff_langevin_ase_steps",
            "mlff_md_energy_stats",
            "mlff_profile_begin",
            "mlff_profile_end", "mlff_radius_graph_noalloc", "mlff_param_grads", "mlff_param_grads_forces",
@@ -152,6 +153,10 @@ def load(build_if_missing: bool = True):
         lib.mlff_langevin_steps.argtypes = [ctypes.POINTER(Dims), _P, ctypes.POINTER(System), i64, i32,
                                             ctypes.POINTER(MDState), ctypes.c_double, ctypes.c_double,
                                             ctypes.c_double, ctypes.c_uint64, i32, _P, sz, _P]
+        lib.mlff_langevin_ase_steps.restype = ctypes.c_int
+        lib.mlff_langevin_ase_steps.argtypes = [ctypes.POINTER(Dims), _P, ctypes.POINTER(System), i64, i32,
+                                                ctypes.POINTER(MDState), ctypes.c_double, ctypes.c_double,
+                                                ctypes.c_double, ctypes.c_uint64, i32, i32, _P, sz, _P]
         lib.mlff_npt_steps.restype = ctypes.c_int
         lib.mlff_npt_steps.argtypes = [ctypes.POINTER(Dims), _P, ctypes.POINTER(System), i64, i32,
                                        ctypes.POINTER(MDState), ctypes.POINTER(NPTState), ctypes.c_double,

@@ -9,9 +9,11 @@ Blocks of steps are captured once in a CUDA graph and replayed, so a step
 costs no host round trip.
 
 ``set_langevin`` (or ``LangevinGPU``) switches the same driver to Langevin
-NVT dynamics (BAOAB splitting, ``mlff_langevin_steps``), the protocol the
-reference's MD benchmark runs through ASE's Langevin
-(benchmarks/md_trajectory.py:400-413); ``set_npt`` (or ``NPTGPU``) to NPT
+NVT dynamics, the protocol the reference's MD benchmark runs through ASE's
+Langevin (benchmarks/md_trajectory.py:407-413): by default ASE's own
+propagator (Vanden-Eijnden and Ciccotti, fixed centre of mass;
+``mlff_langevin_ase_steps``), or the BAOAB splitting
+(``mlff_langevin_steps``); ``set_npt`` (or ``NPTGPU``) to NPT
 with the equations of motion of ASE's NPT (Nose-Hoover thermostat,
 Parrinello-Rahman barostat; ``mlff_npt_steps``), the reference's NPT
 protocol (:415-424), on orthorhombic periodic boxes.
@@ -123,18 +125,23 @@ class VelocityVerletGPU:
         self.npt: Optional[Dict[str, float]] = None
         self.box64 = self.zeta = self.eta = self.xi = self.virial = None
 
-    def set_langevin(self, temperature_K: float, friction: float = 0.01, seed: int = 0):
+    def set_langevin(self, temperature_K: float, friction: float = 0.01, seed: int = 0, scheme: str = "ase",
+                     fixcm: bool = True):
         """Langevin NVT from now on: ``friction`` in inverse ASE time units
         (the reference's NVT protocol uses 0.01), target temperature in K;
-        ``None`` temperature switches back to NVE."""
+        ``None`` temperature switches back to NVE.  ``scheme``: "ase" (the
+        Vanden-Eijnden-Ciccotti propagator ASE's Langevin integrates, with
+        ``fixcm`` as ASE's: centre of mass held in place) or "baoab"."""
         if temperature_K is None:
             self.thermostat = None
             return
         if friction < 0 or temperature_K < 0:
             raise ValueError("friction and temperature must be non-negative")
+        if scheme not in ("ase", "baoab"):
+            raise ValueError(f"unknown Langevin scheme {scheme!r}: use 'ase' or 'baoab'")
         self.npt = None
         self.thermostat = {"friction": float(friction), "kT": float(units.kB * temperature_K),
-                           "seed": int(seed) & 0xFFFFFFFFFFFFFFFF}
+                           "seed": int(seed) & 0xFFFFFFFFFFFFFFFF, "scheme": scheme, "fixcm": bool(fixcm)}
 
     def set_npt(self, temperature_K: Optional[float], externalstress: float = 0.0, ttime: float = 25.0 * units.fs,
                 pfactor: float = 75.0 * units.fs ** 2):
@@ -267,6 +274,13 @@ class VelocityVerletGPU:
                                                   ctypes.byref(sysd), cap, self.path, ctypes.byref(st),
                                                   ctypes.c_double(self.dt), n_steps, ws.data_ptr(), ws.numel(),
                                                   _stream_handle()))
+        elif th["scheme"] == "ase":
+            _lib.check(self.lib.mlff_langevin_ase_steps(ctypes.byref(self.engine.dims), self.engine.packed.data_ptr(),
+                                                        ctypes.byref(sysd), cap, self.path, ctypes.byref(st),
+                                                        ctypes.c_double(self.dt), ctypes.c_double(th["friction"]),
+                                                        ctypes.c_double(th["kT"]), ctypes.c_uint64(th["seed"]),
+                                                        1 if th["fixcm"] else 0, n_steps, ws.data_ptr(), ws.numel(),
+                                                        _stream_handle()))
         else:
             _lib.check(self.lib.mlff_langevin_steps(ctypes.byref(self.engine.dims), self.engine.packed.data_ptr(),
                                                     ctypes.byref(sysd), cap, self.path, ctypes.byref(st),
@@ -341,13 +355,15 @@ class VelocityVerletGPU:
 
 class LangevinGPU(VelocityVerletGPU):
     """Langevin NVT driver with ASE Langevin's arguments (timestep in fs,
-    temperature_K, friction in inverse ASE time units): the reference's NVT
-    protocol (benchmarks/md_trajectory.py:408-413) on the fused GPU step."""
+    temperature_K, friction in inverse ASE time units, fixcm): the
+    reference's NVT protocol (benchmarks/md_trajectory.py:407-413) on the
+    fused GPU step.  scheme "ase" (default) integrates ASE's propagator,
+    "baoab" the BAOAB splitting."""
 
     def __init__(self, model, numbers, positions, mol_ptr, temperature_K: float, friction: float = 0.01,
-                 seed: int = 0, timestep_fs: float = 0.5, **kwargs):
+                 seed: int = 0, timestep_fs: float = 0.5, fixcm: bool = True, scheme: str = "ase", **kwargs):
         super().__init__(model, numbers, positions, mol_ptr, timestep_fs=timestep_fs, **kwargs)
-        self.set_langevin(temperature_K, friction, seed)
+        self.set_langevin(temperature_K, friction, seed, scheme=scheme, fixcm=fixcm)
 
 
 class NPTGPU(VelocityVerletGPU):

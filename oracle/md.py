@@ -70,6 +70,61 @@ def langevin_baoab(pos: np.ndarray, vel: np.ndarray, masses: np.ndarray,
     return r, v, F, epot, ekin
 
 
+def langevin_vec(pos: np.ndarray, vel: np.ndarray, masses: np.ndarray,
+                 force_fn: Callable[[np.ndarray], Tuple[np.ndarray, np.ndarray]], dt: float, friction: float,
+                 kT: float, seed: int, step0: int, n_steps: int, mol_ptr: np.ndarray, fix_com: bool = True):
+    """Float64 Langevin of Vanden-Eijnden and Ciccotti (Chem. Phys. Lett.
+    429, 310 (2006), Eq. 23), the scheme of ASE's Langevin (the reference's
+    NVT protocol, benchmarks/md_trajectory.py:407-413), with its default
+    fixed centre of mass, and the normals of oracle/philox.py:vec_normals
+    keyed by (seed, step0 + step, atom) as the GPU integrator draws them.
+    sigma = sqrt(2 kT gamma / m); c1 = dt/2 - dt^2 gamma/8, c2 = gamma dt/2 -
+    gamma^2 dt^2/8, c3 = sqrt(dt) sigma/2 - dt^1.5 gamma sigma/8, c5 =
+    dt^1.5 sigma/(2 sqrt 3), c4 = gamma c5/2;
+        v += c1 F/m - c2 v + c3 xi - c4 eta;  r += dt v + c5 eta
+        (fix_com: shift each structure back to its old centre of mass,
+         v = (r_new - r - c5 eta) / dt);  F = F(r);
+        v += c1 F/m - c2 v + c3 xi - c4 eta;  (fix_com: v -= v_com)."""
+    from oracle.philox import vec_normals
+    r = np.array(pos, dtype=np.float64)
+    v = np.array(vel, dtype=np.float64)
+    m = np.asarray(masses, dtype=np.float64)[:, None]
+    g = float(friction)
+    sig = np.sqrt(2.0 * kT * g / m)
+    c1 = dt / 2.0 - dt * dt * g / 8.0
+    c2 = g * dt / 2.0 - g * g * dt * dt / 8.0
+    c3 = np.sqrt(dt) * sig / 2.0 - dt ** 1.5 * g * sig / 8.0
+    c5 = dt ** 1.5 * sig / (2.0 * np.sqrt(3.0))
+    c4 = g / 2.0 * c5
+    e, F = force_fn(r)
+    B = len(mol_ptr) - 1
+    epot = np.zeros((n_steps, B))
+    ekin = np.zeros((n_steps, B))
+    groups = [slice(mol_ptr[b], mol_ptr[b + 1]) for b in range(B)]
+    for s in range(n_steps):
+        nz = vec_normals(seed, step0 + s, r.shape[0])
+        xi, eta = nz[:, :3], nz[:, 3:]
+        v = v + (c1 * F / m - c2 * v + c3 * xi - c4 * eta)
+        x_old = r
+        r = r + dt * v + c5 * eta
+        if fix_com:
+            for sl in groups:
+                mm = m[sl]
+                shift = ((mm * x_old[sl]).sum(axis=0) - (mm * r[sl]).sum(axis=0)) / mm.sum()
+                r[sl] = r[sl] + shift
+                v[sl] = v[sl] + shift / dt
+        e, F = force_fn(r)
+        v = v + (c1 * F / m - c2 * v + c3 * xi - c4 * eta)
+        if fix_com:
+            for sl in groups:
+                mm = m[sl]
+                v[sl] = v[sl] - (mm * v[sl]).sum(axis=0) / mm.sum()
+        ke = 0.5 * m * v * v
+        epot[s] = e
+        ekin[s] = [ke[sl].sum() for sl in groups]
+    return r, v, F, epot, ekin
+
+
 def npt_melchionna(pos: np.ndarray, vel: np.ndarray, masses: np.ndarray, box: np.ndarray,
                    force_fn: Callable[[np.ndarray, np.ndarray], Tuple[float, np.ndarray, np.ndarray]], dt: float,
                    kT: float, ttime: float, pfactor: float, pressure: float, n_steps: int,

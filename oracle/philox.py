@@ -52,3 +52,27 @@ def langevin_normals(seed: int, step: int, n_atoms: int) -> np.ndarray:
     t0 = 2.0 * np.pi * u[:, 1]
     t1 = 2.0 * np.pi * u[:, 3]
     return np.stack([r0 * np.cos(t0), r0 * np.sin(t0), r1 * np.cos(t1)], axis=1)
+
+
+def vec_normals(seed: int, step: int, n_atoms: int) -> np.ndarray:
+    """The six standard normals [n_atoms, 6] per atom of one step of the
+    Vanden-Eijnden-Ciccotti Langevin integrator (xi: columns 0-2, eta:
+    3-5): two Philox blocks with counters (step low, step high, atom, 1) and
+    (..., 2), key (seed low, seed high); Box-Muller on (u0, u1) and (u2, u3)
+    of each block, cosine then sine."""
+    a = np.arange(n_atoms, dtype=np.uint64)
+    key = np.zeros((n_atoms, 2), dtype=np.uint32)
+    key[:, 0] = np.uint32(seed & 0xFFFFFFFF)
+    key[:, 1] = np.uint32((seed >> 32) & 0xFFFFFFFF)
+    out = []
+    for word in (1, 2):
+        ctr = np.zeros((n_atoms, 4), dtype=np.uint32)
+        ctr[:, 0] = np.uint32(step & 0xFFFFFFFF)
+        ctr[:, 1] = np.uint32((step >> 32) & 0xFFFFFFFF)
+        ctr[:, 2] = a.astype(np.uint32)
+        ctr[:, 3] = np.uint32(word)
+        u = (philox4x32_10(ctr, key).astype(np.float64) + 0.5) * 2.0 ** -32
+        r0, r1 = np.sqrt(-2.0 * np.log(u[:, 0])), np.sqrt(-2.0 * np.log(u[:, 2]))
+        t0, t1 = 2.0 * np.pi * u[:, 1], 2.0 * np.pi * u[:, 3]
+        out += [r0 * np.cos(t0), r0 * np.sin(t0), r1 * np.cos(t1), r1 * np.sin(t1)]
+    return np.stack(out[:6], axis=1)

@@ -267,3 +267,21 @@ def test_force_metrics_oracle_pinned_to_reference():
         m = force_metrics.metrics(g[pre + "pred"], g[pre + "ref"])
         for key, v in m.items():
             np.testing.assert_allclose(v, g[pre + key], rtol=1e-9, atol=1e-12, err_msg=pre + key)
+
+
+def test_oracle_vec_langevin_thermostat_and_fixed_centre():
+    """The float64 Vanden-Eijnden-Ciccotti restatement on free particles:
+    centre of mass fixed, kinetic temperature at T over 3n - 3 degrees of
+    freedom."""
+    from oracle.md import langevin_vec
+    n = 200
+    rng = np.random.default_rng(5)
+    pos = rng.uniform(0, 50, (n, 3))
+    masses = rng.choice([1.008, 12.011, 15.999], n)
+    kT = 8.617333262e-5 * 300.0
+    free = lambda r: (np.zeros(1), np.zeros_like(r))
+    r, v, _, _, ek = langevin_vec(pos, np.zeros((n, 3)), masses, free, 0.05, 0.5, kT, 3, 0, 3000, np.array([0, n]))
+    com = lambda x: (masses[:, None] * x).sum(0) / masses.sum()
+    assert np.abs(com(r) - com(pos)).max() < 1e-9
+    T = ek[1000:, 0].mean() / (0.5 * (3 * n - 3) * 8.617333262e-5)
+    assert abs(T / 300.0 - 1.0) < 0.03
