@@ -65,7 +65,8 @@ def test_energy_metrics_vs_reference_outputs():
     energy_metrics outputs (golden_metrics.npz)."""
     from mlff_gb300 import energy_metrics as em
     g = _golden()
-    close = lambda a, b, key: np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-12, err_msg=key)
+    # absolute 1e-10: R^2 = 1 - ss_res / ss_tot cancels where a fit explains nothing
+    close = lambda a, b, key: np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-10, err_msg=key)
     for i in range(4):
         pre = f"e{i}/"
         t, k, p = g[pre + "time"], g[pre + "kinetic"], g[pre + "potential"]
@@ -96,7 +97,8 @@ def test_force_metrics_vs_reference_outputs():
     functions against the reference's own force_metrics outputs."""
     from mlff_gb300 import force_metrics as fm
     g = _golden()
-    close = lambda a, b, key: np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-12, err_msg=key)
+    # absolute 1e-10: R^2 = 1 - ss_res / ss_tot cancels where a fit explains nothing
+    close = lambda a, b, key: np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-10, err_msg=key)
     for i in range(3):
         pre = f"f{i}/"
         pred, ref = g[pre + "pred"], g[pre + "ref"]
