@@ -85,6 +85,7 @@ WsLayout ws_layout(const mlff_dims& d, int32_t n_atoms, int32_t n_mol, int64_t c
     L.edge_acc = take(sizeof(float4) * cap);
     L.scan_tmp = take(4 * ((scan_n + 1023) / 1024 + 2));
     L.mol_grid = take(sizeof(int4) * (B + 1));   // + the count of cell codes in use
+    L.mol_box = take(sizeof(float4) * 2 * B);
     L.cell_count = take(4 * (L.ncell_cap + 1));
     L.cell_fill = take(4 * L.ncell_cap);
     L.cell_pos = take(sizeof(float4) * N);

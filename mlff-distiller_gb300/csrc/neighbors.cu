@@ -8,9 +8,12 @@
 // reference's edge_index (src-major, then dst) element for element.  In the
 // model kernels row a is the receiver of the message b -> a.
 //
-// Open structures: every atom pair of the structure is tested (one warp per
-// row, warp-ballot compaction keeps the ascending order).  Periodic boxes:
-// atoms are binned into cells of edge >= cutoff, the cells numbered along a
+// Open structures below OPEN_CELL_MIN atoms: every atom pair of the
+// structure is tested (one warp per row, warp-ballot compaction keeps the
+// ascending order).  Larger open structures get a cell grid over their
+// bounding box (cells of width >= 1.001 cutoff, at most 1024 per axis and
+// max(n, 27) in all, no wrap).  Periodic boxes: atoms are binned into
+// cells of edge >= cutoff.  In both the cells are numbered along a
 // Morton (Z-order) curve, and the atoms copied in that order (position and
 // atom index in one float4, so a cell's candidates are contiguous and
 // neighbouring cells lie close in memory); a row's warp looks up its 27 (or
@@ -18,7 +21,11 @@
 // neighbouring cells in one step -- one cell per lane, a warp scan of their
 // sizes -- and walks the concatenated candidates 32 at a time, each lane
 // finding its cell by a binary search over the scan; hits are compacted
-// with a warp ballot into shared memory and rank-sorted.
+// with a warp ballot into shared memory and rank-sorted.  The cell grid
+// only chooses candidates: every candidate pair goes through the same
+// distance decision, and two atoms within the cutoff always sit in the same
+// or adjacent cells (clamped, monotone cell indices of width >= cutoff), so
+// the edge set is the all-pairs one.
 #include "common.cuh"
 #include "workspace.h"
 #include "profile.h"
@@ -26,7 +33,10 @@
 namespace mlff {
 
 constexpr int NBR_WARPS = 8;        // warps per block in the row kernels
-constexpr int ROW_CAP = 512;        // neighbours one periodic row can hold
+constexpr int ROW_CAP = 512;        // neighbours one cell-list row can hold
+constexpr int OPEN_CELL_MIN = 256;  // open structures with at least this many atoms use a cell grid
+constexpr int OPEN_NC_MAX = 1024;   // cells per axis of an open structure's grid
+constexpr float OPEN_CELL_MARGIN = 1.001f;   // open cell width / cutoff: covers the float32 cell-index rounding
 
 // ------------------------------------------------------------------ scan
 __global__ void scan_local_kernel(int32_t* __restrict__ data, int64_t n, int32_t* __restrict__ sums) {
@@ -222,15 +232,66 @@ __device__ __forceinline__ int morton3(int x, int y, int z, int bx, int by, int 
     return code;
 }
 
+__device__ __forceinline__ bool mol_celled_open(const int64_t* mol_ptr, const uint8_t* pbc, const float* box,
+                                                int m) {
+    const bool per = pbc != nullptr && box != nullptr && pbc[m] != 0;
+    return !per && mol_ptr[m + 1] - mol_ptr[m] >= OPEN_CELL_MIN;
+}
+
+// Bounding box (lower and upper corner) of every open structure that gets a
+// cell grid: one block per structure, fixed-order min / max.
+__global__ void __launch_bounds__(256) mol_bbox_kernel(const float4* __restrict__ pos4,
+                                                       const int64_t* __restrict__ mol_ptr,
+                                                       const uint8_t* __restrict__ pbc, const float* __restrict__ box,
+                                                       int32_t n_mol, float4* __restrict__ mol_box) {
+    pdl_wait();
+    pdl_trigger();
+    __shared__ float lo[3][256], hi[3][256];
+    const int t = threadIdx.x;
+    for (int m = blockIdx.x; m < n_mol; m += gridDim.x) {
+        if (!mol_celled_open(mol_ptr, pbc, box, m)) continue;
+        float l[3] = {INFINITY, INFINITY, INFINITY}, h[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int64_t a = mol_ptr[m] + t; a < mol_ptr[m + 1]; a += 256) {
+            const float4 p = pos4[a];
+            l[0] = fminf(l[0], p.x); l[1] = fminf(l[1], p.y); l[2] = fminf(l[2], p.z);
+            h[0] = fmaxf(h[0], p.x); h[1] = fmaxf(h[1], p.y); h[2] = fmaxf(h[2], p.z);
+        }
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            lo[q][t] = l[q];
+            hi[q][t] = h[q];
+        }
+        __syncthreads();
+        for (int o = 128; o > 0; o >>= 1) {
+            if (t < o)
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    lo[q][t] = fminf(lo[q][t], lo[q][t + o]);
+                    hi[q][t] = fmaxf(hi[q][t], hi[q][t + o]);
+                }
+            __syncthreads();
+        }
+        if (t == 0) {
+            mol_box[2 * m] = make_float4(lo[0][0], lo[1][0], lo[2][0], 0.f);
+            mol_box[2 * m + 1] = make_float4(hi[0][0], hi[1][0], hi[2][0], 0.f);
+        }
+        __syncthreads();
+    }
+}
+
 // One block: per periodic structure choose the cell grid (cells of edge
 // >= cutoff, at most max(n_atoms, 27) cells) and the first cell code (the
 // structure's Morton code space is under 8 times its cell count).
 // It also zeroes the counters and fill cursors of the codes in use and
 // writes their count to grid[n_mol].x.
+// Open structures with a cell grid: cells of width max(1.001 cutoff,
+// extent / nc) over the bounding box, the cell count limited the same way;
+// mol_box[2m + 1] becomes 1 / cell width per axis.
 __global__ void mol_grid_kernel(const int64_t* __restrict__ mol_ptr, const float* __restrict__ box,
                                 const uint8_t* __restrict__ pbc, int32_t n_mol, float cutoff,
-                                int4* __restrict__ grid, int32_t* __restrict__ cell_count,
-                                int32_t* __restrict__ cell_fill, int64_t ncell_cap, Status* st) {
+                                int4* __restrict__ grid, float4* __restrict__ mol_box,
+                                int32_t* __restrict__ cell_count, int32_t* __restrict__ cell_fill,
+                                int64_t ncell_cap, Status* st) {
     pdl_wait();
     pdl_trigger();
     __shared__ int32_t warp_tot[32];
@@ -261,6 +322,28 @@ __global__ void mol_grid_kernel(const int64_t* __restrict__ mol_ptr, const float
                 nc[a] -= 1;
             }
             // cells are numbered by their Morton code: the code space holds 2^(bits x + y + z)
+            ncell = 1 << (cell_bits(nc[0]) + cell_bits(nc[1]) + cell_bits(nc[2]));
+        } else if (m < n_mol && mol_celled_open(mol_ptr, pbc, box, m)) {
+            const int n_m = (int)(mol_ptr[m + 1] - mol_ptr[m]);
+            const float4 lo = mol_box[2 * m], hi = mol_box[2 * m + 1];
+            const float ext[3] = {hi.x - lo.x, hi.y - lo.y, hi.z - lo.z};
+            const float w0 = cutoff * OPEN_CELL_MARGIN;
+            for (int a = 0; a < 3; ++a) {
+                // a non-finite extent (inf or NaN positions) gets one cell: every pair is then a candidate
+                nc[a] = isfinite(ext[a]) ? (int)fminf(floorf(ext[a] / w0) + 1.0f, (float)OPEN_NC_MAX) : 1;
+                nc[a] = max(nc[a], 1);
+            }
+            const int lim = max(n_m, 27);
+            while ((long long)nc[0] * nc[1] * nc[2] > lim) {
+                int a = (nc[0] >= nc[1] && nc[0] >= nc[2]) ? 0 : (nc[1] >= nc[2] ? 1 : 2);
+                nc[a] -= 1;
+            }
+            float inv[3];
+            for (int a = 0; a < 3; ++a) {
+                const float wa = isfinite(ext[a]) ? fmaxf(w0, ext[a] / (float)nc[a] * OPEN_CELL_MARGIN) : 1.0f;
+                inv[a] = nc[a] > 1 ? 1.0f / wa : 0.0f;
+            }
+            mol_box[2 * m + 1] = make_float4(inv[0], inv[1], inv[2], 0.f);
             ncell = 1 << (cell_bits(nc[0]) + cell_bits(nc[1]) + cell_bits(nc[2]));
         }
         int32_t x = ncell;
@@ -319,22 +402,39 @@ __device__ __forceinline__ int cell_coord(float x, float L, float invL, int nc) 
     int c = (int)(w * invL * (float)nc);
     return min(max(c, 0), nc - 1);
 }
+// open structure: cell of coordinate x on a grid starting at lo (no wrap;
+// NaN lands in cell 0)
+__device__ __forceinline__ int open_cell_coord(float x, float lo, float inv_w, int nc) {
+    const float f = (x - lo) * inv_w;
+    const int c = f > 0.f ? (int)fminf(f, (float)(nc - 1)) : 0;
+    return min(max(c, 0), nc - 1);
+}
 
 __global__ void cell_count_kernel(const float4* __restrict__ pos4, const int32_t* __restrict__ atom_mol,
-                                  const float* __restrict__ box, const uint8_t* __restrict__ pbc,
-                                  const int4* __restrict__ grid, int32_t n_atoms,
+                                  const int64_t* __restrict__ mol_ptr, const float* __restrict__ box,
+                                  const uint8_t* __restrict__ pbc, const int4* __restrict__ grid,
+                                  const float4* __restrict__ mol_box, int32_t n_atoms,
                                   int32_t* __restrict__ atom_cell, int32_t* __restrict__ cell_count) {
     pdl_wait();
     pdl_trigger();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_atoms; i += gridDim.x * blockDim.x) {
         int m = atom_mol[i];
-        if (!mol_periodic(pbc, box, m)) { atom_cell[i] = -1; continue; }
+        const bool open_cells = mol_celled_open(mol_ptr, pbc, box, m);
+        if (!mol_periodic(pbc, box, m) && !open_cells) { atom_cell[i] = -1; continue; }
         int4 g = grid[m];
-        Box b = load_box(box, pbc, m);
         float4 p = pos4[i];
-        int cx = cell_coord(p.x, b.L[0], b.invL[0], g.x);
-        int cy = cell_coord(p.y, b.L[1], b.invL[1], g.y);
-        int cz = cell_coord(p.z, b.L[2], b.invL[2], g.z);
+        int cx, cy, cz;
+        if (open_cells) {
+            const float4 lo = mol_box[2 * m], iw = mol_box[2 * m + 1];
+            cx = open_cell_coord(p.x, lo.x, iw.x, g.x);
+            cy = open_cell_coord(p.y, lo.y, iw.y, g.y);
+            cz = open_cell_coord(p.z, lo.z, iw.z, g.z);
+        } else {
+            Box b = load_box(box, pbc, m);
+            cx = cell_coord(p.x, b.L[0], b.invL[0], g.x);
+            cy = cell_coord(p.y, b.L[1], b.invL[1], g.y);
+            cz = cell_coord(p.z, b.L[2], b.invL[2], g.z);
+        }
         int c = g.w + morton3(cx, cy, cz, cell_bits(g.x), cell_bits(g.y), cell_bits(g.z));
         atom_cell[i] = c;
         atomicAdd(&cell_count[c], 1);
@@ -363,6 +463,7 @@ struct NbrArgs {
     const float* box;
     const uint8_t* pbc;
     const int4* grid;
+    const float4* mol_box;
     const int32_t* cell_start;
     const float4* cell_pos;
     int32_t n_atoms;
@@ -391,7 +492,8 @@ __global__ void __launch_bounds__(NBR_WARPS * 32) nbr_rows_kernel(NbrArgs a) {
         const Box b = load_box(a.box, a.pbc, m);
         int cnt = 0;
         const int base = FILL ? a.counts[i] : 0;
-        if (!b.periodic) {
+        const bool open_cells = !b.periodic && a.mol_ptr[m + 1] - a.mol_ptr[m] >= OPEN_CELL_MIN;
+        if (!b.periodic && !open_cells) {
             const int a0 = (int)a.mol_ptr[m], a1 = (int)a.mol_ptr[m + 1];
             for (int j0 = a0; j0 < a1; j0 += 32) {
                 const int j = j0 + lane;
@@ -412,13 +514,23 @@ __global__ void __launch_bounds__(NBR_WARPS * 32) nbr_rows_kernel(NbrArgs a) {
         } else {
             const int4 g = a.grid[m];
             // the row atom's cell, computed as the binning did
-            const int cc[3] = {cell_coord(pi.x, b.L[0], b.invL[0], g.x), cell_coord(pi.y, b.L[1], b.invL[1], g.y),
-                               cell_coord(pi.z, b.L[2], b.invL[2], g.z)};
+            int cc[3];
+            if (open_cells) {
+                const float4 lo = a.mol_box[2 * m], iw = a.mol_box[2 * m + 1];
+                cc[0] = open_cell_coord(pi.x, lo.x, iw.x, g.x);
+                cc[1] = open_cell_coord(pi.y, lo.y, iw.y, g.y);
+                cc[2] = open_cell_coord(pi.z, lo.z, iw.z, g.z);
+            } else {
+                cc[0] = cell_coord(pi.x, b.L[0], b.invL[0], g.x);
+                cc[1] = cell_coord(pi.y, b.L[1], b.invL[1], g.y);
+                cc[2] = cell_coord(pi.z, b.L[2], b.invL[2], g.z);
+            }
             const int ncs[3] = {g.x, g.y, g.z};
             const int bits[3] = {cell_bits(g.x), cell_bits(g.y), cell_bits(g.z)};
             bool overflow = false;
             // lane k < 27 looks up neighbour cell (k / 9, k / 3 % 3, k % 3) - 1 (wrapped); on an
-            // axis with fewer than 3 cells the offsets 0 .. nc-1 name its cells directly
+            // axis with fewer than 3 cells the offsets 0 .. nc-1 name its cells directly; an open
+            // grid does not wrap (cells outside it are skipped)
             int c0 = 0, len = 0;
             if (lane < 27) {
                 const int o[3] = {lane / 9, (lane / 3) % 3, lane % 3};
@@ -426,7 +538,10 @@ __global__ void __launch_bounds__(NBR_WARPS * 32) nbr_rows_kernel(NbrArgs a) {
                 int q[3];
 #pragma unroll
                 for (int ax = 0; ax < 3; ++ax) {
-                    if (ncs[ax] >= 3) {
+                    if (open_cells) {
+                        q[ax] = cc[ax] + o[ax] - 1;
+                        keep = keep && q[ax] >= 0 && q[ax] < ncs[ax];
+                    } else if (ncs[ax] >= 3) {
                         q[ax] = (cc[ax] + o[ax] - 1 + ncs[ax]) % ncs[ax];
                     } else {
                         keep = keep && o[ax] < ncs[ax];
@@ -577,15 +692,22 @@ static int scan_with_total(int32_t* data, int64_t n_in, int32_t* tmp, Status* st
 int launch_neighbors_into(const mlff_dims& d, const mlff_system& sys, const NbrBuffers& b, cudaStream_t st) {
     const int N = sys.n_atoms;
     const bool any_pbc = sys.pbc != nullptr && sys.box != nullptr;
+    // an open structure of OPEN_CELL_MIN atoms or more needs at least that many atoms in all
+    const bool any_open_cells = N >= OPEN_CELL_MIN;
     const int tb = 256;
     const int gb = (int)std::max<int64_t>(1, std::min<int64_t>((N + tb - 1) / tb, 152 * 16));
     MLFF_LAUNCH_PDL("prep_atoms", prep_atoms_kernel, gb, tb, 0, st, sys.pos, sys.mol_ptr, sys.n_mol, N, b.pos4,
                     b.atom_mol);
-    if (any_pbc) {
+    if (any_pbc || any_open_cells) {
+        if (any_open_cells) {
+            const int mb = std::max(1, std::min(sys.n_mol, 152 * 8));
+            MLFF_LAUNCH_PDL("mol_bbox", mol_bbox_kernel, mb, 256, 0, st, b.pos4, sys.mol_ptr, sys.pbc, sys.box,
+                            sys.n_mol, b.mol_box);
+        }
         MLFF_LAUNCH_PDL("mol_grid", mol_grid_kernel, 1, 1024, 0, st, sys.mol_ptr, sys.box, sys.pbc, sys.n_mol, d.cutoff,
-                        b.mol_grid, b.cell_count, b.cell_fill, b.ncell_cap, b.status);
-        MLFF_LAUNCH_PDL("cell_count", cell_count_kernel, gb, tb, 0, st, b.pos4, b.atom_mol, sys.box, sys.pbc, b.mol_grid,
-                        N, b.atom_cell, b.cell_count);
+                        b.mol_grid, b.mol_box, b.cell_count, b.cell_fill, b.ncell_cap, b.status);
+        MLFF_LAUNCH_PDL("cell_count", cell_count_kernel, gb, tb, 0, st, b.pos4, b.atom_mol, sys.mol_ptr, sys.box,
+                        sys.pbc, b.mol_grid, b.mol_box, N, b.atom_cell, b.cell_count);
         // the cell codes in use (grid[n_mol].x, at most ncell_cap), scanned by one block
         int r = scan_with_total(b.cell_count, b.ncell_cap, b.scan_tmp, nullptr, 0, st,
                                 reinterpret_cast<const int32_t*>(b.mol_grid + sys.n_mol));
@@ -595,7 +717,7 @@ int launch_neighbors_into(const mlff_dims& d, const mlff_system& sys, const NbrB
     }
     NbrArgs a;
     a.pos4 = b.pos4; a.atom_mol = b.atom_mol; a.mol_ptr = sys.mol_ptr; a.box = sys.box; a.pbc = sys.pbc;
-    a.grid = b.mol_grid; a.cell_start = b.cell_count; a.cell_pos = b.cell_pos;
+    a.grid = b.mol_grid; a.mol_box = b.mol_box; a.cell_start = b.cell_count; a.cell_pos = b.cell_pos;
     a.n_atoms = N; a.cutoff = d.cutoff; a.cap = b.cap; a.counts = b.row_ptr;
     a.col = b.col; a.erecv = b.erecv; a.st = b.status;
     const int rows_blocks = (int)std::max<int64_t>(1, std::min<int64_t>((N + NBR_WARPS - 1) / NBR_WARPS, 152 * 32));
@@ -618,6 +740,7 @@ int launch_neighbors(const mlff_dims& d, const mlff_system& sys, const WsLayout&
     b.erecv = ws_ptr<int32_t>(ws, L.erecv);
     b.scan_tmp = ws_ptr<int32_t>(ws, L.scan_tmp);
     b.mol_grid = ws_ptr<int4>(ws, L.mol_grid);
+    b.mol_box = ws_ptr<float4>(ws, L.mol_box);
     b.cell_count = ws_ptr<int32_t>(ws, L.cell_count);
     b.cell_fill = ws_ptr<int32_t>(ws, L.cell_fill);
     b.cell_pos = ws_ptr<float4>(ws, L.cell_pos);

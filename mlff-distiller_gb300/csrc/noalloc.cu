@@ -39,7 +39,8 @@ constexpr int64_t kOffAtomMol = align256(kOffPos4 + 16 * NOALLOC_MAX_ATOMS);
 constexpr int64_t kOffErecv = align256(kOffAtomMol + 4 * NOALLOC_MAX_ATOMS);
 constexpr int64_t kOffScan = align256(kOffErecv + 4 * NOALLOC_MAX_EDGES);
 constexpr int64_t kOffGrid = align256(kOffScan + 4 * ((kScanN + 1023) / 1024 + 2));
-constexpr int64_t kOffCellCount = align256(kOffGrid + 16 * (NOALLOC_MAX_MOLS + 1));
+constexpr int64_t kOffMolBox = align256(kOffGrid + 16 * (NOALLOC_MAX_MOLS + 1));
+constexpr int64_t kOffCellCount = align256(kOffMolBox + 16 * 2 * NOALLOC_MAX_MOLS);
 constexpr int64_t kOffCellFill = align256(kOffCellCount + 4 * (kNcellCap + 1));
 constexpr int64_t kOffCellPos = align256(kOffCellFill + 4 * kNcellCap);
 constexpr int64_t kOffAtomCell = align256(kOffCellPos + 16 * NOALLOC_MAX_ATOMS);
@@ -123,6 +124,7 @@ extern "C" int mlff_radius_graph_noalloc(const mlff_system* sys, float cutoff, i
     b.erecv = reinterpret_cast<int32_t*>(s + kOffErecv);
     b.scan_tmp = reinterpret_cast<int32_t*>(s + kOffScan);
     b.mol_grid = reinterpret_cast<int4*>(s + kOffGrid);
+    b.mol_box = reinterpret_cast<float4*>(s + kOffMolBox);
     b.cell_count = reinterpret_cast<int32_t*>(s + kOffCellCount);
     b.cell_fill = reinterpret_cast<int32_t*>(s + kOffCellFill);
     b.cell_pos = reinterpret_cast<float4*>(s + kOffCellPos);

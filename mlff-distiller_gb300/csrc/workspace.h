@@ -13,7 +13,7 @@ constexpr int GRAD_MIX_BLOCKS = 304;  // blocks of the mixing-matrix gradient
 struct WsLayout {
     int32_t N, B, L, P;        // atoms, structures, layers, persistent CTAs
     int64_t cap;               // edge capacity
-    int64_t ncell_cap;         // cell-code capacity, 8 (N + 27 B) (Morton code spaces of periodic structures)
+    int64_t ncell_cap;         // cell-code capacity, 8 (N + 27 B) (Morton code spaces of the cell grids)
     size_t status;             // Status
     size_t pos4;               // float4 [N]
     size_t atom_mol;           // int32 [N]
@@ -24,6 +24,7 @@ struct WsLayout {
     size_t edge_acc;           // float4 [cap] (dE/dd, dE/du) summed over layers
     size_t scan_tmp;           // int32 [scan_blocks + 1]
     size_t mol_grid;           // int4 [B + 1]  (ncx, ncy, ncz, first cell code); [B].x = codes in use
+    size_t mol_box;            // float4 [2 B]  open structures with a cell grid: origin, 1 / cell width
     size_t cell_count;         // int32 [ncell_cap + 1]
     size_t cell_fill;          // int32 [ncell_cap]
     size_t cell_pos;           // float4 [N]  atoms in cell order: x, y, z, atom index (int bits)
@@ -82,6 +83,7 @@ struct NbrBuffers {
     int32_t* erecv;         // [cap]
     int32_t* scan_tmp;      // [(max(N+1, ncell_cap+1) + 1023) / 1024 + 2]
     int4* mol_grid;         // [B + 1]
+    float4* mol_box;        // [2 B] open structures with a cell grid: origin (then upper corner), 1 / cell width
     int32_t* cell_count;    // [ncell_cap + 1]
     int32_t* cell_fill;     // [ncell_cap]
     float4* cell_pos;       // [N] atoms in cell order (x, y, z, index bits)

@@ -197,3 +197,62 @@ def test_bad_inputs_reported(weights_seed0):
         eng.energy_forces(make_batch([1, 1], [[0, 0, 0], [1, 0, 0]], [0, 2], box=[[6.0, 6.0, 6.0]],
                                      pbc=[True]), _lib.PATH_TUNED_FP32)
     assert ei.value.code == _lib.ERR_BOX
+
+
+def _open_cluster(n_atoms, seed):
+    """An open cluster at the 100k box's density: the jittered lattice of
+    large_box without periodicity."""
+    from mlff_gb300 import systems
+    s = systems.large_box(n_atoms=n_atoms, seed=seed)
+    s.pbc = np.zeros(1, bool)
+    s.box = np.zeros((1, 3))
+    return s
+
+
+@pytest.mark.parametrize("n_atoms", [256, 20_000])
+def test_neighbors_open_cluster_cell_grid_vs_oracle(weights_seed0, n_atoms):
+    """Open structures of 256 atoms or more are binned into a bounding-box
+    cell grid; the edge set must equal the oracle's all-pairs search bit for
+    bit."""
+    from mlff_gb300.engine import make_batch
+    s = _open_cluster(n_atoms, seed=6)
+    pos32 = s.pos.astype(np.float32)
+    src, dst, _ = nbr.radius_graph(pos32, s.mol_ptr, 5.0)
+    m = engine_for(weights_seed0)
+    row_ptr, col = m.engine().neighbors(make_batch(s.Z, pos32, s.mol_ptr))
+    row_ptr = row_ptr.cpu().numpy().astype(np.int64)
+    assert int(row_ptr[-1]) == len(src)
+    np.testing.assert_array_equal(np.repeat(np.arange(s.n_atoms), np.diff(row_ptr)), src)
+    np.testing.assert_array_equal(col.cpu().numpy(), dst)
+
+
+def test_neighbors_mixed_batch_vs_oracle(weights_seed0):
+    """Small open molecules (all pairs), large open clusters (cell grid), an
+    elongated open chain (few cells on two axes) and a periodic box in one
+    batch."""
+    from mlff_gb300 import systems
+    from mlff_gb300.engine import make_batch
+    rng = np.random.default_rng(7)
+    chain = systems.lattice_molecule(300, seed=8)
+    chain.pos = np.stack([np.arange(300) * 1.1, 0.3 * rng.standard_normal(300), 0.3 * rng.standard_normal(300)], 1)
+    parts = [systems.lattice_molecule(50, seed=1), _open_cluster(1000, seed=2), chain,
+             systems.water_box(n_water=60, L=11.5, d_oo=2.2, seed=8), _open_cluster(300, seed=3)]
+    s = systems.concat(parts)
+    pos32 = s.pos.astype(np.float32)
+    src, dst, _ = nbr.radius_graph(pos32, s.mol_ptr, 5.0, s.box, s.pbc)
+    m = engine_for(weights_seed0)
+    row_ptr, col = m.engine().neighbors(make_batch(s.Z, pos32, s.mol_ptr, s.box, s.pbc))
+    row_ptr = row_ptr.cpu().numpy().astype(np.int64)
+    np.testing.assert_array_equal(np.repeat(np.arange(s.n_atoms), np.diff(row_ptr)), src)
+    np.testing.assert_array_equal(col.cpu().numpy(), dst)
+
+
+@pytest.mark.parametrize("path", ["fp16x3", "fp32"])
+def test_open_cluster_energy_forces_vs_oracle(weights_bias, path):
+    s = _open_cluster(600, seed=9)
+    pos32 = s.pos.astype(np.float32)
+    m = engine_for(weights_bias, path)
+    E, F, _ = run(m, s.Z, pos32, s.mol_ptr)
+    E0, F0 = painn.energy_forces(weights_bias, s.Z, pos32.astype(np.float64), s.mol_ptr)
+    assert abs(E[0] - float(E0[0])) <= E_TOL_PER_ATOM * s.n_atoms
+    assert np.abs(F - F0.numpy()).max() <= F_TOL
