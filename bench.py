@@ -389,12 +389,16 @@ def time_replays(step, steps, flush):
 
 def graph_step(model, sysm, warmup):
     """A CUDA graph of one E+F evaluation of the workload on the model's
-    path (edge capacity sized first); returns (replay, E, F, n_edges)."""
+    path (edge capacity sized and, for the tensor-core path, the partition
+    factor tuned first); returns (replay, E, F, n_edges)."""
+    from mlff_gb300 import _lib
     from mlff_gb300.engine import make_batch
     eng = model.engine()
     batch = make_batch(sysm.Z, sysm.pos, sysm.mol_ptr, sysm.box if sysm.pbc.any() else None,
                        sysm.pbc if sysm.pbc.any() else None)
-    eng.energy_forces(batch, model.path)
+    eng.energy_forces(batch, model.path, graph=False)
+    if model.path == _lib.PATH_TUNED_TC:
+        eng.autotune(batch, model.path)
     _, n_edges, _ = eng.status()
     step, E, F = eng.capture(batch, model.path)
     for _ in range(max(3, warmup)):
@@ -455,7 +459,8 @@ def main():
     path = model.path
     batch = make_batch(sysm.Z, sysm.pos, sysm.mol_ptr, sysm.box if sysm.pbc.any() else None,
                        sysm.pbc if sysm.pbc.any() else None)
-    eng.energy_forces(batch, path)            # sizes the edge capacity, checks status
+    eng.energy_forces(batch, path, graph=False)   # sizes the edge capacity, checks status
+    tune = eng.autotune(batch, path) if path == _lib.PATH_TUNED_TC else None
     _, n_edges, _ = eng.status()
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     for _ in range(max(3, args.warmup)):
@@ -594,7 +599,7 @@ def main():
                        "directed_edges": n_edges, "path": args.path, "l2": "256 MiB buffer rewritten "
                        "between timed steps", "per_rank": "independent copy of the workload",
                        "launch": "CUDA graph of one step" if args.graph else "eager library call per step",
-                       "hbm_peak_bytes": hbm_peak},
+                       "hbm_peak_bytes": hbm_peak, "autotune": tune},
             "vs_plain_fp32": compare, "accuracy": acc,
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches,
             "kernel_ms": {k: round(v, 3) for k, v in prof.ms.items() if v > 0},

@@ -355,6 +355,28 @@ int mlff_param_grads_forces(const mlff_dims *dims, const void *packed, const mlf
 int mlff_profile_begin(void);
 int mlff_profile_end(double *ms_by_kind, int64_t *launches_by_kind, int32_t n_kinds);
 
+/* Autotuning (no counterpart in the reference, whose only GPU kernels fix
+ * their block sizes by hand).  The tensor-core path splits the receivers
+ * into 2 x SMs x f partitions; the partition factor f (1, 2 or 4) is
+ * chosen per size bucket (path, ceil(log2 n_atoms), ceil(log2 n_mol)) and
+ * kept in a process-wide cache guarded by a mutex; every call of that
+ * bucket then uses it.  Results do not depend on f (each receiver's sums run
+ * over its edges in order inside one partition), and the workspace size
+ * does not either.  mlff_autotune times `repeats` calls of
+ * mlff_energy_forces per candidate (same arguments; the outputs are
+ * overwritten) with CUDA events on the stream, synchronises the stream,
+ * caches the fastest and writes it to *chosen (host) and the milliseconds
+ * per call of f = 1, 2, 4 to ms_per_candidate (host double [3], or NULL).
+ * Not for use while the stream is being captured.  Other paths: *chosen = 1,
+ * nothing timed.  _query reads the factor a call of that size would use,
+ * _set pins one (0 removes the entry), _reset empties the cache. */
+int mlff_autotune(const mlff_dims *dims, const void *packed, const mlff_system *sys, int64_t edge_capacity,
+                  int32_t path, const mlff_outputs *out, void *workspace, size_t workspace_bytes,
+                  mlff_stream_t stream, int32_t repeats, int32_t *chosen, double *ms_per_candidate);
+int mlff_autotune_query(int32_t path, int32_t n_atoms, int32_t n_mol, int32_t *factor);
+int mlff_autotune_set(int32_t path, int32_t n_atoms, int32_t n_mol, int32_t factor);
+int mlff_autotune_reset(void);
+
 /* Force-accuracy statistics on the device (testing/force_metrics.py:46-384,
  * whose functions take host arrays): pred and ref are double [n_vectors,3]
  * device arrays; stats (double [MLFF_FORCE_STATS], device) receives

@@ -6,6 +6,9 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cmath>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <atomic>
 #include "common.cuh"
 #include "workspace.h"
@@ -50,8 +53,41 @@ int persistent_ctas(int32_t path) {
     // Receiver partitions: the CUDA-core fused kernels run 4 CTAs of 128
     // threads per SM; the tensor-core kernels run one CTA per SM with two
     // partitions each (the reverse kernel's two pipelines take one each,
-    // the forward kernel walks both as one receiver range).
+    // the forward kernel walks both as one receiver range), times the
+    // partition factor the autotuner chose for the call's size.
     return path == MLFF_PATH_TUNED_TC ? 2 * num_sms() : num_sms() * 4;
+}
+
+// ----------------------------------------------------------- autotuning
+// The tensor-core path's receiver partitions per CTA pipeline (the
+// partition factor; 1, 2 or 4: more, smaller partitions balance uneven
+// rows better at the cost of more partial edge tiles) chosen per size
+// bucket (path, ceil(log2 atoms), ceil(log2 structures)) by mlff_autotune
+// and kept in a process-wide cache guarded by a mutex.  Results do not
+// depend on the factor: every receiver's sums run over its edges in order
+// within one partition.  The workspace is sized for the largest factor.
+constexpr int TUNE_FACTORS[3] = {1, 2, 4};
+constexpr int TUNE_FACTOR_MAX = 4;
+namespace {
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int>, int> g_tune;
+thread_local int g_tune_override = 0;   // set by mlff_autotune while it times a candidate
+int ceil_log2(int64_t x) {
+    int b = 0;
+    while ((int64_t(1) << b) < x) ++b;
+    return b;
+}
+std::tuple<int, int, int> tune_key(int32_t path, int32_t n_atoms, int32_t n_mol) {
+    return {path, ceil_log2(std::max(n_atoms, 1)), ceil_log2(std::max(n_mol, 1))};
+}
+}  // namespace
+
+int tuned_part_factor(int32_t path, int32_t n_atoms, int32_t n_mol) {
+    if (path != MLFF_PATH_TUNED_TC) return 1;
+    if (g_tune_override) return g_tune_override;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(tune_key(path, n_atoms, n_mol));
+    return it == g_tune.end() ? 1 : it->second;
 }
 
 WsLayout ws_layout(const mlff_dims& d, int32_t n_atoms, int32_t n_mol, int64_t cap, int32_t path) {
@@ -59,7 +95,9 @@ WsLayout ws_layout(const mlff_dims& d, int32_t n_atoms, int32_t n_mol, int64_t c
     L.N = n_atoms;
     L.B = n_mol;
     L.L = d.n_layers;
-    L.P = persistent_ctas(path);
+    // arrays sized for the largest partition factor, so that tuning never changes the size
+    const int64_t P_max = (int64_t)persistent_ctas(path) * (path == MLFF_PATH_TUNED_TC ? TUNE_FACTOR_MAX : 1);
+    L.P = persistent_ctas(path) * tuned_part_factor(path, n_atoms, n_mol);
     L.cap = cap;
     // Morton code spaces of the cell grids: under 8 x max(n_atoms, 27) per structure
     L.ncell_cap = 8LL * ((int64_t)n_atoms + 27LL * n_mol);
@@ -90,7 +128,7 @@ WsLayout ws_layout(const mlff_dims& d, int32_t n_atoms, int32_t n_mol, int64_t c
     L.cell_fill = take(4 * L.ncell_cap);
     L.cell_pos = take(sizeof(float4) * N);
     L.atom_cell = take(4 * N);
-    L.part = take(4 * (L.P + 1));
+    L.part = take(4 * (P_max + 1));
     L.X = take(fs * (Ly + 1) * N * 4 * H);
     L.Xt = take(fs * Ly * N * 4 * H);
     L.uz = take(fs * Ly * N * H);
@@ -105,9 +143,9 @@ WsLayout ws_layout(const mlff_dims& d, int32_t n_atoms, int32_t n_mol, int64_t c
         // at most cap / tile + one partial tile per tiled range: forward
         // tiles of 128 edges (16 KB) over ranges of two partitions, reverse
         // tiles of 32 edges (8 KB) per partition
-        L.n_etile_f = cap / 128 + L.P / 2 + 2;
-        L.n_etile_b = cap / 32 + L.P + 1;
-        L.etile_base = take(4 * 2 * ((size_t)L.P + 1));
+        L.n_etile_f = cap / 128 + P_max / 2 + 2;
+        L.n_etile_b = cap / 32 + P_max + 1;
+        L.etile_base = take(4 * 2 * ((size_t)P_max + 1));
         L.etile_f = take((size_t)L.n_etile_f * 16384);
         L.etile_b = take((size_t)L.n_etile_b * 8192);
     }
@@ -302,6 +340,87 @@ int mlff_energy_forces(const mlff_dims* dims, const void* packed, const mlff_sys
 }
 
 // One integrator for both entry points: Verlet (langevin false) or BAOAB.
+int mlff_autotune(const mlff_dims* dims, const void* packed, const mlff_system* sys, int64_t edge_capacity,
+                  int32_t path, const mlff_outputs* out, void* workspace, size_t workspace_bytes, mlff_stream_t stream,
+                  int32_t repeats, int32_t* chosen, double* ms_per_candidate) {
+    if (path != MLFF_PATH_TUNED_TC) {
+        if (chosen) *chosen = 1;
+        return MLFF_OK;   // the other paths have no tunable shape
+    }
+    if (repeats < 1 || repeats > 1000) { set_error("repeats %d outside 1..1000", repeats); return MLFF_ERR_INVALID; }
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    MLFF_CUDA(cudaEventCreate(&e0));
+    cudaError_t ce = cudaEventCreate(&e1);
+    if (ce != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return cuda_status(ce, "cudaEventCreate");
+    }
+    int best = 1, r = MLFF_OK;
+    float best_ms = 0.f;
+    for (int i = 0; i < 3 && r == MLFF_OK; ++i) {
+        g_tune_override = TUNE_FACTORS[i];
+        r = mlff_energy_forces(dims, packed, sys, edge_capacity, path, out, workspace, workspace_bytes, stream);
+        if (r == MLFF_OK && (ce = cudaEventRecord(e0, st)) != cudaSuccess) r = cuda_status(ce, "cudaEventRecord");
+        for (int k = 0; k < repeats && r == MLFF_OK; ++k)
+            r = mlff_energy_forces(dims, packed, sys, edge_capacity, path, out, workspace, workspace_bytes, stream);
+        float ms = 0.f;
+        if (r == MLFF_OK && (ce = cudaEventRecord(e1, st)) != cudaSuccess) r = cuda_status(ce, "cudaEventRecord");
+        if (r == MLFF_OK && (ce = cudaEventSynchronize(e1)) != cudaSuccess) r = cuda_status(ce, "cudaEventSynchronize");
+        if (r == MLFF_OK && (ce = cudaEventElapsedTime(&ms, e0, e1)) != cudaSuccess) r = cuda_status(ce, "cudaEventElapsedTime");
+        if (r == MLFF_OK) {
+            ms /= repeats;
+            if (ms_per_candidate) ms_per_candidate[i] = ms;
+            if (i == 0 || ms < best_ms) {
+                best_ms = ms;
+                best = TUNE_FACTORS[i];
+            }
+        }
+    }
+    g_tune_override = 0;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (r) return r;
+    // a device error (capacity, box, ...) in the timed calls makes the timings meaningless
+    Status s{};
+    MLFF_CUDA(cudaMemcpyAsync(&s, workspace, sizeof(Status), cudaMemcpyDeviceToHost, st));
+    MLFF_CUDA(cudaStreamSynchronize(st));
+    if (s.code != MLFF_OK) {
+        set_error("device status %d during autotuning: nothing cached", s.code);
+        return s.code;
+    }
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune[tune_key(path, sys->n_atoms, sys->n_mol)] = best;
+    }
+    if (chosen) *chosen = best;
+    return MLFF_OK;
+}
+
+int mlff_autotune_query(int32_t path, int32_t n_atoms, int32_t n_mol, int32_t* factor) {
+    if (!factor) { set_error("factor is required"); return MLFF_ERR_INVALID; }
+    *factor = tuned_part_factor(path, n_atoms, n_mol);
+    return MLFF_OK;
+}
+
+int mlff_autotune_set(int32_t path, int32_t n_atoms, int32_t n_mol, int32_t factor) {
+    if (factor != 0 && factor != 1 && factor != 2 && factor != 4) {
+        set_error("partition factor %d: use 1, 2 or 4 (0 removes the entry)", factor);
+        return MLFF_ERR_INVALID;
+    }
+    if (path != MLFF_PATH_TUNED_TC) { set_error("only the tensor-core path has a tunable shape"); return MLFF_ERR_INVALID; }
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    if (factor == 0) g_tune.erase(tune_key(path, n_atoms, n_mol));
+    else g_tune[tune_key(path, n_atoms, n_mol)] = factor;
+    return MLFF_OK;
+}
+
+int mlff_autotune_reset(void) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune.clear();
+    return MLFF_OK;
+}
+
 // One integrator for three entry points: scheme 0 velocity Verlet, 1 BAOAB
 // Langevin, 2 ASE's Langevin (Vanden-Eijnden-Ciccotti; fix_com as ASE's fixcm).
 enum { MD_VERLET = 0, MD_BAOAB = 1, MD_VEC = 2 };

@@ -576,8 +576,10 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
             fence_before_sync();
             __syncthreads();
             fence_after_sync();
-            {   // epilogue 1: h = silu(z + b1) -> H tile (split fp16), 32 edges per warp
-                const int k = c, col = 32 * r;
+            {   // epilogue 1: h = silu(z + b1) -> H tile (split fp16), 32 edges per warp.
+                // Padding edges of a partial tile get h = 0 and a zero bias fill, so
+                // their filter is exactly 0 and epilogue 2 gathers without predicates.
+                const int k = c, col = 32 * r, nv = n - col;
                 const float bias = b1s[k];
                 float z[32];
                 tmem_ld32(lane_base + TM_F + col, z);
@@ -586,21 +588,27 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
 #pragma unroll
                 for (int i = 0; i < 32; i += 2) {
                     const float z0 = z[i] + bias, z1 = z[i + 1] + bias;
-                    hc.put_pair(i, z0 * fast_sigmoid(z0), z1 * fast_sigmoid(z1));
+                    hc.put_pair(i, i < nv ? z0 * fast_sigmoid(z0) : 0.f, i + 1 < nv ? z1 * fast_sigmoid(z1) : 0.f);
                 }
                 // GEMM2 accumulates onto b2[g * 128 + channel]: this warp refills
                 // the 32 chunk-0 cells it has just read, and 64 columns of
-                // chunks 1 and 2 (warps r = 0, 1: chunk 1; r = 2, 3: chunk 2)
+                // chunks 1 and 2 (warps r = 0, 1: chunk 1; r = 2, 3: chunk 2; the
+                // columns of edges 64 (r & 1) .. 64 (r & 1) + 63)
                 float bv[16];
                 const float b0c = b2s[c], b12 = b2s[(1 + (r >> 1)) * H + c];
 #pragma unroll
-                for (int i = 0; i < 16; ++i) bv[i] = b0c;
+                for (int i = 0; i < 16; ++i) bv[i] = i < nv ? b0c : 0.f;
                 tmem_st16(lane_base + TM_F + col, bv);
+#pragma unroll
+                for (int i = 0; i < 16; ++i) bv[i] = 16 + i < nv ? b0c : 0.f;
                 tmem_st16(lane_base + TM_F + col + 16, bv);
 #pragma unroll
-                for (int i = 0; i < 16; ++i) bv[i] = b12;
+                for (int kk = 0; kk < 4; ++kk) {
+                    const int e0 = 64 * (r & 1) + 16 * kk;
 #pragma unroll
-                for (int kk = 0; kk < 4; ++kk) tmem_st16(lane_base + TM_F + 128 + 64 * r + 16 * kk, bv);
+                    for (int i = 0; i < 16; ++i) bv[i] = e0 + i < n ? b12 : 0.f;
+                    tmem_st16(lane_base + TM_F + 128 + 64 * r + 16 * kk, bv);
+                }
                 tmem_st_wait();
             }
             fence_async_smem();
@@ -609,14 +617,16 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
             // epilogue 2's first two 16-edge blocks of sender features are
             // gathered while GEMM2 runs
             float xa[16], xn[16];
+            // (padding edges read row 0; their filter is 0)
+            const float* xin_f = a.X + fidx;
             auto gather16 = [&](float (&x)[16], int col) {
 #pragma unroll
                 for (int i = 0; i < 16; i += 4) {
                     const int4 so = *reinterpret_cast<const int4*>(soff + col + i);
-                    x[i] = col + i < n ? __ldg(a.X + so.x + fidx) : 0.f;
-                    x[i + 1] = col + i + 1 < n ? __ldg(a.X + so.y + fidx) : 0.f;
-                    x[i + 2] = col + i + 2 < n ? __ldg(a.X + so.z + fidx) : 0.f;
-                    x[i + 3] = col + i + 3 < n ? __ldg(a.X + so.w + fidx) : 0.f;
+                    x[i] = __ldg(xin_f + so.x);
+                    x[i + 1] = __ldg(xin_f + so.y);
+                    x[i + 2] = __ldg(xin_f + so.z);
+                    x[i + 3] = __ldg(xin_f + so.w);
                 }
             };
             gather16(xa, 0);
@@ -1171,8 +1181,11 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
             }
             fence_before_sync();
             pipe_sync(pp);
-            if (tp < n) {   // per-edge sums over the pipeline's 8 warps, fixed order
-                const float* rr = red + tp * 3;
+            // per-edge sums over the pipeline's 8 warps, fixed order, by its last
+            // warp (warp 0 issues the next tile's GEMM1 meanwhile)
+            const int te = tp - (PT - 32);
+            if (te >= 0 && te < n) {
+                const float* rr = red + te * 3;
                 float dd = 0.f, du0 = 0.f, du1 = 0.f, du2 = 0.f;
 #pragma unroll
                 for (int ww = 0; ww < 8; ++ww) {
@@ -1185,12 +1198,12 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                     }
                 }
                 float4 ea = a.eacc_init ? make_float4(0.f, 0.f, 0.f, 0.f)
-                                        : reinterpret_cast<const float4*>(sb + R_SB_EACC)[tp];
+                                        : reinterpret_cast<const float4*>(sb + R_SB_EACC)[te];
                 ea.x += dd;
                 ea.y += du0;
                 ea.z += du1;
                 ea.w += du2;
-                a.eacc[t0 + tp] = ea;
+                a.eacc[t0 + te] = ea;
             }
             if (abort_now) {
                 aborted = true;

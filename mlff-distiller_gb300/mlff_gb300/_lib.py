@@ -48,7 +48,8 @@ EXPORTS = ["mlff_version", "mlff_last_error_string", "mlff_packed_weights_size",
            "mlff_profile_end", "mlff_radius_graph_noalloc", "mlff_param_grads", "mlff_param_grads_forces",
            "mlff_debug_stall_test", "mlff_painn_message_workspace_size", "mlff_painn_message",
            "mlff_painn_message_backward", "mlff_painn_update_workspace_size", "mlff_painn_update",
-           "mlff_painn_update_backward", "mlff_force_stats_workspace_size", "mlff_force_stats"]
+           "mlff_painn_update_backward", "mlff_force_stats_workspace_size", "mlff_force_stats",
+           "mlff_autotune", "mlff_autotune_query", "mlff_autotune_set", "mlff_autotune_reset"]
 
 PROFILE_KINDS = ["neighbors", "edge_fwd", "edge_bwd", "update_fwd", "update_bwd", "readout", "forces",
                  "plain_gemm", "plain_edge", "other", "md"]
@@ -185,6 +186,16 @@ def load(build_if_missing: bool = True):
         lib.mlff_painn_update.argtypes = [i32, i32] + [_P] * 10 + [sz, _P]
         lib.mlff_painn_update_backward.restype = ctypes.c_int
         lib.mlff_painn_update_backward.argtypes = [i32, i32] + [_P] * 17 + [sz, _P]
+        lib.mlff_autotune.restype = ctypes.c_int
+        lib.mlff_autotune.argtypes = [ctypes.POINTER(Dims), _P, ctypes.POINTER(System), i64, i32,
+                                      ctypes.POINTER(Outputs), _P, sz, _P, i32, ctypes.POINTER(i32),
+                                      ctypes.POINTER(ctypes.c_double)]
+        lib.mlff_autotune_query.restype = ctypes.c_int
+        lib.mlff_autotune_query.argtypes = [i32, i32, i32, ctypes.POINTER(i32)]
+        lib.mlff_autotune_set.restype = ctypes.c_int
+        lib.mlff_autotune_set.argtypes = [i32, i32, i32, i32]
+        lib.mlff_autotune_reset.restype = ctypes.c_int
+        lib.mlff_autotune_reset.argtypes = []
         lib.mlff_force_stats_workspace_size.restype = sz
         lib.mlff_force_stats_workspace_size.argtypes = []
         lib.mlff_force_stats.restype = ctypes.c_int

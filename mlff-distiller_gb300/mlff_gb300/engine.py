@@ -27,6 +27,12 @@ from . import _lib
 
 DEFAULT_EDGES_PER_ATOM = 64
 GRAPH_CACHE_SIZE = 4
+AUTOTUNE_REPEATS = 3
+_tuned_buckets = set()   # (path, ceil log2 atoms, ceil log2 structures) tuned in this process
+
+
+def _bucket(path: int, n_atoms: int, n_mol: int):
+    return (path, max(n_atoms - 1, 0).bit_length(), max(n_mol - 1, 0).bit_length())
 
 
 def _stream_handle() -> int:
@@ -100,6 +106,7 @@ class Engine:
         self.edge_capacity: Dict[int, int] = {}
         self._param_version = None
         self.use_graphs = True          # replay cached CUDA graphs for repeated shapes
+        self.auto_tune = True           # tune the tensor-core path's partition factor once per size bucket
         self._graphs: Dict[tuple, dict] = {}
 
     # -------------------------------------------------------------- weights
@@ -228,6 +235,10 @@ class Engine:
             del self._graphs[key]
             ent = None
         if ent is None:
+            if self.auto_tune and path == _lib.PATH_TUNED_TC and _bucket(path, N, B) not in _tuned_buckets:
+                db = batch if not to_host else Batch(batch.Z.to(self.device), batch.pos.to(self.device),
+                                                     batch.mol_ptr, batch.box, batch.pbc)
+                self.autotune(db, path)
             if to_host:
                 dev = self.device
                 db = Batch(batch.Z.to(dev), batch.pos.to(dev), batch.mol_ptr, batch.box, batch.pbc)
@@ -300,6 +311,30 @@ class Engine:
             self._graphs.pop(next(iter(self._graphs)))
         self._graphs[key] = {"graph": g, "batch": st, "out": out, "cap": cap, "ws": self.workspace.data_ptr(),
                              "src": {"mol_ptr": batch.mol_ptr, "box": batch.box, "pbc": batch.pbc}}
+
+    def autotune(self, batch: Batch, path: int = _lib.PATH_TUNED_TC, repeats: int = AUTOTUNE_REPEATS) -> dict:
+        """Choose the partition factor of this batch's size bucket
+        (mlff_autotune: a few timed calls per candidate, then cached by the
+        library for every call of the bucket).  Returns the choice and the
+        milliseconds per call of each candidate.  Synchronises the stream;
+        not for use during stream capture."""
+        self.energy_forces(batch, path, graph=False)       # sizes the edge capacity and workspace
+        N, B = batch.n_atoms, batch.n_mol
+        cap = self.capacity(N, path)
+        ws = self.workspace_for(N, B, cap, path)
+        E = torch.empty(B, dtype=torch.float64, device=self.device)
+        F = torch.empty(N, 3, dtype=torch.float32, device=self.device)
+        out = _lib.Outputs()
+        out.energy, out.forces = E.data_ptr(), F.data_ptr()
+        chosen = ctypes.c_int32(1)
+        ms = (ctypes.c_double * 3)()
+        sysd = batch.system()
+        _lib.check(self.lib.mlff_autotune(ctypes.byref(self.dims), self.packed.data_ptr(), ctypes.byref(sysd), cap,
+                                          path, ctypes.byref(out), ws.data_ptr(), ws.numel(), _stream_handle(),
+                                          int(repeats), ctypes.byref(chosen), ms))
+        _tuned_buckets.add(_bucket(path, N, B))
+        return {"partition_factor": int(chosen.value),
+                "ms_per_call": {f: round(ms[i], 4) for i, f in enumerate((1, 2, 4))}}
 
     def capture(self, batch: Batch, path: int = _lib.PATH_TUNED_TC, forces: bool = True):
         """One energy_forces call captured in a CUDA graph, for repeated

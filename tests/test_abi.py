@@ -169,3 +169,34 @@ def test_npt_arguments_checked_on_host():
     assert call(ctypes.byref(npt), fake.value, 0.0, 2.5, 1.0) == _lib.ERR_INVALID
     assert call(ctypes.byref(npt), fake.value, 0.025, 2.5, -1.0) == _lib.ERR_INVALID
     assert b"pfactor" in lib.mlff_last_error_string()
+
+
+def test_autotune_cache_on_host():
+    """The partition-factor cache: per (path, ceil log2 atoms, ceil log2
+    structures) bucket, pinned with _set, read with _query, emptied with
+    _reset; the workspace size does not depend on it."""
+    import ctypes
+    from mlff_gb300 import _lib
+    from mlff_gb300.engine import dims_of
+    lib = _lib.load()
+    tc = _lib.PATH_TUNED_TC
+    f = ctypes.c_int32()
+    assert lib.mlff_autotune_reset() == _lib.OK
+    d = dims_of(128, 20, 3, 119, 5.0)
+    ws0 = lib.mlff_workspace_size(ctypes.byref(d), 9000, 200, 500_000, tc)
+    assert lib.mlff_autotune_query(tc, 9000, 200, ctypes.byref(f)) == _lib.OK and f.value == 1
+    assert lib.mlff_autotune_set(tc, 9000, 200, 4) == _lib.OK
+    for n_atoms, n_mol, want in ((9000, 200, 4), (16384, 256, 4), (8193, 129, 4),   # same bucket (14, 8)
+                                 (16385, 200, 1), (8192, 200, 1), (9000, 257, 1)):   # neighbouring buckets
+        assert lib.mlff_autotune_query(tc, n_atoms, n_mol, ctypes.byref(f)) == _lib.OK
+        assert f.value == want, (n_atoms, n_mol, f.value)
+    assert lib.mlff_workspace_size(ctypes.byref(d), 9000, 200, 500_000, tc) == ws0
+    # other paths have nothing to tune
+    assert lib.mlff_autotune_query(_lib.PATH_PLAIN_FP32, 9000, 200, ctypes.byref(f)) == _lib.OK and f.value == 1
+    assert lib.mlff_autotune_set(_lib.PATH_PLAIN_FP32, 9000, 200, 2) == _lib.ERR_INVALID
+    assert lib.mlff_autotune_set(tc, 9000, 200, 3) == _lib.ERR_INVALID
+    assert lib.mlff_autotune_set(tc, 9000, 200, 0) == _lib.OK
+    assert lib.mlff_autotune_query(tc, 9000, 200, ctypes.byref(f)) == _lib.OK and f.value == 1
+    lib.mlff_autotune_set(tc, 9000, 200, 2)
+    assert lib.mlff_autotune_reset() == _lib.OK
+    assert lib.mlff_autotune_query(tc, 9000, 200, ctypes.byref(f)) == _lib.OK and f.value == 1
