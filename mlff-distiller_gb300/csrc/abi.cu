@@ -143,10 +143,10 @@ WsLayout ws_layout(const mlff_dims& d, int32_t n_atoms, int32_t n_mol, int64_t c
         // at most cap / tile + one partial tile per tiled range: forward
         // tiles of 128 edges (16 KB) over ranges of two partitions, reverse
         // tiles of 32 edges (8 KB) per partition
-        L.n_etile_f = cap / 128 + P_max / 2 + 2;
-        L.n_etile_b = cap / 32 + P_max + 1;
+        L.n_etile_f = cap / 64 + P_max + 1;   // sum over partitions of ceil(E_p / 64)
+        L.n_etile_b = cap / 32 + P_max + 1;   // ceil(E_p / 32)
         L.etile_base = take(4 * 2 * ((size_t)P_max + 1));
-        L.etile_f = take((size_t)L.n_etile_f * 16384);
+        L.etile_f = take((size_t)L.n_etile_f * 8192);
         L.etile_b = take((size_t)L.n_etile_b * 8192);
     }
     if (path == MLFF_PATH_PLAIN_FP32 || path == MLFF_PATH_TRAIN || dual) {

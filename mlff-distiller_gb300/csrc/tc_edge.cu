@@ -54,12 +54,9 @@ constexpr uint32_t W2_HALF = W2_TILES * A_TILE;   // all hi tiles (96 KB), then 
 constexpr uint32_t W2L_BYTES = 8 * A_TILE;    // lo tiles of W2 chunk 2 (resident in shared memory)
 
 // TMEM columns (512 allocated): [0,128) the lo halves of W2 chunks 0 and 1
-// as MMA A operands (chunk g, K-step s at 64 g + 8 s); [128,512) the GEMM2
-// accumulators (forward: chunk g at 128 + 128 g, GEMM1 writes z into chunk
-// 0's columns, which epilogue 1 reads before it refills them with the bias;
-// reverse: see the reverse kernel).
+// as MMA A operands (chunk g, K-step s at 64 g + 8 s); [128,512) two
+// pipelines' GEMM accumulators, 192 columns each (see the kernels).
 constexpr uint32_t TM_W2LO = 0;
-constexpr uint32_t TM_F = 128;
 
 // ------------------------------------------------------------- packing
 // W1 [H][RMAX] -> 2 K-step blocks (hi, lo); W2 [3H][H] -> 24 hi tiles
@@ -119,9 +116,6 @@ constexpr int NT = 512;                        // threads per CTA (16 warps)
 constexpr long long STALL_BUDGET = 1LL << 16;
 constexpr int WHERE_STALL_TEST = 99;
 
-// Barrier 1 over the first n threads (whole warps) of the CTA.
-__device__ __forceinline__ void bar_sync_first(int n) { asm volatile("bar.sync 1, %0;" ::"r"(n) : "memory"); }
-
 __device__ __forceinline__ void signal_timeout(const EdgeArgs& a, volatile int* abort_flag, int where) {
     set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, where);
     *abort_flag = 1;
@@ -177,23 +171,20 @@ __device__ __forceinline__ void rbf16_d(float d, bool valid, int r0, int R, cons
 // no-swizzle layout (16-byte core matrices: K-step s at rows * 32 s, its
 // second 8 columns rows * 16 further, 8-row groups 128 apart; the hi image,
 // then the lo image rows * 64 further), computed once per call for all
-// layers.  Forward tiles: 128 edges, one row each, over receiver ranges of
-// two partitions (the forward kernel walks a CTA's two partitions as one
-// range).  Reverse tiles: 32 edges, rows 0-31 the RBF rows and rows 32-63
-// their d-derivatives, per partition.  Tile k of a range is the k-th tile
-// its kernel processes.
-constexpr uint32_t ET_BYTES = 16384, ET_HALF = 8192;     // forward: 128 rows
-constexpr uint32_t ETR_BYTES = 8192, ETR_HALF = 4096;    // reverse: 64 rows
-constexpr int FWD_GROUP = 2;                              // partitions per forward range
+// layers, 64 rows per tile: forward tiles of 64 edges, reverse tiles of 32
+// edges with rows 0-31 the RBF rows and rows 32-63 their d-derivatives.
+// Tiles follow the receiver partitions: tile k of partition p is the k-th
+// tile the pipeline that owns p processes.
+constexpr uint32_t ET_ROWS = 64;
+constexpr uint32_t ET_BYTES = ET_ROWS * 128, ET_HALF = ET_ROWS * 64;   // 8 KB, hi then lo
 __device__ __forceinline__ uint32_t et_off(int rows, int row, int k) {
     return (uint32_t)((k >> 4) * rows * 32 + ((k >> 3) & 1) * rows * 16 + (row >> 3) * 128 + (row & 7) * 16 +
                       (k & 7) * 2);
 }
-__host__ __device__ constexpr int fwd_ranges(int nparts) { return (nparts + FWD_GROUP - 1) / FWD_GROUP; }
 
-// Tile counts of all forward ranges and reverse partitions, then exclusive
-// scans (one block, 1024 at a time): forward bases at base[0..R], reverse
-// bases at base[P+1 .. 2P+1].
+// Tile counts of all partitions (forward: 64 edges per tile, reverse: 32),
+// then exclusive scans (one block, 1024 partitions at a time): forward bases
+// at base[0..P], reverse bases at base[P+1 .. 2P+1].
 __global__ void __launch_bounds__(1024) etile_index_kernel(const int32_t* __restrict__ row_ptr,
                                                            const int32_t* __restrict__ part, int P,
                                                            int32_t* __restrict__ base) {
@@ -202,18 +193,14 @@ __global__ void __launch_bounds__(1024) etile_index_kernel(const int32_t* __rest
     __shared__ int cf[1024], cb[1024];
     __shared__ int carry[2];
     const int t = threadIdx.x;
-    const int R = fwd_ranges(P);
     if (t == 0) carry[0] = carry[1] = 0;
     __syncthreads();
     for (int p0 = 0; p0 < P; p0 += 1024) {
         const int p = p0 + t;
         int nf = 0, nb = 0;
-        if (p < R) {
-            const int E = row_ptr[part[min(FWD_GROUP * p + FWD_GROUP, P)]] - row_ptr[part[FWD_GROUP * p]];
-            nf = (E + 127) / 128;
-        }
         if (p < P) {
             const int E = row_ptr[part[p + 1]] - row_ptr[part[p]];
+            nf = (E + 63) / 64;
             nb = (E + 31) / 32;
         }
         cf[t] = nf;
@@ -226,8 +213,10 @@ __global__ void __launch_bounds__(1024) etile_index_kernel(const int32_t* __rest
             cb[t] += xb;
             __syncthreads();
         }
-        if (p < R) base[p] = carry[0] + cf[t] - nf;
-        if (p < P) base[P + 1 + p] = carry[1] + cb[t] - nb;
+        if (p < P) {
+            base[p] = carry[0] + cf[t] - nf;
+            base[P + 1 + p] = carry[1] + cb[t] - nb;
+        }
         __syncthreads();
         if (t == 1023) {
             carry[0] += cf[1023];
@@ -236,7 +225,7 @@ __global__ void __launch_bounds__(1024) etile_index_kernel(const int32_t* __rest
         __syncthreads();
     }
     if (t == 0) {
-        base[R] = carry[0];
+        base[P] = carry[0];
         base[2 * P + 1] = carry[1];
     }
 }
@@ -253,18 +242,15 @@ __global__ void __launch_bounds__(256) etile_fill_kernel(EdgeArgs a, const int32
     }
     __syncthreads();
     if (a.st->code != 0) return;
-    constexpr int TE = REV ? 32 : 128;                  // edges per tile
-    constexpr int ROWS = REV ? 64 : 128;                // rows per tile
-    constexpr uint32_t BYTES = ROWS * 128, HALF = ROWS * 64;
+    constexpr int TE = REV ? 32 : 64;                   // edges per tile
+    constexpr int ROWS = ET_ROWS;
     constexpr int PER = 2 * ROWS;                       // threads per tile: (row, K-step)
     constexpr int TPI = 256 / PER;                      // tiles per block iteration
     const int t = threadIdx.x, sub = t / PER, loc = t % PER;
     const int row = loc % ROWS, s = loc / ROWS;
     const int which = REV ? (row >> 5) : 0, erow = REV ? (row & 31) : row;
-    const int nr = REV ? a.nparts : fwd_ranges(a.nparts);
-    for (int p = blockIdx.x; p < nr; p += gridDim.x) {
-        const int g0 = REV ? p : FWD_GROUP * p, g1 = REV ? p + 1 : min(FWD_GROUP * p + FWD_GROUP, a.nparts);
-        const int e0 = a.row_ptr[a.part[g0]], e1 = a.row_ptr[a.part[g1]];
+    for (int p = blockIdx.x; p < a.nparts; p += gridDim.x) {
+        const int e0 = a.row_ptr[a.part[p]], e1 = a.row_ptr[a.part[p + 1]];
         const int b0 = base[(REV ? a.nparts + 1 : 0) + p];
         for (int k = blockIdx.y * TPI + sub; e0 + k * TE < e1; k += gridDim.y * TPI) {
             const int e = e0 + k * TE + erow;
@@ -277,11 +263,12 @@ __global__ void __launch_bounds__(256) etile_fill_kernel(EdgeArgs a, const int32
             __align__(16) __half2 lo[8];
 #pragma unroll
             for (int i = 0; i < 8; ++i) split2(v[2 * i], v[2 * i + 1], hi[i], lo[i]);
-            unsigned char* tile = out + (size_t)(b0 + k) * BYTES;
+            unsigned char* tile = out + (size_t)(b0 + k) * ET_BYTES;
             *reinterpret_cast<uint4*>(tile + et_off(ROWS, row, 16 * s)) = *reinterpret_cast<const uint4*>(&hi[0]);
             *reinterpret_cast<uint4*>(tile + et_off(ROWS, row, 16 * s + 8)) = *reinterpret_cast<const uint4*>(&hi[4]);
-            *reinterpret_cast<uint4*>(tile + HALF + et_off(ROWS, row, 16 * s)) = *reinterpret_cast<const uint4*>(&lo[0]);
-            *reinterpret_cast<uint4*>(tile + HALF + et_off(ROWS, row, 16 * s + 8)) =
+            *reinterpret_cast<uint4*>(tile + ET_HALF + et_off(ROWS, row, 16 * s)) =
+                *reinterpret_cast<const uint4*>(&lo[0]);
+            *reinterpret_cast<uint4*>(tile + ET_HALF + et_off(ROWS, row, 16 * s + 8)) =
                 *reinterpret_cast<const uint4*>(&lo[4]);
         }
     }
@@ -289,9 +276,8 @@ __global__ void __launch_bounds__(256) etile_fill_kernel(EdgeArgs a, const int32
 
 int launch_etiles(const EdgeArgs& a, int32_t* base, unsigned char* fwd, unsigned char* rev, cudaStream_t st) {
     MLFF_LAUNCH_PDL("etile_index", etile_index_kernel, 1, 1024, 0, st, a.row_ptr, a.part, a.nparts, base);
-    // tiles of a range spread over gridDim.y blocks
-    MLFF_LAUNCH_PDL("etile_fill_fwd", etile_fill_kernel<false>, dim3(fwd_ranges(a.nparts), 16), 256, 0, st, a, base,
-                    fwd);
+    // tiles of a partition spread over gridDim.y blocks
+    MLFF_LAUNCH_PDL("etile_fill_fwd", etile_fill_kernel<false>, dim3(a.nparts, 16), 256, 0, st, a, base, fwd);
     if (rev) {
         MLFF_LAUNCH_PDL("etile_fill_rev", etile_fill_kernel<true>, dim3(a.nparts, 16), 256, 0, st, a, base, rev);
     }
@@ -378,7 +364,6 @@ __device__ __forceinline__ int reduce_scatter8_index(int lane) {
 // parallel: a thread issues about one MMA per 50 cycles and stalls while the
 // tensor core is busy, so one issuer adds its own latency to every MMA; each
 // chunk keeps a fixed accumulation order.
-constexpr uint32_t HALF128 = 2 * b_block(128);   // K = 128: two K-blocks
 template <int NR>
 __device__ __forceinline__ void issue_gemm2_chunk(int g, uint32_t tmem, uint32_t dcol, const unsigned char* w2h,
                                                   const unsigned char* w2l, const unsigned char* Hs) {
@@ -409,58 +394,84 @@ __device__ __forceinline__ void zero_empty_rows(float* out, const int32_t* row_p
             for (int k = lane; k < 4 * H; k += 32) out[(int64_t)j * 4 * H + k] = 0.0f;
 }
 __device__ __forceinline__ void copy_empty_rows(float* out, const float* base, const int32_t* row_ptr, int j0, int j1,
-                                                int w, int lane) {
-    for (int j = j0 + w; j < j1; j += NT / 32)
+                                                int w, int lane, int nwarps = NT / 32) {
+    for (int j = j0 + w; j < j1; j += nwarps)
         if (row_ptr[j] == row_ptr[j + 1])
             for (int k = lane; k < 4 * H; k += 32) out[(int64_t)j * 4 * H + k] = base[(int64_t)j * 4 * H + k];
 }
 
-// ------------------------------------------------------- forward kernel
-constexpr int FN = 128;                                   // edges per tile
-constexpr uint32_t F_HH = 2 * b_block(FN);                // H tile, one half (K = 128)
-static_assert(F_HH == HALF128, "GEMM2 B layout");
-constexpr uint32_t F_OFF_W1 = 0;
-constexpr uint32_t F_OFF_W2H = F_OFF_W1 + W1_BYTES;
-constexpr uint32_t F_OFF_H = align1k(F_OFF_W2H + W2_HALF);     // H tile; the E tile shares its start
-constexpr uint32_t F_OFF_W2L = align1k(F_OFF_H + 2 * F_HH);
-// per-tile edge arrays, two buffers: (u, d), sender, receiver, sender row
-// offset, u components, receiver-change bits
-constexpr uint32_t F_SB_US = 0;
-constexpr uint32_t F_SB_SRC = F_SB_US + FN * 16;
-constexpr uint32_t F_SB_RCV = F_SB_SRC + FN * 4;
-constexpr uint32_t F_SB_SOFF = F_SB_RCV + FN * 4;
-constexpr uint32_t F_SB_UC = F_SB_SOFF + FN * 4;
-constexpr uint32_t F_SB_CHG = F_SB_UC + 3 * FN * 4;
-constexpr uint32_t F_SB_BYTES = F_SB_CHG + (FN / 32) * 4;
-constexpr uint32_t F_OFF_SB = F_OFF_W2L + W2L_BYTES;
-constexpr uint32_t F_OFF_B1 = F_OFF_SB + 2 * F_SB_BYTES;
-constexpr uint32_t F_OFF_B2 = F_OFF_B1 + H * 4;
-constexpr uint32_t F_OFF_BAR = F_OFF_B2 + H3 * 4;
-constexpr uint32_t F_OFF_MISC = F_OFF_BAR + 8 * 5;
-constexpr uint32_t F_SMEM = align1k(F_OFF_MISC + 16);
-static_assert(ET_BYTES <= 2 * F_HH, "E tile fits in the H tile's space");
-static_assert(F_SMEM <= 232448, "forward kernel shared memory");
+// ------------------------------------------------ pipelines (both kernels)
+// Each kernel runs two independent pipelines per CTA, warps 0-7 and 8-15,
+// each on its own receiver partition (CTA b: partitions 2b and 2b + 1, then
+// 2b + 2G ...), so that one pipeline's MMAs, copies and barrier waits overlap
+// the other pipeline's CUDA-core epilogues.  A pipeline owns 192 TMEM
+// columns (three filter chunks of 64), an H tile, its barriers and a named
+// CTA barrier.
+constexpr int PT = 256;                              // threads per pipeline
+__device__ __forceinline__ void pipe_sync(int pp) {
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + pp), "r"(PT) : "memory");
+}
+// Pipeline barrier that also ORs v over the pipeline's threads: every thread
+// gets the same answer.
+__device__ __forceinline__ bool pipe_sync_or(int pp, bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.or.pred q, %2, %3, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(1 + pp), "r"(PT)
+        : "memory");
+    return r != 0;
+}
+// the first n threads (whole warps) of pipeline pp
+__device__ __forceinline__ void pipe_sync_first(int pp, int n) {
+    asm volatile("bar.sync %0, %1;" ::"r"(3 + pp), "r"(n) : "memory");
+}
 
-// 16 warps.  Epilogue roles: warp w reads TMEM lane quarter q = w % 4
-// (channels / hidden units 32q..32q+31); r = w / 4 selects the edge quarter
-// (epilogue 1) or the feature component s, v_x, v_y, v_z (epilogue 2).
+// ------------------------------------------------------- forward kernel
+// 64-edge tiles per pipeline: GEMM1 (z = W1 e, N = 64) into the columns of
+// the pipeline's chunk 0, epilogue 1 (h = silu(z + b1) into the H tile, bias
+// refills), GEMM2 (three 128 x 64 chunks), epilogue 2: warp (q, h) of the
+// pipeline reads TMEM lane quarter q (channels 32q..32q+31) and sums two
+// feature components of every edge per receiver in registers (h = 0 the
+// scalar and v_x, h = 1 v_y and v_z), Xt = X + messages written once per
+// receiver.  Padding edges of a partial tile get h = 0 and a zero bias fill:
+// their filter is exactly zero and every gather runs unpredicated.
+constexpr int QN = 64;                               // edges per forward tile
+constexpr uint32_t Q_HH = 2 * b_block(QN);           // one half (hi or lo) of the H tile: 16 KB
+constexpr uint32_t Q_SB_US = 0;
+constexpr uint32_t Q_SB_SRC = Q_SB_US + QN * 16;
+constexpr uint32_t Q_SB_RCV = Q_SB_SRC + QN * 4;
+constexpr uint32_t Q_SB_SOFF = Q_SB_RCV + QN * 4;
+constexpr uint32_t Q_SB_UC = Q_SB_SOFF + QN * 4;
+constexpr uint32_t Q_SB_CHG = Q_SB_UC + 3 * QN * 4;
+constexpr uint32_t Q_SB_BYTES = Q_SB_CHG + 16;
+constexpr uint32_t Q_OFF_W1 = 0;
+constexpr uint32_t Q_OFF_W2H = Q_OFF_W1 + W1_BYTES;
+constexpr uint32_t Q_OFF_H = align1k(Q_OFF_W2H + W2_HALF);   // pipeline p's H tile at + 2 Q_HH p
+constexpr uint32_t Q_OFF_W2L = align1k(Q_OFF_H + 4 * Q_HH);
+constexpr uint32_t Q_OFF_SB = Q_OFF_W2L + W2L_BYTES;        // [pipeline][buffer] edge arrays
+constexpr uint32_t Q_OFF_B1 = Q_OFF_SB + 4 * Q_SB_BYTES;
+constexpr uint32_t Q_OFF_B2 = Q_OFF_B1 + H * 4;
+constexpr uint32_t Q_OFF_BAR = Q_OFF_B2 + H3 * 4;
+constexpr uint32_t Q_OFF_MISC = Q_OFF_BAR + 8 * 8;
+constexpr uint32_t Q_SMEM = align1k(Q_OFF_MISC + 16);
+static_assert(ET_BYTES <= 2 * Q_HH, "E tile fits in the H tile's space");
+static_assert(Q_SB_BYTES % 16 == 0, "edge array alignment");
+static_assert(Q_SMEM <= 232448, "forward kernel shared memory");
+
 __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const unsigned char* __restrict__ w1g,
                                                             const unsigned char* __restrict__ w2g) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char* w1s = smem + F_OFF_W1;
-    unsigned char* w2h = smem + F_OFF_W2H;
-    unsigned char* Hs = smem + F_OFF_H;
-    unsigned char* Es = smem + F_OFF_H;            // E tile (bulk-copied) lives in the H tile's space
-    unsigned char* w2l = smem + F_OFF_W2L;        // resident lo tiles of W2 chunk 2
-    float* b1s = reinterpret_cast<float*>(smem + F_OFF_B1);
-    float* b2s = reinterpret_cast<float*>(smem + F_OFF_B2);
-    uint64_t* mma_bar = reinterpret_cast<uint64_t*>(smem + F_OFF_BAR);
-    uint64_t* w2h_bar = mma_bar + 1;
-    uint64_t* e_bar = mma_bar + 2;
-    uint64_t* g2_bar = mma_bar + 3;                 // GEMM2: one commit per chunk issuer
-    uint64_t* never_bar = mma_bar + 4;              // test hook: nothing arrives here
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + F_OFF_MISC);
-    volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + F_OFF_MISC + 4);
+    unsigned char* w1s = smem + Q_OFF_W1;
+    unsigned char* w2h = smem + Q_OFF_W2H;
+    unsigned char* w2l = smem + Q_OFF_W2L;        // resident lo tiles of W2 chunk 2
+    float* b1s = reinterpret_cast<float*>(smem + Q_OFF_B1);
+    float* b2s = reinterpret_cast<float*>(smem + Q_OFF_B2);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + Q_OFF_BAR);
+    uint64_t* w2h_bar = bars;                       // resident W2 operands
+    uint64_t* never_bar = bars + 1;                 // test hook: nothing arrives here
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + Q_OFF_MISC);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + Q_OFF_MISC + 4);
 
     // waits for the previous kernel at entry: reading the status word first
     // and returning early keeps the main loop's register allocation lean
@@ -472,11 +483,13 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
         tmem_relinquish();
     }
     if (t == 0) {
-        mbar_init(mma_bar, 1);
         mbar_init(w2h_bar, 1);
-        mbar_init(e_bar, 1);
-        mbar_init(g2_bar, 3);
         mbar_init(never_bar, 1);
+        for (int p = 0; p < 2; ++p) {
+            mbar_init(bars + 2 + 3 * p, 1);   // GEMM1
+            mbar_init(bars + 3 + 3 * p, 1);   // E tile
+            mbar_init(bars + 4 + 3 * p, 3);   // GEMM2: one commit per chunk issuer
+        }
         fence_mbar_init();
         *abort_flag = 0;
     }
@@ -489,265 +502,280 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
     __syncthreads();
     fence_after_sync();
     const uint32_t tmem = *tslot;
-
-    uint32_t mma_phase = 0, g2_phase = 0;   // GEMM1 / GEMM2 barrier phases
-    bool w2h_ready = false;                 // (GEMM2 issuers)
     if (t == 32) load_w2_resident(w2h, w2l, w2g, w2h_bar);
-
-    const int q = w & 3, r = w >> 2;
+    const int q = w & 3;
     const int c = 32 * q + lane;
-    const int fidx = r * H + c;                      // this thread's feature element in a [4][H] row
     const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
-    load_w2_lo_tmem(lane_base, reinterpret_cast<const uint32_t*>(a.P + a.lo.w2_tm), r, c);
+    load_w2_lo_tmem(lane_base, reinterpret_cast<const uint32_t*>(a.P + a.lo.w2_tm), w >> 2, c);
     tmem_st_wait();
     fence_before_sync();
     __syncthreads();
     fence_after_sync();
     pdl_trigger();   // after the TMEM allocation
 
+    // ---- this thread's pipeline
+    const int pp = w >> 3, wl = w & 7, tp = t & (PT - 1), hh = wl >> 2;
+    const uint32_t TB = 128 + 192 * pp;             // the pipeline's TMEM columns: chunk g at TB + 64 g
+    unsigned char* Hs = smem + Q_OFF_H + pp * 2 * Q_HH;   // H hi, then lo
+    unsigned char* Es = Hs;                         // E tile (bulk-copied) before H is written
+    uint64_t* mma_bar = bars + 2 + 3 * pp;
+    uint64_t* e_bar = bars + 3 + 3 * pp;
+    uint64_t* g2_bar = bars + 4 + 3 * pp;
+    unsigned char* sbase = smem + Q_OFF_SB + 2 * pp * Q_SB_BYTES;
+    // components 2 hh and 2 hh + 1; the second sits H floats after the first
+    const int fidx0 = 2 * hh * H + c;
+    const float* xx = a.X + fidx0;
+    float* out = a.Xt + fidx0;
+
+    uint32_t mma_phase = 0, g2_phase = 0;   // GEMM1 / GEMM2 barrier phases
+    uint32_t e_phase = 0, e_issued = 0;     // E-tile copies: barrier phase, copies issued (thread tp 64)
+    bool w2h_ready = false;                 // (GEMM2 issuers)
     bool aborted = false;
-    uint32_t e_phase = 0, e_issued = 0;   // E-tile copies: barrier phase, copies issued (thread 32)
-    // GEMM1: z^T = W1 e^T on the bulk-copied E tile, into chunk 0's columns
-    auto issue_gemm1 = [&]() {
-        if (!mbar_wait(e_bar, e_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 8);
-        fence_after_sync();
-        constexpr uint32_t idesc = idesc_f16(FN);
-#pragma unroll
-        for (int s = 0; s < 2; ++s)
-#pragma unroll
-            for (int pr = 0; pr < 3; ++pr) {
-                const uint32_t ahl = pr == 2 ? 1 : 0, bhl = pr == 1 ? 1 : 0;
-                const uint64_t ad = sdesc(smem_u32(w1s + s * SLAB + ahl * A_TILE), A_LBO, A_SBO);
-                const uint64_t bd = sdesc(smem_u32(Es + bhl * ET_HALF + s * 4096), 2048, 128);
-                mma_f16(tmem + TM_F, ad, bd, idesc, (s | pr) != 0);
-            }
-        mma_commit(mma_bar);
+    auto prep = [&](unsigned char* sbx, int nn, int prev) {
+        tile_prep<QN>(tp, nn, prev, reinterpret_cast<int*>(sbx + Q_SB_SRC), reinterpret_cast<int*>(sbx + Q_SB_RCV),
+                      reinterpret_cast<float4*>(sbx + Q_SB_US), reinterpret_cast<int*>(sbx + Q_SB_SOFF), nullptr,
+                      reinterpret_cast<float*>(sbx + Q_SB_UC), reinterpret_cast<uint32_t*>(sbx + Q_SB_CHG));
     };
-    bool g1_issued = false;   // GEMM1 of the current tile already issued (at the end of the previous tile)
-    // receiver ranges of FWD_GROUP consecutive partitions
-    for (int p = blockIdx.x; p < fwd_ranges(a.nparts) && !aborted; p += gridDim.x) {
-        const int j0 = a.part[FWD_GROUP * p], j1 = a.part[min(FWD_GROUP * p + FWD_GROUP, a.nparts)];
+    auto fetch = [&](unsigned char* sbx, int t0, int nn) {
+        fetch_tile_edges(a, tp, QN, t0, nn, reinterpret_cast<float4*>(sbx + Q_SB_US),
+                         reinterpret_cast<int*>(sbx + Q_SB_SRC), reinterpret_cast<int*>(sbx + Q_SB_RCV));
+    };
+    for (int p = 2 * blockIdx.x + pp; p < a.nparts && !aborted; p += 2 * gridDim.x) {
+        const int j0 = a.part[p], j1 = a.part[p + 1];
         if (j0 >= j1) continue;
         const int e0 = a.row_ptr[j0], e1 = a.row_ptr[j1];
-        const int ntl = (e1 - e0 + FN - 1) / FN;
+        const int ntl = (e1 - e0 + QN - 1) / QN;
         const unsigned char* etiles = a.etile + (size_t)a.etile_base[p] * ET_BYTES;
-        copy_empty_rows(a.Xt, a.X, a.row_ptr, j0, j1, w, lane);
+        copy_empty_rows(a.Xt, a.X, a.row_ptr, j0, j1, wl, lane, PT / 32);
         int cur = j0;
-        float acc = 0.f, accu = 0.f;   // x * phi and u * phi_v2 parts of the current receiver's sum
-        // X of the current receiver (the residual term of Xt), loaded when the
-        // receiver starts so that the load is long done when its sum is stored
-        float base = a.X[(int64_t)cur * 4 * H + fidx];
+        float acc0 = 0.f, acc1 = 0.f;   // message sums of the current receiver, two components
+        // X of the current receiver (the residual term of Xt)
+        float base0 = xx[(int64_t)cur * 4 * H], base1 = xx[(int64_t)cur * 4 * H + H];
         if (ntl > 0) {   // the partition's first tile: edge arrays and E tile
-            unsigned char* sb = smem + F_OFF_SB;
-            fetch_tile_edges(a, t, FN, e0, min(FN, e1 - e0), reinterpret_cast<float4*>(sb + F_SB_US),
-                             reinterpret_cast<int*>(sb + F_SB_SRC), reinterpret_cast<int*>(sb + F_SB_RCV));
-            if (t == 32) {
+            fetch(sbase, e0, min(QN, e1 - e0));
+            if (tp == QN) {
                 mbar_expect_tx(e_bar, ET_BYTES);
                 bulk_g2s(Es, etiles, ET_BYTES, e_bar);
                 ++e_issued;
             }
             cp_async_wait_all();
-            __syncthreads();
-            if (t < FN)
-                tile_prep<FN>(t, min(FN, e1 - e0), j0, reinterpret_cast<int*>(sb + F_SB_SRC),
-                              reinterpret_cast<int*>(sb + F_SB_RCV), reinterpret_cast<float4*>(sb + F_SB_US),
-                              reinterpret_cast<int*>(sb + F_SB_SOFF), nullptr, reinterpret_cast<float*>(sb + F_SB_UC),
-                              reinterpret_cast<uint32_t*>(sb + F_SB_CHG));
-            __syncthreads();
+            pipe_sync(pp);
+            if (tp < QN) prep(sbase, min(QN, e1 - e0), j0);
+            pipe_sync(pp);
         }
         for (int k = 0; k < ntl; ++k) {
-            const int t0 = e0 + k * FN, n = min(FN, e1 - t0), buf = k & 1;
-            unsigned char* sb = smem + F_OFF_SB + buf * F_SB_BYTES;
-            unsigned char* sbn = smem + F_OFF_SB + (buf ^ 1) * F_SB_BYTES;
-            const int* rcv_s = reinterpret_cast<const int*>(sb + F_SB_RCV);
-            const int* soff = reinterpret_cast<const int*>(sb + F_SB_SOFF);
-            const float* uc = reinterpret_cast<const float*>(sb + F_SB_UC);
-            const uint32_t* chg = reinterpret_cast<const uint32_t*>(sb + F_SB_CHG);
-            if (t == 0 && !g1_issued) issue_gemm1();
-            g1_issued = false;
+            const int t0 = e0 + k * QN, n = min(QN, e1 - t0), buf = k & 1;
+            unsigned char* sb = sbase + buf * Q_SB_BYTES;
+            unsigned char* sbn = sbase + (buf ^ 1) * Q_SB_BYTES;
+            const int* rcv_s = reinterpret_cast<const int*>(sb + Q_SB_RCV);
+            const int* soff = reinterpret_cast<const int*>(sb + Q_SB_SOFF);
+            const float* uc = reinterpret_cast<const float*>(sb + Q_SB_UC);
+            const uint32_t* chg = reinterpret_cast<const uint32_t*>(sb + Q_SB_CHG);
+            if (tp == 0) {   // z^T = W1 e^T on the bulk-copied tile, into chunk 0's columns
+                if (!mbar_wait(e_bar, e_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 8);
+                fence_after_sync();
+                constexpr uint32_t idesc = idesc_f16(QN);
+#pragma unroll
+                for (int s = 0; s < 2; ++s)
+#pragma unroll
+                    for (int pr = 0; pr < 3; ++pr) {
+                        const uint32_t ahl = pr == 2 ? 1 : 0, bhl = pr == 1 ? 1 : 0;
+                        const uint64_t ad = sdesc(smem_u32(w1s + s * SLAB + ahl * A_TILE), A_LBO, A_SBO);
+                        const uint64_t bd = sdesc(smem_u32(Es + bhl * ET_HALF + s * (ET_ROWS * 32)), ET_ROWS * 16, 128);
+                        mma_f16(tmem + TB, ad, bd, idesc, (s | pr) != 0);
+                    }
+                mma_commit(mma_bar);
+            }
             e_phase ^= 1;
-            if (w == 0) __syncwarp();
-            // only warp 0 polls the MMA barrier; the others wait at the CTA
-            // barrier instead of spinning on shared memory the MMAs read from
-            if (w == 0 && (a.stall_test & 1) && k == 0 && !mbar_wait(never_bar, 0, STALL_BUDGET))
-                signal_timeout(a, abort_flag, WHERE_STALL_TEST);
-            if (w == 0 && !mbar_wait(mma_bar, mma_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 1);
+            if (wl == 0) {
+                __syncwarp();
+                // one warp polls the MMA barrier; the others wait at the pipeline barrier
+                if ((a.stall_test & 1) && k == 0 && !mbar_wait(never_bar, 0, STALL_BUDGET))
+                    signal_timeout(a, abort_flag, WHERE_STALL_TEST);
+                if (!mbar_wait(mma_bar, mma_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 1);
+            }
             mma_phase ^= 1;
             fence_before_sync();
-            __syncthreads();
+            pipe_sync(pp);
             fence_after_sync();
-            {   // epilogue 1: h = silu(z + b1) -> H tile (split fp16), 32 edges per warp.
-                // Padding edges of a partial tile get h = 0 and a zero bias fill, so
-                // their filter is exactly 0 and epilogue 2 gathers without predicates.
-                const int k = c, col = 32 * r, nv = n - col;
-                const float bias = b1s[k];
+            {   // epilogue 1: h = silu(z + b1) -> H tile (split fp16); warp (q, hh) takes
+                // hidden unit c of edges 32 hh .. 32 hh + 31
+                const int col = 32 * hh, nv = n - col;
+                const float bias = b1s[c];
                 float z[32];
-                tmem_ld32(lane_base + TM_F + col, z);
+                tmem_ld32(lane_base + TB + col, z);
                 tmem_ld_wait();
-                const BColumn hc(Hs, F_HH, FN, col, k);
-#pragma unroll
-                for (int i = 0; i < 32; i += 2) {
-                    const float z0 = z[i] + bias, z1 = z[i + 1] + bias;
-                    hc.put_pair(i, i < nv ? z0 * fast_sigmoid(z0) : 0.f, i + 1 < nv ? z1 * fast_sigmoid(z1) : 0.f);
-                }
-                // GEMM2 accumulates onto b2[g * 128 + channel]: this warp refills
-                // the 32 chunk-0 cells it has just read, and 64 columns of
-                // chunks 1 and 2 (warps r = 0, 1: chunk 1; r = 2, 3: chunk 2; the
-                // columns of edges 64 (r & 1) .. 64 (r & 1) + 63)
+                const BColumn hc(Hs, Q_HH, QN, col, c);
+                // GEMM2 accumulates onto b2 (0 for padding edges): this warp refills the
+                // chunk-0 cells it has just read and all 64 columns of chunk 1 + hh
                 float bv[16];
-                const float b0c = b2s[c], b12 = b2s[(1 + (r >> 1)) * H + c];
+                const float b0c = b2s[c], bch = b2s[(1 + hh) * H + c];
+                if (n == QN) {   // a full tile (all but the last of a partition)
 #pragma unroll
-                for (int i = 0; i < 16; ++i) bv[i] = i < nv ? b0c : 0.f;
-                tmem_st16(lane_base + TM_F + col, bv);
+                    for (int i = 0; i < 32; i += 2) {
+                        const float z0 = z[i] + bias, z1 = z[i + 1] + bias;
+                        hc.put_pair(i, z0 * fast_sigmoid(z0), z1 * fast_sigmoid(z1));
+                    }
 #pragma unroll
-                for (int i = 0; i < 16; ++i) bv[i] = 16 + i < nv ? b0c : 0.f;
-                tmem_st16(lane_base + TM_F + col + 16, bv);
+                    for (int i = 0; i < 16; ++i) bv[i] = b0c;
+                    tmem_st16(lane_base + TB + col, bv);
+                    tmem_st16(lane_base + TB + col + 16, bv);
 #pragma unroll
-                for (int kk = 0; kk < 4; ++kk) {
-                    const int e0 = 64 * (r & 1) + 16 * kk;
+                    for (int i = 0; i < 16; ++i) bv[i] = bch;
 #pragma unroll
-                    for (int i = 0; i < 16; ++i) bv[i] = e0 + i < n ? b12 : 0.f;
-                    tmem_st16(lane_base + TM_F + 128 + 64 * r + 16 * kk, bv);
+                    for (int kk = 0; kk < 4; ++kk) tmem_st16(lane_base + TB + 64 * (1 + hh) + 16 * kk, bv);
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 32; i += 2) {
+                        const float z0 = z[i] + bias, z1 = z[i + 1] + bias;
+                        hc.put_pair(i, i < nv ? z0 * fast_sigmoid(z0) : 0.f, i + 1 < nv ? z1 * fast_sigmoid(z1) : 0.f);
+                    }
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) bv[i] = i < nv ? b0c : 0.f;
+                    tmem_st16(lane_base + TB + col, bv);
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) bv[i] = 16 + i < nv ? b0c : 0.f;
+                    tmem_st16(lane_base + TB + col + 16, bv);
+#pragma unroll
+                    for (int kk = 0; kk < 4; ++kk) {
+#pragma unroll
+                        for (int i = 0; i < 16; ++i) bv[i] = 16 * kk + i < n ? bch : 0.f;
+                        tmem_st16(lane_base + TB + 64 * (1 + hh) + 16 * kk, bv);
+                    }
                 }
                 tmem_st_wait();
             }
             fence_async_smem();
             fence_before_sync();
-            __syncthreads();
-            // epilogue 2's first two 16-edge blocks of sender features are
-            // gathered while GEMM2 runs
-            float xa[16], xn[16];
-            // (padding edges read row 0; their filter is 0)
-            const float* xin_f = a.X + fidx;
-            auto gather16 = [&](float (&x)[16], int col) {
+            pipe_sync(pp);
+            // epilogue 2's first two 8-edge blocks of sender features are
+            // gathered while GEMM2 runs (padding edges read row 0)
+            float xa0[8], xa1[8], xb0[8], xb1[8];
+            auto gather8 = [&](float (&x0)[8], float (&x1)[8], int col) {
 #pragma unroll
-                for (int i = 0; i < 16; i += 4) {
+                for (int i = 0; i < 8; i += 4) {
                     const int4 so = *reinterpret_cast<const int4*>(soff + col + i);
-                    x[i] = __ldg(xin_f + so.x);
-                    x[i + 1] = __ldg(xin_f + so.y);
-                    x[i + 2] = __ldg(xin_f + so.z);
-                    x[i + 3] = __ldg(xin_f + so.w);
+                    const int sv[4] = {so.x, so.y, so.z, so.w};
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        x0[i + j] = __ldg(xx + sv[j]);
+                        x1[i + j] = __ldg(xx + sv[j] + H);
+                    }
                 }
             };
-            gather16(xa, 0);
-            if (16 < n) gather16(xn, 16);
-            if (w < 3 && lane == 0) {   // GEMM2: f^T = W2 h^T, chunk w issued by warp w
+            gather8(xa0, xa1, 0);
+            if (8 < n) gather8(xb0, xb1, 8);
+            if (wl < 3 && lane == 0) {   // f^T = W2 h^T, chunk wl issued by warp wl
                 fence_after_sync();
                 if (!w2h_ready) {
                     if (!mbar_wait(w2h_bar, 0, WAIT_BUDGET)) signal_timeout(a, abort_flag, 6);
                     w2h_ready = true;
                 }
-                issue_gemm2_chunk<FN>(w, tmem, TM_F + 128 * w, w2h, w2l, Hs);
+                issue_gemm2_chunk<QN>(wl, tmem, TB + 64 * wl, w2h, w2l, Hs);
                 mma_commit(g2_bar);
             }
-            if (w < 3) __syncwarp();   // lanes 1-31 of the issuing warps wait here, not in a spin loop
-            // only warp 0 polls the MMA barrier; the others wait at the CTA
-            // barrier instead of spinning on shared memory the MMAs read from
-            if (w == 0 && !mbar_wait(g2_bar, g2_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 4);
+            if (wl < 3) __syncwarp();   // lanes 1-31 of the issuing warps wait here, not in a spin loop
+            if (wl == 0 && !mbar_wait(g2_bar, g2_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 4);
             g2_phase ^= 1;
             fence_before_sync();
-            __syncthreads();
+            // the abort decision is the same for every thread of the pipeline
+            const bool abort_now = pipe_sync_or(pp, *abort_flag != 0);
             fence_after_sync();
-            // ... and the H tile is free: the next tile's E tile and edge arrays
-            // arrive while epilogue 2 runs
-            const bool more = k + 1 < ntl && !*abort_flag;
+            // the H tile is free: the next tile's E tile and edge arrays arrive
+            // while epilogue 2 runs
+            const bool more = k + 1 < ntl && !abort_now;
             if (more) {
-                fetch_tile_edges(a, t, FN, t0 + FN, min(FN, e1 - t0 - FN), reinterpret_cast<float4*>(sbn + F_SB_US),
-                                 reinterpret_cast<int*>(sbn + F_SB_SRC), reinterpret_cast<int*>(sbn + F_SB_RCV));
-                if (t == 32) {
+                fetch(sbn, t0 + QN, min(QN, e1 - t0 - QN));
+                if (tp == QN) {
                     mbar_expect_tx(e_bar, ET_BYTES);
                     bulk_g2s(Es, etiles + (size_t)(k + 1) * ET_BYTES, ET_BYTES, e_bar);
                     ++e_issued;
                 }
             }
-            if (w == 1) __syncwarp();
-            {   // epilogue 2: component r of the message sums, segmented by receiver;
-                // 16-edge blocks, the next block's gathers in flight.  Padding
-                // edges gather 0 (and have u = 0), so they add nothing.
-                const float* ur = uc + (r == 0 ? 0 : (r - 1) * FN);
-                const uint32_t f1col = r == 0 ? 128 : 256;
-                float* out = a.Xt + fidx;          // Xt = X + message sum (student_model.py:359-385)
-                const float* xin = a.X + fidx;
-                auto process16 = [&](const float (&x)[16], int col) {
-                    float f1[16], f2[16];
-                    tmem_ld16(lane_base + f1col + col, f1);
-                    if (r != 0) tmem_ld16(lane_base + 384 + col, f2);
-                    const uint32_t mask = (chg[col >> 5] >> (col & 31)) & 0xFFFFu;
+            if (wl == 2) __syncwarp();
+            {   // epilogue 2: components 2 hh, 2 hh + 1 of the message sums, segmented
+                // by receiver; 8-edge blocks, the next block's gathers in flight
+                const float* u0 = uc + (hh == 0 ? 0 : QN);        // u component of comp. 2 hh (hh = 1: y)
+                const float* u1 = uc + (hh == 0 ? 0 : 2 * QN);    // of comp. 2 hh + 1 (x or z)
+                auto process8 = [&](const float (&x0)[8], const float (&x1)[8], int col) {
+                    float fa[8], f1[8], f2[8];
+                    if (hh == 0) tmem_ld8(lane_base + TB + col, fa);   // phi_s
+                    tmem_ld8(lane_base + TB + 64 + col, f1);            // phi_v1
+                    tmem_ld8(lane_base + TB + 128 + col, f2);           // phi_v2
+                    const uint32_t m = (chg[col >> 5] >> (col & 31)) & 0xFFu;
                     tmem_ld_wait();
-                    const float* u = ur + col;
-                    if (mask == 0) {
-                        if (r == 0) {
+                    float m0[8], m1[8];   // this block's message terms of the two components
+                    if (hh == 0) {
 #pragma unroll
-                            for (int i = 0; i < 16; ++i) acc = fmaf(x[i], f1[i], acc);
-                        } else {
-#pragma unroll
-                            for (int i = 0; i < 16; ++i) {
-                                acc = fmaf(x[i], f1[i], acc);
-                                accu = fmaf(u[i], f2[i], accu);
-                            }
+                        for (int i = 0; i < 8; ++i) {
+                            m0[i] = x0[i] * fa[i];
+                            m1[i] = fmaf(x1[i], f1[i], u1[col + i] * f2[i]);
                         }
-                    } else {   // a receiver changes in this block: flush its finished sum
+                    } else {
 #pragma unroll
-                        for (int i = 0; i < 16; ++i) {
-                            if (mask & (1u << i)) {
-                                out[(int64_t)cur * 4 * H] = base + (acc + accu);
+                        for (int i = 0; i < 8; ++i) {
+                            m0[i] = fmaf(x0[i], f1[i], u0[col + i] * f2[i]);
+                            m1[i] = fmaf(x1[i], f1[i], u1[col + i] * f2[i]);
+                        }
+                    }
+                    if (m == 0) {
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) {
+                            acc0 += m0[i];
+                            acc1 += m1[i];
+                        }
+                    } else {   // a receiver starts in this block: store the finished sums
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) {
+                            if (m & (1u << i)) {
+                                out[(int64_t)cur * 4 * H] = base0 + acc0;
+                                out[(int64_t)cur * 4 * H + H] = base1 + acc1;
                                 cur = rcv_s[col + i];
-                                base = xin[(int64_t)cur * 4 * H];
-                                acc = 0.f;
-                                accu = 0.f;
+                                base0 = xx[(int64_t)cur * 4 * H];
+                                base1 = xx[(int64_t)cur * 4 * H + H];
+                                acc0 = 0.f;
+                                acc1 = 0.f;
                             }
-                            acc = fmaf(x[i], f1[i], acc);
-                            if (r != 0) accu = fmaf(u[i], f2[i], accu);
+                            acc0 += m0[i];
+                            acc1 += m1[i];
                         }
                     }
                 };
-                for (int col = 0; col < n; col += 32) {   // blocks col and col + 16 are in flight
-                    process16(xa, col);
-                    if (col + 16 >= n) break;
-                    if (col + 32 < n) gather16(xa, col + 32);
-                    process16(xn, col + 16);
-                    if (col + 48 < n) gather16(xn, col + 48);
+                for (int col = 0; col < n; col += 16) {   // blocks col and col + 8 are in flight
+                    process8(xa0, xa1, col);
+                    if (col + 8 >= n) break;
+                    if (col + 16 < n) gather8(xa0, xa1, col + 16);
+                    process8(xb0, xb1, col + 8);
+                    if (col + 24 < n) gather8(xb0, xb1, col + 24);
                 }
             }
-            // chunk 0 is read by the scalar warps only (r = 0, warps 0-3): once
-            // all four are through epilogue 2, the next tile's GEMM1 can write z
-            // there while the vector warps finish
-            if (more && r == 0) {
-                tmem_ld_wait();
-                fence_before_sync();
-                bar_sync_first(4 * 32);
-                if (t == 0) issue_gemm1();
+            if (more && tp < QN) {   // the next tile's prep, by the two warps that fetched it
+                cp_async_wait_all();
+                pipe_sync_first(pp, QN);
+                prep(sbn, min(QN, e1 - t0 - QN), rcv_s[QN - 1]);
             }
-            g1_issued = more;
-            cp_async_wait_all();
             fence_before_sync();
-            __syncthreads();
-            if (*abort_flag) {
+            pipe_sync(pp);
+            if (abort_now) {
                 aborted = true;
                 break;
             }
-            if (more && t < FN)
-                tile_prep<FN>(t, min(FN, e1 - t0 - FN), rcv_s[FN - 1], reinterpret_cast<int*>(sbn + F_SB_SRC),
-                              reinterpret_cast<int*>(sbn + F_SB_RCV), reinterpret_cast<float4*>(sbn + F_SB_US),
-                              reinterpret_cast<int*>(sbn + F_SB_SOFF), nullptr, reinterpret_cast<float*>(sbn + F_SB_UC),
-                              reinterpret_cast<uint32_t*>(sbn + F_SB_CHG));
         }
-        if (!aborted) a.Xt[(int64_t)cur * 4 * H + fidx] = base + (acc + accu);
+        if (!aborted) {
+            out[(int64_t)cur * 4 * H] = base0 + acc0;
+            out[(int64_t)cur * 4 * H + H] = base1 + acc1;
+        }
     }
-    // drain: the resident-weight load, any E-tile copy and a GEMM1 issued
-    // for a tile that never ran (abort) must be complete before the CTA exits
+    // drain: every MMA and copy this CTA issued must be complete before it
+    // frees its tensor memory and exits (a wait on the parity of the phase
+    // before the current one returns at once)
     __syncthreads();
-    // the last GEMM1 and GEMM2 committed must be complete: a GEMM1 issued for
-    // a tile that never ran (abort), or MMAs whose wait timed out.  A wait on
-    // the parity of the phase before the current one returns at once, so
-    // these also hold when nothing was committed.
-    if (t == 0 && !mbar_wait(mma_bar, g1_issued ? mma_phase : (mma_phase ^ 1), WAIT_BUDGET))
-        set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 3);
-    if (t == 0 && !mbar_wait(g2_bar, g2_phase ^ 1, WAIT_BUDGET))
-        set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 5);
-    if (t == 32) {
+    if (tp == 0) {
+        if (!mbar_wait(mma_bar, mma_phase ^ 1, WAIT_BUDGET)) set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 3);
+        if (!mbar_wait(g2_bar, g2_phase ^ 1, WAIT_BUDGET)) set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 5);
+    }
+    if (tp == QN) {
         if (!mbar_wait(w2h_bar, 0, WAIT_BUDGET)) set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 7);
-        // an E-tile copy issued for a tile that never ran (abort) must land first
         if (e_issued > 0 && !mbar_wait(e_bar, (e_issued - 1) & 1, WAIT_BUDGET))
             set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 9);
     }
@@ -781,7 +809,6 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
 // their filter is exactly zero and every gather runs unpredicated (padding
 // gathers read row 0).
 constexpr int PN = 32;                               // edges per reverse tile
-constexpr int PT = 256;                              // threads per pipeline
 constexpr uint32_t P_HH = 2 * b_block(2 * PN);       // one half (hi or lo) of a [H; H'] tile: 16 KB
 constexpr uint32_t R_SB_US = 0;
 constexpr uint32_t R_SB_SRC = R_SB_US + PN * 16;
@@ -804,24 +831,9 @@ constexpr uint32_t R_RED_FLOATS = 8 * PN * 3;
 constexpr uint32_t R_OFF_BAR = R_OFF_RED + 2 * R_RED_FLOATS * 4;
 constexpr uint32_t R_OFF_MISC = R_OFF_BAR + 8 * 8;
 constexpr uint32_t R_SMEM = align1k(R_OFF_MISC + 16);
-static_assert(ETR_BYTES <= 2 * P_HH, "E tile fits in the H tile's space");
+static_assert(ET_BYTES <= 2 * P_HH, "E tile fits in the H tile's space");
 static_assert(R_SB_EACC % 16 == 0 && R_SB_BYTES % 16 == 0, "edge array alignment");
 static_assert(R_SMEM <= 232448, "reverse kernel shared memory");
-
-__device__ __forceinline__ void pipe_sync(int pp) {
-    asm volatile("bar.sync %0, %1;" ::"r"(1 + pp), "r"(PT) : "memory");
-}
-// Pipeline barrier that also ORs v over the pipeline's threads: every thread
-// gets the same answer.
-__device__ __forceinline__ bool pipe_sync_or(int pp, bool v) {
-    uint32_t r;
-    asm volatile(
-        "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.or.pred q, %2, %3, p;\n selp.u32 %0, 1, 0, q;\n}\n"
-        : "=r"(r)
-        : "r"((uint32_t)v), "r"(1 + pp), "r"(PT)
-        : "memory");
-    return r != 0;
-}
 
 // Sum 4 per-lane values over the 32 lanes of a warp (reduce-scatter):
 // afterwards lanes with (lane & 7) == 0 hold the sum of value index
@@ -936,15 +948,15 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
         if (j0 >= j1) continue;
         const int e0 = a.row_ptr[j0], e1 = a.row_ptr[j1];
         const int ntl = (e1 - e0 + PN - 1) / PN;
-        const unsigned char* etiles = a.etile + (size_t)a.etile_base[p] * ETR_BYTES;
+        const unsigned char* etiles = a.etile + (size_t)a.etile_base[p] * ET_BYTES;
         if (a.write_nodes) zero_empty_rows(a.xbar, a.row_ptr, j0, j1, wl, lane, PT / 32);
         int cur = j0;
         float acc0 = 0.f, acc1 = 0.f;   // node adjoints of the current receiver, two components
         if (ntl > 0) {   // the partition's first tile: edge arrays and [E; E'] tile
             fetch(sbase, e0, min(PN, e1 - e0));
             if (tp == 32) {
-                mbar_expect_tx(e_bar, ETR_BYTES);
-                bulk_g2s(Es, etiles, ETR_BYTES, e_bar);
+                mbar_expect_tx(e_bar, ET_BYTES);
+                bulk_g2s(Es, etiles, ET_BYTES, e_bar);
                 ++e_issued;
             }
             cp_async_wait_all();
@@ -970,7 +982,7 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                     for (int pr = 0; pr < 3; ++pr) {
                         const uint32_t ahl = pr == 2 ? 1 : 0, bhl = pr == 1 ? 1 : 0;
                         const uint64_t ad = sdesc(smem_u32(w1s + s * SLAB + ahl * A_TILE), A_LBO, A_SBO);
-                        const uint64_t bd = sdesc(smem_u32(Es + bhl * ETR_HALF + s * (2 * PN * 32)), 2 * PN * 16, 128);
+                        const uint64_t bd = sdesc(smem_u32(Es + bhl * ET_HALF + s * (ET_ROWS * 32)), ET_ROWS * 16, 128);
                         mma_f16(tmem + TB + 128, ad, bd, idesc, (s | pr) != 0);
                     }
                 mma_commit(mma_bar);
@@ -997,14 +1009,24 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                 tmem_ld16(lane_base + TB + 128 + PN + col, zd);
                 tmem_ld_wait();
                 const BColumn hc(Hs, P_HH, 2 * PN, col, c), hdc(Hs, P_HH, 2 * PN, PN + col, c);
+                if (n == PN) {   // a full tile (all but the last of a partition)
 #pragma unroll
-                for (int i = 0; i < 16; i += 2) {
-                    const float z0 = z[i] + bias, z1 = z[i + 1] + bias;
-                    const float s0 = fast_sigmoid(z0), s1 = fast_sigmoid(z1);
-                    const bool v0 = i < nv, v1 = i + 1 < nv;
-                    hc.put_pair(i, v0 ? z0 * s0 : 0.f, v1 ? z1 * s1 : 0.f);
-                    hdc.put_pair(i, v0 ? s0 * (1.0f + z0 * (1.0f - s0)) * zd[i] : 0.f,
-                                 v1 ? s1 * (1.0f + z1 * (1.0f - s1)) * zd[i + 1] : 0.f);
+                    for (int i = 0; i < 16; i += 2) {
+                        const float z0 = z[i] + bias, z1 = z[i + 1] + bias;
+                        const float s0 = fast_sigmoid(z0), s1 = fast_sigmoid(z1);
+                        hc.put_pair(i, z0 * s0, z1 * s1);
+                        hdc.put_pair(i, s0 * (1.0f + z0 * (1.0f - s0)) * zd[i], s1 * (1.0f + z1 * (1.0f - s1)) * zd[i + 1]);
+                    }
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 16; i += 2) {
+                        const float z0 = z[i] + bias, z1 = z[i + 1] + bias;
+                        const float s0 = fast_sigmoid(z0), s1 = fast_sigmoid(z1);
+                        const bool v0 = i < nv, v1 = i + 1 < nv;
+                        hc.put_pair(i, v0 ? z0 * s0 : 0.f, v1 ? z1 * s1 : 0.f);
+                        hdc.put_pair(i, v0 ? s0 * (1.0f + z0 * (1.0f - s0)) * zd[i] : 0.f,
+                                     v1 ? s1 * (1.0f + z1 * (1.0f - s1)) * zd[i + 1] : 0.f);
+                    }
                 }
                 // f = W2 h accumulates onto b2 (0 for padding edges), f' = W2 h'
                 // onto 0: this warp refills the chunk-2 cells it has just read
@@ -1090,8 +1112,8 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
             if (more) {
                 fetch(sbn, t0 + PN, min(PN, e1 - t0 - PN));
                 if (tp == 32) {
-                    mbar_expect_tx(e_bar, ETR_BYTES);
-                    bulk_g2s(Es, etiles + (size_t)(k + 1) * ETR_BYTES, ETR_BYTES, e_bar);
+                    mbar_expect_tx(e_bar, ET_BYTES);
+                    bulk_g2s(Es, etiles + (size_t)(k + 1) * ET_BYTES, ET_BYTES, e_bar);
                     ++e_issued;
                 }
             }
@@ -1253,12 +1275,13 @@ int launch_edge_fwd_tc(const EdgeArgs& a, int layer, cudaStream_t st) {
     static std::once_flag once;
     static cudaError_t attr_err = cudaSuccess;
     std::call_once(once, [] {
-        attr_err = cudaFuncSetAttribute(edge_fwd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, F_SMEM);
+        attr_err = cudaFuncSetAttribute(edge_fwd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, Q_SMEM);
     });
     if (attr_err != cudaSuccess) return cuda_status(attr_err, "edge_fwd_tc smem attribute");
     const unsigned char* w1 = reinterpret_cast<const unsigned char*>(a.P + a.lo.w1_bf);
     const unsigned char* w2 = reinterpret_cast<const unsigned char*>(a.P + a.lo.w2_bf);
-    MLFF_LAUNCH_PDL("edge_fwd_tc", edge_fwd_tc_kernel, tc_grid(fwd_ranges(a.nparts)), NT, F_SMEM, st, a, w1, w2);
+    // two pipelines (partitions) per CTA
+    MLFF_LAUNCH_PDL("edge_fwd_tc", edge_fwd_tc_kernel, tc_grid((a.nparts + 1) / 2), NT, Q_SMEM, st, a, w1, w2);
     return MLFF_OK;
 }
 

@@ -41,8 +41,8 @@ struct WsLayout {
     // plain path (materialised per-edge tensors, like the reference's graph)
     size_t geo;                // float4 [cap] (u_x, u_y, u_z, d)
     size_t etile_base;         // int32 [2][P+1] first E tile of each partition (forward, reverse)
-    size_t etile_f;            // forward E tiles: 128 edges x K 32, split fp16, 16 KB each
-    size_t etile_b;            // reverse [E; E'] tiles: 64 edges, 16 KB each
+    size_t etile_f;            // forward E tiles: 64 edges x K 32, split fp16, 8 KB each
+    size_t etile_b;            // reverse [E; E'] tiles: 32 edges, 64 rows, 8 KB each
     int64_t n_etile_f, n_etile_b;
     size_t erbf;               // float [cap][RMAX]
     size_t erbf_d;             // float [cap][RMAX]
