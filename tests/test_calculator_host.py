@@ -31,6 +31,42 @@ def test_jit_without_path(ckpt):
         StudentForceFieldCalculator(ckpt, device="cpu", use_jit=True)
 
 
+class _Archive(torch.nn.Module):
+    """A TorchScript module holding a state_dict under the reference's
+    parameter names (what ``torch.jit.save`` of a scripted StudentForceField
+    stores)."""
+
+    def __init__(self, sd):
+        super().__init__()
+        for k, v in sd.items():
+            *path, leaf = k.split(".")
+            mod = self
+            for name in path:
+                if not hasattr(mod, name):
+                    mod.add_module(name, torch.nn.Module())
+                mod = getattr(mod, name)
+            mod.register_buffer(leaf, v.clone())
+
+    def forward(self, x: torch.Tensor) -> torch.Tensor:
+        return x
+
+
+def test_jit_archive_loads(tmp_path):
+    """use_jit=True with a TorchScript archive (ase_calculator.py:216-237):
+    the calculator's model carries the archive's weights, key for key."""
+    torch.manual_seed(3)
+    sd = StudentForceField().state_dict()
+    path = tmp_path / "model_jit.pt"
+    torch.jit.save(torch.jit.script(_Archive(sd)), str(path))
+    c = StudentForceFieldCalculator(tmp_path / "unused.pt", device="cpu", use_jit=True, jit_path=path)
+    got = c.model.state_dict()
+    assert set(got) == set(sd)
+    for k, v in sd.items():
+        assert torch.equal(got[k].cpu(), v), k
+    with pytest.raises(FileNotFoundError):
+        StudentForceFieldCalculator(tmp_path / "unused.pt", device="cpu", use_jit=True, jit_path=tmp_path / "no.pt")
+
+
 def test_properties(ckpt):
     c = StudentForceFieldCalculator(ckpt, device="cpu")
     assert c.implemented_properties == ["energy", "forces"]
