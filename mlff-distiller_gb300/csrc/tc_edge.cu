@@ -704,25 +704,17 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                     tmem_ld8(lane_base + TB + 128 + col, f2);           // phi_v2
                     const uint32_t m = (chg[col >> 5] >> (col & 31)) & 0xFFu;
                     tmem_ld_wait();
-                    float m0[8], m1[8];   // this block's message terms of the two components
-                    if (hh == 0) {
-#pragma unroll
-                        for (int i = 0; i < 8; ++i) {
-                            m0[i] = x0[i] * fa[i];
-                            m1[i] = fmaf(x1[i], f1[i], u1[col + i] * f2[i]);
-                        }
-                    } else {
-#pragma unroll
-                        for (int i = 0; i < 8; ++i) {
-                            m0[i] = fmaf(x0[i], f1[i], u0[col + i] * f2[i]);
-                            m1[i] = fmaf(x1[i], f1[i], u1[col + i] * f2[i]);
-                        }
-                    }
+                    // message terms of edge i, the same expressions on both branches
+                    // (a block's branch depends on where the tile starts)
+                    auto m0 = [&](int i) {
+                        return hh == 0 ? x0[i] * fa[i] : fmaf(x0[i], f1[i], u0[col + i] * f2[i]);
+                    };
+                    auto m1 = [&](int i) { return fmaf(x1[i], f1[i], u1[col + i] * f2[i]); };
                     if (m == 0) {
 #pragma unroll
                         for (int i = 0; i < 8; ++i) {
-                            acc0 += m0[i];
-                            acc1 += m1[i];
+                            acc0 += m0(i);
+                            acc1 += m1(i);
                         }
                     } else {   // a receiver starts in this block: store the finished sums
 #pragma unroll
@@ -736,8 +728,8 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                                 acc0 = 0.f;
                                 acc1 = 0.f;
                             }
-                            acc0 += m0[i];
-                            acc1 += m1[i];
+                            acc0 += m0(i);
+                            acc1 += m1(i);
                         }
                     }
                 };
@@ -804,7 +796,9 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
 // of the tile: h = 0 the scalar and v_x, h = 1 v_y and v_z.  Node adjoints
 // are gathered from the sender side (exact: f(d_ab) = f(d_ba)) and summed per
 // receiver in registers; each thread adds its two components' shares of
-// dE/dd (and its dE/du components) before the cross-lane reduction.
+// dE/dd before the cross-lane reduction.  dE/du_k needs only the receiver's
+// v_k adjoint and phi_v2: warp (q, 0) reduces du_x and du_y, warp (q, 1)
+// du_z, so both warps reduce the same number of values per edge.
 // Padding edges of a partial tile get h = h' = 0 and a zero bias fill, so
 // their filter is exactly zero and every gather runs unpredicated (padding
 // gathers read row 0).
@@ -1054,13 +1048,14 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
             fence_before_sync();
             pipe_sync(pp);
             // epilogue 2's first two 4-edge blocks of gathers are issued while
-            // GEMM2 runs: the senders' dE/dXt and X rows, the receiver's dE/dXt
-            // row (once per block when no receiver starts inside it)
+            // GEMM2 runs: the senders' dE/dXt and X rows and the dE/dXt row of
+            // the block's first receiver (edges where another receiver starts
+            // inside the block reload theirs in epilogue 2)
             const uint32_t chw = *reinterpret_cast<const uint32_t*>(sb + R_SB_CHG);
-            float tba0[4], tba1[4], xba0[4], xba1[4], tra0[4], tra1[4];
-            float tbb0[4], tbb1[4], xbb0[4], xbb1[4], trb0[4], trb1[4];
-            auto gather4 = [&](float (&tb0)[4], float (&tb1)[4], float (&xb0)[4], float (&xb1)[4], float (&tr0)[4],
-                               float (&tr1)[4], int col) {
+            float tba0[4], tba1[4], xba0[4], xba1[4], ra0, ra1, ra2;
+            float tbb0[4], tbb1[4], xbb0[4], xbb1[4], rb0, rb1, rb2;
+            auto gather4 = [&](float (&tb0)[4], float (&tb1)[4], float (&xb0)[4], float (&xb1)[4], float& r0,
+                               float& r1, float& r2, int col) {
                 const int4 so = *reinterpret_cast<const int4*>(soff + col);
                 const int sv[4] = {so.x, so.y, so.z, so.w};
 #pragma unroll
@@ -1070,26 +1065,13 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                     xb0[i] = __ldg(xx + sv[i]);
                     xb1[i] = __ldg(xx + sv[i] + H);
                 }
-                if (((chw >> col) & 0xEu) == 0) {   // one receiver for the whole block
-                    const int ro = roff[col];
-                    const float r0 = __ldg(xtb + ro), r1 = __ldg(xtb + ro + H);
-#pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        tr0[i] = r0;
-                        tr1[i] = r1;
-                    }
-                } else {
-                    const int4 ro = *reinterpret_cast<const int4*>(roff + col);
-                    const int rv[4] = {ro.x, ro.y, ro.z, ro.w};
-#pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        tr0[i] = __ldg(xtb + rv[i]);
-                        tr1[i] = __ldg(xtb + rv[i] + H);
-                    }
-                }
+                const int ro = roff[col];
+                r0 = __ldg(xtb + ro);
+                r1 = __ldg(xtb + ro + H);
+                r2 = hh == 0 ? __ldg(xtb + ro + 2 * H) : 0.f;   // v_y, for dE/du_y
             };
-            gather4(tba0, tba1, xba0, xba1, tra0, tra1, 0);
-            if (4 < n) gather4(tbb0, tbb1, xbb0, xbb1, trb0, trb1, 4);
+            gather4(tba0, tba1, xba0, xba1, ra0, ra1, ra2, 0);
+            if (4 < n) gather4(tbb0, tbb1, xbb0, xbb1, rb0, rb1, rb2, 4);
             if (wl < 3 && lane == 0) {   // [f; f']^T = W2 [h; h']^T, chunk wl issued by warp wl
                 fence_after_sync();
                 if (!w2h_ready) {
@@ -1118,9 +1100,12 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                 }
             }
             if (wl == 1) __syncwarp();
-            {   // epilogue 2 over 4-edge blocks, the next block's gathers in flight
+            {   // epilogue 2 over 4-edge blocks, the next block's gathers in flight.
+                // Warp (q, 0) owns the scalar and v_x: dE/dd share, dE/du_x and
+                // dE/du_y; warp (q, 1) owns v_y and v_z: dE/dd share and dE/du_z
+                // (both halves then do the same amount of work)
                 auto process4 = [&](const float (&tb0)[4], const float (&tb1)[4], const float (&xb0)[4],
-                                    const float (&xb1)[4], const float (&tr0)[4], const float (&tr1)[4], int col) {
+                                    const float (&xb1)[4], float r0, float r1, float r2, int col) {
                     float fa[4], da[4], f1[4], d1[4], f2[4], d2[4];
                     if (hh == 0) {
                         tmem_ld4(lane_base + TB + col, fa);        // phi_s (bias included)
@@ -1138,6 +1123,21 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                             fa[i] = f1[i];
                             da[i] = d1[i];
                         }
+                    }
+                    // receiver dE/dXt rows per edge: the block's first receiver unless
+                    // another one starts at edges 1-3 (then reloaded from there on)
+                    float tr0[4], tr1[4], tr2[4];
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        if (i > 0 && (m & (1u << i))) {
+                            const int ro = roff[col + i];
+                            r0 = __ldg(xtb + ro);
+                            r1 = __ldg(xtb + ro + H);
+                            if (hh == 0) r2 = __ldg(xtb + ro + 2 * H);
+                        }
+                        tr0[i] = r0;
+                        tr1[i] = r1;
+                        tr2[i] = r2;
                     }
                     if (m == 0) {
 #pragma unroll
@@ -1162,38 +1162,37 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                         }
                     }
                     // this thread's shares of dE/dd and dE/du for the 4 edges
-                    float pv[8], p2[4];
-                    if (hh == 0) {   // scalar and v_x
+                    float pv[8];
+                    if (hh == 0) {   // scalar and v_x; dE/du_x, dE/du_y
                         const float* ux = uc + col;
+                        float p2[4];
 #pragma unroll
                         for (int i = 0; i < 4; ++i) {
                             pv[i] = fmaf(tr0[i] * xb0[i], da[i], tr1[i] * fmaf(xb1[i], d1[i], ux[i] * d2[i]));
                             pv[4 + i] = tr1[i] * f2[i];
+                            p2[i] = tr2[i] * f2[i];
                         }
-                    } else {         // v_y and v_z
+                        const float s4 = warp_reduce_scatter4(p2, lane);
+                        if ((lane & 7) == 0) red[(wl * PN + col + rs4_idx) * 3 + 2] = s4;
+                    } else {         // v_y and v_z; dE/du_z
                         const float* uy = uc + PN + col;
                         const float* uz = uc + 2 * PN + col;
 #pragma unroll
                         for (int i = 0; i < 4; ++i) {
                             pv[i] = fmaf(tr0[i], fmaf(xb0[i], d1[i], uy[i] * d2[i]),
                                          tr1[i] * fmaf(xb1[i], d1[i], uz[i] * d2[i]));
-                            pv[4 + i] = tr0[i] * f2[i];
-                            p2[i] = tr1[i] * f2[i];
+                            pv[4 + i] = tr1[i] * f2[i];
                         }
                     }
                     const float s8 = warp_reduce_scatter8(pv, lane);
                     if ((lane & 3) == 0) red[(wl * PN + col + (rs_idx & 3)) * 3 + (rs_idx >> 2)] = s8;
-                    if (hh != 0) {
-                        const float s4 = warp_reduce_scatter4(p2, lane);
-                        if ((lane & 7) == 0) red[(wl * PN + col + rs4_idx) * 3 + 2] = s4;
-                    }
                 };
                 for (int col = 0; col < n; col += 8) {   // blocks col and col + 4 are in flight
-                    process4(tba0, tba1, xba0, xba1, tra0, tra1, col);
+                    process4(tba0, tba1, xba0, xba1, ra0, ra1, ra2, col);
                     if (col + 4 >= n) break;
-                    if (col + 8 < n) gather4(tba0, tba1, xba0, xba1, tra0, tra1, col + 8);
-                    process4(tbb0, tbb1, xbb0, xbb1, trb0, trb1, col + 4);
-                    if (col + 12 < n) gather4(tbb0, tbb1, xbb0, xbb1, trb0, trb1, col + 12);
+                    if (col + 8 < n) gather4(tba0, tba1, xba0, xba1, ra0, ra1, ra2, col + 8);
+                    process4(tbb0, tbb1, xbb0, xbb1, rb0, rb1, rb2, col + 4);
+                    if (col + 12 < n) gather4(tbb0, tbb1, xbb0, xbb1, rb0, rb1, rb2, col + 12);
                 }
             }
             if (more && tp < PN) {   // the next tile's prep, by the warp that fetched it
@@ -1210,13 +1209,14 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                 const float* rr = red + te * 3;
                 float dd = 0.f, du0 = 0.f, du1 = 0.f, du2 = 0.f;
 #pragma unroll
-                for (int ww = 0; ww < 8; ++ww) {
+                for (int ww = 0; ww < 8; ++ww) {   // warps 0-3: (dd, du_x, du_y), 4-7: (dd, du_z)
                     const float* rw = rr + ww * PN * 3;
                     dd += rw[0];
-                    if (ww < 4) du0 += rw[1];
-                    else {
-                        du1 += rw[1];
-                        du2 += rw[2];
+                    if (ww < 4) {
+                        du0 += rw[1];
+                        du1 += rw[2];
+                    } else {
+                        du2 += rw[1];
                     }
                 }
                 float4 ea = a.eacc_init ? make_float4(0.f, 0.f, 0.f, 0.f)
