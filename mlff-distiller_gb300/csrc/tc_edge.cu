@@ -37,6 +37,7 @@
 #include <cuda_fp16.h>
 #include <mutex>
 #include "common.cuh"
+#include <type_traits>
 #include "workspace.h"
 #include "edge_common.cuh"
 #include "profile.h"
@@ -697,9 +698,11 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                 // by receiver; 8-edge blocks, the next block's gathers in flight
                 const float* u0 = uc + (hh == 0 ? 0 : QN);        // u component of comp. 2 hh (hh = 1: y)
                 const float* u1 = uc + (hh == 0 ? 0 : 2 * QN);    // of comp. 2 hh + 1 (x or z)
-                auto process8 = [&](const float (&x0)[8], const float (&x1)[8], int col) {
+                // (compiled once per warp half: hc is std::integral_constant<int, hh>)
+                auto process8 = [&](auto hc, const float (&x0)[8], const float (&x1)[8], int col) {
+                    constexpr int HH = decltype(hc)::value;
                     float fa[8], f1[8], f2[8];
-                    if (hh == 0) tmem_ld8(lane_base + TB + col, fa);   // phi_s
+                    if (HH == 0) tmem_ld8(lane_base + TB + col, fa);   // phi_s
                     tmem_ld8(lane_base + TB + 64 + col, f1);            // phi_v1
                     tmem_ld8(lane_base + TB + 128 + col, f2);           // phi_v2
                     const uint32_t m = (chg[col >> 5] >> (col & 31)) & 0xFFu;
@@ -707,7 +710,7 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                     // message terms of edge i, the same expressions on both branches
                     // (a block's branch depends on where the tile starts)
                     auto m0 = [&](int i) {
-                        return hh == 0 ? x0[i] * fa[i] : fmaf(x0[i], f1[i], u0[col + i] * f2[i]);
+                        return HH == 0 ? x0[i] * fa[i] : fmaf(x0[i], f1[i], u0[col + i] * f2[i]);
                     };
                     auto m1 = [&](int i) { return fmaf(x1[i], f1[i], u1[col + i] * f2[i]); };
                     if (m == 0) {
@@ -733,13 +736,17 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                         }
                     }
                 };
-                for (int col = 0; col < n; col += 16) {   // blocks col and col + 8 are in flight
-                    process8(xa0, xa1, col);
-                    if (col + 8 >= n) break;
-                    if (col + 16 < n) gather8(xa0, xa1, col + 16);
-                    process8(xb0, xb1, col + 8);
-                    if (col + 24 < n) gather8(xb0, xb1, col + 24);
-                }
+                auto blocks = [&](auto hc) {
+                    for (int col = 0; col < n; col += 16) {   // blocks col and col + 8 are in flight
+                        process8(hc, xa0, xa1, col);
+                        if (col + 8 >= n) break;
+                        if (col + 16 < n) gather8(xa0, xa1, col + 16);
+                        process8(hc, xb0, xb1, col + 8);
+                        if (col + 24 < n) gather8(xb0, xb1, col + 24);
+                    }
+                };
+                if (hh == 0) blocks(std::integral_constant<int, 0>{});
+                else blocks(std::integral_constant<int, 1>{});
             }
             if (more && tp < QN) {   // the next tile's prep, by the two warps that fetched it
                 cp_async_wait_all();
@@ -1104,10 +1111,12 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                 // Warp (q, 0) owns the scalar and v_x: dE/dd share, dE/du_x and
                 // dE/du_y; warp (q, 1) owns v_y and v_z: dE/dd share and dE/du_z
                 // (both halves then do the same amount of work)
-                auto process4 = [&](const float (&tb0)[4], const float (&tb1)[4], const float (&xb0)[4],
+                // (compiled once per warp half: hc is std::integral_constant<int, hh>)
+                auto process4 = [&](auto hc, const float (&tb0)[4], const float (&tb1)[4], const float (&xb0)[4],
                                     const float (&xb1)[4], float r0, float r1, float r2, int col) {
+                    constexpr int HH = decltype(hc)::value;
                     float fa[4], da[4], f1[4], d1[4], f2[4], d2[4];
-                    if (hh == 0) {
+                    if (HH == 0) {
                         tmem_ld4(lane_base + TB + col, fa);        // phi_s (bias included)
                         tmem_ld4(lane_base + TB + PN + col, da);   // dphi_s / dd
                     }
@@ -1117,33 +1126,35 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                     tmem_ld4(lane_base + TB + 128 + PN + col, d2);
                     const uint32_t m = (chw >> col) & 0xFu;
                     tmem_ld_wait();
-                    if (hh != 0) {
+                    if (HH != 0) {
 #pragma unroll
                         for (int i = 0; i < 4; ++i) {
                             fa[i] = f1[i];
                             da[i] = d1[i];
                         }
                     }
-                    // receiver dE/dXt rows per edge: the block's first receiver unless
-                    // another one starts at edges 1-3 (then reloaded from there on)
-                    float tr0[4], tr1[4], tr2[4];
-#pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        if (i > 0 && (m & (1u << i))) {
-                            const int ro = roff[col + i];
-                            r0 = __ldg(xtb + ro);
-                            r1 = __ldg(xtb + ro + H);
-                            if (hh == 0) r2 = __ldg(xtb + ro + 2 * H);
+                    // this thread's shares of dE/dd and dE/du of edge i, given the
+                    // receiver's dE/dXt rows t0, t1 (t2: v_y, warps (q, 0) only); the
+                    // same expressions on both branches below (a block's branch depends
+                    // on where the tile starts)
+                    float pv[8], p2[4];
+                    auto edge_terms = [&](int i, float t0, float t1, float t2) {
+                        if (HH == 0) {   // scalar and v_x; dE/du_x, dE/du_y
+                            pv[i] = fmaf(t0 * xb0[i], da[i], t1 * fmaf(xb1[i], d1[i], uc[col + i] * d2[i]));
+                            pv[4 + i] = t1 * f2[i];
+                            p2[i] = t2 * f2[i];
+                        } else {         // v_y and v_z; dE/du_z
+                            pv[i] = fmaf(t0, fmaf(xb0[i], d1[i], uc[PN + col + i] * d2[i]),
+                                         t1 * fmaf(xb1[i], d1[i], uc[2 * PN + col + i] * d2[i]));
+                            pv[4 + i] = t1 * f2[i];
                         }
-                        tr0[i] = r0;
-                        tr1[i] = r1;
-                        tr2[i] = r2;
-                    }
-                    if (m == 0) {
+                    };
+                    if (m == 0) {   // one receiver for the whole block, no sum finishes here
 #pragma unroll
                         for (int i = 0; i < 4; ++i) {
                             acc0 = fmaf(tb0[i], fa[i], acc0);
                             acc1 = fmaf(tb1[i], f1[i], acc1);
+                            edge_terms(i, r0, r1, r2);
                         }
                     } else {   // a receiver starts in this block: store the finished sums
 #pragma unroll
@@ -1156,44 +1167,36 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                                 cur = rcv_s[col + i];
                                 acc0 = 0.f;
                                 acc1 = 0.f;
+                                if (i > 0) {   // edge 0's receiver rows came with the gathers
+                                    const int ro = roff[col + i];
+                                    r0 = __ldg(xtb + ro);
+                                    r1 = __ldg(xtb + ro + H);
+                                    if (HH == 0) r2 = __ldg(xtb + ro + 2 * H);
+                                }
                             }
                             acc0 = fmaf(tb0[i], fa[i], acc0);
                             acc1 = fmaf(tb1[i], f1[i], acc1);
+                            edge_terms(i, r0, r1, r2);
                         }
                     }
-                    // this thread's shares of dE/dd and dE/du for the 4 edges
-                    float pv[8];
-                    if (hh == 0) {   // scalar and v_x; dE/du_x, dE/du_y
-                        const float* ux = uc + col;
-                        float p2[4];
-#pragma unroll
-                        for (int i = 0; i < 4; ++i) {
-                            pv[i] = fmaf(tr0[i] * xb0[i], da[i], tr1[i] * fmaf(xb1[i], d1[i], ux[i] * d2[i]));
-                            pv[4 + i] = tr1[i] * f2[i];
-                            p2[i] = tr2[i] * f2[i];
-                        }
+                    if (HH == 0) {
                         const float s4 = warp_reduce_scatter4(p2, lane);
                         if ((lane & 7) == 0) red[(wl * PN + col + rs4_idx) * 3 + 2] = s4;
-                    } else {         // v_y and v_z; dE/du_z
-                        const float* uy = uc + PN + col;
-                        const float* uz = uc + 2 * PN + col;
-#pragma unroll
-                        for (int i = 0; i < 4; ++i) {
-                            pv[i] = fmaf(tr0[i], fmaf(xb0[i], d1[i], uy[i] * d2[i]),
-                                         tr1[i] * fmaf(xb1[i], d1[i], uz[i] * d2[i]));
-                            pv[4 + i] = tr1[i] * f2[i];
-                        }
                     }
                     const float s8 = warp_reduce_scatter8(pv, lane);
                     if ((lane & 3) == 0) red[(wl * PN + col + (rs_idx & 3)) * 3 + (rs_idx >> 2)] = s8;
                 };
-                for (int col = 0; col < n; col += 8) {   // blocks col and col + 4 are in flight
-                    process4(tba0, tba1, xba0, xba1, ra0, ra1, ra2, col);
-                    if (col + 4 >= n) break;
-                    if (col + 8 < n) gather4(tba0, tba1, xba0, xba1, ra0, ra1, ra2, col + 8);
-                    process4(tbb0, tbb1, xbb0, xbb1, rb0, rb1, rb2, col + 4);
-                    if (col + 12 < n) gather4(tbb0, tbb1, xbb0, xbb1, rb0, rb1, rb2, col + 12);
-                }
+                auto blocks = [&](auto hc) {
+                    for (int col = 0; col < n; col += 8) {   // blocks col and col + 4 are in flight
+                        process4(hc, tba0, tba1, xba0, xba1, ra0, ra1, ra2, col);
+                        if (col + 4 >= n) break;
+                        if (col + 8 < n) gather4(tba0, tba1, xba0, xba1, ra0, ra1, ra2, col + 8);
+                        process4(hc, tbb0, tbb1, xbb0, xbb1, rb0, rb1, rb2, col + 4);
+                        if (col + 12 < n) gather4(tbb0, tbb1, xbb0, xbb1, rb0, rb1, rb2, col + 12);
+                    }
+                };
+                if (hh == 0) blocks(std::integral_constant<int, 0>{});
+                else blocks(std::integral_constant<int, 1>{});
             }
             if (more && tp < PN) {   // the next tile's prep, by the warp that fetched it
                 cp_async_wait_all();
