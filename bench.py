@@ -540,6 +540,11 @@ def main():
                                     if path == _lib.PATH_TUNED_TC else None),
                 "step": {"gemm_flop_per_step": step_flop, "achieved": round(step_tf, 2),
                          "frac": round(step_tf / peak_tf, 4)}}
+        if dom == "edge_bwd" and prof.launches.get("edge_bwd_q", 0) > 0:
+            # the reverse pass's companion kernel (per-atom Q rows, launched just before each
+            # reverse launch): not part of the FLOPs above, reported beside them
+            roof["companion"] = {"kernel": "edge_bwd_q",
+                                 "avg_launch_ms": round(prof.ms["edge_bwd_q"] / prof.launches["edge_bwd_q"], 4)}
     gpu_launches = sum(prof.launches.values())
 
     # e2e through the public module API with host buffers

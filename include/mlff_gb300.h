@@ -350,8 +350,9 @@ int mlff_param_grads_forces(const mlff_dims *dims, const void *packed, const mlf
  * and the number of launches.  Kinds: 0 neighbours, 1 fused edge forward,
  * 2 fused edge reverse, 3 update forward, 4 update reverse, 5 readout,
  * 6 forces, 7 plain-path GEMMs, 8 plain-path edge ops, 9 other, 10 MD
- * integrator.  Do not enable while a stream is being captured. */
-#define MLFF_PROFILE_KINDS 11
+ * integrator, 11 the per-atom Q rows of the tensor-core reverse edge pass.
+ * Do not enable while a stream is being captured. */
+#define MLFF_PROFILE_KINDS 12
 int mlff_profile_begin(void);
 int mlff_profile_end(double *ms_by_kind, int64_t *launches_by_kind, int32_t n_kinds);
 

@@ -111,6 +111,7 @@ struct LayerOffsets {
     int64_t u2_tc;  //   U1 [H][2H] and U2 [3H][H] (forward),
     int64_t u2t_tc; //   U2^T [H][3H] and U1^T [2H][H] (reverse)
     int64_t u1t_tc;
+    int64_t w2q_tc; // W2 rows [2H,3H) transposed as split-fp16 A tiles (reverse pass: per-atom Q rows)
 };
 
 struct PackedOffsets {

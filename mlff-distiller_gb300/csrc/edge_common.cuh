@@ -30,6 +30,8 @@ struct EdgeArgs {
     const float* xtbar;       // reverse: dE/dXt
     float* xbar;              // reverse: dE/dX
     float4* eacc;             // reverse: per-edge (dE/dd, dE/du)
+    const unsigned char* qs;  // reverse, tensor-core path: per-atom Q rows (split fp16) of the current layer
+    const float* qb;          // reverse, tensor-core path: per-atom b2 . dE/dXt_v of the current layer
     int32_t eacc_init;        // reverse: 1 = first layer processed, eacc is written rather than added to
     int32_t write_nodes;      // reverse: also produce dE/dX (unused for the first layer)
     int32_t n_atoms;

@@ -62,6 +62,7 @@ PackedOffsets packed_offsets(const mlff_dims& d) {
         L.u2_tc = take(2 * H3 * H / 2);
         L.u2t_tc = take(2 * H3 * H / 2);
         L.u1t_tc = take(2 * H * 2 * H / 2);
+        L.w2q_tc = take(2 * H * H / 2);
     }
     o.total = p;
     return o;

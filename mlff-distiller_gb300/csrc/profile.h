@@ -19,7 +19,8 @@ enum ProfKind {
     PK_PLAIN_EDGE = 8,
     PK_OTHER = 9,
     PK_MD = 10,
-    PK_COUNT = 11
+    PK_EDGE_BWD_Q = 11,   // per-atom Q rows of the reverse tensor-core edge kernel
+    PK_COUNT = 12
 };
 
 bool prof_enabled();

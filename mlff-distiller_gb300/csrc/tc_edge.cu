@@ -61,11 +61,20 @@ constexpr uint32_t TM_W2LO = 0;
 
 // ------------------------------------------------------------- packing
 // W1 [H][RMAX] -> 2 K-step blocks (hi, lo); W2 [3H][H] -> 24 hi tiles
-// followed by the 24 matching lo tiles.
+// followed by the 24 matching lo tiles; W2's third chunk transposed
+// (rows = hidden units, K = channels) -> 8 K-step pairs (hi tile, lo tile)
+// for the per-atom Q rows of the reverse pass.
 __global__ void pack_tc_kernel(const float* __restrict__ w1, const float* __restrict__ w2,
                                unsigned char* __restrict__ w1_out, unsigned char* __restrict__ w2_out,
-                               uint32_t* __restrict__ w2_tm) {
+                               uint32_t* __restrict__ w2_tm, unsigned char* __restrict__ w2q_out) {
     const int stride = gridDim.x * blockDim.x;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 8 * 128 * 16; i += stride) {
+        const int s = i / 2048, m = (i / 16) % 128, kk = i % 16;
+        __half hi, lo;
+        split_f16(w2[(2 * H + 16 * s + kk) * H + m], hi, lo);
+        *reinterpret_cast<__half*>(w2q_out + s * A_PAIR + a_off(m, kk)) = hi;
+        *reinterpret_cast<__half*>(w2q_out + s * A_PAIR + A_TILE + a_off(m, kk)) = lo;
+    }
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 2 * 128 * 16; i += stride) {
         const int s = i / 2048, m = (i / 16) % 128, kk = i % 16;
         __half hi, lo;
@@ -103,7 +112,8 @@ int pack_bf16(const mlff_dims& d, float* out, const PackedOffsets& o, cudaStream
         const LayerOffsets& L = o.layer[l];
         pack_tc_kernel<<<64, 256, 0, st>>>(out + L.w1, out + L.w2, reinterpret_cast<unsigned char*>(out + L.w1_bf),
                                            reinterpret_cast<unsigned char*>(out + L.w2_bf),
-                                           reinterpret_cast<uint32_t*>(out + L.w2_tm));
+                                           reinterpret_cast<uint32_t*>(out + L.w2_tm),
+                                           reinterpret_cast<unsigned char*>(out + L.w2q_tc));
         MLFF_LAUNCH_CHECK("pack_tc");
     }
     return pack_update_tc(d, out, o, st);
@@ -790,27 +800,40 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
 // so that one pipeline's MMAs, copies and barrier waits overlap the other
 // pipeline's CUDA-core epilogues.  A pipeline processes 32-edge tiles with
 // E and E' (then H and H') stacked as rows 0-31 / 32-63 of one 64-row B
-// tile: every MMA is 128 x 64 x 16 and one pass gives the filter f and its
-// d-derivative f' (forward mode, no transposed GEMM, no stored activation).
+// tile: every MMA is 128 x 64 x 16 and one pass gives the filter and its
+// d-derivative (forward mode, no transposed GEMM, no stored activation).
+//
+// The third filter chunk (phi_v2, the u-direction term) enters the reverse
+// pass only through sums over channels with the receiver's v adjoint:
+//   dE/du_k(e) = sum_c dE/dXt_{v_k}(i)[c] phi_v2(e)[c] = Q_k(i) . h_e + beta_k(i)
+//   its dE/dd term = sum_k u_k(e) Q_k(i) . h'_e
+// with Q_k(i) = W2[2H:3H]^T dE/dXt_{v_k}(i) and beta_k(i) = b2[2H:3H] .
+// dE/dXt_{v_k}(i) precomputed per atom (vq_kernel).  So GEMM2 computes
+// chunks 0 and 1 only, and GEMM3 multiplies the Q rows of the tile's
+// receivers (rows 3 r + k, 21 receivers per round) with the same [H; H']
+// tile: its outputs are already summed over channels.
 //
 // TMEM (512 columns): [0,128) the lo halves of W2 chunks 0-1 (shared A
-// operands); pipeline p owns [128 + 192 p, 320 + 192 p): chunk g at
+// operands); pipeline p owns [128 + 192 p, 320 + 192 p): chunk g (0, 1) at
 // + 64 g with f in its first 32 columns and f' in the next 32; GEMM1's
-// [z | z'] output aliases chunk 2 until epilogue 1 has read it.
+// [z | z'] output at + 128 until epilogue 1 has read it, then GEMM3's
+// [Q h | Q h'].
 //
 // Epilogue 2 roles: warp (q, h) of a pipeline reads TMEM lane quarter q
 // (channels 32q..32q+31) and handles two feature components of every edge
 // of the tile: h = 0 the scalar and v_x, h = 1 v_y and v_z.  Node adjoints
 // are gathered from the sender side (exact: f(d_ab) = f(d_ba)) and summed per
-// receiver in registers; each thread adds its two components' shares of
-// dE/dd before the cross-lane reduction.  dE/du_k needs only the receiver's
-// v_k adjoint and phi_v2: warp (q, 0) reduces du_x and du_y, warp (q, 1)
-// du_z, so both warps reduce the same number of values per edge.
+// receiver in registers; each thread's share of the remaining dE/dd terms
+// is reduced across lanes (one value per edge).  Epilogue 3: the threads
+// owning GEMM3's rows (warps of quarters 0 and 1) scatter dE/du and the
+// u-term of dE/dd of their receiver's edges.
 // Padding edges of a partial tile get h = h' = 0 and a zero bias fill, so
 // their filter is exactly zero and every gather runs unpredicated (padding
 // gathers read row 0).
 constexpr int PN = 32;                               // edges per reverse tile
 constexpr uint32_t P_HH = 2 * b_block(2 * PN);       // one half (hi or lo) of a [H; H'] tile: 16 KB
+constexpr int QR = 21;                               // receivers per GEMM3 round (rows 3 r + k < 64)
+constexpr uint32_t QT_HALF = 8 * 2048;               // one half (hi or lo) of a Q tile: 64 rows x K 128
 constexpr uint32_t R_SB_US = 0;
 constexpr uint32_t R_SB_SRC = R_SB_US + PN * 16;
 constexpr uint32_t R_SB_RCV = R_SB_SRC + PN * 4;
@@ -821,19 +844,26 @@ constexpr uint32_t R_SB_CHG = R_SB_UC + 3 * PN * 4;
 constexpr uint32_t R_SB_EACC = R_SB_CHG + 16;
 constexpr uint32_t R_SB_BYTES = R_SB_EACC + PN * 16;
 constexpr uint32_t R_OFF_W1 = 0;
-constexpr uint32_t R_OFF_W2H = R_OFF_W1 + W1_BYTES;
-constexpr uint32_t R_OFF_H = align1k(R_OFF_W2H + W2_HALF);   // pipeline p's [H; H'] tile at + 2 P_HH p
-constexpr uint32_t R_OFF_W2L = align1k(R_OFF_H + 4 * P_HH);
-constexpr uint32_t R_OFF_SB = R_OFF_W2L + W2L_BYTES;        // [pipeline][buffer] edge arrays
+constexpr uint32_t R_OFF_W2H = R_OFF_W1 + W1_BYTES;           // hi tiles of W2 chunks 0-1
+constexpr uint32_t R_OFF_H = align1k(R_OFF_W2H + 16 * A_TILE);  // pipeline p's [H; H'] tile at + 2 P_HH p
+constexpr uint32_t R_OFF_Q = align1k(R_OFF_H + 4 * P_HH);       // pipeline p's Q tile (hi, lo) at + 2 QT_HALF p
+constexpr uint32_t R_OFF_SB = R_OFF_Q + 4 * QT_HALF;            // [pipeline][buffer] edge arrays
 constexpr uint32_t R_OFF_B1 = R_OFF_SB + 4 * R_SB_BYTES;
-constexpr uint32_t R_OFF_B2 = R_OFF_B1 + H * 4;
-constexpr uint32_t R_OFF_RED = R_OFF_B2 + H3 * 4;            // [pipeline][warp][edge][3] partial sums
-constexpr uint32_t R_RED_FLOATS = 8 * PN * 3;
+constexpr uint32_t R_OFF_B2 = R_OFF_B1 + H * 4;                // b2 of chunks 0-1
+constexpr uint32_t R_OFF_RED = R_OFF_B2 + 2 * H * 4;           // [pipeline] per-edge partial sums
+constexpr uint32_t R_RED_DU = 8 * PN;                          // red: [8 warps][PN] dE/dd shares,
+constexpr uint32_t R_RED_DDU = R_RED_DU + 3 * PN;              //      [3][PN] dE/du_k, [3][PN] u_k terms of dE/dd
+constexpr uint32_t R_RED_FLOATS = R_RED_DDU + 3 * PN;
 constexpr uint32_t R_OFF_BAR = R_OFF_RED + 2 * R_RED_FLOATS * 4;
-constexpr uint32_t R_OFF_MISC = R_OFF_BAR + 8 * 8;
+constexpr uint32_t R_OFF_MISC = R_OFF_BAR + 10 * 8;
 constexpr uint32_t R_SMEM = align1k(R_OFF_MISC + 16);
 static_assert(ET_BYTES <= 2 * P_HH, "E tile fits in the H tile's space");
 static_assert(R_SB_EACC % 16 == 0 && R_SB_BYTES % 16 == 0, "edge array alignment");
+// GEMM3 is an M = 128 MMA on a 64-row A tile: its rows 64-127 read the
+// 1 KB after each K-step (the next K-step, the next half or tile, and after
+// the last Q half the edge arrays), results never read back
+static_assert(4 * R_SB_BYTES >= 1024, "bytes behind the last Q half");
+static_assert(3 * QR <= 64, "Q rows of a round");
 static_assert(R_SMEM <= 232448, "reverse kernel shared memory");
 
 // Sum 4 per-lane values over the 32 lanes of a warp (reduce-scatter):
@@ -857,12 +887,192 @@ __device__ __forceinline__ float warp_reduce_scatter4(const float (&v)[4], int l
     return w1;
 }
 
+// GEMM3: D (64 TMEM columns at dcol) = Q [H; H']^T, the Q tile at qt (hi
+// half, then lo half QT_HALF bytes later; K-major, no swizzle, rows 0-63,
+// LBO 1024, K-steps 2048 bytes apart), B the split-fp16 [H; H'] tile.
+__device__ __forceinline__ void issue_gemm3(uint32_t tmem, uint32_t dcol, const unsigned char* qt,
+                                            const unsigned char* Hs) {
+    constexpr uint32_t idesc = idesc_f16(2 * PN);
+    constexpr uint64_t DH = (2 * b_block(2 * PN)) >> 4;
+    const uint64_t a0 = sdesc(smem_u32(qt), 1024, 128);
+    const uint64_t b0 = sdesc_b(smem_u32(Hs));
+    const uint32_t d = tmem + dcol;
+#pragma unroll 1
+    for (int s = 0; s < 8; ++s) {
+        const uint64_t bh = b0 + (uint64_t)(b_kstep_off(2 * PN, s) >> 4);
+        const uint64_t ah = a0 + (uint64_t)((2048 * s) >> 4), al = ah + (uint64_t)(QT_HALF >> 4);
+        mma_f16(d, ah, bh, idesc, s > 0 ? 1u : 0u);
+        mma_f16(d, ah, bh + DH, idesc, 1);
+        mma_f16(d, al, bh, idesc, 1);
+    }
+}
+
+// Per-atom Q rows of the reverse kernel (one layer), on the tensor cores:
+// for atom i and k in {x, y, z}, Q_k(i)[h] = sum_c W2[2H + c][h]
+// dE/dXt[i][1 + k][c], stored as split fp16 (128 hi, then 128 lo), and
+// beta_k(i) = sum_c b2[2H + c] dE/dXt[i][1 + k][c].  Persistent, one CTA per
+// SM, 64-atom tiles: B = the tile's 192 rows (atom, k) of dE/dXt_v (K = 128
+// channels, split fp16, 128-byte swizzle), A = the packed transpose of W2's
+// third chunk (resident), D = Q^T in TMEM (lane = hidden unit, column = row);
+// the epilogue thread of hidden unit h writes its values of 48 rows.  Two
+// CTAs per SM, 32-atom tiles.
+constexpr int VQ_TA = 32, VQ_TR = 3 * VQ_TA, VQ_NT = 256;
+constexpr uint32_t VQ_BH = 2 * b_block(VQ_TR);                 // one half of the B tile (K = 128)
+constexpr uint32_t VQ_OFF_A = 0;                               // 8 K-step pairs, 64 KB
+constexpr uint32_t VQ_OFF_B = VQ_OFF_A + 8 * A_PAIR;
+constexpr uint32_t VQ_OFF_BAR = VQ_OFF_B + 2 * VQ_BH;
+constexpr uint32_t VQ_SMEM = align1k(VQ_OFF_BAR + 32);
+static_assert(VQ_SMEM <= 232448, "vq shared memory");
+
+__global__ void __launch_bounds__(VQ_NT, 2) vq_tc_kernel(const float* __restrict__ P, LayerOffsets lo,
+                                                        const float* __restrict__ xtbar, int n_atoms,
+                                                        unsigned char* __restrict__ qs, float* __restrict__ qb,
+                                                        Status* st) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char* As = smem + VQ_OFF_A;
+    unsigned char* Bs = smem + VQ_OFF_B;
+    uint64_t* a_bar = reinterpret_cast<uint64_t*>(smem + VQ_OFF_BAR);
+    uint64_t* mma_bar = a_bar + 1;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + VQ_OFF_BAR + 16);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + VQ_OFF_BAR + 20);
+    pdl_wait();
+    if (st->code != 0) return;
+    const int t = threadIdx.x, w = t >> 5, lane = t & 31;
+    if (w == 0) {
+        tmem_alloc(tslot, 128);
+        tmem_relinquish();
+    }
+    if (t == 0) {
+        mbar_init(a_bar, 1);
+        mbar_init(mma_bar, 1);
+        fence_mbar_init();
+        *abort_flag = 0;
+    }
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tmem = *tslot;
+    pdl_trigger();   // after the TMEM allocation
+    if (t == 0) {
+        const unsigned char* src = reinterpret_cast<const unsigned char*>(P + lo.w2q_tc);
+        mbar_expect_tx(a_bar, 8 * A_PAIR);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) bulk_g2s(As + i * 2 * A_PAIR, src + i * 2 * A_PAIR, 2 * A_PAIR, a_bar);
+    }
+    float4 bb;   // b2[2H + 4 lane .. 4 lane + 3]
+    bb = reinterpret_cast<const float4*>(P + lo.b2 + 2 * H)[lane];
+    const int q = w & 3, ch = w >> 2;       // epilogue: lane quarter q, column half ch
+    const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
+    const int h = 32 * q + lane;
+    uint32_t phase = 0;
+    bool a_ready = false;
+    const int ntiles = (n_atoms + VQ_TA - 1) / VQ_TA;
+    for (int tile = blockIdx.x; tile < ntiles && !*abort_flag; tile += gridDim.x) {
+        const int a0 = tile * VQ_TA;
+        // B tile: warp w builds rows w, w + 8, ..., w + 88 (all loads issued
+        // first); lane takes channels 4 lane .. 4 lane + 3; beta by warp sums
+        {
+            float4 x[12];
+#pragma unroll
+            for (int u = 0; u < 12; ++u) {
+                const int row = w + 8 * u, atom = a0 + row / 3;
+                x[u] = atom < n_atoms ? reinterpret_cast<const float4*>(xtbar + ((int64_t)atom * 4 + 1 + row % 3) * H)[lane]
+                                      : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+#pragma unroll
+            for (int u = 0; u < 12; ++u) {
+                const int row = w + 8 * u, atom = a0 + row / 3;
+                __half2 h0, l0, h1, l1;
+                split2(x[u].x, x[u].y, h0, l0);
+                split2(x[u].z, x[u].w, h1, l1);
+                const uint32_t o = b_off(VQ_TR, row, 4 * lane);
+                uint2 hv, lv;
+                hv.x = *reinterpret_cast<uint32_t*>(&h0);
+                hv.y = *reinterpret_cast<uint32_t*>(&h1);
+                lv.x = *reinterpret_cast<uint32_t*>(&l0);
+                lv.y = *reinterpret_cast<uint32_t*>(&l1);
+                *reinterpret_cast<uint2*>(Bs + o) = hv;
+                *reinterpret_cast<uint2*>(Bs + VQ_BH + o) = lv;
+                float b = fmaf(bb.x, x[u].x, fmaf(bb.y, x[u].y, fmaf(bb.z, x[u].z, bb.w * x[u].w)));
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) b += __shfl_xor_sync(0xffffffffu, b, off);
+                if (lane == 0 && atom < n_atoms) qb[(int64_t)a0 * 3 + row] = b;
+            }
+        }
+        fence_async_smem();
+        fence_before_sync();
+        __syncthreads();
+        if (t == 0) {   // Q^T = W2q^T B^T: 8 K-steps x (hi hi, hi lo, lo hi)
+            fence_after_sync();
+            if (!a_ready) {
+                if (!mbar_wait(a_bar, 0, WAIT_BUDGET)) {
+                    set_status(st, MLFF_ERR_TIMEOUT, 40);
+                    *abort_flag = 1;
+                }
+                a_ready = true;
+            }
+            constexpr uint32_t idesc = idesc_f16(VQ_TR);
+            const uint64_t b0 = sdesc_b(smem_u32(Bs));
+#pragma unroll 1
+            for (int s = 0; s < 8; ++s) {
+                const uint64_t ah = sdesc(smem_u32(As + s * A_PAIR), A_LBO, A_SBO);
+                const uint64_t al = sdesc(smem_u32(As + s * A_PAIR + A_TILE), A_LBO, A_SBO);
+                const uint64_t bh = b0 + (uint64_t)(b_kstep_off(VQ_TR, s) >> 4);
+                mma_f16(tmem, ah, bh, idesc, s > 0 ? 1u : 0u);
+                mma_f16(tmem, ah, bh + (VQ_BH >> 4), idesc, 1);
+                mma_f16(tmem, al, bh, idesc, 1);
+            }
+            mma_commit(mma_bar);
+        }
+        if (w == 0) {
+            __syncwarp();
+            if (!mbar_wait(mma_bar, phase, WAIT_BUDGET)) {
+                set_status(st, MLFF_ERR_TIMEOUT, 41);
+                *abort_flag = 1;
+            }
+        }
+        phase ^= 1;
+        fence_before_sync();
+        __syncthreads();
+        fence_after_sync();
+        // epilogue: thread of hidden unit h, rows 48 ch .. 48 ch + 47
+        {
+            float v[48];
+            tmem_ld32(lane_base + 48 * ch, *reinterpret_cast<float(*)[32]>(v));
+            tmem_ld16(lane_base + 48 * ch + 32, *reinterpret_cast<float(*)[16]>(v + 32));
+            tmem_ld_wait();
+            const int nrow = min(48, 3 * (n_atoms - a0) - 48 * ch);
+#pragma unroll
+            for (int i = 0; i < 48; ++i) {
+                if (i >= nrow) break;
+                __half hi, lo;
+                split_f16(v[i], hi, lo);
+                __half* dst = reinterpret_cast<__half*>(qs + ((int64_t)a0 * 3 + 48 * ch + i) * 2 * (2 * H));
+                dst[h] = hi;
+                dst[H + h] = lo;
+            }
+        }
+        fence_before_sync();
+        __syncthreads();   // D and the B tile are free for the next tile
+        fence_after_sync();
+    }
+    // drain: the weight copy and the last MMAs are complete before the TMEM
+    // is freed (a wait on the phase before the current one returns at once)
+    if (t == 0) {
+        if (!mbar_wait(a_bar, 0, WAIT_BUDGET)) set_status(st, MLFF_ERR_TIMEOUT, 42);
+        if (!mbar_wait(mma_bar, phase ^ 1, WAIT_BUDGET)) set_status(st, MLFF_ERR_TIMEOUT, 43);
+    }
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    if (w == 0) tmem_dealloc(tmem, 128);
+}
+
 __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const unsigned char* __restrict__ w1g,
                                                             const unsigned char* __restrict__ w2g) {
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* w1s = smem + R_OFF_W1;
     unsigned char* w2h = smem + R_OFF_W2H;
-    unsigned char* w2l = smem + R_OFF_W2L;        // resident lo tiles of W2 chunk 2
     float* b1s = reinterpret_cast<float*>(smem + R_OFF_B1);
     float* b2s = reinterpret_cast<float*>(smem + R_OFF_B2);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + R_OFF_BAR);
@@ -884,9 +1094,10 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
         mbar_init(w2h_bar, 1);
         mbar_init(never_bar, 1);
         for (int p = 0; p < 2; ++p) {
-            mbar_init(bars + 2 + 3 * p, 1);   // GEMM1
-            mbar_init(bars + 3 + 3 * p, 1);   // E tile
-            mbar_init(bars + 4 + 3 * p, 3);   // GEMM2: one commit per chunk issuer
+            mbar_init(bars + 2 + 4 * p, 1);   // GEMM1
+            mbar_init(bars + 3 + 4 * p, 1);   // E tile
+            mbar_init(bars + 4 + 4 * p, 2);   // GEMM2: one commit per chunk issuer
+            mbar_init(bars + 5 + 4 * p, 1);   // GEMM3
         }
         fence_mbar_init();
         *abort_flag = 0;
@@ -894,13 +1105,17 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
     for (int i = t; i < (int)(W1_BYTES / 16); i += NT)
         reinterpret_cast<uint4*>(w1s)[i] = reinterpret_cast<const uint4*>(w1g)[i];
     if (t < H) b1s[t] = a.P[a.lo.b1 + t];
-    for (int i = t; i < H3; i += NT) b2s[i] = a.P[a.lo.b2 + i];
+    for (int i = t; i < 2 * H; i += NT) b2s[i] = a.P[a.lo.b2 + i];
     fence_async_smem();
     fence_before_sync();
     __syncthreads();
     fence_after_sync();
     const uint32_t tmem = *tslot;
-    if (t == 32) load_w2_resident(w2h, w2l, w2g, w2h_bar);
+    if (t == 32) {   // hi tiles of W2 chunks 0-1 (the first 16 tiles of the packed hi half)
+        mbar_expect_tx(w2h_bar, 16 * A_TILE);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) bulk_g2s(w2h + i * 4 * A_TILE, w2g + i * 4 * A_TILE, 4 * A_TILE, w2h_bar);
+    }
     const int q = w & 3;
     const int c = 32 * q + lane;
     const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
@@ -916,12 +1131,13 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
     const uint32_t TB = 128 + 192 * pp;             // the pipeline's TMEM columns
     unsigned char* Hs = smem + R_OFF_H + pp * 2 * P_HH;   // [H; H'] hi, then lo
     unsigned char* Es = Hs;                         // [E; E'] tile (bulk-copied) before H is written
-    uint64_t* mma_bar = bars + 2 + 3 * pp;
-    uint64_t* e_bar = bars + 3 + 3 * pp;
-    uint64_t* g2_bar = bars + 4 + 3 * pp;
+    unsigned char* qt = smem + R_OFF_Q + pp * 2 * QT_HALF;   // Q tile hi, then lo
+    uint64_t* mma_bar = bars + 2 + 4 * pp;
+    uint64_t* e_bar = bars + 3 + 4 * pp;
+    uint64_t* g2_bar = bars + 4 + 4 * pp;
+    uint64_t* g3_bar = bars + 5 + 4 * pp;
     float* red = reinterpret_cast<float*>(smem + R_OFF_RED) + pp * R_RED_FLOATS;
     unsigned char* sbase = smem + R_OFF_SB + 2 * pp * R_SB_BYTES;
-    const int rs_idx = reduce_scatter8_index(lane);
     const int rs4_idx = ((lane >> 4) & 1) * 2 + ((lane >> 3) & 1);
     // components 2 hh and 2 hh + 1; the second sits H floats after the first
     const int fidx0 = 2 * hh * H + c;
@@ -929,7 +1145,7 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
     const float* xx = a.X + fidx0;
     float* out = a.xbar + fidx0;
 
-    uint32_t mma_phase = 0, g2_phase = 0;   // GEMM1 / GEMM2 barrier phases
+    uint32_t mma_phase = 0, g2_phase = 0, g3_phase = 0;   // GEMM1 / GEMM2 / GEMM3 barrier phases
     uint32_t e_phase = 0, e_issued = 0;     // E-tile copies: barrier phase, copies issued (thread tp 32)
     bool w2h_ready = false;                 // (GEMM2 issuers)
     bool aborted = false;
@@ -973,6 +1189,24 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
             const int* soff = reinterpret_cast<const int*>(sb + R_SB_SOFF);
             const int* roff = reinterpret_cast<const int*>(sb + R_SB_ROFF);
             const float* uc = reinterpret_cast<const float*>(sb + R_SB_UC);
+            const uint32_t chw = *reinterpret_cast<const uint32_t*>(sb + R_SB_CHG);
+            // the tile's receivers: local receiver r starts at edge r_first(r)
+            const uint32_t starts = chw & ~1u;
+            const int nrcv = 1 + __popc(starts);
+            auto r_first = [&](int r) { return r == 0 ? 0 : (int)__fns(starts, 0, r); };
+            // Q rows of receivers QR b .. QR b + 20 into the Q tile (row 3 r' + k)
+            auto fill_q = [&](int b) {
+                const int nrow = 3 * min(QR, nrcv - QR * b);
+                for (int i = tp; i < 32 * nrow; i += PT) {
+                    const int m = i >> 5, j = i & 15, hl = (i >> 4) & 1;
+                    const int atom = rcv_s[r_first(QR * b + m / 3)];
+                    const unsigned char* src = a.qs + (((int64_t)atom * 3 + m % 3) * 2 + hl) * (2 * H) + 16 * j;
+                    cp_async16(qt + hl * QT_HALF + (j >> 1) * 2048 + (j & 1) * 1024 + (m >> 3) * 128 + (m & 7) * 16,
+                               src);
+                }
+                cp_async_commit();
+            };
+            fill_q(0);
             if (tp == 0) {   // [z; z']^T = W1 [e; e']^T on the bulk-copied tile
                 if (!mbar_wait(e_bar, e_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 18);
                 fence_after_sync();
@@ -1030,19 +1264,15 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                     }
                 }
                 // f = W2 h accumulates onto b2 (0 for padding edges), f' = W2 h'
-                // onto 0: this warp refills the chunk-2 cells it has just read
-                // and chunk hh (f: 32 columns, f': 32 columns)
+                // onto 0: this warp refills chunk hh (f: 32 columns, f': 32
+                // columns); GEMM3 overwrites the [z | z'] columns
                 float bv[16], bz[16];
-                const float b2c = b2s[2 * H + c], bch = b2s[hh * H + c];
+                const float bch = b2s[hh * H + c];
 #pragma unroll
                 for (int i = 0; i < 16; ++i) {
-                    bv[i] = i < nv ? b2c : 0.0f;
+                    bv[i] = i < n ? bch : 0.0f;
                     bz[i] = 0.0f;
                 }
-                tmem_st16(lane_base + TB + 128 + col, bv);
-                tmem_st16(lane_base + TB + 128 + PN + col, bz);
-#pragma unroll
-                for (int i = 0; i < 16; ++i) bv[i] = i < n ? bch : 0.0f;
                 tmem_st16(lane_base + TB + 64 * hh, bv);
 #pragma unroll
                 for (int i = 0; i < 16; ++i) bv[i] = 16 + i < n ? bch : 0.0f;
@@ -1051,6 +1281,7 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                 tmem_st16(lane_base + TB + 64 * hh + PN + 16, bz);
                 tmem_st_wait();
             }
+            cp_async_wait_all();   // this thread's Q-tile rows
             fence_async_smem();
             fence_before_sync();
             pipe_sync(pp);
@@ -1058,11 +1289,10 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
             // GEMM2 runs: the senders' dE/dXt and X rows and the dE/dXt row of
             // the block's first receiver (edges where another receiver starts
             // inside the block reload theirs in epilogue 2)
-            const uint32_t chw = *reinterpret_cast<const uint32_t*>(sb + R_SB_CHG);
-            float tba0[4], tba1[4], xba0[4], xba1[4], ra0, ra1, ra2;
-            float tbb0[4], tbb1[4], xbb0[4], xbb1[4], rb0, rb1, rb2;
+            float tba0[4], tba1[4], xba0[4], xba1[4], ra0, ra1;
+            float tbb0[4], tbb1[4], xbb0[4], xbb1[4], rb0, rb1;
             auto gather4 = [&](float (&tb0)[4], float (&tb1)[4], float (&xb0)[4], float (&xb1)[4], float& r0,
-                               float& r1, float& r2, int col) {
+                               float& r1, int col) {
                 const int4 so = *reinterpret_cast<const int4*>(soff + col);
                 const int sv[4] = {so.x, so.y, so.z, so.w};
 #pragma unroll
@@ -1075,26 +1305,82 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                 const int ro = roff[col];
                 r0 = __ldg(xtb + ro);
                 r1 = __ldg(xtb + ro + H);
-                r2 = hh == 0 ? __ldg(xtb + ro + 2 * H) : 0.f;   // v_y, for dE/du_y
             };
-            gather4(tba0, tba1, xba0, xba1, ra0, ra1, ra2, 0);
-            if (4 < n) gather4(tbb0, tbb1, xbb0, xbb1, rb0, rb1, rb2, 4);
-            if (wl < 3 && lane == 0) {   // [f; f']^T = W2 [h; h']^T, chunk wl issued by warp wl
+            gather4(tba0, tba1, xba0, xba1, ra0, ra1, 0);
+            if (4 < n) gather4(tbb0, tbb1, xbb0, xbb1, rb0, rb1, 4);
+            if (wl < 3 && lane == 0) {   // GEMM2 chunks 0, 1 (warps 0, 1), GEMM3 (warp 2)
                 fence_after_sync();
-                if (!w2h_ready) {
-                    if (!mbar_wait(w2h_bar, 0, WAIT_BUDGET)) signal_timeout(a, abort_flag, 16);
-                    w2h_ready = true;
+                if (wl < 2) {
+                    if (!w2h_ready) {
+                        if (!mbar_wait(w2h_bar, 0, WAIT_BUDGET)) signal_timeout(a, abort_flag, 16);
+                        w2h_ready = true;
+                    }
+                    issue_gemm2_chunk<2 * PN>(wl, tmem, TB + 64 * wl, w2h, w2h, Hs);   // (chunk 2's lo tile unused)
+                    mma_commit(g2_bar);
+                } else {
+                    issue_gemm3(tmem, TB + 128, qt, Hs);
+                    mma_commit(g3_bar);
                 }
-                issue_gemm2_chunk<2 * PN>(wl, tmem, TB + 64 * wl, w2h, w2l, Hs);
-                mma_commit(g2_bar);
             }
             if (wl < 3) __syncwarp();   // lanes 1-31 of the issuing warps wait here, not in a spin loop
             if (wl == 0 && !mbar_wait(g2_bar, g2_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 14);
+            if (wl == 3 && !mbar_wait(g3_bar, g3_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 30);
             g2_phase ^= 1;
+            g3_phase ^= 1;
             fence_before_sync();
             // the abort decision is the same for every thread of the pipeline
             const bool abort_now = pipe_sync_or(pp, *abort_flag != 0);
             fence_after_sync();
+            // epilogue 3 (warps of lane quarters 0-1): GEMM3 row l = 3 r' + kk is
+            // receiver QR b + r', component kk; its columns are the tile's edges
+            // ([Q h | Q h']); the row owner writes the values of its receiver's edges
+            auto epi3 = [&](int b) {
+                if (q >= 2) return;
+                const int l = 32 * q + lane, r = QR * b + l / 3, kk = l % 3;
+                const bool on = l < 3 * QR && r < nrcv;
+                const int s0 = on ? r_first(r) : 0;
+                const int s1 = on ? (r + 1 < nrcv ? r_first(r + 1) : n) : 0;
+                float v[32];
+                tmem_ld32(lane_base + TB + 128 + 32 * hh, v);   // hh 0: Q h, hh 1: Q h'
+                tmem_ld_wait();
+                if (hh == 0) {   // dE/du_kk = Q h + beta
+                    const float beta = on ? __ldg(a.qb + (int64_t)rcv_s[s0] * 3 + kk) : 0.f;
+                    float* dst = red + R_RED_DU + kk * PN;
+#pragma unroll
+                    for (int i = 0; i < 32; ++i)
+                        if (i >= s0 && i < s1) dst[i] = v[i] + beta;
+                } else {         // u_kk (Q h') of dE/dd
+                    float* dst = red + R_RED_DDU + kk * PN;
+                    const float* u = uc + kk * PN;
+#pragma unroll
+                    for (int i = 0; i < 32; ++i)
+                        if (i >= s0 && i < s1) dst[i] = u[i] * v[i];
+                }
+            };
+            epi3(0);
+            const int nround = (nrcv + QR - 1) / QR;
+            for (int b = 1; b < nround && !abort_now; ++b) {   // tiles of more than 21 receivers
+                tmem_ld_wait();
+                fence_before_sync();
+                pipe_sync(pp);   // round b - 1's rows are read: refill the Q tile
+                fill_q(b);
+                cp_async_wait_all();
+                fence_async_smem();
+                fence_before_sync();
+                pipe_sync(pp);
+                if (wl == 2 && lane == 0) {
+                    fence_after_sync();
+                    issue_gemm3(tmem, TB + 128, qt, Hs);
+                    mma_commit(g3_bar);
+                }
+                if (wl == 2) __syncwarp();
+                if (wl == 3 && !mbar_wait(g3_bar, g3_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 31);
+                g3_phase ^= 1;
+                fence_before_sync();
+                pipe_sync(pp);
+                fence_after_sync();
+                epi3(b);
+            }
             // the H tile is free: the next tile's [E; E'] tile and edge arrays
             // arrive while epilogue 2 runs
             const bool more = k + 1 < ntl && !abort_now;
@@ -1107,54 +1393,39 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                 }
             }
             if (wl == 1) __syncwarp();
-            {   // epilogue 2 over 4-edge blocks, the next block's gathers in flight.
-                // Warp (q, 0) owns the scalar and v_x: dE/dd share, dE/du_x and
-                // dE/du_y; warp (q, 1) owns v_y and v_z: dE/dd share and dE/du_z
-                // (both halves then do the same amount of work)
+            {   // epilogue 2 over 4-edge blocks, the next block's gathers in flight
                 // (compiled once per warp half: hc is std::integral_constant<int, hh>)
                 auto process4 = [&](auto hc, const float (&tb0)[4], const float (&tb1)[4], const float (&xb0)[4],
-                                    const float (&xb1)[4], float r0, float r1, float r2, int col) {
+                                    const float (&xb1)[4], float r0, float r1, int col) {
                     constexpr int HH = decltype(hc)::value;
-                    float fa[4], da[4], f1[4], d1[4], f2[4], d2[4];
+                    float fa[4], da[4], f1[4], d1[4];
                     if (HH == 0) {
                         tmem_ld4(lane_base + TB + col, fa);        // phi_s (bias included)
                         tmem_ld4(lane_base + TB + PN + col, da);   // dphi_s / dd
                     }
                     tmem_ld4(lane_base + TB + 64 + col, f1);       // phi_v1
                     tmem_ld4(lane_base + TB + 64 + PN + col, d1);
-                    tmem_ld4(lane_base + TB + 128 + col, f2);      // phi_v2
-                    tmem_ld4(lane_base + TB + 128 + PN + col, d2);
                     const uint32_t m = (chw >> col) & 0xFu;
                     tmem_ld_wait();
                     if (HH != 0) {
 #pragma unroll
-                        for (int i = 0; i < 4; ++i) {
-                            fa[i] = f1[i];
-                            da[i] = d1[i];
-                        }
+                        for (int i = 0; i < 4; ++i) fa[i] = f1[i];
                     }
-                    // this thread's shares of dE/dd and dE/du of edge i, given the
-                    // receiver's dE/dXt rows t0, t1 (t2: v_y, warps (q, 0) only); the
-                    // same expressions on both branches below (a block's branch depends
-                    // on where the tile starts)
-                    float pv[8], p2[4];
-                    auto edge_terms = [&](int i, float t0, float t1, float t2) {
-                        if (HH == 0) {   // scalar and v_x; dE/du_x, dE/du_y
-                            pv[i] = fmaf(t0 * xb0[i], da[i], t1 * fmaf(xb1[i], d1[i], uc[col + i] * d2[i]));
-                            pv[4 + i] = t1 * f2[i];
-                            p2[i] = t2 * f2[i];
-                        } else {         // v_y and v_z; dE/du_z
-                            pv[i] = fmaf(t0, fmaf(xb0[i], d1[i], uc[PN + col + i] * d2[i]),
-                                         t1 * fmaf(xb1[i], d1[i], uc[2 * PN + col + i] * d2[i]));
-                            pv[4 + i] = t1 * f2[i];
-                        }
+                    // this thread's share of dE/dd of edge i (sender features and
+                    // phi_s', phi_v1'), given the receiver's dE/dXt rows t0, t1;
+                    // the same expressions on both branches below (a block's branch
+                    // depends on where the tile starts)
+                    float pv[4];
+                    auto edge_term = [&](int i, float t0, float t1) {
+                        if (HH == 0) pv[i] = fmaf(t0 * xb0[i], da[i], t1 * xb1[i] * d1[i]);
+                        else pv[i] = fmaf(t0 * xb0[i], d1[i], t1 * xb1[i] * d1[i]);
                     };
                     if (m == 0) {   // one receiver for the whole block, no sum finishes here
 #pragma unroll
                         for (int i = 0; i < 4; ++i) {
                             acc0 = fmaf(tb0[i], fa[i], acc0);
                             acc1 = fmaf(tb1[i], f1[i], acc1);
-                            edge_terms(i, r0, r1, r2);
+                            edge_term(i, r0, r1);
                         }
                     } else {   // a receiver starts in this block: store the finished sums
 #pragma unroll
@@ -1171,28 +1442,23 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                                     const int ro = roff[col + i];
                                     r0 = __ldg(xtb + ro);
                                     r1 = __ldg(xtb + ro + H);
-                                    if (HH == 0) r2 = __ldg(xtb + ro + 2 * H);
                                 }
                             }
                             acc0 = fmaf(tb0[i], fa[i], acc0);
                             acc1 = fmaf(tb1[i], f1[i], acc1);
-                            edge_terms(i, r0, r1, r2);
+                            edge_term(i, r0, r1);
                         }
                     }
-                    if (HH == 0) {
-                        const float s4 = warp_reduce_scatter4(p2, lane);
-                        if ((lane & 7) == 0) red[(wl * PN + col + rs4_idx) * 3 + 2] = s4;
-                    }
-                    const float s8 = warp_reduce_scatter8(pv, lane);
-                    if ((lane & 3) == 0) red[(wl * PN + col + (rs_idx & 3)) * 3 + (rs_idx >> 2)] = s8;
+                    const float s4 = warp_reduce_scatter4(pv, lane);
+                    if ((lane & 7) == 0) red[wl * PN + col + rs4_idx] = s4;
                 };
                 auto blocks = [&](auto hc) {
                     for (int col = 0; col < n; col += 8) {   // blocks col and col + 4 are in flight
-                        process4(hc, tba0, tba1, xba0, xba1, ra0, ra1, ra2, col);
+                        process4(hc, tba0, tba1, xba0, xba1, ra0, ra1, col);
                         if (col + 4 >= n) break;
-                        if (col + 8 < n) gather4(tba0, tba1, xba0, xba1, ra0, ra1, ra2, col + 8);
-                        process4(hc, tbb0, tbb1, xbb0, xbb1, rb0, rb1, rb2, col + 4);
-                        if (col + 12 < n) gather4(tbb0, tbb1, xbb0, xbb1, rb0, rb1, rb2, col + 12);
+                        if (col + 8 < n) gather4(tba0, tba1, xba0, xba1, ra0, ra1, col + 8);
+                        process4(hc, tbb0, tbb1, xbb0, xbb1, rb0, rb1, col + 4);
+                        if (col + 12 < n) gather4(tbb0, tbb1, xbb0, xbb1, rb0, rb1, col + 12);
                     }
                 };
                 if (hh == 0) blocks(std::integral_constant<int, 0>{});
@@ -1205,29 +1471,21 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
             }
             fence_before_sync();
             pipe_sync(pp);
-            // per-edge sums over the pipeline's 8 warps, fixed order, by its last
-            // warp (warp 0 issues the next tile's GEMM1 meanwhile)
+            // per-edge sums, fixed order, by the pipeline's last warp (warp 0
+            // issues the next tile's GEMM1 meanwhile): dE/dd = the 8 warps'
+            // shares + the three u terms; dE/du from epilogue 3
             const int te = tp - (PT - 32);
             if (te >= 0 && te < n) {
-                const float* rr = red + te * 3;
-                float dd = 0.f, du0 = 0.f, du1 = 0.f, du2 = 0.f;
+                float dd = 0.f;
 #pragma unroll
-                for (int ww = 0; ww < 8; ++ww) {   // warps 0-3: (dd, du_x, du_y), 4-7: (dd, du_z)
-                    const float* rw = rr + ww * PN * 3;
-                    dd += rw[0];
-                    if (ww < 4) {
-                        du0 += rw[1];
-                        du1 += rw[2];
-                    } else {
-                        du2 += rw[1];
-                    }
-                }
+                for (int ww = 0; ww < 8; ++ww) dd += red[ww * PN + te];
+                dd += (red[R_RED_DDU + te] + red[R_RED_DDU + PN + te]) + red[R_RED_DDU + 2 * PN + te];
                 float4 ea = a.eacc_init ? make_float4(0.f, 0.f, 0.f, 0.f)
                                         : reinterpret_cast<const float4*>(sb + R_SB_EACC)[te];
                 ea.x += dd;
-                ea.y += du0;
-                ea.z += du1;
-                ea.w += du2;
+                ea.y += red[R_RED_DU + te];
+                ea.z += red[R_RED_DU + PN + te];
+                ea.w += red[R_RED_DU + 2 * PN + te];
                 a.eacc[t0 + te] = ea;
             }
             if (abort_now) {
@@ -1249,6 +1507,7 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
     if (tp == 0) {
         if (!mbar_wait(mma_bar, mma_phase ^ 1, WAIT_BUDGET)) set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 13);
         if (!mbar_wait(g2_bar, g2_phase ^ 1, WAIT_BUDGET)) set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 15);
+        if (!mbar_wait(g3_bar, g3_phase ^ 1, WAIT_BUDGET)) set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 32);
     }
     if (tp == 32) {
         if (t == 32 && !mbar_wait(w2h_bar, 0, WAIT_BUDGET)) set_status(const_cast<Status*>(a.st), MLFF_ERR_TIMEOUT, 17);
@@ -1261,7 +1520,6 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
     if (w == 0) tmem_dealloc(tmem, 512);
 }
 
-// ------------------------------------------------------------- launchers
 static int tc_grid(int nparts) {
     static int sms = 0;
     if (sms == 0) {
@@ -1300,6 +1558,20 @@ int launch_edge_bwd_tc(const EdgeArgs& a, int layer, cudaStream_t st) {
     const unsigned char* w2 = reinterpret_cast<const unsigned char*>(a.P + a.lo.w2_bf);
     // two pipelines (partitions) per CTA
     MLFF_LAUNCH_PDL("edge_bwd_tc", edge_bwd_tc_kernel, tc_grid((a.nparts + 1) / 2), NT, R_SMEM, st, a, w1, w2);
+    return MLFF_OK;
+}
+
+int launch_vq(const float* P, const LayerOffsets& lo, const float* xtbar, int n_atoms, unsigned char* qs, float* qb,
+              Status* st_word, cudaStream_t st) {
+    static std::once_flag once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(once, [] {
+        attr_err = cudaFuncSetAttribute(vq_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, VQ_SMEM);
+    });
+    if (attr_err != cudaSuccess) return cuda_status(attr_err, "vq_tc smem attribute");
+    const int tiles = (n_atoms + VQ_TA - 1) / VQ_TA;
+    const int grid = std::max(1, std::min(tiles, 2 * num_sms()));
+    MLFF_LAUNCH_PDL("vq_tc", vq_tc_kernel, grid, VQ_NT, VQ_SMEM, st, P, lo, xtbar, n_atoms, qs, qb, st_word);
     return MLFF_OK;
 }
 

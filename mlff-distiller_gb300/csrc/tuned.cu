@@ -298,6 +298,8 @@ __global__ void __launch_bounds__(128) edge_bwd_simt_kernel(EdgeArgs a) {
 
 int launch_edge_fwd_tc(const EdgeArgs& a, int layer, cudaStream_t st);
 int launch_edge_bwd_tc(const EdgeArgs& a, int layer, cudaStream_t st);
+int launch_vq(const float* P, const LayerOffsets& lo, const float* xtbar, int n_atoms, unsigned char* qs, float* qb,
+              Status* st_word, cudaStream_t st);
 int launch_etiles(const EdgeArgs& a, int32_t* base, unsigned char* fwd, unsigned char* rev, cudaStream_t st);
 
 
@@ -417,6 +419,14 @@ int run_tuned(const mlff_dims& d, const float* P, const PackedOffsets& po, const
         a.xbar = xbo;
         a.write_nodes = l > 0 ? 1 : 0;
         a.eacc_init = l == d.n_layers - 1 ? 1 : 0;
+        if (tc) {
+            ProfScope prof(PK_EDGE_BWD_Q, st);
+            a.qs = ws_ptr<unsigned char>(ws, L.qs);
+            a.qb = ws_ptr<float>(ws, L.qb);
+            if ((r = launch_vq(P, po.layer[l], xtb, L.N, ws_ptr<unsigned char>(ws, L.qs), ws_ptr<float>(ws, L.qb),
+                               ws_ptr<Status>(ws, L.status), st)))
+                return r;
+        }
         {
             ProfScope prof(PK_EDGE_BWD, st);   // the reverse edge kernel alone
             if (tc) {

@@ -43,6 +43,8 @@ struct WsLayout {
     size_t etile_base;         // int32 [2][P+1] first E tile of each partition (forward, reverse)
     size_t etile_f;            // forward E tiles: 64 edges x K 32, split fp16, 8 KB each
     size_t etile_b;            // reverse [E; E'] tiles: 32 edges, 64 rows, 8 KB each
+    size_t qs;                 // reverse: per-atom Q rows [N][3][hi, lo][H] fp16 (W2's third chunk^T dE/dXt_v)
+    size_t qb;                 // reverse: per-atom b2 . dE/dXt_v [N][3] float
     int64_t n_etile_f, n_etile_b;
     size_t erbf;               // float [cap][RMAX]
     size_t erbf_d;             // float [cap][RMAX]

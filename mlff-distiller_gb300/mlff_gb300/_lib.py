@@ -52,7 +52,7 @@ EXPORTS = ["mlff_version", "mlff_last_error_string", "mlff_packed_weights_size",
            "mlff_autotune", "mlff_autotune_query", "mlff_autotune_set", "mlff_autotune_reset"]
 
 PROFILE_KINDS = ["neighbors", "edge_fwd", "edge_bwd", "update_fwd", "update_bwd", "readout", "forces",
-                 "plain_gemm", "plain_edge", "other", "md"]
+                 "plain_gemm", "plain_edge", "other", "md", "edge_bwd_q"]
 
 
 class Dims(ctypes.Structure):
