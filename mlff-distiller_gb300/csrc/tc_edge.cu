@@ -437,6 +437,16 @@ __device__ __forceinline__ bool pipe_sync_or(int pp, bool v) {
 __device__ __forceinline__ void pipe_sync_first(int pp, int n) {
     asm volatile("bar.sync %0, %1;" ::"r"(3 + pp), "r"(n) : "memory");
 }
+// The warps that read the TMEM columns the next tile's GEMM1 writes (n
+// threads, warp 0 of the pipeline among them) signal that their reads are
+// done (arrive, no wait); warp 0 waits for them, then issues that GEMM1 while
+// the rest of the pipeline is still in epilogue 2.
+__device__ __forceinline__ void cols_free_arrive(int pp, int n) {
+    asm volatile("bar.arrive %0, %1;" ::"r"(5 + pp), "r"(n) : "memory");
+}
+__device__ __forceinline__ void cols_free_sync(int pp, int n) {
+    asm volatile("bar.sync %0, %1;" ::"r"(5 + pp), "r"(n) : "memory");
+}
 
 // ------------------------------------------------------- forward kernel
 // 64-edge tiles per pipeline: GEMM1 (z = W1 e, N = 64) into the columns of
@@ -551,6 +561,23 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
         fetch_tile_edges(a, tp, QN, t0, nn, reinterpret_cast<float4*>(sbx + Q_SB_US),
                          reinterpret_cast<int*>(sbx + Q_SB_SRC), reinterpret_cast<int*>(sbx + Q_SB_RCV));
     };
+    // z^T = W1 e^T on the E tile at Es into chunk 0's columns, once its copy
+    // has landed (thread tp 0)
+    auto issue_gemm1 = [&]() {
+        if (!mbar_wait(e_bar, e_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 8);
+        fence_after_sync();
+        constexpr uint32_t idesc = idesc_f16(QN);
+#pragma unroll
+        for (int s = 0; s < 2; ++s)
+#pragma unroll
+            for (int pr = 0; pr < 3; ++pr) {
+                const uint32_t ahl = pr == 2 ? 1 : 0, bhl = pr == 1 ? 1 : 0;
+                const uint64_t ad = sdesc(smem_u32(w1s + s * SLAB + ahl * A_TILE), A_LBO, A_SBO);
+                const uint64_t bd = sdesc(smem_u32(Es + bhl * ET_HALF + s * (ET_ROWS * 32)), ET_ROWS * 16, 128);
+                mma_f16(tmem + TB, ad, bd, idesc, (s | pr) != 0);
+            }
+        mma_commit(mma_bar);
+    };
     for (int p = 2 * blockIdx.x + pp; p < a.nparts && !aborted; p += 2 * gridDim.x) {
         const int j0 = a.part[p], j1 = a.part[p + 1];
         if (j0 >= j1) continue;
@@ -582,21 +609,9 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
             const int* soff = reinterpret_cast<const int*>(sb + Q_SB_SOFF);
             const float* uc = reinterpret_cast<const float*>(sb + Q_SB_UC);
             const uint32_t* chg = reinterpret_cast<const uint32_t*>(sb + Q_SB_CHG);
-            if (tp == 0) {   // z^T = W1 e^T on the bulk-copied tile, into chunk 0's columns
-                if (!mbar_wait(e_bar, e_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 8);
-                fence_after_sync();
-                constexpr uint32_t idesc = idesc_f16(QN);
-#pragma unroll
-                for (int s = 0; s < 2; ++s)
-#pragma unroll
-                    for (int pr = 0; pr < 3; ++pr) {
-                        const uint32_t ahl = pr == 2 ? 1 : 0, bhl = pr == 1 ? 1 : 0;
-                        const uint64_t ad = sdesc(smem_u32(w1s + s * SLAB + ahl * A_TILE), A_LBO, A_SBO);
-                        const uint64_t bd = sdesc(smem_u32(Es + bhl * ET_HALF + s * (ET_ROWS * 32)), ET_ROWS * 16, 128);
-                        mma_f16(tmem + TB, ad, bd, idesc, (s | pr) != 0);
-                    }
-                mma_commit(mma_bar);
-            }
+            // z^T = W1 e^T on the bulk-copied tile, into chunk 0's columns (read
+            // by the scalar warps until the end of the previous tile's epilogue 2)
+            if (tp == 0) issue_gemm1();
             e_phase ^= 1;
             if (wl == 0) {
                 __syncwarp();
@@ -1160,6 +1175,23 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                          reinterpret_cast<int*>(sbx + R_SB_SRC), reinterpret_cast<int*>(sbx + R_SB_RCV),
                          a.eacc_init ? nullptr : reinterpret_cast<float4*>(sbx + R_SB_EACC));
     };
+    // [z; z']^T = W1 [e; e']^T on the [E; E'] tile at Es into the [z | z']
+    // columns, once its copy has landed (thread tp 0)
+    auto issue_gemm1 = [&]() {
+        if (!mbar_wait(e_bar, e_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 18);
+        fence_after_sync();
+        constexpr uint32_t idesc = idesc_f16(2 * PN);
+#pragma unroll
+        for (int s = 0; s < 2; ++s)
+#pragma unroll
+            for (int pr = 0; pr < 3; ++pr) {
+                const uint32_t ahl = pr == 2 ? 1 : 0, bhl = pr == 1 ? 1 : 0;
+                const uint64_t ad = sdesc(smem_u32(w1s + s * SLAB + ahl * A_TILE), A_LBO, A_SBO);
+                const uint64_t bd = sdesc(smem_u32(Es + bhl * ET_HALF + s * (ET_ROWS * 32)), ET_ROWS * 16, 128);
+                mma_f16(tmem + TB + 128, ad, bd, idesc, (s | pr) != 0);
+            }
+        mma_commit(mma_bar);
+    };
     for (int p = 2 * blockIdx.x + pp; p < a.nparts && !aborted; p += 2 * gridDim.x) {
         const int j0 = a.part[p], j1 = a.part[p + 1];
         if (j0 >= j1) continue;
@@ -1207,21 +1239,10 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                 cp_async_commit();
             };
             fill_q(0);
-            if (tp == 0) {   // [z; z']^T = W1 [e; e']^T on the bulk-copied tile
-                if (!mbar_wait(e_bar, e_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 18);
-                fence_after_sync();
-                constexpr uint32_t idesc = idesc_f16(2 * PN);
-#pragma unroll
-                for (int s = 0; s < 2; ++s)
-#pragma unroll
-                    for (int pr = 0; pr < 3; ++pr) {
-                        const uint32_t ahl = pr == 2 ? 1 : 0, bhl = pr == 1 ? 1 : 0;
-                        const uint64_t ad = sdesc(smem_u32(w1s + s * SLAB + ahl * A_TILE), A_LBO, A_SBO);
-                        const uint64_t bd = sdesc(smem_u32(Es + bhl * ET_HALF + s * (ET_ROWS * 32)), ET_ROWS * 16, 128);
-                        mma_f16(tmem + TB + 128, ad, bd, idesc, (s | pr) != 0);
-                    }
-                mma_commit(mma_bar);
-            }
+            // [z; z']^T = W1 [e; e']^T on the bulk-copied tile: the partition's
+            // first tile here, later tiles at the end of the previous tile's
+            // epilogue 2
+            if (k == 0 && tp == 0) issue_gemm1();
             e_phase ^= 1;
             if (wl == 0) {
                 __syncwarp();
@@ -1381,6 +1402,13 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                 fence_after_sync();
                 epi3(b);
             }
+            // epilogue 3's TMEM reads are done: the [z | z'] columns are free for
+            // the next tile's GEMM1 (issued by warp 5, an epilogue-3 warp that
+            // does no prep, after its epilogue 2)
+            if (q < 2 && wl != 5) {
+                fence_before_sync();
+                cols_free_arrive(pp, 128);
+            }
             // the H tile is free: the next tile's [E; E'] tile and edge arrays
             // arrive while epilogue 2 runs
             const bool more = k + 1 < ntl && !abort_now;
@@ -1418,7 +1446,7 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                     float pv[4];
                     auto edge_term = [&](int i, float t0, float t1) {
                         if (HH == 0) pv[i] = fmaf(t0 * xb0[i], da[i], t1 * xb1[i] * d1[i]);
-                        else pv[i] = fmaf(t0 * xb0[i], d1[i], t1 * xb1[i] * d1[i]);
+                        else pv[i] = fmaf(t0, xb0[i], t1 * xb1[i]) * d1[i];
                     };
                     if (m == 0) {   // one receiver for the whole block, no sum finishes here
 #pragma unroll
@@ -1464,6 +1492,12 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                 if (hh == 0) blocks(std::integral_constant<int, 0>{});
                 else blocks(std::integral_constant<int, 1>{});
             }
+            if (wl == 5) {   // the next tile's GEMM1, once epilogue 3's warps are through
+                fence_before_sync();
+                cols_free_sync(pp, 128);
+                if (more && lane == 0) issue_gemm1();
+                __syncwarp();
+            }
             if (more && tp < PN) {   // the next tile's prep, by the warp that fetched it
                 cp_async_wait_all();
                 __syncwarp();
@@ -1471,9 +1505,9 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
             }
             fence_before_sync();
             pipe_sync(pp);
-            // per-edge sums, fixed order, by the pipeline's last warp (warp 0
-            // issues the next tile's GEMM1 meanwhile): dE/dd = the 8 warps'
-            // shares + the three u terms; dE/du from epilogue 3
+            // per-edge sums, fixed order, by the pipeline's last warp (the next
+            // tile's GEMM1 is already running): dE/dd = the 8 warps' shares +
+            // the three u terms; dE/du from epilogue 3
             const int te = tp - (PT - 32);
             if (te >= 0 && te < n) {
                 float dd = 0.f;

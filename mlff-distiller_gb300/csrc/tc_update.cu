@@ -7,13 +7,15 @@
 // lane is an output channel, a column an atom, so the epilogue thread that
 // owns channel c touches channel c of consecutive atoms -- coalesced rows of
 // the [N][4][H] feature arrays.  64-atom tiles (MMA N = 64, so that a
-// 3,000-atom system still spreads over 47 SMs), persistent CTAs, 8 warps:
+// 3,000-atom system still spreads over 47 SMs), persistent CTAs of 8 warps,
+// two per SM (one CTA's epilogues overlap the other's weight stream and MMAs):
 // in the epilogues warp w reads TMEM lane quarter w % 4 for atoms
 // 32 (w / 4) .. +31; the B tiles are built one atom row per warp (lane l:
 // channels 4l..4l+3, coalesced 512-byte rows).
 //
 // The weights (split-FP16 A-operand tile pairs, 8 KB per 128 x 16 block)
-// stream through a 16-slot ring of bulk copies in the order the MMAs use
+// stream through a ring of bulk copies (5 slots forward, 2 reverse: what
+// two CTAs per SM leave of shared memory) in the order the MMAs use
 // them: one thread issues the MMAs and commits each slot, another refills
 // the slots (during a GEMM, and ahead of the next GEMM while the epilogue
 // runs).  The forward accumulators are pre-filled with the bias, so every
@@ -67,10 +69,12 @@ int pack_update_tc(const mlff_dims& d, float* out, const PackedOffsets& o, cudaS
 }
 
 // ------------------------------------------------------- weight stream
-constexpr int URING = 16;
+constexpr int URING_F = 5;    // forward: two CTAs per SM (at most 113 KB of shared memory each)
+constexpr int URING_B = 2;    // reverse: two CTAs per SM (the 96 KB abar tile leaves room for two slots)
 constexpr int UNT = 256;
 constexpr int UN = 64;
 
+template <int URING>
 struct UStream {
     unsigned char* ring;
     uint64_t* full;
@@ -81,7 +85,8 @@ struct UStream {
     uint32_t consumed;             // consumer: pairs whose copy was seen complete
 };
 
-__device__ __forceinline__ const unsigned char* ustream_src(const UStream& s, uint32_t P) {
+template <int URING>
+__device__ __forceinline__ const unsigned char* ustream_src(const UStream<URING>& s, uint32_t P) {
     const uint32_t per = s.npairs[0] + s.npairs[1];
     const uint32_t q = P % per;
     return q < (uint32_t)s.npairs[0] ? s.src[0] + (size_t)q * A_PAIR : s.src[1] + (size_t)(q - s.npairs[0]) * A_PAIR;
@@ -90,7 +95,8 @@ __device__ __forceinline__ const unsigned char* ustream_src(const UStream& s, ui
 // producer: copy pairs until `target` (exclusive) are issued; a slot is
 // reused once the commit of the pair that used it URING pairs earlier has
 // arrived
-__device__ __forceinline__ bool ustream_fill(UStream& s, uint32_t target) {
+template <int URING>
+__device__ __forceinline__ bool ustream_fill(UStream<URING>& s, uint32_t target) {
     while (s.issued < target) {
         const uint32_t slot = s.issued % URING;
         if (s.issued >= (uint32_t)URING && !mbar_wait(&s.empty[slot], ((s.issued / URING) - 1) & 1, WAIT_BUDGET))
@@ -105,8 +111,8 @@ __device__ __forceinline__ bool ustream_fill(UStream& s, uint32_t target) {
 // consumer: one GEMM of a tile.  Pair i of n (global pair P0 + i): D[d_of(i)]
 // += A_hi B_hi(i) + A_hi B_lo(i) + A_lo B_hi(i); the first MMA of pair i
 // overwrites D instead when fresh(i).
-template <typename DOf, typename BOf, typename Fresh>
-__device__ __forceinline__ bool ustream_gemm(UStream& s, uint32_t P0, int n, DOf d_of, BOf b_of, uint64_t bhalf,
+template <int URING, typename DOf, typename BOf, typename Fresh>
+__device__ __forceinline__ bool ustream_gemm(UStream<URING>& s, uint32_t P0, int n, DOf d_of, BOf b_of, uint64_t bhalf,
                                              Fresh fresh) {
     constexpr uint32_t idesc = idesc_f16(UN);
     const uint64_t a0 = sdesc(smem_u32(s.ring), A_LBO, A_SBO);
@@ -175,19 +181,19 @@ __device__ __forceinline__ void uwait_mma(UCtl& c, int w, int where) {
 
 // ------------------------------------------------------- forward kernel
 // smem: B tile [s, |v|] (K = 256: 4 K-blocks; hi half then lo half, 64 KB),
-// the H tile (K = 128, 32 KB) aliased into it after GEMM1, the ring (128 KB).
+// the H tile (K = 128, 32 KB) aliased into it after GEMM1, the ring (40 KB).
 // TMEM: D1 = z (cols 0-63), D2 chunk g = (ds, g1, g2)[g] (64 + 64 g).
 constexpr uint32_t UF_BH = 4 * b_block(UN);
 constexpr uint32_t UF_HH = 2 * b_block(UN);
 constexpr uint32_t UF_OFF_B = 0;
 constexpr uint32_t UF_OFF_RING = UF_OFF_B + 2 * UF_BH;
-constexpr uint32_t UF_OFF_C = UF_OFF_RING + URING * A_PAIR;      // c1 [H], c2 [3H], mix [9]
+constexpr uint32_t UF_OFF_C = UF_OFF_RING + URING_F * A_PAIR;      // c1 [H], c2 [3H], mix [9]
 constexpr uint32_t UF_OFF_BAR = UF_OFF_C + 4 * (H + H3 + 16);
-constexpr uint32_t UF_OFF_MISC = UF_OFF_BAR + 8 * (1 + 2 * URING);
+constexpr uint32_t UF_OFF_MISC = UF_OFF_BAR + 8 * (1 + 2 * URING_F);
 constexpr uint32_t UF_SMEM = align1k(UF_OFF_MISC + 16);
-static_assert(UF_SMEM <= 232448, "update kernel shared memory");
+static_assert(2 * (UF_SMEM + 1024) <= 228 * 1024, "two update CTAs per SM");
 
-__global__ void __launch_bounds__(UNT, 1) update_fwd_tc_kernel(const float* __restrict__ P, LayerOffsets lo,
+__global__ void __launch_bounds__(UNT, 2) update_fwd_tc_kernel(const float* __restrict__ P, LayerOffsets lo,
                                                                const float* __restrict__ Xt, int32_t n_atoms,
                                                                float* __restrict__ Xout, float* __restrict__ uz,
                                                                float* __restrict__ ua, Status* st) {
@@ -198,7 +204,7 @@ __global__ void __launch_bounds__(UNT, 1) update_fwd_tc_kernel(const float* __re
     float* mix = c2s + H3;
     uint64_t* mma_bar = reinterpret_cast<uint64_t*>(smem + UF_OFF_BAR);
     uint64_t* full = mma_bar + 1;
-    uint64_t* empty = full + URING;
+    uint64_t* empty = full + URING_F;
     uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + UF_OFF_MISC);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + UF_OFF_MISC + 4);
     const int t = threadIdx.x, w = t >> 5, lane = t & 31;
@@ -209,7 +215,7 @@ __global__ void __launch_bounds__(UNT, 1) update_fwd_tc_kernel(const float* __re
     }
     if (t == 0) {
         mbar_init(mma_bar, 1);
-        for (int i = 0; i < URING; ++i) {
+        for (int i = 0; i < URING_F; ++i) {
             mbar_init(&full[i], 1);
             mbar_init(&empty[i], 1);
         }
@@ -223,14 +229,14 @@ __global__ void __launch_bounds__(UNT, 1) update_fwd_tc_kernel(const float* __re
     __syncthreads();
     fence_after_sync();
     const uint32_t tmem = *tslot;
-    UStream ws{smem + UF_OFF_RING, full, empty,
+    UStream<URING_F> ws{smem + UF_OFF_RING, full, empty,
                {reinterpret_cast<const unsigned char*>(P + lo.u1_tc), reinterpret_cast<const unsigned char*>(P + lo.u2_tc)},
                {16, 24}, 0, 0};
     UCtl ctl{mma_bar, abort_flag, st, 0};
     const int my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
     const uint32_t P_end = (uint32_t)my_tiles * 40;
     const bool producer = t == 32;
-    if (producer && !ustream_fill(ws, min((uint32_t)URING, P_end))) ufail(ctl, 20);
+    if (producer && !ustream_fill(ws, min((uint32_t)URING_F, P_end))) ufail(ctl, 20);
     // everything above reads packed weights only and overlaps the previous kernel
     pdl_wait();
     if (t == 0 && st->code != 0) *abort_flag = 1;
@@ -283,7 +289,7 @@ __global__ void __launch_bounds__(UNT, 1) update_fwd_tc_kernel(const float* __re
         if (producer && !ustream_fill(ws, min(P0 + 16, P_end))) ufail(ctl, 26);
         uwait_mma(ctl, w, 22);
         // GEMM1 is done, so every slot is free: fetch GEMM2's pairs during epilogue 1
-        if (producer && !ustream_fill(ws, min(P0 + 16 + URING, P_end))) ufail(ctl, 27);
+        if (producer && !ustream_fill(ws, min(P0 + 16 + URING_F, P_end))) ufail(ctl, 27);
         {   // epilogue 1: z -> uz, h = silu(z) -> H tile (aliases the B tile)
             const int col = 32 * hh;
             float z[32];
@@ -315,7 +321,7 @@ __global__ void __launch_bounds__(UNT, 1) update_fwd_tc_kernel(const float* __re
         if (producer && !ustream_fill(ws, min(P0 + 40, P_end))) ufail(ctl, 28);
         uwait_mma(ctl, w, 24);
         // the next tile's GEMM1 pairs arrive while this epilogue and the next build run
-        if (producer && !ustream_fill(ws, min(P0 + 40 + URING, P_end))) ufail(ctl, 29);
+        if (producer && !ustream_fill(ws, min(P0 + 40 + URING_F, P_end))) ufail(ctl, 29);
         {   // epilogue 2: (ds, g1, g2) -> ua; s' = s + ds, v' = v g1 + (M v) g2 (:452-468).
             // The TMEM owner of channel c writes (ds, g1, g2) of 32 atoms to
             // shared memory (the B tile is free), then each warp handles
@@ -389,10 +395,10 @@ __global__ void __launch_bounds__(UNT, 1) update_fwd_tc_kernel(const float* __re
     // drain: every pair copied must have landed before the CTA exits
     __syncthreads();
     if (producer) {
-        // copies still in flight are among the last URING issued (a slot is
+        // copies still in flight are among the last URING_F issued (a slot is
         // refilled only after its previous copy was consumed)
-        for (uint32_t f = ws.issued > (uint32_t)URING ? ws.issued - URING : 0u; f < ws.issued; ++f)
-            if (!mbar_wait(&full[f % URING], (f / URING) & 1, WAIT_BUDGET)) {
+        for (uint32_t f = ws.issued > (uint32_t)URING_F ? ws.issued - URING_F : 0u; f < ws.issued; ++f)
+            if (!mbar_wait(&full[f % URING_F], (f / URING_F) & 1, WAIT_BUDGET)) {
                 set_status(st, MLFF_ERR_TIMEOUT, 25);
                 break;
             }
@@ -419,7 +425,8 @@ int launch_update_fwd_tc(const float* packed, const LayerOffsets& lo, const WsLa
     float* uz = ws_ptr<float>(ws, L.uz) + (int64_t)layer * L.N * H;
     float* ua = ws_ptr<float>(ws, L.ua) + (int64_t)layer * L.N * H3;
     const int ntiles = (L.N + UN - 1) / UN;
-    const int grid = std::max(1, std::min(ntiles, num_sms()));
+    // two CTAs per SM: one's epilogues overlap the other's weight stream and MMAs
+    const int grid = std::max(1, std::min(ntiles, 2 * num_sms()));
     MLFF_LAUNCH_PDL("update_fwd_tc", update_fwd_tc_kernel, grid, UNT, UF_SMEM, st, packed, lo, Xt, L.N, Xout, uz, ua,
                     ws_ptr<Status>(ws, L.status));
     return MLFF_OK;
@@ -429,19 +436,19 @@ int launch_update_fwd_tc(const float* packed, const LayerOffsets& lo, const WsLa
 // abar = dE/d(ds, g1, g2) [atom][3H] -> zbar = (U2^T abar) silu'(uz) ->
 // cb = U1^T zbar = dE/d[s, |v|]; xtbar = (sb + cs, vb + cn v / |v|).
 // smem: abar B tile (K = 384: 6 K-blocks, hi then lo, 96 KB), the zbar tile
-// (K = 128, 32 KB) aliased into it after GEMM3, the ring (128 KB).
+// (K = 128, 32 KB) aliased into it after GEMM3, the ring (16 KB).
 // TMEM: D3 = zbar pre-activation (cols 0-63), D4 = (cs, cn) (64-191).
 constexpr uint32_t UB_AH = 6 * b_block(UN);
 constexpr uint32_t UB_ZH = 2 * b_block(UN);
 constexpr uint32_t UB_OFF_B = 0;
 constexpr uint32_t UB_OFF_RING = UB_OFF_B + 2 * UB_AH;
-constexpr uint32_t UB_OFF_MIX = UB_OFF_RING + URING * A_PAIR;
+constexpr uint32_t UB_OFF_MIX = UB_OFF_RING + URING_B * A_PAIR;
 constexpr uint32_t UB_OFF_BAR = UB_OFF_MIX + 64;
-constexpr uint32_t UB_OFF_MISC = UB_OFF_BAR + 8 * (1 + 2 * URING);
+constexpr uint32_t UB_OFF_MISC = UB_OFF_BAR + 8 * (1 + 2 * URING_B);
 constexpr uint32_t UB_SMEM = align1k(UB_OFF_MISC + 16);
-static_assert(UB_SMEM <= 232448, "update reverse kernel shared memory");
+static_assert(2 * (UB_SMEM + 1024) <= 228 * 1024, "two update reverse CTAs per SM");
 
-__global__ void __launch_bounds__(UNT, 1) update_bwd_tc_kernel(const float* __restrict__ P, LayerOffsets lo,
+__global__ void __launch_bounds__(UNT, 2) update_bwd_tc_kernel(const float* __restrict__ P, LayerOffsets lo,
                                                                const float* __restrict__ Xt, const float* __restrict__ uz,
                                                                const float* __restrict__ ua,
                                                                const float* __restrict__ xbo, int32_t n_atoms,
@@ -451,7 +458,7 @@ __global__ void __launch_bounds__(UNT, 1) update_bwd_tc_kernel(const float* __re
     float* mix = reinterpret_cast<float*>(smem + UB_OFF_MIX);
     uint64_t* mma_bar = reinterpret_cast<uint64_t*>(smem + UB_OFF_BAR);
     uint64_t* full = mma_bar + 1;
-    uint64_t* empty = full + URING;
+    uint64_t* empty = full + URING_B;
     uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + UB_OFF_MISC);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + UB_OFF_MISC + 4);
     const int t = threadIdx.x, w = t >> 5, lane = t & 31;
@@ -462,7 +469,7 @@ __global__ void __launch_bounds__(UNT, 1) update_bwd_tc_kernel(const float* __re
     }
     if (t == 0) {
         mbar_init(mma_bar, 1);
-        for (int i = 0; i < URING; ++i) {
+        for (int i = 0; i < URING_B; ++i) {
             mbar_init(&full[i], 1);
             mbar_init(&empty[i], 1);
         }
@@ -474,14 +481,14 @@ __global__ void __launch_bounds__(UNT, 1) update_bwd_tc_kernel(const float* __re
     __syncthreads();
     fence_after_sync();
     const uint32_t tmem = *tslot;
-    UStream ws{smem + UB_OFF_RING, full, empty,
+    UStream<URING_B> ws{smem + UB_OFF_RING, full, empty,
                {reinterpret_cast<const unsigned char*>(P + lo.u2t_tc), reinterpret_cast<const unsigned char*>(P + lo.u1t_tc)},
                {24, 16}, 0, 0};
     UCtl ctl{mma_bar, abort_flag, st, 0};
     const int my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
     const uint32_t P_end = (uint32_t)my_tiles * 40;
     const bool producer = t == 32;
-    if (producer && !ustream_fill(ws, min((uint32_t)URING, P_end))) ufail(ctl, 30);
+    if (producer && !ustream_fill(ws, min((uint32_t)URING_B, P_end))) ufail(ctl, 30);
     // everything above reads packed weights only and overlaps the previous kernel
     pdl_wait();
     if (t == 0 && st->code != 0) *abort_flag = 1;
@@ -542,7 +549,7 @@ __global__ void __launch_bounds__(UNT, 1) update_bwd_tc_kernel(const float* __re
         }
         if (producer && !ustream_fill(ws, min(P0 + 24, P_end))) ufail(ctl, 36);
         uwait_mma(ctl, w, 32);
-        if (producer && !ustream_fill(ws, min(P0 + 24 + URING, P_end))) ufail(ctl, 37);
+        if (producer && !ustream_fill(ws, min(P0 + 24 + URING_B, P_end))) ufail(ctl, 37);
         {   // epilogue 3: zbar = D3 silu'(uz) -> zbar tile (aliases the abar tile)
             const int col = 32 * hh;
             float zb[32];
@@ -572,7 +579,7 @@ __global__ void __launch_bounds__(UNT, 1) update_bwd_tc_kernel(const float* __re
         }
         if (producer && !ustream_fill(ws, min(P0 + 40, P_end))) ufail(ctl, 38);
         uwait_mma(ctl, w, 34);
-        if (producer && !ustream_fill(ws, min(P0 + 40 + URING, P_end))) ufail(ctl, 39);
+        if (producer && !ustream_fill(ws, min(P0 + 40 + URING_B, P_end))) ufail(ctl, 39);
         {   // epilogue 4: xtbar = (sb + cs, xb g1 + M^T xb g2 + cn v / |v|).  The
             // TMEM owner of channel c writes (cs, cn) of its 32 atoms to shared
             // memory (the abar tile is free), then each warp handles whole atom
@@ -639,10 +646,10 @@ __global__ void __launch_bounds__(UNT, 1) update_bwd_tc_kernel(const float* __re
     }
     __syncthreads();
     if (producer) {
-        // copies still in flight are among the last URING issued (a slot is
+        // copies still in flight are among the last URING_B issued (a slot is
         // refilled only after its previous copy was consumed)
-        for (uint32_t f = ws.issued > (uint32_t)URING ? ws.issued - URING : 0u; f < ws.issued; ++f)
-            if (!mbar_wait(&full[f % URING], (f / URING) & 1, WAIT_BUDGET)) {
+        for (uint32_t f = ws.issued > (uint32_t)URING_B ? ws.issued - URING_B : 0u; f < ws.issued; ++f)
+            if (!mbar_wait(&full[f % URING_B], (f / URING_B) & 1, WAIT_BUDGET)) {
                 set_status(st, MLFF_ERR_TIMEOUT, 35);
                 break;
             }
@@ -668,7 +675,8 @@ int launch_update_bwd_tc(const float* packed, const LayerOffsets& lo, const WsLa
     const float* uz = ws_ptr<float>(ws, L.uz) + (int64_t)layer * L.N * H;
     const float* ua = ws_ptr<float>(ws, L.ua) + (int64_t)layer * L.N * H3;
     const int ntiles = (L.N + UN - 1) / UN;
-    const int grid = std::max(1, std::min(ntiles, num_sms()));
+    // two CTAs per SM: one's epilogues overlap the other's weight stream and MMAs
+    const int grid = std::max(1, std::min(ntiles, 2 * num_sms()));
     MLFF_LAUNCH_PDL("update_bwd_tc", update_bwd_tc_kernel, grid, UNT, UB_SMEM, st, packed, lo, Xt, uz, ua, xbar_out,
                     L.N, xtbar, ws_ptr<Status>(ws, L.status));
     return MLFF_OK;
