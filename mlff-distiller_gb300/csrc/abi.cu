@@ -219,14 +219,15 @@ namespace mlff {
 // neighbour build + model + reverse pass; leaves the status word alone so
 // that an error raised in an earlier MD step stays visible
 int energy_forces_impl(const mlff_dims& d, const void* packed, const mlff_system& sys, const WsLayout& L,
-                       int32_t path, const mlff_outputs& out, void* ws, cudaStream_t st) {
+                       int32_t path, const mlff_outputs& out, void* ws, cudaStream_t st,
+                       const VerletFuse* vf = nullptr) {
     PackedOffsets po = packed_offsets(d);
     int r = launch_neighbors(d, sys, L, ws, st);
     if (r) return r;
     const float* P = static_cast<const float*>(packed);
     if (path == MLFF_PATH_PLAIN_FP32 || path == MLFF_PATH_TRAIN || path == MLFF_PATH_TRAIN_FORCES)
-        return run_plain(d, P, po, sys, L, ws, out, st);
-    return run_tuned(d, P, po, sys, L, ws, out, path, st);
+        return run_plain(d, P, po, sys, L, ws, out, st, nullptr, vf);
+    return run_tuned(d, P, po, sys, L, ws, out, path, st, vf);
 }
 int md_kick_drift(const WsLayout& L, void* ws, mlff_md_state* s, double dt, cudaStream_t st);
 int md_langevin_baoa(const WsLayout& L, void* ws, mlff_md_state* s, double dt, double friction, double kT,
@@ -237,6 +238,8 @@ int md_vec_close(const WsLayout& L, void* ws, mlff_md_state* s, double dt, doubl
                  int32_t fix_com, const int64_t* mol_ptr, int32_t n_mol, double* kinetic, cudaStream_t st);
 int md_energy_stats(const double* epot, const double* ekin, int32_t n, int32_t B, const int64_t* mol_ptr,
                     double dt_ps, double* out, cudaStream_t st);
+int md_kinetic_from_atoms(const double* ke_atom, mlff_md_state* s, const int64_t* mol_ptr, int32_t n_mol,
+                          cudaStream_t st);
 int md_kick(const WsLayout& L, void* ws, mlff_md_state* s, double dt, const int64_t* mol_ptr, int32_t n_mol,
             bool kinetic, cudaStream_t st);
 int md_npt_open(const WsLayout& L, void* ws, const mlff_md_state* s, const mlff_npt_state* n, double dt, double kT,
@@ -452,6 +455,13 @@ static int md_steps(const mlff_dims* dims, const void* packed, const mlff_system
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     MLFF_CUDA(cudaMemsetAsync(ws_ptr<Status>(workspace, L.status), 0, sizeof(Status), st));
     const int64_t B = sys->n_mol;
+    // Velocity Verlet: the force kernel of step s closes step s (half kick,
+    // kinetic energy terms) and opens step s + 1 (half kick, drift), so only
+    // the first step of a call has a kick-drift launch of its own.  The
+    // per-atom kinetic terms go to the per-atom virial scratch's far end
+    // (the second adjoint buffer, free once the force kernel runs).
+    double* ke_atom = reinterpret_cast<double*>(ws_ptr<float>(workspace, L.xbar) + (int64_t)L.N * 4 * H) +
+                      (int64_t)9 * L.N;
     int r;
     for (int s = 0; s < n_steps; ++s) {
         const bool last = s == n_steps - 1;
@@ -459,17 +469,25 @@ static int md_steps(const mlff_dims* dims, const void* packed, const mlff_system
                          nullptr, nullptr};
         mlff_md_state ks = *state;
         if (state->kinetic_trace) ks.kinetic = state->kinetic_trace + s * B;
+        const bool want_ke = (last || state->kinetic_trace) && ks.kinetic;
         if (scheme == MD_VEC) r = md_vec_open(L, workspace, state, dt, friction, kT, seed, fix_com, sys->mol_ptr,
                                               sys->n_mol, st);
         else if (scheme == MD_BAOAB) r = md_langevin_baoa(L, workspace, state, dt, friction, kT, seed, st);
-        else r = md_kick_drift(L, workspace, state, dt, st);
+        else r = s == 0 ? md_kick_drift(L, workspace, state, dt, st) : MLFF_OK;
         if (r) return r;
-        if ((r = energy_forces_impl(*dims, packed, s2, L, path, out, workspace, st))) return r;
-        if (scheme == MD_VEC)
-            r = md_vec_close(L, workspace, &ks, dt, friction, kT, fix_com, sys->mol_ptr, sys->n_mol,
-                             (last || state->kinetic_trace) ? ks.kinetic : nullptr, st);
-        else
-            r = md_kick(L, workspace, &ks, dt, sys->mol_ptr, sys->n_mol, last || state->kinetic_trace, st);
+        if (scheme == MD_VERLET) {
+            const VerletFuse vf{state->vel, state->inv_mass, state->pos, ws_ptr<float>(workspace, L.md_pos32),
+                                want_ke ? ke_atom : nullptr, state->step_counter, dt, last ? 0 : 1};
+            if ((r = energy_forces_impl(*dims, packed, s2, L, path, out, workspace, st, &vf))) return r;
+            if (want_ke) r = md_kinetic_from_atoms(ke_atom, &ks, sys->mol_ptr, sys->n_mol, st);
+        } else {
+            if ((r = energy_forces_impl(*dims, packed, s2, L, path, out, workspace, st))) return r;
+            if (scheme == MD_VEC)
+                r = md_vec_close(L, workspace, &ks, dt, friction, kT, fix_com, sys->mol_ptr, sys->n_mol,
+                                 (last || state->kinetic_trace) ? ks.kinetic : nullptr, st);
+            else
+                r = md_kick(L, workspace, &ks, dt, sys->mol_ptr, sys->n_mol, last || state->kinetic_trace, st);
+        }
         if (r) return r;
         if (last) {
             if (state->energy_trace)

@@ -55,6 +55,16 @@ __device__ __forceinline__ float dsilu_f(float x) {
     return s * (1.0f + x * (1.0f - s));
 }
 
+// Velocity-Verlet half kick v + dt/2 F/m in float64 (F is the float32
+// force) and the kinetic energy 1/2 m v^2 of one atom; the integrator
+// kernels and the force kernel's fused update share these expressions.
+__device__ __forceinline__ double verlet_half_kick(double v, float f, double inv_mass, double dt) {
+    return v + 0.5 * dt * (double)f * inv_mass;
+}
+__device__ __forceinline__ double kinetic_term(double vx, double vy, double vz, double inv_mass) {
+    return 0.5 * (vx * vx + vy * vy + vz * vz) / inv_mass;
+}
+
 // float32 |d| rounded as the reference's torch.norm: x*x rounded, then two
 // fused multiply-adds, then a correctly rounded square root.
 __device__ __forceinline__ float pair_distance(float dx, float dy, float dz) {

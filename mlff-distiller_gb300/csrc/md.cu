@@ -20,7 +20,7 @@ __global__ void kick_drift_kernel(double* __restrict__ pos, double* __restrict__
     if (st->code != 0) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 3 * n_atoms; i += gridDim.x * blockDim.x) {
         const int a = i / 3;
-        const double v = vel[i] + 0.5 * dt * (double)F[i] * inv_mass[a];
+        const double v = verlet_half_kick(vel[i], F[i], inv_mass[a], dt);
         vel[i] = v;
         const double p = pos[i] + dt * v;
         pos[i] = p;
@@ -38,7 +38,7 @@ __global__ void kick_kernel(double* __restrict__ vel, const double* __restrict__
     if (st->code != 0) return;
     if (step_counter && blockIdx.x == 0 && threadIdx.x == 0) *step_counter += 1;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 3 * n_atoms; i += gridDim.x * blockDim.x)
-        vel[i] += 0.5 * dt * (double)F[i] * inv_mass[i / 3];
+        vel[i] = verlet_half_kick(vel[i], F[i], inv_mass[i / 3], dt);
 }
 
 // ------------------------------------------------------------ Langevin
@@ -296,18 +296,19 @@ int md_vec_close(const WsLayout& L, void* ws, mlff_md_state* s, double dt, doubl
     return MLFF_OK;
 }
 
-// kinetic energy 1/2 m v^2 per structure (fixed-order tree)
+// kinetic energy 1/2 m v^2 per structure (fixed-order tree), from the
+// velocities or, when ke_atom is given, from per-atom terms the force
+// kernel's fused Verlet update wrote
 __global__ void kinetic_kernel(const double* __restrict__ vel, const double* __restrict__ inv_mass,
-                               const int64_t* __restrict__ mol_ptr, int32_t n_mol, double* __restrict__ ke) {
+                               const double* __restrict__ ke_atom, const int64_t* __restrict__ mol_ptr, int32_t n_mol,
+                               double* __restrict__ ke) {
     pdl_wait();
     pdl_trigger();
     __shared__ double red[256];
     for (int m = blockIdx.x; m < n_mol; m += gridDim.x) {
         double s = 0.0;
-        for (int64_t a = mol_ptr[m] + threadIdx.x; a < mol_ptr[m + 1]; a += blockDim.x) {
-            const double v2 = vel[3 * a] * vel[3 * a] + vel[3 * a + 1] * vel[3 * a + 1] + vel[3 * a + 2] * vel[3 * a + 2];
-            s += 0.5 * v2 / inv_mass[a];
-        }
+        for (int64_t a = mol_ptr[m] + threadIdx.x; a < mol_ptr[m + 1]; a += blockDim.x)
+            s += ke_atom ? ke_atom[a] : kinetic_term(vel[3 * a], vel[3 * a + 1], vel[3 * a + 2], inv_mass[a]);
         red[threadIdx.x] = s;
         __syncthreads();
         for (int o = 128; o > 0; o >>= 1) {
@@ -346,9 +347,19 @@ int md_kick(const WsLayout& L, void* ws, mlff_md_state* s, double dt, const int6
     MLFF_LAUNCH_PDL("kick", kick_kernel, blocks, 256, 0, st, s->vel, s->inv_mass, s->forces, dt, L.N, s->step_counter,
                     ws_ptr<Status>(ws, L.status));
     if (kinetic && s->kinetic) {
-        MLFF_LAUNCH_PDL("kinetic", kinetic_kernel, std::min(std::max(n_mol, 1), 152 * 8), 256, 0, st, s->vel, s->inv_mass, mol_ptr, n_mol,
-                                                                              s->kinetic);
+        MLFF_LAUNCH_PDL("kinetic", kinetic_kernel, std::min(std::max(n_mol, 1), 152 * 8), 256, 0, st, s->vel,
+                        s->inv_mass, (const double*)nullptr, mol_ptr, n_mol, s->kinetic);
     }
+    return MLFF_OK;
+}
+
+// Per-structure kinetic energy from the per-atom terms of the force kernel's
+// fused Verlet update (no separate kick).
+int md_kinetic_from_atoms(const double* ke_atom, mlff_md_state* s, const int64_t* mol_ptr, int32_t n_mol,
+                          cudaStream_t st) {
+    ProfScope prof(PK_MD, st);
+    MLFF_LAUNCH_PDL("kinetic", kinetic_kernel, std::min(std::max(n_mol, 1), 152 * 8), 256, 0, st,
+                    (const double*)s->vel, (const double*)s->inv_mass, ke_atom, mol_ptr, n_mol, s->kinetic);
     return MLFF_OK;
 }
 

@@ -412,11 +412,12 @@ __global__ void forces_kernel(const float4* __restrict__ pos4, const int32_t* __
                               const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
                               const int32_t* __restrict__ rev, const float4* __restrict__ acc,
                               int32_t n_atoms, float* __restrict__ forces, double* __restrict__ vir_atom,
-                              const Status* st) {
+                              VerletFuse vf, const Status* st) {
     pdl_wait();
     pdl_trigger();
     if (st->code != 0) return;
     const int lane = threadIdx.x & 31;
+    if (vf.step_counter && blockIdx.x == 0 && threadIdx.x == 0) *vf.step_counter += 1;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     for (int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; a < n_atoms; a += nw) {
         const int m = atom_mol[a];
@@ -453,6 +454,25 @@ __global__ void forces_kernel(const float4* __restrict__ pos4, const int32_t* __
             forces[3 * a + 1] = fy;
             forces[3 * a + 2] = fz;
         }
+        if (vf.vel && lane < 3) {   // the integrator's update of this atom, lane = component
+            const double im = vf.inv_mass[a];
+            const float f = lane == 0 ? fx : (lane == 1 ? fy : fz);
+            const int64_t i = 3 * (int64_t)a + lane;
+            const double v = verlet_half_kick(vf.vel[i], f, im, vf.dt);   // closes this step
+            if (vf.ke_atom) {
+                const double vx = __shfl_sync(0x7u, v, 0), vy = __shfl_sync(0x7u, v, 1), vz = __shfl_sync(0x7u, v, 2);
+                if (lane == 0) vf.ke_atom[a] = kinetic_term(vx, vy, vz, im);
+            }
+            if (vf.open_next) {   // the next step's half kick and drift
+                const double vn = verlet_half_kick(v, f, im, vf.dt);
+                vf.vel[i] = vn;
+                const double p = vf.pos[i] + vf.dt * vn;
+                vf.pos[i] = p;
+                vf.pos32[i] = (float)p;
+            } else {
+                vf.vel[i] = v;
+            }
+        }
         if (vir_atom) {
 #pragma unroll
             for (int i = 0; i < 9; ++i) v[i] = warp_sum_d(v[i]);
@@ -484,7 +504,7 @@ __global__ void virial_sum_kernel(const double* __restrict__ vir_atom, const int
 }
 
 int launch_forces(const mlff_dims& d, const mlff_system& sys, const WsLayout& L, void* ws,
-                  const mlff_outputs& out, cudaStream_t st) {
+                  const mlff_outputs& out, cudaStream_t st, const VerletFuse* vf) {
     (void)d;
     ProfScope prof(PK_FORCES, st);
     const Status* status = ws_ptr<Status>(ws, L.status);
@@ -495,7 +515,7 @@ int launch_forces(const mlff_dims& d, const mlff_system& sys, const WsLayout& L,
     MLFF_LAUNCH_PDL("forces", forces_kernel, std::max(blocks, 1), 128, 0, st, 
         ws_ptr<float4>(ws, L.pos4), ws_ptr<int32_t>(ws, L.atom_mol), sys.box, sys.pbc,
         ws_ptr<int32_t>(ws, L.row_ptr), ws_ptr<int32_t>(ws, L.col), ws_ptr<int32_t>(ws, L.rev),
-        ws_ptr<float4>(ws, L.edge_acc), sys.n_atoms, out.forces, vir_atom, status);
+        ws_ptr<float4>(ws, L.edge_acc), sys.n_atoms, out.forces, vir_atom, vf ? *vf : VerletFuse{}, status);
     if (out.virial) {
         MLFF_LAUNCH_PDL("virial_sum", virial_sum_kernel, std::min(std::max(sys.n_mol, 1), 152 * 8), 128, 0, st, vir_atom, sys.mol_ptr, sys.n_mol,
                                                                                       out.virial, status);

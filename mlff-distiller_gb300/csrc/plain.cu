@@ -415,7 +415,7 @@ __global__ void pl_embed_dual_kernel(const float* __restrict__ emb, const int64_
 template <class T>
 static int run_plain_t(const mlff_dims& d, const float* P, const PackedOffsets& po, const mlff_system& sys,
                        const WsLayout& L, void* ws, const mlff_outputs& out, cudaStream_t st, const GradCtx* grad,
-                       const float* pos_t, const double* strain_t) {
+                       const float* pos_t, const double* strain_t, const VerletFuse* vf = nullptr) {
     constexpr bool DUAL = is_dual_v<T>;
     const int N = sys.n_atoms;
     const int64_t NX = (int64_t)N * 4 * H;
@@ -567,7 +567,7 @@ static int run_plain_t(const mlff_dims& d, const float* P, const PackedOffsets& 
     if (grad && (r = grad_embedding<T>(d, sys, L, ws, xbo, grad->g, st))) return r;
     if constexpr (DUAL) return MLFF_OK;
     if (!out.forces && !out.virial) return MLFF_OK;
-    return launch_forces(d, sys, L, ws, out, st);
+    return launch_forces(d, sys, L, ws, out, st, vf);
 }
 
 // Float32 C[M][N] = A[M][K] B[K][N] (+ bias) for the per-module entry points
@@ -581,8 +581,9 @@ int plain_sgemm(int mode, const float* A, const float* B, const float* bias, flo
 }
 
 int run_plain(const mlff_dims& d, const float* P, const PackedOffsets& po, const mlff_system& sys,
-              const WsLayout& L, void* ws, const mlff_outputs& out, cudaStream_t st, const GradCtx* grad) {
-    return run_plain_t<float>(d, P, po, sys, L, ws, out, st, grad, nullptr, nullptr);
+              const WsLayout& L, void* ws, const mlff_outputs& out, cudaStream_t st, const GradCtx* grad,
+              const VerletFuse* vf) {
+    return run_plain_t<float>(d, P, po, sys, L, ws, out, st, grad, nullptr, nullptr, vf);
 }
 
 int run_plain_tangent(const mlff_dims& d, const float* P, const PackedOffsets& po, const mlff_system& sys,

@@ -344,7 +344,8 @@ static int add_rows(float* dst, const float* src, int64_t n, const Status* st, c
 }
 
 int run_tuned(const mlff_dims& d, const float* P, const PackedOffsets& po, const mlff_system& sys,
-              const WsLayout& L, void* ws, const mlff_outputs& out, int path, cudaStream_t st) {
+              const WsLayout& L, void* ws, const mlff_outputs& out, int path, cudaStream_t st,
+              const VerletFuse* vf) {
     const int N = sys.n_atoms;
     const int64_t NX = (int64_t)N * 4 * H;
     int r;
@@ -443,7 +444,7 @@ int run_tuned(const mlff_dims& d, const float* P, const PackedOffsets& po, const
             if ((r = add_rows(xbo, xtb, NX, a.st, st))) return r;   // dE/dX = dE/dXt + gathered part
         }
     }
-    return launch_forces(d, sys, L, ws, out, st);
+    return launch_forces(d, sys, L, ws, out, st, vf);
 }
 
 }  // namespace mlff

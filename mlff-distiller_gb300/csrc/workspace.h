@@ -103,8 +103,23 @@ int launch_embed(const mlff_dims& d, const float* packed, const PackedOffsets& p
 int launch_readout(const mlff_dims& d, const float* packed, const PackedOffsets& po,
                    const mlff_system& sys, const WsLayout& L, void* ws, const mlff_outputs& out,
                    int want_grad, cudaStream_t st);
+// Velocity-Verlet update fused into the force kernel: with the new force F
+// of atom a, the closing half kick v += dt/2 F/m of this step, the atom's
+// kinetic energy 1/2 m v^2 (into ke_atom, when given), and, with open_next,
+// the next step's opening half kick and drift (v += dt/2 F/m; r += dt v;
+// pos32 = (float)r).  step_counter (when given) advances by one.
+struct VerletFuse {
+    double* vel;
+    const double* inv_mass;
+    double* pos;
+    float* pos32;
+    double* ke_atom;
+    int64_t* step_counter;
+    double dt;
+    int open_next;
+};
 int launch_forces(const mlff_dims& d, const mlff_system& sys, const WsLayout& L, void* ws,
-                  const mlff_outputs& out, cudaStream_t st);
+                  const mlff_outputs& out, cudaStream_t st, const VerletFuse* vf = nullptr);
 // Training: per-structure loss weights dL/dE_b and the gradient outputs.
 struct GradCtx {
     const double* w;
@@ -112,7 +127,7 @@ struct GradCtx {
 };
 int run_plain(const mlff_dims& d, const float* packed, const PackedOffsets& po,
               const mlff_system& sys, const WsLayout& L, void* ws, const mlff_outputs& out,
-              cudaStream_t st, const GradCtx* grad = nullptr);
+              cudaStream_t st, const GradCtx* grad = nullptr, const VerletFuse* vf = nullptr);
 // Pass of the plain path over (value, tangent) pairs along positions moved
 // by -pos_t [N][3] and cells strained by strain_t [B][3][3] (either may be
 // NULL): adds the derivative of grad_theta sum_b E_b along that direction
@@ -141,7 +156,7 @@ int grad_embedding(const mlff_dims& d, const mlff_system& sys, const WsLayout& L
                    const mlff_grads& g, cudaStream_t st);
 int run_tuned(const mlff_dims& d, const float* packed, const PackedOffsets& po,
               const mlff_system& sys, const WsLayout& L, void* ws, const mlff_outputs& out,
-              int path, cudaStream_t st);
+              int path, cudaStream_t st, const VerletFuse* vf = nullptr);
 int launch_partition(const WsLayout& L, void* ws, cudaStream_t st);
 int launch_scan(int32_t* data, int64_t n, int32_t* tmp, cudaStream_t st);
 int launch_update_fwd(const mlff_dims& d, const float* packed, const LayerOffsets& lo,
