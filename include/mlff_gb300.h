@@ -357,25 +357,36 @@ int mlff_profile_begin(void);
 int mlff_profile_end(double *ms_by_kind, int64_t *launches_by_kind, int32_t n_kinds);
 
 /* Autotuning (no counterpart in the reference, whose only GPU kernels fix
- * their block sizes by hand).  The tensor-core path splits the receivers
- * into 2 x SMs x f partitions; the partition factor f (1, 2 or 4) is
+ * their block sizes by hand).  Two shapes of the tensor-core path are
  * chosen per size bucket (path, ceil(log2 n_atoms), ceil(log2 n_mol)) and
  * kept in a process-wide cache guarded by a mutex; every call of that
- * bucket then uses it.  Results do not depend on f (each receiver's sums run
- * over its edges in order inside one partition), and the workspace size
- * does not either.  mlff_autotune times `repeats` calls of
- * mlff_energy_forces per candidate (same arguments; the outputs are
- * overwritten) with CUDA events on the stream, synchronises the stream,
- * caches the fastest and writes it to *chosen (host) and the milliseconds
- * per call of f = 1, 2, 4 to ms_per_candidate (host double [3], or NULL).
- * Not for use while the stream is being captured.  Other paths: *chosen = 1,
- * nothing timed.  _query reads the factor a call of that size would use,
- * _set pins one (0 removes the entry), _reset empties the cache. */
+ * bucket then uses them:
+ *  - the partition factor f (1, 2 or 4): the edge kernels split the
+ *    receivers into 2 x SMs x f partitions;
+ *  - the update tile (64 or 32 atoms per CTA tile of the update kernels;
+ *    32 spreads a small system over more SMs).
+ * Results do not depend on either (each receiver's sums run over its edges
+ * in order inside one partition; each atom's update is the same sequence of
+ * MMAs), and the workspace size does not either.  mlff_autotune times
+ * `repeats` calls of mlff_energy_forces per candidate (same arguments; the
+ * outputs are overwritten) with CUDA events on the stream: f = 1, 2, 4 with
+ * 64-atom update tiles, then the fastest f with 32-atom tiles; it
+ * synchronises the stream, caches the fastest shape and writes its f to
+ * *chosen (host) and the milliseconds per call of f = 1, 2, 4 (64-atom
+ * tiles) to ms_per_candidate (host double [3], or NULL).  Not for use while
+ * the stream is being captured.  Other paths: *chosen = 1, nothing timed.
+ * _query reads the factor a call of that size would use, _set pins one
+ * (0 removes the entry; the bucket's update tile is kept), _query_shape
+ * reads both shapes (f, update_atoms) and _set_shape pins both (f = 0
+ * removes the entry), _reset empties the cache.  Untuned buckets use f = 1
+ * and 64-atom update tiles. */
 int mlff_autotune(const mlff_dims *dims, const void *packed, const mlff_system *sys, int64_t edge_capacity,
                   int32_t path, const mlff_outputs *out, void *workspace, size_t workspace_bytes,
                   mlff_stream_t stream, int32_t repeats, int32_t *chosen, double *ms_per_candidate);
 int mlff_autotune_query(int32_t path, int32_t n_atoms, int32_t n_mol, int32_t *factor);
 int mlff_autotune_set(int32_t path, int32_t n_atoms, int32_t n_mol, int32_t factor);
+int mlff_autotune_query_shape(int32_t path, int32_t n_atoms, int32_t n_mol, int32_t *factor, int32_t *update_atoms);
+int mlff_autotune_set_shape(int32_t path, int32_t n_atoms, int32_t n_mol, int32_t factor, int32_t update_atoms);
 int mlff_autotune_reset(void);
 
 /* Force-accuracy statistics on the device (testing/force_metrics.py:46-384,

@@ -59,19 +59,29 @@ int persistent_ctas(int32_t path) {
 }
 
 // ----------------------------------------------------------- autotuning
-// The tensor-core path's receiver partitions per CTA pipeline (the
-// partition factor; 1, 2 or 4: more, smaller partitions balance uneven
-// rows better at the cost of more partial edge tiles) chosen per size
-// bucket (path, ceil(log2 atoms), ceil(log2 structures)) by mlff_autotune
-// and kept in a process-wide cache guarded by a mutex.  Results do not
-// depend on the factor: every receiver's sums run over its edges in order
-// within one partition.  The workspace is sized for the largest factor.
+// Two shapes of the tensor-core path, chosen per size bucket (path,
+// ceil(log2 atoms), ceil(log2 structures)) by mlff_autotune and kept in a
+// process-wide cache guarded by a mutex:
+//  * the receiver partitions per CTA pipeline of the edge kernels (the
+//    partition factor; 1, 2 or 4: more, smaller partitions balance uneven
+//    rows better at the cost of more partial edge tiles);
+//  * the atoms per tile of the update kernels (64 or 32: 32-atom tiles
+//    spread a small system over more SMs, 64-atom tiles stream the weights
+//    once per 64 atoms).
+// Results do not depend on either: every receiver's sums run over its
+// edges in order within one partition, and every atom's update is the same
+// sequence of MMAs.  The workspace is sized for the largest factor.
 constexpr int TUNE_FACTORS[3] = {1, 2, 4};
 constexpr int TUNE_FACTOR_MAX = 4;
+struct TunedShape {
+    int factor;          // partition factor (0: none)
+    int update_atoms;    // atoms per update-kernel tile
+};
+constexpr TunedShape DEFAULT_SHAPE{1, 64};
 namespace {
 std::mutex g_tune_mu;
-std::map<std::tuple<int, int, int>, int> g_tune;
-thread_local int g_tune_override = 0;   // set by mlff_autotune while it times a candidate
+std::map<std::tuple<int, int, int>, TunedShape> g_tune;
+thread_local TunedShape g_tune_override{0, 0};   // set by mlff_autotune while it times a candidate
 int ceil_log2(int64_t x) {
     int b = 0;
     while ((int64_t(1) << b) < x) ++b;
@@ -82,12 +92,12 @@ std::tuple<int, int, int> tune_key(int32_t path, int32_t n_atoms, int32_t n_mol)
 }
 }  // namespace
 
-int tuned_part_factor(int32_t path, int32_t n_atoms, int32_t n_mol) {
-    if (path != MLFF_PATH_TUNED_TC) return 1;
-    if (g_tune_override) return g_tune_override;
+TunedShape tuned_shape(int32_t path, int32_t n_atoms, int32_t n_mol) {
+    if (path != MLFF_PATH_TUNED_TC) return DEFAULT_SHAPE;
+    if (g_tune_override.factor) return g_tune_override;
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(tune_key(path, n_atoms, n_mol));
-    return it == g_tune.end() ? 1 : it->second;
+    return it == g_tune.end() ? DEFAULT_SHAPE : it->second;
 }
 
 WsLayout ws_layout(const mlff_dims& d, int32_t n_atoms, int32_t n_mol, int64_t cap, int32_t path) {
@@ -97,7 +107,9 @@ WsLayout ws_layout(const mlff_dims& d, int32_t n_atoms, int32_t n_mol, int64_t c
     L.L = d.n_layers;
     // arrays sized for the largest partition factor, so that tuning never changes the size
     const int64_t P_max = (int64_t)persistent_ctas(path) * (path == MLFF_PATH_TUNED_TC ? TUNE_FACTOR_MAX : 1);
-    L.P = persistent_ctas(path) * tuned_part_factor(path, n_atoms, n_mol);
+    const TunedShape shape = tuned_shape(path, n_atoms, n_mol);
+    L.P = persistent_ctas(path) * shape.factor;
+    L.UT = shape.update_atoms;
     L.cap = cap;
     // Morton code spaces of the cell grids: under 8 x max(n_atoms, 27) per structure
     L.ncell_cap = 8LL * ((int64_t)n_atoms + 27LL * n_mol);
@@ -360,28 +372,39 @@ int mlff_autotune(const mlff_dims* dims, const void* packed, const mlff_system* 
         cudaEventDestroy(e0);
         return cuda_status(ce, "cudaEventCreate");
     }
-    int best = 1, r = MLFF_OK;
-    float best_ms = 0.f;
-    for (int i = 0; i < 3 && r == MLFF_OK; ++i) {
-        g_tune_override = TUNE_FACTORS[i];
+    int r = MLFF_OK;
+    // mean milliseconds per call of one candidate shape
+    auto time_shape = [&](TunedShape sh, float& ms) {
+        g_tune_override = sh;
         r = mlff_energy_forces(dims, packed, sys, edge_capacity, path, out, workspace, workspace_bytes, stream);
         if (r == MLFF_OK && (ce = cudaEventRecord(e0, st)) != cudaSuccess) r = cuda_status(ce, "cudaEventRecord");
         for (int k = 0; k < repeats && r == MLFF_OK; ++k)
             r = mlff_energy_forces(dims, packed, sys, edge_capacity, path, out, workspace, workspace_bytes, stream);
-        float ms = 0.f;
         if (r == MLFF_OK && (ce = cudaEventRecord(e1, st)) != cudaSuccess) r = cuda_status(ce, "cudaEventRecord");
         if (r == MLFF_OK && (ce = cudaEventSynchronize(e1)) != cudaSuccess) r = cuda_status(ce, "cudaEventSynchronize");
         if (r == MLFF_OK && (ce = cudaEventElapsedTime(&ms, e0, e1)) != cudaSuccess) r = cuda_status(ce, "cudaEventElapsedTime");
+        if (r == MLFF_OK) ms /= repeats;
+    };
+    // the partition factor with 64-atom update tiles, then the winner with 32-atom tiles
+    TunedShape best = DEFAULT_SHAPE;
+    float best_ms = 0.f;
+    for (int i = 0; i < 3 && r == MLFF_OK; ++i) {
+        float ms = 0.f;
+        time_shape(TunedShape{TUNE_FACTORS[i], 64}, ms);
         if (r == MLFF_OK) {
-            ms /= repeats;
             if (ms_per_candidate) ms_per_candidate[i] = ms;
             if (i == 0 || ms < best_ms) {
                 best_ms = ms;
-                best = TUNE_FACTORS[i];
+                best = TunedShape{TUNE_FACTORS[i], 64};
             }
         }
     }
-    g_tune_override = 0;
+    if (r == MLFF_OK) {
+        float ms = 0.f;
+        time_shape(TunedShape{best.factor, 32}, ms);
+        if (r == MLFF_OK && ms < best_ms) best.update_atoms = 32;
+    }
+    g_tune_override = TunedShape{0, 0};
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (r) return r;
@@ -397,13 +420,21 @@ int mlff_autotune(const mlff_dims* dims, const void* packed, const mlff_system* 
         std::lock_guard<std::mutex> lk(g_tune_mu);
         g_tune[tune_key(path, sys->n_atoms, sys->n_mol)] = best;
     }
-    if (chosen) *chosen = best;
+    if (chosen) *chosen = best.factor;
     return MLFF_OK;
 }
 
 int mlff_autotune_query(int32_t path, int32_t n_atoms, int32_t n_mol, int32_t* factor) {
     if (!factor) { set_error("factor is required"); return MLFF_ERR_INVALID; }
-    *factor = tuned_part_factor(path, n_atoms, n_mol);
+    *factor = tuned_shape(path, n_atoms, n_mol).factor;
+    return MLFF_OK;
+}
+
+int mlff_autotune_query_shape(int32_t path, int32_t n_atoms, int32_t n_mol, int32_t* factor, int32_t* update_atoms) {
+    if (!factor || !update_atoms) { set_error("factor and update_atoms are required"); return MLFF_ERR_INVALID; }
+    const TunedShape sh = tuned_shape(path, n_atoms, n_mol);
+    *factor = sh.factor;
+    *update_atoms = sh.update_atoms;
     return MLFF_OK;
 }
 
@@ -414,8 +445,29 @@ int mlff_autotune_set(int32_t path, int32_t n_atoms, int32_t n_mol, int32_t fact
     }
     if (path != MLFF_PATH_TUNED_TC) { set_error("only the tensor-core path has a tunable shape"); return MLFF_ERR_INVALID; }
     std::lock_guard<std::mutex> lk(g_tune_mu);
+    const auto key = tune_key(path, n_atoms, n_mol);
+    if (factor == 0) {
+        g_tune.erase(key);
+    } else {
+        auto it = g_tune.find(key);   // the bucket's update tile stays as it was
+        g_tune[key] = TunedShape{factor, it == g_tune.end() ? DEFAULT_SHAPE.update_atoms : it->second.update_atoms};
+    }
+    return MLFF_OK;
+}
+
+int mlff_autotune_set_shape(int32_t path, int32_t n_atoms, int32_t n_mol, int32_t factor, int32_t update_atoms) {
+    if (factor != 0 && factor != 1 && factor != 2 && factor != 4) {
+        set_error("partition factor %d: use 1, 2 or 4 (0 removes the entry)", factor);
+        return MLFF_ERR_INVALID;
+    }
+    if (factor != 0 && update_atoms != 32 && update_atoms != 64) {
+        set_error("update tile %d atoms: use 32 or 64", update_atoms);
+        return MLFF_ERR_INVALID;
+    }
+    if (path != MLFF_PATH_TUNED_TC) { set_error("only the tensor-core path has a tunable shape"); return MLFF_ERR_INVALID; }
+    std::lock_guard<std::mutex> lk(g_tune_mu);
     if (factor == 0) g_tune.erase(tune_key(path, n_atoms, n_mol));
-    else g_tune[tune_key(path, n_atoms, n_mol)] = factor;
+    else g_tune[tune_key(path, n_atoms, n_mol)] = TunedShape{factor, update_atoms};
     return MLFF_OK;
 }
 

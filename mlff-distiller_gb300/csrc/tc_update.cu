@@ -21,6 +21,7 @@
 // runs).  The forward accumulators are pre-filled with the bias, so every
 // MMA accumulates.  Every wait is bounded (MLFF_ERR_TIMEOUT).
 #include <cuda_fp16.h>
+#include <mutex>
 #include "common.cuh"
 #include "workspace.h"
 #include "profile.h"
@@ -69,10 +70,7 @@ int pack_update_tc(const mlff_dims& d, float* out, const PackedOffsets& o, cudaS
 }
 
 // ------------------------------------------------------- weight stream
-constexpr int URING_F = 5;    // forward: two CTAs per SM (at most 113 KB of shared memory each)
-constexpr int URING_B = 2;    // reverse: two CTAs per SM (the 96 KB abar tile leaves room for two slots)
 constexpr int UNT = 256;
-constexpr int UN = 64;
 
 template <int URING>
 struct UStream {
@@ -111,7 +109,7 @@ __device__ __forceinline__ bool ustream_fill(UStream<URING>& s, uint32_t target)
 // consumer: one GEMM of a tile.  Pair i of n (global pair P0 + i): D[d_of(i)]
 // += A_hi B_hi(i) + A_hi B_lo(i) + A_lo B_hi(i); the first MMA of pair i
 // overwrites D instead when fresh(i).
-template <int URING, typename DOf, typename BOf, typename Fresh>
+template <int UN, int URING, typename DOf, typename BOf, typename Fresh>
 __device__ __forceinline__ bool ustream_gemm(UStream<URING>& s, uint32_t P0, int n, DOf d_of, BOf b_of, uint64_t bhalf,
                                              Fresh fresh) {
     constexpr uint32_t idesc = idesc_f16(UN);
@@ -141,11 +139,12 @@ __device__ __forceinline__ void ufill_tmem(uint32_t taddr, float v, int n16) {
 }
 
 // four consecutive K values (k % 4 == 0) of one row as split fp16
-__device__ __forceinline__ void store_row4(unsigned char* tile, uint32_t half_bytes, int row, int k, float4 v) {
+__device__ __forceinline__ void store_row4(unsigned char* tile, uint32_t half_bytes, int n_rows, int row, int k,
+                                           float4 v) {
     __half2 h0, l0, h1, l1;
     split2(v.x, v.y, h0, l0);
     split2(v.z, v.w, h1, l1);
-    const uint32_t o = b_off(UN, row, k);
+    const uint32_t o = b_off(n_rows, row, k);
     uint2 hv, lv;
     hv.x = *reinterpret_cast<uint32_t*>(&h0);
     hv.y = *reinterpret_cast<uint32_t*>(&h1);
@@ -182,40 +181,52 @@ __device__ __forceinline__ void uwait_mma(UCtl& c, int w, int where) {
 // ------------------------------------------------------- forward kernel
 // smem: B tile [s, |v|] (K = 256: 4 K-blocks; hi half then lo half, 64 KB),
 // the H tile (K = 128, 32 KB) aliased into it after GEMM1, the ring (40 KB).
-// TMEM: D1 = z (cols 0-63), D2 chunk g = (ds, g1, g2)[g] (64 + 64 g).
-constexpr uint32_t UF_BH = 4 * b_block(UN);
-constexpr uint32_t UF_HH = 2 * b_block(UN);
-constexpr uint32_t UF_OFF_B = 0;
-constexpr uint32_t UF_OFF_RING = UF_OFF_B + 2 * UF_BH;
-constexpr uint32_t UF_OFF_C = UF_OFF_RING + URING_F * A_PAIR;      // c1 [H], c2 [3H], mix [9]
-constexpr uint32_t UF_OFF_BAR = UF_OFF_C + 4 * (H + H3 + 16);
-constexpr uint32_t UF_OFF_MISC = UF_OFF_BAR + 8 * (1 + 2 * URING_F);
-constexpr uint32_t UF_SMEM = align1k(UF_OFF_MISC + 16);
-static_assert(2 * (UF_SMEM + 1024) <= 228 * 1024, "two update CTAs per SM");
+// TMEM: D1 = z (cols 0..UN-1), D2 chunk g = (ds, g1, g2)[g] (UN + UN g).
+// UN-atom tiles, UN = 64 or 32 (the autotuner's update tile: small systems
+// spread over more SMs with 32); the ring takes what two CTAs per SM leave.
+template <int UN>
+struct UFwd {
+    static constexpr uint32_t BH = 4 * b_block(UN);
+    static constexpr uint32_t HH = 2 * b_block(UN);
+    // epilogue 2 stages (ds, g1, g2) of 32 atoms, [3][32][H] floats, in the B region
+    static constexpr uint32_t T_BYTES = 3 * 32 * H * 4;
+    static constexpr uint32_t B_REGION = 2 * BH > T_BYTES ? 2 * BH : T_BYTES;
+    static constexpr int RING = UN == 64 ? 5 : 7;
+    static constexpr uint32_t OFF_B = 0;
+    static constexpr uint32_t OFF_RING = OFF_B + B_REGION;
+    static constexpr uint32_t OFF_C = OFF_RING + RING * A_PAIR;      // c1 [H], c2 [3H], mix [9]
+    static constexpr uint32_t OFF_BAR = OFF_C + 4 * (H + H3 + 16);
+    static constexpr uint32_t OFF_MISC = OFF_BAR + 8 * (1 + 2 * RING);
+    static constexpr uint32_t SMEM = align1k(OFF_MISC + 16);
+    static constexpr uint32_t TMEM_COLS = 4 * UN;
+    static_assert(2 * (SMEM + 1024) <= 228 * 1024, "two update CTAs per SM");
+};
 
+template <int UN>
 __global__ void __launch_bounds__(UNT, 2) update_fwd_tc_kernel(const float* __restrict__ P, LayerOffsets lo,
                                                                const float* __restrict__ Xt, int32_t n_atoms,
                                                                float* __restrict__ Xout, float* __restrict__ uz,
                                                                float* __restrict__ ua, Status* st) {
+    using LF = UFwd<UN>;
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char* Bs = smem + UF_OFF_B;
-    float* c1s = reinterpret_cast<float*>(smem + UF_OFF_C);
+    unsigned char* Bs = smem + LF::OFF_B;
+    float* c1s = reinterpret_cast<float*>(smem + LF::OFF_C);
     float* c2s = c1s + H;
     float* mix = c2s + H3;
-    uint64_t* mma_bar = reinterpret_cast<uint64_t*>(smem + UF_OFF_BAR);
+    uint64_t* mma_bar = reinterpret_cast<uint64_t*>(smem + LF::OFF_BAR);
     uint64_t* full = mma_bar + 1;
-    uint64_t* empty = full + URING_F;
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + UF_OFF_MISC);
-    volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + UF_OFF_MISC + 4);
+    uint64_t* empty = full + LF::RING;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + LF::OFF_MISC);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + LF::OFF_MISC + 4);
     const int t = threadIdx.x, w = t >> 5, lane = t & 31;
     const int ntiles = (n_atoms + UN - 1) / UN;
     if (w == 0) {
-        tmem_alloc(tslot, 256);
+        tmem_alloc(tslot, LF::TMEM_COLS);
         tmem_relinquish();
     }
     if (t == 0) {
         mbar_init(mma_bar, 1);
-        for (int i = 0; i < URING_F; ++i) {
+        for (int i = 0; i < LF::RING; ++i) {
             mbar_init(&full[i], 1);
             mbar_init(&empty[i], 1);
         }
@@ -229,14 +240,14 @@ __global__ void __launch_bounds__(UNT, 2) update_fwd_tc_kernel(const float* __re
     __syncthreads();
     fence_after_sync();
     const uint32_t tmem = *tslot;
-    UStream<URING_F> ws{smem + UF_OFF_RING, full, empty,
+    UStream<LF::RING> ws{smem + LF::OFF_RING, full, empty,
                {reinterpret_cast<const unsigned char*>(P + lo.u1_tc), reinterpret_cast<const unsigned char*>(P + lo.u2_tc)},
                {16, 24}, 0, 0};
     UCtl ctl{mma_bar, abort_flag, st, 0};
     const int my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
     const uint32_t P_end = (uint32_t)my_tiles * 40;
     const bool producer = t == 32;
-    if (producer && !ustream_fill(ws, min((uint32_t)URING_F, P_end))) ufail(ctl, 20);
+    if (producer && !ustream_fill(ws, min((uint32_t)LF::RING, P_end))) ufail(ctl, 20);
     // everything above reads packed weights only and overlaps the previous kernel
     pdl_wait();
     if (t == 0 && st->code != 0) *abort_flag = 1;
@@ -249,9 +260,9 @@ __global__ void __launch_bounds__(UNT, 2) update_fwd_tc_kernel(const float* __re
     for (int tile = blockIdx.x; tile < ntiles && !*abort_flag; tile += gridDim.x, P0 += 40) {
         const int a0 = tile * UN;
         // accumulators <- bias: D1 c1, D2 chunk g c2[g]
-        ufill_tmem(lane_base + 32 * hh, c1s[c], 2);
+        ufill_tmem(lane_base + (UN / 2) * hh, c1s[c], UN / 32);
 #pragma unroll 1
-        for (int g = 0; g < 3; ++g) ufill_tmem(lane_base + 64 + 64 * g + 32 * hh, c2s[g * H + c], 2);
+        for (int g = 0; g < 3; ++g) ufill_tmem(lane_base + UN + UN * g + (UN / 2) * hh, c2s[g * H + c], UN / 32);
         // B tile: row = atom, K = [s (128), |v| (128)]; warp w builds rows w, w + 8, ...,
         // two rows per step so that their loads overlap
 #pragma unroll 1
@@ -269,8 +280,8 @@ __global__ void __launch_bounds__(UNT, 2) update_fwd_tc_kernel(const float* __re
                 const float4 vx = r[k][1], vy = r[k][2], vz = r[k][3];
                 const float4 nv = make_float4(pair_distance(vx.x, vy.x, vz.x), pair_distance(vx.y, vy.y, vz.y),
                                               pair_distance(vx.z, vy.z, vz.z), pair_distance(vx.w, vy.w, vz.w));  // |v| (:437)
-                store_row4(Bs, UF_BH, i0 + 8 * k, 4 * lane, r[k][0]);
-                store_row4(Bs, UF_BH, i0 + 8 * k, H + 4 * lane, nv);
+                store_row4(Bs, LF::BH, UN, i0 + 8 * k, 4 * lane, r[k][0]);
+                store_row4(Bs, LF::BH, UN, i0 + 8 * k, H + 4 * lane, nv);
             }
         }
         tmem_st_wait();
@@ -280,8 +291,8 @@ __global__ void __launch_bounds__(UNT, 2) update_fwd_tc_kernel(const float* __re
         if (t == 0) {   // GEMM1: z^T = U1 [s, |v|]^T, K = 256
             fence_after_sync();
             const uint64_t b0 = sdesc_b(smem_u32(Bs));
-            if (!ustream_gemm(ws, P0, 16, [&](int) { return tmem; },
-                              [&](int i) { return b0 + (uint64_t)(b_kstep_off(UN, i) >> 4); }, (uint64_t)(UF_BH >> 4),
+            if (!ustream_gemm<UN>(ws, P0, 16, [&](int) { return tmem; },
+                              [&](int i) { return b0 + (uint64_t)(b_kstep_off(UN, i) >> 4); }, (uint64_t)(LF::BH >> 4),
                               [](int) { return false; }))
                 ufail(ctl, 21);
             mma_commit(mma_bar);
@@ -289,15 +300,17 @@ __global__ void __launch_bounds__(UNT, 2) update_fwd_tc_kernel(const float* __re
         if (producer && !ustream_fill(ws, min(P0 + 16, P_end))) ufail(ctl, 26);
         uwait_mma(ctl, w, 22);
         // GEMM1 is done, so every slot is free: fetch GEMM2's pairs during epilogue 1
-        if (producer && !ustream_fill(ws, min(P0 + 16 + URING_F, P_end))) ufail(ctl, 27);
+        if (producer && !ustream_fill(ws, min(P0 + 16 + LF::RING, P_end))) ufail(ctl, 27);
         {   // epilogue 1: z -> uz, h = silu(z) -> H tile (aliases the B tile)
-            const int col = 32 * hh;
-            float z[32];
-            tmem_ld32(lane_base + col, z);
+            constexpr int NC = UN / 2;   // this warp half's atoms
+            const int col = NC * hh;
+            float z[NC];
+            if constexpr (NC == 32) tmem_ld32(lane_base + col, z);
+            else tmem_ld16(lane_base + col, z);
             tmem_ld_wait();
-            const BColumn hcol(Bs, UF_HH, UN, col, c);
+            const BColumn hcol(Bs, LF::HH, UN, col, c);
 #pragma unroll
-            for (int i = 0; i < 32; i += 2) {
+            for (int i = 0; i < NC; i += 2) {
                 const int a = a0 + col + i;
                 if (a < n_atoms) uz[(int64_t)a * H + c] = z[i];
                 if (a + 1 < n_atoms) uz[(int64_t)(a + 1) * H + c] = z[i + 1];
@@ -312,28 +325,28 @@ __global__ void __launch_bounds__(UNT, 2) update_fwd_tc_kernel(const float* __re
         if (t == 0) {   // GEMM2: a^T = U2 h^T, 3 chunks x 8 K-steps
             fence_after_sync();
             const uint64_t b0 = sdesc_b(smem_u32(Bs));
-            if (!ustream_gemm(ws, P0 + 16, 24, [&](int i) { return tmem + 64 + 64 * (i >> 3); },
+            if (!ustream_gemm<UN>(ws, P0 + 16, 24, [&](int i) { return tmem + UN + UN * (i >> 3); },
                               [&](int i) { return b0 + (uint64_t)(b_kstep_off(UN, i & 7) >> 4); },
-                              (uint64_t)(UF_HH >> 4), [](int) { return false; }))
+                              (uint64_t)(LF::HH >> 4), [](int) { return false; }))
                 ufail(ctl, 23);
             mma_commit(mma_bar);
         }
         if (producer && !ustream_fill(ws, min(P0 + 40, P_end))) ufail(ctl, 28);
         uwait_mma(ctl, w, 24);
         // the next tile's GEMM1 pairs arrive while this epilogue and the next build run
-        if (producer && !ustream_fill(ws, min(P0 + 40 + URING_F, P_end))) ufail(ctl, 29);
+        if (producer && !ustream_fill(ws, min(P0 + 40 + LF::RING, P_end))) ufail(ctl, 29);
         {   // epilogue 2: (ds, g1, g2) -> ua; s' = s + ds, v' = v g1 + (M v) g2 (:452-468).
             // The TMEM owner of channel c writes (ds, g1, g2) of 32 atoms to
             // shared memory (the B tile is free), then each warp handles
-            // whole atom rows with 128-bit accesses; two passes of 32 atoms.
+            // whole atom rows with 128-bit accesses; UN / 32 passes of 32 atoms.
             float* T = reinterpret_cast<float*>(Bs);      // [3][32 atoms][H]
 #pragma unroll 1
-            for (int pass = 0; pass < 2; ++pass) {
+            for (int pass = 0; pass < UN / 32; ++pass) {
                 if (hh == pass) {
 #pragma unroll 1
                     for (int g = 0; g < 3; ++g) {
                         float v[32];
-                        tmem_ld32(lane_base + 64 + 64 * g + 32 * pass, v);
+                        tmem_ld32(lane_base + UN + UN * g + 32 * pass, v);
                         tmem_ld_wait();
 #pragma unroll
                         for (int i = 0; i < 32; ++i) T[(g * 32 + i) * H + c] = v[i];
@@ -395,10 +408,10 @@ __global__ void __launch_bounds__(UNT, 2) update_fwd_tc_kernel(const float* __re
     // drain: every pair copied must have landed before the CTA exits
     __syncthreads();
     if (producer) {
-        // copies still in flight are among the last URING_F issued (a slot is
+        // copies still in flight are among the last LF::RING issued (a slot is
         // refilled only after its previous copy was consumed)
-        for (uint32_t f = ws.issued > (uint32_t)URING_F ? ws.issued - URING_F : 0u; f < ws.issued; ++f)
-            if (!mbar_wait(&full[f % URING_F], (f / URING_F) & 1, WAIT_BUDGET)) {
+        for (uint32_t f = ws.issued > (uint32_t)LF::RING ? ws.issued - LF::RING : 0u; f < ws.issued; ++f)
+            if (!mbar_wait(&full[f % LF::RING], (f / LF::RING) & 1, WAIT_BUDGET)) {
                 set_status(st, MLFF_ERR_TIMEOUT, 25);
                 break;
             }
@@ -406,18 +419,21 @@ __global__ void __launch_bounds__(UNT, 2) update_fwd_tc_kernel(const float* __re
     fence_before_sync();
     __syncthreads();
     fence_after_sync();
-    if (w == 0) tmem_dealloc(tmem, 256);
+    if (w == 0) tmem_dealloc(tmem, LF::TMEM_COLS);
 }
 
-int launch_update_fwd_tc(const float* packed, const LayerOffsets& lo, const WsLayout& L, void* ws, int layer,
-                         cudaStream_t st) {
-    static bool attr_done = false;
-    if (!attr_done) {
-        cudaError_t e = cudaFuncSetAttribute(update_fwd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             UF_SMEM);
-        if (e != cudaSuccess) return cuda_status(e, "update_fwd_tc smem attribute");
-        attr_done = true;
-    }
+// UN-atom tiles, two CTAs per SM: one CTA's epilogues overlap the other's
+// weight stream and MMAs
+template <int UN>
+static int launch_update_fwd_tc_t(const float* packed, const LayerOffsets& lo, const WsLayout& L, void* ws, int layer,
+                                  cudaStream_t st) {
+    static std::once_flag once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(once, [] {
+        attr_err = cudaFuncSetAttribute(update_fwd_tc_kernel<UN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        UFwd<UN>::SMEM);
+    });
+    if (attr_err != cudaSuccess) return cuda_status(attr_err, "update_fwd_tc smem attribute");
     ProfScope prof(PK_UPDATE_FWD, st);
     const int64_t NX = (int64_t)L.N * 4 * H;
     const float* Xt = ws_ptr<float>(ws, L.Xt) + layer * NX;
@@ -425,11 +441,16 @@ int launch_update_fwd_tc(const float* packed, const LayerOffsets& lo, const WsLa
     float* uz = ws_ptr<float>(ws, L.uz) + (int64_t)layer * L.N * H;
     float* ua = ws_ptr<float>(ws, L.ua) + (int64_t)layer * L.N * H3;
     const int ntiles = (L.N + UN - 1) / UN;
-    // two CTAs per SM: one's epilogues overlap the other's weight stream and MMAs
     const int grid = std::max(1, std::min(ntiles, 2 * num_sms()));
-    MLFF_LAUNCH_PDL("update_fwd_tc", update_fwd_tc_kernel, grid, UNT, UF_SMEM, st, packed, lo, Xt, L.N, Xout, uz, ua,
-                    ws_ptr<Status>(ws, L.status));
+    MLFF_LAUNCH_PDL("update_fwd_tc", update_fwd_tc_kernel<UN>, grid, UNT, UFwd<UN>::SMEM, st, packed, lo, Xt, L.N,
+                    Xout, uz, ua, ws_ptr<Status>(ws, L.status));
     return MLFF_OK;
+}
+
+int launch_update_fwd_tc(const float* packed, const LayerOffsets& lo, const WsLayout& L, void* ws, int layer,
+                         cudaStream_t st) {
+    return L.UT == 32 ? launch_update_fwd_tc_t<32>(packed, lo, L, ws, layer, st)
+                      : launch_update_fwd_tc_t<64>(packed, lo, L, ws, layer, st);
 }
 
 // ------------------------------------------------------- reverse kernel
@@ -437,39 +458,47 @@ int launch_update_fwd_tc(const float* packed, const LayerOffsets& lo, const WsLa
 // cb = U1^T zbar = dE/d[s, |v|]; xtbar = (sb + cs, vb + cn v / |v|).
 // smem: abar B tile (K = 384: 6 K-blocks, hi then lo, 96 KB), the zbar tile
 // (K = 128, 32 KB) aliased into it after GEMM3, the ring (16 KB).
-// TMEM: D3 = zbar pre-activation (cols 0-63), D4 = (cs, cn) (64-191).
-constexpr uint32_t UB_AH = 6 * b_block(UN);
-constexpr uint32_t UB_ZH = 2 * b_block(UN);
-constexpr uint32_t UB_OFF_B = 0;
-constexpr uint32_t UB_OFF_RING = UB_OFF_B + 2 * UB_AH;
-constexpr uint32_t UB_OFF_MIX = UB_OFF_RING + URING_B * A_PAIR;
-constexpr uint32_t UB_OFF_BAR = UB_OFF_MIX + 64;
-constexpr uint32_t UB_OFF_MISC = UB_OFF_BAR + 8 * (1 + 2 * URING_B);
-constexpr uint32_t UB_SMEM = align1k(UB_OFF_MISC + 16);
-static_assert(2 * (UB_SMEM + 1024) <= 228 * 1024, "two update reverse CTAs per SM");
+// TMEM: D3 = zbar pre-activation (cols 0..UN-1), D4 = (cs, cn) (UN + UN g).
+template <int UN>
+struct UBwd {
+    static constexpr uint32_t AH = 6 * b_block(UN);
+    static constexpr uint32_t ZH = 2 * b_block(UN);
+    static constexpr int RING = UN == 64 ? 2 : 7;
+    static constexpr uint32_t OFF_B = 0;
+    static constexpr uint32_t OFF_RING = OFF_B + 2 * AH;
+    static constexpr uint32_t OFF_MIX = OFF_RING + RING * A_PAIR;
+    static constexpr uint32_t OFF_BAR = OFF_MIX + 64;
+    static constexpr uint32_t OFF_MISC = OFF_BAR + 8 * (1 + 2 * RING);
+    static constexpr uint32_t SMEM = align1k(OFF_MISC + 16);
+    static constexpr uint32_t TMEM_COLS = UN == 64 ? 256 : 128;   // 3 UN columns, a power of two
+    static_assert(2 * (SMEM + 1024) <= 228 * 1024, "two update reverse CTAs per SM");
+    static_assert(2 * UN * H * 4 <= 2 * AH, "epilogue 4 stages (cs, cn) of the tile in the abar region");
+};
 
+template <int UN>
 __global__ void __launch_bounds__(UNT, 2) update_bwd_tc_kernel(const float* __restrict__ P, LayerOffsets lo,
                                                                const float* __restrict__ Xt, const float* __restrict__ uz,
                                                                const float* __restrict__ ua,
                                                                const float* __restrict__ xbo, int32_t n_atoms,
                                                                float* __restrict__ xtbar, Status* st) {
+    using LB = UBwd<UN>;
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char* Bs = smem + UB_OFF_B;
-    float* mix = reinterpret_cast<float*>(smem + UB_OFF_MIX);
-    uint64_t* mma_bar = reinterpret_cast<uint64_t*>(smem + UB_OFF_BAR);
+    unsigned char* Bs = smem + LB::OFF_B;
+    float* mix = reinterpret_cast<float*>(smem + LB::OFF_MIX);
+    uint64_t* mma_bar = reinterpret_cast<uint64_t*>(smem + LB::OFF_BAR);
     uint64_t* full = mma_bar + 1;
-    uint64_t* empty = full + URING_B;
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + UB_OFF_MISC);
-    volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + UB_OFF_MISC + 4);
+    uint64_t* empty = full + LB::RING;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + LB::OFF_MISC);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + LB::OFF_MISC + 4);
     const int t = threadIdx.x, w = t >> 5, lane = t & 31;
     const int ntiles = (n_atoms + UN - 1) / UN;
     if (w == 0) {
-        tmem_alloc(tslot, 256);
+        tmem_alloc(tslot, LB::TMEM_COLS);
         tmem_relinquish();
     }
     if (t == 0) {
         mbar_init(mma_bar, 1);
-        for (int i = 0; i < URING_B; ++i) {
+        for (int i = 0; i < LB::RING; ++i) {
             mbar_init(&full[i], 1);
             mbar_init(&empty[i], 1);
         }
@@ -481,14 +510,14 @@ __global__ void __launch_bounds__(UNT, 2) update_bwd_tc_kernel(const float* __re
     __syncthreads();
     fence_after_sync();
     const uint32_t tmem = *tslot;
-    UStream<URING_B> ws{smem + UB_OFF_RING, full, empty,
+    UStream<LB::RING> ws{smem + LB::OFF_RING, full, empty,
                {reinterpret_cast<const unsigned char*>(P + lo.u2t_tc), reinterpret_cast<const unsigned char*>(P + lo.u1t_tc)},
                {24, 16}, 0, 0};
     UCtl ctl{mma_bar, abort_flag, st, 0};
     const int my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
     const uint32_t P_end = (uint32_t)my_tiles * 40;
     const bool producer = t == 32;
-    if (producer && !ustream_fill(ws, min((uint32_t)URING_B, P_end))) ufail(ctl, 30);
+    if (producer && !ustream_fill(ws, min((uint32_t)LB::RING, P_end))) ufail(ctl, 30);
     // everything above reads packed weights only and overlaps the previous kernel
     pdl_wait();
     if (t == 0 && st->code != 0) *abort_flag = 1;
@@ -530,9 +559,9 @@ __global__ void __launch_bounds__(UNT, 2) update_bwd_tc_kernel(const float* __re
                 gpart(bx.z, by.z, bz.z, vx.z, vy.z, vz.z, g1.z, g2.z);
                 gpart(bx.w, by.w, bz.w, vx.w, vy.w, vz.w, g1.w, g2.w);
                 const int i = i0 + 8 * k;
-                store_row4(Bs, UB_AH, i, 4 * lane, r[k][0]);
-                store_row4(Bs, UB_AH, i, H + 4 * lane, g1);
-                store_row4(Bs, UB_AH, i, 2 * H + 4 * lane, g2);
+                store_row4(Bs, LB::AH, UN, i, 4 * lane, r[k][0]);
+                store_row4(Bs, LB::AH, UN, i, H + 4 * lane, g1);
+                store_row4(Bs, LB::AH, UN, i, 2 * H + 4 * lane, g2);
             }
         }
         fence_async_smem();
@@ -541,29 +570,31 @@ __global__ void __launch_bounds__(UNT, 2) update_bwd_tc_kernel(const float* __re
         if (t == 0) {   // GEMM3: zbar_pre^T = U2^T abar^T, K = 384
             fence_after_sync();
             const uint64_t b0 = sdesc_b(smem_u32(Bs));
-            if (!ustream_gemm(ws, P0, 24, [&](int) { return tmem; },
-                              [&](int i) { return b0 + (uint64_t)(b_kstep_off(UN, i) >> 4); }, (uint64_t)(UB_AH >> 4),
+            if (!ustream_gemm<UN>(ws, P0, 24, [&](int) { return tmem; },
+                              [&](int i) { return b0 + (uint64_t)(b_kstep_off(UN, i) >> 4); }, (uint64_t)(LB::AH >> 4),
                               [](int i) { return i == 0; }))
                 ufail(ctl, 31);
             mma_commit(mma_bar);
         }
         if (producer && !ustream_fill(ws, min(P0 + 24, P_end))) ufail(ctl, 36);
         uwait_mma(ctl, w, 32);
-        if (producer && !ustream_fill(ws, min(P0 + 24 + URING_B, P_end))) ufail(ctl, 37);
+        if (producer && !ustream_fill(ws, min(P0 + 24 + LB::RING, P_end))) ufail(ctl, 37);
         {   // epilogue 3: zbar = D3 silu'(uz) -> zbar tile (aliases the abar tile)
-            const int col = 32 * hh;
-            float zb[32];
-            tmem_ld32(lane_base + col, zb);
-            float zz[32];
+            constexpr int NC = UN / 2;   // this warp half's atoms
+            const int col = NC * hh;
+            float zb[NC];
+            if constexpr (NC == 32) tmem_ld32(lane_base + col, zb);
+            else tmem_ld16(lane_base + col, zb);
+            float zz[NC];
 #pragma unroll
-            for (int i = 0; i < 32; ++i) {
+            for (int i = 0; i < NC; ++i) {
                 const int a = a0 + col + i;
                 zz[i] = a < n_atoms ? uz[(int64_t)a * H + c] : 0.f;
             }
             tmem_ld_wait();
-            const BColumn zcol(Bs, UB_ZH, UN, col, c);
+            const BColumn zcol(Bs, LB::ZH, UN, col, c);
 #pragma unroll
-            for (int i = 0; i < 32; i += 2) zcol.put_pair(i, zb[i] * dsilu_f(zz[i]), zb[i + 1] * dsilu_f(zz[i + 1]));
+            for (int i = 0; i < NC; i += 2) zcol.put_pair(i, zb[i] * dsilu_f(zz[i]), zb[i + 1] * dsilu_f(zz[i + 1]));
         }
         fence_async_smem();
         fence_before_sync();
@@ -571,15 +602,15 @@ __global__ void __launch_bounds__(UNT, 2) update_bwd_tc_kernel(const float* __re
         if (t == 0) {   // GEMM4: cb^T = U1^T zbar^T, 2 chunks x 8 K-steps
             fence_after_sync();
             const uint64_t b0 = sdesc_b(smem_u32(Bs));
-            if (!ustream_gemm(ws, P0 + 24, 16, [&](int i) { return tmem + 64 + 64 * (i >> 3); },
+            if (!ustream_gemm<UN>(ws, P0 + 24, 16, [&](int i) { return tmem + UN + UN * (i >> 3); },
                               [&](int i) { return b0 + (uint64_t)(b_kstep_off(UN, i & 7) >> 4); },
-                              (uint64_t)(UB_ZH >> 4), [](int i) { return (i & 7) == 0; }))
+                              (uint64_t)(LB::ZH >> 4), [](int i) { return (i & 7) == 0; }))
                 ufail(ctl, 33);
             mma_commit(mma_bar);
         }
         if (producer && !ustream_fill(ws, min(P0 + 40, P_end))) ufail(ctl, 38);
         uwait_mma(ctl, w, 34);
-        if (producer && !ustream_fill(ws, min(P0 + 40 + URING_B, P_end))) ufail(ctl, 39);
+        if (producer && !ustream_fill(ws, min(P0 + 40 + LB::RING, P_end))) ufail(ctl, 39);
         {   // epilogue 4: xtbar = (sb + cs, xb g1 + M^T xb g2 + cn v / |v|).  The
             // TMEM owner of channel c writes (cs, cn) of its 32 atoms to shared
             // memory (the abar tile is free), then each warp handles whole atom
@@ -587,11 +618,13 @@ __global__ void __launch_bounds__(UNT, 2) update_bwd_tc_kernel(const float* __re
             float* T = reinterpret_cast<float*>(Bs);      // [2][UN atoms][H]
 #pragma unroll 1
             for (int g = 0; g < 2; ++g) {
-                float v[32];
-                tmem_ld32(lane_base + 64 + 64 * g + 32 * hh, v);
+                constexpr int NC = UN / 2;
+                float v[NC];
+                if constexpr (NC == 32) tmem_ld32(lane_base + UN + UN * g + NC * hh, v);
+                else tmem_ld16(lane_base + UN + UN * g + NC * hh, v);
                 tmem_ld_wait();
 #pragma unroll
-                for (int i = 0; i < 32; ++i) T[(g * UN + 32 * hh + i) * H + c] = v[i];
+                for (int i = 0; i < NC; ++i) T[(g * UN + NC * hh + i) * H + c] = v[i];
             }
             __syncthreads();
 #pragma unroll 1
@@ -646,10 +679,10 @@ __global__ void __launch_bounds__(UNT, 2) update_bwd_tc_kernel(const float* __re
     }
     __syncthreads();
     if (producer) {
-        // copies still in flight are among the last URING_B issued (a slot is
+        // copies still in flight are among the last LB::RING issued (a slot is
         // refilled only after its previous copy was consumed)
-        for (uint32_t f = ws.issued > (uint32_t)URING_B ? ws.issued - URING_B : 0u; f < ws.issued; ++f)
-            if (!mbar_wait(&full[f % URING_B], (f / URING_B) & 1, WAIT_BUDGET)) {
+        for (uint32_t f = ws.issued > (uint32_t)LB::RING ? ws.issued - LB::RING : 0u; f < ws.issued; ++f)
+            if (!mbar_wait(&full[f % LB::RING], (f / LB::RING) & 1, WAIT_BUDGET)) {
                 set_status(st, MLFF_ERR_TIMEOUT, 35);
                 break;
             }
@@ -657,29 +690,35 @@ __global__ void __launch_bounds__(UNT, 2) update_bwd_tc_kernel(const float* __re
     fence_before_sync();
     __syncthreads();
     fence_after_sync();
-    if (w == 0) tmem_dealloc(tmem, 256);
+    if (w == 0) tmem_dealloc(tmem, LB::TMEM_COLS);
 }
 
-int launch_update_bwd_tc(const float* packed, const LayerOffsets& lo, const WsLayout& L, void* ws, int layer,
-                         const float* xbar_out, float* xtbar, cudaStream_t st) {
-    static bool attr_done = false;
-    if (!attr_done) {
-        cudaError_t e = cudaFuncSetAttribute(update_bwd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             UB_SMEM);
-        if (e != cudaSuccess) return cuda_status(e, "update_bwd_tc smem attribute");
-        attr_done = true;
-    }
+template <int UN>
+static int launch_update_bwd_tc_t(const float* packed, const LayerOffsets& lo, const WsLayout& L, void* ws, int layer,
+                                  const float* xbar_out, float* xtbar, cudaStream_t st) {
+    static std::once_flag once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(once, [] {
+        attr_err = cudaFuncSetAttribute(update_bwd_tc_kernel<UN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        UBwd<UN>::SMEM);
+    });
+    if (attr_err != cudaSuccess) return cuda_status(attr_err, "update_bwd_tc smem attribute");
     ProfScope prof(PK_UPDATE_BWD, st);
     const int64_t NX = (int64_t)L.N * 4 * H;
     const float* Xt = ws_ptr<float>(ws, L.Xt) + layer * NX;
     const float* uz = ws_ptr<float>(ws, L.uz) + (int64_t)layer * L.N * H;
     const float* ua = ws_ptr<float>(ws, L.ua) + (int64_t)layer * L.N * H3;
     const int ntiles = (L.N + UN - 1) / UN;
-    // two CTAs per SM: one's epilogues overlap the other's weight stream and MMAs
     const int grid = std::max(1, std::min(ntiles, 2 * num_sms()));
-    MLFF_LAUNCH_PDL("update_bwd_tc", update_bwd_tc_kernel, grid, UNT, UB_SMEM, st, packed, lo, Xt, uz, ua, xbar_out,
-                    L.N, xtbar, ws_ptr<Status>(ws, L.status));
+    MLFF_LAUNCH_PDL("update_bwd_tc", update_bwd_tc_kernel<UN>, grid, UNT, UBwd<UN>::SMEM, st, packed, lo, Xt, uz, ua,
+                    xbar_out, L.N, xtbar, ws_ptr<Status>(ws, L.status));
     return MLFF_OK;
+}
+
+int launch_update_bwd_tc(const float* packed, const LayerOffsets& lo, const WsLayout& L, void* ws, int layer,
+                         const float* xbar_out, float* xtbar, cudaStream_t st) {
+    return L.UT == 32 ? launch_update_bwd_tc_t<32>(packed, lo, L, ws, layer, xbar_out, xtbar, st)
+                      : launch_update_bwd_tc_t<64>(packed, lo, L, ws, layer, xbar_out, xtbar, st);
 }
 
 }  // namespace mlff

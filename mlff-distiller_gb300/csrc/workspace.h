@@ -12,6 +12,7 @@ constexpr int GRAD_MIX_BLOCKS = 304;  // blocks of the mixing-matrix gradient
 
 struct WsLayout {
     int32_t N, B, L, P;        // atoms, structures, layers, persistent CTAs
+    int32_t UT;                // atoms per tile of the tensor-core update kernels (64 or 32)
     int64_t cap;               // edge capacity
     int64_t ncell_cap;         // cell-code capacity, 8 (N + 27 B) (Morton code spaces of the cell grids)
     size_t status;             // Status

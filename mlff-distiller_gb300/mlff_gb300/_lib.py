@@ -49,7 +49,8 @@ EXPORTS = ["mlff_version", "mlff_last_error_string", "mlff_packed_weights_size",
            "mlff_debug_stall_test", "mlff_painn_message_workspace_size", "mlff_painn_message",
            "mlff_painn_message_backward", "mlff_painn_update_workspace_size", "mlff_painn_update",
            "mlff_painn_update_backward", "mlff_force_stats_workspace_size", "mlff_force_stats",
-           "mlff_autotune", "mlff_autotune_query", "mlff_autotune_set", "mlff_autotune_reset"]
+           "mlff_autotune", "mlff_autotune_query", "mlff_autotune_set", "mlff_autotune_query_shape",
+           "mlff_autotune_set_shape", "mlff_autotune_reset"]
 
 PROFILE_KINDS = ["neighbors", "edge_fwd", "edge_bwd", "update_fwd", "update_bwd", "readout", "forces",
                  "plain_gemm", "plain_edge", "other", "md", "edge_bwd_q"]
@@ -194,6 +195,10 @@ def load(build_if_missing: bool = True):
         lib.mlff_autotune_query.argtypes = [i32, i32, i32, ctypes.POINTER(i32)]
         lib.mlff_autotune_set.restype = ctypes.c_int
         lib.mlff_autotune_set.argtypes = [i32, i32, i32, i32]
+        lib.mlff_autotune_query_shape.restype = ctypes.c_int
+        lib.mlff_autotune_query_shape.argtypes = [i32, i32, i32, ctypes.POINTER(i32), ctypes.POINTER(i32)]
+        lib.mlff_autotune_set_shape.restype = ctypes.c_int
+        lib.mlff_autotune_set_shape.argtypes = [i32, i32, i32, i32, i32]
         lib.mlff_autotune_reset.restype = ctypes.c_int
         lib.mlff_autotune_reset.argtypes = []
         lib.mlff_force_stats_workspace_size.restype = sz

@@ -313,11 +313,11 @@ class Engine:
                              "src": {"mol_ptr": batch.mol_ptr, "box": batch.box, "pbc": batch.pbc}}
 
     def autotune(self, batch: Batch, path: int = _lib.PATH_TUNED_TC, repeats: int = AUTOTUNE_REPEATS) -> dict:
-        """Choose the partition factor of this batch's size bucket
-        (mlff_autotune: a few timed calls per candidate, then cached by the
-        library for every call of the bucket).  Returns the choice and the
-        milliseconds per call of each candidate.  Synchronises the stream;
-        not for use during stream capture."""
+        """Choose the partition factor and the update tile of this batch's
+        size bucket (mlff_autotune: a few timed calls per candidate, then
+        cached by the library for every call of the bucket).  Returns the
+        choices and the milliseconds per call of each partition factor.
+        Synchronises the stream; not for use during stream capture."""
         self.energy_forces(batch, path, graph=False)       # sizes the edge capacity and workspace
         N, B = batch.n_atoms, batch.n_mol
         cap = self.capacity(N, path)
@@ -333,7 +333,9 @@ class Engine:
                                           path, ctypes.byref(out), ws.data_ptr(), ws.numel(), _stream_handle(),
                                           int(repeats), ctypes.byref(chosen), ms))
         _tuned_buckets.add(_bucket(path, N, B))
-        return {"partition_factor": int(chosen.value),
+        f, ut = ctypes.c_int32(), ctypes.c_int32()
+        _lib.check(self.lib.mlff_autotune_query_shape(path, N, B, ctypes.byref(f), ctypes.byref(ut)))
+        return {"partition_factor": int(chosen.value), "update_tile_atoms": int(ut.value),
                 "ms_per_call": {f: round(ms[i], 4) for i, f in enumerate((1, 2, 4))}}
 
     def capture(self, batch: Batch, path: int = _lib.PATH_TUNED_TC, forces: bool = True):

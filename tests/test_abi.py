@@ -200,3 +200,37 @@ def test_autotune_cache_on_host():
     lib.mlff_autotune_set(tc, 9000, 200, 2)
     assert lib.mlff_autotune_reset() == _lib.OK
     assert lib.mlff_autotune_query(tc, 9000, 200, ctypes.byref(f)) == _lib.OK and f.value == 1
+
+
+def test_autotune_shape_cache_on_host():
+    """The update-tile half of the shape cache: untuned buckets use 64-atom
+    tiles, _set_shape pins (factor, tile), _set keeps a bucket's tile, other
+    tile sizes and other paths are rejected, the workspace size does not
+    depend on the shape."""
+    import ctypes
+    from mlff_gb300 import _lib
+    from mlff_gb300.engine import dims_of
+    lib = _lib.load()
+    tc = _lib.PATH_TUNED_TC
+    f, ut = ctypes.c_int32(), ctypes.c_int32()
+    assert lib.mlff_autotune_reset() == _lib.OK
+    d = dims_of(128, 20, 3, 119, 5.0)
+    ws0 = lib.mlff_workspace_size(ctypes.byref(d), 3000, 1, 200_000, tc)
+    assert lib.mlff_autotune_query_shape(tc, 3000, 1, ctypes.byref(f), ctypes.byref(ut)) == _lib.OK
+    assert (f.value, ut.value) == (1, 64)
+    assert lib.mlff_autotune_set_shape(tc, 3000, 1, 2, 32) == _lib.OK
+    assert lib.mlff_autotune_query_shape(tc, 2049, 1, ctypes.byref(f), ctypes.byref(ut)) == _lib.OK   # same bucket
+    assert (f.value, ut.value) == (2, 32)
+    assert lib.mlff_autotune_query(tc, 3000, 1, ctypes.byref(f)) == _lib.OK and f.value == 2
+    assert lib.mlff_autotune_set(tc, 3000, 1, 4) == _lib.OK                                          # tile kept
+    assert lib.mlff_autotune_query_shape(tc, 3000, 1, ctypes.byref(f), ctypes.byref(ut)) == _lib.OK
+    assert (f.value, ut.value) == (4, 32)
+    assert lib.mlff_workspace_size(ctypes.byref(d), 3000, 1, 200_000, tc) == ws0
+    assert lib.mlff_autotune_set_shape(tc, 3000, 1, 1, 48) == _lib.ERR_INVALID
+    assert lib.mlff_autotune_set_shape(tc, 3000, 1, 3, 32) == _lib.ERR_INVALID
+    assert lib.mlff_autotune_set_shape(_lib.PATH_PLAIN_FP32, 3000, 1, 1, 32) == _lib.ERR_INVALID
+    assert lib.mlff_autotune_query_shape(tc, 3000, 1, None, ctypes.byref(ut)) == _lib.ERR_INVALID
+    assert lib.mlff_autotune_set_shape(tc, 3000, 1, 0, 0) == _lib.OK                                  # removed
+    assert lib.mlff_autotune_query_shape(tc, 3000, 1, ctypes.byref(f), ctypes.byref(ut)) == _lib.OK
+    assert (f.value, ut.value) == (1, 64)
+    assert lib.mlff_autotune_reset() == _lib.OK
