@@ -72,6 +72,9 @@ def parse():
     ap.add_argument("--no-compare", action="store_true", help="skip the plain-FP32 / water-box comparison")
     ap.add_argument("--compare-steps", type=int, default=10)
     ap.add_argument("--no-accuracy", action="store_true", help="skip the float64 oracle accuracy check")
+    ap.add_argument("--no-training", action="store_true", help="skip the training-step timing")
+    ap.add_argument("--training-structures", type=int, default=64,
+                    help="structures of a multi-structure workload in the timed training batch")
     ap.add_argument("--accuracy-structures", type=int, default=64,
                     help="structures of a multi-structure workload checked against the float64 oracle")
     return ap.parse_args()
@@ -372,6 +375,46 @@ def run_md(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def training_throughput(sysm, n_structures, steps=5, warmup=2):
+    """One optimisation step of the GPU trainer (ForceFieldTrainer with the
+    reference's loss defaults: energy weight 1, force weight 100): forward
+    and forces on the plain FP32 path, the loss derivatives, the parameter
+    gradients of the energy and force terms from the hand-written reverse
+    pass and its forward-mode derivative, gradient clipping and AdamW.
+    Timed (CUDA events, after warm-up) on the first n_structures structures
+    of the workload, targets = the untrained network's own outputs plus
+    seeded noise (the cost of a step does not depend on the values)."""
+    from mlff_gb300 import _lib
+    from mlff_gb300.engine import make_batch
+    from mlff_gb300.training import ForceFieldTrainer
+    sub = sysm.subset(list(range(min(n_structures, sysm.n_mol)))) if sysm.n_mol > 1 else sysm
+    per = bool(sub.pbc.any())
+    b = make_batch(sub.Z, sub.pos.astype(np.float32), sub.mol_ptr, sub.box if per else None,
+                   sub.pbc if per else None)
+    model = seed_model("fp32").cuda()
+    tr = ForceFieldTrainer(model)
+    E0, F0, _ = model.engine().energy_forces(b, _lib.PATH_PLAIN_FP32, graph=False)
+    g = torch.Generator(device="cuda").manual_seed(7)
+    E_ref = E0.to(torch.float64) + 0.05 * torch.randn(E0.shape, generator=g, device="cuda", dtype=torch.float64)
+    F_ref = F0.to(torch.float64) + 0.1 * torch.randn(F0.shape, generator=g, device="cuda", dtype=torch.float64)
+    for _ in range(warmup):
+        tr.step(b, E_ref, F_ref)
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        tr.step(b, E_ref, F_ref)
+        e1.record()
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    med = statistics.median(ms)
+    return {"structures": sub.n_mol, "atoms": sub.n_atoms, "steps": steps, "ms_per_step": round(med, 3),
+            "atom_steps_per_s": round(sub.n_atoms / (med * 1e-3), 1),
+            "step": "ForceFieldTrainer.step: energy + force loss (weights 1, 100), second-order parameter "
+                    "gradients on the plain FP32 path, grad-norm clip 1.0, AdamW"}
+
+
 def time_replays(step, steps, flush):
     """CUDA-event times (ms) of `steps` calls of step(), an L2-sized buffer
     rewritten before each one."""
@@ -595,6 +638,9 @@ def main():
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(sysm, args.cpu_seconds, os.cpu_count())
+    train = None
+    if not args.no_training and world == 1:
+        train = training_throughput(sysm, args.training_structures)
     dtype = {"fp16x3": "fp16x3 (split-fp16 operands, fp32 accumulate)", "tuned_fp32": "f32", "fp32": "f32"}[args.path]
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
@@ -605,7 +651,7 @@ def main():
                        "between timed steps", "per_rank": "independent copy of the workload",
                        "launch": "CUDA graph of one step" if args.graph else "eager library call per step",
                        "hbm_peak_bytes": hbm_peak, "autotune": tune},
-            "vs_plain_fp32": compare, "accuracy": acc,
+            "vs_plain_fp32": compare, "accuracy": acc, "training": train,
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches,
             "kernel_ms": {k: round(v, 3) for k, v in prof.ms.items() if v > 0},
             "kernel_launches": {k: v for k, v in prof.launches.items() if v > 0},

@@ -731,13 +731,22 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                     tmem_ld8(lane_base + TB + 64 + col, f1);            // phi_v1
                     tmem_ld8(lane_base + TB + 128 + col, f2);           // phi_v2
                     const uint32_t m = (chg[col >> 5] >> (col & 31)) & 0xFFu;
+                    // the block's u components, two 16-byte shared loads per array
+                    // (u arrays and col are 32-byte aligned)
+                    float ua[8], ub[8];
+                    *reinterpret_cast<float4*>(ub) = *reinterpret_cast<const float4*>(u1 + col);
+                    *reinterpret_cast<float4*>(ub + 4) = *reinterpret_cast<const float4*>(u1 + col + 4);
+                    if (HH != 0) {
+                        *reinterpret_cast<float4*>(ua) = *reinterpret_cast<const float4*>(u0 + col);
+                        *reinterpret_cast<float4*>(ua + 4) = *reinterpret_cast<const float4*>(u0 + col + 4);
+                    }
                     tmem_ld_wait();
                     // message terms of edge i, the same expressions on both branches
                     // (a block's branch depends on where the tile starts)
                     auto m0 = [&](int i) {
-                        return HH == 0 ? x0[i] * fa[i] : fmaf(x0[i], f1[i], u0[col + i] * f2[i]);
+                        return HH == 0 ? x0[i] * fa[i] : fmaf(x0[i], f1[i], ua[i] * f2[i]);
                     };
-                    auto m1 = [&](int i) { return fmaf(x1[i], f1[i], u1[col + i] * f2[i]); };
+                    auto m1 = [&](int i) { return fmaf(x1[i], f1[i], ub[i] * f2[i]); };
                     if (m == 0) {
 #pragma unroll
                         for (int i = 0; i < 8; ++i) {
