@@ -1210,6 +1210,7 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
         if (a.write_nodes) zero_empty_rows(a.xbar, a.row_ptr, j0, j1, wl, lane, PT / 32);
         int cur = j0;
         float acc0 = 0.f, acc1 = 0.f;   // node adjoints of the current receiver, two components
+        float cr0 = 0.f, cr1 = 0.f;     // its dE/dXt rows (the same two components)
         if (ntl > 0) {   // the partition's first tile: edge arrays and [E; E'] tile
             fetch(sbase, e0, min(PN, e1 - e0));
             if (tp == 32) {
@@ -1219,7 +1220,9 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
             }
             cp_async_wait_all();
             pipe_sync(pp);
-            if (tp < PN) prep(sbase, min(PN, e1 - e0), j0);
+            // prev = -1 marks edge 0 as a receiver start, so that the first
+            // block loads its receiver's rows
+            if (tp < PN) prep(sbase, min(PN, e1 - e0), -1);
             pipe_sync(pp);
         }
         for (int k = 0; k < ntl; ++k) {
@@ -1316,11 +1319,12 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
             fence_before_sync();
             pipe_sync(pp);
             // epilogue 2's first two 4-edge blocks of gathers are issued while
-            // GEMM2 runs: the senders' dE/dXt and X rows and the dE/dXt row of
-            // the block's first receiver (edges where another receiver starts
-            // inside the block reload theirs in epilogue 2)
-            float tba0[4], tba1[4], xba0[4], xba1[4], ra0, ra1;
-            float tbb0[4], tbb1[4], xbb0[4], xbb1[4], rb0, rb1;
+            // GEMM2 runs: the senders' dE/dXt and X rows and, when a receiver
+            // starts at the block's first edge, that receiver's dE/dXt rows
+            // (receivers that start inside a block load theirs in epilogue 2;
+            // otherwise the rows carry over from the previous block)
+            float tba0[4], tba1[4], xba0[4], xba1[4], ra0 = 0.f, ra1 = 0.f;
+            float tbb0[4], tbb1[4], xbb0[4], xbb1[4], rb0 = 0.f, rb1 = 0.f;
             auto gather4 = [&](float (&tb0)[4], float (&tb1)[4], float (&xb0)[4], float (&xb1)[4], float& r0,
                                float& r1, int col) {
                 const int4 so = *reinterpret_cast<const int4*>(soff + col);
@@ -1332,9 +1336,11 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                     xb0[i] = __ldg(xx + sv[i]);
                     xb1[i] = __ldg(xx + sv[i] + H);
                 }
-                const int ro = roff[col];
-                r0 = __ldg(xtb + ro);
-                r1 = __ldg(xtb + ro + H);
+                if ((chw >> col) & 1u) {
+                    const int ro = roff[col];
+                    r0 = __ldg(xtb + ro);
+                    r1 = __ldg(xtb + ro + H);
+                }
             };
             gather4(tba0, tba1, xba0, xba1, ra0, ra1, 0);
             if (4 < n) gather4(tbb0, tbb1, xbb0, xbb1, rb0, rb1, 4);
@@ -1433,7 +1439,7 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
             {   // epilogue 2 over 4-edge blocks, the next block's gathers in flight
                 // (compiled once per warp half: hc is std::integral_constant<int, hh>)
                 auto process4 = [&](auto hc, const float (&tb0)[4], const float (&tb1)[4], const float (&xb0)[4],
-                                    const float (&xb1)[4], float r0, float r1, int col) {
+                                    const float (&xb1)[4], float rn0, float rn1, int col) {
                     constexpr int HH = decltype(hc)::value;
                     float fa[4], da[4], f1[4], d1[4];
                     if (HH == 0) {
@@ -1453,6 +1459,7 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                     // the same expressions on both branches below (a block's branch
                     // depends on where the tile starts)
                     float pv[4];
+                    float r0 = cr0, r1 = cr1;   // the current receiver's dE/dXt rows
                     auto edge_term = [&](int i, float t0, float t1) {
                         if (HH == 0) pv[i] = fmaf(t0 * xb0[i], da[i], t1 * xb1[i] * d1[i]);
                         else pv[i] = fmaf(t0, xb0[i], t1 * xb1[i]) * d1[i];
@@ -1475,10 +1482,13 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                                 cur = rcv_s[col + i];
                                 acc0 = 0.f;
                                 acc1 = 0.f;
-                                if (i > 0) {   // edge 0's receiver rows came with the gathers
+                                if (i > 0) {
                                     const int ro = roff[col + i];
                                     r0 = __ldg(xtb + ro);
                                     r1 = __ldg(xtb + ro + H);
+                                } else {   // edge 0's receiver rows came with the gathers
+                                    r0 = rn0;
+                                    r1 = rn1;
                                 }
                             }
                             acc0 = fmaf(tb0[i], fa[i], acc0);
@@ -1486,6 +1496,8 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                             edge_term(i, r0, r1);
                         }
                     }
+                    cr0 = r0;
+                    cr1 = r1;
                     const float s4 = warp_reduce_scatter4(pv, lane);
                     if ((lane & 7) == 0) red[wl * PN + col + rs4_idx] = s4;
                 };
