@@ -55,6 +55,14 @@ __device__ __forceinline__ float dsilu_f(float x) {
     return s * (1.0f + x * (1.0f - s));
 }
 
+// Pair layout of the tensor-core path's node features and adjoints (the
+// layer inputs X[0..L-1] and dE/dXt): per atom, (s, v_x) of channel c at
+// floats 2c, 2c + 1 and (v_y, v_z) at 2H + 2c, 2H + 2c + 1, so that a thread
+// that owns two components of one channel loads both with one 8-byte
+// access.  (The other per-atom arrays keep the component-major layout
+// comp * H + c.)
+__host__ __device__ constexpr int pair_off(int comp, int c) { return (comp >> 1) * 2 * H + 2 * c + (comp & 1); }
+
 // Velocity-Verlet half kick v + dt/2 F/m in float64 (F is the float32
 // force) and the kinetic energy 1/2 m v^2 of one atom; the integrator
 // kernels and the force kernel's fused update share these expressions.

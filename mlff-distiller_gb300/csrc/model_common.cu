@@ -143,32 +143,34 @@ int pack_fp32(const mlff_dims& d, const mlff_params& p, float* out, const Packed
 
 // ------------------------------------------------------------- embedding
 __global__ void embed_kernel(const float* __restrict__ emb, const int64_t* __restrict__ Z, int32_t n_atoms,
-                             int32_t n_species, float* __restrict__ X, Status* st) {
+                             int32_t n_species, float* __restrict__ X, int pairs, Status* st) {
     pdl_wait();
     pdl_trigger();
-    // X[a] = (emb[Z[a]], 0, 0, 0)
+    // X[a] = (emb[Z[a]], 0, 0, 0), component-major or in the pair layout
     const int64_t total = (int64_t)n_atoms * 4 * H;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
         int64_t a = i / (4 * H);
         int q = (int)(i % (4 * H));
+        const int comp = pairs ? 2 * (q / (2 * H)) + (q & 1) : q / H;
+        const int ch = pairs ? (q % (2 * H)) / 2 : q % H;
         float v = 0.0f;
-        if (q < H) {
+        if (comp == 0) {
             int64_t z = Z[a];
             if (z < 0 || z >= n_species) {
                 set_status(st, MLFF_ERR_INVALID, (int)a);
                 z = 0;
             }
-            v = emb[z * H + q];
+            v = emb[z * H + ch];
         }
         X[i] = v;
     }
 }
 
 int launch_embed(const mlff_dims& d, const float* packed, const PackedOffsets& po, const mlff_system& sys,
-                 const WsLayout& L, void* ws, cudaStream_t st) {
+                 const WsLayout& L, void* ws, cudaStream_t st, bool pairs) {
     ProfScope prof(PK_OTHER, st);
     MLFF_LAUNCH_PDL("embed", embed_kernel, 152 * 8, 256, 0, st, packed + po.emb, sys.Z, sys.n_atoms, d.n_species,
-                                          ws_ptr<float>(ws, L.X), ws_ptr<Status>(ws, L.status));
+                    ws_ptr<float>(ws, L.X), pairs ? 1 : 0, ws_ptr<Status>(ws, L.status));
     return MLFF_OK;
 }
 

@@ -324,8 +324,8 @@ __device__ __forceinline__ void tile_prep(int e, int n, int prev, const int* src
                                           const float4* us, int* soff, int* roff, float* uc, uint32_t* chg) {
     const bool valid = e < n;
     const int ra = rcv_s[e];
-    soff[e] = src_s[e] * 4 * H;
-    if (roff) roff[e] = max(ra, 0) * 4 * H;
+    soff[e] = src_s[e] * 2 * H;   // row offsets in float2 units of the pair layout
+    if (roff) roff[e] = max(ra, 0) * 2 * H;
     if (uc) {
         const float4 u = us[e];
         uc[e] = u.x;
@@ -404,11 +404,15 @@ __device__ __forceinline__ void zero_empty_rows(float* out, const int32_t* row_p
         if (row_ptr[j] == row_ptr[j + 1])
             for (int k = lane; k < 4 * H; k += 32) out[(int64_t)j * 4 * H + k] = 0.0f;
 }
+// (out in the component-major layout, base in the pair layout)
 __device__ __forceinline__ void copy_empty_rows(float* out, const float* base, const int32_t* row_ptr, int j0, int j1,
                                                 int w, int lane, int nwarps = NT / 32) {
     for (int j = j0 + w; j < j1; j += nwarps)
         if (row_ptr[j] == row_ptr[j + 1])
-            for (int k = lane; k < 4 * H; k += 32) out[(int64_t)j * 4 * H + k] = base[(int64_t)j * 4 * H + k];
+            for (int k = lane; k < 4 * H; k += 32) {
+                const int comp = k / H, ch = k % H;
+                out[(int64_t)j * 4 * H + k] = base[(int64_t)j * 4 * H + pair_off(comp, ch)];
+            }
 }
 
 // ------------------------------------------------ pipelines (both kernels)
@@ -543,10 +547,10 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
     uint64_t* e_bar = bars + 3 + 3 * pp;
     uint64_t* g2_bar = bars + 4 + 3 * pp;
     unsigned char* sbase = smem + Q_OFF_SB + 2 * pp * Q_SB_BYTES;
-    // components 2 hh and 2 hh + 1; the second sits H floats after the first
-    const int fidx0 = 2 * hh * H + c;
-    const float* xx = a.X + fidx0;
-    float* out = a.Xt + fidx0;
+    // components 2 hh and 2 hh + 1: one float2 of the pair layout of X,
+    // H floats apart in the component-major Xt
+    const float2* xx = reinterpret_cast<const float2*>(a.X + pair_off(2 * hh, c));
+    float* out = a.Xt + 2 * hh * H + c;
 
     uint32_t mma_phase = 0, g2_phase = 0;   // GEMM1 / GEMM2 barrier phases
     uint32_t e_phase = 0, e_issued = 0;     // E-tile copies: barrier phase, copies issued (thread tp 64)
@@ -588,7 +592,7 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
         int cur = j0;
         float acc0 = 0.f, acc1 = 0.f;   // message sums of the current receiver, two components
         // X of the current receiver (the residual term of Xt)
-        float base0 = xx[(int64_t)cur * 4 * H], base1 = xx[(int64_t)cur * 4 * H + H];
+        float2 base = xx[(int64_t)cur * 2 * H];
         if (ntl > 0) {   // the partition's first tile: edge arrays and E tile
             fetch(sbase, e0, min(QN, e1 - e0));
             if (tp == QN) {
@@ -684,8 +688,9 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                     const int sv[4] = {so.x, so.y, so.z, so.w};
 #pragma unroll
                     for (int j = 0; j < 4; ++j) {
-                        x0[i + j] = __ldg(xx + sv[j]);
-                        x1[i + j] = __ldg(xx + sv[j] + H);
+                        const float2 v = __ldg(xx + sv[j]);
+                        x0[i + j] = v.x;
+                        x1[i + j] = v.y;
                     }
                 }
             };
@@ -757,11 +762,10 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
 #pragma unroll
                         for (int i = 0; i < 8; ++i) {
                             if (m & (1u << i)) {
-                                out[(int64_t)cur * 4 * H] = base0 + acc0;
-                                out[(int64_t)cur * 4 * H + H] = base1 + acc1;
+                                out[(int64_t)cur * 4 * H] = base.x + acc0;
+                                out[(int64_t)cur * 4 * H + H] = base.y + acc1;
                                 cur = rcv_s[col + i];
-                                base0 = xx[(int64_t)cur * 4 * H];
-                                base1 = xx[(int64_t)cur * 4 * H + H];
+                                base = xx[(int64_t)cur * 2 * H];
                                 acc0 = 0.f;
                                 acc1 = 0.f;
                             }
@@ -795,8 +799,8 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
             }
         }
         if (!aborted) {
-            out[(int64_t)cur * 4 * H] = base0 + acc0;
-            out[(int64_t)cur * 4 * H + H] = base1 + acc1;
+            out[(int64_t)cur * 4 * H] = base.x + acc0;
+            out[(int64_t)cur * 4 * H + H] = base.y + acc1;
         }
     }
     // drain: every MMA and copy this CTA issued must be complete before it
@@ -996,12 +1000,19 @@ __global__ void __launch_bounds__(VQ_NT, 2) vq_tc_kernel(const float* __restrict
         // B tile: warp w builds rows w, w + 8, ..., w + 88 (all loads issued
         // first); lane takes channels 4 lane .. 4 lane + 3; beta by warp sums
         {
+            // (dE/dXt in the pair layout: component k of channels 4 lane .. +3
+            // is every other float of two 16-byte words)
             float4 x[12];
 #pragma unroll
             for (int u = 0; u < 12; ++u) {
-                const int row = w + 8 * u, atom = a0 + row / 3;
-                x[u] = atom < n_atoms ? reinterpret_cast<const float4*>(xtbar + ((int64_t)atom * 4 + 1 + row % 3) * H)[lane]
-                                      : make_float4(0.f, 0.f, 0.f, 0.f);
+                const int row = w + 8 * u, atom = a0 + row / 3, comp = 1 + row % 3;
+                if (atom < n_atoms) {
+                    const float4* pr = reinterpret_cast<const float4*>(xtbar + (int64_t)atom * 4 * H + (comp >> 1) * 2 * H);
+                    const float4 p0 = pr[2 * lane], p1 = pr[2 * lane + 1];
+                    x[u] = (comp & 1) ? make_float4(p0.y, p0.w, p1.y, p1.w) : make_float4(p0.x, p0.z, p1.x, p1.z);
+                } else {
+                    x[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+                }
             }
 #pragma unroll
             for (int u = 0; u < 12; ++u) {
@@ -1163,11 +1174,11 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
     float* red = reinterpret_cast<float*>(smem + R_OFF_RED) + pp * R_RED_FLOATS;
     unsigned char* sbase = smem + R_OFF_SB + 2 * pp * R_SB_BYTES;
     const int rs4_idx = ((lane >> 4) & 1) * 2 + ((lane >> 3) & 1);
-    // components 2 hh and 2 hh + 1; the second sits H floats after the first
-    const int fidx0 = 2 * hh * H + c;
-    const float* xtb = a.xtbar + fidx0;
-    const float* xx = a.X + fidx0;
-    float* out = a.xbar + fidx0;
+    // components 2 hh and 2 hh + 1: one float2 of the pair layout of dE/dXt
+    // and X, H floats apart in the component-major dE/dX
+    const float2* xtb = reinterpret_cast<const float2*>(a.xtbar + pair_off(2 * hh, c));
+    const float2* xx = reinterpret_cast<const float2*>(a.X + pair_off(2 * hh, c));
+    float* out = a.xbar + 2 * hh * H + c;
 
     uint32_t mma_phase = 0, g2_phase = 0, g3_phase = 0;   // GEMM1 / GEMM2 / GEMM3 barrier phases
     uint32_t e_phase = 0, e_issued = 0;     // E-tile copies: barrier phase, copies issued (thread tp 32)
@@ -1331,15 +1342,16 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                 const int sv[4] = {so.x, so.y, so.z, so.w};
 #pragma unroll
                 for (int i = 0; i < 4; ++i) {
-                    tb0[i] = __ldg(xtb + sv[i]);
-                    tb1[i] = __ldg(xtb + sv[i] + H);
-                    xb0[i] = __ldg(xx + sv[i]);
-                    xb1[i] = __ldg(xx + sv[i] + H);
+                    const float2 t = __ldg(xtb + sv[i]), x = __ldg(xx + sv[i]);
+                    tb0[i] = t.x;
+                    tb1[i] = t.y;
+                    xb0[i] = x.x;
+                    xb1[i] = x.y;
                 }
                 if ((chw >> col) & 1u) {
-                    const int ro = roff[col];
-                    r0 = __ldg(xtb + ro);
-                    r1 = __ldg(xtb + ro + H);
+                    const float2 r = __ldg(xtb + roff[col]);
+                    r0 = r.x;
+                    r1 = r.y;
                 }
             };
             gather4(tba0, tba1, xba0, xba1, ra0, ra1, 0);
@@ -1483,9 +1495,9 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                                 acc0 = 0.f;
                                 acc1 = 0.f;
                                 if (i > 0) {
-                                    const int ro = roff[col + i];
-                                    r0 = __ldg(xtb + ro);
-                                    r1 = __ldg(xtb + ro + H);
+                                    const float2 r = __ldg(xtb + roff[col + i]);
+                                    r0 = r.x;
+                                    r1 = r.y;
                                 } else {   // edge 0's receiver rows came with the gathers
                                     r0 = rn0;
                                     r1 = rn1;

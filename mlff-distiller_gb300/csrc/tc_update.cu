@@ -154,6 +154,25 @@ __device__ __forceinline__ void store_row4(unsigned char* tile, uint32_t half_by
     *reinterpret_cast<uint2*>(tile + half_bytes + o) = lv;
 }
 
+// One atom's row of a [N][4][H] array (lane: channels 4 lane .. 4 lane + 3
+// of each component) in the component-major layout or, with pairs, in the
+// pair layout of the edge kernels' gathers (pair_off).
+__device__ __forceinline__ void store_atom_row(float* row, int lane, float4 s, float4 x, float4 y, float4 z,
+                                               bool pairs) {
+    float4* o = reinterpret_cast<float4*>(row);
+    if (pairs) {
+        o[2 * lane] = make_float4(s.x, x.x, s.y, x.y);
+        o[2 * lane + 1] = make_float4(s.z, x.z, s.w, x.w);
+        o[64 + 2 * lane] = make_float4(y.x, z.x, y.y, z.y);
+        o[64 + 2 * lane + 1] = make_float4(y.z, z.z, y.w, z.w);
+    } else {
+        o[lane] = s;
+        o[32 + lane] = x;
+        o[64 + lane] = y;
+        o[96 + lane] = z;
+    }
+}
+
 // Synchronisation helpers shared by both kernels: one thread issues the
 // MMAs of a GEMM while the producer keeps the ring full; then the CTA waits
 // for the MMAs (warp 0 polls, the others wait at the barrier).
@@ -205,8 +224,9 @@ struct UFwd {
 template <int UN>
 __global__ void __launch_bounds__(UNT, 2) update_fwd_tc_kernel(const float* __restrict__ P, LayerOffsets lo,
                                                                const float* __restrict__ Xt, int32_t n_atoms,
-                                                               float* __restrict__ Xout, float* __restrict__ uz,
-                                                               float* __restrict__ ua, Status* st) {
+                                                               float* __restrict__ Xout, int out_pairs,
+                                                               float* __restrict__ uz, float* __restrict__ ua,
+                                                               Status* st) {
     using LF = UFwd<UN>;
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* Bs = smem + LF::OFF_B;
@@ -391,11 +411,9 @@ __global__ void __launch_bounds__(UNT, 2) update_fwd_tc_kernel(const float* __re
                         oz.y = vnew(vx.y, vy.y, vz.y, vz.y, g1.y, g2.y, 2);
                         oz.z = vnew(vx.z, vy.z, vz.z, vz.z, g1.z, g2.z, 2);
                         oz.w = vnew(vx.w, vy.w, vz.w, vz.w, g1.w, g2.w, 2);
-                        float4* xo = reinterpret_cast<float4*>(Xout + (int64_t)a * 4 * H);
-                        xo[lane] = make_float4(sv.x + ds.x, sv.y + ds.y, sv.z + ds.z, sv.w + ds.w);
-                        xo[32 + lane] = ox;
-                        xo[64 + lane] = oy;
-                        xo[96 + lane] = oz;
+                        store_atom_row(Xout + (int64_t)a * 4 * H, lane,
+                                       make_float4(sv.x + ds.x, sv.y + ds.y, sv.z + ds.z, sv.w + ds.w), ox, oy, oz,
+                                       out_pairs != 0);
                     }
                 }
                 __syncthreads();
@@ -442,8 +460,11 @@ static int launch_update_fwd_tc_t(const float* packed, const LayerOffsets& lo, c
     float* ua = ws_ptr<float>(ws, L.ua) + (int64_t)layer * L.N * H3;
     const int ntiles = (L.N + UN - 1) / UN;
     const int grid = std::max(1, std::min(ntiles, 2 * num_sms()));
+    // the next layer's input in the pair layout of the edge kernels' gathers;
+    // the last layer's output (read by the readout) component-major
+    const int out_pairs = layer + 1 < L.L ? 1 : 0;
     MLFF_LAUNCH_PDL("update_fwd_tc", update_fwd_tc_kernel<UN>, grid, UNT, UFwd<UN>::SMEM, st, packed, lo, Xt, L.N,
-                    Xout, uz, ua, ws_ptr<Status>(ws, L.status));
+                    Xout, out_pairs, uz, ua, ws_ptr<Status>(ws, L.status));
     return MLFF_OK;
 }
 
@@ -652,8 +673,6 @@ __global__ void __launch_bounds__(UNT, 2) update_bwd_tc_kernel(const float* __re
                     const float4 cn = reinterpret_cast<const float4*>(T + (UN + i) * H)[lane];
                     const float4 sb = r[k][0], bx = r[k][1], by = r[k][2], bz = r[k][3];
                     const float4 vx = r[k][4], vy = r[k][5], vz = r[k][6], g1 = r[k][7], g2 = r[k][8];
-                    float4* o = reinterpret_cast<float4*>(xtbar + (int64_t)a * 4 * H);
-                    o[lane] = make_float4(sb.x + cs.x, sb.y + cs.y, sb.z + cs.z, sb.w + cs.w);
                     float4 ox, oy, oz;
                     auto one = [&](float b_x, float b_y, float b_z, float v_x, float v_y, float v_z, float a1, float a2,
                                    float n_c, float& px, float& py, float& pz) {
@@ -667,9 +686,9 @@ __global__ void __launch_bounds__(UNT, 2) update_bwd_tc_kernel(const float* __re
                     one(bx.y, by.y, bz.y, vx.y, vy.y, vz.y, g1.y, g2.y, cn.y, ox.y, oy.y, oz.y);
                     one(bx.z, by.z, bz.z, vx.z, vy.z, vz.z, g1.z, g2.z, cn.z, ox.z, oy.z, oz.z);
                     one(bx.w, by.w, bz.w, vx.w, vy.w, vz.w, g1.w, g2.w, cn.w, ox.w, oy.w, oz.w);
-                    o[32 + lane] = ox;
-                    o[64 + lane] = oy;
-                    o[96 + lane] = oz;
+                    // dE/dXt in the pair layout the reverse edge kernel gathers from
+                    store_atom_row(xtbar + (int64_t)a * 4 * H, lane,
+                                   make_float4(sb.x + cs.x, sb.y + cs.y, sb.z + cs.z, sb.w + cs.w), ox, oy, oz, true);
                 }
             }
         }

@@ -99,8 +99,9 @@ struct NbrBuffers {
 int launch_neighbors_into(const mlff_dims& d, const mlff_system& sys, const NbrBuffers& b, cudaStream_t st);
 int launch_neighbors(const mlff_dims& d, const mlff_system& sys, const WsLayout& L, void* ws,
                      cudaStream_t st);
+// X[0] component-major or (pairs: the tensor-core path) in the pair layout
 int launch_embed(const mlff_dims& d, const float* packed, const PackedOffsets& po,
-                 const mlff_system& sys, const WsLayout& L, void* ws, cudaStream_t st);
+                 const mlff_system& sys, const WsLayout& L, void* ws, cudaStream_t st, bool pairs = false);
 int launch_readout(const mlff_dims& d, const float* packed, const PackedOffsets& po,
                    const mlff_system& sys, const WsLayout& L, void* ws, const mlff_outputs& out,
                    int want_grad, cudaStream_t st);
