@@ -1280,32 +1280,48 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
             pipe_sync(pp);
             fence_after_sync();
             {   // epilogue 1: h = silu(z + b1) (rows 0-31), h' = silu'(z + b1) z'
-                // (rows 32-63); warp (q, hh) takes hidden unit c of edges 16 hh..16 hh + 15
+                // (rows 32-63); warp (q, hh) takes hidden units 32 q .. 32 q + 31 of
+                // edges 16 hh .. 16 hh + 15 in the 16x256b fragment -- thread t holds
+                // hidden units 16 g + t/4 and 16 g + 8 + t/4 of lane group g, edges
+                // 2 (t % 4), + 1 and the same + 8 --, which is the m8n8 fragment of
+                // 8 x 8 (hidden x edge) blocks: stmatrix .trans writes each block's
+                // edge rows as the 16-byte chunks of the K-major tile
                 const int col = 16 * hh, nv = n - col;   // valid edges among this warp's 16
-                const float bias = b1s[c];
-                float z[16], zd[16];
-                tmem_ld16(lane_base + TB + 128 + col, z);
-                tmem_ld16(lane_base + TB + 128 + PN + col, zd);
-                tmem_ld_wait();
-                const BColumn hc(Hs, P_HH, 2 * PN, col, c), hdc(Hs, P_HH, 2 * PN, PN + col, c);
-                if (n == PN) {   // a full tile (all but the last of a partition)
+                const int r4 = lane >> 2, c2 = 2 * (lane & 3);
+                // this thread's stmatrix row: row R = lane % 8 of block m = lane / 8
+                // (edge half s = m / 2, hidden half w = m % 2)
+                const int mb = lane >> 3, R = lane & 7;
+                const uint32_t rowaddr = smem_u32(Hs) + (uint32_t)((q >> 1) * b_block(2 * PN) +
+                                                                   ((col >> 3) + (mb >> 1)) * 1024 + R * 128);
 #pragma unroll
-                    for (int i = 0; i < 16; i += 2) {
-                        const float z0 = z[i] + bias, z1 = z[i + 1] + bias;
-                        const float s0 = fast_sigmoid(z0), s1 = fast_sigmoid(z1);
-                        hc.put_pair(i, z0 * s0, z1 * s1);
-                        hdc.put_pair(i, s0 * (1.0f + z0 * (1.0f - s0)) * zd[i], s1 * (1.0f + z1 * (1.0f - s1)) * zd[i + 1]);
-                    }
-                } else {
+                for (int g = 0; g < 2; ++g) {
+                    float z[8], zd[8];
+                    tmem_ld16x256_x2(lane_base + ((uint32_t)(16 * g) << 16) + TB + 128 + col, z);
+                    tmem_ld16x256_x2(lane_base + ((uint32_t)(16 * g) << 16) + TB + 128 + PN + col, zd);
+                    const float bA = b1s[32 * q + 16 * g + r4], bB = b1s[32 * q + 16 * g + 8 + r4];
+                    tmem_ld_wait();
+                    float hv[8], hd[8];
 #pragma unroll
-                    for (int i = 0; i < 16; i += 2) {
-                        const float z0 = z[i] + bias, z1 = z[i + 1] + bias;
-                        const float s0 = fast_sigmoid(z0), s1 = fast_sigmoid(z1);
-                        const bool v0 = i < nv, v1 = i + 1 < nv;
-                        hc.put_pair(i, v0 ? z0 * s0 : 0.f, v1 ? z1 * s1 : 0.f);
-                        hdc.put_pair(i, v0 ? s0 * (1.0f + z0 * (1.0f - s0)) * zd[i] : 0.f,
-                                     v1 ? s1 * (1.0f + z1 * (1.0f - s1)) * zd[i + 1] : 0.f);
+                    for (int i = 0; i < 8; ++i) {   // value i: edge 8 (i / 4) + c2 + i % 2, hidden block (i / 2) % 2
+                        const float zz = z[i] + (((i >> 1) & 1) ? bB : bA);
+                        const float sg = fast_sigmoid(zz);
+                        const bool valid = 8 * (i >> 2) + c2 + (i & 1) < nv;
+                        hv[i] = valid ? zz * sg : 0.f;
+                        hd[i] = valid ? sg * (1.0f + zz * (1.0f - sg)) * zd[i] : 0.f;
                     }
+                    // block m (registers 4 (m / 2) + 2 (m % 2), + 1) -> 16-byte rows
+                    uint32_t fh[4], fl[4], dh[4], dl[4];
+#pragma unroll
+                    for (int m = 0; m < 4; ++m) {
+                        const int i0 = 4 * (m >> 1) + 2 * (m & 1);
+                        split_pack(hv[i0], hv[i0 + 1], fh[m], fl[m]);
+                        split_pack(hd[i0], hd[i0 + 1], dh[m], dl[m]);
+                    }
+                    const uint32_t a = rowaddr + ((((4 * (q & 1) + 2 * g + (mb & 1)) ^ R)) << 4);
+                    stmatrix_x4_trans(a, fh[0], fh[1], fh[2], fh[3]);                       // h hi
+                    stmatrix_x4_trans(a + P_HH, fl[0], fl[1], fl[2], fl[3]);                // h lo
+                    stmatrix_x4_trans(a + 4 * 1024, dh[0], dh[1], dh[2], dh[3]);            // h' hi (rows + 32)
+                    stmatrix_x4_trans(a + 4 * 1024 + P_HH, dl[0], dl[1], dl[2], dl[3]);     // h' lo
                 }
                 // f = W2 h accumulates onto b2 (0 for padding edges), f' = W2 h'
                 // onto 0: this warp refills chunk hh (f: 32 columns, f': 32

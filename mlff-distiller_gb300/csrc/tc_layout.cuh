@@ -53,6 +53,23 @@ __device__ __forceinline__ void split2(float a, float b, __half2& hi, __half2& l
     lo = __floats2half2_rn(a - f.x, b - f.y);
 }
 
+// hi and lo fp16 halves of the pair (a, b), each packed in one 32-bit word
+// (a in the low half)
+__device__ __forceinline__ void split_pack(float a, float b, uint32_t& hi, uint32_t& lo) {
+    __half2 h, l;
+    split2(a, b, h, l);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    lo = *reinterpret_cast<const uint32_t*>(&l);
+}
+
+// Shared-memory address of the 16-byte chunk of a K-major 128-byte-swizzle
+// B tile of n_rows rows that holds row `row`, K values k0 .. k0 + 7 (k0 a
+// multiple of 8): the destination of one stmatrix row.
+__device__ __forceinline__ uint32_t b_chunk(uint32_t tile, int n_rows, int row, int k0) {
+    return tile + (uint32_t)((k0 >> 6) * b_block(n_rows) + (row >> 3) * 1024 + (row & 7) * 128 +
+                             ((((k0 >> 3) & 7) ^ (row & 7)) << 4));
+}
+
 // store 16 consecutive K values (one K-step, both 8-column chunks) of one
 // row as split fp16 into a B-operand tile (hi half, lo half)
 __device__ __forceinline__ void store_row16(unsigned char* tile, uint32_t half_bytes, int n_rows, int row, int s,

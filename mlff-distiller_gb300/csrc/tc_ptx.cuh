@@ -177,6 +177,30 @@ __device__ __forceinline__ void tmem_ld4(uint32_t taddr, float (&v)[4]) {
 #pragma unroll
     for (int i = 0; i < 4; ++i) v[i] = __uint_as_float(r[i]);
 }
+// TMEM -> registers in the 16-lane x 256-bit shape (the m16n8 accumulator
+// fragment): thread t of the warp gets lanes base + t/4 and base + 8 + t/4,
+// columns 2 (t % 4) and 2 (t % 4) + 1 of every 8-column group:
+// v[4 j + 0..1] = (lane base + t/4, columns 8 j + 2 (t % 4) + 0..1),
+// v[4 j + 2..3] = (lane base + 8 + t/4, the same columns); .x2 covers 16
+// columns (j = 0, 1).
+__device__ __forceinline__ void tmem_ld16x256_x2(uint32_t taddr, float (&v)[8]) {
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.16x256b.x2.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+// Four 8 x 8 matrices of 16-bit elements from the m8n8 fragment (thread t
+// holds row t/4, elements 2 (t % 4) and 2 (t % 4) + 1 of matrix i in r_i,
+// low half first), stored transposed: column R of matrix i becomes 16
+// contiguous bytes at the address thread 8 i + R gives (16-byte aligned).
+__device__ __forceinline__ void stmatrix_x4_trans(uint32_t saddr, uint32_t r0, uint32_t r1, uint32_t r2, uint32_t r3) {
+    asm volatile("stmatrix.sync.aligned.m8n8.x4.trans.shared.b16 [%0], {%1,%2,%3,%4};" ::"r"(saddr), "r"(r0), "r"(r1),
+                 "r"(r2), "r"(r3)
+                 : "memory");
+}
+
 // registers -> TMEM, the same lane / column mapping as the loads
 __device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16]) {
     asm volatile(
