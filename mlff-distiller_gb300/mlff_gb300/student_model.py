@@ -117,6 +117,7 @@ class _MessageFn(torch.autograd.Function):
         return so.to(s.dtype), vo.to(v.dtype)
 
     @staticmethod
+    @torch.autograd.function.once_differentiable
     def backward(ctx, gso, gvo):
         lib = _lib.load()
         sf, vf, ei, rf, ef, w1f, b1f, w2f, b2f = ctx.saved_tensors
@@ -166,6 +167,7 @@ class _UpdateFn(torch.autograd.Function):
         return so.to(s.dtype), vo.to(v.dtype)
 
     @staticmethod
+    @torch.autograd.function.once_differentiable
     def backward(ctx, gso, gvo):
         lib = _lib.load()
         sf, vf, w1f, b1f, w2f, b2f, mf = ctx.saved_tensors
@@ -326,8 +328,22 @@ class _ForceTerm(torch.autograd.Function):
                                                     for (n, _), p in zip(_trainable(ctx.model), params))
 
 
+# Width of the fused whole-model CUDA paths (every reference configuration
+# and checkpoint); other widths run the module-level path.
+FUSED_HIDDEN = 128
+
+
 class StudentForceField(nn.Module):
-    """PaiNN-style energy model (student_model.py:532-1176) on GB300."""
+    """PaiNN-style energy model (student_model.py:532-1176) on GB300.
+
+    hidden_dim = 128 runs the fused CUDA paths (``precision``).  Other widths
+    (the reference's unit tests build width-64 models) run the module-level
+    path: the reference's forward (student_model.py:675-757) with the radius
+    graph and every message and update block on the library's CUDA kernels
+    (``PaiNNMessage``, ``PaiNNUpdate``) and the edge geometry, radial basis,
+    embedding lookup and energy head as tensor operations on the GPU; forces
+    and the virial by autograd through the blocks' reverse kernels
+    (first-order: a force loss cannot be differentiated again there)."""
 
     def __init__(self, hidden_dim: int = 128, num_interactions: int = 3, num_rbf: int = 20,
                  cutoff: float = 5.0, max_z: int = 118, learnable_rbf: bool = False,
@@ -368,6 +384,79 @@ class StudentForceField(nn.Module):
 
     def num_parameters(self) -> int:
         return sum(p.numel() for p in self.parameters() if p.requires_grad)
+
+    @property
+    def fused(self) -> bool:
+        """True when the fused CUDA paths evaluate this model (hidden width 128)."""
+        return self.hidden_dim == FUSED_HIDDEN
+
+    # ------------------------------------------------- module-level path
+    def _neighbor_engine(self) -> Engine:
+        """Radius-graph builder of the module-level path.  The neighbour build
+        reads only the cutoff and the species count, so it runs at the fused
+        width with a one-layer, one-basis-function shape."""
+        dev = self.embedding.weight.device
+        eng = getattr(self, "_nbr_engine", None)
+        if eng is None or eng.device != dev:
+            eng = Engine(dims_of(FUSED_HIDDEN, 1, 1, self.max_z + 1, float(self.cutoff)), dev)
+            self._nbr_engine = eng
+        return eng
+
+    def _module_energy(self, positions: torch.Tensor, bt: Batch, mol_index: torch.Tensor,
+                       strain: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """Energies [B] (float64) of the module-level path, differentiable
+        with respect to positions, parameters and (given) the strain [B,3,3]
+        applied to every edge vector (dE/dstrain at 0 is the virial)."""
+        dev = positions.device
+        N = bt.n_atoms
+        row_ptr, col = self._neighbor_engine().neighbors(bt)
+        # edge_index as the reference's radius graph: source-major, rows then columns
+        src = torch.repeat_interleave(torch.arange(N, device=dev), (row_ptr[1:] - row_ptr[:-1]).to(torch.int64))
+        dst = col.to(torch.int64)
+        x = positions.to(torch.float32)
+        vec = x[src] - x[dst]                                   # student_model.py:709
+        if bt.box is not None:   # minimum image in orthorhombic periodic boxes
+            L = bt.box[mol_index[dst]]
+            per = bt.pbc[mol_index[dst]].to(torch.bool).unsqueeze(1)
+            vec = torch.where(per, vec - L * torch.round(vec / L), vec)
+        if strain is not None:
+            vec = torch.einsum("eab,eb->ea", torch.eye(3, device=dev, dtype=vec.dtype) + strain[mol_index[dst]], vec)
+        dist = torch.norm(vec, dim=1)
+        unit = vec / (dist.unsqueeze(1) + 1e-8)
+        rbf = self.rbf(dist) * self.cutoff_fn(dist).unsqueeze(-1)
+        s = self.embedding(bt.Z)
+        v = torch.zeros(N, 3, self.hidden_dim, device=dev, dtype=s.dtype)
+        edge_index = torch.stack([src, dst])
+        for block in self.interactions:
+            s, v = block(s, v, edge_index, rbf, unit)
+        e_atom = self.energy_head(s)[:, 0].to(torch.float64)
+        # per-structure sums in a fixed order (atoms are grouped by structure)
+        cs = torch.cat([e_atom.new_zeros(1), torch.cumsum(e_atom, 0)])
+        return cs[bt.mol_ptr[1:]] - cs[bt.mol_ptr[:-1]]
+
+    def _module_call(self, atomic_numbers, positions, cell, pbc, batch, forces=True, virial=False,
+                     create_graph=False):
+        """(energies [B] float64, forces [N,3] float32 or None, virial [B,3,3]
+        or None, structures) of the module-level path."""
+        dev = self.embedding.weight.device
+        host = positions.device.type == "cpu"
+        Zd = atomic_numbers.to(dev) if host else atomic_numbers
+        Pd = positions.to(dev) if host else positions
+        bt, mol_index, n_mol = self._make_batch(Zd, Pd, cell, pbc, batch)
+        need = forces or virial
+        x = Pd if (Pd.requires_grad or not need) else Pd.detach().requires_grad_(True)
+        eps = torch.zeros(n_mol, 3, 3, device=dev, requires_grad=True) if virial else None
+        with torch.enable_grad() if need else torch.no_grad():
+            E = self._module_energy(x, bt, mol_index, eps)
+            F = W = None
+            if need:
+                inputs = [x] + ([eps] if virial else [])
+                g = torch.autograd.grad(E.sum(), inputs, create_graph=create_graph, allow_unused=True)
+                if forces:
+                    F = -(g[0] if g[0] is not None else torch.zeros_like(x))
+                if virial:
+                    W = g[1] if g[1] is not None else torch.zeros(n_mol, 3, 3, device=dev)
+        return E, F, W, n_mol
 
     # ------------------------------------------------------------- engine
     @property
@@ -491,6 +580,10 @@ class StudentForceField(nn.Module):
                 batch: Optional[torch.Tensor] = None) -> torch.Tensor:
         """Total energy: 0-dim for one structure, [B] for a batch
         (student_model.py:634-757).  Differentiable w.r.t. positions."""
+        if not self.fused:
+            bt, mol_index, n_mol = self._make_batch(atomic_numbers, positions, cell, pbc, batch)
+            E = self._module_energy(positions, bt, mol_index).to(positions.dtype)
+            return E.sum() if n_mol <= 1 else E
         bt, mol_index, n_mol = self._make_batch(atomic_numbers, positions, cell, pbc, batch)
         train = _trainable(self) if self.training and torch.is_grad_enabled() else []
         if train:
@@ -509,6 +602,11 @@ class StudentForceField(nn.Module):
         parameters the forces are -dE/dpos taken with create_graph=True, as
         the reference does, so a loss on them back-propagates into the
         parameters."""
+        if not self.fused:
+            train = self.training and torch.is_grad_enabled() and bool(_trainable(self))
+            E, F, _, _ = self._module_call(atomic_numbers, positions, cell, pbc, None, create_graph=train)
+            E = E.to(positions.dtype).sum()
+            return (E, F.to(positions.dtype)) if train else (E.detach(), F.detach().to(positions.dtype))
         if self.training and torch.is_grad_enabled() and _trainable(self):
             x = positions if positions.requires_grad else positions.detach().requires_grad_(True)
             E = self.forward(atomic_numbers, x, cell=cell, pbc=pbc)
@@ -528,6 +626,10 @@ class StudentForceField(nn.Module):
         the library's CUDA adjoint.  energy is 0-dim for one structure and
         [B] for a batch (as ``forward``); forces [N,3]; neither carries an
         autograd graph."""
+        if not self.fused:
+            E, F, _, n_mol = self._module_call(atomic_numbers, positions, cell, pbc, batch)
+            E = E.detach().to(positions.dtype)
+            return (E.sum() if n_mol <= 1 else E), F.detach().to(positions.dtype)
         bt, _, n_mol = self._make_batch(atomic_numbers, positions, cell, pbc, batch, need_index=False)
         E, F, _ = self._engine_call(bt, forces=True)
         E = E.to(positions.dtype)
@@ -543,6 +645,10 @@ class StudentForceField(nn.Module):
         the inputs go straight into the cached CUDA graph's buffers and the
         results and status come back behind one synchronisation."""
         host = positions.device.type == "cpu" and atomic_numbers.device.type == "cpu"
+        if not self.fused:
+            E, F, _, _ = self._module_call(atomic_numbers, positions, cell, pbc, batch)
+            E, F = E.detach(), F.detach().to(torch.float32)
+            return (E.cpu(), F.cpu()) if host else (E, F)
         bt, _, _ = self._make_batch(atomic_numbers, positions, cell, pbc, batch, need_index=False,
                                     host_inputs=host)
         E, F, _ = self._engine_call(bt, forces=True, to_host=host)
@@ -550,6 +656,9 @@ class StudentForceField(nn.Module):
 
     def energy_forces_virial(self, atomic_numbers, positions, cell=None, pbc=None, batch=None):
         """Energies [B], forces [N,3] and dE/d(strain) [B,3,3] in one call."""
+        if not self.fused:
+            E, F, W, _ = self._module_call(atomic_numbers, positions, cell, pbc, batch, virial=True)
+            return E.detach(), F.detach().to(torch.float32), W.detach().to(torch.float64)
         bt, _, _ = self._make_batch(atomic_numbers, positions, cell, pbc, batch)
         return self._engine_call(bt, forces=True, virial=True)
 
