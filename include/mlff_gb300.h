@@ -307,9 +307,9 @@ int mlff_md_energy_stats(const double *epot, const double *ekin, int32_t n_sampl
  * the energy loss.  Runs the plain FP32 path forward (energies into
  * out->energy) and its hand-written reverse pass with the weight-gradient
  * reductions added; out->forces (optional) receives -sum_b w_b dE_b/dpos.
- * The weight-gradient reductions add in a fixed order; the plain path's
- * message scatter-adds are float atomics (as index_add_ on a GPU), so
- * repeated calls agree to rounding, not bit for bit.
+ * The plain path sums messages and node adjoints per receiver row in edge
+ * order and the weight-gradient reductions in a fixed order, so repeated
+ * calls give the same bits.
  * Workspace: mlff_workspace_size(..., MLFF_PATH_TRAIN). */
 int mlff_param_grads(const mlff_dims *dims, const void *packed, const mlff_system *sys,
                      int64_t edge_capacity, const double *energy_weights, const mlff_grads *grads,

@@ -175,28 +175,72 @@ static int sgemm(const T* A, const float* B, const float* bias, T* C, T* C2, con
 }
 
 // ------------------------------------------------------------- message
-// Xt[dst] += X[src] * phi  (index_add_, :359-385) -- one thread per
-// (edge, channel), float atomics.
+// Xt[a] = X[a] + sum over receiver a's edges (index_add_, :359-385) of
+// X[src] * phi, in edge order: one block per receiver row (the edges are
+// receiver-sorted), thread c = channel, so the sums are deterministic.
 template <class T>
-__global__ void pl_message_kernel(const T* __restrict__ X, const T* __restrict__ F,
-                                  const Vec4<T>* __restrict__ geo, const int32_t* __restrict__ col,
-                                  const int32_t* __restrict__ erecv, const int32_t* __restrict__ E_dev,
-                                  T* __restrict__ Xt, const Status* st) {
+__global__ void __launch_bounds__(128) pl_message_kernel(const T* __restrict__ X, const T* __restrict__ F,
+                                                         const Vec4<T>* __restrict__ geo,
+                                                         const int32_t* __restrict__ col,
+                                                         const int32_t* __restrict__ row_ptr, int32_t n_atoms,
+                                                         T* __restrict__ Xt, const Status* st) {
     if (st->code != 0) return;
-    const int64_t total = (int64_t)(*E_dev) * H;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t k = i / H;
-        const int c = (int)(i % H);
-        const int a = erecv[k], b = col[k];
-        const T* xs = X + (int64_t)b * 4 * H;
-        const T* f = F + k * H3;
-        const Vec4<T> g = geo[k];
+    const int c = threadIdx.x;
+    for (int a = blockIdx.x; a < n_atoms; a += gridDim.x) {
+        const T* xa = X + (int64_t)a * 4 * H;
+        T s = xa[c], v0 = xa[H + c], v1 = xa[2 * H + c], v2 = xa[3 * H + c];
+        const int k1 = row_ptr[a + 1];
+        for (int k = row_ptr[a]; k < k1; ++k) {
+            const T* xs = X + (int64_t)col[k] * 4 * H;
+            const T* f = F + (int64_t)k * H3;
+            const Vec4<T> g = geo[k];
+            const T f1 = f[H + c], f2 = f[2 * H + c];
+            s = s + xs[c] * f[c];
+            v0 = v0 + (xs[H + c] * f1 + g.x * f2);
+            v1 = v1 + (xs[2 * H + c] * f1 + g.y * f2);
+            v2 = v2 + (xs[3 * H + c] * f1 + g.z * f2);
+        }
         T* xt = Xt + (int64_t)a * 4 * H;
-        tatomic_add(&xt[c], xs[c] * f[c]);
-        const T f1 = f[H + c], f2 = f[2 * H + c];
-        tatomic_add(&xt[H + c], xs[H + c] * f1 + g.x * f2);
-        tatomic_add(&xt[2 * H + c], xs[2 * H + c] * f1 + g.y * f2);
-        tatomic_add(&xt[3 * H + c], xs[3 * H + c] * f1 + g.z * f2);
+        xt[c] = s;
+        xt[H + c] = v0;
+        xt[2 * H + c] = v1;
+        xt[3 * H + c] = v2;
+    }
+}
+
+// Node adjoints of the message step: dE/dX[b] = dE/dXt[b] + sum over the
+// edges k with sender b of (dE/dXt[a].s phi_s(k), dE/dXt[a].v phi_v1(k)),
+// a the receiver of k.  Gathered from b's own receiver row instead of
+// scattered from the senders: the edge k' = (a -> b) of that row is the
+// reverse of k and has the same filter (the same distance, bit for bit), so
+// the sum runs over b's row in order -- one block per atom, thread c =
+// channel, deterministic.
+template <class T>
+__global__ void __launch_bounds__(128) pl_message_bwd_nodes_kernel(const T* __restrict__ F,
+                                                                   const int32_t* __restrict__ col,
+                                                                   const int32_t* __restrict__ row_ptr,
+                                                                   int32_t n_atoms, const T* __restrict__ xtbar,
+                                                                   T* __restrict__ xbar, const Status* st) {
+    if (st->code != 0) return;
+    const int c = threadIdx.x;
+    for (int b = blockIdx.x; b < n_atoms; b += gridDim.x) {
+        const T* tb = xtbar + (int64_t)b * 4 * H;
+        T s = tb[c], v0 = tb[H + c], v1 = tb[2 * H + c], v2 = tb[3 * H + c];
+        const int k1 = row_ptr[b + 1];
+        for (int k = row_ptr[b]; k < k1; ++k) {
+            const T* ta = xtbar + (int64_t)col[k] * 4 * H;
+            const T* f = F + (int64_t)k * H3;
+            const T f1 = f[H + c];
+            s = s + ta[c] * f[c];
+            v0 = v0 + ta[H + c] * f1;
+            v1 = v1 + ta[2 * H + c] * f1;
+            v2 = v2 + ta[3 * H + c] * f1;
+        }
+        T* ob = xbar + (int64_t)b * 4 * H;
+        ob[c] = s;
+        ob[H + c] = v0;
+        ob[2 * H + c] = v1;
+        ob[3 * H + c] = v2;
     }
 }
 
@@ -292,8 +336,8 @@ __global__ void pl_update_bwd_post_kernel(const T* __restrict__ Xt, const T* __r
 // ---------------------------------------------------- message reverse
 // Per edge k (sender b -> receiver a), channel c:
 //   fbar[k] = (xtb_a.s * x_b.s, sum_i xtb_a.v_i * x_b.v_i, sum_i xtb_a.v_i * u_i)
-//   xbar_b += (xtb_a.s * phi_s, xtb_a.v * phi_v1)        (atomics)
 //   dE/du_k += sum_c xtb_a.v * phi_v2                    (block reduction)
+// (the node adjoints xbar_b: pl_message_bwd_nodes_kernel)
 // The dE/du accumulation feeds the forces only; the Dual instantiation
 // (parameter gradients of the force loss) leaves it out.
 constexpr int MB_EDGES = 8;
@@ -303,8 +347,7 @@ __global__ void __launch_bounds__(128) pl_message_bwd_kernel(const T* __restrict
                                                              const int32_t* __restrict__ col,
                                                              const int32_t* __restrict__ erecv,
                                                              const int32_t* __restrict__ E_dev,
-                                                             const T* __restrict__ xtbar,
-                                                             T* __restrict__ xbar, T* __restrict__ fbar,
+                                                             const T* __restrict__ xtbar, T* __restrict__ fbar,
                                                              float4* __restrict__ eacc, const Status* st) {
     __shared__ float red[4][MB_EDGES][3];
     if (st->code != 0) return;
@@ -327,13 +370,8 @@ __global__ void __launch_bounds__(128) pl_message_bwd_kernel(const T* __restrict
             fb[c] = tas * xb[c];
             fb[H + c] = tv0 * xb[H + c] + tv1 * xb[2 * H + c] + tv2 * xb[3 * H + c];
             fb[2 * H + c] = tv0 * g.x + tv1 * g.y + tv2 * g.z;
-            T* ob = xbar + (int64_t)b * 4 * H;
-            const T f1 = f[H + c], f2 = f[2 * H + c];
-            tatomic_add(&ob[c], tas * f[c]);
-            tatomic_add(&ob[H + c], tv0 * f1);
-            tatomic_add(&ob[2 * H + c], tv1 * f1);
-            tatomic_add(&ob[3 * H + c], tv2 * f1);
             if constexpr (!is_dual_v<T>) {
+                const T f2 = f[2 * H + c];
                 pu[q][0] = tv0 * f2;
                 pu[q][1] = tv1 * f2;
                 pu[q][2] = tv2 * f2;
@@ -442,6 +480,7 @@ static int run_plain_t(const mlff_dims& d, const float* P, const PackedOffsets& 
     float4* eacc = ws_ptr<float4>(ws, L.edge_acc);
     const int eblocks = 152 * 8;
     const int nblocks = (int)std::max<int64_t>(1, std::min<int64_t>(((int64_t)N * H + 255) / 256, 152 * 8));
+    const int rblocks = std::max(1, std::min(N, 152 * 16));   // receiver-row kernels: one block per atom
     int r;
     if (DUAL && (!grad || (!pos_t && !strain_t))) {
         set_error("the tangent pass needs gradient outputs and a position or strain direction");
@@ -477,10 +516,8 @@ static int run_plain_t(const mlff_dims& d, const float* P, const PackedOffsets& 
                           st))) return r;
         {
             ProfScope prof(PK_PLAIN_EDGE, st);
-            copy_kernel<T><<<nblocks, 256, 0, st>>>(X + l * NX, Xt + l * NX, NX, status);
-            MLFF_LAUNCH_CHECK("copy");
-            pl_message_kernel<T><<<eblocks, 256, 0, st>>>(X + l * NX, fl, geo, ws_ptr<int32_t>(ws, L.col),
-                                                          ws_ptr<int32_t>(ws, L.erecv), E_dev, Xt + l * NX, status);
+            pl_message_kernel<T><<<rblocks, 128, 0, st>>>(X + l * NX, fl, geo, ws_ptr<int32_t>(ws, L.col),
+                                                          ws_ptr<int32_t>(ws, L.row_ptr), N, Xt + l * NX, status);
             MLFF_LAUNCH_CHECK("pl_message");
         }
         // update (:434-470)
@@ -543,11 +580,14 @@ static int run_plain_t(const mlff_dims& d, const float* P, const PackedOffsets& 
         // message reverse: dE/dX^(l) = xtb + scatter; fbar; dE/du
         {
             ProfScope prof(PK_PLAIN_EDGE, st);
-            copy_kernel<T><<<nblocks, 256, 0, st>>>(xtb, xbo, NX, status);
-            MLFF_LAUNCH_CHECK("copy");
+            pl_message_bwd_nodes_kernel<T><<<rblocks, 128, 0, st>>>(ff + (int64_t)l * cap * H3,
+                                                                    ws_ptr<int32_t>(ws, L.col),
+                                                                    ws_ptr<int32_t>(ws, L.row_ptr), N, xtb, xbo,
+                                                                    status);
+            MLFF_LAUNCH_CHECK("pl_message_bwd_nodes");
             pl_message_bwd_kernel<T><<<eblocks, 128, 0, st>>>(X + l * NX, ff + (int64_t)l * cap * H3, geo,
                                                               ws_ptr<int32_t>(ws, L.col), ws_ptr<int32_t>(ws, L.erecv),
-                                                              E_dev, xtb, xbo, fbar, DUAL ? nullptr : eacc, status);
+                                                              E_dev, xtb, fbar, DUAL ? nullptr : eacc, status);
             MLFF_LAUNCH_CHECK("pl_message_bwd");
         }
         if (grad && (r = grad_filter_out<T>(L, ws, l, E_dev, grad->g, st))) return r;

@@ -52,18 +52,27 @@ def test_param_grads_vs_oracle(weights_seed0, weights_bias, wname):
 
 
 def test_param_grads_repeatable(weights_bias):
-    """Repeated calls agree to rounding (the plain path scatter-adds with
-    float atomics, as index_add_ does on a GPU)."""
-    from mlff_gb300 import systems
+    """Repeated calls give the same bits: the plain path sums messages and
+    node adjoints per receiver row in edge order and the weight-gradient
+    reductions in fixed splits (no float atomics), for the energy term and
+    for the force term's forward-mode pass; so do its energies and forces."""
+    from mlff_gb300 import _lib, systems
     from mlff_gb300.training import param_grads
     s = systems.molecule_batch(6, 10, 60, seed=12)
     m = _model(weights_bias)
     w = torch.linspace(-1, 1, s.n_mol, dtype=torch.float64)
-    _, g1, _ = param_grads(m, _batch(s), w)
-    _, g2, _ = param_grads(m, _batch(s), w)
+    G = torch.tensor(np.random.default_rng(3).normal(size=(s.n_atoms, 3)))
+    runs = [param_grads(m, _batch(s), w, forces=True, force_weights=G) for _ in range(2)]
+    (E1, g1, F1), (E2, g2, F2) = runs
+    torch.testing.assert_close(E1, E2, rtol=0, atol=0)
+    torch.testing.assert_close(F1, F2, rtol=0, atol=0)
     for k in g1:
-        scale = float(g1[k].abs().max()) + 1e-12
-        assert float((g1[k] - g2[k]).abs().max()) <= 1e-5 * scale, k
+        torch.testing.assert_close(g1[k], g2[k], rtol=0, atol=0, msg=k)
+    eng = m.engine()
+    a = [t.cpu() for t in eng.energy_forces(_batch(s), _lib.PATH_PLAIN_FP32, graph=False)[:2]]
+    b = [t.cpu() for t in eng.energy_forces(_batch(s), _lib.PATH_PLAIN_FP32, graph=False)[:2]]
+    for x, y in zip(a, b):
+        torch.testing.assert_close(x, y, rtol=0, atol=0)
 
 
 def test_training_gain_over_untrained(weights_seed0, weights_bias):
