@@ -746,18 +746,16 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                         *reinterpret_cast<float4*>(ua + 4) = *reinterpret_cast<const float4*>(u0 + col + 4);
                     }
                     tmem_ld_wait();
-                    // message terms of edge i, the same expressions on both branches
-                    // (a block's branch depends on where the tile starts)
-                    auto m0 = [&](int i) {
-                        return HH == 0 ? x0[i] * fa[i] : fmaf(x0[i], f1[i], ua[i] * f2[i]);
+                    // message terms of edge i added to the sums, the same expressions on
+                    // both branches (a block's branch depends on where the tile starts)
+                    auto add_m = [&](int i) {
+                        if (HH == 0) acc0 = fmaf(x0[i], fa[i], acc0);
+                        else acc0 = fmaf(x0[i], f1[i], fmaf(ua[i], f2[i], acc0));
+                        acc1 = fmaf(x1[i], f1[i], fmaf(ub[i], f2[i], acc1));
                     };
-                    auto m1 = [&](int i) { return fmaf(x1[i], f1[i], ub[i] * f2[i]); };
                     if (m == 0) {
 #pragma unroll
-                        for (int i = 0; i < 8; ++i) {
-                            acc0 += m0(i);
-                            acc1 += m1(i);
-                        }
+                        for (int i = 0; i < 8; ++i) add_m(i);
                     } else {   // a receiver starts in this block: store the finished sums
 #pragma unroll
                         for (int i = 0; i < 8; ++i) {
@@ -769,8 +767,7 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                                 acc0 = 0.f;
                                 acc1 = 0.f;
                             }
-                            acc0 += m0(i);
-                            acc1 += m1(i);
+                            add_m(i);
                         }
                     }
                 };
@@ -1402,6 +1399,7 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                 if (q >= 2) return;
                 const int l = 32 * q + lane, r = QR * b + l / 3, kk = l % 3;
                 const bool on = l < 3 * QR && r < nrcv;
+                if (!__any_sync(0xffffffffu, on)) return;   // no receiver row of this round in this warp
                 const int s0 = on ? r_first(r) : 0;
                 const int s1 = on ? (r + 1 < nrcv ? r_first(r + 1) : n) : 0;
                 float v[32];
@@ -1415,10 +1413,17 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                         if (i >= s0 && i < s1) dst[i] = v[i] + beta;
                 } else {         // u_kk (Q h') of dE/dd
                     float* dst = red + R_RED_DDU + kk * PN;
-                    const float* u = uc + kk * PN;
+                    const float4* u4 = reinterpret_cast<const float4*>(uc + kk * PN);   // 16-byte aligned
 #pragma unroll
-                    for (int i = 0; i < 32; ++i)
-                        if (i >= s0 && i < s1) dst[i] = u[i] * v[i];
+                    for (int i4 = 0; i4 < 8; ++i4) {
+                        const float4 u = u4[i4];
+                        const float uu[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            const int i = 4 * i4 + j;
+                            if (i >= s0 && i < s1) dst[i] = uu[j] * v[i];
+                        }
+                    }
                 }
             };
             epi3(0);
