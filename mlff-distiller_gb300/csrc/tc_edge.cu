@@ -397,14 +397,8 @@ __device__ __forceinline__ void issue_gemm2_chunk(int g, uint32_t tmem, uint32_t
 
 // out = base + (sum over the receiver's edges): receivers in [j0, j1)
 // without edges get the base row (the epilogues store base + sum once per
-// receiver that has edges).
-__device__ __forceinline__ void zero_empty_rows(float* out, const int32_t* row_ptr, int j0, int j1, int w, int lane,
-                                                int nwarps = NT / 32) {
-    for (int j = j0 + w; j < j1; j += nwarps)
-        if (row_ptr[j] == row_ptr[j + 1])
-            for (int k = lane; k < 4 * H; k += 32) out[(int64_t)j * 4 * H + k] = 0.0f;
-}
-// (out in the component-major layout, base in the pair layout)
+// receiver that has edges); out in the component-major layout, base in the
+// pair layout.
 __device__ __forceinline__ void copy_empty_rows(float* out, const float* base, const int32_t* row_ptr, int j0, int j1,
                                                 int w, int lane, int nwarps = NT / 32) {
     for (int j = j0 + w; j < j1; j += nwarps)
@@ -1215,10 +1209,16 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
         const int e0 = a.row_ptr[j0], e1 = a.row_ptr[j1];
         const int ntl = (e1 - e0 + PN - 1) / PN;
         const unsigned char* etiles = a.etile + (size_t)a.etile_base[p] * ET_BYTES;
-        if (a.write_nodes) zero_empty_rows(a.xbar, a.row_ptr, j0, j1, wl, lane, PT / 32);
+        // dE/dX = dE/dXt + the gathered sums: receivers without edges get their dE/dXt row
+        if (a.write_nodes) copy_empty_rows(a.xbar, a.xtbar, a.row_ptr, j0, j1, wl, lane, PT / 32);
         int cur = j0;
-        float acc0 = 0.f, acc1 = 0.f;   // node adjoints of the current receiver, two components
-        float cr0 = 0.f, cr1 = 0.f;     // its dE/dXt rows (the same two components)
+        float acc0 = 0.f, acc1 = 0.f;   // gathered node adjoints of the current receiver, two components
+        float cr0, cr1;                 // its dE/dXt rows (the same two components)
+        {
+            const float2 r = __ldg(xtb + (int64_t)j0 * 2 * H);
+            cr0 = r.x;
+            cr1 = r.y;
+        }
         if (ntl > 0) {   // the partition's first tile: edge arrays and [E; E'] tile
             fetch(sbase, e0, min(PN, e1 - e0));
             if (tp == 32) {
@@ -1228,9 +1228,7 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
             }
             cp_async_wait_all();
             pipe_sync(pp);
-            // prev = -1 marks edge 0 as a receiver start, so that the first
-            // block loads its receiver's rows
-            if (tp < PN) prep(sbase, min(PN, e1 - e0), -1);
+            if (tp < PN) prep(sbase, min(PN, e1 - e0), j0);
             pipe_sync(pp);
         }
         for (int k = 0; k < ntl; ++k) {
@@ -1509,8 +1507,8 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                         for (int i = 0; i < 4; ++i) {
                             if (m & (1u << i)) {
                                 if (a.write_nodes) {
-                                    out[(int64_t)cur * 4 * H] = acc0;
-                                    out[(int64_t)cur * 4 * H + H] = acc1;
+                                    out[(int64_t)cur * 4 * H] = r0 + acc0;
+                                    out[(int64_t)cur * 4 * H + H] = r1 + acc1;
                                 }
                                 cur = rcv_s[col + i];
                                 acc0 = 0.f;
@@ -1582,8 +1580,8 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
             }
         }
         if (!aborted && a.write_nodes) {
-            out[(int64_t)cur * 4 * H] = acc0;
-            out[(int64_t)cur * 4 * H + H] = acc1;
+            out[(int64_t)cur * 4 * H] = cr0 + acc0;
+            out[(int64_t)cur * 4 * H + H] = cr1 + acc1;
         }
     }
     // drain: every MMA and copy this CTA issued must be complete before it

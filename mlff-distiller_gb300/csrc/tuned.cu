@@ -319,43 +319,6 @@ __global__ void edge_geom_kernel(EdgeArgs a, float4* __restrict__ geo) {
 
 // dst += src over n4 float4 elements (the reverse tensor-core edge kernel
 // writes the gathered part of dE/dX only)
-// dst (component-major) += src, src component-major or (pairs) in the pair
-// layout: float4 i of dst holds channels 4 (i % 32) .. + 3 of component
-// (i / 32) % 4, which the pair layout keeps as every other float of two
-// 16-byte words
-__global__ void add_rows_kernel(float4* __restrict__ dst, const float4* __restrict__ src, int64_t n4, int pairs,
-                                const Status* st) {
-    pdl_wait();
-    pdl_trigger();
-    if (st->code != 0) return;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n4; i += (int64_t)gridDim.x * blockDim.x) {
-        float4 d = dst[i];
-        float4 s;
-        if (pairs) {
-            const int64_t a = i / 128;
-            const int q = (int)(i % 128), comp = q / 32, l = q % 32;
-            const float4* pr = src + a * 128 + (comp >> 1) * 64 + 2 * l;
-            const float4 p0 = pr[0], p1 = pr[1];
-            s = (comp & 1) ? make_float4(p0.y, p0.w, p1.y, p1.w) : make_float4(p0.x, p0.z, p1.x, p1.z);
-        } else {
-            s = src[i];
-        }
-        d.x += s.x;
-        d.y += s.y;
-        d.z += s.z;
-        d.w += s.w;
-        dst[i] = d;
-    }
-}
-
-static int add_rows(float* dst, const float* src, int64_t n, bool pairs, const Status* st, cudaStream_t s) {
-    const int64_t n4 = n / 4;
-    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((n4 + 255) / 256, 152 * 8));
-    MLFF_LAUNCH_PDL("add_rows", add_rows_kernel, blocks, 256, 0, s, reinterpret_cast<float4*>(dst),
-                    reinterpret_cast<const float4*>(src), n4, pairs ? 1 : 0, st);
-    return MLFF_OK;
-}
-
 int run_tuned(const mlff_dims& d, const float* P, const PackedOffsets& po, const mlff_system& sys,
               const WsLayout& L, void* ws, const mlff_outputs& out, int path, cudaStream_t st,
               const VerletFuse* vf) {
@@ -454,10 +417,7 @@ int run_tuned(const mlff_dims& d, const float* P, const PackedOffsets& po, const
                 MLFF_LAUNCH_CHECK("edge_bwd_simt");
             }
         }
-        if (tc && l > 0) {
-            ProfScope prof(PK_OTHER, st);
-            if ((r = add_rows(xbo, xtb, NX, true, a.st, st))) return r;   // dE/dX = dE/dXt + gathered part
-        }
+        // (the tensor-core reverse kernel writes dE/dX = dE/dXt + the gathered part itself)
     }
     return launch_forces(d, sys, L, ws, out, st, vf);
 }
