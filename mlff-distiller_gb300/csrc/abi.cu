@@ -152,13 +152,10 @@ WsLayout ws_layout(const mlff_dims& d, int32_t n_atoms, int32_t n_mol, int64_t c
     L.md_noise = take(sizeof(double) * 6 * N);
     if (path == MLFF_PATH_TUNED_TC) {
         L.geo = take(sizeof(float4) * cap);
-        // at most cap / tile + one partial tile per partition: forward tiles
-        // of 64 edges, reverse tiles of 32 edges, 8 KB each
-        L.n_etile_f = cap / 64 + P_max + 1;   // sum over partitions of ceil(E_p / 64)
-        L.n_etile_b = cap / 32 + P_max + 1;   // ceil(E_p / 32)
-        L.etile_base = take(4 * 2 * ((size_t)P_max + 1));
-        L.etile_f = take((size_t)L.n_etile_f * 8192);
-        L.etile_b = take((size_t)L.n_etile_b * 8192);
+        // at most cap / 32 + one partial tile per partition: sum over partitions of ceil(E_p / 32)
+        L.n_etile = cap / 32 + P_max + 1;
+        L.etile_base = take(4 * ((size_t)P_max + 1));
+        L.etile = take((size_t)L.n_etile * 8192);
         L.qs = take((size_t)N * 3 * 2 * H * 2);
         L.qb = take(sizeof(float) * 3 * N);
     }

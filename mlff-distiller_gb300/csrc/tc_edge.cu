@@ -178,14 +178,14 @@ __device__ __forceinline__ void rbf16_d(float d, bool valid, int r0, int R, cons
 }
 
 // ------------------------------------------------------ E tiles (per call)
-// The RBF x cutoff rows of every edge tile as split fp16 in the K-major
-// no-swizzle layout (16-byte core matrices: K-step s at rows * 32 s, its
-// second 8 columns rows * 16 further, 8-row groups 128 apart; the hi image,
-// then the lo image rows * 64 further), computed once per call for all
-// layers, 64 rows per tile: forward tiles of 64 edges, reverse tiles of 32
-// edges with rows 0-31 the RBF rows and rows 32-63 their d-derivatives.
-// Tiles follow the receiver partitions: tile k of partition p is the k-th
-// tile the pipeline that owns p processes.
+// [E; E'] tiles: for every 32 consecutive edges of a receiver partition, the
+// RBF x cutoff rows (rows 0-31) and their d-derivatives (rows 32-63) as
+// split fp16 in the K-major no-swizzle layout (16-byte core matrices:
+// K-step s at rows * 32 s, its second 8 columns rows * 16 further, 8-row
+// groups 128 apart; the hi image, then the lo image rows * 64 further),
+// computed once per call for all layers.  Tile k of partition p is the
+// reverse kernel's k-th tile of p; the forward kernel's 64-edge tile k reads
+// the E rows of tiles 2k and 2k + 1.
 constexpr uint32_t ET_ROWS = 64;
 constexpr uint32_t ET_BYTES = ET_ROWS * 128, ET_HALF = ET_ROWS * 64;   // 8 KB, hi then lo
 __device__ __forceinline__ uint32_t et_off(int rows, int row, int k) {
@@ -193,55 +193,41 @@ __device__ __forceinline__ uint32_t et_off(int rows, int row, int k) {
                       (k & 7) * 2);
 }
 
-// Tile counts of all partitions (forward: 64 edges per tile, reverse: 32),
-// then exclusive scans (one block, 1024 partitions at a time): forward bases
-// at base[0..P], reverse bases at base[P+1 .. 2P+1].
+// Tile counts of all partitions (32 edges per tile), then their exclusive
+// scan (one block, 1024 partitions at a time): bases at base[0..P].
 __global__ void __launch_bounds__(1024) etile_index_kernel(const int32_t* __restrict__ row_ptr,
                                                            const int32_t* __restrict__ part, int P,
                                                            int32_t* __restrict__ base) {
     pdl_wait();
     pdl_trigger();
-    __shared__ int cf[1024], cb[1024];
-    __shared__ int carry[2];
+    __shared__ int cb[1024];
+    __shared__ int carry;
     const int t = threadIdx.x;
-    if (t == 0) carry[0] = carry[1] = 0;
+    if (t == 0) carry = 0;
     __syncthreads();
     for (int p0 = 0; p0 < P; p0 += 1024) {
         const int p = p0 + t;
-        int nf = 0, nb = 0;
+        int nb = 0;
         if (p < P) {
             const int E = row_ptr[part[p + 1]] - row_ptr[part[p]];
-            nf = (E + 63) / 64;
             nb = (E + 31) / 32;
         }
-        cf[t] = nf;
         cb[t] = nb;
         __syncthreads();
         for (int o = 1; o < 1024; o <<= 1) {   // inclusive scan (Hillis-Steele)
-            const int xf = t >= o ? cf[t - o] : 0, xb = t >= o ? cb[t - o] : 0;
+            const int xb = t >= o ? cb[t - o] : 0;
             __syncthreads();
-            cf[t] += xf;
             cb[t] += xb;
             __syncthreads();
         }
-        if (p < P) {
-            base[p] = carry[0] + cf[t] - nf;
-            base[P + 1 + p] = carry[1] + cb[t] - nb;
-        }
+        if (p < P) base[p] = carry + cb[t] - nb;
         __syncthreads();
-        if (t == 1023) {
-            carry[0] += cf[1023];
-            carry[1] += cb[1023];
-        }
+        if (t == 1023) carry += cb[1023];
         __syncthreads();
     }
-    if (t == 0) {
-        base[P] = carry[0];
-        base[2 * P + 1] = carry[1];
-    }
+    if (t == 0) base[P] = carry;
 }
 
-template <bool REV>
 __global__ void __launch_bounds__(256) etile_fill_kernel(EdgeArgs a, const int32_t* __restrict__ base,
                                                          unsigned char* __restrict__ out) {
     pdl_wait();
@@ -253,16 +239,16 @@ __global__ void __launch_bounds__(256) etile_fill_kernel(EdgeArgs a, const int32
     }
     __syncthreads();
     if (a.st->code != 0) return;
-    constexpr int TE = REV ? 32 : 64;                   // edges per tile
+    constexpr int TE = 32;                              // edges per tile
     constexpr int ROWS = ET_ROWS;
     constexpr int PER = 2 * ROWS;                       // threads per tile: (row, K-step)
     constexpr int TPI = 256 / PER;                      // tiles per block iteration
     const int t = threadIdx.x, sub = t / PER, loc = t % PER;
     const int row = loc % ROWS, s = loc / ROWS;
-    const int which = REV ? (row >> 5) : 0, erow = REV ? (row & 31) : row;
+    const int which = row >> 5, erow = row & 31;
     for (int p = blockIdx.x; p < a.nparts; p += gridDim.x) {
         const int e0 = a.row_ptr[a.part[p]], e1 = a.row_ptr[a.part[p + 1]];
-        const int b0 = base[(REV ? a.nparts + 1 : 0) + p];
+        const int b0 = base[p];
         for (int k = blockIdx.y * TPI + sub; e0 + k * TE < e1; k += gridDim.y * TPI) {
             const int e = e0 + k * TE + erow;
             const bool valid = e < e1;
@@ -285,13 +271,10 @@ __global__ void __launch_bounds__(256) etile_fill_kernel(EdgeArgs a, const int32
     }
 }
 
-int launch_etiles(const EdgeArgs& a, int32_t* base, unsigned char* fwd, unsigned char* rev, cudaStream_t st) {
+int launch_etiles(const EdgeArgs& a, int32_t* base, unsigned char* tiles, cudaStream_t st) {
     MLFF_LAUNCH_PDL("etile_index", etile_index_kernel, 1, 1024, 0, st, a.row_ptr, a.part, a.nparts, base);
     // tiles of a partition spread over gridDim.y blocks
-    MLFF_LAUNCH_PDL("etile_fill_fwd", etile_fill_kernel<false>, dim3(a.nparts, 16), 256, 0, st, a, base, fwd);
-    if (rev) {
-        MLFF_LAUNCH_PDL("etile_fill_rev", etile_fill_kernel<true>, dim3(a.nparts, 16), 256, 0, st, a, base, rev);
-    }
+    MLFF_LAUNCH_PDL("etile_fill", etile_fill_kernel, dim3(a.nparts, 16), 256, 0, st, a, base, tiles);
     return MLFF_OK;
 }
 
@@ -474,7 +457,7 @@ constexpr uint32_t Q_OFF_B2 = Q_OFF_B1 + H * 4;
 constexpr uint32_t Q_OFF_BAR = Q_OFF_B2 + H3 * 4;
 constexpr uint32_t Q_OFF_MISC = Q_OFF_BAR + 8 * 8;
 constexpr uint32_t Q_SMEM = align1k(Q_OFF_MISC + 16);
-static_assert(ET_BYTES <= 2 * Q_HH, "E tile fits in the H tile's space");
+static_assert(2 * ET_BYTES <= 2 * Q_HH, "two [E; E'] tiles fit in the H tile's space");
 static_assert(Q_SB_BYTES % 16 == 0, "edge array alignment");
 static_assert(Q_SMEM <= 232448, "forward kernel shared memory");
 
@@ -536,7 +519,7 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
     const int pp = w >> 3, wl = w & 7, tp = t & (PT - 1), hh = wl >> 2;
     const uint32_t TB = 128 + 192 * pp;             // the pipeline's TMEM columns: chunk g at TB + 64 g
     unsigned char* Hs = smem + Q_OFF_H + pp * 2 * Q_HH;   // H hi, then lo
-    unsigned char* Es = Hs;                         // E tile (bulk-copied) before H is written
+    unsigned char* Es = Hs;                         // [E; E'] tiles (bulk-copied) before H is written
     uint64_t* mma_bar = bars + 2 + 3 * pp;
     uint64_t* e_bar = bars + 3 + 3 * pp;
     uint64_t* g2_bar = bars + 4 + 3 * pp;
@@ -559,41 +542,48 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
         fetch_tile_edges(a, tp, QN, t0, nn, reinterpret_cast<float4*>(sbx + Q_SB_US),
                          reinterpret_cast<int*>(sbx + Q_SB_SRC), reinterpret_cast<int*>(sbx + Q_SB_RCV));
     };
-    // z^T = W1 e^T on the E tile at Es into chunk 0's columns, once its copy
-    // has landed (thread tp 0)
-    auto issue_gemm1 = [&]() {
+    // z^T = W1 e^T into chunk 0's columns, once the copies have landed
+    // (thread tp 0): the tile's 64 edges are the E rows (0-31) of nt
+    // consecutive [E; E'] tiles at Es (edges 32 j .. 32 j + 31 from tile j)
+    auto issue_gemm1 = [&](int nt) {
         if (!mbar_wait(e_bar, e_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 8);
         fence_after_sync();
-        constexpr uint32_t idesc = idesc_f16(QN);
+        constexpr uint32_t idesc = idesc_f16(32);
+        for (int j = 0; j < nt; ++j)
 #pragma unroll
-        for (int s = 0; s < 2; ++s)
+            for (int s = 0; s < 2; ++s)
 #pragma unroll
-            for (int pr = 0; pr < 3; ++pr) {
-                const uint32_t ahl = pr == 2 ? 1 : 0, bhl = pr == 1 ? 1 : 0;
-                const uint64_t ad = sdesc(smem_u32(w1s + s * SLAB + ahl * A_TILE), A_LBO, A_SBO);
-                const uint64_t bd = sdesc(smem_u32(Es + bhl * ET_HALF + s * (ET_ROWS * 32)), ET_ROWS * 16, 128);
-                mma_f16(tmem + TB, ad, bd, idesc, (s | pr) != 0);
-            }
+                for (int pr = 0; pr < 3; ++pr) {
+                    const uint32_t ahl = pr == 2 ? 1 : 0, bhl = pr == 1 ? 1 : 0;
+                    const uint64_t ad = sdesc(smem_u32(w1s + s * SLAB + ahl * A_TILE), A_LBO, A_SBO);
+                    const uint64_t bd = sdesc(smem_u32(Es + j * ET_BYTES + bhl * ET_HALF + s * (ET_ROWS * 32)),
+                                              ET_ROWS * 16, 128);
+                    mma_f16(tmem + TB + 32 * j, ad, bd, idesc, (s | pr) != 0);
+                }
         mma_commit(mma_bar);
+    };
+    // copies of the [E; E'] tiles of forward tile k (thread tp QN)
+    auto copy_etiles = [&](const unsigned char* etiles, int nrev, int k) {
+        const int nt = min(2, nrev - 2 * k);
+        mbar_expect_tx(e_bar, nt * ET_BYTES);
+        for (int j = 0; j < nt; ++j) bulk_g2s(Es + j * ET_BYTES, etiles + (size_t)(2 * k + j) * ET_BYTES, ET_BYTES, e_bar);
+        ++e_issued;
     };
     for (int p = 2 * blockIdx.x + pp; p < a.nparts && !aborted; p += 2 * gridDim.x) {
         const int j0 = a.part[p], j1 = a.part[p + 1];
         if (j0 >= j1) continue;
         const int e0 = a.row_ptr[j0], e1 = a.row_ptr[j1];
         const int ntl = (e1 - e0 + QN - 1) / QN;
+        const int nrev = (e1 - e0 + 31) / 32;   // [E; E'] tiles of the partition
         const unsigned char* etiles = a.etile + (size_t)a.etile_base[p] * ET_BYTES;
         copy_empty_rows(a.Xt, a.X, a.row_ptr, j0, j1, wl, lane, PT / 32);
         int cur = j0;
         float acc0 = 0.f, acc1 = 0.f;   // message sums of the current receiver, two components
         // X of the current receiver (the residual term of Xt)
         float2 base = xx[(int64_t)cur * 2 * H];
-        if (ntl > 0) {   // the partition's first tile: edge arrays and E tile
+        if (ntl > 0) {   // the partition's first tile: edge arrays and E tiles
             fetch(sbase, e0, min(QN, e1 - e0));
-            if (tp == QN) {
-                mbar_expect_tx(e_bar, ET_BYTES);
-                bulk_g2s(Es, etiles, ET_BYTES, e_bar);
-                ++e_issued;
-            }
+            if (tp == QN) copy_etiles(etiles, nrev, 0);
             cp_async_wait_all();
             pipe_sync(pp);
             if (tp < QN) prep(sbase, min(QN, e1 - e0), j0);
@@ -609,7 +599,7 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
             const uint32_t* chg = reinterpret_cast<const uint32_t*>(sb + Q_SB_CHG);
             // z^T = W1 e^T on the bulk-copied tile, into chunk 0's columns (read
             // by the scalar warps until the end of the previous tile's epilogue 2)
-            if (tp == 0) issue_gemm1();
+            if (tp == 0) issue_gemm1((n + 31) / 32);
             e_phase ^= 1;
             if (wl == 0) {
                 __syncwarp();
@@ -711,11 +701,7 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
             const bool more = k + 1 < ntl && !abort_now;
             if (more) {
                 fetch(sbn, t0 + QN, min(QN, e1 - t0 - QN));
-                if (tp == QN) {
-                    mbar_expect_tx(e_bar, ET_BYTES);
-                    bulk_g2s(Es, etiles + (size_t)(k + 1) * ET_BYTES, ET_BYTES, e_bar);
-                    ++e_issued;
-                }
+                if (tp == QN) copy_etiles(etiles, nrev, k + 1);
             }
             if (wl == 2) __syncwarp();
             {   // epilogue 2: components 2 hh, 2 hh + 1 of the message sums, segmented

@@ -300,7 +300,7 @@ int launch_edge_fwd_tc(const EdgeArgs& a, int layer, cudaStream_t st);
 int launch_edge_bwd_tc(const EdgeArgs& a, int layer, cudaStream_t st);
 int launch_vq(const float* P, const LayerOffsets& lo, const float* xtbar, int n_atoms, unsigned char* qs, float* qb,
               Status* st_word, cudaStream_t st);
-int launch_etiles(const EdgeArgs& a, int32_t* base, unsigned char* fwd, unsigned char* rev, cudaStream_t st);
+int launch_etiles(const EdgeArgs& a, int32_t* base, unsigned char* tiles, cudaStream_t st);
 
 
 __global__ void edge_geom_kernel(EdgeArgs a, float4* __restrict__ geo) {
@@ -357,12 +357,13 @@ int run_tuned(const mlff_dims& d, const float* P, const PackedOffsets& po, const
         const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((L.cap + 255) / 256, 152 * 8));
         MLFF_LAUNCH_PDL("edge_geom", edge_geom_kernel, blocks, 256, 0, st, a, geo);
         a.geo = geo;
-        // RBF x cutoff tiles for every edge tile of every layer (and their
-        // d-derivative for the reverse pass when forces are asked for)
-        const bool rev = out.forces != nullptr || out.virial != nullptr;
-        if ((r = launch_etiles(a, ws_ptr<int32_t>(ws, L.etile_base), ws_ptr<unsigned char>(ws, L.etile_f),
-                               rev ? ws_ptr<unsigned char>(ws, L.etile_b) : nullptr, st)))
+        // [E; E'] tiles (RBF x cutoff and its d-derivative) of every 32 edges,
+        // for every layer: the forward kernel reads their E rows, the reverse
+        // kernel both
+        if ((r = launch_etiles(a, ws_ptr<int32_t>(ws, L.etile_base), ws_ptr<unsigned char>(ws, L.etile), st)))
             return r;
+        a.etile = ws_ptr<unsigned char>(ws, L.etile);
+        a.etile_base = ws_ptr<int32_t>(ws, L.etile_base);
     }
     for (int l = 0; l < d.n_layers; ++l) {
         a.lo = po.layer[l];
@@ -371,8 +372,6 @@ int run_tuned(const mlff_dims& d, const float* P, const PackedOffsets& po, const
         {
             ProfScope prof(PK_EDGE_FWD, st);
             if (tc) {
-                a.etile = ws_ptr<unsigned char>(ws, L.etile_f);
-                a.etile_base = ws_ptr<int32_t>(ws, L.etile_base);
                 if ((r = launch_edge_fwd_tc(a, l, st))) return r;   // writes Xt = X + messages
             } else {
                 edge_fwd_simt_kernel<<<L.P, 128, 0, st>>>(a);
@@ -409,8 +408,6 @@ int run_tuned(const mlff_dims& d, const float* P, const PackedOffsets& po, const
         {
             ProfScope prof(PK_EDGE_BWD, st);   // the reverse edge kernel alone
             if (tc) {
-                a.etile = ws_ptr<unsigned char>(ws, L.etile_b);
-                a.etile_base = ws_ptr<int32_t>(ws, L.etile_base) + L.P + 1;
                 if ((r = launch_edge_bwd_tc(a, l, st))) return r;
             } else {
                 edge_bwd_simt_kernel<<<L.P, 128, 0, st>>>(a);

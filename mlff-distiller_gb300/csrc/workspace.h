@@ -41,12 +41,11 @@ struct WsLayout {
     size_t md_noise;           // double [N][6] Langevin normals of a step (ASE's scheme: xi, eta)
     // plain path (materialised per-edge tensors, like the reference's graph)
     size_t geo;                // float4 [cap] (u_x, u_y, u_z, d)
-    size_t etile_base;         // int32 [2][P+1] first E tile of each partition (forward, reverse)
-    size_t etile_f;            // forward E tiles: 64 edges x K 32, split fp16, 8 KB each
-    size_t etile_b;            // reverse [E; E'] tiles: 32 edges, 64 rows, 8 KB each
+    size_t etile_base;         // int32 [P+1] first [E; E'] tile of each partition
+    size_t etile;              // [E; E'] tiles: 32 edges, 64 rows (E, then E'), split fp16, 8 KB each
     size_t qs;                 // reverse: per-atom Q rows [N][3][hi, lo][H] fp16 (W2's third chunk^T dE/dXt_v)
     size_t qb;                 // reverse: per-atom b2 . dE/dXt_v [N][3] float
-    int64_t n_etile_f, n_etile_b;
+    int64_t n_etile;
     size_t erbf;               // float [cap][RMAX]
     size_t erbf_d;             // float [cap][RMAX]
     size_t fz;                 // float [L][cap][H]
