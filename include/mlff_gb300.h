@@ -370,7 +370,8 @@ int mlff_profile_end(double *ms_by_kind, int64_t *launches_by_kind, int32_t n_ki
  * MMAs), and the workspace size does not either.  mlff_autotune times
  * `repeats` calls of mlff_energy_forces per candidate (same arguments; the
  * outputs are overwritten) with CUDA events on the stream: f = 1, 2, 4 with
- * 64-atom update tiles, then the fastest f with 32-atom tiles; it
+ * 64-atom update tiles, then the fastest f with 32-atom tiles (kept when at
+ * least 1 % faster); it
  * synchronises the stream, caches the fastest shape and writes its f to
  * *chosen (host) and the milliseconds per call of f = 1, 2, 4 (64-atom
  * tiles) to ms_per_candidate (host double [3], or NULL).  Not for use while
