@@ -27,7 +27,7 @@ from . import _lib
 
 DEFAULT_EDGES_PER_ATOM = 64
 GRAPH_CACHE_SIZE = 4
-AUTOTUNE_REPEATS = 3
+AUTOTUNE_REPEATS = 6
 _tuned_buckets = set()   # (path, ceil log2 atoms, ceil log2 structures) tuned in this process
 
 
