@@ -871,27 +871,6 @@ static_assert(4 * R_SB_BYTES >= 1024, "bytes behind the last Q half");
 static_assert(3 * QR <= 64, "Q rows of a round");
 static_assert(R_SMEM <= 232448, "reverse kernel shared memory");
 
-// Sum 4 per-lane values over the 32 lanes of a warp (reduce-scatter):
-// afterwards lanes with (lane & 7) == 0 hold the sum of value index
-// bits 4..3 of the lane id.
-__device__ __forceinline__ float warp_reduce_scatter4(const float (&v)[4], int lane) {
-    float w2[2];
-    const bool b16 = lane & 16, b8 = lane & 8;
-#pragma unroll
-    for (int j = 0; j < 2; ++j) {
-        const float send = b16 ? v[j] : v[j + 2];
-        const float keep = b16 ? v[j + 2] : v[j];
-        w2[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
-    }
-    const float send = b8 ? w2[0] : w2[1];
-    const float keep = b8 ? w2[1] : w2[0];
-    float w1 = keep + __shfl_xor_sync(0xffffffffu, send, 8);
-    w1 += __shfl_xor_sync(0xffffffffu, w1, 4);
-    w1 += __shfl_xor_sync(0xffffffffu, w1, 2);
-    w1 += __shfl_xor_sync(0xffffffffu, w1, 1);
-    return w1;
-}
-
 // GEMM3: D (64 TMEM columns at dcol) = Q [H; H']^T, the Q tile at qt (hi
 // half, then lo half QT_HALF bytes later; K-major, no swizzle, rows 0-63,
 // LBO 1024, K-steps 2048 bytes apart), B the split-fp16 [H; H'] tile.
@@ -1150,7 +1129,7 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
     uint64_t* g3_bar = bars + 5 + 4 * pp;
     float* red = reinterpret_cast<float*>(smem + R_OFF_RED) + pp * R_RED_FLOATS;
     unsigned char* sbase = smem + R_OFF_SB + 2 * pp * R_SB_BYTES;
-    const int rs4_idx = ((lane >> 4) & 1) * 2 + ((lane >> 3) & 1);
+    const int rs8_idx = reduce_scatter8_index(lane);
     // components 2 hh and 2 hh + 1: one float2 of the pair layout of dE/dXt
     // and X, H floats apart in the component-major dE/dX
     const float2* xtb = reinterpret_cast<const float2*>(a.xtbar + pair_off(2 * hh, c));
@@ -1456,7 +1435,7 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
             {   // epilogue 2 over 4-edge blocks, the next block's gathers in flight
                 // (compiled once per warp half: hc is std::integral_constant<int, hh>)
                 auto process4 = [&](auto hc, const float (&tb0)[4], const float (&tb1)[4], const float (&xb0)[4],
-                                    const float (&xb1)[4], float rn0, float rn1, int col) {
+                                    const float (&xb1)[4], float rn0, float rn1, int col, float* pv) {
                     constexpr int HH = decltype(hc)::value;
                     float fa[4], da[4], f1[4], d1[4];
                     if (HH == 0) {
@@ -1475,7 +1454,6 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                     // phi_s', phi_v1'), given the receiver's dE/dXt rows t0, t1;
                     // the same expressions on both branches below (a block's branch
                     // depends on where the tile starts)
-                    float pv[4];
                     float r0 = cr0, r1 = cr1;   // the current receiver's dE/dXt rows
                     auto edge_term = [&](int i, float t0, float t1) {
                         if (HH == 0) pv[i] = fmaf(t0 * xb0[i], da[i], t1 * xb1[i] * d1[i]);
@@ -1515,16 +1493,24 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
                     }
                     cr0 = r0;
                     cr1 = r1;
-                    const float s4 = warp_reduce_scatter4(pv, lane);
-                    if ((lane & 7) == 0) red[wl * PN + col + rs4_idx] = s4;
                 };
+                // the shares of dE/dd of blocks col and col + 4 are reduced
+                // across lanes together (9 shuffles for 8 edges); a missing
+                // second block (padding edges, never read) contributes zeros
                 auto blocks = [&](auto hc) {
                     for (int col = 0; col < n; col += 8) {   // blocks col and col + 4 are in flight
-                        process4(hc, tba0, tba1, xba0, xba1, ra0, ra1, col);
-                        if (col + 4 >= n) break;
-                        if (col + 8 < n) gather4(tba0, tba1, xba0, xba1, ra0, ra1, col + 8);
-                        process4(hc, tbb0, tbb1, xbb0, xbb1, rb0, rb1, col + 4);
-                        if (col + 12 < n) gather4(tbb0, tbb1, xbb0, xbb1, rb0, rb1, col + 12);
+                        float pv[8];
+                        process4(hc, tba0, tba1, xba0, xba1, ra0, ra1, col, pv);
+                        if (col + 4 < n) {
+                            if (col + 8 < n) gather4(tba0, tba1, xba0, xba1, ra0, ra1, col + 8);
+                            process4(hc, tbb0, tbb1, xbb0, xbb1, rb0, rb1, col + 4, pv + 4);
+                            if (col + 12 < n) gather4(tbb0, tbb1, xbb0, xbb1, rb0, rb1, col + 12);
+                        } else {
+#pragma unroll
+                            for (int i = 4; i < 8; ++i) pv[i] = 0.f;
+                        }
+                        const float s8 = warp_reduce_scatter8(pv, lane);
+                        if ((lane & 3) == 0) red[wl * PN + col + rs8_idx] = s8;
                     }
                 };
                 if (hh == 0) blocks(std::integral_constant<int, 0>{});
