@@ -180,17 +180,19 @@ __device__ __forceinline__ void rbf16_d(float d, bool valid, int r0, int R, cons
 // ------------------------------------------------------ E tiles (per call)
 // [E; E'] tiles: for every 32 consecutive edges of a receiver partition, the
 // RBF x cutoff rows (rows 0-31) and their d-derivatives (rows 32-63) as
-// split fp16 in the K-major no-swizzle layout (16-byte core matrices:
-// K-step s at rows * 32 s, its second 8 columns rows * 16 further, 8-row
-// groups 128 apart; the hi image, then the lo image rows * 64 further),
-// computed once per call for all layers.  Tile k of partition p is the
-// reverse kernel's k-th tile of p; the forward kernel's 64-edge tile k reads
+// split fp16 in a K-major no-swizzle layout (16-byte core matrices of 8 rows
+// x 8 columns: the 8-column chunks of an 8-row group 128 bytes apart, the
+// groups 512 bytes apart; the hi image, then the lo image), computed once
+// per call for all layers.  Each image holds the E rows in its first 2 KB
+// and the E' rows in its second.  Tile k of partition p is the reverse
+// kernel's k-th tile of p; the forward kernel's 64-edge tile k copies only
 // the E rows of tiles 2k and 2k + 1.
 constexpr uint32_t ET_ROWS = 64;
 constexpr uint32_t ET_BYTES = ET_ROWS * 128, ET_HALF = ET_ROWS * 64;   // 8 KB, hi then lo
-__device__ __forceinline__ uint32_t et_off(int rows, int row, int k) {
-    return (uint32_t)((k >> 4) * rows * 32 + ((k >> 3) & 1) * rows * 16 + (row >> 3) * 128 + (row & 7) * 16 +
-                      (k & 7) * 2);
+constexpr uint32_t ET_LBO = 128, ET_SBO = 512;     // chunk and row-group strides
+constexpr uint32_t ET_E = 32 * 64;                 // the E rows of one image: 2 KB
+__device__ __forceinline__ uint32_t et_off(int row, int k) {
+    return (uint32_t)((row >> 3) * ET_SBO + (k >> 3) * ET_LBO + (row & 7) * 16 + (k & 7) * 2);
 }
 
 // Tile counts of all partitions (32 edges per tile), then their exclusive
@@ -261,11 +263,10 @@ __global__ void __launch_bounds__(256) etile_fill_kernel(EdgeArgs a, const int32
 #pragma unroll
             for (int i = 0; i < 8; ++i) split2(v[2 * i], v[2 * i + 1], hi[i], lo[i]);
             unsigned char* tile = out + (size_t)(b0 + k) * ET_BYTES;
-            *reinterpret_cast<uint4*>(tile + et_off(ROWS, row, 16 * s)) = *reinterpret_cast<const uint4*>(&hi[0]);
-            *reinterpret_cast<uint4*>(tile + et_off(ROWS, row, 16 * s + 8)) = *reinterpret_cast<const uint4*>(&hi[4]);
-            *reinterpret_cast<uint4*>(tile + ET_HALF + et_off(ROWS, row, 16 * s)) =
-                *reinterpret_cast<const uint4*>(&lo[0]);
-            *reinterpret_cast<uint4*>(tile + ET_HALF + et_off(ROWS, row, 16 * s + 8)) =
+            *reinterpret_cast<uint4*>(tile + et_off(row, 16 * s)) = *reinterpret_cast<const uint4*>(&hi[0]);
+            *reinterpret_cast<uint4*>(tile + et_off(row, 16 * s + 8)) = *reinterpret_cast<const uint4*>(&hi[4]);
+            *reinterpret_cast<uint4*>(tile + ET_HALF + et_off(row, 16 * s)) = *reinterpret_cast<const uint4*>(&lo[0]);
+            *reinterpret_cast<uint4*>(tile + ET_HALF + et_off(row, 16 * s + 8)) =
                 *reinterpret_cast<const uint4*>(&lo[4]);
         }
     }
@@ -457,7 +458,7 @@ constexpr uint32_t Q_OFF_B2 = Q_OFF_B1 + H * 4;
 constexpr uint32_t Q_OFF_BAR = Q_OFF_B2 + H3 * 4;
 constexpr uint32_t Q_OFF_MISC = Q_OFF_BAR + 8 * 8;
 constexpr uint32_t Q_SMEM = align1k(Q_OFF_MISC + 16);
-static_assert(2 * ET_BYTES <= 2 * Q_HH, "two [E; E'] tiles fit in the H tile's space");
+static_assert(4 * ET_E <= 2 * Q_HH, "the E rows of two [E; E'] tiles fit in the H tile's space");
 static_assert(Q_SB_BYTES % 16 == 0, "edge array alignment");
 static_assert(Q_SMEM <= 232448, "forward kernel shared memory");
 
@@ -544,7 +545,8 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
     };
     // z^T = W1 e^T into chunk 0's columns, once the copies have landed
     // (thread tp 0): the tile's 64 edges are the E rows (0-31) of nt
-    // consecutive [E; E'] tiles at Es (edges 32 j .. 32 j + 31 from tile j)
+    // consecutive [E; E'] tiles, copied to Es (edges 32 j .. 32 j + 31 from
+    // tile j: its hi E rows at 4 KB j, its lo E rows 2 KB further)
     auto issue_gemm1 = [&](int nt) {
         if (!mbar_wait(e_bar, e_phase, WAIT_BUDGET)) signal_timeout(a, abort_flag, 8);
         fence_after_sync();
@@ -556,17 +558,21 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                 for (int pr = 0; pr < 3; ++pr) {
                     const uint32_t ahl = pr == 2 ? 1 : 0, bhl = pr == 1 ? 1 : 0;
                     const uint64_t ad = sdesc(smem_u32(w1s + s * SLAB + ahl * A_TILE), A_LBO, A_SBO);
-                    const uint64_t bd = sdesc(smem_u32(Es + j * ET_BYTES + bhl * ET_HALF + s * (ET_ROWS * 32)),
-                                              ET_ROWS * 16, 128);
+                    const uint64_t bd =
+                        sdesc(smem_u32(Es + j * 2 * ET_E + bhl * ET_E + s * 2 * ET_LBO), ET_LBO, ET_SBO);
                     mma_f16(tmem + TB + 32 * j, ad, bd, idesc, (s | pr) != 0);
                 }
         mma_commit(mma_bar);
     };
-    // copies of the [E; E'] tiles of forward tile k (thread tp QN)
+    // copies of the E rows of the [E; E'] tiles of forward tile k (thread tp QN)
     auto copy_etiles = [&](const unsigned char* etiles, int nrev, int k) {
         const int nt = min(2, nrev - 2 * k);
-        mbar_expect_tx(e_bar, nt * ET_BYTES);
-        for (int j = 0; j < nt; ++j) bulk_g2s(Es + j * ET_BYTES, etiles + (size_t)(2 * k + j) * ET_BYTES, ET_BYTES, e_bar);
+        mbar_expect_tx(e_bar, nt * 2 * ET_E);
+        for (int j = 0; j < nt; ++j) {
+            const unsigned char* src = etiles + (size_t)(2 * k + j) * ET_BYTES;
+            bulk_g2s(Es + j * 2 * ET_E, src, ET_E, e_bar);                     // hi image
+            bulk_g2s(Es + j * 2 * ET_E + ET_E, src + ET_HALF, ET_E, e_bar);    // lo image
+        }
         ++e_issued;
     };
     for (int p = 2 * blockIdx.x + pp; p < a.nparts && !aborted; p += 2 * gridDim.x) {
@@ -1163,7 +1169,7 @@ __global__ void __launch_bounds__(NT, 1) edge_bwd_tc_kernel(EdgeArgs a, const un
             for (int pr = 0; pr < 3; ++pr) {
                 const uint32_t ahl = pr == 2 ? 1 : 0, bhl = pr == 1 ? 1 : 0;
                 const uint64_t ad = sdesc(smem_u32(w1s + s * SLAB + ahl * A_TILE), A_LBO, A_SBO);
-                const uint64_t bd = sdesc(smem_u32(Es + bhl * ET_HALF + s * (ET_ROWS * 32)), ET_ROWS * 16, 128);
+                const uint64_t bd = sdesc(smem_u32(Es + bhl * ET_HALF + s * 2 * ET_LBO), ET_LBO, ET_SBO);
                 mma_f16(tmem + TB + 128, ad, bd, idesc, (s | pr) != 0);
             }
         mma_commit(mma_bar);
