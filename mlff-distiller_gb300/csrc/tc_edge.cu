@@ -622,9 +622,6 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                 // hidden unit c of edges 32 hh .. 32 hh + 31
                 const int col = 32 * hh, nv = n - col;
                 const float bias = b1s[c];
-                float z[32];
-                tmem_ld32(lane_base + TB + col, z);
-                tmem_ld_wait();
                 const BColumn hc(Hs, Q_HH, QN, col, c);
                 // GEMM2 accumulates onto b2 (0 for padding edges): this warp refills the
                 // chunk-0 cells it has just read and all 64 columns of chunk 1 + hh
@@ -632,9 +629,15 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                 const float b0c = b2s[c], bch = b2s[(1 + hh) * H + c];
                 if (n == QN) {   // a full tile (all but the last of a partition)
 #pragma unroll
-                    for (int i = 0; i < 32; i += 2) {
-                        const float z0 = z[i] + bias, z1 = z[i + 1] + bias;
-                        hc.put_pair(i, z0 * fast_sigmoid(z0), z1 * fast_sigmoid(z1));
+                    for (int i0 = 0; i0 < 32; i0 += 16) {   // 16 edges per TMEM load
+                        float z[16];
+                        tmem_ld16(lane_base + TB + col + i0, z);
+                        tmem_ld_wait();
+#pragma unroll
+                        for (int i = 0; i < 16; i += 2) {
+                            const float z0 = z[i] + bias, z1 = z[i + 1] + bias;
+                            hc.put_pair(i0 + i, z0 * fast_sigmoid(z0), z1 * fast_sigmoid(z1));
+                        }
                     }
 #pragma unroll
                     for (int i = 0; i < 16; ++i) bv[i] = b0c;
@@ -646,9 +649,16 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                     for (int kk = 0; kk < 4; ++kk) tmem_st16(lane_base + TB + 64 * (1 + hh) + 16 * kk, bv);
                 } else {
 #pragma unroll
-                    for (int i = 0; i < 32; i += 2) {
-                        const float z0 = z[i] + bias, z1 = z[i + 1] + bias;
-                        hc.put_pair(i, i < nv ? z0 * fast_sigmoid(z0) : 0.f, i + 1 < nv ? z1 * fast_sigmoid(z1) : 0.f);
+                    for (int i0 = 0; i0 < 32; i0 += 16) {
+                        float z[16];
+                        tmem_ld16(lane_base + TB + col + i0, z);
+                        tmem_ld_wait();
+#pragma unroll
+                        for (int i = 0; i < 16; i += 2) {
+                            const float z0 = z[i] + bias, z1 = z[i + 1] + bias;
+                            hc.put_pair(i0 + i, i0 + i < nv ? z0 * fast_sigmoid(z0) : 0.f,
+                                        i0 + i + 1 < nv ? z1 * fast_sigmoid(z1) : 0.f);
+                        }
                     }
 #pragma unroll
                     for (int i = 0; i < 16; ++i) bv[i] = i < nv ? b0c : 0.f;
