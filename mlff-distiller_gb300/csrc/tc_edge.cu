@@ -627,51 +627,33 @@ __global__ void __launch_bounds__(NT, 1) edge_fwd_tc_kernel(EdgeArgs a, const un
                 // chunk-0 cells it has just read and all 64 columns of chunk 1 + hh
                 float bv[16];
                 const float b0c = b2s[c], bch = b2s[(1 + hh) * H + c];
-                if (n == QN) {   // a full tile (all but the last of a partition)
 #pragma unroll
-                    for (int i0 = 0; i0 < 32; i0 += 16) {   // 16 edges per TMEM load
-                        float z[16];
-                        tmem_ld16(lane_base + TB + col + i0, z);
-                        tmem_ld_wait();
+                for (int i0 = 0; i0 < 32; i0 += 16) {   // 16 edges per TMEM load
+                    float z[16];
+                    tmem_ld16(lane_base + TB + col + i0, z);
+                    tmem_ld_wait();
 #pragma unroll
-                        for (int i = 0; i < 16; i += 2) {
-                            const float z0 = z[i] + bias, z1 = z[i + 1] + bias;
-                            hc.put_pair(i0 + i, z0 * fast_sigmoid(z0), z1 * fast_sigmoid(z1));
-                        }
+                    for (int i = 0; i < 16; i += 2) {
+                        const float z0 = z[i] + bias, z1 = z[i + 1] + bias;
+                        hc.put_pair(i0 + i, z0 * fast_sigmoid(z0), z1 * fast_sigmoid(z1));
                     }
+                }
 #pragma unroll
-                    for (int i = 0; i < 16; ++i) bv[i] = b0c;
-                    tmem_st16(lane_base + TB + col, bv);
-                    tmem_st16(lane_base + TB + col + 16, bv);
+                for (int i = 0; i < 16; ++i) bv[i] = b0c;
+                tmem_st16(lane_base + TB + col, bv);
+                tmem_st16(lane_base + TB + col + 16, bv);
 #pragma unroll
-                    for (int i = 0; i < 16; ++i) bv[i] = bch;
+                for (int i = 0; i < 16; ++i) bv[i] = bch;
 #pragma unroll
-                    for (int kk = 0; kk < 4; ++kk) tmem_st16(lane_base + TB + 64 * (1 + hh) + 16 * kk, bv);
-                } else {
-#pragma unroll
-                    for (int i0 = 0; i0 < 32; i0 += 16) {
-                        float z[16];
-                        tmem_ld16(lane_base + TB + col + i0, z);
-                        tmem_ld_wait();
-#pragma unroll
-                        for (int i = 0; i < 16; i += 2) {
-                            const float z0 = z[i] + bias, z1 = z[i + 1] + bias;
-                            hc.put_pair(i0 + i, i0 + i < nv ? z0 * fast_sigmoid(z0) : 0.f,
-                                        i0 + i + 1 < nv ? z1 * fast_sigmoid(z1) : 0.f);
-                        }
-                    }
-#pragma unroll
-                    for (int i = 0; i < 16; ++i) bv[i] = i < nv ? b0c : 0.f;
-                    tmem_st16(lane_base + TB + col, bv);
-#pragma unroll
-                    for (int i = 0; i < 16; ++i) bv[i] = 16 + i < nv ? b0c : 0.f;
-                    tmem_st16(lane_base + TB + col + 16, bv);
-#pragma unroll
-                    for (int kk = 0; kk < 4; ++kk) {
-#pragma unroll
-                        for (int i = 0; i < 16; ++i) bv[i] = 16 * kk + i < n ? bch : 0.f;
-                        tmem_st16(lane_base + TB + 64 * (1 + hh) + 16 * kk, bv);
-                    }
+                for (int kk = 0; kk < 4; ++kk) tmem_st16(lane_base + TB + 64 * (1 + hh) + 16 * kk, bv);
+                if (n < QN) {   // the last tile of a partition: its padding edges get h = 0 and no bias
+                    tmem_st_wait();   // the fills above land before the zeros below
+#pragma unroll 1
+                    for (int i = max(nv, 0); i < 32; ++i) hc.put_one(i, 0.f);
+#pragma unroll 1
+                    for (int i = max(nv, 0); i < 32; ++i) tmem_st1(lane_base + TB + col + i, 0.f);
+#pragma unroll 1
+                    for (int i = n; i < QN; ++i) tmem_st1(lane_base + TB + 64 * (1 + hh) + i, 0.f);
                 }
                 tmem_st_wait();
             }

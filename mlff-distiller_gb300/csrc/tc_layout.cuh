@@ -120,6 +120,14 @@ struct BColumn {
         *reinterpret_cast<__half*>(base + half_bytes + o0) = __low2half(lo);
         *reinterpret_cast<__half*>(base + half_bytes + o1) = __high2half(lo);
     }
+    // row row0 + i alone (any i): the split fp16 value of a
+    __device__ __forceinline__ void put_one(int i, float a) const {
+        const __half hi = __float2half_rn(a);
+        const __half lo = __float2half_rn(a - __half2float(hi));
+        const uint32_t o = (uint32_t)i * 128 + ((kj ^ (uint32_t)(i & 7)) << 4);
+        *reinterpret_cast<__half*>(base + o) = hi;
+        *reinterpret_cast<__half*>(base + half_bytes + o) = lo;
+    }
 };
 
 }  // namespace tc
