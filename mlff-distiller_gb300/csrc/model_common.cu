@@ -182,11 +182,13 @@ int launch_embed(const mlff_dims& d, const float* packed, const PackedOffsets& p
 // independent 128-bit loads, so the dot products read shared memory only.
 constexpr int RO_ATOMS = 32;
 constexpr int RO_NT = 256;
-constexpr int RO_W1T = 0;                       // [H][64]
-constexpr int RO_W2T = RO_W1T + H * 64;         // [64][32]
-constexpr int RO_W2 = RO_W2T + 64 * 32;         // [32][64]
-constexpr int RO_W1 = RO_W2 + 32 * 64;          // [64][H]
-constexpr int RO_S = RO_W1 + 64 * H;            // [RO_ATOMS][H]     s
+// the head's weights transposed, rows padded by one float so that both the
+// forward (threads along a row) and the backward products (threads along a
+// column) read shared memory without bank conflicts; two CTAs per SM
+constexpr int RO_W1T_LD = 64 + 1, RO_W2T_LD = 32 + 1;
+constexpr int RO_W1T = 0;                       // [H][65]: W1T[i][o] = W1[o][i]
+constexpr int RO_W2T = RO_W1T + H * RO_W1T_LD;  // [64][33]
+constexpr int RO_S = ((RO_W2T + 64 * RO_W2T_LD) + 3) & ~3;   // [RO_ATOMS][H]     s (16-byte aligned)
 constexpr int RO_Z1 = RO_S + RO_ATOMS * H;      // [RO_ATOMS][64]    z1
 constexpr int RO_H1 = RO_Z1 + RO_ATOMS * 64;    // [RO_ATOMS][64]    silu(z1)
 constexpr int RO_G1 = RO_H1 + RO_ATOMS * 64;    // [RO_ATOMS][64]    dE/dz1
@@ -195,24 +197,19 @@ constexpr int RO_G2 = RO_Z2 + RO_ATOMS * 32;    // [RO_ATOMS][32]    dE/dz2
 constexpr int RO_FLOATS = RO_G2 + RO_ATOMS * 32;
 constexpr size_t RO_SMEM = sizeof(float) * RO_FLOATS;
 
-__device__ __forceinline__ void ro_stage(float* dst, const float* __restrict__ src, int n) {
-    const float4* s4 = reinterpret_cast<const float4*>(src);
-    float4* d4 = reinterpret_cast<float4*>(dst);
-    for (int i = threadIdx.x; i < n / 4; i += RO_NT) d4[i] = __ldg(s4 + i);
+// rows x cols floats into rows of ld floats
+__device__ __forceinline__ void ro_stage(float* dst, const float* __restrict__ src, int rows, int cols, int ld) {
+    for (int i = threadIdx.x; i < rows * cols; i += RO_NT) dst[(i / cols) * ld + i % cols] = __ldg(src + i);
 }
 
-__global__ void __launch_bounds__(RO_NT) readout_kernel(const float* __restrict__ P, PackedOffsets po,
+__global__ void __launch_bounds__(RO_NT, 2) readout_kernel(const float* __restrict__ P, PackedOffsets po,
                                                         const float* __restrict__ X, int32_t n_atoms,
                                                         float* __restrict__ e_atom, float* __restrict__ xbar,
                                                         int want_grad, const Status* st) {
     extern __shared__ __align__(16) float ro[];
     const int t = threadIdx.x;
-    ro_stage(ro + RO_W1T, P + po.head_w1t, H * 64);
-    ro_stage(ro + RO_W2T, P + po.head_w2t, 64 * 32);
-    if (want_grad) {
-        ro_stage(ro + RO_W2, P + po.head_w2, 32 * 64);
-        ro_stage(ro + RO_W1, P + po.head_w1, 64 * H);
-    }
+    ro_stage(ro + RO_W1T, P + po.head_w1t, H, 64, RO_W1T_LD);
+    ro_stage(ro + RO_W2T, P + po.head_w2t, 64, 32, RO_W2T_LD);
     pdl_wait();   // the weights above overlap the previous kernel
     pdl_trigger();
     if (st->code != 0) return;
@@ -239,8 +236,8 @@ __global__ void __launch_bounds__(RO_NT) readout_kernel(const float* __restrict_
             for (int q = 0; q < 8; ++q) acc[q] = b;
 #pragma unroll 4
             for (int i = 0; i < H; i += 4) {
-                const float w0 = ro[RO_W1T + (i + 0) * 64 + o], w1 = ro[RO_W1T + (i + 1) * 64 + o];
-                const float w2 = ro[RO_W1T + (i + 2) * 64 + o], w3 = ro[RO_W1T + (i + 3) * 64 + o];
+                const float w0 = ro[RO_W1T + (i + 0) * RO_W1T_LD + o], w1 = ro[RO_W1T + (i + 1) * RO_W1T_LD + o];
+                const float w2 = ro[RO_W1T + (i + 2) * RO_W1T_LD + o], w3 = ro[RO_W1T + (i + 3) * RO_W1T_LD + o];
 #pragma unroll
                 for (int q = 0; q < 8; ++q) {
                     const float4 x = *reinterpret_cast<const float4*>(S + (q0 + q) * H + i);
@@ -262,8 +259,8 @@ __global__ void __launch_bounds__(RO_NT) readout_kernel(const float* __restrict_
             for (int q = 0; q < 4; ++q) acc[q] = b;
 #pragma unroll 4
             for (int i = 0; i < 64; i += 4) {
-                const float w0 = ro[RO_W2T + (i + 0) * 32 + o], w1 = ro[RO_W2T + (i + 1) * 32 + o];
-                const float w2 = ro[RO_W2T + (i + 2) * 32 + o], w3 = ro[RO_W2T + (i + 3) * 32 + o];
+                const float w0 = ro[RO_W2T + (i + 0) * RO_W2T_LD + o], w1 = ro[RO_W2T + (i + 1) * RO_W2T_LD + o];
+                const float w2 = ro[RO_W2T + (i + 2) * RO_W2T_LD + o], w3 = ro[RO_W2T + (i + 3) * RO_W2T_LD + o];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     const float4 h = *reinterpret_cast<const float4*>(H1 + (q0 + q) * 64 + i);
@@ -297,7 +294,7 @@ __global__ void __launch_bounds__(RO_NT) readout_kernel(const float* __restrict_
                 for (int q = 0; q < 8; ++q) acc[q] = 0.0f;
 #pragma unroll 4
                 for (int j = 0; j < 32; ++j) {
-                    const float w = ro[RO_W2 + j * 64 + o];
+                    const float w = ro[RO_W2T + o * RO_W2T_LD + j];   // W2[j][o]
 #pragma unroll
                     for (int q = 0; q < 8; ++q) acc[q] = fmaf(w, G2[(q0 + q) * 32 + j], acc[q]);
                 }
@@ -312,8 +309,8 @@ __global__ void __launch_bounds__(RO_NT) readout_kernel(const float* __restrict_
                 for (int q = 0; q < 16; ++q) acc[q] = 0.0f;
 #pragma unroll 2
                 for (int j = 0; j < 64; j += 4) {
-                    const float w0 = ro[RO_W1 + (j + 0) * H + o], w1 = ro[RO_W1 + (j + 1) * H + o];
-                    const float w2 = ro[RO_W1 + (j + 2) * H + o], w3 = ro[RO_W1 + (j + 3) * H + o];
+                    const float* wr = ro + RO_W1T + o * RO_W1T_LD + j;   // W1[j .. j + 3][o]
+                    const float w0 = wr[0], w1 = wr[1], w2 = wr[2], w3 = wr[3];
 #pragma unroll
                     for (int q = 0; q < 16; ++q) {
                         const float4 g = *reinterpret_cast<const float4*>(G1 + (q0 + q) * 64 + j);
@@ -371,7 +368,7 @@ int launch_readout(const mlff_dims& d, const float* packed, const PackedOffsets&
         attr_err = cudaFuncSetAttribute(readout_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RO_SMEM);
     });
     if (attr_err != cudaSuccess) return cuda_status(attr_err, "readout smem attribute");
-    const int blocks = (int)std::min<int64_t>((sys.n_atoms + RO_ATOMS - 1) / RO_ATOMS, num_sms());
+    const int blocks = (int)std::min<int64_t>((sys.n_atoms + RO_ATOMS - 1) / RO_ATOMS, 2 * num_sms());
     MLFF_LAUNCH_PDL("readout", readout_kernel, std::max(blocks, 1), RO_NT, RO_SMEM, st, packed, po, X, sys.n_atoms,
                     e_atom, xbar, want_grad, status);
     MLFF_LAUNCH_PDL("energy_sum", energy_sum_kernel, std::min(std::max(sys.n_mol, 1), 152 * 8), 256, 0, st, e_atom, sys.mol_ptr, sys.n_mol,
