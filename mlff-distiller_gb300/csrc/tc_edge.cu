@@ -17,8 +17,9 @@
 //     of W2 (384 x 128) and the lo half of W2's third chunk in shared
 //     memory, the lo halves of chunks 0 and 1 in TMEM (A operands of
 //     tcgen05.mma with A in tensor memory);
-//   * the E tiles (RBF x cutoff, split fp16) are computed once per call for
-//     all layers and bulk-copied per edge tile; per-tile edge arrays are
+//   * the [E; E'] tiles (RBF x cutoff and its d-derivative, split fp16) are
+//     computed once per call for all layers and bulk-copied per edge tile
+//     (the forward kernel copies the E rows only); per-tile edge arrays are
 //     fetched with cp.async while the previous tile's epilogue runs;
 //   * GEMM2's three 128-channel chunks are issued by three threads: a thread
 //     stalls on tcgen05.mma issue while the tensor core is busy (about one
@@ -26,14 +27,13 @@
 //   * every wait is bounded (clock64 budget); on expiry the kernel records
 //     MLFF_ERR_TIMEOUT, drains its own copies, frees TMEM and returns.
 //
-// TMEM (512 columns): [0,128) lo halves of W2 chunks 0 and 1; [128,512) the
-// GEMM2 accumulators (forward: 128-edge tiles, chunk g at 128 + 128 g;
-// reverse: two pipelines of 32-edge tiles, 192 columns each, with [f | f']
-// per chunk, f' = df/dd in forward mode); GEMM1's output aliases one chunk
-// until epilogue 1 has read it: chunk 0 in the forward kernel (read by the
-// scalar warps only, so the next tile's GEMM1 is issued while the vector
-// warps finish epilogue 2), chunk 2 ([z; z']) of the pipeline in the
-// reverse kernel.
+// TMEM (512 columns): [0,128) lo halves of W2 chunks 0 and 1; [128,512) two
+// pipelines of 192 columns each, three 64-column accumulator chunks per
+// pipeline (forward: 64-edge tiles, one chunk per W2 chunk; reverse: 32-edge
+// tiles with [f | f'] per chunk, f' = df/dd in forward mode, chunks 0-1 for
+// GEMM2 and the third for GEMM3).  GEMM1's output aliases one chunk until
+// epilogue 1 has read it: chunk 0 in the forward kernel, the third chunk
+// ([z | z']) in the reverse kernel.
 #include <cuda_fp16.h>
 #include <mutex>
 #include "common.cuh"
