@@ -431,14 +431,16 @@ __device__ __forceinline__ void cols_free_sync(int pp, int n) {
 }
 
 // ------------------------------------------------------- forward kernel
-// 64-edge tiles per pipeline: GEMM1 (z = W1 e, N = 64) into the columns of
-// the pipeline's chunk 0, epilogue 1 (h = silu(z + b1) into the H tile, bias
-// refills), GEMM2 (three 128 x 64 chunks), epilogue 2: warp (q, h) of the
+// 64-edge tiles per pipeline: GEMM1 (z = W1 e, two N = 32 halves, one per
+// [E; E'] tile) into the columns of the pipeline's chunk 0, epilogue 1
+// (h = silu(z + b1) into the H tile, bias refills), GEMM2 (three 128 x 64
+// chunks), epilogue 2: warp (q, h) of the
 // pipeline reads TMEM lane quarter q (channels 32q..32q+31) and sums two
 // feature components of every edge per receiver in registers (h = 0 the
 // scalar and v_x, h = 1 v_y and v_z), Xt = X + messages written once per
-// receiver.  Padding edges of a partial tile get h = 0 and a zero bias fill:
-// their filter is exactly zero and every gather runs unpredicated.
+// receiver.  Padding edges of a partition's last tile get h = 0 and a zero
+// bias fill (a fix-up after epilogue 1): their filter is exactly zero and
+// every gather runs unpredicated.
 constexpr int QN = 64;                               // edges per forward tile
 constexpr uint32_t Q_HH = 2 * b_block(QN);           // one half (hi or lo) of the H tile: 16 KB
 constexpr uint32_t Q_SB_US = 0;
