@@ -25,7 +25,7 @@ def test_flop_counts_follow_from_the_layer_shapes():
     # forward pass plus the input-gradient pass (the same GEMMs again)
     expect = 2 * (layers * (n_edges * filt + n_atoms * update) + n_atoms * head)
     assert bench.step_gemm_flop(n_atoms, n_edges, layers) == expect
-    # per atom-step on the 256-structure batch: ~33 MFLOP, as the path's survey states
+    # per atom-step on the 256-structure batch: ~33 MFLOP
     assert 30e6 < expect / n_atoms < 36e6
 
 
