@@ -59,6 +59,48 @@ def test_two_rank_sharding_gather_and_throughput():
     assert u0 == u1 == s.n_atoms and t0 == t1 == 1.5 and abs(v0 - s.n_atoms / 1.5) < 1e-9
 
 
+def _oracle_worker(rank: int, world: int, port: int, Z, pos, mol_ptr, weights, out_q):
+    import torch.distributed as dist
+    from mlff_gb300.replicas import gather_structure_values, local_slice, shard_structures
+    from oracle import painn
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        m0, m1 = shard_structures(mol_ptr, rank, world)
+        a0, a1, lptr = local_slice(mol_ptr, m0, m1)
+        E, _ = painn.energy_forces(weights, Z[a0:a1], pos[a0:a1], lptr)   # this rank's structures only
+        full = gather_structure_values(torch.as_tensor(E), m0, m1, len(mol_ptr) - 1)
+        out_q.put((rank, full.numpy()))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_rank_model_energies_equal_the_single_process_batch():
+    """Each rank evaluates the model (the float64 oracle stands in for a
+    rank's engine on CPU) on its own structures; the gathered per-structure
+    energies equal one evaluation of the whole batch."""
+    from mlff_gb300 import systems
+    from oracle import painn
+    golden = os.path.join(os.path.dirname(__file__), "golden")
+    w = dict(np.load(os.path.join(golden, "weights_seed0.npz")))
+    s = systems.molecule_batch(9, 10, 40, seed=6)
+    pos = s.pos.astype(np.float32).astype(np.float64)
+    E_ref, _ = painn.energy_forces(w, s.Z, pos, s.mol_ptr)
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_oracle_worker, args=(r, 2, port, s.Z, pos, s.mol_ptr, w, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=300) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for _, full in res:
+        np.testing.assert_allclose(full, E_ref.numpy(), rtol=1e-12, atol=1e-12)
+
+
 def test_shard_edge_cases():
     from mlff_gb300.replicas import shard_structures
     ptr = np.array([0, 5, 10])
